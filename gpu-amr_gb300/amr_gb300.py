@@ -1,0 +1,222 @@
+"""Python binding of the GB300 AMR C ABI (include/amr_gb300.h) over ctypes.
+
+The library must be the in-tree CUDA build (gpu-amr_gb300/lib/libamr_gb300.so);
+there is no CPU fallback: every call raises if the library or a GPU is missing.
+
+    tree = Tree(rank=2, n=16, halo=1, depth=7, capacity=20000)
+    tree.refine_uniform(2)
+    tree.upload_state(u)                 # (size, P1, P1) float64
+    tree.advance(10, velocity=(1.0, 0.5), cfl=0.4)
+    sum_dt, steps = tree.finish_advance()
+    tree.flags_gradient(0.05, 0.01, 1, 5); tree.remesh()
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libamr_gb300.so"
+
+AMR_OK, AMR_ERR_INVALID, AMR_ERR_CUDA, AMR_ERR_CAPACITY, AMR_ERR_UNBALANCED, AMR_ERR_UNSUPPORTED, AMR_ERR_NO_DEVICE = range(7)
+F64, F32 = 0, 1
+
+HALO_META = np.dtype(
+    [("neighbor", "<i4"), ("finer_ids", "<i4", (4,)), ("quadrant", "<i4", (3,)), ("relation", "i1"), ("padding", "i1", (3,))]
+)
+assert HALO_META.itemsize == 36
+
+
+class AmrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"amr status {code}: {msg}")
+        self.code = code
+
+
+class PatchGeometry(C.Structure):
+    _fields_ = [("rank", C.c_int32), ("n", C.c_int32), ("halo", C.c_int32), ("depth", C.c_int32),
+                ("lengths", C.c_double * 3)]
+
+
+class TreeDesc(C.Structure):
+    _fields_ = [("geom", PatchGeometry), ("capacity", C.c_size_t), ("dtype", C.c_int32), ("stream", C.c_void_p)]
+
+
+class TransferTask(C.Structure):
+    _fields_ = [("source_patch", C.c_int32), ("destination_patch", C.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(str(LIB_PATH))
+        vp, sz, i32, dbl = C.c_void_p, C.c_size_t, C.c_int, C.c_double
+        for name in ("amr_tree_create",):
+            getattr(L, name).argtypes = [C.POINTER(TreeDesc), C.POINTER(vp)]
+        L.amr_last_error.restype = C.c_char_p
+        L.amr_launch_count.restype = C.c_uint64
+        L.amr_tree_destroy.argtypes = [vp]
+        L.amr_tree_size.argtypes = [vp, C.POINTER(sz)]
+        L.amr_tree_patch_cells.argtypes = [vp, C.POINTER(sz)]
+        L.amr_tree_upload_state.argtypes = [vp, vp, sz]
+        L.amr_tree_download_state.argtypes = [vp, vp, sz]
+        L.amr_tree_device_state.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+        L.amr_tree_get_ids.argtypes = [vp, vp, sz]
+        L.amr_tree_get_levels.argtypes = [vp, vp, sz]
+        L.amr_tree_get_neighbors.argtypes = [vp, vp, sz]
+        L.amr_tree_halo_exchange.argtypes = [vp]
+        L.amr_tree_flags_gradient.argtypes = [vp, dbl, dbl, i32, i32]
+        L.amr_tree_flags_max.argtypes = [vp, dbl, dbl, i32, i32]
+        L.amr_tree_set_flags.argtypes = [vp, vp, sz]
+        L.amr_tree_get_flags.argtypes = [vp, vp, sz]
+        L.amr_tree_remesh.argtypes = [vp, C.POINTER(i32)]
+        L.amr_tree_refine_uniform.argtypes = [vp, i32]
+        L.amr_tree_advance.argtypes = [vp, sz, C.POINTER(dbl), dbl, dbl]
+        L.amr_tree_finish_advance.argtypes = [vp, C.POINTER(dbl), C.POINTER(sz)]
+        L.amr_tree_synchronize.argtypes = [vp]
+        L.amr_halo_exchange_f64.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
+        L.amr_halo_exchange_f32.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
+        L.amr_interpolate_patches_f64.argtypes = [vp, vp, sz, C.POINTER(PatchGeometry), vp]
+        L.amr_restrict_patches_f64.argtypes = [vp, vp, sz, C.POINTER(PatchGeometry), vp]
+        L.amr_gather_patches.argtypes = [vp, vp, sz, vp, sz, vp]
+        L.amr_compute_step_dt.argtypes = [vp, sz, C.POINTER(PatchGeometry), C.POINTER(dbl), dbl, vp, vp, vp, vp, vp]
+        L.amr_time_step_f64.argtypes = [vp, vp, vp, sz, C.POINTER(PatchGeometry), C.POINTER(dbl), vp, vp]
+        L.amr_flags_max_f64.argtypes = [vp, vp, sz, C.POINTER(PatchGeometry), dbl, dbl, i32, i32, vp, vp]
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != AMR_OK:
+        raise AmrError(code, lib().amr_last_error().decode())
+
+
+def launch_count() -> int:
+    return int(lib().amr_launch_count())
+
+
+def geometry(rank, n, halo=1, depth=7, lengths=(1.0, 1.0, 1.0)) -> PatchGeometry:
+    g = PatchGeometry()
+    g.rank, g.n, g.halo, g.depth = rank, n, halo, depth
+    for i in range(3):
+        g.lengths[i] = lengths[i] if i < len(lengths) else 1.0
+    return g
+
+
+def _vec3(v):
+    a = (C.c_double * 3)()
+    for i, x in enumerate(list(v)[:3]):
+        a[i] = float(x)
+    return a
+
+
+class Tree:
+    """Device-resident ndtree + amr_solver state for one scalar field."""
+
+    def __init__(self, rank, n, halo=1, depth=7, capacity=20000, dtype=F64, lengths=(1.0, 1.0, 1.0), stream=None):
+        self.rank, self.n, self.halo, self.depth = rank, n, halo, depth
+        self.dtype = dtype
+        self.np_dtype = np.float64 if dtype == F64 else np.float32
+        self.pad1 = n + 2 * halo
+        d = TreeDesc()
+        d.geom = geometry(rank, n, halo, depth, lengths)
+        d.capacity = capacity
+        d.dtype = dtype
+        d.stream = stream
+        h = C.c_void_p()
+        check(lib().amr_tree_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().amr_tree_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    @property
+    def size(self) -> int:
+        s = C.c_size_t()
+        check(lib().amr_tree_size(self._h, C.byref(s)))
+        return s.value
+
+    @property
+    def flat(self) -> int:
+        s = C.c_size_t()
+        check(lib().amr_tree_patch_cells(self._h, C.byref(s)))
+        return s.value
+
+    def upload_state(self, state):
+        a = np.ascontiguousarray(state, self.np_dtype)
+        if a.size % self.flat:
+            raise AmrError(AMR_ERR_INVALID, "state is not a whole number of patches")
+        check(lib().amr_tree_upload_state(self._h, a.ctypes.data, a.size // self.flat))
+
+    def download_state(self):
+        out = np.empty((self.size,) + (self.pad1,) * self.rank, self.np_dtype)
+        check(lib().amr_tree_download_state(self._h, out.ctypes.data, self.size))
+        return out
+
+    def device_state(self):
+        cur, nxt = C.c_void_p(), C.c_void_p()
+        check(lib().amr_tree_device_state(self._h, C.byref(cur), C.byref(nxt)))
+        return cur.value, nxt.value
+
+    def ids(self):
+        out = np.empty(self.size, np.uint64)
+        check(lib().amr_tree_get_ids(self._h, out.ctypes.data, self.size))
+        return out
+
+    def levels(self):
+        out = np.empty(self.size, np.int32)
+        check(lib().amr_tree_get_levels(self._h, out.ctypes.data, self.size))
+        return out
+
+    def neighbors(self):
+        out = np.zeros(self.size * 2 * self.rank, HALO_META)
+        check(lib().amr_tree_get_neighbors(self._h, out.ctypes.data, self.size))
+        return out.reshape(self.size, 2 * self.rank)
+
+    def halo_exchange(self):
+        check(lib().amr_tree_halo_exchange(self._h))
+
+    def flags_gradient(self, rthr, cthr, min_level, max_level):
+        check(lib().amr_tree_flags_gradient(self._h, rthr, cthr, min_level, max_level))
+
+    def flags_max(self, rthr, cthr, min_level, max_level):
+        check(lib().amr_tree_flags_max(self._h, rthr, cthr, min_level, max_level))
+
+    def set_flags(self, flags):
+        f = np.ascontiguousarray(flags, np.int8)
+        check(lib().amr_tree_set_flags(self._h, f.ctypes.data, f.size))
+
+    def get_flags(self):
+        out = np.empty(self.size, np.int8)
+        check(lib().amr_tree_get_flags(self._h, out.ctypes.data, self.size))
+        return out
+
+    def remesh(self) -> bool:
+        ch = C.c_int(0)
+        check(lib().amr_tree_remesh(self._h, C.byref(ch)))
+        return bool(ch.value)
+
+    def refine_uniform(self, levels):
+        check(lib().amr_tree_refine_uniform(self._h, levels))
+
+    def advance(self, steps, velocity, cfl, remaining=1.7976931348623157e308):
+        check(lib().amr_tree_advance(self._h, steps, _vec3(velocity), cfl, remaining))
+
+    def finish_advance(self):
+        acc, ex = C.c_double(), C.c_size_t()
+        check(lib().amr_tree_finish_advance(self._h, C.byref(acc), C.byref(ex)))
+        return acc.value, ex.value
+
+    def synchronize(self):
+        check(lib().amr_tree_synchronize(self._h))

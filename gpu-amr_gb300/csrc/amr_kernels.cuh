@@ -1,0 +1,689 @@
+// Kernels of the GB300 AMR hot path.  Every kernel takes plain device pointers
+// and a Geo by value; launch helpers live in amr_tree.cu.
+#pragma once
+
+#include "amr_device.cuh"
+
+namespace amr_gb300 {
+
+// Per-(step, level) update coefficients of the upwind form of the reference's
+// Rusanov flux for linear advection (AdvectionPhysics.hpp:45-66 inside
+// amr_solver::time_step_cpu, amr_solver.hpp:317-346):
+//   F(uL,uR) = v+ uL + v- uR  =>  u' = c0 u + sum_a c_a u_upwind(a)
+// with c_a = (dt/dx_a) |v_a| and c0 = 1 - sum_a c_a.
+struct Coef {
+    double c0, c[3];
+};
+
+// ------------------------------------------------------------ time step
+// One forward-Euler step over `P` patches.  Ghost values on the upwind faces
+// come from the neighbour patches through the halo rules (GhostsOnTheFly) or
+// from the padded buffer itself (the reference's launch contract, where the
+// caller exchanged halos first).
+// With CoefFromDt the coefficients are formed per patch in shared memory from
+// the device dt (drop-in launcher, no per-step table); ppb <= 64.
+template <typename T, bool GhostsOnTheFly, bool CoefFromDt = false>
+__global__ void __launch_bounds__(256)
+k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
+       const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef,
+       int up0, int up1, int up2, int ppb, const double* __restrict__ dt_dev = nullptr, double v0 = 0.0,
+       double v1 = 0.0, double v2 = 0.0)
+{
+    const int cells = g.cells;
+    const int p0    = blockIdx.x * ppb;
+    const int up[3] = { up0, up1, up2 };
+    __shared__ Coef local[CoefFromDt ? 64 : 1];
+    if (CoefFromDt) {
+        const int q = threadIdx.x;
+        if (q < ppb && p0 + q < P) {
+            const double v[3] = { v0, v1, v2 };
+            const double dt   = *dt_dev;
+            const int    lev  = levels[p0 + q];
+            Coef         c;
+            double       tot = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                c.c[a] = 0.0;
+                if (a < g.rank) {
+                    c.c[a] = (dt / cell_size(g, a, lev)) * fabs(v[a]);
+                    tot += c.c[a];
+                }
+            }
+            c.c0     = 1.0 - tot;
+            local[q] = c;
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
+        const int p = p0 + t / cells;
+        if (p >= P) break;
+        int c = t - (p - p0) * cells;
+        int idx[3];
+        for (int L = g.rank - 1; L >= 0; --L) {
+            idx[L] = c % g.n + g.h;
+            c /= g.n;
+        }
+        if (g.rank == 2) idx[2] = 0;
+        const size_t base = static_cast<size_t>(p) * g.flat;
+        const int    li   = padded_index(g, idx);
+        const Coef   cf   = CoefFromDt ? local[p - p0] : coef[levels[p]];
+        const T      u    = in[base + li];
+        T            acc  = static_cast<T>(cf.c0) * u;
+        for (int a = 0; a < g.rank; ++a) {
+            const int dirn = up[a];
+            if (dirn == 0) continue;
+            const int L    = g.rank - 1 - a;
+            const int nidx = idx[L] + dirn;
+            T         val;
+            if (!GhostsOnTheFly || (nidx >= g.h && nidx < g.n + g.h)) {
+                val = in[base + li + dirn * g.s[L]];
+            } else {
+                int G[3] = { idx[0], idx[1], idx[2] };
+                G[L]     = nidx;
+                const int pos = dirn > 0 ? 1 : 0;
+                val = static_cast<T>(ghost_value<T>(in, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos],
+                                                    G, L, pos, g, in + base));
+            }
+            acc = fma(static_cast<T>(cf.c[a]), val, acc);
+        }
+        out[base + li] = acc;
+    }
+}
+
+// --------------------------------------------------------- halo exchange
+// One thread per face ghost cell: P * 2*rank * h * n^(rank-1) cells.  Only
+// interior cells are read, so the in-place update has no read/write overlap.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_halo(T* __restrict__ buf, const amr_halo_meta* __restrict__ meta, long long total, Geo g)
+{
+    const long long per_dir   = static_cast<long long>(g.h) * (g.cells / g.n);
+    const long long per_patch = per_dir * g.ndir;
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long p   = t / per_patch;
+        long long       r   = t - p * per_patch;
+        const int       d   = static_cast<int>(r / per_dir);
+        int             f   = static_cast<int>(r - d * per_dir);
+        const int       L   = d / 2, pos = d % 2;
+        int             G[3] = { 0, 0, 0 };
+        // tangential coordinates (row-major over the other dims), then layer
+        for (int k = g.rank - 1; k >= 0; --k) {
+            if (k == L) continue;
+            G[k] = f % g.n + g.h;
+            f /= g.n;
+        }
+        const int layer = f; // 0..h-1
+        G[L]            = pos ? g.n + g.h + layer : layer;
+        const amr_halo_meta m = meta[p * g.ndir + d];
+        if (m.relation == REL_NONE) continue;
+        T* self = buf + p * g.flat;
+        self[padded_index(g, G)] = static_cast<T>(ghost_value<T>(buf, g.flat, m, G, L, pos, g, self));
+    }
+}
+
+// ------------------------------------------------------------------ flags
+// max|grad u|*h from central differences over face ghosts, evaluated in
+// double with explicit rounding (no contraction) so the oracle's arithmetic
+// is reproduced bit for bit; any/all patch rule of
+// dg_helpers/globals/amr_indicators.hpp:186-225.
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_flags_gradient(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g,
+                 double rthr, double cthr, int min_level, int max_level, int8_t* __restrict__ flags)
+{
+    const int p = blockIdx.x;
+    if (p >= P) return;
+    const T* u   = buf + static_cast<size_t>(p) * g.flat;
+    int      any = 0, all = 1;
+    const int st[3] = { 1, g.rank == 2 ? g.s[0] : g.s[1], g.rank == 3 ? g.s[0] : 0 };
+    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
+        int idx[3] = { 0, 0, 0 }, cc = c;
+        for (int L = g.rank - 1; L >= 0; --L) {
+            idx[L] = cc % g.n + g.h;
+            cc /= g.n;
+        }
+        const int li = padded_index(g, idx);
+        double    s  = 0.0;
+        for (int a = 0; a < g.rank; ++a) {
+            const double gr = __dmul_rn(0.5, __dsub_rn(static_cast<double>(u[li + st[a]]),
+                                                       static_cast<double>(u[li - st[a]])));
+            s = __dadd_rn(s, __dmul_rn(gr, gr));
+        }
+        const double v = __dsqrt_rn(s);
+        if (v > rthr) any = 1;
+        if (!(v < cthr)) all = 0;
+    }
+    any = __syncthreads_or(any);
+    all = __syncthreads_and(all);
+    if (threadIdx.x == 0) {
+        const int level = levels[p];
+        flags[p] = (level < max_level && any) ? FLAG_REFINE : (level > min_level && all) ? FLAG_COARSEN : FLAG_STABLE;
+    }
+}
+
+// Max-value rule (fvm_refinement_criterion.cu:27-67, tests'
+// advection_equation_amr.t.cpp:155-170) over interior and face-ghost cells.
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g, double rthr,
+            double cthr, int min_level, int max_level, int8_t* __restrict__ flags)
+{
+    const int p = blockIdx.x;
+    if (p >= P) return;
+    const T* u = buf + static_cast<size_t>(p) * g.flat;
+    double   m = 0.0;
+    for (int c = threadIdx.x; c < g.flat; c += blockDim.x) {
+        int outside = 0, cc = c;
+        for (int L = g.rank - 1; L >= 0; --L) {
+            const int i = cc % g.P1;
+            cc /= g.P1;
+            outside += (i < g.h || i >= g.n + g.h) ? 1 : 0;
+        }
+        if (outside <= 1) m = fmax(m, static_cast<double>(u[c]));
+    }
+    __shared__ double red[128];
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = 64; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double mx    = red[0];
+        const int    level = levels[p];
+        flags[p] = (mx > rthr && level < max_level) ? FLAG_REFINE : (mx < cthr && level > min_level) ? FLAG_COARSEN : FLAG_STABLE;
+    }
+}
+
+// ------------------------------------------------------------- time step dt
+// Per-batch prologue (one thread per instance): the CFL step size of
+// compute_time_step_cpu (amr_solver.hpp:355-413; the advection wave speed is
+// |v| in every cell, so the minimum over cells is attained at the finest
+// level), clamped like finalize_step_dt_kernel (fvm_time_step.cu:204-233),
+// and the per-(step, level) update coefficients.
+__global__ void k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel,
+                              int ninst, double cfl, int steps, int reset, double remaining0,
+                              double* __restrict__ acc, double* __restrict__ remaining,
+                              uint32_t* __restrict__ count, double* __restrict__ step_dt,
+                              Coef* __restrict__ coef)
+{
+    const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+    if (inst >= ninst) return;
+    const double* v    = vel + 3 * inst;
+    const int     lmax = max_level[inst];
+    double        raw  = 1.7976931348623157e308;
+    for (int a = 0; a < g.rank; ++a) {
+        const double sp = fabs(v[a]);
+        if (sp > 1e-12) raw = fmin(raw, cell_size(g, a, lmax) / sp);
+    }
+    if (reset) {
+        acc[inst]       = 0.0;
+        remaining[inst] = remaining0;
+        count[inst]     = 0;
+    }
+    double   rem = remaining[inst], sum = acc[inst];
+    uint32_t cnt = count[inst];
+    const int nl = g.depth + 1;
+    for (int s = 0; s < steps; ++s) {
+        double dt = raw * cfl;
+        if (rem <= 0.0) dt = 0.0;
+        else if (dt > rem) dt = rem;
+        sum += dt;
+        if (dt > 0.0) {
+            rem -= dt;
+            ++cnt;
+        }
+        step_dt[static_cast<size_t>(s) * ninst + inst] = dt;
+        Coef* row = coef + (static_cast<size_t>(s) * ninst + inst) * nl;
+        for (int l = 0; l < nl; ++l) {
+            Coef   c;
+            double tot = 0.0;
+            for (int a = 0; a < 3; ++a) {
+                c.c[a] = 0.0;
+                if (a < g.rank) {
+                    const double lam = dt / cell_size(g, a, l);
+                    c.c[a]           = lam * fabs(v[a]);
+                    tot += c.c[a];
+                }
+            }
+            c.c0   = 1.0 - tot;
+            row[l] = c;
+        }
+    }
+    acc[inst]       = sum;
+    remaining[inst] = rem;
+    count[inst]     = cnt;
+}
+
+// Maximum level over a level array (per instance: keys carry the instance).
+__global__ void k_max_level(const int32_t* __restrict__ levels, int P, int32_t* __restrict__ out)
+{
+    int m = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) m = max(m, levels[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ------------------------------------------------------------ re-mesh
+// (C1-C9) Every leaf array is in Morton order on entry and on exit.
+
+// Refine eligibility (is_refine_elegible, ndtree.hpp:1888-1896) and coarsen
+// candidates: a leaf that is child 0 of its parent, followed by its 2^rank-1
+// siblings, all flagged Coarsen (apply_refine_coarsen + is_coarsen_elegible,
+// ndtree.hpp:904-940, 1899-1917).
+__global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restrict__ flags, int P, Geo g,
+                       uint8_t* __restrict__ rmark, uint8_t* __restrict__ chead)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const uint64_t k     = keys[i];
+    const int      level = key_level(k);
+    rmark[i]             = (flags[i] == FLAG_REFINE && level < g.depth) ? 1 : 0;
+    uint8_t head         = 0;
+    if (level > 0 && key_offset(g, k) == 0 && i + g.nd <= P) {
+        const uint64_t parent = key_parent(g, k);
+        head                  = 1;
+        for (int j = 0; j < g.nd && head; ++j)
+            if (keys[i + j] != key_child(g, parent, j) || flags[i + j] != FLAG_COARSEN) head = 0;
+    }
+    chead[i] = head;
+}
+
+// One round of the 2:1 refinement closure (balancing, ndtree.hpp:1129-1165):
+// a refining leaf marks its coarser face neighbours.  Marks only grow, so
+// `depth` rounds reach the fixed point the reference's work list reaches.
+__global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, uint8_t* __restrict__ rmark)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P || !rmark[i]) return;
+    for (int d = 0; d < g.ndir; ++d) {
+        const amr_halo_meta& m = meta[static_cast<size_t>(i) * g.ndir + d];
+        if (m.relation == REL_COARSER) rmark[m.neighbor] = 1;
+    }
+}
+
+// Coarsening veto (balancing, ndtree.hpp:1173-1239): a candidate parent is
+// dropped if a boundary child has a finer neighbour across that face, or a
+// same-level neighbour that refines.
+__global__ void k_veto(const amr_halo_meta* __restrict__ meta, int P, Geo g, const uint8_t* __restrict__ rmark,
+                       uint8_t* __restrict__ chead)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P || !chead[i]) return;
+    for (int d = 0; d < g.ndir; ++d) {
+        const int L = d / 2, pos = d % 2;
+        for (int off = 0; off < g.nd; ++off) {
+            if (child_coord(g, off, L) != pos) continue; // boundary children of face d
+            const amr_halo_meta& m = meta[static_cast<size_t>(i + off) * g.ndir + d];
+            if (m.relation == REL_FINER || (m.relation == REL_SAME && rmark[m.neighbor])) {
+                chead[i] = 0;
+                return;
+            }
+        }
+    }
+}
+
+__device__ inline bool in_coarsen_group(const uint64_t* keys, const uint8_t* chead, int i, const Geo& g)
+{
+    const uint64_t k = keys[i];
+    if (key_level(k) == 0) return false;
+    const int h = i - key_offset(g, k);
+    return h >= 0 && chead[h];
+}
+
+// Output count per old leaf: 2^rank for a refined leaf, 1 for the head of a
+// coarsened group (the new parent), 0 for the other members, 1 otherwise.
+__global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+                        const uint8_t* __restrict__ chead, int P, Geo g, uint32_t* __restrict__ cnt,
+                        int32_t* __restrict__ changed)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    uint32_t c = 1;
+    if (rmark[i]) {
+        c = g.nd;
+        *changed = 1;
+    } else if (in_coarsen_group(keys, chead, i, g)) {
+        c = chead[i] ? 1u : 0u;
+        *changed = 1;
+    }
+    cnt[i] = c;
+}
+
+// Exclusive scan of cnt[0..P) into pos[0..P], one block.  pos[P] = new size.
+__global__ void __launch_bounds__(1024)
+k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size_t cap,
+       int32_t* __restrict__ status)
+{
+    __shared__ uint32_t part[1024];
+    const int per = (P + blockDim.x - 1) / blockDim.x;
+    const int lo = threadIdx.x * per, hi = min(P, lo + per);
+    uint32_t  s  = 0;
+    for (int i = lo; i < hi; ++i) s += cnt[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < blockDim.x; o <<= 1) {
+        uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (int i = lo; i < hi; ++i) {
+        pos[i] = run;
+        run += cnt[i];
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        pos[P]    = part[threadIdx.x];
+        status[2] = static_cast<int32_t>(part[threadIdx.x]);
+        if (part[threadIdx.x] > cap) status[0] = AMR_ERR_CAPACITY;
+    }
+}
+
+// Source descriptor of a new leaf: kind 0 copy, 1..2^rank child (offset+1)
+// of a refined leaf, -1 parent of a coarsened group.
+__global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+                       const uint8_t* __restrict__ chead, const uint32_t* __restrict__ pos, int P, Geo g,
+                       uint64_t* __restrict__ nkeys, int32_t* __restrict__ nlevels, int32_t* __restrict__ src,
+                       int8_t* __restrict__ skind, int32_t* __restrict__ max_level)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const uint64_t k = keys[i];
+    const uint32_t q = pos[i];
+    const int      l = key_level(k);
+    int            lmax;
+    if (rmark[i]) {
+        for (int j = 0; j < g.nd; ++j) {
+            nkeys[q + j]   = key_child(g, k, j);
+            nlevels[q + j] = l + 1;
+            src[q + j]     = i;
+            skind[q + j]   = static_cast<int8_t>(j + 1);
+        }
+        lmax = l + 1;
+    } else if (in_coarsen_group(keys, chead, i, g)) {
+        if (!chead[i]) return;
+        nkeys[q]   = key_parent(g, k);
+        nlevels[q] = l - 1;
+        src[q]     = i;
+        skind[q]   = -1;
+        lmax       = l - 1;
+    } else {
+        nkeys[q]   = k;
+        nlevels[q] = l;
+        src[q]     = i;
+        skind[q]   = 0;
+        lmax       = l;
+    }
+    const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(k >> g.inst_shift);
+    atomicMax(max_level + inst, lmax);
+}
+
+// New state from old: whole-patch copy, piecewise-constant prolongation
+// (interpolate_patch, ndtree.hpp:1528-1555) or mean restriction
+// (restrict_patches, :1499-1526; sum order of hypercube_offset,
+// patch_utils.hpp:203-234).  One block per new leaf.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_t* __restrict__ src,
+        const int8_t* __restrict__ skind, int P, Geo g)
+{
+    const int j = blockIdx.x;
+    if (j >= P) return;
+    const int kind = skind[j];
+    const T*  from = old_state + static_cast<size_t>(src[j]) * g.flat;
+    T*        to   = new_state + static_cast<size_t>(j) * g.flat;
+    if (kind == 0) {
+        const size_t bytes = static_cast<size_t>(g.flat) * sizeof(T);
+        const uint4* f4    = reinterpret_cast<const uint4*>(from);
+        uint4*       t4    = reinterpret_cast<uint4*>(to);
+        for (size_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) t4[w] = f4[w];
+        return;
+    }
+    const int half = g.n / 2;
+    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
+        int idx[3] = { 0, 0, 0 }, cc = c;
+        for (int L = g.rank - 1; L >= 0; --L) {
+            idx[L] = cc % g.n + g.h;
+            cc /= g.n;
+        }
+        const int li = padded_index(g, idx);
+        if (kind > 0) {
+            const int off = kind - 1;
+            int       pc[3] = { 0, 0, 0 };
+            for (int L = 0; L < g.rank; ++L) pc[L] = g.h + child_coord(g, off, L) * half + (idx[L] - g.h) / 2;
+            to[li] = from[padded_index(g, pc)];
+        } else {
+            int child = 0, base[3] = { 0, 0, 0 };
+            for (int L = 0; L < g.rank; ++L) {
+                child   = (child << 1) | ((idx[L] - g.h) / half);
+                base[L] = ((idx[L] - g.h) % half) * 2 + g.h;
+            }
+            const T* fp = from + static_cast<size_t>(child) * g.flat + padded_index(g, base);
+            double   sum = 0.0;
+            if (g.rank == 2) {
+                sum += static_cast<double>(fp[0]);
+                sum += static_cast<double>(fp[1]);
+                sum += static_cast<double>(fp[g.s[0]]);
+                sum += static_cast<double>(fp[g.s[0] + 1]);
+                to[li] = static_cast<T>(sum / 4.0);
+            } else {
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2; ++b)
+                        for (int e = 0; e < 2; ++e) sum += static_cast<double>(fp[a * g.s[0] + b * g.s[1] + e]);
+                to[li] = static_cast<T>(sum / 8.0);
+            }
+        }
+    }
+}
+
+__device__ inline int upper_bound_u64(const uint64_t* a, int n, uint64_t x)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] <= x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline int find_u64(const uint64_t* a, int n, uint64_t x)
+{
+    const int u = upper_bound_u64(a, n, x);
+    return (u > 0 && a[u - 1] == x) ? u - 1 : -1;
+}
+
+// Neighbour tables from geometry.  The reference maintains them
+// incrementally through fragment/recombine (neighbor.hpp:420-572,
+// ndtree.hpp:942-1125); on a 2:1-balanced periodic tree its tables equal
+// the geometric relation of each face:
+//   same    : the leaf covering the adjacent same-size region,
+//   coarser : the covering leaf one level up, with the quadrant of it that
+//             touches this leaf (neighbor.hpp:367-379),
+//   finer   : the children of the adjacent region on the shared face, in
+//             compute_boundary_children order (neighbor.hpp:397-417).
+// The domain wraps in every direction (the root is its own neighbour,
+// ndtree.hpp:411-421).
+__global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr_halo_meta* __restrict__ meta,
+                            int32_t* __restrict__ status)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P * g.ndir) return;
+    const int      i = t / g.ndir, d = t % g.ndir;
+    const int      L = d / 2, pos = d % 2, axis = g.rank - 1 - L;
+    const uint64_t k = keys[i];
+    const int      l = key_level(k);
+    uint32_t       c[3];
+    key_decode(g, k, c);
+    const uint32_t s    = 1u << (g.depth - l);
+    const uint32_t wrap = (g.depth >= 32) ? 0xFFFFFFFFu : ((1u << g.depth) - 1u);
+    c[axis]             = (pos ? c[axis] + s : c[axis] - s) & wrap;
+    const uint64_t pre  = key_prefix(g, k);
+    const int      b    = upper_bound_u64(keys, P, key_encode(g, pre, c, 63)) - 1;
+    amr_halo_meta  m;
+    m.neighbor = -1;
+    for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
+    for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
+    m.relation = REL_NONE;
+    m.padding[0] = m.padding[1] = m.padding[2] = 0;
+    const int lb = b >= 0 ? key_level(keys[b]) : -1;
+    if (b >= 0 && lb == l) {
+        m.relation = REL_SAME;
+        m.neighbor = b;
+    } else if (b >= 0 && lb == l - 1) {
+        uint32_t cb[3];
+        key_decode(g, keys[b], cb);
+        m.relation = REL_COARSER;
+        m.neighbor = b;
+        for (int LL = 0; LL < g.rank; ++LL) {
+            const int ax = g.rank - 1 - LL;
+            m.quadrant[LL] = static_cast<int32_t>(((c[ax] - cb[ax]) >> (g.depth - l)) & 1u);
+        }
+    } else if (b >= 0 && lb > l) {
+        const uint64_t region = key_encode(g, pre, c, l);
+        const int      opp_pos = 1 - pos;
+        bool           found   = true;
+        for (int off = 0; off < g.nd; ++off) {
+            if (child_coord(g, off, L) != opp_pos) continue;
+            int kk = 0, mult = 1; // compute_fine_boundary_linear_index: dim 0 fastest
+            for (int LL = 0; LL < g.rank; ++LL) {
+                if (LL == L) continue;
+                kk += child_coord(g, off, LL) * mult;
+                mult *= 2;
+            }
+            const int f = find_u64(keys, P, key_child(g, region, off));
+            found       = found && f >= 0;
+            m.finer_ids[kk] = f;
+        }
+        if (found) {
+            m.relation = REL_FINER;
+        } else { // never leave an invalid index behind a live relation
+            for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
+            status[0] = AMR_ERR_UNBALANCED;
+        }
+    } else {
+        status[0] = AMR_ERR_UNBALANCED;
+    }
+    meta[t] = m;
+}
+
+// --------------------------------------------------- reference drop-ins
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_intergrid(T* __restrict__ buf, const amr_transfer_task* __restrict__ tasks, int ntask, Geo g, int restrict_mode)
+{
+    const int task = blockIdx.x;
+    if (task >= ntask) return;
+    const amr_transfer_task tk   = tasks[task];
+    const int               half = g.n / 2;
+    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
+        int idx[3] = { 0, 0, 0 }, cc = c;
+        for (int L = g.rank - 1; L >= 0; --L) {
+            idx[L] = cc % g.n + g.h;
+            cc /= g.n;
+        }
+        int child = 0, base[3] = { 0, 0, 0 };
+        for (int L = 0; L < g.rank; ++L) {
+            child   = (child << 1) | ((idx[L] - g.h) / half);
+            base[L] = ((idx[L] - g.h) % half) * 2 + g.h;
+        }
+        const int bi = padded_index(g, base);
+        const int ci = padded_index(g, idx);
+        if (restrict_mode) {
+            const T* fp  = buf + static_cast<size_t>(tk.source_patch + child) * g.flat + bi;
+            double   sum = 0.0;
+            if (g.rank == 2) {
+                sum += static_cast<double>(fp[0]);
+                sum += static_cast<double>(fp[1]);
+                sum += static_cast<double>(fp[g.s[0]]);
+                sum += static_cast<double>(fp[g.s[0] + 1]);
+                buf[static_cast<size_t>(tk.destination_patch) * g.flat + ci] = static_cast<T>(sum / 4.0);
+            } else {
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2; ++b)
+                        for (int e = 0; e < 2; ++e) sum += static_cast<double>(fp[a * g.s[0] + b * g.s[1] + e]);
+                buf[static_cast<size_t>(tk.destination_patch) * g.flat + ci] = static_cast<T>(sum / 8.0);
+            }
+        } else {
+            const T v  = buf[static_cast<size_t>(tk.source_patch) * g.flat + ci];
+            T*      fp = buf + static_cast<size_t>(tk.destination_patch + child) * g.flat + bi;
+            if (g.rank == 2) {
+                fp[0] = v;
+                fp[1] = v;
+                fp[g.s[0]] = v;
+                fp[g.s[0] + 1] = v;
+            } else {
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2; ++b)
+                        for (int e = 0; e < 2; ++e) fp[a * g.s[0] + b * g.s[1] + e] = v;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_gather(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t words_per_patch,
+         const int32_t* __restrict__ sources, int count)
+{
+    const int j = blockIdx.x;
+    if (j >= count) return;
+    const uint4* f = src + static_cast<size_t>(sources[j]) * words_per_patch;
+    uint4*       t = dst + static_cast<size_t>(j) * words_per_patch;
+    for (size_t w = threadIdx.x; w < words_per_patch; w += blockDim.x) t[w] = f[w];
+}
+
+__global__ void k_gather_bytes(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst,
+                               size_t bytes, const int32_t* __restrict__ sources, int count)
+{
+    const int j = blockIdx.x;
+    if (j >= count) return;
+    const unsigned char* f = src + static_cast<size_t>(sources[j]) * bytes;
+    unsigned char*       t = dst + static_cast<size_t>(j) * bytes;
+    for (size_t w = threadIdx.x; w < bytes; w += blockDim.x) t[w] = f[w];
+}
+
+// finalize_step_dt_kernel semantics (fvm_time_step.cu:204-233) for the
+// drop-in dt entry point.
+__global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, double v0, double v1, double v2,
+                              double cfl, double* dt_buf, double* acc, double* remaining, uint32_t* count)
+{
+    const double v[3] = { v0, v1, v2 };
+    double       raw  = 1.7976931348623157e308;
+    for (int a = 0; a < g.rank; ++a) {
+        const double sp = fabs(v[a]);
+        if (sp > 1e-12) raw = fmin(raw, cell_size(g, a, *max_level) / sp);
+    }
+    double step_dt = raw * cfl;
+    if (*remaining <= 0.0) step_dt = 0.0;
+    else if (step_dt > *remaining) step_dt = *remaining;
+    *dt_buf = step_dt;
+    *acc += step_dt;
+    if (step_dt > 0.0) {
+        *remaining -= step_dt;
+        ++(*count);
+    }
+}
+
+// Per-level coefficients for one step from a device dt (drop-in step).
+__global__ void k_coef_from_dt(const double* __restrict__ dt_buf, Geo g, double v0, double v1, double v2,
+                               Coef* __restrict__ coef)
+{
+    const int l = threadIdx.x;
+    if (l > g.depth) return;
+    const double v[3] = { v0, v1, v2 };
+    const double dt   = *dt_buf;
+    Coef         c;
+    double       tot = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        c.c[a] = 0.0;
+        if (a < g.rank) {
+            c.c[a] = (dt / cell_size(g, a, l)) * fabs(v[a]);
+            tot += c.c[a];
+        }
+    }
+    c.c0    = 1.0 - tot;
+    coef[l] = c;
+}
+
+} // namespace amr_gb300

@@ -1,0 +1,205 @@
+/*
+ * gb300-amr — C ABI of the GB300-native (sm_103a) hot path of gpu-amr:
+ * the per-leaf-patch finite-volume update over the Morton-ordered ndtree, the
+ * face halo exchange with coarse-fine prolongation/restriction, and the
+ * refine/coarsen cycle (flagging, 2:1 balance, Morton order, compaction).
+ *
+ * All functions return an amr_status (0 = success).  Pointers named `device_*`
+ * are CUDA device pointers; `host_*` are host pointers.  `stream` is a
+ * cudaStream_t passed as void* (NULL = legacy default stream).  No torch or
+ * C++ types cross this boundary.
+ *
+ * Layout contract (identical to the reference's patch<double, padded_layout>):
+ * one leaf = one padded patch of (n + 2*halo)^rank cells, row-major, layout
+ * dimension 0 slowest, physical x on the last (fastest) index; patches are
+ * contiguous, patch-major, in Morton order.
+ */
+#ifndef AMR_GB300_H
+#define AMR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum amr_status {
+    AMR_OK                = 0,
+    AMR_ERR_INVALID       = 1, /* bad argument or size */
+    AMR_ERR_CUDA          = 2, /* a CUDA call failed; see amr_last_error() */
+    AMR_ERR_CAPACITY      = 3, /* a re-mesh would exceed the tree capacity */
+    AMR_ERR_UNBALANCED    = 4, /* neighbour rebuild met a non-2:1 configuration */
+    AMR_ERR_UNSUPPORTED   = 5, /* rank/size combination not built */
+    AMR_ERR_NO_DEVICE     = 6
+} amr_status;
+
+typedef enum amr_dtype { AMR_F64 = 0, AMR_F32 = 1 } amr_dtype;
+
+/* Neighbour relation per (leaf, direction); direction = 2*dim + positive with
+ * dim 0 the slowest layout index.  Same memory layout as the reference's
+ * amr::cuda::halo_direction_metadata (include/cuda/halo_exchange.hpp:19-26):
+ * relation 0 none, 1 same, 2 finer, 3 coarser. */
+typedef struct amr_halo_meta {
+    int32_t neighbor;
+    int32_t finer_ids[4];
+    int32_t quadrant[3];
+    int8_t  relation;
+    int8_t  padding[3];
+} amr_halo_meta;
+
+/* Reference-compatible launch configuration for the free-function entry
+ * points (include/cuda/halo_exchange.hpp:28-40, intergrid_transfer.hpp:17-26,
+ * fvm_time_step.hpp:9-27), reduced to what the kernels need. */
+typedef struct amr_patch_geometry {
+    int32_t rank;      /* 2 or 3 */
+    int32_t n;         /* interior cells per dimension (even, >= 2*halo) */
+    int32_t halo;      /* ghost layers */
+    int32_t depth;     /* Morton depth of the patch index (morton_id<Depth,Rank>) */
+    double  lengths[3];/* physical domain lengths per Morton axis x, y, z */
+} amr_patch_geometry;
+
+/* Reference intergrid_transfer_task_metadata (intergrid_transfer.hpp:11-15). */
+typedef struct amr_transfer_task {
+    int32_t source_patch;
+    int32_t destination_patch;
+} amr_transfer_task;
+
+/* ------------------------------------------------------------------ info */
+const char* amr_last_error(void);
+int         amr_version(void);
+
+/* ---------------------------------------------- free-function drop-ins
+ * Each replaces one amr::cuda:: launcher of the reference; they operate on
+ * caller-owned device buffers with the reference layout. */
+
+/* Replaces amr::cuda::halo_exchange_scalar_patches_inplace
+ * (include/cuda/halo_exchange.hpp:42-47; src/cuda/halo_exchange.cu:351-403):
+ * fills every face ghost cell of `num_patches` patches from `meta`
+ * (num_patches * 2*rank records).  Corners are left untouched. */
+amr_status amr_halo_exchange_f64(double* device_patches, const amr_halo_meta* device_meta,
+                                 size_t meta_count, size_t num_patches,
+                                 const amr_patch_geometry* geom, void* stream);
+amr_status amr_halo_exchange_f32(float* device_patches, const amr_halo_meta* device_meta,
+                                 size_t meta_count, size_t num_patches,
+                                 const amr_patch_geometry* geom, void* stream);
+
+/* Replace interpolate_scalar_patches_inplace / restrict_scalar_patches_inplace
+ * (include/cuda/intergrid_transfer.hpp:28-42): for each task, copy the parent
+ * at source_patch into the 2^rank children starting at destination_patch
+ * (piecewise constant), or average the 2^rank children starting at
+ * source_patch into the parent at destination_patch. */
+amr_status amr_interpolate_patches_f64(double* device_patches, const amr_transfer_task* device_tasks,
+                                       size_t task_count, const amr_patch_geometry* geom, void* stream);
+amr_status amr_restrict_patches_f64(double* device_patches, const amr_transfer_task* device_tasks,
+                                    size_t task_count, const amr_patch_geometry* geom, void* stream);
+
+/* Replaces permute_patches_inplace_batch's gather (include/cuda/permutation.hpp:10-17):
+ * dst[i] = src[sources[i]] for whole patches of patch_bytes bytes (out of place). */
+amr_status amr_gather_patches(void* device_dst, const void* device_src, size_t patch_bytes,
+                              const int32_t* device_sources, size_t count, void* stream);
+
+/* Replaces launch_compute_dt_kernel_device + launch_finalize_step_dt
+ * (include/cuda/fvm_time_step.hpp:39-58) for linear advection: raw dt =
+ * min over leaves and axes of dx/|v|, step dt = cfl*raw clamped to the
+ * remaining time; accumulates into *device_dt_accumulator and counts the
+ * step in *device_step_count when the step dt is positive. */
+amr_status amr_compute_step_dt(const int32_t* device_levels, size_t num_patches,
+                               const amr_patch_geometry* geom, const double* velocity3, double cfl,
+                               double* device_dt, double* device_dt_accumulator,
+                               double* device_remaining_time, uint32_t* device_step_count,
+                               void* stream);
+
+/* Replaces launch_time_step_kernel_with_device_dt<AdvectionPhysics,DIM>
+ * (include/cuda/fvm_time_step.hpp:30-37): one forward-Euler Rusanov step of
+ * linear advection with velocity `velocity3`, reading the face ghosts the
+ * caller filled, writing the interior of device_out. */
+amr_status amr_time_step_f64(const double* device_in, double* device_out,
+                             const int32_t* device_levels, size_t num_patches,
+                             const amr_patch_geometry* geom, const double* velocity3,
+                             const double* device_dt, void* stream);
+
+/* Replaces compute_scalar_patch_amr_decisions_from_device
+ * (include/cuda/fvm_refinement_criterion.hpp:20-27): per patch, Refine (1) if
+ * the maximum exceeds refine_threshold and level < max_level, Coarsen (2) if
+ * it is below coarsen_threshold and level > min_level, else Stable (0).  The
+ * maximum runs over interior and face-ghost cells. */
+amr_status amr_flags_max_f64(const double* device_patches, const int32_t* device_levels,
+                             size_t num_patches, const amr_patch_geometry* geom,
+                             double refine_threshold, double coarsen_threshold, int min_level,
+                             int max_level, int8_t* device_flags, void* stream);
+
+/* ------------------------------------------------- device-resident tree
+ * The GB300-native core behind the ndtree / amr_solver API: state, Morton
+ * ids, levels and neighbour tables live in HBM; the whole refine/coarsen
+ * cycle runs on the device. */
+typedef struct amr_tree amr_tree;
+
+typedef struct amr_tree_desc {
+    amr_patch_geometry geom;
+    size_t             capacity;  /* maximum number of leaves */
+    int32_t            dtype;     /* amr_dtype of the cell state */
+    void*              stream;    /* cudaStream_t for every call on this tree */
+} amr_tree_desc;
+
+/* ndtree(capacity) (include/ndtree/ndtree.hpp:320-425): one root leaf with
+ * periodic self-neighbours. */
+amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out);
+amr_status amr_tree_destroy(amr_tree* t);
+/* ndtree::size() */
+amr_status amr_tree_size(const amr_tree* t, size_t* out);
+/* Flat cell count of one padded patch. */
+amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out);
+
+/* State transfer, the reference's sync_current_{to,from}_device
+ * (ndtree.hpp:583-613); host layout = size() padded patches in Morton order,
+ * elements of the tree's dtype. */
+amr_status amr_tree_upload_state(amr_tree* t, const void* host_state, size_t num_patches);
+amr_status amr_tree_download_state(amr_tree* t, void* host_state, size_t num_patches);
+/* Device pointers of the current/next state buffers (get_device_buffer). */
+amr_status amr_tree_device_state(amr_tree* t, void** current, void** next);
+
+/* Topology readback: Morton ids (get_node_index_at), levels, neighbour tables. */
+amr_status amr_tree_get_ids(const amr_tree* t, uint64_t* host_ids, size_t num_patches);
+amr_status amr_tree_get_levels(const amr_tree* t, int32_t* host_levels, size_t num_patches);
+amr_status amr_tree_get_neighbors(const amr_tree* t, amr_halo_meta* host_meta, size_t num_patches);
+
+/* ndtree::halo_exchange_update (ndtree.hpp:1862-1877). */
+amr_status amr_tree_halo_exchange(amr_tree* t);
+
+/* Refinement flags: ndtree::update_refine_flags (ndtree.hpp:886-902). */
+amr_status amr_tree_flags_gradient(amr_tree* t, double refine_threshold, double coarsen_threshold,
+                                   int min_level, int max_level);
+amr_status amr_tree_flags_max(amr_tree* t, double refine_threshold, double coarsen_threshold,
+                              int min_level, int max_level);
+amr_status amr_tree_set_flags(amr_tree* t, const int8_t* host_flags, size_t num_patches);
+amr_status amr_tree_get_flags(const amr_tree* t, int8_t* host_flags, size_t num_patches);
+
+/* ndtree::reconstruct_tree after the flags are set (ndtree.hpp:1249-1271):
+ * 2:1 balance, refinement (prolongation), coarsening (restriction), Morton
+ * order and neighbour tables, all on the device.  *changed (optional) tells
+ * whether the topology changed. */
+amr_status amr_tree_remesh(amr_tree* t, int* changed);
+/* Uniform refinement, `levels` times (reconstruct_tree with refine-all). */
+amr_status amr_tree_refine_uniform(amr_tree* t, int levels);
+
+/* amr_solver::advance_batch_async / finish_advance_batch
+ * (include/solver/amr_solver.hpp:155-262) for linear advection with constant
+ * velocity: `steps` forward-Euler Rusanov steps, each with dt = cfl * min(dx/|v|)
+ * clamped to the remaining time.  Face ghosts are produced on the fly from
+ * neighbour patches, so no halo pass runs between steps; call
+ * amr_tree_halo_exchange before reading ghost cells. */
+amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl,
+                            double remaining_time);
+amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed_steps);
+
+/* Block until all work queued on the tree's stream has finished. */
+amr_status amr_tree_synchronize(amr_tree* t);
+
+/* Kernel launches issued by this library since load (for launch accounting). */
+uint64_t amr_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMR_GB300_H */

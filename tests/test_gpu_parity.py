@@ -1,0 +1,229 @@
+"""CUDA path vs the reference (golden dumps) and the oracle, through the C ABI.
+
+Bars (stated per test):
+  * Morton ids, neighbour tables, refine/coarsen flags, tree after every
+    re-mesh: bit-exact.
+  * Halo ghosts, prolongation, restriction on identical inputs: bit-exact.
+  * FP64 cell states after many steps: relative L2 <= 1e-12 (the fused
+    kernel evaluates the upwind form of the Rusanov flux with FMA).
+  * Sum of time steps: exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import bumps_of, face_mask, interior, load_golden, rel_l2, vel_of
+
+pytestmark = pytest.mark.gpu
+
+STATE_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def amr():
+    import amr_gb300 as A
+
+    A.lib()
+    return A
+
+
+def _pad(inner, rank, n, h):
+    P1 = n + 2 * h
+    out = np.zeros((inner.shape[0],) + (P1,) * rank)
+    out[(slice(None),) + (slice(h, n + h),) * rank] = inner
+    return out
+
+
+def _tables(tree, rank):
+    nb = tree.neighbors()
+    kind = nb["relation"].astype(np.int8)
+    nbid = np.full(nb["finer_ids"].shape, -1, np.int32)
+    same = (kind == 1) | (kind == 3)
+    nbid[..., 0][same] = nb["neighbor"][same]
+    nf = 2 ** (rank - 1)
+    fin = kind == 2
+    nbid[..., :nf][fin] = nb["finer_ids"][..., :nf][fin]
+    quad = nb["quadrant"].astype(np.int8)
+    quad[kind != 3] = 0
+    return kind, nbid, quad
+
+
+def _assert_tables(tree, z, k, rank):
+    np.testing.assert_array_equal(tree.ids(), z[f"ids_{k}"])
+    kind, nbid, quad = _tables(tree, rank)
+    np.testing.assert_array_equal(kind, z[f"kind_{k}"])
+    np.testing.assert_array_equal(nbid, z[f"nbid_{k}"])
+    np.testing.assert_array_equal(quad, z[f"quad_{k}"])
+
+
+@pytest.mark.parametrize("name", ["config1_uniform_2d", "config2_amr_2d", "config3_amr_3d"])
+def test_solver_run_matches_reference(amr, name):
+    z, meta = load_golden(name)
+    p = meta["params"]
+    rank, n, h = meta["rank"], meta["n"], meta["halo"]
+    t = amr.Tree(rank, n, h, meta["depth"], capacity=20000)
+    t.refine_uniform(int(p["init_levels"]))
+    np.testing.assert_array_equal(t.ids(), z["init_ids"])
+    t.upload_state(_pad(z["state_init"], rank, n, h))
+    t.halo_exchange()
+    steps, interval = int(p["steps"]), int(p["remesh"])
+    vel, cfl = vel_of(meta), float(p["cfl"])
+    done, sum_dt, k, mid = 0, 0.0, 0, 0
+    while done < steps:
+        todo = min(interval, steps - done) if interval > 0 else steps - done
+        t.advance(todo, vel, cfl)
+        acc, ex = t.finish_advance()
+        sum_dt += acc
+        done += ex
+        if interval > 0 and p["crit"] != "none":
+            if f"state_mid_{mid}" in z and int(z[f"state_mid_step_{mid}"]) == done:
+                got = interior(t.download_state(), rank, n, h)
+                assert rel_l2(got, z[f"state_mid_{mid}"]) <= STATE_TOL
+                mid += 1
+            t.flags_gradient(float(p["rthr"]), float(p["cthr"]), int(p["min_level"]), int(p["max_level"]))
+            np.testing.assert_array_equal(t.get_flags(), z[f"flags_{k}"])
+            t.remesh()
+            _assert_tables(t, z, k, rank)
+            k += 1
+    assert k == int(z["n_remesh"])
+    assert done == int(z["steps"])
+    assert sum_dt == float(z["sum_dt"])
+    np.testing.assert_array_equal(t.ids(), z["final_ids"])
+    err = rel_l2(interior(t.download_state(), rank, n, h), z["state_final"])
+    assert err <= STATE_TOL, err
+
+
+@pytest.mark.parametrize(
+    "name", ["tree_random_2d_n4", "tree_random_2d_n8", "tree_random_3d_n4", "tree_random_2d_h2"]
+)
+def test_tree_cycle_matches_reference(amr, name):
+    z, meta = load_golden(name)
+    p = meta["params"]
+    rank, n, h = meta["rank"], meta["n"], meta["halo"]
+    t = amr.Tree(rank, n, h, meta["depth"], capacity=20000)
+    t.refine_uniform(int(p["init_levels"]))
+    np.testing.assert_array_equal(t.ids(), z["ids_init"])
+    t.upload_state(z["state_init"])
+    m = face_mask(rank, n, h).reshape(-1)
+    for k in range(int(z["passes"])):
+        t.set_flags(z[f"flags_{k}"])
+        t.remesh()
+        t.halo_exchange()
+        _assert_tables(t, z, k, rank)
+        if f"state_{k}" in z:
+            a = t.download_state().reshape(t.size, -1)[:, m]
+            b = z[f"state_{k}"].reshape(t.size, -1)[:, m]
+            np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("rank,n,h,levels,maxl,seed", [(2, 8, 1, 2, 6, 21), (3, 4, 1, 1, 4, 22), (2, 6, 2, 1, 5, 23)])
+def test_random_cycles_against_oracle(amr, oracle_mod, rank, n, h, levels, maxl, seed):
+    """Longer random refine/coarsen sequences than the fixtures hold, checked
+    against the C restatement on the same inputs."""
+    o = oracle_mod.OracleTree(rank, n, h, 7, 40000)
+    o.refine_all(levels)
+    o.random_state(seed)
+    o.halo_exchange()
+    t = amr.Tree(rank, n, h, 7, capacity=40000)
+    t.refine_uniform(levels)
+    t.upload_state(o.state())
+    m = face_mask(rank, n, h).reshape(-1)
+    for k in range(12):
+        f = o.flags_random(seed, k + 1, 0.15, 0.6, 1, maxl)
+        assert o.reconstruct(f) == 0
+        o.halo_exchange()
+        t.set_flags(f)
+        t.remesh()
+        t.halo_exchange()
+        np.testing.assert_array_equal(t.ids(), o.ids())
+        a = t.download_state().reshape(t.size, -1)[:, m]
+        b = o.state().reshape(o.size, -1)[:, m]
+        np.testing.assert_array_equal(a, b)
+
+
+def test_known_answer_pulse_with_amr(amr, oracle_mod):
+    """The reference's PulseCenterMovementAMR (tests/advection_equation_amr.t.cpp:132-232),
+    50x50 patches with halo 2: max-value criterion (refine > 0.1 below level 5,
+    coarsen < 0.05 above level 1) re-meshing every step, advance to t = 0.5;
+    the maximum must sit within one cell of start + v t."""
+    rank, n, h = 2, 50, 2
+    o = oracle_mod.OracleTree(rank, n, h, 7, 64)
+    o.init_state([0.2, 0.2, 0.05, 1.0])
+    o.halo_exchange()
+    t = amr.Tree(rank, n, h, 7, capacity=4096)
+    t.upload_state(o.state())
+    tt = 0.0
+    while tt < 0.5:
+        t.advance(1, [1.0, 0.5], 0.4)
+        acc, _ = t.finish_advance()
+        t.flags_max(0.1, 0.05, 1, 5)
+        t.remesh()
+        tt += acc
+    t.halo_exchange()
+    u = interior(t.download_state(), rank, n, h)
+    ids, best = t.ids(), np.unravel_index(np.argmax(u), u.shape)
+    p, iy, ix = best
+    level = int(ids[p] & 63)
+    m = int(ids[p] >> 6)
+    x0 = sum(((m >> (2 * b)) & 1) << b for b in range(7)) / 2**7
+    y0 = sum(((m >> (2 * b + 1)) & 1) << b for b in range(7)) / 2**7
+    dx = 1.0 / (n * 2**level)
+    x, y = x0 + (ix + 0.5) * dx, y0 + (iy + 0.5) * dx
+    finest = 1.0 / (n * 2 ** int(t.levels().max()))
+    assert abs(x - 0.7) <= max(dx, finest) and abs(y - 0.45) <= max(dx, finest)
+
+
+def test_noop_remesh_and_capacity(amr):
+    t = amr.Tree(2, 8, 1, 7, capacity=20)
+    t.refine_uniform(1)
+    ids = t.ids()
+    t.set_flags(np.zeros(4, np.int8))
+    assert t.remesh() is False
+    np.testing.assert_array_equal(t.ids(), ids)
+    t.set_flags(np.ones(4, np.int8))  # 16 leaves fit
+    assert t.remesh() is True
+    t.set_flags(np.ones(16, np.int8))  # 64 > 20
+    with pytest.raises(amr.AmrError) as e:
+        t.remesh()
+    assert e.value.code == amr.AMR_ERR_CAPACITY
+    assert t.size == 16  # tree left unchanged
+
+
+def test_depth_cap_blocks_refinement(amr):
+    t = amr.Tree(2, 4, 1, depth=2, capacity=100)
+    t.refine_uniform(2)
+    assert t.size == 16
+    t.set_flags(np.ones(16, np.int8))  # level == depth: not eligible
+    assert t.remesh() is False
+
+
+def test_invalid_arguments_are_rejected(amr):
+    for bad in (dict(rank=4, n=8), dict(rank=2, n=7), dict(rank=2, n=2, halo=2), dict(rank=3, n=8, depth=20)):
+        kw = dict(halo=1, depth=7)
+        kw.update(bad)
+        with pytest.raises(amr.AmrError) as e:
+            amr.Tree(capacity=16, **kw)
+        assert e.value.code == amr.AMR_ERR_INVALID
+    t = amr.Tree(2, 8, 1, 7, capacity=16)
+    with pytest.raises(amr.AmrError):
+        t.set_flags(np.zeros(3, np.int8))
+
+
+def test_fp32_form_tracks_fp64(amr):
+    """FP32 state/flux with FP64 dt and restriction: same tree, L2 error vs
+    the FP64 path below 1e-5 on the shortened config-2 run."""
+    z, meta = load_golden("config2_amr_2d")
+    p = meta["params"]
+    res = {}
+    for dt in (amr.F64, amr.F32):
+        t = amr.Tree(2, 16, 1, 7, capacity=20000, dtype=dt)
+        t.refine_uniform(2)
+        t.upload_state(_pad(z["state_init"], 2, 16, 1))
+        t.halo_exchange()
+        for _ in range(3):
+            t.advance(10, vel_of(meta), 0.4)
+            t.finish_advance()
+            t.flags_gradient(0.05, 0.01, 1, 5)
+            t.remesh()
+        res[dt] = (t.ids(), interior(t.download_state(), 2, 16, 1).astype(np.float64))
+    np.testing.assert_array_equal(res[amr.F64][0], res[amr.F32][0])
+    assert rel_l2(res[amr.F32][1], res[amr.F64][1]) <= 1e-5
