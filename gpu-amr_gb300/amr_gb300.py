@@ -67,6 +67,8 @@ def lib():
         L.amr_tree_patch_cells.argtypes = [vp, C.POINTER(sz)]
         L.amr_tree_upload_state.argtypes = [vp, vp, sz]
         L.amr_tree_download_state.argtypes = [vp, vp, sz]
+        L.amr_tree_load_state_device.argtypes = [vp, vp, sz]
+        L.amr_tree_reset.argtypes = [vp]
         L.amr_tree_device_state.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
         L.amr_tree_get_ids.argtypes = [vp, vp, sz]
         L.amr_tree_get_levels.argtypes = [vp, vp, sz]
@@ -81,6 +83,8 @@ def lib():
         L.amr_tree_advance.argtypes = [vp, sz, C.POINTER(dbl), dbl, dbl]
         L.amr_tree_finish_advance.argtypes = [vp, C.POINTER(dbl), C.POINTER(sz)]
         L.amr_tree_synchronize.argtypes = [vp]
+        L.amr_tree_set_timing.argtypes = [vp, i32]
+        L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.amr_halo_exchange_f64.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
         L.amr_halo_exchange_f32.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
         L.amr_interpolate_patches_f64.argtypes = [vp, vp, sz, C.POINTER(PatchGeometry), vp]
@@ -164,6 +168,12 @@ class Tree:
         check(lib().amr_tree_download_state(self._h, out.ctypes.data, self.size))
         return out
 
+    def load_state_device(self, ptr, num_patches):
+        check(lib().amr_tree_load_state_device(self._h, C.c_void_p(ptr), num_patches))
+
+    def reset(self):
+        check(lib().amr_tree_reset(self._h))
+
     def device_state(self):
         cur, nxt = C.c_void_p(), C.c_void_p()
         check(lib().amr_tree_device_state(self._h, C.byref(cur), C.byref(nxt)))
@@ -218,5 +228,103 @@ class Tree:
         check(lib().amr_tree_finish_advance(self._h, C.byref(acc), C.byref(ex)))
         return acc.value, ex.value
 
+    def set_timing(self, enabled: bool):
+        check(lib().amr_tree_set_timing(self._h, int(enabled)))
+
+    def get_timing(self):
+        ms, n, cells = C.c_double(), C.c_uint64(), C.c_uint64()
+        check(lib().amr_tree_get_timing(self._h, C.byref(ms), C.byref(n), C.byref(cells)))
+        return ms.value, n.value, cells.value
+
     def synchronize(self):
         check(lib().amr_tree_synchronize(self._h))
+
+
+# ------------------------------------------------------------ initial data
+# Host-side helpers for amr_solver::initialize (amr_solver.hpp:105-145): cell
+# centres of every interior cell from physics_system::cell_coord
+# (physics_system.hpp:107-138) and a sum-of-Gaussians field with seeded
+# SplitMix64 noise keyed by (seed, Morton id, interior cell index).
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix64(x):
+    with np.errstate(over="ignore"):
+        x = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        x = ((x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        x = ((x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return x ^ (x >> np.uint64(31))
+
+
+def unit_hash(a, b, c):
+    """SplitMix64-based uniform in [0, 1) of three 64-bit keys."""
+    a, b, c = (np.asarray(v, dtype=np.uint64) for v in (a, b, c))
+    h = _mix64(a ^ _mix64(b ^ _mix64(c)))
+    return (h >> np.uint64(11)).astype(np.float64) * 2.0**-53
+
+
+def decode_ids(ids, rank):
+    """Morton ids -> (coords[P, rank] on the 2^depth grid, level[P])."""
+    ids = np.asarray(ids, np.uint64)
+    level = (ids & np.uint64(63)).astype(np.int64)
+    m = ids >> np.uint64(6)
+    coords = np.zeros((ids.size, rank), np.int64)
+    for b in range(64 // rank):
+        for k in range(rank):
+            bit = (m >> np.uint64(rank * b + k)) & np.uint64(1)
+            coords[:, k] |= bit.astype(np.int64) << b
+    return coords, level
+
+
+def cell_centres(ids, rank, n, depth, lengths=(1.0, 1.0, 1.0)):
+    """(P, n, ..., n, rank) physical centres of interior cells; axis k of the
+    last dimension is Morton axis k (x, y, z); cell array axes follow the
+    layout (dim 0 slowest)."""
+    coords, level = decode_ids(ids, rank)
+    maxc = float(1 << depth)
+    P = coords.shape[0]
+    out = np.empty((P,) + (n,) * rank + (rank,))
+    grid = np.indices((n,) * rank)
+    for k in range(rank):
+        L = float(lengths[k])
+        origin = L * coords[:, k].astype(np.float64) / maxc
+        cs = (L * (2.0 ** (depth - level)).astype(np.float64) / maxc) / float(n)
+        data_cell = grid[rank - 1 - k].astype(np.float64)
+        shape = (P,) + (1,) * rank
+        co = origin.reshape(shape) + data_cell[None] * cs.reshape(shape)
+        out[..., k] = co + 0.5 * cs.reshape(shape)
+    return out
+
+
+def gaussian_state(ids, rank, n, halo, depth, bumps, noise=0.0, noise_seed=0, lengths=(1.0, 1.0, 1.0)):
+    """Padded state (P, n+2h, ...) with sum_b a_b exp(-|x - c_b|^2 / (2 s_b^2))
+    in the interior, plus noise * (2 U - 1); ghosts are zero."""
+    x = cell_centres(ids, rank, n, depth, lengths)
+    val = np.zeros(x.shape[:-1])
+    b = np.asarray(bumps, np.float64).reshape(-1, rank + 2)
+    for row in b:
+        r2 = np.zeros(x.shape[:-1])
+        for k in range(rank):
+            diff = x[..., k] - row[k]
+            r2 = r2 + diff * diff
+        val = val + row[rank + 1] * np.exp(-r2 / (2.0 * row[rank] * row[rank]))
+    if noise != 0.0:
+        P = val.shape[0]
+        cell = np.arange(n**rank, dtype=np.uint64).reshape((1,) + (n,) * rank)
+        idv = np.asarray(ids, np.uint64).reshape((P,) + (1,) * rank)
+        val = val + noise * (2.0 * unit_hash(np.uint64(noise_seed), idv, cell) - 1.0)
+    P1 = n + 2 * halo
+    out = np.zeros((val.shape[0],) + (P1,) * rank)
+    out[(slice(None),) + (slice(halo, n + halo),) * rank] = val
+    return out
+
+
+def seeded_bumps(rank, count, seed, sigma=(0.02, 0.06), amp=(0.5, 2.0), lo=0.15, hi=0.85):
+    """Seeded Gaussian bump parameters: centre (rank), sigma, amplitude each."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        c = rng.uniform(lo, hi, size=rank)
+        out.extend(list(c) + [rng.uniform(*sigma), rng.uniform(*amp)])
+    return [float(round(v, 6)) for v in out]

@@ -126,6 +126,12 @@ struct amr_tree {
     bool      batch_open = false;
 
     void* pinned = nullptr; // 64 bytes of readback space
+
+    // opt-in launch timing of the update kernel
+    bool                                          timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+    std::vector<uint64_t>                         event_cells;
+    size_t                                        events_used = 0;
 };
 
 namespace {
@@ -143,6 +149,10 @@ amr_status dispatch_dtype(int dtype, F&& f)
 void free_tree(amr_tree* t)
 {
     if (!t) return;
+    for (auto& e : t->events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
     cudaFree(t->cur);
     cudaFree(t->nxt);
     for (int b = 0; b < 2; ++b) {
@@ -180,6 +190,39 @@ amr_status launch_halo(amr_tree* t)
         t->ghosts_valid = true;
         return AMR_OK;
     });
+}
+
+
+// One root leaf: key 0, level 0, periodic self-neighbours (ndtree.hpp:411-421),
+// zero state in both buffers.
+amr_status init_root(amr_tree* t)
+{
+    const Geo&                 g = t->g;
+    std::vector<amr_halo_meta> root(g.ndir);
+    for (auto& m : root) {
+        m.neighbor = 0;
+        for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
+        for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
+        m.relation   = REL_SAME;
+        m.padding[0] = m.padding[1] = m.padding[2] = 0;
+    }
+    const uint64_t zero_key = 0;
+    const int32_t  zero_lev = 0;
+    const size_t   state_bytes = t->cap * g.flat * t->esize;
+    t->tb = 0;
+    AMR_CUDA(cudaMemsetAsync(t->cur, 0, state_bytes, t->stream));
+    AMR_CUDA(cudaMemsetAsync(t->nxt, 0, state_bytes, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->keys[0], &zero_key, 8, cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->levels[0], &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->maxlev, &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->meta[0], root.data(), g.ndir * sizeof(amr_halo_meta), cudaMemcpyHostToDevice,
+                             t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    t->size           = 1;
+    t->max_level_host = 0;
+    t->ghosts_valid   = true;
+    t->batch_open     = false;
+    return AMR_OK;
 }
 
 } // namespace
@@ -239,31 +282,12 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
         return cuda_fail(e, "amr_tree_create allocation");
     }
     t->coef_steps = kMaxBatch;
-    // root leaf: key 0, level 0, periodic self-neighbours (ndtree.hpp:411-421)
-    std::vector<amr_halo_meta> root(g.ndir);
-    for (auto& m : root) {
-        m.neighbor = 0;
-        for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
-        for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
-        m.relation = REL_SAME;
-        m.padding[0] = m.padding[1] = m.padding[2] = 0;
-    }
-    const uint64_t zero_key = 0;
-    const int32_t  zero_lev = 0;
-    e = cudaMemsetAsync(t->cur, 0, state_bytes, t->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(t->nxt, 0, state_bytes, t->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(t->keys[0], &zero_key, 8, cudaMemcpyHostToDevice, t->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(t->levels[0], &zero_lev, 4, cudaMemcpyHostToDevice, t->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(t->maxlev, &zero_lev, 4, cudaMemcpyHostToDevice, t->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(t->meta[0], root.data(), g.ndir * sizeof(amr_halo_meta), cudaMemcpyHostToDevice, t->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(t->stream);
-    if (e != cudaSuccess) {
+    amr_status rs = init_root(t);
+    if (rs != AMR_OK) {
         free_tree(t);
-        return cuda_fail(e, "amr_tree_create init");
+        return rs;
     }
-    t->size = 1;
-    *out    = t;
+    *out = t;
     return AMR_OK;
 }
 
@@ -306,6 +330,21 @@ amr_status amr_tree_download_state(amr_tree* t, void* host, size_t num)
     AMR_CUDA(cudaMemcpyAsync(host, t->cur, num * t->g.flat * t->esize, cudaMemcpyDeviceToHost, t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     return AMR_OK;
+}
+
+amr_status amr_tree_load_state_device(amr_tree* t, const void* device_state, size_t num)
+{
+    if (!t || !device_state) return fail(AMR_ERR_INVALID, "null argument");
+    if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
+    AMR_CUDA(cudaMemcpyAsync(t->cur, device_state, num * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
+    t->ghosts_valid = true;
+    return AMR_OK;
+}
+
+amr_status amr_tree_reset(amr_tree* t)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    return init_root(t);
 }
 
 amr_status amr_tree_device_state(amr_tree* t, void** current, void** next)
@@ -484,6 +523,20 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
         AMR_LAUNCHED("k_batch_begin");
         first = false;
         for (int k = 0; k < chunk; ++k) {
+            std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
+            if (t->timing) {
+                if (t->events_used == t->events.size()) {
+                    std::pair<cudaEvent_t, cudaEvent_t> e;
+                    AMR_CUDA(cudaEventCreate(&e.first));
+                    AMR_CUDA(cudaEventCreate(&e.second));
+                    t->events.push_back(e);
+                    t->event_cells.push_back(0);
+                }
+                ev = &t->events[t->events_used];
+                t->event_cells[t->events_used] = static_cast<uint64_t>(P) * t->g.cells;
+                ++t->events_used;
+                AMR_CUDA(cudaEventRecord(ev->first, s));
+            }
             amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
                 using T = decltype(z);
                 k_step<T, true><<<grid, 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
@@ -493,6 +546,7 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
                 return AMR_OK;
             });
             if (st != AMR_OK) return st;
+            if (ev) AMR_CUDA(cudaEventRecord(ev->second, s));
             std::swap(t->cur, t->nxt);
         }
         done += chunk;
@@ -520,6 +574,32 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
     }
     if (sum_dt) *sum_dt = acc;
     if (executed) *executed = cnt;
+    return AMR_OK;
+}
+
+amr_status amr_tree_set_timing(amr_tree* t, int enabled)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    t->timing = enabled != 0;
+    return AMR_OK;
+}
+
+amr_status amr_tree_get_timing(amr_tree* t, double* ms, uint64_t* launches, uint64_t* cells)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    double   total = 0.0;
+    uint64_t c     = 0;
+    for (size_t i = 0; i < t->events_used; ++i) {
+        float e = 0.f;
+        AMR_CUDA(cudaEventElapsedTime(&e, t->events[i].first, t->events[i].second));
+        total += e;
+        c += t->event_cells[i];
+    }
+    if (ms) *ms = total;
+    if (launches) *launches = t->events_used;
+    if (cells) *cells = c;
+    t->events_used = 0;
     return AMR_OK;
 }
 

@@ -156,6 +156,12 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out);
  * elements of the tree's dtype. */
 amr_status amr_tree_upload_state(amr_tree* t, const void* host_state, size_t num_patches);
 amr_status amr_tree_download_state(amr_tree* t, void* host_state, size_t num_patches);
+/* Device-to-device state load (same layout as upload_state). */
+amr_status amr_tree_load_state_device(amr_tree* t, const void* device_state, size_t num_patches);
+/* Back to the freshly constructed tree: one root leaf, periodic
+ * self-neighbours, zero state (ndtree::ndtree, ndtree.hpp:320-425),
+ * without reallocating. */
+amr_status amr_tree_reset(amr_tree* t);
 /* Device pointers of the current/next state buffers (get_device_buffer). */
 amr_status amr_tree_device_state(amr_tree* t, void** current, void** next);
 
@@ -192,6 +198,15 @@ amr_status amr_tree_refine_uniform(amr_tree* t, int levels);
 amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl,
                             double remaining_time);
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed_steps);
+
+/* Per-launch timing of the fused update kernel with CUDA events on the tree's
+ * stream (the counterpart of the reference's profiler ranges,
+ * include/cuda/profiler.hpp:7-30).  get_timing synchronizes, returns the
+ * summed kernel time, launch count and cell updates since the last call, and
+ * clears them. */
+amr_status amr_tree_set_timing(amr_tree* t, int enabled);
+amr_status amr_tree_get_timing(amr_tree* t, double* step_kernel_ms, uint64_t* step_launches,
+                               uint64_t* cell_updates);
 
 /* Block until all work queued on the tree's stream has finished. */
 amr_status amr_tree_synchronize(amr_tree* t);
