@@ -211,6 +211,38 @@ amr_status amr_tree_get_timing(amr_tree* t, double* step_kernel_ms, uint64_t* st
 /* Block until all work queued on the tree's stream has finished. */
 amr_status amr_tree_synchronize(amr_tree* t);
 
+/* ------------------------------------------------ allocation-free re-mesh
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory, e.g. code running inside a memory pool or arena
+ * they do not own, or a host process whose allocator is locked down.  It does
+ * what amr_tree_remesh does, on caller-owned buffers, and calls no cudaMalloc,
+ * cudaFree or other allocating routine.  Its working storage is one static
+ * device array of AMR_NOALLOC_SCRATCH_BYTES per GPU that loads the library,
+ * held until the process exits; that bounds the input to
+ * AMR_NOALLOC_MAX_LEAVES leaves, and larger inputs (or out_capacity) are
+ * rejected with AMR_ERR_INVALID.
+ *
+ * Inputs: num_leaves leaves in Morton order (ids, neighbour tables as
+ * produced by amr_tree_get_neighbors, refine/coarsen flags, FP64 padded
+ * state).  Outputs (room for out_capacity leaves): the new ids, levels,
+ * neighbour tables and state, and the new leaf count in *device_out_count
+ * and, if host_out_count is not NULL, in *host_out_count.  The call
+ * synchronizes `stream` before it returns.  AMR_ERR_CAPACITY means the new
+ * tree would not fit in out_capacity; the outputs are then undefined.
+ *
+ * The first call on each device looks up the scratch array's device address
+ * with that device current; make that first call before capturing a stream.
+ * All calls share the one array, so calls that overlap on the GPU (other
+ * streams, other host threads) race and corrupt each other's results. */
+#define AMR_NOALLOC_MAX_LEAVES 65536
+#define AMR_NOALLOC_SCRATCH_BYTES (17 * AMR_NOALLOC_MAX_LEAVES + 4096)
+amr_status amr_remesh_noalloc(const amr_patch_geometry* geom, size_t num_leaves,
+                              const uint64_t* device_ids_in, const amr_halo_meta* device_meta_in,
+                              const int8_t* device_flags, const double* device_state_in,
+                              size_t out_capacity, uint64_t* device_ids_out, int32_t* device_levels_out,
+                              amr_halo_meta* device_meta_out, double* device_state_out,
+                              uint32_t* device_out_count, size_t* host_out_count, void* stream);
+
 /* Kernel launches issued by this library since load (for launch accounting). */
 uint64_t amr_launch_count(void);
 
