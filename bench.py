@@ -115,6 +115,54 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ GPU arm
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def uniform_extra(A, torch, stream, dtype, level=9, steps=40):
+    """Kernel-level figure on an HBM-sized input: uniform 2D tree of 4^level
+    leaves (16x16 + 1 ghost), fused update only (no re-mesh), per-launch
+    kernels timed with CUDA events on the tree's stream.  Each step streams
+    both state buffers (> L2), so no flush is needed."""
+    elem = 8 if dtype == A.F64 else 4
+    t = A.Tree(2, 16, 1, level, capacity=4**level, dtype=dtype, stream=stream.cuda_stream)
+    t.refine_uniform(level)
+    rng = np.random.default_rng(5)
+    t.upload_state(rng.random((t.size, 18, 18)))
+    t.advance(5, (1.0, 0.5), 0.4)
+    t.finish_advance()
+    t.set_timing(True)
+    torch.cuda.synchronize()
+    e0, e1 = _events(torch)
+    e0.record(stream)
+    t.advance(steps, (1.0, 0.5), 0.4)
+    e1.record(stream)
+    acc, ex = t.finish_advance()
+    ms = e0.elapsed_time(e1)
+    k_ms, k_launches, k_cells = t.get_timing()
+    t.close()
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    achieved = elem * 2 * k_cells / (k_ms * 1e-3) / 1e9
+    out = {
+        "workload": f"uniform 2D tree, 4^{level} = {4**level} leaves of 16x16 + 1 ghost, {steps} steps, no re-mesh",
+        "dtype": "f64" if dtype == A.F64 else "f32",
+        "value": ex * 4**level * 256 / (ms * 1e-3),
+        "unit": UNIT,
+        "roofline": {"bound": "hbm", "kernel": f"k_step<{'double' if dtype == A.F64 else 'float'}>",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if hbm else None,
+                     "algorithmic_bytes_per_cell_update": 2 * elem,
+                     "avg_launch_us": k_ms * 1e3 / max(1, k_launches)},
+    }
+    if dtype == A.F64:
+        # the FP64 pipe is the ceiling here: 1 DMUL + 2 DFMA per 2D cell update
+        dfma = 3 * k_cells / (k_ms * 1e-3)
+        out["fp64_pipe"] = {"achieved_ops_per_s": dfma, "peak_ops_per_s": 0.60e12,
+                            "frac": dfma / 0.60e12, "peak_source": "FMA-throughput probe on this GB300 pool"}
+    return out
+
+
 def gpu_arm(args, rank, world):
     import torch
 
@@ -132,74 +180,79 @@ def gpu_arm(args, rank, world):
     init_host = torch.from_numpy(init).pin_memory()
     final_host = torch.empty((4096,) + init.shape[1:], dtype=torch.float64).pin_memory()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")
+    run_args = dict(steps=W["steps"], interval=W["remesh"], velocity=W["velocity"], cfl=W["cfl"], criterion="grad",
+                    rthr=W["rthr"], cthr=W["cthr"], min_level=W["min_level"], max_level=W["max_level"])
 
-    def run(e2e: bool):
+    def setup():
+        # topology of the initial tree: outside the timed interval, as in the
+        # reference benchmark (its timer starts after initialisation)
         tree.reset()
         tree.refine_uniform(W["init_levels"])
+
+    def run(e2e: bool, per_launch=False):
         if e2e:
             A.check(A.lib().amr_tree_upload_state(tree._h, init_host.data_ptr(), P0))
         else:
             tree.load_state_device(init_dev.data_ptr(), P0)
         tree.halo_exchange()
-        done, cells, sum_dt, leaves = 0, 0, 0.0, []
-        while done < W["steps"]:
-            k = min(W["remesh"], W["steps"] - done)
-            P = tree.size
-            tree.advance(k, W["velocity"], W["cfl"])
-            acc, ex = tree.finish_advance()
-            done += ex
-            sum_dt += acc
-            cells += ex * P * W["n"] ** W["rank"]
-            leaves.append(P)
-            tree.flags_gradient(W["rthr"], W["cthr"], W["min_level"], W["max_level"])
-            tree.remesh()
+        st = tree.run(per_launch=per_launch, **run_args)
         d2h = 0
         if e2e:
             P = tree.size
             A.check(A.lib().amr_tree_download_state(tree._h, final_host.data_ptr(), P))
             d2h = P * tree.flat * 8
-        return cells, sum_dt, leaves, d2h
+        return st, d2h
 
-    def timed(e2e: bool, k: int):
-        total_ms, total_cells, launches, d2h_total = 0.0, 0, 0, 0
-        leaves_all = []
+    def timed(e2e: bool, k: int, per_launch=False):
+        total_ms, launches, d2h_total, stats = 0.0, 0, 0, []
         for _ in range(k):
+            setup()
             flush.zero_()
             torch.cuda.synchronize()
             if world > 1:
                 torch.distributed.barrier()
             l0 = A.launch_count()
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0, ev1 = _events(torch)
             ev0.record(stream)
-            cells, sum_dt, leaves, d2h = run(e2e)
+            st, d2h = run(e2e, per_launch)
             ev1.record(stream)
             torch.cuda.synchronize()
             launches += A.launch_count() - l0
             total_ms += ev0.elapsed_time(ev1)
-            total_cells += cells
             d2h_total += d2h
-            leaves_all += leaves
-        return total_ms, total_cells, launches, d2h_total, leaves_all, sum_dt
+            stats.append(st)
+        return total_ms, launches, d2h_total, stats
 
     for _ in range(args.warmup):
+        setup()
         run(False)
     clocks = ClockSampler(dev)
     clocks.start()
-    ms, cells, launches, _, leaves, sum_dt = timed(False, args.steps)
+    ms, launches, _, stats = timed(False, args.steps)
     clock_info = clocks.stop()
-    e2e_ms, e2e_cells, _, d2h_total, _, _ = timed(True, args.steps)
+    cells = sum(s["cell_updates"] for s in stats)
+    e2e_ms, _, d2h_total, e2e_stats = timed(True, args.steps)
+    e2e_cells = sum(s["cell_updates"] for s in e2e_stats)
+    pl_ms, pl_launches, _, pl_stats = timed(False, 1, per_launch=True)
+    pl_cells = sum(s["cell_updates"] for s in pl_stats)
 
-    # dominant kernel (fused update) over a second pass of the same timed runs,
-    # with CUDA events around every launch on the tree's stream
+    # dominant kernel over a second pass of the same timed runs, CUDA events
+    # around every launch of it on the tree's stream
     tree.set_timing(True)
     for _ in range(args.steps):
+        setup()
         flush.zero_()
         torch.cuda.synchronize()
         run(False)
     k_ms, k_launches, k_cells = tree.get_timing()
     tree.set_timing(False)
 
-    # whole-job aggregation over ranks (replicas): max time, summed work
+    extras = {}
+    if not args.no_extras:
+        lv = args.uniform_level
+        extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)
+        extras[f"uniform_fp32_level{lv}"] = uniform_extra(A, torch, stream, A.F32, lv)
+
     if world > 1:
         t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{dev}")
         c = torch.tensor([float(cells), float(e2e_cells)], dtype=torch.float64, device=f"cuda:{dev}")
@@ -214,16 +267,17 @@ def gpu_arm(args, rank, world):
     alg_bytes = 16.0 * k_cells  # one read + one write of an FP64 cell per update
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
     traffic = None
-    prof = REPO / "profiles" / "k_step_fp64_config2.json"
+    prof = REPO / "profiles" / "k_cycle_fp64_config2.json"
     if prof.exists():
         try:
             traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
         except Exception:
             traffic = None
-    value = cells / (ms * 1e-3)
+    persistent = all(s["persistent_intervals"] == s["intervals"] for s in stats)
+    leaves = [(s["leaves_min"], s["leaves_max"], s["leaves_mean"]) for s in stats]
     line = {
         "metric": METRIC,
-        "value": value,
+        "value": cells / (ms * 1e-3),
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
@@ -238,21 +292,23 @@ def gpu_arm(args, rank, world):
             "workload": WORKLOAD_NAME,
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
             "l2": "flushed (256 MiB write) before every timed run, outside the timed interval",
-            "leaves_min": int(min(leaves)),
-            "leaves_max": int(max(leaves)),
-            "leaves_mean": float(np.mean(leaves)),
-            "remesh_per_run": W["steps"] // W["remesh"],
-            "sum_dt_per_run": sum_dt,
+            "step": "one complete 2000-step run (200 re-meshes) from the initial state",
+            "leaves_min": int(min(l[0] for l in leaves)),
+            "leaves_max": int(max(l[1] for l in leaves)),
+            "leaves_mean": float(np.mean([l[2] for l in leaves])),
+            "remesh_per_run": int(stats[0]["remeshes"]),
+            "sum_dt_per_run": stats[0]["sum_dt"],
+            "driver": "one persistent cluster kernel per run" if persistent else "mixed persistent/per-launch",
         },
         "e2e": {
             "value": e2e_cells / (e2e_ms * 1e-3),
             "unit": UNIT,
-            "h2d_bytes_per_step": int(P0 * init.shape[1] * init.shape[2] * 8),
+            "h2d_bytes_per_step": int(init.nbytes),
             "d2h_bytes_per_step": int(d2h_total / max(1, args.steps)),
         },
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_step<double> (fused halo + upwind update)",
+            "kernel": "k_cycle<double> (persistent: fused updates, flags, re-mesh)" if persistent else "k_step<double>",
             "achieved": achieved,
             "peak": hbm,
             "unit": "GB/s",
@@ -262,10 +318,14 @@ def gpu_arm(args, rank, world):
             "launches": k_launches,
             "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
+            "note": "the workload is L2-resident (<= 43 leaves, ~0.1 MB); the figure shows latency, not bandwidth",
         },
+        "per_launch_driver": {"value": pl_cells / (pl_ms * 1e-3), "unit": UNIT, "gpu_launches": int(pl_launches),
+                              "note": "same runs with per-launch kernels and host round trips each interval"},
         "clocks": clock_info,
         "gpu_launches": int(launches),
     }
+    line.update(extras)
     return line
 
 
@@ -339,6 +399,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--extras-only", action="store_true", help="only the uniform kernel-level workloads")
+    ap.add_argument("--uniform-level", type=int, default=9)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -352,6 +415,16 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
+    if args.extras_only:
+        import torch
+
+        import amr_gb300 as A
+
+        stream = torch.cuda.Stream()
+        out = {f"uniform_fp64_level{args.uniform_level}": uniform_extra(A, torch, stream, A.F64, args.uniform_level),
+               f"uniform_fp32_level{args.uniform_level}": uniform_extra(A, torch, stream, A.F32, args.uniform_level)}
+        print(json.dumps(out), flush=True)
+        return
     line = gpu_arm(args, rank, world)
     if line is not None:
         if not args.no_cpu_baseline:

@@ -44,6 +44,23 @@ class TreeDesc(C.Structure):
     _fields_ = [("geom", PatchGeometry), ("capacity", C.c_size_t), ("dtype", C.c_int32), ("stream", C.c_void_p)]
 
 
+class CycleParams(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("remesh_interval", C.c_uint64), ("velocity", C.c_double * 3),
+                ("cfl", C.c_double), ("remaining_time", C.c_double), ("criterion", C.c_int32),
+                ("min_level", C.c_int32), ("max_level", C.c_int32), ("options", C.c_int32),
+                ("refine_threshold", C.c_double), ("coarsen_threshold", C.c_double)]
+
+
+class CycleStats(C.Structure):
+    _fields_ = [("executed_steps", C.c_uint64), ("sum_dt", C.c_double), ("cell_updates", C.c_uint64),
+                ("remeshes", C.c_uint64), ("intervals", C.c_uint64), ("leaves_min", C.c_uint64),
+                ("leaves_max", C.c_uint64), ("leaves_mean", C.c_double), ("persistent_intervals", C.c_uint64)]
+
+
+CRITERIA = {"none": 0, "grad": 1, "gradient": 1, "max": 2}
+RUN_PER_LAUNCH = 1
+
+
 class TransferTask(C.Structure):
     _fields_ = [("source_patch", C.c_int32), ("destination_patch", C.c_int32)]
 
@@ -83,6 +100,7 @@ def lib():
         L.amr_tree_advance.argtypes = [vp, sz, C.POINTER(dbl), dbl, dbl]
         L.amr_tree_finish_advance.argtypes = [vp, C.POINTER(dbl), C.POINTER(sz)]
         L.amr_tree_synchronize.argtypes = [vp]
+        L.amr_tree_run.argtypes = [vp, C.POINTER(CycleParams), C.POINTER(CycleStats)]
         L.amr_tree_set_timing.argtypes = [vp, i32]
         L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.amr_halo_exchange_f64.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
@@ -227,6 +245,23 @@ class Tree:
         acc, ex = C.c_double(), C.c_size_t()
         check(lib().amr_tree_finish_advance(self._h, C.byref(acc), C.byref(ex)))
         return acc.value, ex.value
+
+    def run(self, steps, interval, velocity, cfl, criterion="grad", rthr=0.05, cthr=0.01, min_level=1,
+            max_level=5, remaining=1.7976931348623157e308, per_launch=False) -> dict:
+        """The benchmark loop (advance `interval` steps, flag, re-mesh) for
+        `steps` steps; returns the run statistics."""
+        prm = CycleParams()
+        prm.steps, prm.remesh_interval = steps, interval
+        for i, v in enumerate(list(velocity)[:3]):
+            prm.velocity[i] = float(v)
+        prm.cfl, prm.remaining_time = cfl, remaining
+        prm.criterion = CRITERIA[criterion]
+        prm.min_level, prm.max_level = min_level, max_level
+        prm.refine_threshold, prm.coarsen_threshold = rthr, cthr
+        prm.options = RUN_PER_LAUNCH if per_launch else 0
+        st = CycleStats()
+        check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
+        return {f: getattr(st, f) for f, _ in CycleStats._fields_}
 
     def set_timing(self, enabled: bool):
         check(lib().amr_tree_set_timing(self._h, int(enabled)))

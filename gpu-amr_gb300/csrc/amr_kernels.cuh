@@ -1,5 +1,10 @@
-// Kernels of the GB300 AMR hot path.  Every kernel takes plain device pointers
-// and a Geo by value; launch helpers live in amr_tree.cu.
+// Kernels of the GB300 AMR hot path.
+//
+// Every per-item body is a __device__ function so the same arithmetic runs in
+// the per-launch kernels below and in the persistent cluster kernel
+// (amr_cycle.cuh).  Pointers into buffers that a persistent kernel rewrites
+// between phases are passed without __restrict__ so no load goes through the
+// non-coherent path.
 #pragma once
 
 #include "amr_device.cuh"
@@ -15,13 +20,89 @@ struct Coef {
     double c0, c[3];
 };
 
+__host__ __device__ inline Coef make_coef(const Geo& g, double dt, const double* v, int level)
+{
+    Coef   c;
+    double tot = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        c.c[a] = 0.0;
+        if (a < g.rank) {
+            c.c[a] = (dt / cell_size(g, a, level)) * fabs(v[a]);
+            tot += c.c[a];
+        }
+    }
+    c.c0 = 1.0 - tot;
+    return c;
+}
+
+// Raw CFL step of compute_time_step_cpu (amr_solver.hpp:355-413): the
+// advection wave speed is |v| in every cell, so the minimum over cells of
+// dx/|v| is attained on the finest level present.
+__host__ __device__ inline double raw_dt(const Geo& g, const double* v, int max_level)
+{
+    double raw = 1.7976931348623157e308;
+    for (int a = 0; a < g.rank; ++a) {
+        const double sp = fabs(v[a]);
+        if (sp > 1e-12) raw = fmin(raw, cell_size(g, a, max_level) / sp);
+    }
+    return raw;
+}
+
+// The clamp of finalize_step_dt_kernel (fvm_time_step.cu:204-233).
+__host__ __device__ inline double clamp_step(double raw, double cfl, double rem)
+{
+    double dt = raw * cfl;
+    if (rem <= 0.0) dt = 0.0;
+    else if (dt > rem) dt = rem;
+    return dt;
+}
+
+__device__ inline void interior_coords(const Geo& g, int c, int* idx)
+{
+    idx[2] = 0;
+    for (int L = g.rank - 1; L >= 0; --L) {
+        idx[L] = c % g.n + g.h;
+        c /= g.n;
+    }
+}
+
 // ------------------------------------------------------------ time step
-// One forward-Euler step over `P` patches.  Ghost values on the upwind faces
-// come from the neighbour patches through the halo rules (GhostsOnTheFly) or
-// from the padded buffer itself (the reference's launch contract, where the
-// caller exchanged halos first).
-// With CoefFromDt the coefficients are formed per patch in shared memory from
-// the device dt (drop-in launcher, no per-step table); ppb <= 64.
+// Interior cell c of patch p: u' = c0 u + sum_a c_a u_up(a).  Upwind values
+// outside the interior come from the neighbour patches through the halo rules
+// (GhostsOnTheFly) or from the padded buffer (the caller exchanged halos).
+template <typename T, bool GhostsOnTheFly>
+__device__ inline void step_cell(const T* in, T* out, const amr_halo_meta* meta, const Geo& g, const Coef& cf,
+                                 const int* up, int p, int c)
+{
+    int idx[3];
+    interior_coords(g, c, idx);
+    const size_t base = static_cast<size_t>(p) * g.flat;
+    const int    li   = padded_index(g, idx);
+    const T      u    = in[base + li];
+    T            acc  = static_cast<T>(cf.c0) * u;
+    for (int a = 0; a < g.rank; ++a) {
+        const int dirn = up[a];
+        if (dirn == 0) continue;
+        const int L    = g.rank - 1 - a;
+        const int nidx = idx[L] + dirn;
+        T         val;
+        if (!GhostsOnTheFly || (nidx >= g.h && nidx < g.n + g.h)) {
+            val = in[base + li + dirn * g.s[L]];
+        } else {
+            int G[3] = { idx[0], idx[1], idx[2] };
+            G[L]     = nidx;
+            const int pos = dirn > 0 ? 1 : 0;
+            val = static_cast<T>(
+                ghost_value<T>(in, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos, g, in + base));
+        }
+        acc = fma(static_cast<T>(cf.c[a]), val, acc);
+    }
+    out[base + li] = acc;
+}
+
+// One step over P patches; ppb patches per block.  With CoefFromDt the
+// coefficients are formed per patch in shared memory from the device dt
+// (drop-in launcher, no per-step table); ppb <= 64.
 template <typename T, bool GhostsOnTheFly, bool CoefFromDt = false>
 __global__ void __launch_bounds__(256)
 k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
@@ -37,95 +118,94 @@ k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict_
         const int q = threadIdx.x;
         if (q < ppb && p0 + q < P) {
             const double v[3] = { v0, v1, v2 };
-            const double dt   = *dt_dev;
-            const int    lev  = levels[p0 + q];
-            Coef         c;
-            double       tot = 0.0;
-            for (int a = 0; a < 3; ++a) {
-                c.c[a] = 0.0;
-                if (a < g.rank) {
-                    c.c[a] = (dt / cell_size(g, a, lev)) * fabs(v[a]);
-                    tot += c.c[a];
-                }
-            }
-            c.c0     = 1.0 - tot;
-            local[q] = c;
+            local[q]          = make_coef(g, *dt_dev, v, levels[p0 + q]);
         }
         __syncthreads();
     }
     for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
         const int p = p0 + t / cells;
         if (p >= P) break;
-        int c = t - (p - p0) * cells;
-        int idx[3];
-        for (int L = g.rank - 1; L >= 0; --L) {
-            idx[L] = c % g.n + g.h;
-            c /= g.n;
-        }
-        if (g.rank == 2) idx[2] = 0;
-        const size_t base = static_cast<size_t>(p) * g.flat;
-        const int    li   = padded_index(g, idx);
-        const Coef   cf   = CoefFromDt ? local[p - p0] : coef[levels[p]];
-        const T      u    = in[base + li];
-        T            acc  = static_cast<T>(cf.c0) * u;
-        for (int a = 0; a < g.rank; ++a) {
-            const int dirn = up[a];
-            if (dirn == 0) continue;
-            const int L    = g.rank - 1 - a;
-            const int nidx = idx[L] + dirn;
-            T         val;
-            if (!GhostsOnTheFly || (nidx >= g.h && nidx < g.n + g.h)) {
-                val = in[base + li + dirn * g.s[L]];
-            } else {
-                int G[3] = { idx[0], idx[1], idx[2] };
-                G[L]     = nidx;
-                const int pos = dirn > 0 ? 1 : 0;
-                val = static_cast<T>(ghost_value<T>(in, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos],
-                                                    G, L, pos, g, in + base));
-            }
-            acc = fma(static_cast<T>(cf.c[a]), val, acc);
-        }
-        out[base + li] = acc;
+        const Coef cf = CoefFromDt ? local[p - p0] : coef[levels[p]];
+        step_cell<T, GhostsOnTheFly>(in, out, meta, g, cf, up, p, t - (p - p0) * cells);
     }
 }
 
 // --------------------------------------------------------- halo exchange
-// One thread per face ghost cell: P * 2*rank * h * n^(rank-1) cells.  Only
+// Face ghost cell t of the P * 2*rank * h * n^(rank-1) ghost cells.  Only
 // interior cells are read, so the in-place update has no read/write overlap.
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_halo(T* __restrict__ buf, const amr_halo_meta* __restrict__ meta, long long total, Geo g)
+__device__ inline void halo_cell(T* buf, const amr_halo_meta* meta, const Geo& g, long long t)
 {
     const long long per_dir   = static_cast<long long>(g.h) * (g.cells / g.n);
     const long long per_patch = per_dir * g.ndir;
-    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
-         t += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const long long p   = t / per_patch;
-        long long       r   = t - p * per_patch;
-        const int       d   = static_cast<int>(r / per_dir);
-        int             f   = static_cast<int>(r - d * per_dir);
-        const int       L   = d / 2, pos = d % 2;
-        int             G[3] = { 0, 0, 0 };
-        // tangential coordinates (row-major over the other dims), then layer
-        for (int k = g.rank - 1; k >= 0; --k) {
-            if (k == L) continue;
-            G[k] = f % g.n + g.h;
-            f /= g.n;
-        }
-        const int layer = f; // 0..h-1
-        G[L]            = pos ? g.n + g.h + layer : layer;
-        const amr_halo_meta m = meta[p * g.ndir + d];
-        if (m.relation == REL_NONE) continue;
-        T* self = buf + p * g.flat;
-        self[padded_index(g, G)] = static_cast<T>(ghost_value<T>(buf, g.flat, m, G, L, pos, g, self));
+    const long long p         = t / per_patch;
+    const long long r         = t - p * per_patch;
+    const int       d         = static_cast<int>(r / per_dir);
+    int             f         = static_cast<int>(r - d * per_dir);
+    const int       L = d / 2, pos = d % 2;
+    int             G[3] = { 0, 0, 0 };
+    for (int k = g.rank - 1; k >= 0; --k) { // tangential coordinates, then layer
+        if (k == L) continue;
+        G[k] = f % g.n + g.h;
+        f /= g.n;
     }
+    G[L]                  = pos ? g.n + g.h + f : f;
+    const amr_halo_meta m = meta[p * g.ndir + d];
+    if (m.relation == REL_NONE) return;
+    T* self                  = buf + p * g.flat;
+    self[padded_index(g, G)] = static_cast<T>(ghost_value<T>(buf, g.flat, m, G, L, pos, g, self));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_halo(T* __restrict__ buf, const amr_halo_meta* __restrict__ meta,
+                                              long long total, Geo g)
+{
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+        halo_cell<T>(buf, meta, g, t);
 }
 
 // ------------------------------------------------------------------ flags
-// max|grad u|*h from central differences over face ghosts, evaluated in
-// double with explicit rounding (no contraction) so the oracle's arithmetic
-// is reproduced bit for bit; any/all patch rule of
-// dg_helpers/globals/amr_indicators.hpp:186-225.
+// max|grad u|*h at interior cell c of patch p: central differences over face
+// ghosts, evaluated in double with explicit rounding (no contraction) so the
+// oracle's arithmetic is reproduced bit for bit.  Ghosts come from the buffer
+// or, with GhostsOnTheFly, from the neighbours by the halo rules.
+template <typename T, bool GhostsOnTheFly>
+__device__ inline double gradient_cell(const T* buf, const amr_halo_meta* meta, const Geo& g, int p, int c)
+{
+    int idx[3];
+    interior_coords(g, c, idx);
+    const T*  u  = buf + static_cast<size_t>(p) * g.flat;
+    const int li = padded_index(g, idx);
+    double    s  = 0.0;
+    for (int a = 0; a < g.rank; ++a) {
+        const int L = g.rank - 1 - a;
+        double    side[2];
+        for (int pos = 0; pos < 2; ++pos) {
+            const int nidx = idx[L] + (pos ? 1 : -1);
+            if (!GhostsOnTheFly || (nidx >= g.h && nidx < g.n + g.h)) {
+                side[pos] = static_cast<double>(u[li + (pos ? g.s[L] : -g.s[L])]);
+            } else {
+                int G[3] = { idx[0], idx[1], idx[2] };
+                G[L]     = nidx;
+                side[pos] = ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos,
+                                           g, u);
+            }
+        }
+        const double gr = __dmul_rn(0.5, __dsub_rn(side[1], side[0]));
+        s               = __dadd_rn(s, __dmul_rn(gr, gr));
+    }
+    return __dsqrt_rn(s);
+}
+
+// Patch decision from the any/all rule of
+// dg_helpers/globals/amr_indicators.hpp:186-225 with the level bounds of
+// bench_fvm_solver_integration_active_amr.b.cpp:92-102.
+__device__ inline int8_t gradient_decision(int any, int all, int level, int min_level, int max_level)
+{
+    return (level < max_level && any) ? FLAG_REFINE : (level > min_level && all) ? FLAG_COARSEN : FLAG_STABLE;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_flags_gradient(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g,
@@ -133,36 +213,35 @@ k_flags_gradient(const T* __restrict__ buf, const int32_t* __restrict__ levels, 
 {
     const int p = blockIdx.x;
     if (p >= P) return;
-    const T* u   = buf + static_cast<size_t>(p) * g.flat;
-    int      any = 0, all = 1;
-    const int st[3] = { 1, g.rank == 2 ? g.s[0] : g.s[1], g.rank == 3 ? g.s[0] : 0 };
+    int any = 0, all = 1;
     for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
-        int idx[3] = { 0, 0, 0 }, cc = c;
-        for (int L = g.rank - 1; L >= 0; --L) {
-            idx[L] = cc % g.n + g.h;
-            cc /= g.n;
-        }
-        const int li = padded_index(g, idx);
-        double    s  = 0.0;
-        for (int a = 0; a < g.rank; ++a) {
-            const double gr = __dmul_rn(0.5, __dsub_rn(static_cast<double>(u[li + st[a]]),
-                                                       static_cast<double>(u[li - st[a]])));
-            s = __dadd_rn(s, __dmul_rn(gr, gr));
-        }
-        const double v = __dsqrt_rn(s);
+        const double v = gradient_cell<T, false>(buf, nullptr, g, p, c);
         if (v > rthr) any = 1;
         if (!(v < cthr)) all = 0;
     }
     any = __syncthreads_or(any);
     all = __syncthreads_and(all);
-    if (threadIdx.x == 0) {
-        const int level = levels[p];
-        flags[p] = (level < max_level && any) ? FLAG_REFINE : (level > min_level && all) ? FLAG_COARSEN : FLAG_STABLE;
-    }
+    if (threadIdx.x == 0) flags[p] = gradient_decision(any, all, levels[p], min_level, max_level);
 }
 
 // Max-value rule (fvm_refinement_criterion.cu:27-67, tests'
 // advection_equation_amr.t.cpp:155-170) over interior and face-ghost cells.
+__device__ inline bool face_or_interior(const Geo& g, int c)
+{
+    int outside = 0;
+    for (int L = g.rank - 1; L >= 0; --L) {
+        const int i = c % g.P1;
+        c /= g.P1;
+        outside += (i < g.h || i >= g.n + g.h) ? 1 : 0;
+    }
+    return outside <= 1;
+}
+
+__device__ inline int8_t max_decision(double mx, int level, double rthr, double cthr, int min_level, int max_level)
+{
+    return (mx > rthr && level < max_level) ? FLAG_REFINE : (mx < cthr && level > min_level) ? FLAG_COARSEN : FLAG_STABLE;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g, double rthr,
@@ -172,15 +251,8 @@ k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P
     if (p >= P) return;
     const T* u = buf + static_cast<size_t>(p) * g.flat;
     double   m = 0.0;
-    for (int c = threadIdx.x; c < g.flat; c += blockDim.x) {
-        int outside = 0, cc = c;
-        for (int L = g.rank - 1; L >= 0; --L) {
-            const int i = cc % g.P1;
-            cc /= g.P1;
-            outside += (i < g.h || i >= g.n + g.h) ? 1 : 0;
-        }
-        if (outside <= 1) m = fmax(m, static_cast<double>(u[c]));
-    }
+    for (int c = threadIdx.x; c < g.flat; c += blockDim.x)
+        if (face_or_interior(g, c)) m = fmax(m, static_cast<double>(u[c]));
     __shared__ double red[128];
     red[threadIdx.x] = m;
     __syncthreads();
@@ -188,74 +260,45 @@ k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P
         if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const double mx    = red[0];
-        const int    level = levels[p];
-        flags[p] = (mx > rthr && level < max_level) ? FLAG_REFINE : (mx < cthr && level > min_level) ? FLAG_COARSEN : FLAG_STABLE;
-    }
+    if (threadIdx.x == 0) flags[p] = max_decision(red[0], levels[p], rthr, cthr, min_level, max_level);
 }
 
 // ------------------------------------------------------------- time step dt
-// Per-batch prologue (one thread per instance): the CFL step size of
-// compute_time_step_cpu (amr_solver.hpp:355-413; the advection wave speed is
-// |v| in every cell, so the minimum over cells is attained at the finest
-// level), clamped like finalize_step_dt_kernel (fvm_time_step.cu:204-233),
-// and the per-(step, level) update coefficients.
-__global__ void k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel,
-                              int ninst, double cfl, int steps, int reset, double remaining0,
-                              double* __restrict__ acc, double* __restrict__ remaining,
-                              uint32_t* __restrict__ count, double* __restrict__ step_dt,
-                              Coef* __restrict__ coef)
+// Per-batch prologue for one instance (one block): thread 0 walks the step
+// sizes of the batch (the clamp is sequential in the remaining time), then
+// the block fills the (step, level) coefficient table in parallel.
+__global__ void __launch_bounds__(256)
+k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
+              int reset, double remaining0, double* __restrict__ acc, double* __restrict__ remaining,
+              uint32_t* __restrict__ count, double* __restrict__ step_dt, Coef* __restrict__ coef)
 {
-    const int inst = blockIdx.x * blockDim.x + threadIdx.x;
-    if (inst >= ninst) return;
-    const double* v    = vel + 3 * inst;
-    const int     lmax = max_level[inst];
-    double        raw  = 1.7976931348623157e308;
-    for (int a = 0; a < g.rank; ++a) {
-        const double sp = fabs(v[a]);
-        if (sp > 1e-12) raw = fmin(raw, cell_size(g, a, lmax) / sp);
-    }
-    if (reset) {
-        acc[inst]       = 0.0;
-        remaining[inst] = remaining0;
-        count[inst]     = 0;
-    }
-    double   rem = remaining[inst], sum = acc[inst];
-    uint32_t cnt = count[inst];
-    const int nl = g.depth + 1;
-    for (int s = 0; s < steps; ++s) {
-        double dt = raw * cfl;
-        if (rem <= 0.0) dt = 0.0;
-        else if (dt > rem) dt = rem;
-        sum += dt;
-        if (dt > 0.0) {
-            rem -= dt;
-            ++cnt;
-        }
-        step_dt[static_cast<size_t>(s) * ninst + inst] = dt;
-        Coef* row = coef + (static_cast<size_t>(s) * ninst + inst) * nl;
-        for (int l = 0; l < nl; ++l) {
-            Coef   c;
-            double tot = 0.0;
-            for (int a = 0; a < 3; ++a) {
-                c.c[a] = 0.0;
-                if (a < g.rank) {
-                    const double lam = dt / cell_size(g, a, l);
-                    c.c[a]           = lam * fabs(v[a]);
-                    tot += c.c[a];
-                }
+    __shared__ double dts[1024];
+    const double      v[3] = { vel[0], vel[1], vel[2] };
+    if (threadIdx.x == 0) {
+        const double raw = raw_dt(g, v, max_level[0]);
+        double       rem = reset ? remaining0 : remaining[0];
+        double       sum = reset ? 0.0 : acc[0];
+        uint32_t     cnt = reset ? 0u : count[0];
+        for (int s = 0; s < steps; ++s) {
+            const double dt = clamp_step(raw, cfl, rem);
+            sum += dt;
+            if (dt > 0.0) {
+                rem -= dt;
+                ++cnt;
             }
-            c.c0   = 1.0 - tot;
-            row[l] = c;
+            dts[s]     = dt;
+            step_dt[s] = dt;
         }
+        acc[0]       = sum;
+        remaining[0] = rem;
+        count[0]     = cnt;
     }
-    acc[inst]       = sum;
-    remaining[inst] = rem;
-    count[inst]     = cnt;
+    __syncthreads();
+    const int nl = g.depth + 1;
+    for (int e = threadIdx.x; e < steps * nl; e += blockDim.x) coef[e] = make_coef(g, dts[e / nl], v, e % nl);
 }
 
-// Maximum level over a level array (per instance: keys carry the instance).
+// Maximum level over a level array.
 __global__ void k_max_level(const int32_t* __restrict__ levels, int P, int32_t* __restrict__ out)
 {
     int m = 0;
@@ -271,11 +314,9 @@ __global__ void k_max_level(const int32_t* __restrict__ levels, int P, int32_t* 
 // candidates: a leaf that is child 0 of its parent, followed by its 2^rank-1
 // siblings, all flagged Coarsen (apply_refine_coarsen + is_coarsen_elegible,
 // ndtree.hpp:904-940, 1899-1917).
-__global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restrict__ flags, int P, Geo g,
-                       uint8_t* __restrict__ rmark, uint8_t* __restrict__ chead)
+__device__ inline void mark_leaf(const uint64_t* keys, const int8_t* flags, int P, const Geo& g, uint8_t* rmark,
+                                 uint8_t* chead, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
     const uint64_t k     = keys[i];
     const int      level = key_level(k);
     rmark[i]             = (flags[i] == FLAG_REFINE && level < g.depth) ? 1 : 0;
@@ -290,12 +331,12 @@ __global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restri
 }
 
 // One round of the 2:1 refinement closure (balancing, ndtree.hpp:1129-1165):
-// a refining leaf marks its coarser face neighbours.  Marks only grow, so
-// `depth` rounds reach the fixed point the reference's work list reaches.
-__global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, uint8_t* __restrict__ rmark)
+// a refining leaf marks its coarser face neighbours.  Marks only grow, so as
+// many rounds as the deepest level reach the fixed point the reference's
+// work list reaches.
+__device__ inline void closure_leaf(const amr_halo_meta* meta, const Geo& g, uint8_t* rmark, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P || !rmark[i]) return;
+    if (!rmark[i]) return;
     for (int d = 0; d < g.ndir; ++d) {
         const amr_halo_meta& m = meta[static_cast<size_t>(i) * g.ndir + d];
         if (m.relation == REL_COARSER) rmark[m.neighbor] = 1;
@@ -305,11 +346,9 @@ __global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, 
 // Coarsening veto (balancing, ndtree.hpp:1173-1239): a candidate parent is
 // dropped if a boundary child has a finer neighbour across that face, or a
 // same-level neighbour that refines.
-__global__ void k_veto(const amr_halo_meta* __restrict__ meta, int P, Geo g, const uint8_t* __restrict__ rmark,
-                       uint8_t* __restrict__ chead)
+__device__ inline void veto_leaf(const amr_halo_meta* meta, const Geo& g, const uint8_t* rmark, uint8_t* chead, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P || !chead[i]) return;
+    if (!chead[i]) return;
     for (int d = 0; d < g.ndir; ++d) {
         const int L = d / 2, pos = d % 2;
         for (int off = 0; off < g.nd; ++off) {
@@ -333,29 +372,26 @@ __device__ inline bool in_coarsen_group(const uint64_t* keys, const uint8_t* che
 
 // Output count per old leaf: 2^rank for a refined leaf, 1 for the head of a
 // coarsened group (the new parent), 0 for the other members, 1 otherwise.
-__global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
-                        const uint8_t* __restrict__ chead, int P, Geo g, uint32_t* __restrict__ cnt,
-                        int32_t* __restrict__ changed)
+__device__ inline void count_leaf(const uint64_t* keys, const uint8_t* rmark, const uint8_t* chead, const Geo& g,
+                                  uint32_t* cnt, int32_t* changed, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
     uint32_t c = 1;
     if (rmark[i]) {
-        c = g.nd;
+        c        = g.nd;
         *changed = 1;
     } else if (in_coarsen_group(keys, chead, i, g)) {
-        c = chead[i] ? 1u : 0u;
+        c        = chead[i] ? 1u : 0u;
         *changed = 1;
     }
     cnt[i] = c;
 }
 
-// Exclusive scan of cnt[0..P) into pos[0..P], one block.  pos[P] = new size.
-__global__ void __launch_bounds__(1024)
-k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size_t cap,
-       int32_t* __restrict__ status)
+// Exclusive scan of cnt[0..P) into pos[0..P] by one block (part has one slot
+// per thread); pos[P] = new size; status[2] = new size, status[0] set to
+// AMR_ERR_CAPACITY when it exceeds cap.
+__device__ inline void block_scan(const uint32_t* cnt, uint32_t* pos, int P, size_t cap, int32_t* status,
+                                  uint32_t* part)
 {
-    __shared__ uint32_t part[1024];
     const int per = (P + blockDim.x - 1) / blockDim.x;
     const int lo = threadIdx.x * per, hi = min(P, lo + per);
     uint32_t  s  = 0;
@@ -363,7 +399,7 @@ k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size
     part[threadIdx.x] = s;
     __syncthreads();
     for (int o = 1; o < blockDim.x; o <<= 1) {
-        uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+        const uint32_t v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
         __syncthreads();
         part[threadIdx.x] += v;
         __syncthreads();
@@ -378,17 +414,15 @@ k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size
         status[2] = static_cast<int32_t>(part[threadIdx.x]);
         if (part[threadIdx.x] > cap) status[0] = AMR_ERR_CAPACITY;
     }
+    __syncthreads();
 }
 
 // Source descriptor of a new leaf: kind 0 copy, 1..2^rank child (offset+1)
 // of a refined leaf, -1 parent of a coarsened group.
-__global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
-                       const uint8_t* __restrict__ chead, const uint32_t* __restrict__ pos, int P, Geo g,
-                       uint64_t* __restrict__ nkeys, int32_t* __restrict__ nlevels, int32_t* __restrict__ src,
-                       int8_t* __restrict__ skind, int32_t* __restrict__ max_level)
+__device__ inline void emit_leaf(const uint64_t* keys, const uint8_t* rmark, const uint8_t* chead, const uint32_t* pos,
+                                 const Geo& g, uint64_t* nkeys, int32_t* nlevels, int32_t* src, int8_t* skind,
+                                 int32_t* max_level, int i)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
     const uint64_t k = keys[i];
     const uint32_t q = pos[i];
     const int      l = key_level(k);
@@ -419,10 +453,51 @@ __global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restr
     atomicMax(max_level + inst, lmax);
 }
 
-// New state from old: whole-patch copy, piecewise-constant prolongation
+// Interior cell c of new leaf j: copy, piecewise-constant prolongation
 // (interpolate_patch, ndtree.hpp:1528-1555) or mean restriction
 // (restrict_patches, :1499-1526; sum order of hypercube_offset,
-// patch_utils.hpp:203-234).  One block per new leaf.
+// patch_utils.hpp:203-234).
+template <typename T>
+__device__ inline void remap_cell(const T* old_state, T* new_state, const Geo& g, int kind, int srcj, int j, int c)
+{
+    int idx[3];
+    interior_coords(g, c, idx);
+    const int li   = padded_index(g, idx);
+    const T*  from = old_state + static_cast<size_t>(srcj) * g.flat;
+    T*        to   = new_state + static_cast<size_t>(j) * g.flat;
+    const int half = g.n / 2;
+    if (kind == 0) {
+        to[li] = from[li];
+    } else if (kind > 0) {
+        const int off   = kind - 1;
+        int       pc[3] = { 0, 0, 0 };
+        for (int L = 0; L < g.rank; ++L) pc[L] = g.h + child_coord(g, off, L) * half + (idx[L] - g.h) / 2;
+        to[li] = from[padded_index(g, pc)];
+    } else {
+        int child = 0, base[3] = { 0, 0, 0 };
+        for (int L = 0; L < g.rank; ++L) {
+            child   = (child << 1) | ((idx[L] - g.h) / half);
+            base[L] = ((idx[L] - g.h) % half) * 2 + g.h;
+        }
+        const T* fp  = from + static_cast<size_t>(child) * g.flat + padded_index(g, base);
+        double   sum = 0.0;
+        if (g.rank == 2) {
+            sum += static_cast<double>(fp[0]);
+            sum += static_cast<double>(fp[1]);
+            sum += static_cast<double>(fp[g.s[0]]);
+            sum += static_cast<double>(fp[g.s[0] + 1]);
+            to[li] = static_cast<T>(sum / 4.0);
+        } else {
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b)
+                    for (int e = 0; e < 2; ++e) sum += static_cast<double>(fp[a * g.s[0] + b * g.s[1] + e]);
+            to[li] = static_cast<T>(sum / 8.0);
+        }
+    }
+}
+
+// One block per new leaf; kept patches move whole (16-byte words, ghosts
+// included), new ones are built cell by cell.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_t* __restrict__ src,
@@ -431,50 +506,14 @@ k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_
     const int j = blockIdx.x;
     if (j >= P) return;
     const int kind = skind[j];
-    const T*  from = old_state + static_cast<size_t>(src[j]) * g.flat;
-    T*        to   = new_state + static_cast<size_t>(j) * g.flat;
     if (kind == 0) {
         const size_t bytes = static_cast<size_t>(g.flat) * sizeof(T);
-        const uint4* f4    = reinterpret_cast<const uint4*>(from);
-        uint4*       t4    = reinterpret_cast<uint4*>(to);
+        const uint4* f4    = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(src[j]) * g.flat);
+        uint4*       t4    = reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat);
         for (size_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) t4[w] = f4[w];
         return;
     }
-    const int half = g.n / 2;
-    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
-        int idx[3] = { 0, 0, 0 }, cc = c;
-        for (int L = g.rank - 1; L >= 0; --L) {
-            idx[L] = cc % g.n + g.h;
-            cc /= g.n;
-        }
-        const int li = padded_index(g, idx);
-        if (kind > 0) {
-            const int off = kind - 1;
-            int       pc[3] = { 0, 0, 0 };
-            for (int L = 0; L < g.rank; ++L) pc[L] = g.h + child_coord(g, off, L) * half + (idx[L] - g.h) / 2;
-            to[li] = from[padded_index(g, pc)];
-        } else {
-            int child = 0, base[3] = { 0, 0, 0 };
-            for (int L = 0; L < g.rank; ++L) {
-                child   = (child << 1) | ((idx[L] - g.h) / half);
-                base[L] = ((idx[L] - g.h) % half) * 2 + g.h;
-            }
-            const T* fp = from + static_cast<size_t>(child) * g.flat + padded_index(g, base);
-            double   sum = 0.0;
-            if (g.rank == 2) {
-                sum += static_cast<double>(fp[0]);
-                sum += static_cast<double>(fp[1]);
-                sum += static_cast<double>(fp[g.s[0]]);
-                sum += static_cast<double>(fp[g.s[0] + 1]);
-                to[li] = static_cast<T>(sum / 4.0);
-            } else {
-                for (int a = 0; a < 2; ++a)
-                    for (int b = 0; b < 2; ++b)
-                        for (int e = 0; e < 2; ++e) sum += static_cast<double>(fp[a * g.s[0] + b * g.s[1] + e]);
-                to[li] = static_cast<T>(sum / 8.0);
-            }
-        }
-    }
+    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) remap_cell<T>(old_state, new_state, g, kind, src[j], j, c);
 }
 
 __device__ inline int upper_bound_u64(const uint64_t* a, int n, uint64_t x)
@@ -494,22 +533,21 @@ __device__ inline int find_u64(const uint64_t* a, int n, uint64_t x)
     return (u > 0 && a[u - 1] == x) ? u - 1 : -1;
 }
 
-// Neighbour tables from geometry.  The reference maintains them
-// incrementally through fragment/recombine (neighbor.hpp:420-572,
-// ndtree.hpp:942-1125); on a 2:1-balanced periodic tree its tables equal
-// the geometric relation of each face:
+// Neighbour record t = (leaf, direction) from geometry.  The reference
+// maintains the tables incrementally through fragment/recombine
+// (neighbor.hpp:420-572, ndtree.hpp:942-1125); on a 2:1-balanced periodic
+// tree its tables equal the geometric relation of each face:
 //   same    : the leaf covering the adjacent same-size region,
 //   coarser : the covering leaf one level up, with the quadrant of it that
 //             touches this leaf (neighbor.hpp:367-379),
 //   finer   : the children of the adjacent region on the shared face, in
 //             compute_boundary_children order (neighbor.hpp:397-417).
 // The domain wraps in every direction (the root is its own neighbour,
-// ndtree.hpp:411-421).
-__global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr_halo_meta* __restrict__ meta,
-                            int32_t* __restrict__ status)
+// ndtree.hpp:411-421).  A face that is not 2:1 gets relation none (never an
+// invalid index) and status[0] = AMR_ERR_UNBALANCED.
+__device__ inline void neighbor_entry(const uint64_t* keys, int P, const Geo& g, amr_halo_meta* meta, int32_t* status,
+                                      int t)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P * g.ndir) return;
     const int      i = t / g.ndir, d = t % g.ndir;
     const int      L = d / 2, pos = d % 2, axis = g.rank - 1 - L;
     const uint64_t k = keys[i];
@@ -525,7 +563,7 @@ __global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr
     m.neighbor = -1;
     for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
     for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
-    m.relation = REL_NONE;
+    m.relation   = REL_NONE;
     m.padding[0] = m.padding[1] = m.padding[2] = 0;
     const int lb = b >= 0 ? key_level(keys[b]) : -1;
     if (b >= 0 && lb == l) {
@@ -537,11 +575,11 @@ __global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr
         m.relation = REL_COARSER;
         m.neighbor = b;
         for (int LL = 0; LL < g.rank; ++LL) {
-            const int ax = g.rank - 1 - LL;
+            const int ax   = g.rank - 1 - LL;
             m.quadrant[LL] = static_cast<int32_t>(((c[ax] - cb[ax]) >> (g.depth - l)) & 1u);
         }
     } else if (b >= 0 && lb > l) {
-        const uint64_t region = key_encode(g, pre, c, l);
+        const uint64_t region  = key_encode(g, pre, c, l);
         const int      opp_pos = 1 - pos;
         bool           found   = true;
         for (int off = 0; off < g.nd; ++off) {
@@ -552,13 +590,13 @@ __global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr
                 kk += child_coord(g, off, LL) * mult;
                 mult *= 2;
             }
-            const int f = find_u64(keys, P, key_child(g, region, off));
-            found       = found && f >= 0;
+            const int f     = find_u64(keys, P, key_child(g, region, off));
+            found           = found && f >= 0;
             m.finer_ids[kk] = f;
         }
         if (found) {
             m.relation = REL_FINER;
-        } else { // never leave an invalid index behind a live relation
+        } else {
             for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
             status[0] = AMR_ERR_UNBALANCED;
         }
@@ -566,6 +604,58 @@ __global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr
         status[0] = AMR_ERR_UNBALANCED;
     }
     meta[t] = m;
+}
+
+// --------------------------------------------- per-launch re-mesh kernels
+__global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restrict__ flags, int P, Geo g,
+                       uint8_t* __restrict__ rmark, uint8_t* __restrict__ chead)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) mark_leaf(keys, flags, P, g, rmark, chead, i);
+}
+
+__global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, uint8_t* rmark)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) closure_leaf(meta, g, rmark, i);
+}
+
+__global__ void k_veto(const amr_halo_meta* __restrict__ meta, int P, Geo g, const uint8_t* __restrict__ rmark,
+                       uint8_t* __restrict__ chead)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) veto_leaf(meta, g, rmark, chead, i);
+}
+
+__global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+                        const uint8_t* __restrict__ chead, int P, Geo g, uint32_t* __restrict__ cnt,
+                        int32_t* __restrict__ changed)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) count_leaf(keys, rmark, chead, g, cnt, changed, i);
+}
+
+__global__ void __launch_bounds__(1024)
+k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size_t cap, int32_t* __restrict__ status)
+{
+    __shared__ uint32_t part[1024];
+    block_scan(cnt, pos, P, cap, status, part);
+}
+
+__global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+                       const uint8_t* __restrict__ chead, const uint32_t* __restrict__ pos, int P, Geo g,
+                       uint64_t* __restrict__ nkeys, int32_t* __restrict__ nlevels, int32_t* __restrict__ src,
+                       int8_t* __restrict__ skind, int32_t* __restrict__ max_level)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) emit_leaf(keys, rmark, chead, pos, g, nkeys, nlevels, src, skind, max_level, i);
+}
+
+__global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr_halo_meta* __restrict__ meta,
+                            int32_t* __restrict__ status)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < P * g.ndir) neighbor_entry(keys, P, g, meta, status, t);
 }
 
 // --------------------------------------------------- reference drop-ins
@@ -578,11 +668,8 @@ k_intergrid(T* __restrict__ buf, const amr_transfer_task* __restrict__ tasks, in
     const amr_transfer_task tk   = tasks[task];
     const int               half = g.n / 2;
     for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
-        int idx[3] = { 0, 0, 0 }, cc = c;
-        for (int L = g.rank - 1; L >= 0; --L) {
-            idx[L] = cc % g.n + g.h;
-            cc /= g.n;
-        }
+        int idx[3];
+        interior_coords(g, c, idx);
         int child = 0, base[3] = { 0, 0, 0 };
         for (int L = 0; L < g.rank; ++L) {
             child   = (child << 1) | ((idx[L] - g.h) / half);
@@ -609,9 +696,9 @@ k_intergrid(T* __restrict__ buf, const amr_transfer_task* __restrict__ tasks, in
             const T v  = buf[static_cast<size_t>(tk.source_patch) * g.flat + ci];
             T*      fp = buf + static_cast<size_t>(tk.destination_patch + child) * g.flat + bi;
             if (g.rank == 2) {
-                fp[0] = v;
-                fp[1] = v;
-                fp[g.s[0]] = v;
+                fp[0]          = v;
+                fp[1]          = v;
+                fp[g.s[0]]     = v;
                 fp[g.s[0] + 1] = v;
             } else {
                 for (int a = 0; a < 2; ++a)
@@ -648,42 +735,14 @@ __global__ void k_gather_bytes(const unsigned char* __restrict__ src, unsigned c
 __global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, double v0, double v1, double v2,
                               double cfl, double* dt_buf, double* acc, double* remaining, uint32_t* count)
 {
-    const double v[3] = { v0, v1, v2 };
-    double       raw  = 1.7976931348623157e308;
-    for (int a = 0; a < g.rank; ++a) {
-        const double sp = fabs(v[a]);
-        if (sp > 1e-12) raw = fmin(raw, cell_size(g, a, *max_level) / sp);
-    }
-    double step_dt = raw * cfl;
-    if (*remaining <= 0.0) step_dt = 0.0;
-    else if (step_dt > *remaining) step_dt = *remaining;
-    *dt_buf = step_dt;
+    const double v[3]    = { v0, v1, v2 };
+    const double step_dt = clamp_step(raw_dt(g, v, *max_level), cfl, *remaining);
+    *dt_buf              = step_dt;
     *acc += step_dt;
     if (step_dt > 0.0) {
         *remaining -= step_dt;
         ++(*count);
     }
-}
-
-// Per-level coefficients for one step from a device dt (drop-in step).
-__global__ void k_coef_from_dt(const double* __restrict__ dt_buf, Geo g, double v0, double v1, double v2,
-                               Coef* __restrict__ coef)
-{
-    const int l = threadIdx.x;
-    if (l > g.depth) return;
-    const double v[3] = { v0, v1, v2 };
-    const double dt   = *dt_buf;
-    Coef         c;
-    double       tot = 0.0;
-    for (int a = 0; a < 3; ++a) {
-        c.c[a] = 0.0;
-        if (a < g.rank) {
-            c.c[a] = (dt / cell_size(g, a, l)) * fabs(v[a]);
-            tot += c.c[a];
-        }
-    }
-    c.c0    = 1.0 - tot;
-    coef[l] = c;
 }
 
 } // namespace amr_gb300

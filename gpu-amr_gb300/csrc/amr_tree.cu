@@ -2,6 +2,7 @@
 // drop-in launchers.  Host code only orchestrates launches; every per-leaf
 // or per-cell loop runs in a kernel from amr_kernels.cuh.
 #include <atomic>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -9,7 +10,7 @@
 #include <vector>
 
 #include "amr_gb300.h"
-#include "amr_kernels.cuh"
+#include "amr_cycle.cuh"
 
 using namespace amr_gb300;
 
@@ -126,6 +127,7 @@ struct amr_tree {
     bool      batch_open = false;
 
     void* pinned = nullptr; // 64 bytes of readback space
+    CycleStats* cstats = nullptr;
 
     // opt-in launch timing of the update kernel
     bool                                          timing = false;
@@ -175,6 +177,7 @@ void free_tree(amr_tree* t)
     cudaFree(t->dt_cnt);
     cudaFree(t->step_dt);
     cudaFree(t->coef);
+    cudaFree(t->cstats);
     if (t->pinned) cudaFreeHost(t->pinned);
     delete t;
 }
@@ -222,6 +225,66 @@ amr_status init_root(amr_tree* t)
     t->max_level_host = 0;
     t->ghosts_valid   = true;
     t->batch_open     = false;
+    return AMR_OK;
+}
+
+
+// ------------------------------------------------------------ persistent run
+constexpr int kPersistentLeaves = 1024; // above this, per-launch kernels keep all SMs busy
+constexpr int kMaxInterval      = 256;
+
+template <typename T>
+int cycle_cluster_size(size_t smem)
+{
+    static int cached[2] = { -1, -1 };
+    const int  slot      = sizeof(T) == 8 ? 0 : 1;
+    if (cached[slot] >= 0) return cached[slot];
+    int best = 0;
+    if (cudaFuncSetAttribute(k_cycle<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+        cudaFuncSetAttribute(k_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024) == cudaSuccess) {
+        for (int c : { 16, 8, 4 }) {
+            cudaLaunchConfig_t  cfg{};
+            cudaLaunchAttribute at[1];
+            at[0].id               = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim            = dim3(c, 1, 1);
+            cfg.blockDim           = dim3(kCycleThreads, 1, 1);
+            cfg.dynamicSmemBytes   = smem;
+            cfg.attrs              = at;
+            cfg.numAttrs           = 1;
+            int clusters           = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, k_cycle<T>, &cfg) == cudaSuccess && clusters >= 1) {
+                best = c;
+                break;
+            }
+        }
+    }
+    cudaGetLastError(); // a refused query leaves no sticky error
+    cached[slot] = best;
+    return best;
+}
+
+template <typename T>
+amr_status launch_cycle(amr_tree* t, CycleArgs& A, int cluster)
+{
+    const size_t smem = static_cast<size_t>(A.interval) * (A.g.depth + 1) * sizeof(Coef) +
+                        static_cast<size_t>(A.interval) * sizeof(double);
+    cudaLaunchConfig_t  cfg{};
+    cudaLaunchAttribute at[1];
+    at[0].id               = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim            = dim3(cluster, 1, 1);
+    cfg.blockDim           = dim3(kCycleThreads, 1, 1);
+    cfg.dynamicSmemBytes   = smem;
+    cfg.stream             = t->stream;
+    cfg.attrs              = at;
+    cfg.numAttrs           = 1;
+    AMR_CUDA(cudaLaunchKernelEx(&cfg, k_cycle<T>, A));
+    AMR_LAUNCHED("k_cycle");
     return AMR_OK;
 }
 
@@ -276,7 +339,8 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->dt_cnt), sizeof(uint32_t));
     al(reinterpret_cast<void**>(&t->step_dt), kMaxBatch * sizeof(double));
     al(reinterpret_cast<void**>(&t->coef), kMaxBatch * (g.depth + 1) * sizeof(Coef));
-    if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, 64);
+    al(reinterpret_cast<void**>(&t->cstats), sizeof(CycleStats));
+    if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, 256);
     if (e != cudaSuccess) {
         free_tree(t);
         return cuda_fail(e, "amr_tree_create allocation");
@@ -518,8 +582,8 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
     size_t    done  = 0;
     while (done < steps || (first && steps == 0)) {
         const int chunk = static_cast<int>(std::min(kMaxBatch, steps - done));
-        k_batch_begin<<<1, 32, 0, s>>>(t->maxlev, t->g, t->vel, 1, cfl, chunk, first ? 1 : 0, remaining, t->dt_acc,
-                                       t->dt_rem, t->dt_cnt, t->step_dt, t->coef);
+        k_batch_begin<<<1, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? 1 : 0, remaining, t->dt_acc,
+                                        t->dt_rem, t->dt_cnt, t->step_dt, t->coef);
         AMR_LAUNCHED("k_batch_begin");
         first = false;
         for (int k = 0; k < chunk; ++k) {
@@ -574,6 +638,152 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
     }
     if (sum_dt) *sum_dt = acc;
     if (executed) *executed = cnt;
+    return AMR_OK;
+}
+
+amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats* out)
+{
+    if (!t || !p) return fail(AMR_ERR_INVALID, "null argument");
+    if (p->criterion < 0 || p->criterion > 2) return fail(AMR_ERR_INVALID, "unknown criterion");
+    const Geo&  g = t->g;
+    long long   done = 0;
+    double      sum_dt = 0.0;
+    uint64_t    executed = 0, cells = 0, remeshes = 0, intervals = 0, leaves_sum = 0, persistent = 0;
+    uint64_t    lmin = ~0ull, lmax = 0;
+    const long long total = static_cast<long long>(p->steps);
+    int up[3] = { 0, 0, 0 };
+    for (int a = 0; a < g.rank; ++a) up[a] = p->velocity[a] > 0.0 ? -1 : (p->velocity[a] < 0.0 ? 1 : 0);
+    const size_t smem = static_cast<size_t>(p->remesh_interval) * (g.depth + 1) * sizeof(Coef) +
+                        static_cast<size_t>(p->remesh_interval) * sizeof(double);
+    while (done < total) {
+        const bool small = !(p->options & AMR_RUN_PER_LAUNCH) && t->size <= static_cast<size_t>(kPersistentLeaves) &&
+                           p->remesh_interval >= 1 &&
+                           p->remesh_interval <= static_cast<uint64_t>(kMaxInterval) && smem <= 64 * 1024;
+        const int cluster = small ? (t->dtype == AMR_F64 ? cycle_cluster_size<double>(smem)
+                                                         : cycle_cluster_size<float>(smem))
+                                  : 0;
+        if (cluster > 0) {
+            CycleArgs A{};
+            A.g        = g;
+            A.state[0] = t->cur;
+            A.state[1] = t->nxt;
+            for (int b = 0; b < 2; ++b) {
+                A.keys[b]   = t->keys[b];
+                A.levels[b] = t->levels[b];
+                A.meta[b]   = t->meta[b];
+            }
+            A.flags  = t->flags;
+            A.rmark  = t->rmark;
+            A.chead  = t->chead;
+            A.cnt    = t->cnt;
+            A.pos    = t->pos;
+            A.src    = t->src;
+            A.skind  = t->skind;
+            A.status = t->status;
+            A.maxlev = t->maxlev;
+            A.stats  = t->cstats;
+            for (int a = 0; a < 3; ++a) {
+                A.vel[a] = p->velocity[a];
+                A.up[a]  = up[a];
+            }
+            A.cfl         = p->cfl;
+            A.remaining   = p->remaining_time - sum_dt;
+            A.steps_total = total - done;
+            A.interval    = static_cast<int>(p->remesh_interval);
+            A.crit        = p->criterion;
+            A.rthr        = p->refine_threshold;
+            A.cthr        = p->coarsen_threshold;
+            A.min_level   = p->min_level;
+            A.max_level   = p->max_level;
+            A.P0          = static_cast<int>(t->size);
+            A.tb0         = t->tb;
+            A.max_level0  = t->max_level_host;
+            A.cap         = t->cap;
+            A.leaf_limit  = kPersistentLeaves;
+            size_t ev_slot = SIZE_MAX;
+            if (t->timing) {
+                if (t->events_used == t->events.size()) {
+                    std::pair<cudaEvent_t, cudaEvent_t> e;
+                    AMR_CUDA(cudaEventCreate(&e.first));
+                    AMR_CUDA(cudaEventCreate(&e.second));
+                    t->events.push_back(e);
+                    t->event_cells.push_back(0);
+                }
+                ev_slot = t->events_used++;
+                AMR_CUDA(cudaEventRecord(t->events[ev_slot].first, t->stream));
+            }
+            amr_status st = t->dtype == AMR_F64 ? launch_cycle<double>(t, A, cluster) : launch_cycle<float>(t, A, cluster);
+            if (st != AMR_OK) return st;
+            if (ev_slot != SIZE_MAX) AMR_CUDA(cudaEventRecord(t->events[ev_slot].second, t->stream));
+            CycleStats* hs = static_cast<CycleStats*>(t->pinned);
+            AMR_CUDA(cudaMemcpyAsync(hs, t->cstats, sizeof(CycleStats), cudaMemcpyDeviceToHost, t->stream));
+            AMR_CUDA(cudaStreamSynchronize(t->stream));
+            const CycleStats cs = *hs;
+            if (ev_slot != SIZE_MAX) t->event_cells[ev_slot] = cs.cell_updates;
+            t->size             = static_cast<size_t>(cs.P);
+            t->tb               = cs.tb;
+            if (cs.cur) std::swap(t->cur, t->nxt);
+            t->max_level_host = cs.max_level;
+            t->ghosts_valid   = false;
+            done += static_cast<long long>(cs.executed);
+            sum_dt += cs.sum_dt;
+            executed += cs.executed;
+            cells += cs.cell_updates;
+            remeshes += cs.remeshes;
+            intervals += cs.intervals;
+            persistent += cs.intervals;
+            leaves_sum += cs.leaves_sum;
+            if (cs.intervals) {
+                lmin = std::min<uint64_t>(lmin, static_cast<uint64_t>(cs.leaves_min));
+                lmax = std::max<uint64_t>(lmax, static_cast<uint64_t>(cs.leaves_max));
+            }
+            if (cs.error) return fail(static_cast<amr_status>(cs.error), "persistent re-mesh failed");
+            if (!cs.stopped) break;
+            continue;
+        }
+        // one interval with per-launch kernels
+        const long long k = (p->remesh_interval > 0 && static_cast<long long>(p->remesh_interval) < total - done)
+                                ? static_cast<long long>(p->remesh_interval)
+                                : total - done;
+        const size_t P = t->size;
+        amr_status   st = amr_tree_advance(t, static_cast<size_t>(k), p->velocity, p->cfl, p->remaining_time - sum_dt);
+        if (st != AMR_OK) return st;
+        double acc = 0.0;
+        size_t ex  = 0;
+        st         = amr_tree_finish_advance(t, &acc, &ex);
+        if (st != AMR_OK) return st;
+        done += static_cast<long long>(ex);
+        sum_dt += acc;
+        executed += ex;
+        cells += static_cast<uint64_t>(ex) * P * static_cast<uint64_t>(g.cells);
+        leaves_sum += P;
+        lmin = std::min<uint64_t>(lmin, P);
+        lmax = std::max<uint64_t>(lmax, P);
+        ++intervals;
+        if (p->criterion != 0) {
+            st = p->criterion == 1 ? amr_tree_flags_gradient(t, p->refine_threshold, p->coarsen_threshold,
+                                                             p->min_level, p->max_level)
+                                   : amr_tree_flags_max(t, p->refine_threshold, p->coarsen_threshold, p->min_level,
+                                                        p->max_level);
+            if (st != AMR_OK) return st;
+            int changed = 0;
+            st          = amr_tree_remesh(t, &changed);
+            if (st != AMR_OK) return st;
+            ++remeshes;
+        }
+        if (ex == 0) break;
+    }
+    if (out) {
+        out->executed_steps       = executed;
+        out->sum_dt               = sum_dt;
+        out->cell_updates         = cells;
+        out->remeshes             = remeshes;
+        out->intervals            = intervals;
+        out->leaves_min           = intervals ? lmin : t->size;
+        out->leaves_max           = intervals ? lmax : t->size;
+        out->leaves_mean          = intervals ? static_cast<double>(leaves_sum) / static_cast<double>(intervals) : 0.0;
+        out->persistent_intervals = persistent;
+    }
     return AMR_OK;
 }
 

@@ -199,6 +199,46 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
                             double remaining_time);
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed_steps);
 
+/* The reference benchmark loop (benchmark/bench_fvm_solver_integration_
+ * active_amr.b.cpp:220-250) as one call: repeat { advance
+ * min(remesh_interval, steps left) steps with remaining time
+ * remaining_time - (time advanced so far); flag with the criterion; re-mesh }
+ * until `steps` steps ran or the time is used up.  criterion: 0 none (no
+ * re-mesh), 1 gradient (amr_tree_flags_gradient), 2 max value
+ * (amr_tree_flags_max).  While the tree has few leaves the whole loop runs as
+ * one persistent kernel on a thread-block cluster with no host round trip;
+ * larger trees run interval by interval with per-launch kernels.  Results
+ * are identical either way. */
+typedef struct amr_cycle_params {
+    uint64_t steps;
+    uint64_t remesh_interval;
+    double   velocity[3];
+    double   cfl;
+    double   remaining_time;
+    int32_t  criterion;
+    int32_t  min_level;
+    int32_t  max_level;
+    int32_t  options;        /* AMR_RUN_PER_LAUNCH: never use the cluster kernel */
+    double   refine_threshold;
+    double   coarsen_threshold;
+} amr_cycle_params;
+
+#define AMR_RUN_PER_LAUNCH 1
+
+typedef struct amr_cycle_stats {
+    uint64_t executed_steps;   /* steps with dt > 0 */
+    double   sum_dt;
+    uint64_t cell_updates;     /* sum over intervals of executed x leaves x n^rank */
+    uint64_t remeshes;
+    uint64_t intervals;
+    uint64_t leaves_min;       /* leaf counts at interval starts */
+    uint64_t leaves_max;
+    double   leaves_mean;
+    uint64_t persistent_intervals; /* intervals run inside the cluster kernel */
+} amr_cycle_stats;
+
+amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_stats* stats);
+
 /* Per-launch timing of the fused update kernel with CUDA events on the tree's
  * stream (the counterpart of the reference's profiler ranges,
  * include/cuda/profiler.hpp:7-30).  get_timing synchronizes, returns the

@@ -227,3 +227,101 @@ def test_fp32_form_tracks_fp64(amr):
         res[dt] = (t.ids(), interior(t.download_state(), 2, 16, 1).astype(np.float64))
     np.testing.assert_array_equal(res[amr.F64][0], res[amr.F32][0])
     assert rel_l2(res[amr.F32][1], res[amr.F64][1]) <= 1e-5
+
+
+def _host_loop(amr, t, steps, interval, vel, cfl, crit, rthr, cthr, minl, maxl):
+    done, sum_dt, cells = 0, 0.0, 0
+    while done < steps:
+        k = min(interval, steps - done)
+        P = t.size
+        t.advance(k, vel, cfl)
+        acc, ex = t.finish_advance()
+        done += ex
+        sum_dt += acc
+        cells += ex * P * t.n ** t.rank
+        if crit == "grad":
+            t.flags_gradient(rthr, cthr, minl, maxl)
+        else:
+            t.flags_max(rthr, cthr, minl, maxl)
+        t.remesh()
+        if ex == 0:
+            break
+    return sum_dt, done, cells
+
+
+@pytest.mark.parametrize("name", ["config2_amr_2d", "config3_amr_3d"])
+def test_persistent_run_matches_host_loop_and_reference(amr, name):
+    """amr_tree_run (one cluster kernel per run) == the host-driven loop of
+    advance/flags/remesh, bit for bit, and == the reference fixtures."""
+    z, meta = load_golden(name)
+    p = meta["params"]
+    rank, n, h = meta["rank"], meta["n"], meta["halo"]
+    args = (int(p["steps"]), int(p["remesh"]), vel_of(meta), float(p["cfl"]))
+    crit = (float(p["rthr"]), float(p["cthr"]), int(p["min_level"]), int(p["max_level"]))
+    res = []
+    for mode in ("run", "host"):
+        t = amr.Tree(rank, n, h, meta["depth"], capacity=20000)
+        t.refine_uniform(int(p["init_levels"]))
+        t.upload_state(_pad(z["state_init"], rank, n, h))
+        t.halo_exchange()
+        if mode == "run":
+            st = t.run(*args, criterion="grad", rthr=crit[0], cthr=crit[1], min_level=crit[2], max_level=crit[3])
+            assert st["persistent_intervals"] == st["intervals"] > 0
+            out = (st["sum_dt"], st["executed_steps"], st["cell_updates"])
+        else:
+            out = _host_loop(amr, t, *args, "grad", *crit)
+        res.append((out, t.ids(), interior(t.download_state(), rank, n, h)))
+    (a, ids_a, s_a), (b, ids_b, s_b) = res
+    assert a == b
+    np.testing.assert_array_equal(ids_a, ids_b)
+    np.testing.assert_array_equal(s_a, s_b)
+    assert a[0] == float(z["sum_dt"])
+    np.testing.assert_array_equal(ids_a, z["final_ids"])
+    assert rel_l2(s_a, z["state_final"]) <= STATE_TOL
+
+
+def test_persistent_run_hands_over_to_per_launch_kernels(amr):
+    """A tree that grows past the cluster kernel's leaf limit continues with
+    per-launch kernels; the result equals the host-driven loop."""
+    import amr_gb300 as A
+
+    rank, n, h = 2, 8, 1
+    b = A.seeded_bumps(2, 3, 11, sigma=(0.01, 0.02), amp=(1.0, 2.0))
+    res = []
+    for mode in ("run", "host"):
+        t = amr.Tree(rank, n, h, 7, capacity=40000)
+        t.refine_uniform(4)
+        t.upload_state(A.gaussian_state(t.ids(), rank, n, h, 7, b))
+        t.halo_exchange()
+        if mode == "run":
+            st = t.run(60, 10, (1.0, 0.5), 0.4, "grad", 0.02, 0.005, 1, 6)
+            out = (st["sum_dt"], st["executed_steps"], st["cell_updates"])
+            assert st["leaves_max"] > 1024 and st["persistent_intervals"] < st["intervals"]
+        else:
+            out = _host_loop(amr, t, 60, 10, (1.0, 0.5), 0.4, "grad", 0.02, 0.005, 1, 6)
+        res.append((out, t.ids(), interior(t.download_state(), rank, n, h)))
+    assert res[0][0] == res[1][0]
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    np.testing.assert_array_equal(res[0][2], res[1][2])
+
+
+def test_persistent_run_max_criterion_and_fp32(amr, oracle_mod):
+    """Max-value criterion and FP32 state through the cluster kernel equal the
+    host-driven loop on the same inputs."""
+    o = oracle_mod.OracleTree(2, 10, 2, 7, 64)
+    o.init_state([0.2, 0.2, 0.05, 1.0])
+    o.halo_exchange()
+    for dt in (amr.F64, amr.F32):
+        res = []
+        for mode in ("run", "host"):
+            t = amr.Tree(2, 10, 2, 7, capacity=4096, dtype=dt)
+            t.upload_state(o.state())
+            if mode == "run":
+                st = t.run(40, 1, (1.0, 0.5), 0.4, "max", 0.1, 0.05, 1, 5)
+                out = (st["sum_dt"], st["executed_steps"])
+            else:
+                out = _host_loop(amr, t, 40, 1, (1.0, 0.5), 0.4, "max", 0.1, 0.05, 1, 5)[:2]
+            res.append((out, t.ids(), interior(t.download_state(), 2, 10, 2)))
+        assert res[0][0] == res[1][0]
+        np.testing.assert_array_equal(res[0][1], res[1][1])
+        np.testing.assert_array_equal(res[0][2], res[1][2])
