@@ -247,7 +247,7 @@ class Tree:
         return acc.value, ex.value
 
     def run(self, steps, interval, velocity, cfl, criterion="grad", rthr=0.05, cthr=0.01, min_level=1,
-            max_level=5, remaining=1.7976931348623157e308, per_launch=False) -> dict:
+            max_level=5, remaining=1.7976931348623157e308, per_launch=False, cluster=0) -> dict:
         """The benchmark loop (advance `interval` steps, flag, re-mesh) for
         `steps` steps; returns the run statistics."""
         prm = CycleParams()
@@ -258,7 +258,7 @@ class Tree:
         prm.criterion = CRITERIA[criterion]
         prm.min_level, prm.max_level = min_level, max_level
         prm.refine_threshold, prm.coarsen_threshold = rthr, cthr
-        prm.options = RUN_PER_LAUNCH if per_launch else 0
+        prm.options = (RUN_PER_LAUNCH if per_launch else 0) | ((int(cluster) & 0xFF) << 8)
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}

@@ -58,6 +58,7 @@ struct CycleArgs {
     int            interval;
     int            crit;
     double         rthr, cthr;
+    double         rthr_sq, cthr_sq; // squared-norm thresholds of the gradient rule
     int            min_level, max_level;
     int            P0, tb0, max_level0;
     size_t         cap;
@@ -66,9 +67,10 @@ struct CycleArgs {
 
 constexpr int kCycleThreads = 512;
 
+// barrier.cluster.arrive.release / wait.acquire: orders every thread's
+// earlier global and shared writes before any thread's later reads.
 __device__ __forceinline__ void cluster_barrier()
 {
-    __threadfence();
     cg::this_cluster().sync();
 }
 
@@ -104,7 +106,7 @@ __device__ inline double patch_max_on_the_fly(const T* buf, const amr_halo_meta*
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kCycleThreads) k_cycle(CycleArgs A)
+__global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
 {
     extern __shared__ unsigned char smem_raw[];
     __shared__ uint32_t part[kCycleThreads];
@@ -186,9 +188,9 @@ __global__ void __launch_bounds__(kCycleThreads) k_cycle(CycleArgs A)
             if (A.crit == 1) {
                 int any = 0, all = 1;
                 for (int c = lane; c < g.cells; c += 32) {
-                    const double v = gradient_cell<T, true>(st, mt, g, p, c);
-                    if (v > A.rthr) any = 1;
-                    if (!(v < A.cthr)) all = 0;
+                    const double s2 = gradient_sq_cell<T, true>(st, mt, g, p, c);
+                    if (s2 >= A.rthr_sq) any = 1;
+                    if (!(s2 < A.cthr_sq)) all = 0;
                 }
                 any = __any_sync(0xffffffffu, any);
                 all = __all_sync(0xffffffffu, all);
@@ -205,19 +207,26 @@ __global__ void __launch_bounds__(kCycleThreads) k_cycle(CycleArgs A)
         }
         cluster_barrier();
 
-        // ---- re-mesh (C2-C9)
+        // ---- re-mesh (C2-C9): the O(P) decisions run in block 0 with block
+        // barriers; the per-cell remap and the neighbour search use the cluster
         const uint64_t* keys = A.keys[tb];
-        for (int i = gtid; i < P; i += nthreads) mark_leaf(keys, A.flags, P, g, A.rmark, A.chead, i);
-        cluster_barrier();
-        for (int r = 0; r < (maxlevel > 1 ? maxlevel : 1); ++r) {
-            for (int i = gtid; i < P; i += nthreads) closure_leaf(mt, g, A.rmark, i);
-            cluster_barrier();
+        if (blockIdx.x == 0) {
+            for (int i = threadIdx.x; i < P; i += blockDim.x) mark_leaf(keys, A.flags, P, g, A.rmark, A.chead, i);
+            __syncthreads();
+            for (int rr = 0; rr < (maxlevel > 1 ? maxlevel : 1); ++rr) {
+                for (int i = threadIdx.x; i < P; i += blockDim.x) closure_leaf(mt, g, A.rmark, i);
+                __syncthreads();
+            }
+            for (int i = threadIdx.x; i < P; i += blockDim.x) veto_leaf(mt, g, A.rmark, A.chead, i);
+            __syncthreads();
+            for (int i = threadIdx.x; i < P; i += blockDim.x) count_leaf(keys, A.rmark, A.chead, g, A.cnt, A.status + 1, i);
+            __syncthreads();
+            block_scan(A.cnt, A.pos, P, A.cap, A.status, part);
+            if (A.status[1] && !A.status[0])
+                for (int i = threadIdx.x; i < P; i += blockDim.x)
+                    emit_leaf(keys, A.rmark, A.chead, A.pos, g, A.keys[tb ^ 1], A.levels[tb ^ 1], A.src, A.skind,
+                              A.maxlev, i);
         }
-        for (int i = gtid; i < P; i += nthreads) veto_leaf(mt, g, A.rmark, A.chead, i);
-        cluster_barrier();
-        for (int i = gtid; i < P; i += nthreads) count_leaf(keys, A.rmark, A.chead, g, A.cnt, A.status + 1, i);
-        cluster_barrier();
-        if (blockIdx.x == 0) block_scan(A.cnt, A.pos, P, A.cap, A.status, part);
         cluster_barrier();
         const int err = A.status[0], changed = A.status[1], NP = A.status[2];
         ++remeshes;
@@ -226,10 +235,6 @@ __global__ void __launch_bounds__(kCycleThreads) k_cycle(CycleArgs A)
             break;
         }
         if (changed) {
-            for (int i = gtid; i < P; i += nthreads)
-                emit_leaf(keys, A.rmark, A.chead, A.pos, g, A.keys[tb ^ 1], A.levels[tb ^ 1], A.src, A.skind, A.maxlev,
-                          i);
-            cluster_barrier();
             const T* old_state = static_cast<const T*>(A.state[cur]);
             T*       new_state = static_cast<T*>(A.state[cur ^ 1]);
             for (long long t = gtid; t < static_cast<long long>(NP) * g.cells; t += nthreads) {

@@ -137,6 +137,54 @@ __host__ __device__ inline int key_offset(const Geo& g, uint64_t k)
 // Child offset -> hypercube coordinate in layout dim L (row-major, dim 0 slowest).
 __host__ __device__ inline int child_coord(const Geo& g, int off, int L) { return (off >> (g.rank - 1 - L)) & 1; }
 
+// ------------------------------------------------- bulk async copy (TMA)
+// 1D bulk copies global -> shared completed on an mbarrier (cp.async.bulk,
+// sm_90+), and a wait on the mbarrier with an iteration cap: a copy that
+// never lands sets an error flag instead of spinning forever.
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+constexpr int kWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 // --------------------------------------------------------------- geometry
 __host__ __device__ inline double cell_size(const Geo& g, int axis, int level)
 {
@@ -145,11 +193,10 @@ __host__ __device__ inline double cell_size(const Geo& g, int axis, int level)
     return g.dx_root[axis] / static_cast<double>(1ull << level);
 }
 
-__host__ __device__ inline int padded_index(const Geo& g, const int* idx)
+__host__ __device__ __forceinline__ int padded_index(const Geo& g, const int* idx)
 {
-    int li = 0;
-    for (int L = 0; L < g.rank; ++L) li += idx[L] * g.s[L];
-    return li;
+    // s[2] == 0 and idx[2] == 0 in 2D
+    return idx[0] * g.s[0] + idx[1] * g.s[1] + idx[2] * g.s[2];
 }
 
 // ------------------------------------------------------------- halo cell
@@ -163,33 +210,46 @@ __host__ __device__ inline int padded_index(const Geo& g, const int* idx)
 //   coarser -> injection of the coarse cell picked by the contact quadrant
 //              (patch_utils.hpp:388-441)
 //   none    -> the ghost keeps its current value (:303-313).
-// The mean is formed in double for every state type.
+// The mean is formed in double for every state type.  Coordinates are held
+// in scalars (no runtime-indexed arrays) so the function stays in registers.
 template <typename T>
-__device__ inline double ghost_value(const T* __restrict__ buf, size_t pstride, const amr_halo_meta& m,
-                                     const int* G, int L, int pos, const Geo& g, const T* __restrict__ self)
+__device__ __forceinline__ double ghost_value(const T* buf, size_t pstride, const amr_halo_meta& m, const int* G, int L,
+                                              int pos, const Geo& g, const T* self)
 {
-    int from[3] = { G[0], G[1], G[2] };
-    from[L] += pos ? -g.n : g.n;
-    if (m.relation == REL_SAME) {
-        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + padded_index(g, from)]);
+    const int sh = pos ? -g.n : g.n;
+    int       f0 = G[0] + (L == 0 ? sh : 0);
+    int       f1 = G[1] + (L == 1 ? sh : 0);
+    int       f2 = G[2] + (L == 2 ? sh : 0);
+    const int rel = m.relation;
+    if (rel == REL_SAME)
+        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
+    const int half = g.n / 2;
+    if (rel == REL_COARSER) {
+        f0 = g.h + m.quadrant[0] * half + (f0 - g.h) / 2;
+        f1 = g.h + m.quadrant[1] * half + (f1 - g.h) / 2;
+        if (g.rank == 3) f2 = g.h + m.quadrant[2] * half + (f2 - g.h) / 2;
+        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
     }
-    if (m.relation == REL_COARSER) {
-        for (int k = 0; k < g.rank; ++k) from[k] = g.h + m.quadrant[k] * (g.n / 2) + (from[k] - g.h) / 2;
-        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + padded_index(g, from)]);
-    }
-    if (m.relation == REL_FINER) {
-        int fpi = 0, stride = 1;
-        for (int k = 0; k < g.rank; ++k) {
-            // the reference reduces every coordinate modulo the normal
-            // dimension's size (patch_utils.hpp:357-359); patches are cubic.
-            from[k] = ((from[k] - g.h) * 2) % g.n + g.h;
-            if (k != L) {
-                fpi += ((G[k] - g.h) / (g.n / 2)) * stride;
-                stride *= 2;
-            }
+    if (rel == REL_FINER) {
+        // the reference reduces every coordinate modulo the normal
+        // dimension's size (patch_utils.hpp:357-359); patches are cubic.
+        f0 = ((f0 - g.h) * 2) % g.n + g.h;
+        f1 = ((f1 - g.h) * 2) % g.n + g.h;
+        if (g.rank == 3) f2 = ((f2 - g.h) * 2) % g.n + g.h;
+        // section index over the tangential dims, dim 0 fastest
+        int fpi = 0, st = 1;
+        if (L != 0) {
+            fpi += ((G[0] - g.h) / half) * st;
+            st *= 2;
         }
-        const T* fp = buf + static_cast<size_t>(m.finer_ids[fpi]) * pstride + padded_index(g, from);
-        double   sum = 0.0;
+        if (L != 1) {
+            fpi += ((G[1] - g.h) / half) * st;
+            st *= 2;
+        }
+        if (g.rank == 3 && L != 2) fpi += ((G[2] - g.h) / half) * st;
+        const int id = fpi == 0 ? m.finer_ids[0] : fpi == 1 ? m.finer_ids[1] : fpi == 2 ? m.finer_ids[2] : m.finer_ids[3];
+        const T*  fp = buf + static_cast<size_t>(id) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2];
+        double    sum = 0.0;
         if (g.rank == 2) {
             sum += static_cast<double>(fp[0]);
             sum += static_cast<double>(fp[1]);
@@ -197,12 +257,17 @@ __device__ inline double ghost_value(const T* __restrict__ buf, size_t pstride, 
             sum += static_cast<double>(fp[g.s[0] + 1]);
             return sum / 4.0;
         }
-        for (int a = 0; a < 2; ++a)
-            for (int b = 0; b < 2; ++b)
-                for (int c = 0; c < 2; ++c) sum += static_cast<double>(fp[a * g.s[0] + b * g.s[1] + c]);
+        sum += static_cast<double>(fp[0]);
+        sum += static_cast<double>(fp[1]);
+        sum += static_cast<double>(fp[g.s[1]]);
+        sum += static_cast<double>(fp[g.s[1] + 1]);
+        sum += static_cast<double>(fp[g.s[0]]);
+        sum += static_cast<double>(fp[g.s[0] + 1]);
+        sum += static_cast<double>(fp[g.s[0] + g.s[1]]);
+        sum += static_cast<double>(fp[g.s[0] + g.s[1] + 1]);
         return sum / 8.0;
     }
-    return static_cast<double>(self[padded_index(g, G)]);
+    return static_cast<double>(self[G[0] * g.s[0] + G[1] * g.s[1] + G[2] * g.s[2]]);
 }
 
 } // namespace amr_gb300

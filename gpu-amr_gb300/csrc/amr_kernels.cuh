@@ -198,6 +198,39 @@ __device__ inline double gradient_cell(const T* buf, const amr_halo_meta* meta, 
     return __dsqrt_rn(s);
 }
 
+// Squared form of gradient_cell: the same rounded sum of squares, without the
+// square root.  With S_r = min{s : sqrt_rn(s) > rthr} and
+// S_c = min{s : sqrt_rn(s) >= cthr} (host-side search, sqrt is correctly
+// rounded on both sides), "v > rthr" is "s >= S_r" and "v < cthr" is
+// "s < S_c" for every s, NaN and infinity included.
+template <typename T, bool GhostsOnTheFly>
+__device__ inline double gradient_sq_cell(const T* buf, const amr_halo_meta* meta, const Geo& g, int p, int c)
+{
+    int idx[3];
+    interior_coords(g, c, idx);
+    const T*  u  = buf + static_cast<size_t>(p) * g.flat;
+    const int li = padded_index(g, idx);
+    double    s  = 0.0;
+    for (int a = 0; a < g.rank; ++a) {
+        const int L = g.rank - 1 - a;
+        double    side[2];
+        for (int pos = 0; pos < 2; ++pos) {
+            const int nidx = idx[L] + (pos ? 1 : -1);
+            if (!GhostsOnTheFly || (nidx >= g.h && nidx < g.n + g.h)) {
+                side[pos] = static_cast<double>(u[li + (pos ? g.s[L] : -g.s[L])]);
+            } else {
+                int G[3] = { idx[0], idx[1], idx[2] };
+                G[L]     = nidx;
+                side[pos] = ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos,
+                                           g, u);
+            }
+        }
+        const double gr = __dmul_rn(0.5, __dsub_rn(side[1], side[0]));
+        s               = __dadd_rn(s, __dmul_rn(gr, gr));
+    }
+    return s;
+}
+
 // Patch decision from the any/all rule of
 // dg_helpers/globals/amr_indicators.hpp:186-225 with the level bounds of
 // bench_fvm_solver_integration_active_amr.b.cpp:92-102.
@@ -742,6 +775,121 @@ __global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, doub
     if (step_dt > 0.0) {
         *remaining -= step_dt;
         ++(*count);
+    }
+}
+
+} // namespace amr_gb300
+
+namespace amr_gb300 {
+
+// ------------------------------------------------ 2D update, sized at compile time
+// One warp per patch (grid-stride over patches).  The whole padded patch is
+// contiguous, so it moves into a per-warp shared-memory tile with one bulk
+// async copy (cp.async.bulk, completed on an mbarrier); each warp keeps two
+// tiles and requests its next patch before working on the current one.
+// Lanes write the upwind ghost column and ghost row into the tile (halo
+// rules, ghost_value), each lane updates a contiguous run of N*N/32 interior
+// cells, the results go back into the tile, and the tile is stored to the
+// output patch whole in 16-byte words (ghost cells pass through), so every
+// HBM access is a full aligned sector.  A copy that does not land within the
+// wait cap sets *err = AMR_ERR_TIMEOUT; the warp then drains its other copy
+// (also capped) and stops.
+template <typename T, int N, int H>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 4)
+k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
+         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef, int upx, int upy,
+         int32_t* err)
+{
+    constexpr int      P1    = N + 2 * H;
+    constexpr int      FLAT  = P1 * P1;
+    // Only the interior rows are read and written: the 16-byte-aligned byte
+    // span [LO, HI) covering rows H .. N+H-1 (ghost columns included).  The
+    // upwind ghost row and column are evaluated on the fly, the other ghost
+    // cells are never read.
+    constexpr uint32_t LO    = (H * P1 * sizeof(T)) & ~15u;
+    constexpr uint32_t HI    = ((N + H) * P1 * sizeof(T) + 15u) & ~15u;
+    constexpr uint32_t BYTES = HI - LO;
+    constexpr int      WORDS = BYTES / 16;
+    constexpr int      SEG   = N * N / 32; // interior cells per lane
+    static_assert(FLAT * sizeof(T) % 16 == 0 && HI <= FLAT * sizeof(T), "patch is not a whole number of 16-byte words");
+    static_assert((N * N) % 32 == 0 && N % SEG == 0, "a lane's cells must stay within one row");
+    __shared__ __align__(128) T tiles[8][2][FLAT];
+    __shared__ __align__(8) uint64_t bars[8][2];
+    const int lane  = threadIdx.x & 31;
+    const int wib   = threadIdx.x >> 5;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    int       p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (lane == 0) {
+        mbar_init(&bars[wib][0], 1);
+        mbar_init(&bars[wib][1], 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const char* in_bytes = reinterpret_cast<const char*>(in);
+    if (p < P && lane == 0) {
+        mbar_expect_tx(&bars[wib][0], BYTES);
+        bulk_copy_g2s(reinterpret_cast<char*>(tiles[wib][0]) + LO,
+                      in_bytes + static_cast<size_t>(p) * FLAT * sizeof(T) + LO, BYTES, &bars[wib][0]);
+    }
+    uint32_t  parity[2] = { 0, 0 };
+    const int i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
+    // ghost job of this lane: lanes 0..N-1 the upwind column, lanes N..2N-1
+    // the upwind row (fixed for the whole launch)
+    const bool col  = lane < N;
+    const bool has  = lane < 2 * N && (col ? upx != 0 : upy != 0);
+    const int  L    = col ? 1 : 0;
+    const int  pos  = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
+    const int  tg   = (col ? lane : lane - N) + H;
+    const int  gc   = pos ? N + H : H - 1;
+    int        G[3] = { col ? tg : gc, col ? gc : tg, 0 };
+    amr_halo_meta m_next{};
+    if (has && p < P) m_next = meta[static_cast<size_t>(p) * 4 + 2 * L + pos];
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int b  = it & 1;
+        const int pn = p + nwarp;
+        if (pn < P && lane == 0) { // request the next patch into the other tile
+            fence_proxy_async_smem();
+            mbar_expect_tx(&bars[wib][b ^ 1], BYTES);
+            bulk_copy_g2s(reinterpret_cast<char*>(tiles[wib][b ^ 1]) + LO,
+                          in_bytes + static_cast<size_t>(pn) * FLAT * sizeof(T) + LO, BYTES, &bars[wib][b ^ 1]);
+        }
+        const Coef          cf  = coef[levels[p]];
+        const amr_halo_meta m   = m_next;
+        if (has && pn < P) m_next = meta[static_cast<size_t>(pn) * 4 + 2 * L + pos]; // one patch ahead
+        // relation none keeps the buffer's own ghost value (the tile does not
+        // hold the ghost rows)
+        T gv = T(0);
+        if (has)
+            gv = m.relation != REL_NONE
+                     ? static_cast<T>(ghost_value<T>(in, FLAT, m, G, L, pos, g, nullptr))
+                     : in[static_cast<size_t>(p) * FLAT + G[0] * P1 + G[1]];
+        if (!mbar_wait_bounded(&bars[wib][b], parity[b])) {
+            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
+            if (pn < P) mbar_wait_bounded(&bars[wib][b ^ 1], parity[b ^ 1]);
+            return;
+        }
+        parity[b] ^= 1u;
+        T* tile = tiles[wib][b];
+        if (has) tile[G[0] * P1 + G[1]] = gv;
+        __syncwarp();
+        const T c00 = static_cast<T>(cf.c0), cx = static_cast<T>(cf.c[0]), cy = static_cast<T>(cf.c[1]);
+        T       res[SEG];
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int idx = r * P1 + c0 + k;
+            T         acc = c00 * tile[idx];
+            if (upx != 0) acc = fma(cx, tile[idx + upx], acc);
+            if (upy != 0) acc = fma(cy, tile[idx + upy * P1], acc);
+            res[k] = acc;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) tile[r * P1 + c0 + k] = res[k];
+        __syncwarp();
+        const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
+        uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
+        for (int w = lane; w < WORDS; w += 32) dst[w] = t4[w];
+        __syncwarp();
     }
 }
 

@@ -2,6 +2,8 @@
 // drop-in launchers.  Host code only orchestrates launches; every per-leaf
 // or per-cell loop runs in a kernel from amr_kernels.cuh.
 #include <atomic>
+#include <cmath>
+#include <limits>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -140,6 +142,18 @@ namespace {
 
 constexpr size_t kMaxBatch = 1024;
 
+
+template <typename T, int N, int H>
+amr_status launch_step2d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
+                         const Coef* coef, const int* up, int32_t* err, cudaStream_t s)
+{
+    // one warp per patch, 8 warps per block, at most 16 resident blocks per SM
+    const unsigned grid = static_cast<unsigned>(std::min<long long>(grid_for(P, 8), 152LL * 16));
+    k_step2d<T, N, H><<<grid, 256, 0, s>>>(in, out, levels, meta, P, g, coef, up[0], up[1], err);
+    AMR_LAUNCHED("k_step2d");
+    return AMR_OK;
+}
+
 template <typename F>
 amr_status dispatch_dtype(int dtype, F&& f)
 {
@@ -215,6 +229,7 @@ amr_status init_root(amr_tree* t)
     t->tb = 0;
     AMR_CUDA(cudaMemsetAsync(t->cur, 0, state_bytes, t->stream));
     AMR_CUDA(cudaMemsetAsync(t->nxt, 0, state_bytes, t->stream));
+    AMR_CUDA(cudaMemsetAsync(t->status, 0, 8 * sizeof(int32_t), t->stream));
     AMR_CUDA(cudaMemcpyAsync(t->keys[0], &zero_key, 8, cudaMemcpyHostToDevice, t->stream));
     AMR_CUDA(cudaMemcpyAsync(t->levels[0], &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
     AMR_CUDA(cudaMemcpyAsync(t->maxlev, &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
@@ -228,6 +243,31 @@ amr_status init_root(amr_tree* t)
     return AMR_OK;
 }
 
+
+
+// Smallest non-negative double s whose correctly rounded square root passes
+// `v > thr` (strict) or `v >= thr`; NaN when no s does.  Non-negative doubles
+// are ordered like their bit patterns, so a bisection over the bits is exact.
+double sq_threshold(double thr, bool strict)
+{
+    auto ok = [&](double s) {
+        const double v = std::sqrt(s);
+        return strict ? v > thr : v >= thr;
+    };
+    if (ok(0.0)) return 0.0;
+    if (!ok(std::numeric_limits<double>::infinity())) return std::numeric_limits<double>::quiet_NaN();
+    uint64_t lo = 0, hi = 0x7FF0000000000000ull; // ok(lo) false, ok(hi) true
+    while (hi - lo > 1) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        double         v;
+        std::memcpy(&v, &mid, sizeof v);
+        if (ok(v)) hi = mid;
+        else lo = mid;
+    }
+    double r;
+    std::memcpy(&r, &hi, sizeof r);
+    return r;
+}
 
 // ------------------------------------------------------------ persistent run
 constexpr int kPersistentLeaves = 1024; // above this, per-launch kernels keep all SMs busy
@@ -508,7 +548,7 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     const int    P  = static_cast<int>(t->size);
     cudaStream_t s  = t->stream;
     const int    tb = t->tb, nb = 1 - t->tb;
-    AMR_CUDA(cudaMemsetAsync(t->status, 0, 8 * sizeof(int32_t), s));
+    AMR_CUDA(cudaMemsetAsync(t->status, 0, 3 * sizeof(int32_t), s)); // [7] is the update kernels' wait flag
     k_mark<<<grid_for(P, 256), 256, 0, s>>>(t->keys[tb], t->flags, P, g, t->rmark, t->chead);
     AMR_LAUNCHED("k_mark");
     const int rounds = std::max(1, t->max_level_host);
@@ -602,10 +642,18 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
                 AMR_CUDA(cudaEventRecord(ev->first, s));
             }
             amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
-                using T = decltype(z);
-                k_step<T, true><<<grid, 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                     t->levels[t->tb], t->meta[t->tb], P, t->g,
-                                                     t->coef + static_cast<size_t>(k) * nl, up[0], up[1], up[2], ppb);
+                using T        = decltype(z);
+                const Coef* cf = t->coef + static_cast<size_t>(k) * nl;
+                const T*    in = static_cast<const T*>(t->cur);
+                T*          out = static_cast<T*>(t->nxt);
+                if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
+                    return launch_step2d<T, 16, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
+                                                   t->status + 7, s);
+                if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
+                    return launch_step2d<T, 8, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
+                                                  t->status + 7, s);
+                k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
+                                                     up[1], up[2], ppb);
                 AMR_LAUNCHED("k_step");
                 return AMR_OK;
             });
@@ -627,7 +675,14 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
     char* hp = static_cast<char*>(t->pinned);
     AMR_CUDA(cudaMemcpyAsync(hp + 32, t->dt_acc, sizeof(double), cudaMemcpyDeviceToHost, t->stream));
     AMR_CUDA(cudaMemcpyAsync(hp + 40, t->dt_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(hp + 48, t->status + 7, sizeof(int32_t), cudaMemcpyDeviceToHost, t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
+    int32_t wait_err = 0;
+    std::memcpy(&wait_err, hp + 48, sizeof wait_err);
+    if (wait_err != 0) {
+        AMR_CUDA(cudaMemsetAsync(t->status + 7, 0, sizeof(int32_t), t->stream));
+        return fail(AMR_ERR_TIMEOUT, "a bulk copy did not complete within the wait limit");
+    }
     double   acc;
     uint32_t cnt;
     std::memcpy(&acc, hp + 32, sizeof acc);
@@ -659,9 +714,11 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
         const bool small = !(p->options & AMR_RUN_PER_LAUNCH) && t->size <= static_cast<size_t>(kPersistentLeaves) &&
                            p->remesh_interval >= 1 &&
                            p->remesh_interval <= static_cast<uint64_t>(kMaxInterval) && smem <= 64 * 1024;
-        const int cluster = small ? (t->dtype == AMR_F64 ? cycle_cluster_size<double>(smem)
-                                                         : cycle_cluster_size<float>(smem))
-                                  : 0;
+        int cluster = small ? (t->dtype == AMR_F64 ? cycle_cluster_size<double>(smem)
+                                                   : cycle_cluster_size<float>(smem))
+                            : 0;
+        const int forced = (p->options >> 8) & 0xFF;
+        if (cluster > 0 && forced > 0) cluster = std::min(cluster, forced);
         if (cluster > 0) {
             CycleArgs A{};
             A.g        = g;
@@ -693,6 +750,8 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             A.crit        = p->criterion;
             A.rthr        = p->refine_threshold;
             A.cthr        = p->coarsen_threshold;
+            A.rthr_sq     = sq_threshold(p->refine_threshold, true);
+            A.cthr_sq     = sq_threshold(p->coarsen_threshold, false);
             A.min_level   = p->min_level;
             A.max_level   = p->max_level;
             A.P0          = static_cast<int>(t->size);

@@ -31,7 +31,8 @@ typedef enum amr_status {
     AMR_ERR_CAPACITY      = 3, /* a re-mesh would exceed the tree capacity */
     AMR_ERR_UNBALANCED    = 4, /* neighbour rebuild met a non-2:1 configuration */
     AMR_ERR_UNSUPPORTED   = 5, /* rank/size combination not built */
-    AMR_ERR_NO_DEVICE     = 6
+    AMR_ERR_NO_DEVICE     = 6,
+    AMR_ERR_TIMEOUT       = 7  /* a bounded device-side wait gave up; results are invalid */
 } amr_status;
 
 typedef enum amr_dtype { AMR_F64 = 0, AMR_F32 = 1 } amr_dtype;
@@ -218,7 +219,8 @@ typedef struct amr_cycle_params {
     int32_t  criterion;
     int32_t  min_level;
     int32_t  max_level;
-    int32_t  options;        /* AMR_RUN_PER_LAUNCH: never use the cluster kernel */
+    int32_t  options;        /* AMR_RUN_PER_LAUNCH: never use the cluster kernel;
+                                bits 8-15: cluster size (CTAs) to use, 0 = largest that fits */
     double   refine_threshold;
     double   coarsen_threshold;
 } amr_cycle_params;
