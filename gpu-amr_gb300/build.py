@@ -25,7 +25,7 @@ LIB = LIBDIR / "libamr_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-           "-I", str(REPO / "include"), "-I", str(CSRC)]
+           "-I", str(REPO / "include"), "-I", str(CSRC), "-I", str(PKG / "host")]
 
 
 def nvcc() -> str:
@@ -49,7 +49,7 @@ def _stale(out: Path, deps) -> bool:
 def build(verbose: bool = False, extra=None) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.cuh")) + list((REPO / "include").glob("*.h"))
+    headers = list(CSRC.glob("*.cuh")) + list((REPO / "include").glob("*.h")) + list((PKG / "host").rglob("*.hpp"))
     nv = nvcc()
     jobs = []
     for src in sources():

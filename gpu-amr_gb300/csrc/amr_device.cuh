@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "amr_gb300.h"
+#include "morton/morton_bits.hpp"
 
 namespace amr_gb300 {
 
@@ -25,49 +26,10 @@ enum : int8_t { REL_NONE = 0, REL_SAME = 1, REL_FINER = 2, REL_COARSER = 3 };
 enum : int8_t { FLAG_STABLE = 0, FLAG_REFINE = 1, FLAG_COARSEN = 2 };
 
 // ------------------------------------------------------------------ Morton
-// Bit interleave, coordinate k of a rank-r point at bit r*b + k (x lowest);
-// the layout of libmorton's 64-bit encoders used by morton_id
-// (include/morton/morton_id.hpp:118-140, 334-359), by binary magic numbers.
-__host__ __device__ inline uint64_t spread2(uint64_t v)
-{
-    v &= 0xFFFFFFFFull;
-    v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
-    v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
-    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    v = (v | (v << 2)) & 0x3333333333333333ull;
-    v = (v | (v << 1)) & 0x5555555555555555ull;
-    return v;
-}
-__host__ __device__ inline uint32_t compact2(uint64_t v)
-{
-    v &= 0x5555555555555555ull;
-    v = (v | (v >> 1)) & 0x3333333333333333ull;
-    v = (v | (v >> 2)) & 0x0F0F0F0F0F0F0F0Full;
-    v = (v | (v >> 4)) & 0x00FF00FF00FF00FFull;
-    v = (v | (v >> 8)) & 0x0000FFFF0000FFFFull;
-    v = (v | (v >> 16)) & 0x00000000FFFFFFFFull;
-    return static_cast<uint32_t>(v);
-}
-__host__ __device__ inline uint64_t spread3(uint64_t v)
-{
-    v &= 0x1FFFFFull;
-    v = (v | (v << 32)) & 0x001F00000000FFFFull;
-    v = (v | (v << 16)) & 0x001F0000FF0000FFull;
-    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
-    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
-    v = (v | (v << 2)) & 0x1249249249249249ull;
-    return v;
-}
-__host__ __device__ inline uint32_t compact3(uint64_t v)
-{
-    v &= 0x1249249249249249ull;
-    v = (v | (v >> 2)) & 0x10C30C30C30C30C3ull;
-    v = (v | (v >> 4)) & 0x100F00F00F00F00Full;
-    v = (v | (v >> 8)) & 0x001F0000FF0000FFull;
-    v = (v | (v >> 16)) & 0x001F00000000FFFFull;
-    v = (v | (v >> 32)) & 0x00000000001FFFFFull;
-    return static_cast<uint32_t>(v);
-}
+using amr::morton_bits::compact2;
+using amr::morton_bits::compact3;
+using amr::morton_bits::spread2;
+using amr::morton_bits::spread3;
 
 __host__ __device__ inline int key_level(uint64_t k) { return static_cast<int>(k & 0x3F); }
 

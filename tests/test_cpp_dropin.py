@@ -1,0 +1,57 @@
+"""The C++ drop-in (gpu-amr_gb300/host: ndtree, amr_solver, morton_id, ...)
+compiled against the reference's own solver tests and benchmark loop."""
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import bumps_of, load_golden, rel_l2
+
+REPO = Path(__file__).resolve().parents[1]
+SRC = REPO / "tests" / "cpp" / "dropin_tests.cpp"
+FLAGS = ["-std=c++20", "-O2", "-I", str(REPO / "include"), "-I", str(REPO / "gpu-amr_gb300" / "host")]
+
+
+def test_dropin_headers_compile():
+    subprocess.run(["g++", *FLAGS, "-fsyntax-only", str(SRC)], check=True)
+
+
+@pytest.fixture(scope="module")
+def dropin_exe(tmp_path_factory):
+    import __graft_entry__ as g
+
+    lib = g.build_library()
+    exe = tmp_path_factory.mktemp("cpp") / "dropin_tests"
+    subprocess.run(["g++", *FLAGS, str(SRC), "-o", str(exe), "-L", str(lib.parent), "-lamr_gb300",
+                    f"-Wl,-rpath,{lib.parent}"], check=True)
+    return exe
+
+
+@pytest.mark.gpu
+def test_reference_solver_tests_pass_on_dropin(dropin_exe):
+    """PulseCenterMovement / PulseCenterMovementAMR of the reference
+    (tests/advection_equation_amr.t.cpp:50-232), 10x10 and 50x50 patches."""
+    r = subprocess.run([str(dropin_exe), "tests"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "PASSED" in r.stdout
+
+
+@pytest.mark.gpu
+def test_benchmark_loop_through_dropin_matches_reference(dropin_exe):
+    z, meta = load_golden("config2_amr_2d")
+    p = meta["params"]
+    b = bumps_of(meta)
+    args = [str(dropin_exe), "bench", str(p["steps"]), str(p["remesh"]), str(p["noise"]), str(p["noise_seed"])]
+    args += [repr(float(v)) for v in b]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    head = lines[0].split()
+    sum_dt, steps = float(head[1]), int(head[3])
+    ids = np.array([int(l.split()[1]) for l in lines if l.startswith("id ")], np.uint64)
+    u = np.array([float(l.split()[1]) for l in lines if l.startswith("u ")])
+    assert steps == int(z["steps"]) and sum_dt == float(z["sum_dt"])
+    np.testing.assert_array_equal(ids, z["final_ids"])
+    assert rel_l2(u, z["state_final"].reshape(-1)) <= 1e-12
