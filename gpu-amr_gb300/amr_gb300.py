@@ -41,7 +41,8 @@ class PatchGeometry(C.Structure):
 
 
 class TreeDesc(C.Structure):
-    _fields_ = [("geom", PatchGeometry), ("capacity", C.c_size_t), ("dtype", C.c_int32), ("stream", C.c_void_p)]
+    _fields_ = [("geom", PatchGeometry), ("capacity", C.c_size_t), ("dtype", C.c_int32), ("stream", C.c_void_p),
+                ("instances", C.c_int32)]
 
 
 class CycleParams(C.Structure):
@@ -54,11 +55,14 @@ class CycleParams(C.Structure):
 class CycleStats(C.Structure):
     _fields_ = [("executed_steps", C.c_uint64), ("sum_dt", C.c_double), ("cell_updates", C.c_uint64),
                 ("remeshes", C.c_uint64), ("intervals", C.c_uint64), ("leaves_min", C.c_uint64),
-                ("leaves_max", C.c_uint64), ("leaves_mean", C.c_double), ("persistent_intervals", C.c_uint64)]
+                ("leaves_max", C.c_uint64), ("leaves_mean", C.c_double), ("persistent_intervals", C.c_uint64),
+                ("graph_intervals", C.c_uint64)]
 
 
 CRITERIA = {"none": 0, "grad": 1, "gradient": 1, "max": 2}
 RUN_PER_LAUNCH = 1
+RUN_INSTANCE_PARAMS = 2
+RUN_NO_GRAPH = 4
 
 
 class TransferTask(C.Structure):
@@ -103,6 +107,10 @@ def lib():
         L.amr_tree_run.argtypes = [vp, C.POINTER(CycleParams), C.POINTER(CycleStats)]
         L.amr_tree_set_timing.argtypes = [vp, i32]
         L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.amr_tree_set_instance_params.argtypes = [vp, vp, vp, sz]
+        L.amr_tree_refine_to_levels.argtypes = [vp, vp, sz]
+        L.amr_tree_instance_offsets.argtypes = [vp, vp, sz]
+        L.amr_tree_instance_time.argtypes = [vp, vp, vp, sz]
         L.amr_halo_exchange_f64.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
         L.amr_halo_exchange_f32.argtypes = [vp, vp, sz, sz, C.POINTER(PatchGeometry), vp]
         L.amr_interpolate_patches_f64.argtypes = [vp, vp, sz, C.POINTER(PatchGeometry), vp]
@@ -142,8 +150,11 @@ def _vec3(v):
 class Tree:
     """Device-resident ndtree + amr_solver state for one scalar field."""
 
-    def __init__(self, rank, n, halo=1, depth=7, capacity=20000, dtype=F64, lengths=(1.0, 1.0, 1.0), stream=None):
+    def __init__(self, rank, n, halo=1, depth=7, capacity=20000, dtype=F64, lengths=(1.0, 1.0, 1.0), stream=None,
+                 instances=1):
+        """instances > 1 makes a forest of independent trees (one root each)."""
         self.rank, self.n, self.halo, self.depth = rank, n, halo, depth
+        self.instances = int(instances)
         self.dtype = dtype
         self.np_dtype = np.float64 if dtype == F64 else np.float32
         self.pad1 = n + 2 * halo
@@ -152,6 +163,7 @@ class Tree:
         d.capacity = capacity
         d.dtype = dtype
         d.stream = stream
+        d.instances = self.instances
         h = C.c_void_p()
         check(lib().amr_tree_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -239,7 +251,39 @@ class Tree:
         check(lib().amr_tree_refine_uniform(self._h, levels))
 
     def advance(self, steps, velocity, cfl, remaining=1.7976931348623157e308):
-        check(lib().amr_tree_advance(self._h, steps, _vec3(velocity), cfl, remaining))
+        """velocity None: the per-instance velocities of set_instance_params."""
+        v = None if velocity is None else _vec3(velocity)
+        check(lib().amr_tree_advance(self._h, steps, v, cfl, remaining))
+
+    # ------------------------------------------------------------ forests
+    def set_instance_params(self, velocity=None, level_bounds=None):
+        """velocity: (K, rank or 3) per instance; level_bounds: (K, 2) min/max."""
+        K = self.instances
+        vp = bp = None
+        if velocity is not None:
+            v = np.zeros((K, 3), np.float64)
+            a = np.asarray(velocity, np.float64).reshape(K, -1)
+            v[:, : a.shape[1]] = a
+            vp = v
+        if level_bounds is not None:
+            bp = np.ascontiguousarray(np.asarray(level_bounds, np.int32).reshape(K, 2))
+        check(lib().amr_tree_set_instance_params(self._h, None if vp is None else vp.ctypes.data,
+                                                 None if bp is None else bp.ctypes.data, K))
+
+    def refine_to_levels(self, targets):
+        t = np.ascontiguousarray(np.asarray(targets, np.int32).reshape(self.instances))
+        check(lib().amr_tree_refine_to_levels(self._h, t.ctypes.data, self.instances))
+
+    def instance_offsets(self):
+        out = np.empty(self.instances + 1, np.uint64)
+        check(lib().amr_tree_instance_offsets(self._h, out.ctypes.data, self.instances + 1))
+        return out.astype(np.int64)
+
+    def instance_time(self):
+        acc = np.empty(self.instances, np.float64)
+        cnt = np.empty(self.instances, np.uint32)
+        check(lib().amr_tree_instance_time(self._h, acc.ctypes.data, cnt.ctypes.data, self.instances))
+        return acc, cnt
 
     def finish_advance(self):
         acc, ex = C.c_double(), C.c_size_t()
@@ -247,9 +291,14 @@ class Tree:
         return acc.value, ex.value
 
     def run(self, steps, interval, velocity, cfl, criterion="grad", rthr=0.05, cthr=0.01, min_level=1,
-            max_level=5, remaining=1.7976931348623157e308, per_launch=False, cluster=0) -> dict:
+            max_level=5, remaining=1.7976931348623157e308, per_launch=False, cluster=0, graph=True,
+            instance_params=False) -> dict:
         """The benchmark loop (advance `interval` steps, flag, re-mesh) for
-        `steps` steps; returns the run statistics."""
+        `steps` steps; returns the run statistics.  per_launch: never the
+        cluster kernel; graph=False: host-driven intervals; instance_params:
+        per-instance velocities (set_instance_params)."""
+        if velocity is None:
+            velocity, instance_params = (0.0, 0.0, 0.0), True
         prm = CycleParams()
         prm.steps, prm.remesh_interval = steps, interval
         for i, v in enumerate(list(velocity)[:3]):
@@ -258,7 +307,8 @@ class Tree:
         prm.criterion = CRITERIA[criterion]
         prm.min_level, prm.max_level = min_level, max_level
         prm.refine_threshold, prm.coarsen_threshold = rthr, cthr
-        prm.options = (RUN_PER_LAUNCH if per_launch else 0) | ((int(cluster) & 0xFF) << 8)
+        prm.options = ((RUN_PER_LAUNCH if per_launch else 0) | (0 if graph else RUN_NO_GRAPH)
+                       | (RUN_INSTANCE_PARAMS if instance_params else 0) | ((int(cluster) & 0xFF) << 8))
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}
@@ -299,11 +349,14 @@ def unit_hash(a, b, c):
     return (h >> np.uint64(11)).astype(np.float64) * 2.0**-53
 
 
-def decode_ids(ids, rank):
-    """Morton ids -> (coords[P, rank] on the 2^depth grid, level[P])."""
+def decode_ids(ids, rank, depth=None):
+    """Morton ids -> (coords[P, rank] on the 2^depth grid, level[P]).  With
+    `depth`, an instance prefix above the interleaved bits is dropped."""
     ids = np.asarray(ids, np.uint64)
     level = (ids & np.uint64(63)).astype(np.int64)
     m = ids >> np.uint64(6)
+    if depth is not None and rank * depth < 58:
+        m = m & np.uint64((1 << (rank * depth)) - 1)
     coords = np.zeros((ids.size, rank), np.int64)
     for b in range(64 // rank):
         for k in range(rank):
@@ -316,7 +369,7 @@ def cell_centres(ids, rank, n, depth, lengths=(1.0, 1.0, 1.0)):
     """(P, n, ..., n, rank) physical centres of interior cells; axis k of the
     last dimension is Morton axis k (x, y, z); cell array axes follow the
     layout (dim 0 slowest)."""
-    coords, level = decode_ids(ids, rank)
+    coords, level = decode_ids(ids, rank, depth)
     maxc = float(1 << depth)
     P = coords.shape[0]
     out = np.empty((P,) + (n,) * rank + (rank,))

@@ -24,7 +24,7 @@ BUILD = PKG / "_build"
 LIB = LIBDIR / "libamr_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++20", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
            "-I", str(REPO / "include"), "-I", str(CSRC), "-I", str(PKG / "host")]
 
 

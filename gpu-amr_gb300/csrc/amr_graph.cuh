@@ -1,0 +1,394 @@
+// Device-resident re-mesh interval.  Every kernel here reads the leaf count
+// and the buffer selection (which tree buffer and which state buffer are
+// current) from a control block in device memory and walks its work with a
+// fixed grid, so one interval (step coefficients, k update steps, halo fill,
+// flags, 2:1 closure, counts, scan, emit, remap, neighbour rebuild, commit) is
+// a fixed launch sequence: it is captured once in a CUDA graph and replayed
+// with no host round trip.  The arithmetic of every leaf and cell is the
+// device functions the host-driven kernels use, so results are identical.
+// Once a kernel records an error in the control block, every later kernel
+// returns at once, leaving the tree as it was when the error was found.
+#pragma once
+
+#include "amr_kernels.cuh"
+
+namespace amr_gb300 {
+
+struct RunCtl {
+    int32_t P;          // current leaves
+    int32_t tb;         // tree buffer (keys/levels/meta) of the current tree
+    int32_t sb;         // state buffer of the current state
+    int32_t err;        // first error (amr_status), 0 = none
+    int32_t changed;    // the pending re-mesh changes the tree
+    int32_t NP;         // leaves after the pending re-mesh
+    int32_t max_level;  // finest level over all instances
+    int32_t nerr;       // neighbour rebuild error of the pending re-mesh
+    int32_t leaves_min; // over interval starts
+    int32_t leaves_max;
+    int32_t pad[2];
+    unsigned long long cell_updates, leaves_sum, intervals, remeshes;
+};
+
+struct RunBufs {
+    void*          state[2];
+    uint64_t*      keys[2];
+    int32_t*       levels[2];
+    amr_halo_meta* meta[2];
+    int8_t*        flags;
+    uint8_t*       rmark;
+    uint8_t*       chead;
+    uint32_t*      cnt;
+    uint32_t*      pos;
+    int32_t*       src;
+    int8_t*        skind;
+    int32_t*       maxlev;     // per instance, read by the step prologue
+    int32_t*       maxlev_new; // per instance, filled by emit, zero between re-meshes
+    const double*  vel;        // per instance x3, or null (launch-wide upwind sides)
+    const int32_t* bounds;     // per instance (min, max) level bounds, or null
+    uint32_t*      tile_sums;  // scan partials, one per tile
+    unsigned long long cap;
+    int            ninst;
+};
+
+constexpr int kScanThreads = 512;
+constexpr int kScanPer     = 8;
+constexpr int kScanTile    = kScanThreads * kScanPer;
+
+// ---------------------------------------------------------------- steps
+template <typename T, int N, int H, int W, int S>
+__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
+k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int parity, int upx0, int upy0)
+{
+    if (ctl->err) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
+    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    step2d_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.levels[tb],
+                            B.meta[tb], P, g, coef, upx0, upy0, &ctl->err, B.keys[tb], B.vel, tiles, bars, p, nwarp);
+}
+
+// Any geometry: ppb patches per block per round, grid-stride over rounds.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_run_step(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int parity, int up0, int up1, int up2,
+           int ppb)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    const T*  in     = static_cast<const T*>(B.state[s]);
+    T*        out    = static_cast<T*>(B.state[s ^ 1]);
+    const int cells  = g.cells;
+    const int nl     = g.depth + 1;
+    int       up[3]  = { up0, up1, up2 };
+    for (int p0 = blockIdx.x * ppb; p0 < P; p0 += gridDim.x * ppb) {
+        for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
+            const int p = p0 + t / cells;
+            if (p >= P) break;
+            int inst = 0;
+            if (B.vel) {
+                inst = instance_of(g, B.keys[tb], p);
+                for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(B.vel[3 * inst + a]) : 0;
+            }
+            step_cell<T, true>(in, out, B.meta[tb], g, coef[inst * nl + B.levels[tb][p]], up, p, t - (p - p0) * cells);
+        }
+    }
+}
+
+// --------------------------------------------------------- halo + flags
+// sp: the current state is state[sb ^ sp] (sp = parity of the steps run so
+// far in the interval).
+template <typename T>
+__global__ void __launch_bounds__(256) k_run_halo(RunBufs B, RunCtl* ctl, Geo g, int sp)
+{
+    if (ctl->err) return;
+    const long long total = static_cast<long long>(ctl->P) * g.ndir * g.h * (g.cells / g.n);
+    T*              buf   = static_cast<T*>(B.state[ctl->sb ^ sp]);
+    const amr_halo_meta* meta = B.meta[ctl->tb];
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+        halo_cell<T>(buf, meta, g, t);
+}
+
+// One block per patch, grid-stride; crit 1 = gradient, 2 = max value (the
+// decisions of k_flags_gradient / k_flags_max over the exchanged ghosts).
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_run_flags(RunBufs B, RunCtl* ctl, Geo g, int crit, double rthr, double cthr, int min_level, int max_level, int sp)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    const T*  buf = static_cast<const T*>(B.state[ctl->sb ^ sp]);
+    __shared__ double red[128];
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        int lo = min_level, hi = max_level;
+        if (B.bounds) {
+            const int inst = instance_of(g, B.keys[tb], p);
+            lo             = B.bounds[2 * inst];
+            hi             = B.bounds[2 * inst + 1];
+        }
+        const int level = B.levels[tb][p];
+        if (crit == 1) {
+            int any = 0, all = 1;
+            for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
+                const double v = gradient_cell<T, false>(buf, nullptr, g, p, c);
+                if (v > rthr) any = 1;
+                if (!(v < cthr)) all = 0;
+            }
+            any = __syncthreads_or(any);
+            all = __syncthreads_and(all);
+            if (threadIdx.x == 0) B.flags[p] = gradient_decision(any, all, level, lo, hi);
+        } else {
+            const T* u = buf + static_cast<size_t>(p) * g.flat;
+            double   m = 0.0;
+            for (int c = threadIdx.x; c < g.flat; c += blockDim.x)
+                if (face_or_interior(g, c)) m = fmax(m, static_cast<double>(u[c]));
+            red[threadIdx.x] = m;
+            __syncthreads();
+            for (int w = 64; w > 0; w >>= 1) {
+                if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) B.flags[p] = max_decision(red[0], level, rthr, cthr, lo, hi);
+            __syncthreads();
+        }
+    }
+}
+
+// --------------------------------------------------------------- re-mesh
+#define AMR_RUN_LEAVES(P)                                                                              \
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (P); i += gridDim.x * blockDim.x)
+
+__global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->changed = 0;
+    AMR_RUN_LEAVES(P) mark_leaf(B.keys[tb], B.flags, P, g, B.rmark, B.chead, i);
+}
+
+__global__ void k_run_closure(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    AMR_RUN_LEAVES(P) closure_leaf(B.meta[tb], g, B.rmark, i);
+}
+
+__global__ void k_run_veto(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    AMR_RUN_LEAVES(P) veto_leaf(B.meta[tb], g, B.rmark, B.chead, i);
+}
+
+__global__ void k_run_count(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    AMR_RUN_LEAVES(P) count_leaf(B.keys[tb], B.rmark, B.chead, g, B.cnt, &ctl->changed, i);
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix, *total = block sum.  blockDim.x == kScanThreads.
+__device__ inline uint32_t scan_block_exclusive(uint32_t v, uint32_t* warp_sums, uint32_t* total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t  x    = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kScanThreads / 32) warp_sums[lane] = s; // inclusive
+    }
+    __syncthreads();
+    const uint32_t before = (w > 0 ? warp_sums[w - 1] : 0u) + x - v;
+    *total                = warp_sums[kScanThreads / 32 - 1];
+    __syncthreads();
+    return before;
+}
+
+// Scan, pass 1: sum of the counts of each tile of kScanTile leaves.
+__global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunCtl* ctl)
+{
+    if (ctl->err) return;
+    const int P = ctl->P;
+    __shared__ uint32_t ws[kScanThreads / 32];
+    for (int tile = blockIdx.x; tile * kScanTile < P; tile += gridDim.x) {
+        const int base = tile * kScanTile + threadIdx.x * kScanPer;
+        uint32_t  s    = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k)
+            if (base + k < P) s += B.cnt[base + k];
+        uint32_t tot;
+        scan_block_exclusive(s, ws, &tot);
+        if (threadIdx.x == 0) B.tile_sums[tile] = tot;
+    }
+}
+
+// Scan, pass 2: each tile adds the sums of the tiles before it and writes
+// its exclusive positions; the last tile writes pos[P] and the new size and
+// flags AMR_ERR_CAPACITY when it exceeds the capacity.
+__global__ void __launch_bounds__(kScanThreads) k_run_scan_apply(RunBufs B, RunCtl* ctl)
+{
+    if (ctl->err) return;
+    const int P      = ctl->P;
+    const int ntiles = (P + kScanTile - 1) / kScanTile;
+    __shared__ uint32_t ws[kScanThreads / 32];
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint32_t before = 0;
+        for (int j = threadIdx.x; j < tile; j += blockDim.x) before += B.tile_sums[j];
+        uint32_t prior;
+        scan_block_exclusive(before, ws, &prior);
+        const int base = tile * kScanTile + threadIdx.x * kScanPer;
+        uint32_t  v[kScanPer];
+        uint32_t  s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k) {
+            v[k] = base + k < P ? B.cnt[base + k] : 0u;
+            s += v[k];
+        }
+        uint32_t tot;
+        uint32_t run = prior + scan_block_exclusive(s, ws, &tot);
+#pragma unroll
+        for (int k = 0; k < kScanPer; ++k)
+            if (base + k < P) {
+                B.pos[base + k] = run;
+                run += v[k];
+            }
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
+            const uint32_t np = prior + tot;
+            B.pos[P]          = np;
+            ctl->NP           = static_cast<int32_t>(np);
+            if (np > B.cap) ctl->err = AMR_ERR_CAPACITY;
+        }
+    }
+}
+
+__global__ void k_run_emit(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err || !ctl->changed) return;
+    const int P = ctl->P, tb = ctl->tb, nb = tb ^ 1;
+    AMR_RUN_LEAVES(P)
+    emit_leaf(B.keys[tb], B.rmark, B.chead, B.pos, g, B.keys[nb], B.levels[nb], B.src, B.skind, B.maxlev_new, i);
+}
+
+// One block per new leaf, grid-stride (k_remap's work).
+template <typename T>
+__global__ void __launch_bounds__(256) k_run_remap(RunBufs B, RunCtl* ctl, Geo g, int sp)
+{
+    if (ctl->err || !ctl->changed) return;
+    const int NP = ctl->NP;
+    const T*  old_state = static_cast<const T*>(B.state[ctl->sb ^ sp]);
+    T*        new_state = static_cast<T*>(B.state[ctl->sb ^ sp ^ 1]);
+    for (int j = blockIdx.x; j < NP; j += gridDim.x) {
+        const int kind = B.skind[j];
+        if (kind == 0) {
+            const size_t bytes = static_cast<size_t>(g.flat) * sizeof(T);
+            const uint4* f4    = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(B.src[j]) * g.flat);
+            uint4*       t4    = reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat);
+            for (size_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) t4[w] = f4[w];
+            continue;
+        }
+        for (int c = threadIdx.x; c < g.cells; c += blockDim.x)
+            remap_cell<T>(old_state, new_state, g, kind, B.src[j], j, c);
+    }
+}
+
+__global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
+{
+    if (ctl->err || !ctl->changed) return;
+    const int NP = ctl->NP, nb = ctl->tb ^ 1;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < NP * g.ndir; t += gridDim.x * blockDim.x)
+        neighbor_entry(B.keys[nb], NP, g, B.meta[nb], &ctl->nerr, t);
+}
+
+// End of an interval (one block): statistics of the interval just run and
+// the state buffer the steps left current, then, when the re-mesh changed the
+// tree, the switch to the new buffers and the new per-instance finest levels.
+__global__ void __launch_bounds__(256) k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp)
+{
+    __shared__ int chg;
+    __shared__ int red[256 / 32];
+    if (threadIdx.x == 0) {
+        const int  P  = ctl->P;
+        const bool ok = ctl->err == 0;
+        chg           = (remesh && ok && ctl->changed) ? 1 : 0;
+        if (ok) {
+            ctl->sb ^= sp;
+            ctl->cell_updates += static_cast<unsigned long long>(P) * steps * cells;
+            ctl->leaves_sum += static_cast<unsigned long long>(P);
+            ctl->intervals += 1;
+            ctl->leaves_min = min(ctl->leaves_min, P);
+            ctl->leaves_max = max(ctl->leaves_max, P);
+            if (remesh) ctl->remeshes += 1;
+        }
+    }
+    __syncthreads();
+    if (!chg) return;
+    int m = 0;
+    for (int i = threadIdx.x; i < B.ninst; i += blockDim.x) {
+        const int v     = B.maxlev_new[i];
+        B.maxlev[i]     = v;
+        B.maxlev_new[i] = 0;
+        m               = max(m, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < static_cast<int>(blockDim.x / 32); ++w) m = max(m, red[w]);
+        m              = max(m, red[0]);
+        ctl->max_level = m;
+        ctl->P         = ctl->NP;
+        ctl->tb ^= 1;
+        ctl->sb ^= 1;
+        if (ctl->nerr) ctl->err = ctl->nerr;
+    }
+}
+
+// Per-instance time bookkeeping at the start of a graph chunk: an empty
+// batch, the remaining time, and the totals carried in from earlier work of
+// the run (tot0, ctot0).
+__global__ void k_run_dt_init(DtState d, int ninst, double remaining0, double tot0, uint32_t ctot0)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ninst) return;
+    d.acc[i]  = 0.0;
+    d.rem[i]  = remaining0;
+    d.cnt[i]  = 0u;
+    d.tot[i]  = tot0;
+    d.ctot[i] = ctot0;
+}
+
+// offsets[i] = first leaf of instance i (lower bound of its key prefix).
+__global__ void k_instance_offsets(const uint64_t* __restrict__ keys, int P, Geo g, int ninst,
+                                   unsigned long long* __restrict__ offsets)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > ninst) return;
+    if (i == ninst) {
+        offsets[i] = static_cast<unsigned long long>(P);
+        return;
+    }
+    const uint64_t first = g.inst_shift >= 64 ? 0ull : static_cast<uint64_t>(i) << g.inst_shift;
+    int            lo = 0, hi = P;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (keys[mid] < first) lo = mid + 1;
+        else hi = mid;
+    }
+    offsets[i] = static_cast<unsigned long long>(lo);
+}
+
+} // namespace amr_gb300

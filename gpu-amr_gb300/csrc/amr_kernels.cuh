@@ -57,6 +57,16 @@ __host__ __device__ inline double clamp_step(double raw, double cfl, double rem)
     return dt;
 }
 
+// Instance of a leaf: the key prefix above the Morton field (0 for a single tree).
+__device__ __forceinline__ int instance_of(const Geo& g, const uint64_t* keys, int p)
+{
+    return g.inst_shift >= 64 ? 0 : static_cast<int>(keys[p] >> g.inst_shift);
+}
+
+// Upwind offset per Morton axis from the sign of the velocity: -1 when the
+// flow comes from the lower side, +1 from the upper side, 0 at rest.
+__device__ __forceinline__ int upwind(double v) { return v > 0.0 ? -1 : (v < 0.0 ? 1 : 0); }
+
 __device__ inline void interior_coords(const Geo& g, int c, int* idx)
 {
     idx[2] = 0;
@@ -103,16 +113,20 @@ __device__ inline void step_cell(const T* in, T* out, const amr_halo_meta* meta,
 // One step over P patches; ppb patches per block.  With CoefFromDt the
 // coefficients are formed per patch in shared memory from the device dt
 // (drop-in launcher, no per-step table); ppb <= 64.
+// With `vel` (per-instance velocities, 3 each) and `keys` the upwind sides and
+// the coefficient row (coef + instance * (depth+1)) follow each leaf's
+// instance; otherwise up0..up2 and coef[level] apply to every leaf.
 template <typename T, bool GhostsOnTheFly, bool CoefFromDt = false>
 __global__ void __launch_bounds__(256)
 k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
        const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef,
        int up0, int up1, int up2, int ppb, const double* __restrict__ dt_dev = nullptr, double v0 = 0.0,
-       double v1 = 0.0, double v2 = 0.0)
+       double v1 = 0.0, double v2 = 0.0, const uint64_t* __restrict__ keys = nullptr,
+       const double* __restrict__ vel = nullptr)
 {
     const int cells = g.cells;
     const int p0    = blockIdx.x * ppb;
-    const int up[3] = { up0, up1, up2 };
+    int       up[3] = { up0, up1, up2 };
     __shared__ Coef local[CoefFromDt ? 64 : 1];
     if (CoefFromDt) {
         const int q = threadIdx.x;
@@ -125,7 +139,12 @@ k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict_
     for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
         const int p = p0 + t / cells;
         if (p >= P) break;
-        const Coef cf = CoefFromDt ? local[p - p0] : coef[levels[p]];
+        int inst = 0;
+        if (vel) {
+            inst = instance_of(g, keys, p);
+            for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(vel[3 * inst + a]) : 0;
+        }
+        const Coef cf = CoefFromDt ? local[p - p0] : coef[inst * (g.depth + 1) + levels[p]];
         step_cell<T, GhostsOnTheFly>(in, out, meta, g, cf, up, p, t - (p - p0) * cells);
     }
 }
@@ -239,13 +258,21 @@ __device__ inline int8_t gradient_decision(int any, int all, int level, int min_
     return (level < max_level && any) ? FLAG_REFINE : (level > min_level && all) ? FLAG_COARSEN : FLAG_STABLE;
 }
 
+// bounds (optional): per-instance (min_level, max_level) pairs, indexed by
+// the leaf's instance; they replace min_level/max_level.
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_flags_gradient(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g,
-                 double rthr, double cthr, int min_level, int max_level, int8_t* __restrict__ flags)
+                 double rthr, double cthr, int min_level, int max_level, int8_t* __restrict__ flags,
+                 const uint64_t* __restrict__ keys = nullptr, const int32_t* __restrict__ bounds = nullptr)
 {
     const int p = blockIdx.x;
     if (p >= P) return;
+    if (bounds) {
+        const int inst = instance_of(g, keys, p);
+        min_level      = bounds[2 * inst];
+        max_level      = bounds[2 * inst + 1];
+    }
     int any = 0, all = 1;
     for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
         const double v = gradient_cell<T, false>(buf, nullptr, g, p, c);
@@ -278,10 +305,16 @@ __device__ inline int8_t max_decision(double mx, int level, double rthr, double 
 template <typename T>
 __global__ void __launch_bounds__(128)
 k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g, double rthr,
-            double cthr, int min_level, int max_level, int8_t* __restrict__ flags)
+            double cthr, int min_level, int max_level, int8_t* __restrict__ flags,
+            const uint64_t* __restrict__ keys = nullptr, const int32_t* __restrict__ bounds = nullptr)
 {
     const int p = blockIdx.x;
     if (p >= P) return;
+    if (bounds) {
+        const int inst = instance_of(g, keys, p);
+        min_level      = bounds[2 * inst];
+        max_level      = bounds[2 * inst + 1];
+    }
     const T* u = buf + static_cast<size_t>(p) * g.flat;
     double   m = 0.0;
     for (int c = threadIdx.x; c < g.flat; c += blockDim.x)
@@ -300,18 +333,52 @@ k_flags_max(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P
 // Per-batch prologue for one instance (one block): thread 0 walks the step
 // sizes of the batch (the clamp is sequential in the remaining time), then
 // the block fills the (step, level) coefficient table in parallel.
+// Per-instance time bookkeeping: acc/cnt = simulated time and executed steps
+// of the current batch, rem = time still to go, tot/ctot = the sums of the
+// batches before it in the current run (batch sums are added in order, as
+// the reference's host loop adds finish_advance_batch results).
+struct DtState {
+    double*   acc;
+    double*   rem;
+    uint32_t* cnt;
+    double*   tot;
+    uint32_t* ctot;
+};
+
+// Batch opening modes of k_batch_begin.
+enum : int {
+    BATCH_CONTINUE = 0, // same batch (a further chunk of one advance call)
+    BATCH_RESET    = 1, // first batch: totals, batch sums and remaining time start over
+    BATCH_NEXT     = 2, // next batch of a run: fold the batch into the totals, keep the remaining time
+    BATCH_NEXT_REM = 3, // next batch of a run with the remaining time given by the host
+};
+
+// Block b handles instance b: its CFL step from its own finest level and
+// velocity; coef row (step s, instance b) starts at (s * ninst + b) * (depth+1).
 __global__ void __launch_bounds__(256)
 k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
-              int reset, double remaining0, double* __restrict__ acc, double* __restrict__ remaining,
-              uint32_t* __restrict__ count, double* __restrict__ step_dt, Coef* __restrict__ coef)
+              int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef)
 {
     __shared__ double dts[1024];
-    const double      v[3] = { vel[0], vel[1], vel[2] };
+    const int         inst  = blockIdx.x;
+    const int         ninst = gridDim.x;
+    const double      v[3]  = { vel[3 * inst], vel[3 * inst + 1], vel[3 * inst + 2] };
     if (threadIdx.x == 0) {
-        const double raw = raw_dt(g, v, max_level[0]);
-        double       rem = reset ? remaining0 : remaining[0];
-        double       sum = reset ? 0.0 : acc[0];
-        uint32_t     cnt = reset ? 0u : count[0];
+        const double raw = raw_dt(g, v, max_level[inst]);
+        double       rem = d.rem[inst], sum = d.acc[inst];
+        uint32_t     cnt = d.cnt[inst];
+        if (mode == BATCH_RESET) {
+            d.tot[inst]  = 0.0;
+            d.ctot[inst] = 0u;
+        } else if (mode != BATCH_CONTINUE) {
+            d.tot[inst] += sum;
+            d.ctot[inst] += cnt;
+        }
+        if (mode != BATCH_CONTINUE) {
+            sum = 0.0;
+            cnt = 0u;
+        }
+        if (mode == BATCH_RESET || mode == BATCH_NEXT_REM) rem = remaining0;
         for (int s = 0; s < steps; ++s) {
             const double dt = clamp_step(raw, cfl, rem);
             sum += dt;
@@ -319,16 +386,28 @@ k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __rest
                 rem -= dt;
                 ++cnt;
             }
-            dts[s]     = dt;
-            step_dt[s] = dt;
+            dts[s]                                         = dt;
+            step_dt[static_cast<size_t>(s) * ninst + inst] = dt;
         }
-        acc[0]       = sum;
-        remaining[0] = rem;
-        count[0]     = cnt;
+        d.acc[inst] = sum;
+        d.rem[inst] = rem;
+        d.cnt[inst] = cnt;
     }
     __syncthreads();
     const int nl = g.depth + 1;
-    for (int e = threadIdx.x; e < steps * nl; e += blockDim.x) coef[e] = make_coef(g, dts[e / nl], v, e % nl);
+    for (int e = threadIdx.x; e < steps * nl; e += blockDim.x) {
+        const int st = e / nl, l = e % nl;
+        coef[(static_cast<size_t>(st) * ninst + inst) * nl + l] = make_coef(g, dts[st], v, l);
+    }
+}
+
+// Refinement flags that refine every leaf below its instance's target level.
+__global__ void k_flags_to_level(const uint64_t* __restrict__ keys, int P, Geo g, const int32_t* __restrict__ target,
+                                 int8_t* __restrict__ flags)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    flags[p] = key_level(keys[p]) < target[instance_of(g, keys, p)] ? FLAG_REFINE : FLAG_STABLE;
 }
 
 // Maximum level over a level array.
@@ -783,93 +862,132 @@ __global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, doub
 namespace amr_gb300 {
 
 // ------------------------------------------------ 2D update, sized at compile time
-// One warp per patch (grid-stride over patches).  The whole padded patch is
-// contiguous, so it moves into a per-warp shared-memory tile with one bulk
-// async copy (cp.async.bulk, completed on an mbarrier); each warp keeps two
-// tiles and requests its next patch before working on the current one.
-// Lanes write the upwind ghost column and ghost row into the tile (halo
-// rules, ghost_value), each lane updates a contiguous run of N*N/32 interior
-// cells, the results go back into the tile, and the tile is stored to the
-// output patch whole in 16-byte words (ghost cells pass through), so every
-// HBM access is a full aligned sector.  A copy that does not land within the
-// wait cap sets *err = AMR_ERR_TIMEOUT; the warp then drains its other copy
-// (also capped) and stops.
+// One warp per patch (grid-stride over patches: the Morton-ordered leaf array
+// of every instance is the work list).  The whole padded patch is contiguous,
+// so it moves into a per-warp shared-memory tile with one bulk async copy
+// (cp.async.bulk, completed on an mbarrier).  Each warp owns S tiles in a
+// ring and keeps S-1 copies in flight ahead of the patch it works on (S = 1:
+// load, then compute).  Lanes write the upwind ghost column and ghost row
+// into the tile (halo rules, ghost_value), each lane updates a contiguous run
+// of N*N/32 interior cells, the results go back into the tile, and the tile
+// is stored to the output patch whole in 16-byte words (ghost cells pass
+// through), so every HBM access is a full aligned sector.  A copy that does
+// not land within the wait cap sets *err = AMR_ERR_TIMEOUT; the warp then
+// drains its other copies (also capped) and stops.
 template <typename T, int N, int H>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 6 : 4)
-k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
-         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef, int upx, int upy,
-         int32_t* err)
-{
-    constexpr int      P1    = N + 2 * H;
-    constexpr int      FLAT  = P1 * P1;
+struct Step2dShape {
+    static constexpr int P1   = N + 2 * H;
+    static constexpr int FLAT = P1 * P1;
     // Only the interior rows are read and written: the 16-byte-aligned byte
     // span [LO, HI) covering rows H .. N+H-1 (ghost columns included).  The
     // upwind ghost row and column are evaluated on the fly, the other ghost
     // cells are never read.
-    constexpr uint32_t LO    = (H * P1 * sizeof(T)) & ~15u;
-    constexpr uint32_t HI    = ((N + H) * P1 * sizeof(T) + 15u) & ~15u;
-    constexpr uint32_t BYTES = HI - LO;
-    constexpr int      WORDS = BYTES / 16;
-    constexpr int      SEG   = N * N / 32; // interior cells per lane
-    static_assert(FLAT * sizeof(T) % 16 == 0 && HI <= FLAT * sizeof(T), "patch is not a whole number of 16-byte words");
+    static constexpr uint32_t LO    = (H * P1 * sizeof(T)) & ~15u;
+    static constexpr uint32_t HI    = ((N + H) * P1 * sizeof(T) + 15u) & ~15u;
+    static constexpr uint32_t BYTES = HI - LO;
+    static constexpr int      WORDS = BYTES / 16;
+    static constexpr int      SEG   = N * N / 32; // interior cells per lane
+    static constexpr size_t   TILE  = FLAT * sizeof(T);
+    static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
     static_assert((N * N) % 32 == 0 && N % SEG == 0, "a lane's cells must stay within one row");
-    __shared__ __align__(128) T tiles[8][2][FLAT];
-    __shared__ __align__(8) uint64_t bars[8][2];
-    const int lane  = threadIdx.x & 31;
-    const int wib   = threadIdx.x >> 5;
-    const int nwarp = (gridDim.x * blockDim.x) >> 5;
-    int       p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // dynamic shared memory of a block of W warps with S tiles each
+    static constexpr size_t smem(int W, int S) { return static_cast<size_t>(W) * S * (TILE + 8); }
+};
+
+template <typename T, int N, int H, int S>
+__device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restrict__ out,
+                                            const int32_t* __restrict__ levels,
+                                            const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
+                                            const Coef* __restrict__ coef, int upx0, int upy0, int32_t* err,
+                                            const uint64_t* __restrict__ keys, const double* __restrict__ vel,
+                                            T* tiles, uint64_t* bars, int p, int nwarp)
+{
+    using Sh                = Step2dShape<T, N, H>;
+    constexpr int      P1   = Sh::P1;
+    constexpr int      FLAT = Sh::FLAT;
+    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
+    constexpr int      SEG  = Sh::SEG;
+    const int          lane = threadIdx.x & 31;
     if (lane == 0) {
-        mbar_init(&bars[wib][0], 1);
-        mbar_init(&bars[wib][1], 1);
+        for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
         mbar_init_fence();
     }
     __syncwarp();
     const char* in_bytes = reinterpret_cast<const char*>(in);
-    if (p < P && lane == 0) {
-        mbar_expect_tx(&bars[wib][0], BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles[wib][0]) + LO,
-                      in_bytes + static_cast<size_t>(p) * FLAT * sizeof(T) + LO, BYTES, &bars[wib][0]);
-    }
-    uint32_t  parity[2] = { 0, 0 };
+    auto        request  = [&](int q, int slot) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[slot], BYTES);
+        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
+                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
+    };
+    // prologue: copies for the first S-1 patches of this warp
+    if (lane == 0)
+        for (int j = 0; j < S - 1; ++j)
+            if (p + j * nwarp < P) request(p + j * nwarp, j);
+    uint32_t  phase = 0; // bit b: parity of slot b's next completion
     const int i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
-    // ghost job of this lane: lanes 0..N-1 the upwind column, lanes N..2N-1
-    // the upwind row (fixed for the whole launch)
-    const bool col  = lane < N;
-    const bool has  = lane < 2 * N && (col ? upx != 0 : upy != 0);
-    const int  L    = col ? 1 : 0;
-    const int  pos  = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
-    const int  tg   = (col ? lane : lane - N) + H;
-    const int  gc   = pos ? N + H : H - 1;
-    int        G[3] = { col ? tg : gc, col ? gc : tg, 0 };
-    amr_halo_meta m_next{};
-    if (has && p < P) m_next = meta[static_cast<size_t>(p) * 4 + 2 * L + pos];
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it & 1;
-        const int pn = p + nwarp;
-        if (pn < P && lane == 0) { // request the next patch into the other tile
-            fence_proxy_async_smem();
-            mbar_expect_tx(&bars[wib][b ^ 1], BYTES);
-            bulk_copy_g2s(reinterpret_cast<char*>(tiles[wib][b ^ 1]) + LO,
-                          in_bytes + static_cast<size_t>(pn) * FLAT * sizeof(T) + LO, BYTES, &bars[wib][b ^ 1]);
+    const int nl = g.depth + 1;
+    // Per-leaf instance: upwind sides from its velocity (vel != nullptr),
+    // else the launch-wide upx0/upy0.  Ghost job of this lane: lanes 0..N-1
+    // the upwind column, lanes N..2N-1 the upwind row.
+    const bool col   = lane < N;
+    const int  L     = col ? 1 : 0;
+    const int  tg    = (col ? lane : lane - N) + H;
+    auto       sides = [&](int q, int& ux, int& uy, int& inst) {
+        inst = 0;
+        ux   = upx0;
+        uy   = upy0;
+        if (vel) {
+            inst = instance_of(g, keys, q);
+            ux   = upwind(vel[3 * inst]);
+            uy   = upwind(vel[3 * inst + 1]);
         }
-        const Coef          cf  = coef[levels[p]];
-        const amr_halo_meta m   = m_next;
-        if (has && pn < P) m_next = meta[static_cast<size_t>(pn) * 4 + 2 * L + pos]; // one patch ahead
+    };
+    int           upx = 0, upy = 0, inst = 0;
+    amr_halo_meta m_next{};
+    if (p < P) {
+        sides(p, upx, upy, inst);
+        const bool has0 = lane < 2 * N && (col ? upx != 0 : upy != 0);
+        const int  pos0 = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
+        if (has0) m_next = meta[static_cast<size_t>(p) * 4 + 2 * L + pos0];
+    }
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int  b       = it % S;
+        const int  pn      = p + nwarp;
+        const int  pf      = p + (S - 1) * nwarp; // patch whose copy is issued now
+        const bool has     = lane < 2 * N && (col ? upx != 0 : upy != 0);
+        const int  pos     = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
+        const int  gc      = pos ? N + H : H - 1;
+        int        G[3]    = { col ? tg : gc, col ? gc : tg, 0 };
+        const int  cur_upx = upx, cur_upy = upy, cur_inst = inst;
+        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
+        const Coef          cf = coef[cur_inst * nl + levels[p]];
+        const amr_halo_meta m  = m_next;
+        if (pn < P) { // the next leaf's sides and neighbour record, one patch ahead
+            sides(pn, upx, upy, inst);
+            const bool hasn = lane < 2 * N && (col ? upx != 0 : upy != 0);
+            const int  posn = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
+            if (hasn) m_next = meta[static_cast<size_t>(pn) * 4 + 2 * L + posn];
+        }
         // relation none keeps the buffer's own ghost value (the tile does not
         // hold the ghost rows)
         T gv = T(0);
         if (has)
-            gv = m.relation != REL_NONE
-                     ? static_cast<T>(ghost_value<T>(in, FLAT, m, G, L, pos, g, nullptr))
-                     : in[static_cast<size_t>(p) * FLAT + G[0] * P1 + G[1]];
-        if (!mbar_wait_bounded(&bars[wib][b], parity[b])) {
+            gv = m.relation != REL_NONE ? static_cast<T>(ghost_value<T>(in, FLAT, m, G, L, pos, g, nullptr))
+                                        : in[static_cast<size_t>(p) * FLAT + G[0] * P1 + G[1]];
+        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
             if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            if (pn < P) mbar_wait_bounded(&bars[wib][b ^ 1], parity[b ^ 1]);
+            phase ^= 1u << b;
+            for (int j = 1; j < S; ++j) // drain the copies still in flight
+                if (p + j * nwarp < P) {
+                    const int sl = (it + j) % S;
+                    mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u);
+                    phase ^= 1u << sl;
+                }
             return;
         }
-        parity[b] ^= 1u;
-        T* tile = tiles[wib][b];
+        phase ^= 1u << b;
+        T* tile = tiles + static_cast<size_t>(b) * FLAT;
         if (has) tile[G[0] * P1 + G[1]] = gv;
         __syncwarp();
         const T c00 = static_cast<T>(cf.c0), cx = static_cast<T>(cf.c[0]), cy = static_cast<T>(cf.c[1]);
@@ -878,8 +996,8 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restric
         for (int k = 0; k < SEG; ++k) {
             const int idx = r * P1 + c0 + k;
             T         acc = c00 * tile[idx];
-            if (upx != 0) acc = fma(cx, tile[idx + upx], acc);
-            if (upy != 0) acc = fma(cy, tile[idx + upy * P1], acc);
+            if (cur_upx != 0) acc = fma(cx, tile[idx + cur_upx], acc);
+            if (cur_upy != 0) acc = fma(cy, tile[idx + cur_upy * P1], acc);
             res[k] = acc;
         }
         __syncwarp();
@@ -888,9 +1006,41 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restric
         __syncwarp();
         const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
         uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
-        for (int w = lane; w < WORDS; w += 32) dst[w] = t4[w];
+        for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
         __syncwarp();
     }
+}
+
+// Warp w of the block: its S tiles and S barriers in dynamic shared memory.
+template <typename T, int N, int H, int W, int S>
+__device__ __forceinline__ void step2d_smem(unsigned char* smem, T*& tiles, uint64_t*& bars)
+{
+    using Sh       = Step2dShape<T, N, H>;
+    const int wib  = threadIdx.x >> 5;
+    tiles          = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * S * Sh::FLAT;
+    bars           = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * S * Sh::TILE) + wib * S;
+}
+
+// Register budget: 40 resident warps per SM for FP32, 32 for FP64.
+template <typename T, int W>
+struct Step2dOcc {
+    static constexpr int blocks = ((sizeof(T) == 4 ? 40 : 32) / W) > 0 ? ((sizeof(T) == 4 ? 40 : 32) / W) : 1;
+};
+
+// Host-driven launch: leaf count and buffers from the arguments.
+template <typename T, int N, int H, int W, int S>
+__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
+k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
+         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef, int upx0, int upy0,
+         int32_t* err, const uint64_t* __restrict__ keys, const double* __restrict__ vel)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    step2d_body<T, N, H, S>(in, out, levels, meta, P, g, coef, upx0, upy0, err, keys, vel, tiles, bars, p, nwarp);
 }
 
 } // namespace amr_gb300

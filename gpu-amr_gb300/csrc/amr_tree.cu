@@ -1,8 +1,11 @@
 // C-ABI of the GB300 AMR path: the device-resident tree and the reference
 // drop-in launchers.  Host code only orchestrates launches; every per-leaf
 // or per-cell loop runs in a kernel from amr_kernels.cuh.
+#include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
+#include <map>
 #include <limits>
 #include <cstdint>
 #include <cstdio>
@@ -13,6 +16,7 @@
 
 #include "amr_gb300.h"
 #include "amr_cycle.cuh"
+#include "amr_graph.cuh"
 
 using namespace amr_gb300;
 
@@ -92,8 +96,37 @@ inline unsigned grid_for(long long work, int block)
 
 } // namespace
 
+namespace {
+// One captured interval: the launch sequence of amr_tree_run's graph path for
+// a fixed set of parameters.
+struct GraphKey {
+    int    k = 0, crit = 0, min_level = 0, max_level = 0, rounds = 0, bounds = 0, vel = 0, W = 0, S = 0, grid = 0;
+    int    up[3] = { 0, 0, 0 };
+    double rthr = 0.0, cthr = 0.0, cfl = 0.0;
+    bool   operator==(const GraphKey& o) const
+    {
+        return k == o.k && crit == o.crit && min_level == o.min_level && max_level == o.max_level &&
+               rounds == o.rounds && bounds == o.bounds && vel == o.vel && W == o.W && S == o.S && grid == o.grid &&
+               up[0] == o.up[0] && up[1] == o.up[1] && up[2] == o.up[2] && std::memcmp(&rthr, &o.rthr, 8) == 0 &&
+               std::memcmp(&cthr, &o.cthr, 8) == 0 && std::memcmp(&cfl, &o.cfl, 8) == 0;
+    }
+};
+struct GraphEntry {
+    GraphKey        key;
+    cudaGraph_t     graph   = nullptr;
+    cudaGraphExec_t exec    = nullptr;
+    uint64_t        kernels = 0; // kernel nodes of one replay
+};
+// Launch configuration of the 2D update kernel: W warps per block, S tiles
+// per warp, `grid` blocks (0 = one warp per patch up to full residency).
+struct StepCfg {
+    int W = 8, S = 2, grid = 0;
+};
+} // namespace
+
 struct amr_tree {
     Geo          g{};
+    int          ninst    = 1;
     size_t       cap      = 0;
     int          dtype    = AMR_F64;
     size_t       esize    = 8;
@@ -102,7 +135,8 @@ struct amr_tree {
     int          max_level_host = 0;
     bool         ghosts_valid   = false;
 
-    void*          cur = nullptr;
+    void*          sbuf[2]{};   // the two state buffers (fixed addresses)
+    void*          cur = nullptr; // one of sbuf
     void*          nxt = nullptr;
     uint64_t*      keys[2]{};
     int32_t*       levels[2]{};
@@ -118,17 +152,34 @@ struct amr_tree {
     int8_t*   skind  = nullptr;
     int32_t*  status = nullptr; // [0] error, [1] changed, [2] new size
     int32_t*  maxlev = nullptr; // per instance
-    double*   vel    = nullptr; // per instance, 3 each
+    int32_t*  maxlev_new = nullptr; // per instance, zero between graph re-meshes
+    double*   vel    = nullptr; // per instance, 3 each: the velocities in use
+    double*   vel_inst = nullptr; // per instance, as set by amr_tree_set_instance_params
+    int32_t*  bounds = nullptr; // per instance (min, max) level bounds
+    int32_t*  target = nullptr; // per instance target levels (refine_to_levels)
+    unsigned long long* offs = nullptr; // instance offsets, ninst + 1
+    uint32_t* tile_sums = nullptr;
+    RunCtl*   ctl       = nullptr;
+    bool      vel_inst_set = false;
+    std::vector<double> vel_inst_host;
+    bool      bounds_set   = false;
+    bool      vel_per_leaf = false; // the current advance uses per-instance velocities
+    cudaStream_t          cap_stream = nullptr; // private stream for graph capture
+    std::vector<GraphEntry> graphs;
+    size_t    pinned_bytes = 0;
 
     double*   dt_acc = nullptr;
     double*   dt_rem = nullptr;
     uint32_t* dt_cnt = nullptr;
+    double*   dt_tot = nullptr;
+    uint32_t* dt_ctot = nullptr;
+    DtState   dts() const { return DtState{ dt_acc, dt_rem, dt_cnt, dt_tot, dt_ctot }; }
     double*   step_dt = nullptr;
     Coef*     coef    = nullptr;
     size_t    coef_steps = 0;
     bool      batch_open = false;
 
-    void* pinned = nullptr; // 64 bytes of readback space
+    void* pinned = nullptr; // readback space (pinned_bytes)
     CycleStats* cstats = nullptr;
 
     // opt-in launch timing of the update kernel
@@ -143,14 +194,194 @@ namespace {
 constexpr size_t kMaxBatch = 1024;
 
 
+int num_sms()
+{
+    static int sms[64] = {};
+    int        dev     = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (!sms[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        sms[dev] = v;
+    }
+    return sms[dev];
+}
+
+// Dynamic shared memory limit of both 2D update kernels of one shape, set
+// once per device.
+template <typename T, int N, int H, int W, int S>
+cudaError_t prepare_step2d()
+{
+    static std::atomic<uint64_t> done{ 0 };
+    int                          dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load() & bit) return cudaSuccess;
+    const int   smem = static_cast<int>(Step2dShape<T, N, H>::smem(W, S));
+    cudaError_t e    = cudaFuncSetAttribute(k_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_run_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) done.fetch_or(bit);
+    return e;
+}
+
+// Resident blocks per SM of the 2D update kernel (W, S).
+template <typename T, int N, int H, int W, int S>
+int step2d_occupancy()
+{
+    if (prepare_step2d<T, N, H, W, S>() != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run_step2d<T, N, H, W, S>, W * 32,
+                                                      Step2dShape<T, N, H>::smem(W, S)) != cudaSuccess)
+        nb = 0;
+    cudaGetLastError();
+    return nb;
+}
+
+// Calls f.template operator()<W, S>() for the (W, S) pair of the config; the
+// pairs the autotuner searches.
+template <typename F>
+amr_status with_ws(int W, int S, F&& f)
+{
+    if (W == 4 && S == 2) return f.template operator()<4, 2>();
+    if (W == 4 && S == 3) return f.template operator()<4, 3>();
+    if (W == 8 && S == 1) return f.template operator()<8, 1>();
+    if (W == 8 && S == 2) return f.template operator()<8, 2>();
+    if (W == 8 && S == 3) return f.template operator()<8, 3>();
+    if (W == 16 && S == 2) return f.template operator()<16, 2>();
+    return fail(AMR_ERR_INVALID, "unsupported update kernel configuration");
+}
+constexpr int kStepConfigs[][2] = { { 4, 2 }, { 4, 3 }, { 8, 1 }, { 8, 2 }, { 8, 3 }, { 16, 2 } };
+
+// Grid of the 2D update kernel: cfg.grid, or one warp per patch capped at
+// full residency.
+template <typename T, int N, int H, int W, int S>
+unsigned step2d_grid(int P, int grid)
+{
+    if (grid > 0) return static_cast<unsigned>(grid);
+    const int occ = std::max(1, step2d_occupancy<T, N, H, W, S>());
+    return static_cast<unsigned>(std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
+}
+
 template <typename T, int N, int H>
 amr_status launch_step2d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
-                         const Coef* coef, const int* up, int32_t* err, cudaStream_t s)
+                         const Coef* coef, const int* up, int32_t* err, const uint64_t* keys, const double* vel,
+                         const StepCfg& cfg, cudaStream_t s)
 {
-    // one warp per patch, 8 warps per block, at most 16 resident blocks per SM
-    const unsigned grid = static_cast<unsigned>(std::min<long long>(grid_for(P, 8), 152LL * 16));
-    k_step2d<T, N, H><<<grid, 256, 0, s>>>(in, out, levels, meta, P, g, coef, up[0], up[1], err);
-    AMR_LAUNCHED("k_step2d");
+    return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
+        AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
+        k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(in, out, levels, meta, P, g,
+                                                                                      coef, up[0], up[1], err, keys,
+                                                                                      vel);
+        AMR_LAUNCHED("k_step2d");
+        return AMR_OK;
+    });
+}
+
+// ------------------------------------------------------------ autotuner
+// Picks (W, S, grid) for the 2D update kernel by timing every candidate on
+// the tree's current leaves (reads the current state, writes the next
+// buffer, which the following step overwrites).  Results are cached per
+// device, dtype, patch shape and leaf-count octave.
+struct TuneKey {
+    int dev, esize, n, h, octave, per_leaf;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(dev, esize, n, h, octave, per_leaf) < std::tie(o.dev, o.esize, o.n, o.h, o.octave, o.per_leaf);
+    }
+};
+std::mutex                 g_tune_mu;
+std::map<TuneKey, StepCfg> g_tuned;
+std::atomic<int>           g_tune_mode{ 1 }; // 0 off (defaults), 1 on
+
+TuneKey tune_key(const amr_tree* t, bool per_leaf)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int oct = 0;
+    while ((static_cast<size_t>(1) << oct) < t->size) ++oct;
+    return TuneKey{ dev, static_cast<int>(t->esize), t->g.n, t->g.h, oct, per_leaf ? 1 : 0 };
+}
+
+bool lookup_tuned(const amr_tree* t, bool per_leaf, StepCfg& cfg)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto                        it = g_tuned.find(tune_key(t, per_leaf));
+    if (it == g_tuned.end()) return false;
+    cfg = it->second;
+    return true;
+}
+
+template <typename T, int N, int H>
+amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const double* vel, StepCfg& best)
+{
+    const TuneKey key = tune_key(t, vel != nullptr);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto                        it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            best = it->second;
+            return AMR_OK;
+        }
+    }
+    best = StepCfg{};
+    if (g_tune_mode.load() == 0) return AMR_OK;
+    const int    P = static_cast<int>(t->size);
+    cudaStream_t s = t->stream;
+    cudaEvent_t  e0, e1;
+    AMR_CUDA(cudaEventCreate(&e0));
+    AMR_CUDA(cudaEventCreate(&e1));
+    float     best_ms = 0.0f;
+    bool      have    = false;
+    const int sms     = num_sms();
+    for (const auto& ws : kStepConfigs) {
+        amr_status st = with_ws(ws[0], ws[1], [&]<int W, int S>() -> amr_status {
+            const int occ = step2d_occupancy<T, N, H, W, S>();
+            if (occ < 1) return AMR_OK;
+            const int full = static_cast<int>(grid_for(P, W));
+            for (int bps : { 1, 2, 3, 4, 6, 8, 12, 16 }) {
+                if (bps > occ) break;
+                const int grid = std::min(full, sms * bps);
+                StepCfg   c{ W, S, grid };
+                for (int rep = 0; rep < 2; ++rep) { // warm-up
+                    amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                          t->levels[t->tb], t->meta[t->tb], P, t->g, coef, up,
+                                                          t->status + 7, t->keys[t->tb], vel, c, s);
+                    if (r != AMR_OK) return r;
+                }
+                const int reps = 4;
+                AMR_CUDA(cudaEventRecord(e0, s));
+                for (int rep = 0; rep < reps; ++rep) {
+                    amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                          t->levels[t->tb], t->meta[t->tb], P, t->g, coef, up,
+                                                          t->status + 7, t->keys[t->tb], vel, c, s);
+                    if (r != AMR_OK) return r;
+                }
+                AMR_CUDA(cudaEventRecord(e1, s));
+                AMR_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (!have || ms < best_ms) {
+                    best_ms = ms;
+                    best    = c;
+                    have    = true;
+                }
+                if (grid == full) break; // more blocks would idle
+            }
+            return AMR_OK;
+        });
+        if (st != AMR_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return st;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best;
     return AMR_OK;
 }
 
@@ -169,8 +400,13 @@ void free_tree(amr_tree* t)
         cudaEventDestroy(e.first);
         cudaEventDestroy(e.second);
     }
-    cudaFree(t->cur);
-    cudaFree(t->nxt);
+    for (auto& ge : t->graphs) {
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        if (ge.graph) cudaGraphDestroy(ge.graph);
+    }
+    if (t->cap_stream) cudaStreamDestroy(t->cap_stream);
+    cudaFree(t->sbuf[0]);
+    cudaFree(t->sbuf[1]);
     for (int b = 0; b < 2; ++b) {
         cudaFree(t->keys[b]);
         cudaFree(t->levels[b]);
@@ -185,10 +421,19 @@ void free_tree(amr_tree* t)
     cudaFree(t->skind);
     cudaFree(t->status);
     cudaFree(t->maxlev);
+    cudaFree(t->maxlev_new);
     cudaFree(t->vel);
+    cudaFree(t->vel_inst);
+    cudaFree(t->bounds);
+    cudaFree(t->target);
+    cudaFree(t->offs);
+    cudaFree(t->tile_sums);
+    cudaFree(t->ctl);
     cudaFree(t->dt_acc);
     cudaFree(t->dt_rem);
     cudaFree(t->dt_cnt);
+    cudaFree(t->dt_tot);
+    cudaFree(t->dt_ctot);
     cudaFree(t->step_dt);
     cudaFree(t->coef);
     cudaFree(t->cstats);
@@ -210,40 +455,61 @@ amr_status launch_halo(amr_tree* t)
 }
 
 
-// One root leaf: key 0, level 0, periodic self-neighbours (ndtree.hpp:411-421),
-// zero state in both buffers.
+// One root leaf per instance: key i << inst_shift, level 0, periodic
+// self-neighbours (ndtree.hpp:411-421), zero state in both buffers.
 amr_status init_root(amr_tree* t)
 {
     const Geo&                 g = t->g;
-    std::vector<amr_halo_meta> root(g.ndir);
-    for (auto& m : root) {
-        m.neighbor = 0;
-        for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
-        for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
-        m.relation   = REL_SAME;
-        m.padding[0] = m.padding[1] = m.padding[2] = 0;
+    const int                  K = t->ninst;
+    std::vector<amr_halo_meta> root(static_cast<size_t>(K) * g.ndir);
+    std::vector<uint64_t>      keys(K);
+    std::vector<int32_t>       zeros(K, 0);
+    for (int i = 0; i < K; ++i) {
+        keys[i] = K > 1 ? static_cast<uint64_t>(i) << g.inst_shift : 0ull;
+        for (int d = 0; d < g.ndir; ++d) {
+            amr_halo_meta& m = root[static_cast<size_t>(i) * g.ndir + d];
+            m.neighbor       = i;
+            for (int q = 0; q < 4; ++q) m.finer_ids[q] = -1;
+            for (int q = 0; q < 3; ++q) m.quadrant[q] = 0;
+            m.relation   = REL_SAME;
+            m.padding[0] = m.padding[1] = m.padding[2] = 0;
+        }
     }
-    const uint64_t zero_key = 0;
-    const int32_t  zero_lev = 0;
-    const size_t   state_bytes = t->cap * g.flat * t->esize;
-    t->tb = 0;
+    const size_t state_bytes = t->cap * g.flat * t->esize;
+    t->tb  = 0;
+    t->cur = t->sbuf[0];
+    t->nxt = t->sbuf[1];
     AMR_CUDA(cudaMemsetAsync(t->cur, 0, state_bytes, t->stream));
     AMR_CUDA(cudaMemsetAsync(t->nxt, 0, state_bytes, t->stream));
     AMR_CUDA(cudaMemsetAsync(t->status, 0, 8 * sizeof(int32_t), t->stream));
-    AMR_CUDA(cudaMemcpyAsync(t->keys[0], &zero_key, 8, cudaMemcpyHostToDevice, t->stream));
-    AMR_CUDA(cudaMemcpyAsync(t->levels[0], &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
-    AMR_CUDA(cudaMemcpyAsync(t->maxlev, &zero_lev, 4, cudaMemcpyHostToDevice, t->stream));
-    AMR_CUDA(cudaMemcpyAsync(t->meta[0], root.data(), g.ndir * sizeof(amr_halo_meta), cudaMemcpyHostToDevice,
+    AMR_CUDA(cudaMemsetAsync(t->maxlev_new, 0, K * sizeof(int32_t), t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->keys[0], keys.data(), K * sizeof(uint64_t), cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->levels[0], zeros.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->maxlev, zeros.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(t->meta[0], root.data(), root.size() * sizeof(amr_halo_meta), cudaMemcpyHostToDevice,
                              t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
-    t->size           = 1;
+    t->size           = static_cast<size_t>(K);
     t->max_level_host = 0;
     t->ghosts_valid   = true;
     t->batch_open     = false;
     return AMR_OK;
 }
 
-
+// Finest level over all leaves of a forest after a re-mesh (one tree: the
+// single max_level slot already holds it).
+amr_status forest_max_level(amr_tree* t, int* out)
+{
+    int32_t* hs = static_cast<int32_t*>(t->pinned);
+    AMR_CUDA(cudaMemsetAsync(t->status + 3, 0, sizeof(int32_t), t->stream));
+    k_max_level<<<std::min<unsigned>(grid_for(static_cast<long long>(t->size), 256), 1024u), 256, 0, t->stream>>>(
+        t->levels[t->tb], static_cast<int>(t->size), t->status + 3);
+    AMR_LAUNCHED("k_max_level");
+    AMR_CUDA(cudaMemcpyAsync(hs + 6, t->status + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    *out = hs[6];
+    return AMR_OK;
+}
 
 // Smallest non-negative double s whose correctly rounded square root passes
 // `v > thr` (strict) or `v >= thr`; NaN when no s does.  Non-negative doubles
@@ -328,6 +594,343 @@ amr_status launch_cycle(amr_tree* t, CycleArgs& A, int cluster)
     return AMR_OK;
 }
 
+// ------------------------------------------------------------ graph run
+RunBufs run_bufs(amr_tree* t, bool per_leaf_vel, bool bounds)
+{
+    RunBufs B{};
+    B.state[0] = t->sbuf[0];
+    B.state[1] = t->sbuf[1];
+    for (int b = 0; b < 2; ++b) {
+        B.keys[b]   = t->keys[b];
+        B.levels[b] = t->levels[b];
+        B.meta[b]   = t->meta[b];
+    }
+    B.flags      = t->flags;
+    B.rmark      = t->rmark;
+    B.chead      = t->chead;
+    B.cnt        = t->cnt;
+    B.pos        = t->pos;
+    B.src        = t->src;
+    B.skind      = t->skind;
+    B.maxlev     = t->maxlev;
+    B.maxlev_new = t->maxlev_new;
+    B.vel        = per_leaf_vel ? t->vel : nullptr;
+    B.bounds     = bounds ? t->bounds : nullptr;
+    B.tile_sums  = t->tile_sums;
+    B.cap        = t->cap;
+    B.ninst      = t->ninst;
+    return B;
+}
+
+template <typename T, int N, int H>
+amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, int parity, const int* up,
+                             const StepCfg& cfg, int P, cudaStream_t s)
+{
+    return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
+        AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
+        k_run_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(B, ctl, g, coef, parity,
+                                                                                          up[0], up[1]);
+        AMR_LAUNCHED("k_run_step2d");
+        return AMR_OK;
+    });
+}
+
+// The launch sequence of one interval on stream cs (captured into a graph).
+// Grids are fixed; every kernel takes the leaf count from the control block.
+template <typename T>
+amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaStream_t cs)
+{
+    const Geo& g   = t->g;
+    const int  K   = t->ninst, nl = g.depth + 1, sms = num_sms();
+    RunCtl*    ctl = t->ctl;
+    k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
+                                     t->coef);
+    AMR_LAUNCHED("k_batch_begin");
+    const StepCfg cfg{ key.W, key.S, key.grid };
+    const int     ppb = std::max(1, 256 / g.cells);
+    for (int j = 0; j < key.k; ++j) {
+        const Coef* cf = t->coef + static_cast<size_t>(j) * K * nl;
+        amr_status  st = AMR_OK;
+        if (key.W > 0 && g.n == 16)
+            st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+        else if (key.W > 0)
+            st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+        else {
+            k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, j & 1, key.up[0], key.up[1], key.up[2], ppb);
+            AMR_LAUNCHED("k_run_step");
+        }
+        if (st != AMR_OK) return st;
+    }
+    const int sp = key.k & 1;
+    if (key.crit != 0) {
+        k_run_halo<T><<<sms * 32, 256, 0, cs>>>(B, ctl, g, sp);
+        AMR_LAUNCHED("k_run_halo");
+        k_run_flags<T><<<sms * 16, 128, 0, cs>>>(B, ctl, g, key.crit, key.rthr, key.cthr, key.min_level,
+                                                  key.max_level, sp);
+        AMR_LAUNCHED("k_run_flags");
+        k_run_mark<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_mark");
+        for (int r = 0; r < key.rounds; ++r) {
+            k_run_closure<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+            AMR_LAUNCHED("k_run_closure");
+        }
+        k_run_veto<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_veto");
+        k_run_count<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_count");
+        const unsigned ntile =
+            static_cast<unsigned>(std::min<size_t>(1024, std::max<size_t>(1, (t->cap + kScanTile - 1) / kScanTile)));
+        k_run_scan_tiles<<<ntile, kScanThreads, 0, cs>>>(B, ctl);
+        AMR_LAUNCHED("k_run_scan_tiles");
+        k_run_scan_apply<<<ntile, kScanThreads, 0, cs>>>(B, ctl);
+        AMR_LAUNCHED("k_run_scan_apply");
+        k_run_emit<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_emit");
+        k_run_remap<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, sp);
+        AMR_LAUNCHED("k_run_remap");
+        k_run_neighbors<<<sms * 8, 128, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_neighbors");
+    }
+    k_run_commit<<<1, 256, 0, cs>>>(B, ctl, key.k, g.cells, key.crit != 0 ? 1 : 0, sp);
+    AMR_LAUNCHED("k_run_commit");
+    return AMR_OK;
+}
+
+// Executable graph of one interval, captured on first use and cached on the
+// tree (buffers have fixed addresses for the tree's lifetime).
+amr_status interval_graph(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaGraphExec_t* out,
+                          uint64_t* kernels)
+{
+    for (auto& ge : t->graphs)
+        if (ge.key == key) {
+            *out     = ge.exec;
+            *kernels = ge.kernels;
+            return AMR_OK;
+        }
+    if (!t->cap_stream) AMR_CUDA(cudaStreamCreateWithFlags(&t->cap_stream, cudaStreamNonBlocking));
+    AMR_CUDA(cudaStreamBeginCapture(t->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t before = g_launches.load();
+    amr_status st = t->dtype == AMR_F64 ? record_interval<double>(t, key, B, t->cap_stream)
+                                        : record_interval<float>(t, key, B, t->cap_stream);
+    const uint64_t recorded = g_launches.load() - before;
+    g_launches.fetch_sub(recorded); // counted when replayed
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce    = cudaStreamEndCapture(t->cap_stream, &graph);
+    if (st != AMR_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    GraphEntry ge;
+    ge.key     = key;
+    ge.graph   = graph;
+    ge.kernels = recorded;
+    ce       = cudaGraphInstantiate(&ge.exec, graph, 0);
+    if (ce != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return cuda_fail(ce, "cudaGraphInstantiate");
+    }
+    if (t->graphs.size() >= 8) { // keep a handful of shapes
+        cudaGraphExecDestroy(t->graphs.front().exec);
+        cudaGraphDestroy(t->graphs.front().graph);
+        t->graphs.erase(t->graphs.begin());
+    }
+    t->graphs.push_back(ge);
+    *out     = ge.exec;
+    *kernels = ge.kernels;
+    return AMR_OK;
+}
+
+struct RunTotals {
+    long long done     = 0;
+    double    sum_dt   = 0.0;
+    uint64_t  executed = 0, cells = 0, remeshes = 0, intervals = 0, leaves_sum = 0, persistent = 0, graphs = 0;
+    uint64_t  lmin = ~0ull, lmax = 0;
+};
+
+// Up to `max_intervals` intervals as graph replays, then one readback of the
+// control block.  Requires that no step is clamped by the remaining time.
+amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_params, long long max_intervals,
+                           RunTotals& tot)
+{
+    const Geo&      g     = t->g;
+    const int       K     = t->ninst;
+    cudaStream_t    s     = t->stream;
+    const long long total = static_cast<long long>(p->steps);
+    const long long k     = static_cast<long long>(p->remesh_interval);
+    const bool      per_leaf = inst_params && K > 1;
+    // velocities in use
+    if (inst_params) {
+        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    } else {
+        std::vector<double> v(3 * static_cast<size_t>(K));
+        for (int i = 0; i < K; ++i)
+            for (int a = 0; a < 3; ++a) v[3 * i + a] = p->velocity[a];
+        AMR_CUDA(cudaMemcpyAsync(t->vel, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    const RunBufs B = run_bufs(t, per_leaf, t->bounds_set);
+    // control block and per-instance time
+    RunCtl c{};
+    c.P          = static_cast<int32_t>(t->size);
+    c.tb         = t->tb;
+    c.sb         = t->cur == t->sbuf[0] ? 0 : 1;
+    c.max_level  = t->max_level_host;
+    c.leaves_min = INT_MAX;
+    c.leaves_max = 0;
+    RunCtl* hc   = reinterpret_cast<RunCtl*>(static_cast<char*>(t->pinned) + 64);
+    *hc          = c;
+    AMR_CUDA(cudaMemcpyAsync(t->ctl, hc, sizeof(RunCtl), cudaMemcpyHostToDevice, s));
+    // the key of the interval graph(s)
+    GraphKey key;
+    key.crit      = p->criterion;
+    key.min_level = p->min_level;
+    key.max_level = p->max_level;
+    key.bounds    = t->bounds_set ? 1 : 0;
+    key.vel       = per_leaf ? 1 : 0;
+    key.rthr      = p->refine_threshold;
+    key.cthr      = p->coarsen_threshold;
+    key.cfl       = p->cfl;
+    for (int a = 0; a < g.rank && !per_leaf; ++a)
+        key.up[a] = p->velocity[a] > 0.0 ? -1 : (p->velocity[a] < 0.0 ? 1 : 0);
+    int allowed = p->max_level;
+    if (t->bounds_set) {
+        std::vector<int32_t> b(2 * static_cast<size_t>(K));
+        AMR_CUDA(cudaMemcpy(b.data(), t->bounds, b.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        allowed = 0;
+        for (int i = 0; i < K; ++i) allowed = std::max(allowed, static_cast<int>(b[2 * i + 1]));
+    }
+    key.rounds = std::max(1, std::min(g.depth, std::max(t->max_level_host, allowed)));
+    const bool step2d = g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8);
+    if (step2d) {
+        StepCfg cfg;
+        if (g.n == 16) {
+            // tune on the current leaves with a coefficient table of this run
+            k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, g, t->vel, p->cfl, 1, BATCH_RESET, 1.0, t->dts(), t->step_dt,
+                                            t->coef);
+            AMR_LAUNCHED("k_batch_begin");
+            int up[3] = { key.up[0], key.up[1], key.up[2] };
+            amr_status ts = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+                using T = decltype(z);
+                return tune_step2d<T, 16, 1>(t, t->coef, up, per_leaf ? t->vel : nullptr, cfg);
+            });
+            if (ts != AMR_OK) return ts;
+        }
+        key.W    = cfg.W;
+        key.S    = cfg.S;
+        key.grid = cfg.grid; // 0: full residency
+        // kernel attributes are set outside the capture
+        amr_status ps = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+            using T = decltype(z);
+            return with_ws(key.W, key.S, [&]<int W, int S>() -> amr_status {
+                if (g.n == 16) AMR_CUDA((prepare_step2d<T, 16, 1, W, S>()));
+                else AMR_CUDA((prepare_step2d<T, 8, 1, W, S>()));
+                return AMR_OK;
+            });
+        });
+        if (ps != AMR_OK) return ps;
+    }
+    // per-instance time: the run's totals so far carried in (one tree)
+    k_run_dt_init<<<grid_for(K, 256), 256, 0, s>>>(t->dts(), K, p->remaining_time - tot.sum_dt,
+                                                    K == 1 ? tot.sum_dt : 0.0,
+                                                    K == 1 ? static_cast<uint32_t>(tot.executed) : 0u);
+    AMR_LAUNCHED("k_run_dt_init");
+    const long long left  = total - tot.done;
+    long long       nfull = std::min(left / k, max_intervals);
+    const long long rem   = (nfull < max_intervals) ? left % k : 0;
+    cudaGraphExec_t full = nullptr, tail = nullptr;
+    uint64_t        nk_full = 0, nk_tail = 0;
+    if (nfull > 0) {
+        key.k         = static_cast<int>(k);
+        amr_status st = interval_graph(t, key, B, &full, &nk_full);
+        if (st != AMR_OK) return st;
+    }
+    if (rem > 0) {
+        key.k         = static_cast<int>(rem);
+        amr_status st = interval_graph(t, key, B, &tail, &nk_tail);
+        if (st != AMR_OK) return st;
+    }
+    for (long long i = 0; i < nfull; ++i) {
+        AMR_CUDA(cudaGraphLaunch(full, s));
+        g_launches.fetch_add(nk_full);
+    }
+    if (tail) {
+        AMR_CUDA(cudaGraphLaunch(tail, s));
+        g_launches.fetch_add(nk_tail);
+    }
+    // readback
+    AMR_CUDA(cudaMemcpyAsync(hc, t->ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost, s));
+    char* hp = static_cast<char*>(t->pinned) + 64 + sizeof(RunCtl);
+    AMR_CUDA(cudaMemcpyAsync(hp, t->dt_acc, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaMemcpyAsync(hp + 8 * K, t->dt_tot, K * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaMemcpyAsync(hp + 16 * K, t->dt_cnt, K * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaMemcpyAsync(hp + 20 * K, t->dt_ctot, K * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaStreamSynchronize(s));
+    const RunCtl r = *hc;
+    t->size        = static_cast<size_t>(r.P);
+    t->tb          = r.tb;
+    t->cur         = t->sbuf[r.sb];
+    t->nxt         = t->sbuf[r.sb ^ 1];
+    t->max_level_host = r.max_level;
+    t->ghosts_valid   = false;
+    t->batch_open     = true;
+    // time of each instance = its batch totals + the open batch
+    double   tmax = 0.0;
+    uint32_t cmax = 0;
+    for (int i = 0; i < K; ++i) {
+        double   a, b;
+        uint32_t ca, cb;
+        std::memcpy(&a, hp + 8 * i, sizeof a);
+        std::memcpy(&b, hp + 8 * K + 8 * i, sizeof b);
+        std::memcpy(&ca, hp + 16 * K + 4 * i, sizeof ca);
+        std::memcpy(&cb, hp + 20 * K + 4 * i, sizeof cb);
+        const double ti = b + a;
+        if (i == 0 || ti > tmax) tmax = ti;
+        cmax = std::max(cmax, ca + cb);
+    }
+    tot.done += nfull * k + rem;
+    if (K == 1) { // the totals were carried in
+        tot.sum_dt   = tmax;
+        tot.executed = cmax;
+    } else {
+        tot.sum_dt += tmax;
+        tot.executed += cmax;
+    }
+    tot.cells += r.cell_updates;
+    tot.remeshes += r.remeshes;
+    tot.intervals += r.intervals;
+    tot.graphs += r.intervals;
+    tot.leaves_sum += r.leaves_sum;
+    if (r.intervals) {
+        tot.lmin = std::min<uint64_t>(tot.lmin, static_cast<uint64_t>(r.leaves_min));
+        tot.lmax = std::max<uint64_t>(tot.lmax, static_cast<uint64_t>(r.leaves_max));
+    }
+    if (r.err) {
+        const char* what = r.err == AMR_ERR_CAPACITY     ? "re-mesh would exceed the tree capacity"
+                           : r.err == AMR_ERR_UNBALANCED ? "neighbour rebuild found a non-2:1 face"
+                           : r.err == AMR_ERR_TIMEOUT    ? "a bulk copy did not complete within the wait limit"
+                                                         : "interval graph failed";
+        if (r.err == AMR_ERR_TIMEOUT) AMR_CUDA(cudaMemsetAsync(t->ctl, 0, sizeof(RunCtl), s));
+        return fail(static_cast<amr_status>(r.err), what);
+    }
+    return AMR_OK;
+}
+
+// Largest CFL step any instance can take (level 0) times the steps left: the
+// graph path needs the remaining time to cover it, so no step is clamped.
+bool no_clamp(amr_tree* t, const amr_cycle_params* p, bool inst_params, long long steps_left, double sum_dt)
+{
+    double dmax = 0.0;
+    if (inst_params) {
+        for (size_t i = 0; i < t->vel_inst_host.size() / 3; ++i)
+            dmax = std::max(dmax, p->cfl * raw_dt(t->g, &t->vel_inst_host[3 * i], 0));
+    } else {
+        dmax = p->cfl * raw_dt(t->g, p->velocity, 0);
+    }
+    const double need = 2.0 * static_cast<double>(steps_left) * dmax;
+    return std::isfinite(need) && p->remaining_time - sum_dt >= need;
+}
+
 } // namespace
 
 extern "C" {
@@ -344,10 +947,20 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     if (!make_geo(&desc->geom, g)) return fail(AMR_ERR_INVALID, "bad patch geometry");
     if (desc->capacity < 1 || desc->capacity > (1ull << 30)) return fail(AMR_ERR_INVALID, "bad capacity");
     if (desc->dtype != AMR_F64 && desc->dtype != AMR_F32) return fail(AMR_ERR_INVALID, "bad dtype");
+    const int K = desc->instances > 1 ? desc->instances : 1;
+    if (desc->instances < 0) return fail(AMR_ERR_INVALID, "bad instance count");
+    if (K > 1) {
+        g.inst_shift = 6 + g.rank * g.depth;
+        int bits     = 0;
+        while ((1ll << bits) < K) ++bits;
+        if (g.inst_shift + bits > 64) return fail(AMR_ERR_INVALID, "too many instances for the tree depth");
+    }
+    if (static_cast<size_t>(K) > desc->capacity) return fail(AMR_ERR_INVALID, "capacity below the instance count");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(AMR_ERR_NO_DEVICE, "no CUDA device");
     amr_tree* t = new amr_tree();
     t->g      = g;
+    t->ninst  = K;
     t->cap    = desc->capacity;
     t->dtype  = desc->dtype;
     t->esize  = desc->dtype == AMR_F64 ? 8 : 4;
@@ -357,8 +970,8 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     auto         al  = [&](void** p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
     };
-    al(&t->cur, state_bytes);
-    al(&t->nxt, state_bytes);
+    al(&t->sbuf[0], state_bytes);
+    al(&t->sbuf[1], state_bytes);
     for (int b = 0; b < 2; ++b) {
         al(reinterpret_cast<void**>(&t->keys[b]), cap * sizeof(uint64_t));
         al(reinterpret_cast<void**>(&t->levels[b]), cap * sizeof(int32_t));
@@ -372,20 +985,34 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->src), cap * sizeof(int32_t));
     al(reinterpret_cast<void**>(&t->skind), cap);
     al(reinterpret_cast<void**>(&t->status), 8 * sizeof(int32_t));
-    al(reinterpret_cast<void**>(&t->maxlev), sizeof(int32_t));
-    al(reinterpret_cast<void**>(&t->vel), 3 * sizeof(double));
-    al(reinterpret_cast<void**>(&t->dt_acc), sizeof(double));
-    al(reinterpret_cast<void**>(&t->dt_rem), sizeof(double));
-    al(reinterpret_cast<void**>(&t->dt_cnt), sizeof(uint32_t));
-    al(reinterpret_cast<void**>(&t->step_dt), kMaxBatch * sizeof(double));
-    al(reinterpret_cast<void**>(&t->coef), kMaxBatch * (g.depth + 1) * sizeof(Coef));
+    // coefficient table: up to kMaxBatch steps, at most 16 MiB for a forest
+    const size_t nl          = static_cast<size_t>(g.depth + 1);
+    const size_t coef_steps  = std::max<size_t>(1, std::min<size_t>(kMaxBatch, (16u << 20) / (K * nl * sizeof(Coef))));
+    const size_t ntiles      = (cap + kScanTile - 1) / kScanTile + 1;
+    al(reinterpret_cast<void**>(&t->maxlev), K * sizeof(int32_t));
+    al(reinterpret_cast<void**>(&t->maxlev_new), K * sizeof(int32_t));
+    al(reinterpret_cast<void**>(&t->vel), 3 * K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->vel_inst), 3 * K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->bounds), 2 * K * sizeof(int32_t));
+    al(reinterpret_cast<void**>(&t->target), K * sizeof(int32_t));
+    al(reinterpret_cast<void**>(&t->offs), (K + 1) * sizeof(unsigned long long));
+    al(reinterpret_cast<void**>(&t->tile_sums), ntiles * sizeof(uint32_t));
+    al(reinterpret_cast<void**>(&t->ctl), sizeof(RunCtl));
+    al(reinterpret_cast<void**>(&t->dt_acc), K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->dt_rem), K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->dt_cnt), K * sizeof(uint32_t));
+    al(reinterpret_cast<void**>(&t->dt_tot), K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->dt_ctot), K * sizeof(uint32_t));
+    al(reinterpret_cast<void**>(&t->step_dt), coef_steps * K * sizeof(double));
+    al(reinterpret_cast<void**>(&t->coef), coef_steps * K * nl * sizeof(Coef));
     al(reinterpret_cast<void**>(&t->cstats), sizeof(CycleStats));
-    if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, 256);
+    t->pinned_bytes = std::max<size_t>(1024, 64 + (K + 1) * 32 + sizeof(RunCtl));
+    if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, t->pinned_bytes);
     if (e != cudaSuccess) {
         free_tree(t);
         return cuda_fail(e, "amr_tree_create allocation");
     }
-    t->coef_steps = kMaxBatch;
+    t->coef_steps = coef_steps;
     amr_status rs = init_root(t);
     if (rs != AMR_OK) {
         free_tree(t);
@@ -501,7 +1128,8 @@ amr_status amr_tree_flags_gradient(amr_tree* t, double rthr, double cthr, int mi
     return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
         k_flags_gradient<T><<<P, 128, 0, t->stream>>>(static_cast<const T*>(t->cur), t->levels[t->tb], P, t->g, rthr,
-                                                     cthr, min_level, max_level, t->flags);
+                                                     cthr, min_level, max_level, t->flags,
+            t->keys[t->tb], t->bounds_set ? t->bounds : nullptr);
         AMR_LAUNCHED("k_flags_gradient");
         return AMR_OK;
     });
@@ -518,7 +1146,8 @@ amr_status amr_tree_flags_max(amr_tree* t, double rthr, double cthr, int min_lev
     return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
         k_flags_max<T><<<P, 128, 0, t->stream>>>(static_cast<const T*>(t->cur), t->levels[t->tb], P, t->g, rthr, cthr,
-                                                min_level, max_level, t->flags);
+                                                min_level, max_level, t->flags,
+            t->keys[t->tb], t->bounds_set ? t->bounds : nullptr);
         AMR_LAUNCHED("k_flags_max");
         return AMR_OK;
     });
@@ -568,7 +1197,7 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     if (hs[0] != 0) return fail(static_cast<amr_status>(hs[0]), "re-mesh would exceed the tree capacity");
     if (!hs[1]) return AMR_OK; // reconstruction_is_noop (ndtree.hpp:1242-1246)
     const int NP = hs[2];
-    AMR_CUDA(cudaMemsetAsync(t->maxlev, 0, sizeof(int32_t), s));
+    AMR_CUDA(cudaMemsetAsync(t->maxlev, 0, t->ninst * sizeof(int32_t), s));
     k_emit<<<grid_for(P, 256), 256, 0, s>>>(t->keys[tb], t->rmark, t->chead, t->pos, P, g, t->keys[nb], t->levels[nb],
                                             t->src, t->skind, t->maxlev);
     AMR_LAUNCHED("k_emit");
@@ -585,12 +1214,20 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     AMR_CUDA(cudaMemcpyAsync(hs + 4, t->status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaMemcpyAsync(hs + 5, t->maxlev, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaStreamSynchronize(s));
+    const int nerr = hs[4];
     std::swap(t->cur, t->nxt);
     t->tb             = nb;
     t->size           = static_cast<size_t>(NP);
     t->max_level_host = hs[5];
     t->ghosts_valid   = false;
     if (changed) *changed = 1;
+    if (t->ninst > 1) {
+        int m = 0;
+        amr_status ms = forest_max_level(t, &m);
+        if (ms != AMR_OK) return ms;
+        t->max_level_host = m;
+    }
+    hs[4] = nerr;
     if (hs[4] != 0) return fail(static_cast<amr_status>(hs[4]), "neighbour rebuild found a non-2:1 face");
     return AMR_OK;
 }
@@ -607,23 +1244,38 @@ amr_status amr_tree_refine_uniform(amr_tree* t, int levels)
     return AMR_OK;
 }
 
-amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining)
+static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining,
+                        int first_mode)
 {
-    if (!t || !velocity3) return fail(AMR_ERR_INVALID, "null argument");
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
     cudaStream_t s = t->stream;
-    AMR_CUDA(cudaMemcpyAsync(t->vel, velocity3, 3 * sizeof(double), cudaMemcpyHostToDevice, s));
-    int up[3] = { 0, 0, 0 };
-    for (int a = 0; a < t->g.rank; ++a) up[a] = velocity3[a] > 0.0 ? -1 : (velocity3[a] < 0.0 ? 1 : 0);
+    const int    K = t->ninst;
+    int          up[3] = { 0, 0, 0 };
+    if (velocity3) {
+        std::vector<double> v(3 * static_cast<size_t>(K));
+        for (int i = 0; i < K; ++i)
+            for (int a = 0; a < 3; ++a) v[3 * i + a] = velocity3[a];
+        AMR_CUDA(cudaMemcpyAsync(t->vel, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+        for (int a = 0; a < t->g.rank; ++a) up[a] = velocity3[a] > 0.0 ? -1 : (velocity3[a] < 0.0 ? 1 : 0);
+        t->vel_per_leaf = false;
+    } else {
+        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        t->vel_per_leaf = true;
+    }
+    const double* vleaf = t->vel_per_leaf ? t->vel : nullptr;
     const int P     = static_cast<int>(t->size);
     const int ppb   = std::max(1, 256 / t->g.cells);
     const unsigned grid = grid_for(P, ppb);
     const int nl    = t->g.depth + 1;
     bool      first = true;
     size_t    done  = 0;
+    StepCfg   cfg;
+    lookup_tuned(t, vleaf != nullptr, cfg);
     while (done < steps || (first && steps == 0)) {
-        const int chunk = static_cast<int>(std::min(kMaxBatch, steps - done));
-        k_batch_begin<<<1, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? 1 : 0, remaining, t->dt_acc,
-                                        t->dt_rem, t->dt_cnt, t->step_dt, t->coef);
+        const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
+        k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? first_mode : BATCH_CONTINUE,
+                                        remaining, t->dts(), t->step_dt, t->coef);
         AMR_LAUNCHED("k_batch_begin");
         first = false;
         for (int k = 0; k < chunk; ++k) {
@@ -643,17 +1295,18 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
             }
             amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
                 using T        = decltype(z);
-                const Coef* cf = t->coef + static_cast<size_t>(k) * nl;
+                const Coef* cf = t->coef + static_cast<size_t>(k) * K * nl;
                 const T*    in = static_cast<const T*>(t->cur);
                 T*          out = static_cast<T*>(t->nxt);
                 if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
                     return launch_step2d<T, 16, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
-                                                   t->status + 7, s);
+                                                   t->status + 7, t->keys[t->tb], vleaf, cfg, s);
                 if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
                     return launch_step2d<T, 8, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
-                                                  t->status + 7, s);
+                                                  t->status + 7, t->keys[t->tb], vleaf, StepCfg{}, s);
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
-                                                     up[1], up[2], ppb);
+                                                     up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
+                                                     vleaf);
                 AMR_LAUNCHED("k_step");
                 return AMR_OK;
             });
@@ -669,13 +1322,19 @@ amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, 
     return AMR_OK;
 }
 
+amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining)
+{
+    return advance_impl(t, steps, velocity3, cfl, remaining, BATCH_RESET);
+}
+
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    char* hp = static_cast<char*>(t->pinned);
-    AMR_CUDA(cudaMemcpyAsync(hp + 32, t->dt_acc, sizeof(double), cudaMemcpyDeviceToHost, t->stream));
-    AMR_CUDA(cudaMemcpyAsync(hp + 40, t->dt_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream));
+    char*     hp = static_cast<char*>(t->pinned);
+    const int K  = t->ninst;
     AMR_CUDA(cudaMemcpyAsync(hp + 48, t->status + 7, sizeof(int32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(hp + 64, t->dt_acc, K * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(hp + 64 + 8 * K, t->dt_cnt, K * sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     int32_t wait_err = 0;
     std::memcpy(&wait_err, hp + 48, sizeof wait_err);
@@ -683,10 +1342,17 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
         AMR_CUDA(cudaMemsetAsync(t->status + 7, 0, sizeof(int32_t), t->stream));
         return fail(AMR_ERR_TIMEOUT, "a bulk copy did not complete within the wait limit");
     }
-    double   acc;
-    uint32_t cnt;
-    std::memcpy(&acc, hp + 32, sizeof acc);
-    std::memcpy(&cnt, hp + 40, sizeof cnt);
+    // one tree: its time; a forest: the instance furthest ahead
+    double   acc = 0.0;
+    uint32_t cnt = 0;
+    for (int i = 0; i < K; ++i) {
+        double   a;
+        uint32_t c;
+        std::memcpy(&a, hp + 64 + 8 * i, sizeof a);
+        std::memcpy(&c, hp + 64 + 8 * K + 4 * i, sizeof c);
+        if (i == 0 || a > acc) acc = a;
+        cnt = std::max(cnt, c);
+    }
     if (!t->batch_open) {
         acc = 0.0;
         cnt = 0;
@@ -700,19 +1366,18 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
 {
     if (!t || !p) return fail(AMR_ERR_INVALID, "null argument");
     if (p->criterion < 0 || p->criterion > 2) return fail(AMR_ERR_INVALID, "unknown criterion");
-    const Geo&  g = t->g;
-    long long   done = 0;
-    double      sum_dt = 0.0;
-    uint64_t    executed = 0, cells = 0, remeshes = 0, intervals = 0, leaves_sum = 0, persistent = 0;
-    uint64_t    lmin = ~0ull, lmax = 0;
+    const bool inst_params = (p->options & AMR_RUN_INSTANCE_PARAMS) != 0;
+    if (inst_params && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no per-instance velocities set");
+    const Geo&      g     = t->g;
     const long long total = static_cast<long long>(p->steps);
+    RunTotals       tot;
     int up[3] = { 0, 0, 0 };
     for (int a = 0; a < g.rank; ++a) up[a] = p->velocity[a] > 0.0 ? -1 : (p->velocity[a] < 0.0 ? 1 : 0);
     const size_t smem = static_cast<size_t>(p->remesh_interval) * (g.depth + 1) * sizeof(Coef) +
                         static_cast<size_t>(p->remesh_interval) * sizeof(double);
-    while (done < total) {
-        const bool small = !(p->options & AMR_RUN_PER_LAUNCH) && t->size <= static_cast<size_t>(kPersistentLeaves) &&
-                           p->remesh_interval >= 1 &&
+    while (tot.done < total) {
+        const bool small = t->ninst == 1 && !(p->options & AMR_RUN_PER_LAUNCH) &&
+                           t->size <= static_cast<size_t>(kPersistentLeaves) && p->remesh_interval >= 1 &&
                            p->remesh_interval <= static_cast<uint64_t>(kMaxInterval) && smem <= 64 * 1024;
         int cluster = small ? (t->dtype == AMR_F64 ? cycle_cluster_size<double>(smem)
                                                    : cycle_cluster_size<float>(smem))
@@ -744,8 +1409,8 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
                 A.up[a]  = up[a];
             }
             A.cfl         = p->cfl;
-            A.remaining   = p->remaining_time - sum_dt;
-            A.steps_total = total - done;
+            A.remaining   = p->remaining_time - tot.sum_dt;
+            A.steps_total = total - tot.done;
             A.interval    = static_cast<int>(p->remesh_interval);
             A.crit        = p->criterion;
             A.rthr        = p->refine_threshold;
@@ -754,6 +1419,18 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             A.cthr_sq     = sq_threshold(p->coarsen_threshold, false);
             A.min_level   = p->min_level;
             A.max_level   = p->max_level;
+            if (t->bounds_set) { // one tree: its own (min, max) pair
+                int32_t b[2];
+                AMR_CUDA(cudaMemcpy(b, t->bounds, sizeof b, cudaMemcpyDeviceToHost));
+                A.min_level = b[0];
+                A.max_level = b[1];
+            }
+            if (inst_params) {
+                for (int a = 0; a < 3; ++a) {
+                    A.vel[a] = t->vel_inst_host[a];
+                    A.up[a]  = a < g.rank ? (A.vel[a] > 0.0 ? -1 : (A.vel[a] < 0.0 ? 1 : 0)) : 0;
+                }
+            }
             A.P0          = static_cast<int>(t->size);
             A.tb0         = t->tb;
             A.max_level0  = t->max_level_host;
@@ -784,41 +1461,57 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             if (cs.cur) std::swap(t->cur, t->nxt);
             t->max_level_host = cs.max_level;
             t->ghosts_valid   = false;
-            done += static_cast<long long>(cs.executed);
-            sum_dt += cs.sum_dt;
-            executed += cs.executed;
-            cells += cs.cell_updates;
-            remeshes += cs.remeshes;
-            intervals += cs.intervals;
-            persistent += cs.intervals;
-            leaves_sum += cs.leaves_sum;
+            tot.done += static_cast<long long>(cs.executed);
+            tot.sum_dt += cs.sum_dt;
+            tot.executed += cs.executed;
+            tot.cells += cs.cell_updates;
+            tot.remeshes += cs.remeshes;
+            tot.intervals += cs.intervals;
+            tot.persistent += cs.intervals;
+            tot.leaves_sum += cs.leaves_sum;
             if (cs.intervals) {
-                lmin = std::min<uint64_t>(lmin, static_cast<uint64_t>(cs.leaves_min));
-                lmax = std::max<uint64_t>(lmax, static_cast<uint64_t>(cs.leaves_max));
+                tot.lmin = std::min<uint64_t>(tot.lmin, static_cast<uint64_t>(cs.leaves_min));
+                tot.lmax = std::max<uint64_t>(tot.lmax, static_cast<uint64_t>(cs.leaves_max));
             }
             if (cs.error) return fail(static_cast<amr_status>(cs.error), "persistent re-mesh failed");
             if (!cs.stopped) break;
             continue;
         }
-        // one interval with per-launch kernels
-        const long long k = (p->remesh_interval > 0 && static_cast<long long>(p->remesh_interval) < total - done)
+        const bool graph = !(p->options & AMR_RUN_NO_GRAPH) && p->remesh_interval >= 1 &&
+                           p->remesh_interval <= t->coef_steps &&
+                           no_clamp(t, p, inst_params, total - tot.done, tot.sum_dt);
+        if (graph) {
+            // a single tree that shrinks below the cluster kernel's limit goes
+            // back to it after a short chunk
+            const long long chunk = (t->ninst == 1 && !(p->options & AMR_RUN_PER_LAUNCH)) ? 16 : LLONG_MAX;
+            amr_status      st    = run_graph_chunk(t, p, inst_params, chunk, tot);
+            if (st != AMR_OK) return st;
+            continue;
+        }
+        // one interval with host-driven launches
+        const long long k = (p->remesh_interval > 0 && static_cast<long long>(p->remesh_interval) < total - tot.done)
                                 ? static_cast<long long>(p->remesh_interval)
-                                : total - done;
+                                : total - tot.done;
         const size_t P = t->size;
-        amr_status   st = amr_tree_advance(t, static_cast<size_t>(k), p->velocity, p->cfl, p->remaining_time - sum_dt);
+        // the first batch of the run starts the per-instance totals; later
+        // ones fold into them (one tree: remaining time from the host sum, as
+        // the reference's loop passes it; a forest: each instance's own)
+        const int  mode = tot.intervals == 0 ? BATCH_RESET : (t->ninst == 1 ? BATCH_NEXT_REM : BATCH_NEXT);
+        amr_status st   = advance_impl(t, static_cast<size_t>(k), inst_params ? nullptr : p->velocity, p->cfl,
+                                       p->remaining_time - tot.sum_dt, mode);
         if (st != AMR_OK) return st;
         double acc = 0.0;
         size_t ex  = 0;
         st         = amr_tree_finish_advance(t, &acc, &ex);
         if (st != AMR_OK) return st;
-        done += static_cast<long long>(ex);
-        sum_dt += acc;
-        executed += ex;
-        cells += static_cast<uint64_t>(ex) * P * static_cast<uint64_t>(g.cells);
-        leaves_sum += P;
-        lmin = std::min<uint64_t>(lmin, P);
-        lmax = std::max<uint64_t>(lmax, P);
-        ++intervals;
+        tot.done += static_cast<long long>(ex);
+        tot.sum_dt += acc;
+        tot.executed += ex;
+        tot.cells += static_cast<uint64_t>(ex) * P * static_cast<uint64_t>(g.cells);
+        tot.leaves_sum += P;
+        tot.lmin = std::min<uint64_t>(tot.lmin, P);
+        tot.lmax = std::max<uint64_t>(tot.lmax, P);
+        ++tot.intervals;
         if (p->criterion != 0) {
             st = p->criterion == 1 ? amr_tree_flags_gradient(t, p->refine_threshold, p->coarsen_threshold,
                                                              p->min_level, p->max_level)
@@ -828,20 +1521,100 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             int changed = 0;
             st          = amr_tree_remesh(t, &changed);
             if (st != AMR_OK) return st;
-            ++remeshes;
+            ++tot.remeshes;
         }
         if (ex == 0) break;
     }
     if (out) {
-        out->executed_steps       = executed;
-        out->sum_dt               = sum_dt;
-        out->cell_updates         = cells;
-        out->remeshes             = remeshes;
-        out->intervals            = intervals;
-        out->leaves_min           = intervals ? lmin : t->size;
-        out->leaves_max           = intervals ? lmax : t->size;
-        out->leaves_mean          = intervals ? static_cast<double>(leaves_sum) / static_cast<double>(intervals) : 0.0;
-        out->persistent_intervals = persistent;
+        out->executed_steps       = tot.executed;
+        out->sum_dt               = tot.sum_dt;
+        out->cell_updates         = tot.cells;
+        out->remeshes             = tot.remeshes;
+        out->intervals            = tot.intervals;
+        out->leaves_min           = tot.intervals ? tot.lmin : t->size;
+        out->leaves_max           = tot.intervals ? tot.lmax : t->size;
+        out->leaves_mean          = tot.intervals ? static_cast<double>(tot.leaves_sum) / static_cast<double>(tot.intervals)
+                                                  : 0.0;
+        out->persistent_intervals = tot.persistent;
+        out->graph_intervals      = tot.graphs;
+    }
+    return AMR_OK;
+}
+
+amr_status amr_tree_set_instance_params(amr_tree* t, const double* velocity, const int32_t* level_bounds,
+                                        size_t instances)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (instances != static_cast<size_t>(t->ninst)) return fail(AMR_ERR_INVALID, "instance count mismatch");
+    if (velocity) {
+        t->vel_inst_host.assign(velocity, velocity + 3 * instances);
+        for (size_t i = 0; i < instances; ++i)
+            for (int a = t->g.rank; a < 3; ++a) t->vel_inst_host[3 * i + a] = 0.0;
+        AMR_CUDA(cudaMemcpyAsync(t->vel_inst, t->vel_inst_host.data(), 3 * instances * sizeof(double),
+                                 cudaMemcpyHostToDevice, t->stream));
+        t->vel_inst_set = true;
+    }
+    if (level_bounds) {
+        for (size_t i = 0; i < instances; ++i)
+            if (level_bounds[2 * i] < 0 || level_bounds[2 * i + 1] < level_bounds[2 * i])
+                return fail(AMR_ERR_INVALID, "bad level bounds");
+        AMR_CUDA(cudaMemcpyAsync(t->bounds, level_bounds, 2 * instances * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                 t->stream));
+        t->bounds_set = true;
+    }
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    return AMR_OK;
+}
+
+amr_status amr_tree_refine_to_levels(amr_tree* t, const int32_t* target_levels, size_t instances)
+{
+    if (!t || !target_levels) return fail(AMR_ERR_INVALID, "null argument");
+    if (instances != static_cast<size_t>(t->ninst)) return fail(AMR_ERR_INVALID, "instance count mismatch");
+    int top = 0;
+    for (size_t i = 0; i < instances; ++i) {
+        if (target_levels[i] < 0 || target_levels[i] > t->g.depth) return fail(AMR_ERR_INVALID, "bad target level");
+        top = std::max(top, static_cast<int>(target_levels[i]));
+    }
+    AMR_CUDA(cudaMemcpyAsync(t->target, target_levels, instances * sizeof(int32_t), cudaMemcpyHostToDevice, t->stream));
+    for (int l = 0; l < top; ++l) {
+        const int P = static_cast<int>(t->size);
+        k_flags_to_level<<<grid_for(P, 256), 256, 0, t->stream>>>(t->keys[t->tb], P, t->g, t->target, t->flags);
+        AMR_LAUNCHED("k_flags_to_level");
+        int        changed = 0;
+        amr_status st      = amr_tree_remesh(t, &changed);
+        if (st != AMR_OK) return st;
+        if (!changed) break;
+    }
+    return AMR_OK;
+}
+
+amr_status amr_tree_instance_offsets(amr_tree* t, uint64_t* offsets, size_t instances_plus_one)
+{
+    if (!t || !offsets) return fail(AMR_ERR_INVALID, "null argument");
+    const int K = t->ninst;
+    if (instances_plus_one != static_cast<size_t>(K) + 1) return fail(AMR_ERR_INVALID, "instance count mismatch");
+    k_instance_offsets<<<grid_for(K + 1, 256), 256, 0, t->stream>>>(t->keys[t->tb], static_cast<int>(t->size), t->g, K,
+                                                                     t->offs);
+    AMR_LAUNCHED("k_instance_offsets");
+    AMR_CUDA(cudaMemcpyAsync(offsets, t->offs, (K + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    return AMR_OK;
+}
+
+amr_status amr_tree_instance_time(amr_tree* t, double* sum_dt, uint32_t* executed_steps, size_t instances)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (instances != static_cast<size_t>(t->ninst)) return fail(AMR_ERR_INVALID, "instance count mismatch");
+    std::vector<double>   acc(instances), tot(instances);
+    std::vector<uint32_t> cnt(instances), ctot(instances);
+    AMR_CUDA(cudaMemcpyAsync(acc.data(), t->dt_acc, instances * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(tot.data(), t->dt_tot, instances * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(cnt.data(), t->dt_cnt, instances * sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(ctot.data(), t->dt_ctot, instances * sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    for (size_t i = 0; i < instances; ++i) {
+        if (sum_dt) sum_dt[i] = t->batch_open ? tot[i] + acc[i] : 0.0;
+        if (executed_steps) executed_steps[i] = t->batch_open ? ctot[i] + cnt[i] : 0u;
     }
     return AMR_OK;
 }

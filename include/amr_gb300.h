@@ -138,13 +138,21 @@ typedef struct amr_tree amr_tree;
 
 typedef struct amr_tree_desc {
     amr_patch_geometry geom;
-    size_t             capacity;  /* maximum number of leaves */
+    size_t             capacity;  /* maximum number of leaves (all instances) */
     int32_t            dtype;     /* amr_dtype of the cell state */
     void*              stream;    /* cudaStream_t for every call on this tree */
+    int32_t            instances; /* independent trees held together (a forest);
+                                     0 or 1 = one tree */
 } amr_tree_desc;
 
 /* ndtree(capacity) (include/ndtree/ndtree.hpp:320-425): one root leaf with
- * periodic self-neighbours. */
+ * periodic self-neighbours.  With instances = K > 1 the object holds K
+ * independent trees (a forest): instance i starts as its own root, every
+ * Morton id carries i above its interleaved coordinate bits
+ * (id = i << (6 + rank*depth) | morton id within the instance), so the leaves
+ * of all instances form one Morton-ordered array, instance by instance, and
+ * each instance has its own periodic domain, neighbour tables, 2:1 balance,
+ * CFL step and level bounds.  Every call below acts on all instances. */
 amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out);
 amr_status amr_tree_destroy(amr_tree* t);
 /* ndtree::size() */
@@ -207,9 +215,13 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
  * until `steps` steps ran or the time is used up.  criterion: 0 none (no
  * re-mesh), 1 gradient (amr_tree_flags_gradient), 2 max value
  * (amr_tree_flags_max).  While the tree has few leaves the whole loop runs as
- * one persistent kernel on a thread-block cluster with no host round trip;
- * larger trees run interval by interval with per-launch kernels.  Results
- * are identical either way. */
+ * one persistent kernel on a thread-block cluster with no host round trip.
+ * Larger trees and forests run interval by interval: the interval (step
+ * coefficients, the update steps, flags, 2:1 balance, re-mesh, neighbour
+ * rebuild) is one CUDA graph whose kernels read the leaf count and the
+ * buffer selection from device memory, captured once and replayed with no
+ * host round trip between intervals (AMR_RUN_NO_GRAPH: host-driven launches
+ * with a readback per re-mesh).  Results are identical on every path. */
 typedef struct amr_cycle_params {
     uint64_t steps;
     uint64_t remesh_interval;
@@ -220,12 +232,18 @@ typedef struct amr_cycle_params {
     int32_t  min_level;
     int32_t  max_level;
     int32_t  options;        /* AMR_RUN_PER_LAUNCH: never use the cluster kernel;
+                                AMR_RUN_INSTANCE_PARAMS: per-instance velocities
+                                and bounds (amr_tree_set_instance_params);
+                                AMR_RUN_NO_GRAPH: host-driven intervals instead
+                                of the captured interval graph;
                                 bits 8-15: cluster size (CTAs) to use, 0 = largest that fits */
     double   refine_threshold;
     double   coarsen_threshold;
 } amr_cycle_params;
 
 #define AMR_RUN_PER_LAUNCH 1
+#define AMR_RUN_INSTANCE_PARAMS 2
+#define AMR_RUN_NO_GRAPH 4
 
 typedef struct amr_cycle_stats {
     uint64_t executed_steps;   /* steps with dt > 0 */
@@ -237,9 +255,30 @@ typedef struct amr_cycle_stats {
     uint64_t leaves_max;
     double   leaves_mean;
     uint64_t persistent_intervals; /* intervals run inside the cluster kernel */
+    uint64_t graph_intervals;      /* intervals run as graph replays */
 } amr_cycle_stats;
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_stats* stats);
+
+/* ----------------------------------------------------------- forests
+ * Per-instance parameters (instances > 1): velocity (3 per instance, Morton
+ * axis order x, y, z) and level bounds (min_level, max_level per instance).
+ * Either array may be NULL to leave that part unchanged; level_bounds NULL
+ * also keeps (or, on the first call, leaves off) the per-instance bounds.
+ * amr_tree_advance with velocity3 == NULL and amr_tree_run with
+ * AMR_RUN_INSTANCE_PARAMS use these velocities; the flag calls and
+ * amr_tree_run use these bounds in place of min_level/max_level once set. */
+amr_status amr_tree_set_instance_params(amr_tree* t, const double* velocity, const int32_t* level_bounds,
+                                        size_t instances);
+/* Refine every leaf of instance i until it reaches target_levels[i]
+ * (one reconstruct_tree per level, with 2:1 balance). */
+amr_status amr_tree_refine_to_levels(amr_tree* t, const int32_t* target_levels, size_t instances);
+/* offsets[i] = index of the first leaf of instance i, offsets[instances] =
+ * size(); instances + 1 entries. */
+amr_status amr_tree_instance_offsets(amr_tree* t, uint64_t* offsets, size_t instances_plus_one);
+/* Simulated time and executed steps per instance since the last
+ * amr_tree_advance/amr_tree_run started. */
+amr_status amr_tree_instance_time(amr_tree* t, double* sum_dt, uint32_t* executed_steps, size_t instances);
 
 /* Per-launch timing of the fused update kernel with CUDA events on the tree's
  * stream (the counterpart of the reference's profiler ranges,
