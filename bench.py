@@ -1,15 +1,25 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 AMR hot path: cell-updates/s.
 
-Workload (one bench step = one complete run of it): 2D linear advection with
-active AMR, plain FP64: 16x16-cell patches + 1 ghost layer, Morton depth 7 with
-refinement capped at level 5 by the criterion, gradient criterion
-max|grad u|*h > 0.05 refine / < 0.01 coarsen (min level 1), re-mesh every 10
-steps with 2:1 balance, two seeded Gaussian bumps (sigma 0.02-0.06, amplitude
-0.5-2) plus 1e-3 seeded noise, velocity (1.0, 0.5), periodic, CFL 0.4, 2000
-steps.  cell-updates = sum over re-mesh intervals of executed steps x leaves
-x 16^2, re-mesh time included (the reference's definition,
+Headline workload (one bench step = one complete run of it): the batched
+form, FP32.  512 independent 2D linear-advection AMR instances held in one
+forest (one tree object; each instance is its own periodic unit square):
+16x16-cell patches + 1 ghost layer, seeded depth caps 2-6 (each instance is
+refined to its cap and held there, min = max level, so leaf counts are
+16-4096 and ~560k patches in total), seeded velocities in [-1,1]^2, two
+seeded Gaussian bumps per instance (sigma 0.02-0.06, amplitude 0.5-2), CFL
+0.4, gradient criterion 0.05 / 0.01 and re-mesh every 10 steps, 1000 steps.
+Each re-mesh interval is one CUDA graph replay (step coefficients, 10 update
+steps, halo fill, flags, 2:1 closure, scan, emit, remap, neighbour rebuild);
+the update kernel's launch shape is picked by the autotuner on first use.
+cell-updates = sum over intervals of steps x leaves x 16^2, re-mesh time
+included (the reference's definition,
 benchmark/bench_fvm_solver_integration_active_amr.b.cpp:244-245, 258).
+
+The same forest is run in FP64 (the plain drop-in arithmetic) for the
+FP32/FP64 throughput ratio and the relative L2 error of the FP32 state.  The
+plain FP64 drop-in on the single-tree active-AMR workload (2000 steps, max
+level 5) is reported beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -39,6 +49,15 @@ sys.path.insert(0, str(REPO))
 METRIC = "cell-updates/s FP32-batched vs FP64-plain at stated L2 err; adjoint/forward cost"
 UNIT = "cell-updates/s"
 
+BATCHED = dict(
+    instances=512, n=16, halo=1, depth=6, cap_lo=2, cap_hi=6, steps=1000, remesh=10, cfl=0.4, rthr=0.05, cthr=0.01,
+    seed=3, bumps=2, sigma=(0.02, 0.06), amp=(0.5, 2.0),
+)
+BATCHED_NAME = ("batched: 512 independent 2D advection AMR instances in one forest, 16x16 patches + 1 ghost, "
+                "seeded depth caps 2-6 (refined to the cap and held: min = max level), seeded velocities in "
+                "[-1,1]^2, 2 seeded Gaussian bumps each, grad criterion 0.05/0.01, re-mesh every 10 steps "
+                "(one CUDA graph replay per interval), CFL 0.4, 1000 steps, FP32 state")
+
 WORKLOAD = dict(
     rank=2, n=16, halo=1, depth=7, init_levels=2, steps=2000, remesh=10, velocity=(1.0, 0.5), cfl=0.4,
     rthr=0.05, cthr=0.01, min_level=1, max_level=5, bump_seed=2, noise=1e-3, noise_seed=2,
@@ -53,12 +72,6 @@ def measured_peaks():
         return json.loads((REPO / "MEASURED_PEAKS.json").read_text())
     except Exception:
         return {}
-
-
-def bumps():
-    import amr_gb300 as A
-
-    return A.seeded_bumps(2, 2, WORKLOAD["bump_seed"])
 
 
 # ------------------------------------------------------------------ clocks
@@ -119,6 +132,317 @@ def _events(torch):
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
+# ------------------------------------------------------------ batched form
+def batched_instances():
+    """Seeded per-instance parameters: depth cap, velocity, Gaussian bumps
+    (centre x, centre y, sigma, amplitude per bump)."""
+    B = BATCHED
+    rng = np.random.default_rng(B["seed"])
+    K = B["instances"]
+    caps = rng.integers(B["cap_lo"], B["cap_hi"] + 1, K).astype(np.int32)
+    vel = rng.uniform(-1.0, 1.0, (K, 2))
+    bumps = np.zeros((K, B["bumps"], 4))
+    bumps[..., 0:2] = rng.uniform(0.15, 0.85, (K, B["bumps"], 2))
+    bumps[..., 2] = rng.uniform(*B["sigma"], (K, B["bumps"]))
+    bumps[..., 3] = rng.uniform(*B["amp"], (K, B["bumps"]))
+    return caps, vel, bumps
+
+
+def batched_ic(torch, ids, bumps, dev):
+    """Padded FP64 initial state on the device: per leaf, the sum of its
+    instance's Gaussian bumps at the cell centres (physics_system::cell_coord
+    geometry on the unit square), ghosts zero."""
+    B = BATCHED
+    n, h, depth = B["n"], B["halo"], B["depth"]
+    k = torch.from_numpy(np.asarray(ids, np.uint64).view(np.int64)).to(dev)
+    level = (k & 63).to(torch.float64)
+    m = (k >> 6) & ((1 << (2 * depth)) - 1)
+    inst = k >> (6 + 2 * depth)
+    x = torch.zeros_like(m)
+    y = torch.zeros_like(m)
+    for b in range(depth):
+        x |= ((m >> (2 * b)) & 1) << b
+        y |= ((m >> (2 * b + 1)) & 1) << b
+    maxc = float(1 << depth)
+    cs = (torch.pow(2.0, depth - level) / maxc / n)[:, None, None]
+    i = torch.arange(n, device=dev, dtype=torch.float64)
+    cx = (x.to(torch.float64) / maxc)[:, None, None] + i[None, None, :] * cs + 0.5 * cs
+    cy = (y.to(torch.float64) / maxc)[:, None, None] + i[None, :, None] * cs + 0.5 * cs
+    bp = torch.from_numpy(bumps).to(dev)[inst]  # (P, nb, 4)
+    val = torch.zeros((k.shape[0], n, n), dtype=torch.float64, device=dev)
+    for j in range(bp.shape[1]):
+        c = bp[:, j]
+        r2 = (cx - c[:, 0, None, None]) ** 2 + (cy - c[:, 1, None, None]) ** 2
+        val += c[:, 3, None, None] * torch.exp(-r2 / (2.0 * c[:, 2, None, None] ** 2))
+    out = torch.zeros((k.shape[0], n + 2 * h, n + 2 * h), dtype=torch.float64, device=dev)
+    out[:, h:n + h, h:n + h] = val
+    return out, inst
+
+
+def make_forest(A, dtype, stream, caps, vel):
+    B = BATCHED
+    K = B["instances"]
+    cap = int(np.sum(4 ** caps.astype(np.int64))) + 1024
+    f = A.Tree(2, B["n"], B["halo"], B["depth"], capacity=cap, dtype=dtype, stream=stream.cuda_stream, instances=K)
+    f.refine_to_levels(caps)
+    f.set_instance_params(velocity=vel, level_bounds=np.stack([caps, caps], 1))
+    return f
+
+
+def run_forest(f):
+    B = BATCHED
+    return f.run(B["steps"], B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+
+
+def time_runs(torch, stream, world, k, setup, body, flush, clocks=None):
+    """k timed runs: setup + L2 flush outside, CUDA events around body on the
+    forest's stream.  Returns (ms, launches, stats)."""
+    import amr_gb300 as A
+
+    total_ms, launches, stats = 0.0, 0, []
+    if clocks:
+        clocks.start()
+    for _ in range(k):
+        setup()
+        flush.zero_()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        l0 = A.launch_count()
+        ev0, ev1 = _events(torch)
+        ev0.record(stream)
+        stats.append(body())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        launches += A.launch_count() - l0
+        total_ms += ev0.elapsed_time(ev1)
+    info = clocks.stop() if clocks else None
+    return total_ms, launches, stats, info
+
+
+def batched_arm(args, torch, A, dev, stream, flush, world):
+    B = BATCHED
+    caps, vel, bumps = batched_instances()
+    f32 = make_forest(A, A.F32, stream, caps, vel)
+    ids = f32.ids()
+    P = len(ids)
+    ic64, inst = batched_ic(torch, ids, bumps, dev)
+    ic32 = ic64.to(torch.float32).contiguous()
+    ic32_host = ic32.cpu().pin_memory()
+    out32_host = torch.empty_like(ic32_host).pin_memory()
+
+    def load32():
+        f32.load_state_device(ic32.data_ptr(), P)
+
+    for _ in range(args.warmup):
+        load32()
+        run_forest(f32)
+    ms, launches, stats, clock_info = time_runs(torch, stream, world, args.steps, load32, lambda: run_forest(f32),
+                                                flush, ClockSampler(dev))
+    cells = sum(s["cell_updates"] for s in stats)
+    assert all(s["leaves_min"] == s["leaves_max"] == P for s in stats)
+    fin32 = torch.empty_like(ic32)
+    f32.download_state_device(fin32.data_ptr(), P)
+
+    # end to end: initial state from pinned host memory, final state back
+    def e2e_body():
+        A.check(A.lib().amr_tree_upload_state(f32._h, ic32_host.data_ptr(), P))
+        st = run_forest(f32)
+        A.check(A.lib().amr_tree_download_state(f32._h, out32_host.data_ptr(), P))
+        return st
+
+    e2e_ms, _, e2e_stats, _ = time_runs(torch, stream, world, args.steps, lambda: None, e2e_body, flush)
+    e2e_cells = sum(s["cell_updates"] for s in e2e_stats)
+
+    # the update kernel alone: CUDA events around each launch on the forest's
+    # stream (host-driven steps with the tuned launch shape)
+    load32()
+    f32.set_timing(True)
+    f32.advance(50, None, B["cfl"])
+    f32.finish_advance()
+    k_ms, k_launches, k_cells = f32.get_timing()
+    f32.set_timing(False)
+
+    # FP64 plain arithmetic on the same forest
+    f64 = make_forest(A, A.F64, stream, caps, vel)
+    assert np.array_equal(f64.ids(), ids)
+
+    def load64():
+        f64.load_state_device(ic64.data_ptr(), P)
+
+    load64()
+    run_forest(f64)
+    ms64, _, stats64, _ = time_runs(torch, stream, world, max(1, args.steps), load64, lambda: run_forest(f64), flush)
+    cells64 = sum(s["cell_updates"] for s in stats64)
+    fin64 = torch.empty_like(ic64)
+    f64.download_state_device(fin64.data_ptr(), P)
+    n, h = B["n"], B["halo"]
+    a = fin32[:, h:n + h, h:n + h].to(torch.float64)
+    b = fin64[:, h:n + h, h:n + h]
+    rel = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    K = B["instances"]
+    num = torch.zeros(K, dtype=torch.float64, device=dev).index_add_(0, inst, ((a - b) ** 2).sum((1, 2)))
+    den = torch.zeros(K, dtype=torch.float64, device=dev).index_add_(0, inst, (b ** 2).sum((1, 2)))
+    rel_inst = float(torch.sqrt(num / den).max())
+    ok = np.isfinite(rel) and rel <= 1e-5
+    acc32, _ = f32.instance_time()
+    f32.close()
+    f64.close()
+
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    alg = 8.0 * k_cells  # one FP32 read + one FP32 write per cell update
+    achieved = alg / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    traffic = None
+    prof = REPO / "profiles" / "k_step2d_fp32_forest.json"
+    if prof.exists():
+        try:
+            per_patch = json.loads(prof.read_text()).get("dram_bytes_per_patch")
+            traffic = per_patch * P if per_patch else None
+        except Exception:
+            traffic = None
+    value = cells / (ms * 1e-3)
+    value64 = cells64 / (ms64 * 1e-3)
+    return {
+        "value": value,
+        "ms": ms,
+        "cells": cells,
+        "e2e_ms": e2e_ms,
+        "e2e_cells": e2e_cells,
+        "launches": launches,
+        "clocks": clock_info,
+        "config": {
+            "workload": BATCHED_NAME,
+            "instances": K,
+            "patches": P,
+            "leaves_per_instance": {"min": int(4 ** caps.min()), "max": int(4 ** caps.max())},
+            "cap_histogram": {str(c): int((caps == c).sum()) for c in range(B["cap_lo"], B["cap_hi"] + 1)},
+            "step": "one complete 1000-step run (100 re-mesh intervals, one graph replay each) from the initial state",
+            "l2": "flushed (256 MiB write) before every timed run, outside the timed interval; "
+                  "the state (2 x 0.73 GB) exceeds L2 in any case",
+            "sum_dt_instance0": float(acc32[0]),
+            "driver": f"graph replays per run: {stats[0]['graph_intervals']} of {stats[0]['intervals']} intervals",
+        },
+        "e2e": {"value": e2e_cells / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(ic32_host.numel() * 4),
+                "d2h_bytes_per_step": int(out32_host.numel() * 4)},
+        "roofline": {
+            "bound": "hbm", "kernel": "k_step2d<float,16,1,W,S> (the update kernel of every graph step)",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": (achieved / hbm) if (achieved and hbm) else None,
+            "traffic": traffic,
+            "algorithmic_bytes_per_cell_update": 8,
+            "launches": k_launches, "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured, burst copy)" if hbm else "missing",
+        },
+        "fp64_plain_same_workload": {
+            "value": value64, "unit": UNIT, "ms_per_run": ms64 / max(1, args.steps),
+            "ratio_fp32_batched_over_fp64": value / value64,
+            "note": "the same forest, state and arithmetic in FP64 (the plain drop-in kernels)",
+        },
+        "precision": {
+            "rel_l2_fp32_vs_fp64": rel, "max_instance_rel_l2": rel_inst, "bar": 1e-5, "within_bar": bool(ok),
+            "reference": "FP64 run of the same forest on the GPU (the FP64 path equals the oracle within 1e-12)",
+            "fp64_kept_for": "CFL step, coarse-fine restriction/prolongation means, gradient flags",
+        },
+    }
+
+
+# ----------------------------------------------------- plain FP64 drop-in
+def bumps():
+    import amr_gb300 as A
+
+    return A.seeded_bumps(2, 2, WORKLOAD["bump_seed"])
+
+
+def plain_config2(args, torch, A, dev, stream, flush, world):
+    """The single-tree active-AMR workload in FP64 through the drop-in."""
+    W = WORKLOAD
+    tree = A.Tree(W["rank"], W["n"], W["halo"], W["depth"], capacity=4096, stream=stream.cuda_stream)
+    tree.refine_uniform(W["init_levels"])
+    init = A.gaussian_state(tree.ids(), W["rank"], W["n"], W["halo"], W["depth"], bumps(), W["noise"], W["noise_seed"])
+    P0 = init.shape[0]
+    init_dev = torch.from_numpy(init).to(f"cuda:{dev}")
+    init_host = torch.from_numpy(init).pin_memory()
+    final_host = torch.empty((4096,) + init.shape[1:], dtype=torch.float64).pin_memory()
+    run_args = dict(steps=W["steps"], interval=W["remesh"], velocity=W["velocity"], cfl=W["cfl"], criterion="grad",
+                    rthr=W["rthr"], cthr=W["cthr"], min_level=W["min_level"], max_level=W["max_level"])
+    d2h = [0]
+
+    def setup():
+        tree.reset()
+        tree.refine_uniform(W["init_levels"])
+
+    def body(e2e=False, per_launch=False):
+        if e2e:
+            A.check(A.lib().amr_tree_upload_state(tree._h, init_host.data_ptr(), P0))
+        else:
+            tree.load_state_device(init_dev.data_ptr(), P0)
+        tree.halo_exchange()
+        st = tree.run(per_launch=per_launch, graph=not per_launch, **run_args)
+        if e2e:
+            P = tree.size
+            A.check(A.lib().amr_tree_download_state(tree._h, final_host.data_ptr(), P))
+            d2h[0] += P * tree.flat * 8
+        return st
+
+    for _ in range(args.warmup):
+        setup()
+        body()
+    ms, launches, stats, _ = time_runs(torch, stream, world, args.steps, setup, body, flush)
+    cells = sum(s["cell_updates"] for s in stats)
+    e2e_ms, _, e2e_stats, _ = time_runs(torch, stream, world, args.steps, setup, lambda: body(e2e=True), flush)
+    e2e_cells = sum(s["cell_updates"] for s in e2e_stats)
+    pl_ms, pl_launches, pl_stats, _ = time_runs(torch, stream, world, 1, setup, lambda: body(per_launch=True), flush)
+    pl_cells = sum(s["cell_updates"] for s in pl_stats)
+    tree.set_timing(True)
+    for _ in range(args.steps):
+        setup()
+        flush.zero_()
+        torch.cuda.synchronize()
+        body()
+    k_ms, k_launches, k_cells = tree.get_timing()
+    tree.set_timing(False)
+    tree.close()
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    achieved = 16.0 * k_cells / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    traffic = None
+    prof = REPO / "profiles" / "k_cycle_fp64_config2.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    persistent = all(s["persistent_intervals"] == s["intervals"] for s in stats)
+    leaves = [(s["leaves_min"], s["leaves_max"], s["leaves_mean"]) for s in stats]
+    return {
+        "workload": WORKLOAD_NAME,
+        "dtype": "f64",
+        "value": cells / (ms * 1e-3),
+        "unit": UNIT,
+        "ms_per_run": ms / args.steps,
+        "leaves_min": int(min(l[0] for l in leaves)),
+        "leaves_max": int(max(l[1] for l in leaves)),
+        "leaves_mean": float(np.mean([l[2] for l in leaves])),
+        "remesh_per_run": int(stats[0]["remeshes"]),
+        "sum_dt_per_run": stats[0]["sum_dt"],
+        "driver": "one persistent cluster kernel per run" if persistent else "mixed persistent/graph",
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_cells / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(init.nbytes),
+                "d2h_bytes_per_step": int(d2h[0] / max(1, args.steps))},
+        "roofline": {
+            "bound": "hbm", "kernel": "k_cycle<double> (persistent: fused updates, flags, re-mesh)",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": (achieved / hbm) if (achieved and hbm) else None, "traffic": traffic,
+            "algorithmic_bytes_per_cell_update": 16,
+            "note": "the workload is L2-resident (<= 43 leaves, ~0.1 MB); the figure shows latency, not bandwidth",
+        },
+        "host_driven": {"value": pl_cells / (pl_ms * 1e-3), "unit": UNIT, "gpu_launches": int(pl_launches),
+                        "note": "same runs with host-driven launches and a readback every interval"},
+        "cpu_baseline": None,
+    }
+
+
 def uniform_extra(A, torch, stream, dtype, level=9, steps=40):
     """Kernel-level figure on an HBM-sized input: uniform 2D tree of 4^level
     leaves (16x16 + 1 ghost), fused update only (no re-mesh), per-launch
@@ -141,18 +465,15 @@ def uniform_extra(A, torch, stream, dtype, level=9, steps=40):
     ms = e0.elapsed_time(e1)
     k_ms, k_launches, k_cells = t.get_timing()
     t.close()
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
+    hbm = measured_peaks().get("hbm_gbs")
     achieved = elem * 2 * k_cells / (k_ms * 1e-3) / 1e9
     out = {
         "workload": f"uniform 2D tree, 4^{level} = {4**level} leaves of 16x16 + 1 ghost, {steps} steps, no re-mesh",
         "dtype": "f64" if dtype == A.F64 else "f32",
         "value": ex * 4**level * 256 / (ms * 1e-3),
         "unit": UNIT,
-        "roofline": {"bound": "hbm", "kernel": f"k_step<{'double' if dtype == A.F64 else 'float'}>",
-                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm if hbm else None,
-                     "algorithmic_bytes_per_cell_update": 2 * elem,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if hbm else None, "algorithmic_bytes_per_cell_update": 2 * elem,
                      "avg_launch_us": k_ms * 1e3 / max(1, k_launches)},
     }
     if dtype == A.F64:
@@ -171,88 +492,16 @@ def gpu_arm(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream()
-    W = WORKLOAD
-    tree = A.Tree(W["rank"], W["n"], W["halo"], W["depth"], capacity=4096, stream=stream.cuda_stream)
-    tree.refine_uniform(W["init_levels"])
-    init = A.gaussian_state(tree.ids(), W["rank"], W["n"], W["halo"], W["depth"], bumps(), W["noise"], W["noise_seed"])
-    P0 = init.shape[0]
-    init_dev = torch.from_numpy(init).to(f"cuda:{dev}")
-    init_host = torch.from_numpy(init).pin_memory()
-    final_host = torch.empty((4096,) + init.shape[1:], dtype=torch.float64).pin_memory()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{dev}")
-    run_args = dict(steps=W["steps"], interval=W["remesh"], velocity=W["velocity"], cfl=W["cfl"], criterion="grad",
-                    rthr=W["rthr"], cthr=W["cthr"], min_level=W["min_level"], max_level=W["max_level"])
-
-    def setup():
-        # topology of the initial tree: outside the timed interval, as in the
-        # reference benchmark (its timer starts after initialisation)
-        tree.reset()
-        tree.refine_uniform(W["init_levels"])
-
-    def run(e2e: bool, per_launch=False):
-        if e2e:
-            A.check(A.lib().amr_tree_upload_state(tree._h, init_host.data_ptr(), P0))
-        else:
-            tree.load_state_device(init_dev.data_ptr(), P0)
-        tree.halo_exchange()
-        st = tree.run(per_launch=per_launch, **run_args)
-        d2h = 0
-        if e2e:
-            P = tree.size
-            A.check(A.lib().amr_tree_download_state(tree._h, final_host.data_ptr(), P))
-            d2h = P * tree.flat * 8
-        return st, d2h
-
-    def timed(e2e: bool, k: int, per_launch=False):
-        total_ms, launches, d2h_total, stats = 0.0, 0, 0, []
-        for _ in range(k):
-            setup()
-            flush.zero_()
-            torch.cuda.synchronize()
-            if world > 1:
-                torch.distributed.barrier()
-            l0 = A.launch_count()
-            ev0, ev1 = _events(torch)
-            ev0.record(stream)
-            st, d2h = run(e2e, per_launch)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            launches += A.launch_count() - l0
-            total_ms += ev0.elapsed_time(ev1)
-            d2h_total += d2h
-            stats.append(st)
-        return total_ms, launches, d2h_total, stats
-
-    for _ in range(args.warmup):
-        setup()
-        run(False)
-    clocks = ClockSampler(dev)
-    clocks.start()
-    ms, launches, _, stats = timed(False, args.steps)
-    clock_info = clocks.stop()
-    cells = sum(s["cell_updates"] for s in stats)
-    e2e_ms, _, d2h_total, e2e_stats = timed(True, args.steps)
-    e2e_cells = sum(s["cell_updates"] for s in e2e_stats)
-    pl_ms, pl_launches, _, pl_stats = timed(False, 1, per_launch=True)
-    pl_cells = sum(s["cell_updates"] for s in pl_stats)
-
-    # dominant kernel over a second pass of the same timed runs, CUDA events
-    # around every launch of it on the tree's stream
-    tree.set_timing(True)
-    for _ in range(args.steps):
-        setup()
-        flush.zero_()
-        torch.cuda.synchronize()
-        run(False)
-    k_ms, k_launches, k_cells = tree.get_timing()
-    tree.set_timing(False)
-
+    bt = batched_arm(args, torch, A, dev, stream, flush, world)
     extras = {}
     if not args.no_extras:
-        lv = args.uniform_level
-        extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)
-        extras[f"uniform_fp32_level{lv}"] = uniform_extra(A, torch, stream, A.F32, lv)
-
+        extras["plain_fp64_config2"] = plain_config2(args, torch, A, dev, stream, flush, world)
+        if args.uniform:
+            lv = args.uniform_level
+            extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)
+            extras[f"uniform_fp32_level{lv}"] = uniform_extra(A, torch, stream, A.F32, lv)
+    ms, e2e_ms, cells, e2e_cells = bt["ms"], bt["e2e_ms"], bt["cells"], bt["e2e_cells"]
     if world > 1:
         t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{dev}")
         c = torch.tensor([float(cells), float(e2e_cells)], dtype=torch.float64, device=f"cuda:{dev}")
@@ -262,19 +511,9 @@ def gpu_arm(args, rank, world):
         cells, e2e_cells = c.tolist()
     if rank != 0:
         return None
-    peaks = measured_peaks()
-    hbm = peaks.get("hbm_gbs")
-    alg_bytes = 16.0 * k_cells  # one read + one write of an FP64 cell per update
-    achieved = alg_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
-    traffic = None
-    prof = REPO / "profiles" / "k_cycle_fp64_config2.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
-    persistent = all(s["persistent_intervals"] == s["intervals"] for s in stats)
-    leaves = [(s["leaves_min"], s["leaves_max"], s["leaves_mean"]) for s in stats]
+    bt["e2e"]["value"] = e2e_cells / (e2e_ms * 1e-3)
+    cfg = dict(bt["config"])
+    cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
     line = {
         "metric": METRIC,
         "value": cells / (ms * 1e-3),
@@ -286,72 +525,70 @@ def gpu_arm(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic (seeded Gaussian bumps + seeded noise, shapes of the named config)",
-        "config": {
-            "workload": WORKLOAD_NAME,
-            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-            "l2": "flushed (256 MiB write) before every timed run, outside the timed interval",
-            "step": "one complete 2000-step run (200 re-meshes) from the initial state",
-            "leaves_min": int(min(l[0] for l in leaves)),
-            "leaves_max": int(max(l[1] for l in leaves)),
-            "leaves_mean": float(np.mean([l[2] for l in leaves])),
-            "remesh_per_run": int(stats[0]["remeshes"]),
-            "sum_dt_per_run": stats[0]["sum_dt"],
-            "driver": "one persistent cluster kernel per run" if persistent else "mixed persistent/per-launch",
-        },
-        "e2e": {
-            "value": e2e_cells / (e2e_ms * 1e-3),
-            "unit": UNIT,
-            "h2d_bytes_per_step": int(init.nbytes),
-            "d2h_bytes_per_step": int(d2h_total / max(1, args.steps)),
-        },
-        "roofline": {
-            "bound": "hbm",
-            "kernel": "k_cycle<double> (persistent: fused updates, flags, re-mesh)" if persistent else "k_step<double>",
-            "achieved": achieved,
-            "peak": hbm,
-            "unit": "GB/s",
-            "frac": (achieved / hbm) if (achieved and hbm) else None,
-            "traffic": traffic,
-            "algorithmic_bytes_per_cell_update": 16,
-            "launches": k_launches,
-            "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
-            "note": "the workload is L2-resident (<= 43 leaves, ~0.1 MB); the figure shows latency, not bandwidth",
-        },
-        "per_launch_driver": {"value": pl_cells / (pl_ms * 1e-3), "unit": UNIT, "gpu_launches": int(pl_launches),
-                              "note": "same runs with per-launch kernels and host round trips each interval"},
-        "clocks": clock_info,
-        "gpu_launches": int(launches),
+        "dtype": "f32",
+        "data": "synthetic (seeded per-instance caps, velocities and Gaussian bumps; shapes of the named config)",
+        "config": cfg,
+        "e2e": bt["e2e"],
+        "roofline": bt["roofline"],
+        "fp64_plain_same_workload": bt["fp64_plain_same_workload"],
+        "precision": bt["precision"],
+        "clocks": bt["clocks"],
+        "gpu_launches": int(bt["launches"]),
     }
     line.update(extras)
     return line
 
 
 # ------------------------------------------------------------------ CPU arms
-def cpu_run(threads: int, steps: int):
-    """The oracle (C restatement of the reference) on the host cores: the same
-    workload, truncated to `steps` time steps."""
+def cpu_batched(threads: int, instances: int, steps: int):
+    """The oracle (C restatement of the reference) on the host cores: the
+    first `instances` instances of the batched workload, each a separate
+    tree, truncated to `steps` steps."""
     from oracle import oracle as O
 
     O.set_threads(threads)
+    B = BATCHED
+    caps, vel, bmp = batched_instances()
+    cells, secs = 0, 0.0
+    for i in range(instances):
+        t0 = time.perf_counter()
+        _, _, _, c, _ = O.run_scenario(
+            2, B["n"], B["halo"], B["depth"], init_levels=int(caps[i]), steps=steps, remesh=B["remesh"],
+            velocity=tuple(vel[i]), cfl=B["cfl"], bumps=[float(v) for v in bmp[i].ravel()], crit="grad",
+            rthr=B["rthr"], cthr=B["cthr"], min_level=int(caps[i]), max_level=int(caps[i]),
+            capacity=int(4 ** caps[i]) + 16)
+        secs += time.perf_counter() - t0
+        cells += c
+    return cells, secs, caps[:instances]
+
+
+CPU_SAMPLE = dict(instances=32, steps=100)
+
+
+def cpu_baseline():
+    threads = os.cpu_count() or 1
+    cells, secs, caps = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"])
+    return {"value": cells / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"instances 0-{CPU_SAMPLE['instances'] - 1} of the batched workload ({int(np.sum(4 ** caps))} "
+                      f"patches), first {CPU_SAMPLE['steps']} steps each, FP64, OpenMP over patches like "
+                      f"EXECUTION=PAR"}
+
+
+def cpu_plain(steps=600):
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
     W = WORKLOAD
     t0 = time.perf_counter()
-    _, sum_dt, done, cells, _ = O.run_scenario(
+    _, _, _, cells, _ = O.run_scenario(
         W["rank"], W["n"], W["halo"], W["depth"], init_levels=W["init_levels"], steps=steps, remesh=W["remesh"],
         velocity=W["velocity"], cfl=W["cfl"], bumps=bumps(), noise=W["noise"], noise_seed=W["noise_seed"],
         crit="grad", rthr=W["rthr"], cthr=W["cthr"], min_level=W["min_level"], max_level=W["max_level"],
         capacity=4096)
-    return cells, time.perf_counter() - t0
-
-
-def cpu_baseline(steps=600):
-    threads = os.cpu_count() or 1
-    cells, secs = cpu_run(threads, steps)
+    secs = time.perf_counter() - t0
     return {"value": cells / secs, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {steps} of the 2000 steps ({steps // WORKLOAD['remesh']} re-meshes), "
-                      f"OpenMP over patches like EXECUTION=PAR"}
+            "sample": f"first {steps} of the 2000 steps, OpenMP over patches like EXECUTION=PAR"}
 
 
 def reference_arm(args, rank, world):
@@ -361,15 +598,18 @@ def reference_arm(args, rank, world):
 
     O.build()
     threads = os.cpu_count() or 1
-    steps = WORKLOAD["steps"]
-    for _ in range(args.warmup):
-        cpu_run(threads, 200)
-    total_cells, total_s = 0, 0.0
+    cpu_batched(threads, 4, 20)  # warm-up: page in, thread pool
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_batched(threads, 4, 20)
+    total_cells, total_s, caps = 0, 0.0, None
     for _ in range(args.steps):
-        c, s = cpu_run(threads, steps)
+        c, s, caps = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"])
         total_cells += c
         total_s += s
     value = total_cells / total_s
+    sample = (f"instances 0-{CPU_SAMPLE['instances'] - 1} of the batched workload ({int(np.sum(4 ** caps))} patches), "
+              f"first {CPU_SAMPLE['steps']} steps each, FP64; the C restatement of the reference "
+              f"(the reference's own build is x86-only here), OpenMP over patches")
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -383,11 +623,9 @@ def reference_arm(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded Gaussian bumps + seeded noise, shapes of the named config)",
-        "config": {"workload": WORKLOAD_NAME},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "full 2000-step run per step; the C restatement of the reference "
-                                   "(the reference's own build is x86-only here), OpenMP over patches"},
+        "data": "synthetic (seeded per-instance caps, velocities and Gaussian bumps; shapes of the named config)",
+        "config": {"workload": BATCHED_NAME},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -400,7 +638,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--extras-only", action="store_true", help="only the uniform kernel-level workloads")
+    ap.add_argument("--uniform", action="store_true", help="add the uniform kernel-level workloads")
     ap.add_argument("--uniform-level", type=int, default=9)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -415,20 +653,12 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
-    if args.extras_only:
-        import torch
-
-        import amr_gb300 as A
-
-        stream = torch.cuda.Stream()
-        out = {f"uniform_fp64_level{args.uniform_level}": uniform_extra(A, torch, stream, A.F64, args.uniform_level),
-               f"uniform_fp32_level{args.uniform_level}": uniform_extra(A, torch, stream, A.F32, args.uniform_level)}
-        print(json.dumps(out), flush=True)
-        return
     line = gpu_arm(args, rank, world)
     if line is not None:
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
+            if "plain_fp64_config2" in line:
+                line["plain_fp64_config2"]["cpu_baseline"] = cpu_plain()
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch

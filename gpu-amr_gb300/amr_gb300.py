@@ -89,6 +89,7 @@ def lib():
         L.amr_tree_upload_state.argtypes = [vp, vp, sz]
         L.amr_tree_download_state.argtypes = [vp, vp, sz]
         L.amr_tree_load_state_device.argtypes = [vp, vp, sz]
+        L.amr_tree_download_state_device.argtypes = [vp, vp, sz]
         L.amr_tree_reset.argtypes = [vp]
         L.amr_tree_device_state.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
         L.amr_tree_get_ids.argtypes = [vp, vp, sz]
@@ -200,6 +201,9 @@ class Tree:
 
     def load_state_device(self, ptr, num_patches):
         check(lib().amr_tree_load_state_device(self._h, C.c_void_p(ptr), num_patches))
+
+    def download_state_device(self, ptr, num_patches):
+        check(lib().amr_tree_download_state_device(self._h, C.c_void_p(ptr), num_patches))
 
     def reset(self):
         check(lib().amr_tree_reset(self._h))

@@ -58,7 +58,7 @@ struct CycleArgs {
     int            interval;
     int            crit;
     double         rthr, cthr;
-    double         rthr_sq, cthr_sq; // squared-norm thresholds of the gradient rule
+    GradRule       rule;             // squared-norm thresholds of the gradient rule
     int            min_level, max_level;
     int            P0, tb0, max_level0;
     size_t         cap;
@@ -99,7 +99,7 @@ __device__ inline double patch_max_on_the_fly(const T* buf, const amr_halo_meta*
         }
         G[L]                  = pos ? g.n + g.h + f : f;
         const amr_halo_meta& mm = meta[static_cast<size_t>(p) * g.ndir + d];
-        m = fmax(m, ghost_value<T>(buf, g.flat, mm, G, L, pos, g, u));
+        m = fmax(m, static_cast<double>(static_cast<T>(ghost_value<T>(buf, g.flat, mm, G, L, pos, g, u))));
     }
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     return m;
@@ -187,11 +187,12 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
             int8_t f;
             if (A.crit == 1) {
                 int any = 0, all = 1;
-                for (int c = lane; c < g.cells; c += 32) {
-                    const double s2 = gradient_sq_cell<T, true>(st, mt, g, p, c);
-                    if (s2 >= A.rthr_sq) any = 1;
-                    if (!(s2 < A.cthr_sq)) all = 0;
-                }
+                if (g.rank == 2)
+                    for (int c = lane; c < g.cells; c += 32)
+                        gradient_rule_cell<T, true, 2>(st, mt, g, A.rule, p, c, any, all);
+                else
+                    for (int c = lane; c < g.cells; c += 32)
+                        gradient_rule_cell<T, true, 3>(st, mt, g, A.rule, p, c, any, all);
                 any = __any_sync(0xffffffffu, any);
                 all = __all_sync(0xffffffffu, all);
                 f   = gradient_decision(any, all, lv[p], A.min_level, A.max_level);

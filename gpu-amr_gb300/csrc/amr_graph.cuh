@@ -67,8 +67,8 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int p
     const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.levels[tb],
-                            B.meta[tb], P, g, coef, upx0, upy0, &ctl->err, B.keys[tb], B.vel, tiles, bars, p, nwarp);
+    step2d_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P, g,
+                            coef, upx0, upy0, &ctl->err, B.keys[tb], B.vel, tiles, bars, p, nwarp);
 }
 
 // Any geometry: ppb patches per block per round, grid-stride over rounds.
@@ -88,11 +88,9 @@ k_run_step(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int par
         for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
             const int p = p0 + t / cells;
             if (p >= P) break;
-            int inst = 0;
-            if (B.vel) {
-                inst = instance_of(g, B.keys[tb], p);
+            const int inst = instance_of(g, B.keys[tb], p);
+            if (B.vel)
                 for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(B.vel[3 * inst + a]) : 0;
-            }
             step_cell<T, true>(in, out, B.meta[tb], g, coef[inst * nl + B.levels[tb][p]], up, p, t - (p - p0) * cells);
         }
     }
@@ -113,11 +111,39 @@ __global__ void __launch_bounds__(256) k_run_halo(RunBufs B, RunCtl* ctl, Geo g,
         halo_cell<T>(buf, meta, g, t);
 }
 
-// One block per patch, grid-stride; crit 1 = gradient, 2 = max value (the
-// decisions of k_flags_gradient / k_flags_max over the exchanged ghosts).
+// Gradient flags, one warp per patch, ghosts from the neighbours on the fly
+// (the values a halo exchange would store), so no halo pass runs.
+template <typename T, int R>
+__global__ void __launch_bounds__(256)
+k_run_flags_grad(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int max_level, int sp)
+{
+    if (ctl->err) return;
+    const int            P    = ctl->P, tb = ctl->tb;
+    const T*             buf  = static_cast<const T*>(B.state[ctl->sb ^ sp]);
+    const amr_halo_meta* meta = B.meta[tb];
+    const int            lane = threadIdx.x & 31;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < P; p += (gridDim.x * blockDim.x) >> 5) {
+        int any = 0, all = 1;
+        for (int c = lane; c < g.cells; c += 32) gradient_rule_cell<T, true, R>(buf, meta, g, rule, p, c, any, all);
+        any = __any_sync(0xffffffffu, any);
+        all = __all_sync(0xffffffffu, all);
+        if (lane == 0) {
+            int lo = min_level, hi = max_level;
+            if (B.bounds) {
+                const int inst = instance_of(g, B.keys[tb], p);
+                lo             = B.bounds[2 * inst];
+                hi             = B.bounds[2 * inst + 1];
+            }
+            B.flags[p] = gradient_decision(any, all, B.levels[tb][p], lo, hi);
+        }
+    }
+}
+
+// Max-value flags (k_flags_max's rule over the exchanged ghosts), one block
+// per patch, grid-stride.
 template <typename T>
 __global__ void __launch_bounds__(128)
-k_run_flags(RunBufs B, RunCtl* ctl, Geo g, int crit, double rthr, double cthr, int min_level, int max_level, int sp)
+k_run_flags_max(RunBufs B, RunCtl* ctl, Geo g, double rthr, double cthr, int min_level, int max_level, int sp)
 {
     if (ctl->err) return;
     const int P = ctl->P, tb = ctl->tb;
@@ -130,31 +156,18 @@ k_run_flags(RunBufs B, RunCtl* ctl, Geo g, int crit, double rthr, double cthr, i
             lo             = B.bounds[2 * inst];
             hi             = B.bounds[2 * inst + 1];
         }
-        const int level = B.levels[tb][p];
-        if (crit == 1) {
-            int any = 0, all = 1;
-            for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
-                const double v = gradient_cell<T, false>(buf, nullptr, g, p, c);
-                if (v > rthr) any = 1;
-                if (!(v < cthr)) all = 0;
-            }
-            any = __syncthreads_or(any);
-            all = __syncthreads_and(all);
-            if (threadIdx.x == 0) B.flags[p] = gradient_decision(any, all, level, lo, hi);
-        } else {
-            const T* u = buf + static_cast<size_t>(p) * g.flat;
-            double   m = 0.0;
-            for (int c = threadIdx.x; c < g.flat; c += blockDim.x)
-                if (face_or_interior(g, c)) m = fmax(m, static_cast<double>(u[c]));
-            red[threadIdx.x] = m;
-            __syncthreads();
-            for (int w = 64; w > 0; w >>= 1) {
-                if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) B.flags[p] = max_decision(red[0], level, rthr, cthr, lo, hi);
+        const T* u = buf + static_cast<size_t>(p) * g.flat;
+        double   m = 0.0;
+        for (int c = threadIdx.x; c < g.flat; c += blockDim.x)
+            if (face_or_interior(g, c)) m = fmax(m, static_cast<double>(u[c]));
+        red[threadIdx.x] = m;
+        __syncthreads();
+        for (int w = 64; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
             __syncthreads();
         }
+        if (threadIdx.x == 0) B.flags[p] = max_decision(red[0], B.levels[tb][p], rthr, cthr, lo, hi);
+        __syncthreads();
     }
 }
 

@@ -89,7 +89,9 @@ __device__ inline void step_cell(const T* in, T* out, const amr_halo_meta* meta,
     const size_t base = static_cast<size_t>(p) * g.flat;
     const int    li   = padded_index(g, idx);
     const T      u    = in[base + li];
-    T            acc  = static_cast<T>(cf.c0) * u;
+    // FP64: c0 u + sum c_a u_up (the reference's flux term for term); FP32:
+    // u + sum c_a (u_up - u), which keeps a constant state exactly
+    T            acc  = sizeof(T) == 4 ? u : static_cast<T>(cf.c0) * u;
     for (int a = 0; a < g.rank; ++a) {
         const int dirn = up[a];
         if (dirn == 0) continue;
@@ -105,7 +107,7 @@ __device__ inline void step_cell(const T* in, T* out, const amr_halo_meta* meta,
             val = static_cast<T>(
                 ghost_value<T>(in, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos, g, in + base));
         }
-        acc = fma(static_cast<T>(cf.c[a]), val, acc);
+        acc = fma(static_cast<T>(cf.c[a]), sizeof(T) == 4 ? static_cast<T>(val - u) : val, acc);
     }
     out[base + li] = acc;
 }
@@ -139,11 +141,9 @@ k_step(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict_
     for (int t = threadIdx.x; t < ppb * cells; t += blockDim.x) {
         const int p = p0 + t / cells;
         if (p >= P) break;
-        int inst = 0;
-        if (vel) {
-            inst = instance_of(g, keys, p);
+        const int inst = keys ? instance_of(g, keys, p) : 0;
+        if (vel)
             for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(vel[3 * inst + a]) : 0;
-        }
         const Coef cf = CoefFromDt ? local[p - p0] : coef[inst * (g.depth + 1) + levels[p]];
         step_cell<T, GhostsOnTheFly>(in, out, meta, g, cf, up, p, t - (p - p0) * cells);
     }
@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(256) k_halo(T* __restrict__ buf, const amr_hal
 // max|grad u|*h at interior cell c of patch p: central differences over face
 // ghosts, evaluated in double with explicit rounding (no contraction) so the
 // oracle's arithmetic is reproduced bit for bit.  Ghosts come from the buffer
-// or, with GhostsOnTheFly, from the neighbours by the halo rules.
+// or, with GhostsOnTheFly, from the neighbours by the halo rules, rounded to
+// the state type as a halo exchange would store them.
 template <typename T, bool GhostsOnTheFly>
 __device__ inline double gradient_cell(const T* buf, const amr_halo_meta* meta, const Geo& g, int p, int c)
 {
@@ -207,8 +208,8 @@ __device__ inline double gradient_cell(const T* buf, const amr_halo_meta* meta, 
             } else {
                 int G[3] = { idx[0], idx[1], idx[2] };
                 G[L]     = nidx;
-                side[pos] = ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos,
-                                           g, u);
+                side[pos] = static_cast<double>(static_cast<T>(ghost_value<T>(
+                    buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos, g, u)));
             }
         }
         const double gr = __dmul_rn(0.5, __dsub_rn(side[1], side[0]));
@@ -240,14 +241,100 @@ __device__ inline double gradient_sq_cell(const T* buf, const amr_halo_meta* met
             } else {
                 int G[3] = { idx[0], idx[1], idx[2] };
                 G[L]     = nidx;
-                side[pos] = ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos,
-                                           g, u);
+                side[pos] = static_cast<double>(static_cast<T>(ghost_value<T>(
+                    buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos], G, L, pos, g, u)));
             }
         }
         const double gr = __dmul_rn(0.5, __dsub_rn(side[1], side[0]));
         s               = __dadd_rn(s, __dmul_rn(gr, gr));
     }
     return s;
+}
+
+// The gradient rule on squared norms with an FP32 pre-filter.  Exact tests:
+// refine if s >= rsq, coarsen-eligible if s < csq (sq_threshold makes these
+// equal to the reference's sqrt(s) > rthr and sqrt(s) < cthr for every
+// double s).  An FP32 evaluation s32 of the same sum (FP32 differences of the
+// FP32 state, or FP64 differences rounded once to FP32; FP32 squares and
+// sums) is within a relative 1e-6 of it whenever it is finite and the
+// thresholds lie in [1e-20, 1e30], so s32 >= r_hi proves s >= rsq and
+// s32 < r_lo proves s < rsq (margins of 1e-5, likewise c_lo / c_hi); only
+// cells inside a band re-evaluate in FP64.  fast = 0 turns the filter off.
+struct GradRule {
+    double rsq, csq;
+    float  r_lo, r_hi, c_lo, c_hi;
+    int    fast;
+};
+
+// R: the rank at compile time (2 or 3), so coordinate arrays stay in registers.
+template <typename T, bool GhostsOnTheFly, int R>
+__device__ inline float gradient_sq_f32(const T* buf, const amr_halo_meta* meta, const Geo& g, int p, int c)
+{
+    int idx[3];
+    idx[2] = 0;
+#pragma unroll
+    for (int L = R - 1; L >= 0; --L) {
+        idx[L] = c % g.n + g.h;
+        c /= g.n;
+    }
+    const T*  u  = buf + static_cast<size_t>(p) * g.flat;
+    const int li = padded_index(g, idx);
+    float     s  = 0.0f;
+#pragma unroll
+    for (int a = 0; a < R; ++a) {
+        const int L = R - 1 - a;
+        T         lo, hi;
+        {
+            const int nidx = idx[L] - 1;
+            if (!GhostsOnTheFly || nidx >= g.h) {
+                lo = u[li - g.s[L]];
+            } else {
+                int G[3] = { idx[0], idx[1], idx[2] };
+                G[L]     = nidx;
+                lo = static_cast<T>(ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L], G, L, 0,
+                                                   g, u));
+            }
+        }
+        {
+            const int nidx = idx[L] + 1;
+            if (!GhostsOnTheFly || nidx < g.n + g.h) {
+                hi = u[li + g.s[L]];
+            } else {
+                int G[3] = { idx[0], idx[1], idx[2] };
+                G[L]     = nidx;
+                hi = static_cast<T>(ghost_value<T>(buf, g.flat, meta[static_cast<size_t>(p) * g.ndir + 2 * L + 1], G, L,
+                                                   1, g, u));
+            }
+        }
+        float d;
+        if constexpr (sizeof(T) == 4) d = hi - lo;
+        else d = static_cast<float>(hi - lo);
+        const float gr = 0.5f * d;
+        s              = fmaf(gr, gr, s);
+    }
+    return s;
+}
+
+// Refine (any) / coarsen (all) votes of interior cell c under the rule.
+template <typename T, bool GhostsOnTheFly, int R>
+__device__ inline void gradient_rule_cell(const T* buf, const amr_halo_meta* meta, const Geo& g, const GradRule& r,
+                                          int p, int c, int& any, int& all)
+{
+    if (r.fast) {
+        const float s = gradient_sq_f32<T, GhostsOnTheFly, R>(buf, meta, g, p, c);
+        if (isfinite(s)) {
+            const bool r_sure = s >= r.r_hi || s < r.r_lo;
+            const bool c_sure = s < r.c_lo || s >= r.c_hi;
+            if (r_sure && c_sure) {
+                if (s >= r.r_hi) any = 1;
+                if (s >= r.c_hi) all = 0;
+                return;
+            }
+        }
+    }
+    const double s = gradient_sq_cell<T, GhostsOnTheFly>(buf, meta, g, p, c);
+    if (s >= r.rsq) any = 1;
+    if (!(s < r.csq)) all = 0;
 }
 
 // Patch decision from the any/all rule of
@@ -258,30 +345,32 @@ __device__ inline int8_t gradient_decision(int any, int all, int level, int min_
     return (level < max_level && any) ? FLAG_REFINE : (level > min_level && all) ? FLAG_COARSEN : FLAG_STABLE;
 }
 
-// bounds (optional): per-instance (min_level, max_level) pairs, indexed by
-// the leaf's instance; they replace min_level/max_level.
-template <typename T>
-__global__ void __launch_bounds__(128)
-k_flags_gradient(const T* __restrict__ buf, const int32_t* __restrict__ levels, int P, Geo g,
-                 double rthr, double cthr, int min_level, int max_level, int8_t* __restrict__ flags,
-                 const uint64_t* __restrict__ keys = nullptr, const int32_t* __restrict__ bounds = nullptr)
+// Gradient flags, one warp per patch (grid-stride).  bounds (optional):
+// per-instance (min_level, max_level) pairs, indexed by the leaf's instance;
+// they replace min_level/max_level.
+template <typename T, bool GhostsOnTheFly, int R>
+__global__ void __launch_bounds__(256)
+k_flags_grad(const T* __restrict__ buf, const amr_halo_meta* __restrict__ meta, const int32_t* __restrict__ levels,
+             int P, Geo g, GradRule rule, int min_level, int max_level, int8_t* __restrict__ flags,
+             const uint64_t* __restrict__ keys, const int32_t* __restrict__ bounds)
 {
-    const int p = blockIdx.x;
-    if (p >= P) return;
-    if (bounds) {
-        const int inst = instance_of(g, keys, p);
-        min_level      = bounds[2 * inst];
-        max_level      = bounds[2 * inst + 1];
+    const int lane = threadIdx.x & 31;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < P; p += (gridDim.x * blockDim.x) >> 5) {
+        int any = 0, all = 1;
+        for (int c = lane; c < g.cells; c += 32)
+            gradient_rule_cell<T, GhostsOnTheFly, R>(buf, meta, g, rule, p, c, any, all);
+        any = __any_sync(0xffffffffu, any);
+        all = __all_sync(0xffffffffu, all);
+        if (lane == 0) {
+            int lo = min_level, hi = max_level;
+            if (bounds) {
+                const int inst = instance_of(g, keys, p);
+                lo             = bounds[2 * inst];
+                hi             = bounds[2 * inst + 1];
+            }
+            flags[p] = gradient_decision(any, all, levels[p], lo, hi);
+        }
     }
-    int any = 0, all = 1;
-    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) {
-        const double v = gradient_cell<T, false>(buf, nullptr, g, p, c);
-        if (v > rthr) any = 1;
-        if (!(v < cthr)) all = 0;
-    }
-    any = __syncthreads_or(any);
-    all = __syncthreads_and(all);
-    if (threadIdx.x == 0) flags[p] = gradient_decision(any, all, levels[p], min_level, max_level);
 }
 
 // Max-value rule (fvm_refinement_criterion.cu:27-67, tests'
@@ -896,7 +985,6 @@ struct Step2dShape {
 
 template <typename T, int N, int H, int S>
 __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restrict__ out,
-                                            const int32_t* __restrict__ levels,
                                             const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
                                             const Coef* __restrict__ coef, int upx0, int upy0, int32_t* err,
                                             const uint64_t* __restrict__ keys, const double* __restrict__ vel,
@@ -907,6 +995,7 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     constexpr int      FLAT = Sh::FLAT;
     constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
     constexpr int      SEG  = Sh::SEG;
+    constexpr int      HALF = N / 2;
     const int          lane = threadIdx.x & 31;
     if (lane == 0) {
         for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
@@ -927,54 +1016,132 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     uint32_t  phase = 0; // bit b: parity of slot b's next completion
     const int i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
     const int nl = g.depth + 1;
-    // Per-leaf instance: upwind sides from its velocity (vel != nullptr),
-    // else the launch-wide upx0/upy0.  Ghost job of this lane: lanes 0..N-1
-    // the upwind column, lanes N..2N-1 the upwind row.
-    const bool col   = lane < N;
-    const int  L     = col ? 1 : 0;
-    const int  tg    = (col ? lane : lane - N) + H;
-    auto       sides = [&](int q, int& ux, int& uy, int& inst) {
-        inst = 0;
-        ux   = upx0;
-        uy   = upy0;
+
+    // Ghost job of this lane: lanes 0..N-1 the upwind ghost column (normal
+    // layout dim 1), lanes N..2N-1 the upwind ghost row (dim 0); tg is the
+    // tangential padded coordinate, fsel the finer-neighbour section it lies in.
+    const bool col  = lane < N;
+    const bool job  = lane < 2 * N;
+    const int  L    = col ? 1 : 0;
+    const int  tg   = (col ? lane : lane - N) + H;
+    const int  fsel = (tg - H) / HALF;
+
+    // Per-patch metadata, software-pipelined so that no load is consumed in
+    // the iteration that issues it: the key three patches ahead, the upwind
+    // sides, coefficient row and this lane's neighbour record two ahead, the
+    // raw ghost source values one ahead.  The instance comes from the key;
+    // the upwind sides from its velocity (vel != nullptr) or upx0/upy0.
+    struct Side {
+        int ux, uy;
+        Coef cf;
+    };
+    struct Rec {
+        int rel, nb, fid, q0, q1;
+    };
+    struct Raw {
+        T   v[4];
+        int kind; // 0 none, 1 one value, 4 mean of four
+    };
+    auto side_of = [&](uint64_t key, Side& sd) {
+        const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+        sd.ux          = upx0;
+        sd.uy          = upy0;
         if (vel) {
-            inst = instance_of(g, keys, q);
-            ux   = upwind(vel[3 * inst]);
-            uy   = upwind(vel[3 * inst + 1]);
+            sd.ux = upwind(vel[3 * inst]);
+            sd.uy = upwind(vel[3 * inst + 1]);
+        }
+        sd.cf = coef[inst * nl + key_level(key)];
+    };
+    auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
+    auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
+    auto rec_of  = [&](int q, const Side& sd, Rec& m) {
+        m.rel = REL_NONE;
+        if (!has_job(sd)) return;
+        const amr_halo_meta* rp = meta + static_cast<size_t>(q) * 4 + 2 * L + pos_of(sd);
+        m.rel                   = rp->relation;
+        m.nb                    = rp->neighbor;
+        m.fid                   = rp->finer_ids[fsel];
+        m.q0                    = rp->quadrant[0];
+        m.q1                    = rp->quadrant[1];
+    };
+    // The halo rules of ghost_value for one 2D face ghost cell, split into
+    // issuing the source loads and combining them.
+    auto fetch = [&](int q, const Side& sd, const Rec& m, Raw& raw) {
+        raw.kind = 0;
+        if (!has_job(sd)) return;
+        const int pos = pos_of(sd);
+        const int gc  = pos ? N + H : H - 1;
+        const int G0 = col ? tg : gc, G1 = col ? gc : tg;
+        const int sh = pos ? -N : N;
+        int       f0 = G0 + (L == 0 ? sh : 0), f1 = G1 + (L == 1 ? sh : 0);
+        raw.kind     = 1;
+        if (m.rel == REL_SAME) {
+            raw.v[0] = in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
+        } else if (m.rel == REL_COARSER) {
+            f0       = H + m.q0 * HALF + (f0 - H) / 2;
+            f1       = H + m.q1 * HALF + (f1 - H) / 2;
+            raw.v[0] = in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
+        } else if (m.rel == REL_FINER) {
+            f0          = ((f0 - H) * 2) % N + H;
+            f1          = ((f1 - H) * 2) % N + H;
+            const T* fp = in + static_cast<size_t>(m.fid) * FLAT + f0 * P1 + f1;
+            raw.v[0]    = fp[0];
+            raw.v[1]    = fp[1];
+            raw.v[2]    = fp[P1];
+            raw.v[3]    = fp[P1 + 1];
+            raw.kind    = 4;
+        } else { // relation none: the buffer's own ghost value
+            raw.v[0] = in[static_cast<size_t>(q) * FLAT + G0 * P1 + G1];
         }
     };
-    int           upx = 0, upy = 0, inst = 0;
-    amr_halo_meta m_next{};
-    if (p < P) {
-        sides(p, upx, upy, inst);
-        const bool has0 = lane < 2 * N && (col ? upx != 0 : upy != 0);
-        const int  pos0 = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
-        if (has0) m_next = meta[static_cast<size_t>(p) * 4 + 2 * L + pos0];
-    }
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int  b       = it % S;
-        const int  pn      = p + nwarp;
-        const int  pf      = p + (S - 1) * nwarp; // patch whose copy is issued now
-        const bool has     = lane < 2 * N && (col ? upx != 0 : upy != 0);
-        const int  pos     = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
-        const int  gc      = pos ? N + H : H - 1;
-        int        G[3]    = { col ? tg : gc, col ? gc : tg, 0 };
-        const int  cur_upx = upx, cur_upy = upy, cur_inst = inst;
-        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
-        const Coef          cf = coef[cur_inst * nl + levels[p]];
-        const amr_halo_meta m  = m_next;
-        if (pn < P) { // the next leaf's sides and neighbour record, one patch ahead
-            sides(pn, upx, upy, inst);
-            const bool hasn = lane < 2 * N && (col ? upx != 0 : upy != 0);
-            const int  posn = col ? (upx > 0 ? 1 : 0) : (upy > 0 ? 1 : 0);
-            if (hasn) m_next = meta[static_cast<size_t>(pn) * 4 + 2 * L + posn];
+    auto combine = [&](const Raw& raw) -> T {
+        if (raw.kind == 4) {
+            double sum = static_cast<double>(raw.v[0]);
+            sum += static_cast<double>(raw.v[1]);
+            sum += static_cast<double>(raw.v[2]);
+            sum += static_cast<double>(raw.v[3]);
+            return static_cast<T>(sum / 4.0);
         }
-        // relation none keeps the buffer's own ghost value (the tile does not
-        // hold the ghost rows)
-        T gv = T(0);
-        if (has)
-            gv = m.relation != REL_NONE ? static_cast<T>(ghost_value<T>(in, FLAT, m, G, L, pos, g, nullptr))
-                                        : in[static_cast<size_t>(p) * FLAT + G[0] * P1 + G[1]];
+        return raw.v[0];
+    };
+
+    // pipeline prologue
+    const int q1 = p + nwarp, q2 = p + 2 * nwarp;
+    Side      sd0{}, sd1{}, sd2{};
+    Rec       m1{}, m2{};
+    Raw       g0{}, g1{};
+    uint64_t  k2 = 0;
+    if (p < P) {
+        side_of(keys[p], sd0);
+        Rec m0;
+        rec_of(p, sd0, m0);
+        fetch(p, sd0, m0, g0);
+    }
+    if (q1 < P) {
+        side_of(keys[q1], sd1);
+        rec_of(q1, sd1, m1);
+    }
+    if (q2 < P) k2 = keys[q2];
+
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int b  = it % S;
+        const int pf = p + (S - 1) * nwarp; // patch whose copy is issued now
+        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
+        // advance the metadata pipeline
+        const int pa = p + nwarp, pb = p + 2 * nwarp, pc = p + 3 * nwarp;
+        uint64_t  k3 = 0;
+        if (pc < P) k3 = keys[pc];
+        if (pb < P) {
+            side_of(k2, sd2);
+            rec_of(pb, sd2, m2);
+        }
+        if (pa < P) fetch(pa, sd1, m1, g1);
+        // this patch
+        const bool has = has_job(sd0);
+        const int  pos = pos_of(sd0);
+        const int  gc  = pos ? N + H : H - 1;
+        const int  G0 = col ? tg : gc, G1 = col ? gc : tg;
+        const T    gv  = combine(g0);
         if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
             if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
             phase ^= 1u << b;
@@ -988,17 +1155,34 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         }
         phase ^= 1u << b;
         T* tile = tiles + static_cast<size_t>(b) * FLAT;
-        if (has) tile[G[0] * P1 + G[1]] = gv;
+        if (has) tile[G0 * P1 + G1] = gv;
         __syncwarp();
-        const T c00 = static_cast<T>(cf.c0), cx = static_cast<T>(cf.c[0]), cy = static_cast<T>(cf.c[1]);
-        T       res[SEG];
+        const int ux = sd0.ux, uy = sd0.uy;
+        T         res[SEG];
+        if constexpr (sizeof(T) == 4) {
+            // FP32: u + c (u_up - u), exact for a constant state, so the
+            // rounding of the coefficients does not bias the solution
+            const float cx = static_cast<float>(sd0.cf.c[0]), cy = static_cast<float>(sd0.cf.c[1]);
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int idx = r * P1 + c0 + k;
-            T         acc = c00 * tile[idx];
-            if (cur_upx != 0) acc = fma(cx, tile[idx + cur_upx], acc);
-            if (cur_upy != 0) acc = fma(cy, tile[idx + cur_upy * P1], acc);
-            res[k] = acc;
+            for (int k = 0; k < SEG; ++k) {
+                const int   idx = r * P1 + c0 + k;
+                const float u   = tile[idx];
+                float       acc = u;
+                if (ux != 0) acc = fmaf(cx, tile[idx + ux] - u, acc);
+                if (uy != 0) acc = fmaf(cy, tile[idx + uy * P1] - u, acc);
+                res[k] = acc;
+            }
+        } else {
+            const T c00 = static_cast<T>(sd0.cf.c0), cx = static_cast<T>(sd0.cf.c[0]),
+                    cy = static_cast<T>(sd0.cf.c[1]);
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                const int idx = r * P1 + c0 + k;
+                T         acc = c00 * tile[idx];
+                if (ux != 0) acc = fma(cx, tile[idx + ux], acc);
+                if (uy != 0) acc = fma(cy, tile[idx + uy * P1], acc);
+                res[k] = acc;
+            }
         }
         __syncwarp();
 #pragma unroll
@@ -1008,6 +1192,12 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
         for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
         __syncwarp();
+        // rotate the pipeline
+        sd0 = sd1;
+        g0  = g1;
+        sd1 = sd2;
+        m1  = m2;
+        k2  = k3;
     }
 }
 
@@ -1021,18 +1211,19 @@ __device__ __forceinline__ void step2d_smem(unsigned char* smem, T*& tiles, uint
     bars           = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * S * Sh::TILE) + wib * S;
 }
 
-// Register budget: 40 resident warps per SM for FP32, 32 for FP64.
+// Register budget: 32 resident warps per SM for FP32, 24 for FP64 (the
+// metadata pipeline keeps three patches' records in registers).
 template <typename T, int W>
 struct Step2dOcc {
-    static constexpr int blocks = ((sizeof(T) == 4 ? 40 : 32) / W) > 0 ? ((sizeof(T) == 4 ? 40 : 32) / W) : 1;
+    static constexpr int blocks = ((sizeof(T) == 4 ? 32 : 24) / W) > 0 ? ((sizeof(T) == 4 ? 32 : 24) / W) : 1;
 };
 
 // Host-driven launch: leaf count and buffers from the arguments.
 template <typename T, int N, int H, int W, int S>
 __global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
-         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef, int upx0, int upy0,
-         int32_t* err, const uint64_t* __restrict__ keys, const double* __restrict__ vel)
+k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
+         const Coef* __restrict__ coef, int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
+         const double* __restrict__ vel)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     T*        tiles;
@@ -1040,7 +1231,7 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restric
     step2d_smem<T, N, H, W, S>(smem, tiles, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_body<T, N, H, S>(in, out, levels, meta, P, g, coef, upx0, upy0, err, keys, vel, tiles, bars, p, nwarp);
+    step2d_body<T, N, H, S>(in, out, meta, P, g, coef, upx0, upy0, err, keys, vel, tiles, bars, p, nwarp);
 }
 
 } // namespace amr_gb300

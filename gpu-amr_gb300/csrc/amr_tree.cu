@@ -9,6 +9,7 @@
 #include <limits>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -265,16 +266,15 @@ unsigned step2d_grid(int P, int grid)
 }
 
 template <typename T, int N, int H>
-amr_status launch_step2d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
-                         const Coef* coef, const int* up, int32_t* err, const uint64_t* keys, const double* vel,
-                         const StepCfg& cfg, cudaStream_t s)
+amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coef,
+                         const int* up, int32_t* err, const uint64_t* keys, const double* vel, const StepCfg& cfg,
+                         cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
         const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(in, out, levels, meta, P, g,
-                                                                                      coef, up[0], up[1], err, keys,
-                                                                                      vel);
+        k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(in, out, meta, P, g, coef,
+                                                                                      up[0], up[1], err, keys, vel);
         AMR_LAUNCHED("k_step2d");
         return AMR_OK;
     });
@@ -328,6 +328,7 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const doubl
     }
     best = StepCfg{};
     if (g_tune_mode.load() == 0) return AMR_OK;
+    if (const char* env = std::getenv("AMR_GB300_AUTOTUNE"); env && std::strcmp(env, "0") == 0) return AMR_OK;
     const int    P = static_cast<int>(t->size);
     cudaStream_t s = t->stream;
     cudaEvent_t  e0, e1;
@@ -347,7 +348,7 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const doubl
                 StepCfg   c{ W, S, grid };
                 for (int rep = 0; rep < 2; ++rep) { // warm-up
                     amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->levels[t->tb], t->meta[t->tb], P, t->g, coef, up,
+                                                          t->meta[t->tb], P, t->g, coef, up,
                                                           t->status + 7, t->keys[t->tb], vel, c, s);
                     if (r != AMR_OK) return r;
                 }
@@ -355,7 +356,7 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const doubl
                 AMR_CUDA(cudaEventRecord(e0, s));
                 for (int rep = 0; rep < reps; ++rep) {
                     amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->levels[t->tb], t->meta[t->tb], P, t->g, coef, up,
+                                                          t->meta[t->tb], P, t->g, coef, up,
                                                           t->status + 7, t->keys[t->tb], vel, c, s);
                     if (r != AMR_OK) return r;
                 }
@@ -535,6 +536,34 @@ double sq_threshold(double thr, bool strict)
     return r;
 }
 
+// The gradient rule's exact squared thresholds and its FP32 pre-filter band.
+GradRule make_grad_rule(double rthr, double cthr)
+{
+    GradRule     r{};
+    const double m = 1e-5;
+    r.rsq          = sq_threshold(rthr, true);
+    r.csq          = sq_threshold(cthr, false);
+    auto usable    = [](double t) { return t == 0.0 || (t >= 1e-20 && t <= 1e30); };
+    r.fast         = usable(r.rsq) && usable(r.csq) ? 1 : 0;
+    auto down      = [](double v) {
+        float f = static_cast<float>(v);
+        if (static_cast<double>(f) > v) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+        return f;
+    };
+    auto up = [](double v) {
+        float f = static_cast<float>(v);
+        if (static_cast<double>(f) < v) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+        return f;
+    };
+    const float ninf = -std::numeric_limits<float>::infinity();
+    // s >= 0 always: a zero threshold is decided by s32 >= 0 alone
+    r.r_hi = r.rsq == 0.0 ? 0.0f : up(r.rsq * (1.0 + m));
+    r.r_lo = r.rsq == 0.0 ? ninf : down(r.rsq * (1.0 - m));
+    r.c_hi = r.csq == 0.0 ? 0.0f : up(r.csq * (1.0 + m));
+    r.c_lo = r.csq == 0.0 ? ninf : down(r.csq * (1.0 - m));
+    return r;
+}
+
 // ------------------------------------------------------------ persistent run
 constexpr int kPersistentLeaves = 1024; // above this, per-launch kernels keep all SMs busy
 constexpr int kMaxInterval      = 256;
@@ -664,11 +693,21 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     }
     const int sp = key.k & 1;
     if (key.crit != 0) {
-        k_run_halo<T><<<sms * 32, 256, 0, cs>>>(B, ctl, g, sp);
-        AMR_LAUNCHED("k_run_halo");
-        k_run_flags<T><<<sms * 16, 128, 0, cs>>>(B, ctl, g, key.crit, key.rthr, key.cthr, key.min_level,
-                                                  key.max_level, sp);
-        AMR_LAUNCHED("k_run_flags");
+        if (key.crit == 1) {
+            if (g.rank == 2)
+                k_run_flags_grad<T, 2><<<sms * 16, 256, 0, cs>>>(B, ctl, g, make_grad_rule(key.rthr, key.cthr),
+                                                                 key.min_level, key.max_level, sp);
+            else
+                k_run_flags_grad<T, 3><<<sms * 16, 256, 0, cs>>>(B, ctl, g, make_grad_rule(key.rthr, key.cthr),
+                                                                 key.min_level, key.max_level, sp);
+            AMR_LAUNCHED("k_run_flags_grad");
+        } else {
+            k_run_halo<T><<<sms * 32, 256, 0, cs>>>(B, ctl, g, sp);
+            AMR_LAUNCHED("k_run_halo");
+            k_run_flags_max<T><<<sms * 16, 128, 0, cs>>>(B, ctl, g, key.rthr, key.cthr, key.min_level, key.max_level,
+                                                         sp);
+            AMR_LAUNCHED("k_run_flags_max");
+        }
         k_run_mark<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
         AMR_LAUNCHED("k_run_mark");
         for (int r = 0; r < key.rounds; ++r) {
@@ -1072,6 +1111,15 @@ amr_status amr_tree_load_state_device(amr_tree* t, const void* device_state, siz
     return AMR_OK;
 }
 
+amr_status amr_tree_download_state_device(amr_tree* t, void* device_dst, size_t num)
+{
+    if (!t || !device_dst) return fail(AMR_ERR_INVALID, "null argument");
+    if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
+    AMR_CUDA(cudaMemcpyAsync(device_dst, t->cur, num * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    return AMR_OK;
+}
+
 amr_status amr_tree_reset(amr_tree* t)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
@@ -1120,17 +1168,28 @@ amr_status amr_tree_halo_exchange(amr_tree* t)
 amr_status amr_tree_flags_gradient(amr_tree* t, double rthr, double cthr, int min_level, int max_level)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    if (!t->ghosts_valid) {
-        amr_status s = launch_halo(t);
-        if (s != AMR_OK) return s;
-    }
-    const int P = static_cast<int>(t->size);
+    // ghosts from the buffer when they are current (the caller's or the last
+    // exchange's), else evaluated on the fly by the halo rules (same values)
+    const bool     fly  = !t->ghosts_valid;
+    const int      P    = static_cast<int>(t->size);
+    const GradRule rule = make_grad_rule(rthr, cthr);
+    const unsigned grid = std::min<unsigned>(grid_for(P, 8), static_cast<unsigned>(num_sms() * 16));
     return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
-        k_flags_gradient<T><<<P, 128, 0, t->stream>>>(static_cast<const T*>(t->cur), t->levels[t->tb], P, t->g, rthr,
-                                                     cthr, min_level, max_level, t->flags,
-            t->keys[t->tb], t->bounds_set ? t->bounds : nullptr);
-        AMR_LAUNCHED("k_flags_gradient");
+        const T*       buf = static_cast<const T*>(t->cur);
+        const int32_t* bnd = t->bounds_set ? t->bounds : nullptr;
+        auto launch = [&](auto kern) {
+            kern<<<grid, 256, 0, t->stream>>>(buf, t->meta[t->tb], t->levels[t->tb], P, t->g, rule, min_level,
+                                              max_level, t->flags, t->keys[t->tb], bnd);
+        };
+        if (t->g.rank == 2) {
+            if (fly) launch(k_flags_grad<T, true, 2>);
+            else launch(k_flags_grad<T, false, 2>);
+        } else {
+            if (fly) launch(k_flags_grad<T, true, 3>);
+            else launch(k_flags_grad<T, false, 3>);
+        }
+        AMR_LAUNCHED("k_flags_grad");
         return AMR_OK;
     });
 }
@@ -1299,10 +1358,10 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                 const T*    in = static_cast<const T*>(t->cur);
                 T*          out = static_cast<T*>(t->nxt);
                 if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
-                    return launch_step2d<T, 16, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
+                    return launch_step2d<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, up,
                                                    t->status + 7, t->keys[t->tb], vleaf, cfg, s);
                 if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
-                    return launch_step2d<T, 8, 1>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up,
+                    return launch_step2d<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, up,
                                                   t->status + 7, t->keys[t->tb], vleaf, StepCfg{}, s);
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
                                                      up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
@@ -1415,8 +1474,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             A.crit        = p->criterion;
             A.rthr        = p->refine_threshold;
             A.cthr        = p->coarsen_threshold;
-            A.rthr_sq     = sq_threshold(p->refine_threshold, true);
-            A.cthr_sq     = sq_threshold(p->coarsen_threshold, false);
+            A.rule        = make_grad_rule(p->refine_threshold, p->coarsen_threshold);
             A.min_level   = p->min_level;
             A.max_level   = p->max_level;
             if (t->bounds_set) { // one tree: its own (min, max) pair

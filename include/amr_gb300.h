@@ -165,8 +165,9 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out);
  * elements of the tree's dtype. */
 amr_status amr_tree_upload_state(amr_tree* t, const void* host_state, size_t num_patches);
 amr_status amr_tree_download_state(amr_tree* t, void* host_state, size_t num_patches);
-/* Device-to-device state load (same layout as upload_state). */
+/* Device-to-device state load and copy-out (same layout as upload_state). */
 amr_status amr_tree_load_state_device(amr_tree* t, const void* device_state, size_t num_patches);
+amr_status amr_tree_download_state_device(amr_tree* t, void* device_dst, size_t num_patches);
 /* Back to the freshly constructed tree: one root leaf, periodic
  * self-neighbours, zero state (ndtree::ndtree, ndtree.hpp:320-425),
  * without reallocating. */
