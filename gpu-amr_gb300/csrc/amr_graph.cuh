@@ -139,6 +139,23 @@ k_run_flags_grad(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, in
     }
 }
 
+// 2D gradient flags of the sized kernel (flags2d_body), ghosts on the fly.
+template <typename T, int N, int H>
+__global__ void __launch_bounds__(256)
+k_run_flags2d(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int max_level, int sp)
+{
+    if (ctl->err) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    flags2d_smem<T, N, H, false>(smem, blockDim.x >> 5, tiles, bars);
+    const int tb    = ctl->tb;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    flags2d_body<T, N, H, false>(static_cast<const T*>(B.state[ctl->sb ^ sp]), B.meta[tb], B.keys[tb], ctl->P, g, rule,
+                                 min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp);
+}
+
 // Max-value flags (k_flags_max's rule over the exchanged ghosts), one block
 // per patch, grid-stride.
 template <typename T>

@@ -1235,3 +1235,225 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __r
 }
 
 } // namespace amr_gb300
+
+namespace amr_gb300 {
+
+// ------------------------------------------------ 2D gradient flags, sized at compile time
+// One warp per patch (grid-stride).  The patch's interior rows move into a
+// per-warp shared-memory tile by bulk async copy (double-buffered); the
+// lanes fill all four ghost faces (lanes 0..N-1 the two ghost columns at row
+// tg, lanes N..2N-1 the two ghost rows at column tg) by the halo rules, the
+// values a halo exchange would store; FromBuffer copies the whole padded
+// patch and takes the buffer's ghosts instead.  Each lane then applies the
+// gradient rule (FP32 sum with the proven band, FP64 inside it, the same
+// arithmetic as gradient_sq_cell) to N*N/32 cells and the warp votes.
+template <typename T, int N, int H, bool FromBuffer>
+struct Flags2dShape {
+    static constexpr int      P1    = N + 2 * H;
+    static constexpr int      FLAT  = P1 * P1;
+    static constexpr uint32_t LO    = FromBuffer ? 0u : ((H * P1 * sizeof(T)) & ~15u);
+    static constexpr uint32_t HI    = FromBuffer ? FLAT * sizeof(T) : (((N + H) * P1 * sizeof(T) + 15u) & ~15u);
+    static constexpr uint32_t BYTES = HI - LO;
+    static constexpr int      SEG   = N * N / 32;
+    static constexpr size_t   TILE  = FLAT * sizeof(T);
+    static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
+    static constexpr size_t smem(int W) { return static_cast<size_t>(W) * 2 * (TILE + 8); }
+};
+
+// FP64 squared gradient of a 2D cell from its four neighbour values, in
+// gradient_sq_cell's order (Morton x, then y) and rounding.
+template <typename T>
+__device__ __forceinline__ double grad_sq_exact2(T xl, T xh, T yl, T yh)
+{
+    const double gx = __dmul_rn(0.5, __dsub_rn(static_cast<double>(xh), static_cast<double>(xl)));
+    double       s  = __dadd_rn(0.0, __dmul_rn(gx, gx));
+    const double gy = __dmul_rn(0.5, __dsub_rn(static_cast<double>(yh), static_cast<double>(yl)));
+    return __dadd_rn(s, __dmul_rn(gy, gy));
+}
+
+template <typename T>
+__device__ __forceinline__ float grad_sq_f32_2(T xl, T xh, T yl, T yh)
+{
+    float dx, dy;
+    if constexpr (sizeof(T) == 4) {
+        dx = xh - xl;
+        dy = yh - yl;
+    } else {
+        dx = static_cast<float>(xh - xl);
+        dy = static_cast<float>(yh - yl);
+    }
+    const float gx = 0.5f * dx, gy = 0.5f * dy;
+    return fmaf(gy, gy, fmaf(gx, gx, 0.0f));
+}
+
+template <typename T, int N, int H, bool FromBuffer>
+__device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta,
+                                             const uint64_t* __restrict__ keys, int P, const Geo& g,
+                                             const GradRule& rule, int min_level, int max_level,
+                                             const int32_t* __restrict__ bounds, int8_t* __restrict__ flags,
+                                             int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp)
+{
+    using Sh                = Flags2dShape<T, N, H, FromBuffer>;
+    constexpr int      P1   = Sh::P1;
+    constexpr int      FLAT = Sh::FLAT;
+    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
+    constexpr int      SEG  = Sh::SEG;
+    constexpr int      HALF = N / 2;
+    const int          lane = threadIdx.x & 31;
+    if (lane == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const char* in_bytes = reinterpret_cast<const char*>(in);
+    auto        request  = [&](int q, int slot) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[slot], BYTES);
+        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
+                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
+    };
+    if (p < P && lane == 0) request(p, 0);
+    uint32_t   phase = 0;
+    const int  i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
+    // ghost jobs: lanes 0..N-1 column faces (normal layout dim 1) at row tg,
+    // lanes N..2N-1 row faces (dim 0) at column tg; pos 0 and 1
+    const bool col  = lane < N;
+    const bool job  = !FromBuffer && lane < 2 * N;
+    const int  L    = col ? 1 : 0;
+    const int  tg   = (col ? lane : lane - N) + H;
+    const int  fsel = (tg - H) / HALF;
+    struct Rec {
+        int rel, nb, fid, q0, q1;
+    };
+    auto rec_of = [&](int q, int pos, Rec& m) {
+        m.rel = REL_NONE;
+        if (!job) return;
+        const amr_halo_meta* rp = meta + static_cast<size_t>(q) * 4 + 2 * L + pos;
+        m.rel                   = rp->relation;
+        m.nb                    = rp->neighbor;
+        m.fid                   = rp->finer_ids[fsel];
+        m.q0                    = rp->quadrant[0];
+        m.q1                    = rp->quadrant[1];
+    };
+    // ghost cell (G0, G1) of face pos from record m: the halo rules of
+    // ghost_value, rounded to T
+    auto ghost = [&](int q, int pos, const Rec& m, int& G0, int& G1) -> T {
+        const int gc = pos ? N + H : H - 1;
+        G0           = col ? tg : gc;
+        G1           = col ? gc : tg;
+        const int sh = pos ? -N : N;
+        int       f0 = G0 + (L == 0 ? sh : 0), f1 = G1 + (L == 1 ? sh : 0);
+        if (m.rel == REL_SAME) return in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
+        if (m.rel == REL_COARSER) {
+            f0 = H + m.q0 * HALF + (f0 - H) / 2;
+            f1 = H + m.q1 * HALF + (f1 - H) / 2;
+            return in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
+        }
+        if (m.rel == REL_FINER) {
+            f0           = ((f0 - H) * 2) % N + H;
+            f1           = ((f1 - H) * 2) % N + H;
+            const T* fp  = in + static_cast<size_t>(m.fid) * FLAT + f0 * P1 + f1;
+            double   sum = static_cast<double>(fp[0]);
+            sum += static_cast<double>(fp[1]);
+            sum += static_cast<double>(fp[P1]);
+            sum += static_cast<double>(fp[P1 + 1]);
+            return static_cast<T>(sum / 4.0);
+        }
+        return in[static_cast<size_t>(q) * FLAT + G0 * P1 + G1];
+    };
+    Rec mn0{}, mn1{};
+    if (p < P) {
+        rec_of(p, 0, mn0);
+        rec_of(p, 1, mn1);
+    }
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int b  = it & 1;
+        const int pn = p + nwarp;
+        if (pn < P && lane == 0) request(pn, b ^ 1);
+        const uint64_t key = keys[p];
+        const Rec      m0 = mn0, m1 = mn1;
+        if (pn < P) {
+            rec_of(pn, 0, mn0);
+            rec_of(pn, 1, mn1);
+        }
+        T   gv0 = T(0), gv1 = T(0);
+        int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+        if (job) {
+            gv0 = ghost(p, 0, m0, a0, a1);
+            gv1 = ghost(p, 1, m1, b0, b1);
+        }
+        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
+            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
+            phase ^= 1u << b;
+            if (pn < P) mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+            return;
+        }
+        phase ^= 1u << b;
+        T* tile = tiles + static_cast<size_t>(b) * FLAT;
+        if (job) {
+            tile[a0 * P1 + a1] = gv0;
+            tile[b0 * P1 + b1] = gv1;
+        }
+        __syncwarp();
+        int any = 0, all = 1;
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int idx = r * P1 + c0 + k;
+            const T   xl = tile[idx - 1], xh = tile[idx + 1], yl = tile[idx - P1], yh = tile[idx + P1];
+            bool      done = false;
+            if (rule.fast) {
+                const float s = grad_sq_f32_2<T>(xl, xh, yl, yh);
+                if (isfinite(s) && (s >= rule.r_hi || s < rule.r_lo) && (s < rule.c_lo || s >= rule.c_hi)) {
+                    if (s >= rule.r_hi) any = 1;
+                    if (s >= rule.c_hi) all = 0;
+                    done = true;
+                }
+            }
+            if (!done) {
+                const double s = grad_sq_exact2<T>(xl, xh, yl, yh);
+                if (s >= rule.rsq) any = 1;
+                if (!(s < rule.csq)) all = 0;
+            }
+        }
+        any = __any_sync(0xffffffffu, any);
+        all = __all_sync(0xffffffffu, all);
+        if (lane == 0) {
+            int lo = min_level, hi = max_level;
+            if (bounds) {
+                const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+                lo             = bounds[2 * inst];
+                hi             = bounds[2 * inst + 1];
+            }
+            flags[p] = gradient_decision(any, all, key_level(key), lo, hi);
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T, int N, int H, bool FromBuffer>
+__device__ __forceinline__ void flags2d_smem(unsigned char* smem, int W, T*& tiles, uint64_t*& bars)
+{
+    using Sh      = Flags2dShape<T, N, H, FromBuffer>;
+    const int wib = threadIdx.x >> 5;
+    tiles         = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * 2 * Sh::FLAT;
+    bars          = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * 2 * Sh::TILE) + wib * 2;
+}
+
+template <typename T, int N, int H, bool FromBuffer>
+__global__ void __launch_bounds__(256)
+k_flags2d(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys, int P,
+          Geo g, GradRule rule, int min_level, int max_level, const int32_t* __restrict__ bounds,
+          int8_t* __restrict__ flags, int32_t* err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    flags2d_smem<T, N, H, FromBuffer>(smem, blockDim.x >> 5, tiles, bars);
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    flags2d_body<T, N, H, FromBuffer>(in, meta, keys, P, g, rule, min_level, max_level, bounds, flags, err, tiles, bars,
+                                      p, nwarp);
+}
+
+} // namespace amr_gb300

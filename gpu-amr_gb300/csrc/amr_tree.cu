@@ -693,7 +693,17 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     }
     const int sp = key.k & 1;
     if (key.crit != 0) {
-        if (key.crit == 1) {
+        if (key.crit == 1 && g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8)) {
+            const GradRule rule = make_grad_rule(key.rthr, key.cthr);
+            const unsigned fgrid = static_cast<unsigned>(sms * 4);
+            if (g.n == 16)
+                k_run_flags2d<T, 16, 1><<<fgrid, 256, Flags2dShape<T, 16, 1, false>::smem(8), cs>>>(
+                    B, ctl, g, rule, key.min_level, key.max_level, sp);
+            else
+                k_run_flags2d<T, 8, 1><<<fgrid, 256, Flags2dShape<T, 8, 1, false>::smem(8), cs>>>(
+                    B, ctl, g, rule, key.min_level, key.max_level, sp);
+            AMR_LAUNCHED("k_run_flags2d");
+        } else if (key.crit == 1) {
             if (g.rank == 2)
                 k_run_flags_grad<T, 2><<<sms * 16, 256, 0, cs>>>(B, ctl, g, make_grad_rule(key.rthr, key.cthr),
                                                                  key.min_level, key.max_level, sp);
@@ -1178,6 +1188,21 @@ amr_status amr_tree_flags_gradient(amr_tree* t, double rthr, double cthr, int mi
         using T = decltype(z);
         const T*       buf = static_cast<const T*>(t->cur);
         const int32_t* bnd = t->bounds_set ? t->bounds : nullptr;
+        if (t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8)) {
+            auto sized = [&](auto kern, size_t smem) {
+                kern<<<grid, 256, smem, t->stream>>>(buf, t->meta[t->tb], t->keys[t->tb], P, t->g, rule, min_level,
+                                                     max_level, bnd, t->flags, t->status + 7);
+            };
+            if (t->g.n == 16) {
+                if (fly) sized(k_flags2d<T, 16, 1, false>, Flags2dShape<T, 16, 1, false>::smem(8));
+                else sized(k_flags2d<T, 16, 1, true>, Flags2dShape<T, 16, 1, true>::smem(8));
+            } else {
+                if (fly) sized(k_flags2d<T, 8, 1, false>, Flags2dShape<T, 8, 1, false>::smem(8));
+                else sized(k_flags2d<T, 8, 1, true>, Flags2dShape<T, 8, 1, true>::smem(8));
+            }
+            AMR_LAUNCHED("k_flags2d");
+            return AMR_OK;
+        }
         auto launch = [&](auto kern) {
             kern<<<grid, 256, 0, t->stream>>>(buf, t->meta[t->tb], t->levels[t->tb], P, t->g, rule, min_level,
                                               max_level, t->flags, t->keys[t->tb], bnd);
