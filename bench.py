@@ -443,6 +443,145 @@ def plain_config2(args, torch, A, dev, stream, flush, world):
     }
 
 
+# ------------------------------------------------------------ adjoint form
+ADJOINT = dict(n=16, halo=1, depth=8, base_level=5, max_level=7, rthr=0.01, cthr=0.002, rounds=3, steps=400,
+               every=20, cfl=0.4, velocity=(1.0, 0.5), directions=64, eps=1e-4, pert=0.05, seed=7)
+
+
+def adjoint_mesh(A, dtype, stream, flag_log=None):
+    """Frozen mesh: config 2's initial field (two seeded bumps + noise) on a
+    uniform level-5 base, adapted at step 0 by the gradient criterion (0.01 /
+    0.002, up to level 7), three rounds.  flag_log replays recorded flags."""
+    J, W = ADJOINT, WORKLOAD
+    t = A.Tree(2, J["n"], J["halo"], J["depth"], capacity=40000, dtype=dtype, stream=stream.cuda_stream)
+    t.refine_uniform(J["base_level"])
+    log = []
+    for r in range(J["rounds"]):
+        if flag_log is None:
+            t.upload_state(A.gaussian_state(t.ids(), 2, J["n"], J["halo"], J["depth"], bumps(), W["noise"],
+                                            W["noise_seed"]))
+            t.flags_gradient(J["rthr"], J["cthr"], J["base_level"], J["max_level"])
+            f = t.get_flags()
+        else:
+            f = flag_log[r]
+            t.set_flags(f)
+        log.append(f)
+        t.remesh()
+    return t, log
+
+
+def adjoint_extra(torch, A, dev, stream, with_oracle=True):
+    J, W = ADJOINT, WORKLOAD
+    t64, log = adjoint_mesh(A, A.F64, stream)
+    t32, _ = adjoint_mesh(A, A.F32, stream, log)
+    ids = t64.ids()
+    assert np.array_equal(ids, t32.ids())
+    P = len(ids)
+    n, h = J["n"], J["halo"]
+    u0_np = A.gaussian_state(ids, 2, n, h, J["depth"], bumps(), W["noise"], W["noise_seed"])
+    mask = torch.zeros(u0_np.shape, dtype=torch.bool, device=f"cuda:{dev}")
+    mask[:, h:n + h, h:n + h] = True
+    u0 = torch.from_numpy(u0_np).to(f"cuda:{dev}")
+    rng = np.random.default_rng(J["seed"])
+    pert = torch.from_numpy(rng.standard_normal(u0_np.shape)).to(f"cuda:{dev}") * mask
+
+    def run(tree, u, dtype):
+        x = u.to(dtype).contiguous()
+        tree.load_state_device(x.data_ptr(), P)
+        tree.advance(J["steps"], J["velocity"], J["cfl"])
+        tree.finish_advance()
+        out = torch.empty_like(x)
+        tree.download_state_device(out.data_ptr(), P)
+        return out
+
+    target = run(t64, u0 + J["pert"] * pert, torch.float64)
+
+    def loss64(u):
+        r = (run(t64, u, torch.float64) - target) * mask
+        return 0.5 * torch.sum(r * r)
+
+    res = {}
+    for name, tree, dt in (("f64", t64, torch.float64), ("f32", t32, torch.float32)):
+        adj = A.Adjoint(tree, J["steps"], J["velocity"], J["cfl"], every=J["every"])
+        x = u0.to(dt).contiguous()
+        lam0 = torch.empty_like(x)
+        fw, bw = [], []
+        for rep in range(4):
+            tree.load_state_device(x.data_ptr(), P)
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            adj.forward()
+            e1.record(stream)
+            uT = torch.empty_like(x)
+            tree.download_state_device(uT.data_ptr(), P)
+            r = ((uT - target.to(dt)) * mask).contiguous()
+            torch.cuda.synchronize()
+            e1b = torch.cuda.Event(enable_timing=True)
+            e1b.record(stream)
+            adj.backward(r.data_ptr(), lam0.data_ptr())
+            e2.record(stream)
+            torch.cuda.synchronize()
+            if rep:  # first repetition warms up
+                fw.append(e0.elapsed_time(e1))
+                bw.append(e1b.elapsed_time(e2))
+        res[name] = dict(uT=uT.double(), grad=lam0.double(), r=r.double(), fw_ms=float(np.median(fw)),
+                         bw_ms=float(np.median(bw)))
+        adj.close()
+    g = res["f64"]["grad"]
+    # central finite differences of the FP64 loss along seeded directions
+    worst, errs = 0.0, []
+    for _ in range(J["directions"]):
+        v = torch.from_numpy(rng.standard_normal(u0_np.shape)).to(f"cuda:{dev}") * mask
+        fd = (loss64(u0 + J["eps"] * v) - loss64(u0 - J["eps"] * v)) / (2 * J["eps"])
+        gv = torch.sum(g * v)
+        e = float(abs(fd - gv) / abs(gv))
+        errs.append(e)
+        worst = max(worst, e)
+
+    def rel(a, b):
+        return float(torch.linalg.vector_norm((a - b)[mask]) / torch.linalg.vector_norm(b[mask]))
+
+    out = {
+        "workload": (f"adjoint: frozen 2D mesh of {P} leaves (16x16 + 1 ghost; config-2 initial field on a uniform "
+                     f"level-{J['base_level']} base adapted at step 0 up to level {J['max_level']}), velocity "
+                     f"{J['velocity']}, CFL {J['cfl']}, {J['steps']} steps, checkpoint every {J['every']}; loss "
+                     f"0.5||u_T - u_target||^2, u_target = the solver's image of u_0 + {J['pert']} x seeded noise"),
+        "leaves": P,
+        "cost_ratio_fp64": res["f64"]["bw_ms"] / res["f64"]["fw_ms"],
+        "cost_ratio_fp32": res["f32"]["bw_ms"] / res["f32"]["fw_ms"],
+        "forward_ms": {"f64": res["f64"]["fw_ms"], "f32": res["f32"]["fw_ms"]},
+        "backward_ms": {"f64": res["f64"]["bw_ms"], "f32": res["f32"]["bw_ms"]},
+        "fd_check": {"directions": J["directions"], "eps": J["eps"], "max_rel_err": worst,
+                     "median_rel_err": float(np.median(errs)), "bar": 1e-6, "within_bar": bool(worst <= 1e-6),
+                     "precision": "FP64 forward and adjoint"},
+        "fp32": {"rel_l2_uT_vs_fp64": rel(res["f32"]["uT"], res["f64"]["uT"]),
+                 "rel_l2_grad_vs_fp64": rel(res["f32"]["grad"], g)},
+        "cost_bar": 3.0,
+    }
+    if with_oracle:
+        from oracle import oracle as O
+
+        O.build()
+        O.set_threads(os.cpu_count() or 1)
+        o = O.OracleTree(2, n, h, J["depth"], 40000)
+        o.refine_all(J["base_level"])
+        for f in log:
+            assert o.reconstruct(f) == 0
+        assert np.array_equal(o.ids(), ids)
+        o.set_state(u0_np)
+        o.halo_exchange()
+        t0 = time.perf_counter()
+        ref = o.adjoint(J["steps"], J["velocity"], J["cfl"], res["f64"]["r"].cpu().numpy())
+        secs = time.perf_counter() - t0
+        ref_t = torch.from_numpy(ref).to(f"cuda:{dev}")
+        out["oracle_reference_gradient"] = {"rel_l2_gpu_fp64": rel(g, ref_t), "rel_l2_gpu_fp32": rel(res["f32"]["grad"], ref_t),
+                                            "cpu_seconds": secs, "threads": os.cpu_count() or 1}
+    t64.close()
+    t32.close()
+    return out
+
+
 def uniform_extra(A, torch, stream, dtype, level=9, steps=40):
     """Kernel-level figure on an HBM-sized input: uniform 2D tree of 4^level
     leaves (16x16 + 1 ghost), fused update only (no re-mesh), per-launch
@@ -497,6 +636,7 @@ def gpu_arm(args, rank, world):
     extras = {}
     if not args.no_extras:
         extras["plain_fp64_config2"] = plain_config2(args, torch, A, dev, stream, flush, world)
+        extras["adjoint"] = adjoint_extra(torch, A, dev, stream, with_oracle=not args.no_cpu_baseline)
         if args.uniform:
             lv = args.uniform_level
             extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)

@@ -109,6 +109,12 @@ def lib():
         L.amr_tree_set_timing.argtypes = [vp, i32]
         L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.amr_tree_set_instance_params.argtypes = [vp, vp, vp, sz]
+        L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
+        L.amr_adjoint_destroy.argtypes = [vp]
+        L.amr_adjoint_forward.argtypes = [vp]
+        L.amr_adjoint_backward.argtypes = [vp, vp, vp]
+        L.amr_adjoint_checkpoint.argtypes = [vp, sz, vp]
+        L.amr_adjoint_checkpoint_count.argtypes = [vp, C.POINTER(sz)]
         L.amr_tree_refine_to_levels.argtypes = [vp, vp, sz]
         L.amr_tree_instance_offsets.argtypes = [vp, vp, sz]
         L.amr_tree_instance_time.argtypes = [vp, vp, vp, sz]
@@ -327,6 +333,46 @@ class Tree:
 
     def synchronize(self):
         check(lib().amr_tree_synchronize(self._h))
+
+
+class Adjoint:
+    """Discrete adjoint of Tree.advance(steps, velocity, cfl, remaining) on
+    the tree's current (frozen) mesh, with a checkpoint every `every` steps.
+
+        adj = Adjoint(tree, 400, (1.0, 0.5), 0.4, every=20)
+        adj.forward()                           # u_0 (tree state) -> u_T
+        adj.backward(lam_T_ptr, lam_0_ptr)      # device pointers
+
+    velocity None: the per-instance velocities of set_instance_params."""
+
+    def __init__(self, tree, steps, velocity, cfl, remaining=1.7976931348623157e308, every=20):
+        self.tree = tree
+        h = C.c_void_p()
+        v = None if velocity is None else _vec3(velocity)
+        check(lib().amr_adjoint_create(tree._h, steps, v, cfl, remaining, every, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().amr_adjoint_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def forward(self):
+        check(lib().amr_adjoint_forward(self._h))
+
+    def backward(self, lam_T_ptr, lam_0_ptr):
+        check(lib().amr_adjoint_backward(self._h, C.c_void_p(lam_T_ptr), C.c_void_p(lam_0_ptr)))
+
+    def checkpoint(self, index, dst_ptr):
+        check(lib().amr_adjoint_checkpoint(self._h, index, C.c_void_p(dst_ptr)))
+
+    @property
+    def checkpoints(self) -> int:
+        n = C.c_size_t()
+        check(lib().amr_adjoint_checkpoint_count(self._h, C.byref(n)))
+        return n.value
 
 
 # ------------------------------------------------------------ initial data

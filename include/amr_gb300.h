@@ -281,6 +281,44 @@ amr_status amr_tree_instance_offsets(amr_tree* t, uint64_t* offsets, size_t inst
  * amr_tree_advance/amr_tree_run started. */
 amr_status amr_tree_instance_time(amr_tree* t, double* sum_dt, uint32_t* executed_steps, size_t instances);
 
+/* ------------------------------------------------------------ adjoint
+ * Discrete adjoint of amr_tree_advance on a frozen mesh (no counterpart in
+ * the reference; it differentiates the reference's flux update
+ * (amr_solver.hpp:265-353), halo fill (patch_utils.hpp:162-441) and forward
+ * Euler integrator).  The map from the interior of u_0 to the interior of
+ * u_T is linear; amr_adjoint_backward applies its transpose, step by step in
+ * reverse order: the transposed flux update (upwind -> downwind) and the
+ * transposed halo rules (copy, restriction mean, injection), with the step
+ * sizes of the forward run.
+ *
+ * amr_adjoint_forward runs the steps from the tree's current state (the
+ * kernels of amr_tree_advance, velocity and CFL of create, or the
+ * per-instance velocities when velocity3 is NULL) and stores a checkpoint
+ * every checkpoint_every steps: the state and the step sizes of the segment.
+ * The reverse sweep walks the segments from the last to the first and
+ * rebuilds each segment's step coefficients from its checkpoint; the
+ * transposed update of linear advection reads no forward state, so the
+ * checkpointed states are not recomputed step by step (they remain
+ * available through amr_adjoint_checkpoint).  Memory: (steps /
+ * checkpoint_every + 1) states.  Any re-mesh of the tree after create makes
+ * forward/backward fail with AMR_ERR_INVALID. */
+typedef struct amr_adjoint amr_adjoint;
+amr_status amr_adjoint_create(amr_tree* t, size_t steps, const double* velocity3, double cfl,
+                              double remaining_time, size_t checkpoint_every, amr_adjoint** out);
+amr_status amr_adjoint_destroy(amr_adjoint* a);
+amr_status amr_adjoint_forward(amr_adjoint* a);
+/* lambda_T, lambda_0: device buffers of size() padded patches of the tree's
+ * dtype.  lambda_0 = d<lambda_T, u_T>/d u_0 on interior cells (the ghost
+ * entries of lambda_T are ignored; those of lambda_0 are zero). */
+amr_status amr_adjoint_backward(amr_adjoint* a, const void* device_lambda_T, void* device_lambda_0);
+/* The same with host buffers (copied through the adjoint's own device
+ * buffers). */
+amr_status amr_adjoint_backward_host(amr_adjoint* a, const void* host_lambda_T, void* host_lambda_0);
+/* State at step index * checkpoint_every (index 0 = u_0; the last index
+ * holds u_T), copied to a device buffer. */
+amr_status amr_adjoint_checkpoint(amr_adjoint* a, size_t index, void* device_dst);
+amr_status amr_adjoint_checkpoint_count(const amr_adjoint* a, size_t* count);
+
 /* Per-launch timing of the fused update kernel with CUDA events on the tree's
  * stream (the counterpart of the reference's profiler ranges,
  * include/cuda/profiler.hpp:7-30).  get_timing synchronizes, returns the

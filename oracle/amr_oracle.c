@@ -983,6 +983,179 @@ double oracle_advance(oracle_tree* t, size_t steps, const double* v, double cfl,
     return acc;
 }
 
+/* ------------------------------------------------------------- adjoint */
+/* Transpose of one oracle step (time_step: flux update on exchanged ghosts,
+ * then the halo fill of the new state), written as a scatter from the
+ * forward loops so it is independent of the GPU's gather form.  As a linear
+ * map of the padded input, time_step's cell update is
+ *   out = uc - sum_d k_d [0.5 (v-|v|) uR + |v| uc - 0.5 (v+|v|) uL],
+ * k_d = dt / cs_d (the Rusanov flux of AdvectionPhysics.hpp:45-66 expanded),
+ * and halo_one's ghost = copy / mean of 2^rank fine cells / injection.
+ * lam_in: adjoint of the state after the step (interior cells; ghost entries
+ * ignored); lam_out: adjoint of the state before it, interior cells, ghost
+ * entries zero.  The initial state's ghosts are the halo fill of its
+ * interior (oracle_init_state + oracle_halo_exchange), so the halo transpose
+ * applies before every step, the first included. */
+static void adjoint_step(oracle_tree* t, const double* v, double dt, const double* lam_in, double* lam_out)
+{
+    const int    rank = t->rank, n = t->n, h = t->h;
+    const size_t P1 = t->pad1;
+    const size_t stride[3] = { 1, P1, P1 * P1 };
+    const long   np = (long)t->size;
+    memset(lam_out, 0, t->size * t->flat * sizeof(double));
+    /* flux update transposed: scatter within each padded patch */
+#pragma omp parallel for schedule(static) if (np > 16) num_threads(g_threads > 0 ? g_threads : 1)
+    for (long pi = 0; pi < np; ++pi) {
+        const size_t  p = (size_t)pi;
+        double        cs[3];
+        cell_sizes(t, t->ids[p], cs);
+        const double* li_in = lam_in + p * t->flat;
+        double*       lo    = lam_out + p * t->flat;
+        int           idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    size_t li = 0;
+                    for (int k = 0; k < rank; ++k) li = li * P1 + (size_t)idx[k];
+                    const double w  = li_in[li];
+                    double       cc = 1.0;
+                    for (int d = 0; d < rank; ++d) {
+                        const double k_d = dt / cs[d], sp = fabs(v[d]);
+                        cc -= k_d * sp;
+                        lo[li + stride[d]] += -k_d * 0.5 * (v[d] - sp) * w;
+                        lo[li - stride[d]] += k_d * 0.5 * (v[d] + sp) * w;
+                    }
+                    lo[li] += cc * w;
+                }
+    }
+    /* halo fill transposed: every face ghost passes its adjoint to the cells
+     * it was filled from (halo_one's loops), then is cleared */
+    for (size_t i = 0; i < t->size; ++i) {
+        double* self = lam_out + i * t->flat;
+        for (int d = 0; d < t->ndir; ++d) {
+            const oracle_neighbor* nb = &t->nb[i * t->ndir + d];
+            const int              dim = dir_dim(d), pos = dir_pos(d);
+            int                    lo[3], hi[3], idx[3] = { 0, 0, 0 };
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = 0;
+                hi[k] = 1;
+            }
+            for (int k = 0; k < rank; ++k) {
+                if (k != dim) {
+                    lo[k] = h;
+                    hi[k] = n + h;
+                } else {
+                    lo[k] = pos ? n + h : 0;
+                    hi[k] = pos ? n + 2 * h : h;
+                }
+            }
+            int     ok = 1;
+            double* other[4] = { 0, 0, 0, 0 };
+            if (nb->kind == NB_SAME || nb->kind == NB_COARSER)
+                other[0] = lam_out + index_of(t, nb->ids[0], &ok) * t->flat;
+            else if (nb->kind == NB_FINER)
+                for (int k = 0; k < t->nf; ++k) other[k] = lam_out + index_of(t, nb->ids[k], &ok) * t->flat;
+            for (idx[0] = lo[0]; idx[0] < hi[0]; ++idx[0])
+                for (idx[1] = lo[1]; idx[1] < hi[1]; ++idx[1])
+                    for (idx[2] = lo[2]; idx[2] < hi[2]; ++idx[2]) {
+                        size_t to = 0;
+                        for (int k = 0; k < rank; ++k) to = to * P1 + (size_t)idx[k];
+                        const double gadj = self[to];
+                        self[to]          = 0.0;
+                        if (nb->kind == NB_NONE) continue;
+                        if (nb->kind == NB_SAME) {
+                            int from[3] = { idx[0], idx[1], idx[2] };
+                            from[dim] += pos ? -n : n;
+                            size_t f = 0;
+                            for (int k = 0; k < rank; ++k) f = f * P1 + (size_t)from[k];
+                            other[0][f] += gadj;
+                        } else if (nb->kind == NB_FINER) {
+                            int base[3] = { idx[0], idx[1], idx[2] };
+                            base[dim] += pos ? -n : n;
+                            int fpi = 0, str = 1;
+                            for (int k = 0; k < rank; ++k) {
+                                base[k] = ((base[k] - h) * 2) % n + h;
+                                if (k != dim) {
+                                    fpi += ((idx[k] - h) / (n / 2)) * str;
+                                    str *= 2;
+                                }
+                            }
+                            size_t b = 0;
+                            for (int k = 0; k < rank; ++k) b = b * P1 + (size_t)base[k];
+                            double* fp = other[fpi];
+                            if (rank == 2) {
+                                fp[b] += gadj / 4.0;
+                                fp[b + 1] += gadj / 4.0;
+                                fp[b + P1] += gadj / 4.0;
+                                fp[b + P1 + 1] += gadj / 4.0;
+                            } else {
+                                const size_t s0 = P1 * P1;
+                                for (int a = 0; a < 2; ++a)
+                                    for (int bb = 0; bb < 2; ++bb)
+                                        for (int c = 0; c < 2; ++c) fp[b + a * s0 + bb * P1 + c] += gadj / 8.0;
+                            }
+                        } else {
+                            int from[3] = { idx[0], idx[1], idx[2] };
+                            from[dim] += pos ? -n : n;
+                            for (int k = 0; k < rank; ++k) {
+                                const int fine = from[k] - h;
+                                from[k]        = h + nb->quadrant[k] * (n / 2) + fine / 2;
+                            }
+                            size_t f = 0;
+                            for (int k = 0; k < rank; ++k) f = f * P1 + (size_t)from[k];
+                            other[0][f] += gadj;
+                        }
+                    }
+        }
+    }
+}
+
+/* Gradient of <lam_T, u_T> with respect to the interior of u_0 for
+ * oracle_advance(steps, v, cfl, remaining) started from the tree's current
+ * (frozen) mesh: the step sizes of the forward run, then the transposed
+ * steps in reverse order.  Returns the number of executed steps. */
+size_t oracle_adjoint(oracle_tree* t, size_t steps, const double* v, double cfl, double remaining,
+                      const double* lam_T, double* lam_0)
+{
+    double* dts = (double*)malloc((steps ? steps : 1) * sizeof(double));
+    size_t  ex  = 0;
+    for (size_t s = 0; s < steps; ++s) { /* oracle_advance's step sizes */
+        if (remaining <= 0.0) break;
+        const double dt      = oracle_compute_dt(t, v, cfl);
+        const double step_dt = dt < remaining ? dt : remaining;
+        if (step_dt <= 0.0) break;
+        dts[ex++] = step_dt;
+        remaining -= step_dt;
+    }
+    const size_t bytes = t->size * t->flat * sizeof(double);
+    double*      a     = (double*)malloc(bytes);
+    double*      b     = (double*)malloc(bytes);
+    memcpy(a, lam_T, bytes);
+    /* ghost entries of the terminal adjoint are not part of the interior map */
+    const int rank = t->rank, n = t->n, h = t->h;
+    for (size_t i = 0; i < t->size * t->flat; ++i) {
+        size_t r = i % t->flat;
+        int    inside = 1;
+        for (int k = rank - 1; k >= 0; --k) {
+            const int c = (int)(r % t->pad1);
+            r /= t->pad1;
+            inside = inside && c >= h && c < n + h;
+        }
+        if (!inside) a[i] = 0.0;
+    }
+    for (size_t s = ex; s-- > 0;) {
+        adjoint_step(t, v, dts[s], a, b);
+        double* tmp = a;
+        a           = b;
+        b           = tmp;
+    }
+    memcpy(lam_0, a, bytes);
+    free(a);
+    free(b);
+    free(dts);
+    return ex;
+}
+
 /* ------------------------------------------------------------ criteria */
 /* max|grad u|*h with central differences over face ghosts and the any/all
  * patch rule of dg_helpers/globals/amr_indicators.hpp:186-225; level bounds

@@ -70,6 +70,11 @@ void oracle_random_state(oracle_tree* t, uint64_t seed);
 double oracle_compute_dt(const oracle_tree* t, const double* velocity, double cfl);
 double oracle_advance(oracle_tree* t, size_t steps, const double* velocity,
                       double cfl, double remaining, size_t* executed);
+/* Gradient of <lam_T, u_T> w.r.t. the interior of u_0 for oracle_advance on
+ * the current (frozen) mesh: transposed steps in reverse order (size*flat
+ * padded buffers; ghost entries of lam_0 are zero).  Returns executed steps. */
+size_t oracle_adjoint(oracle_tree* t, size_t steps, const double* velocity, double cfl, double remaining,
+                      const double* lam_T, double* lam_0);
 
 /* Hash shared by oracle, fixtures and product initialiser. */
 double oracle_unit_hash(uint64_t a, uint64_t b, uint64_t c);

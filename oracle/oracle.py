@@ -61,6 +61,9 @@ def lib():
         L.oracle_compute_dt.argtypes = [vp, P(np.float64, flags="C"), dbl]
         L.oracle_advance.restype = dbl
         L.oracle_advance.argtypes = [vp, sz, P(np.float64, flags="C"), dbl, dbl, C.POINTER(sz)]
+        L.oracle_adjoint.restype = sz
+        L.oracle_adjoint.argtypes = [vp, sz, P(np.float64, flags="C"), dbl, dbl, P(np.float64, flags="C"),
+                                     P(np.float64, flags="C")]
         L.oracle_unit_hash.restype = dbl
         L.oracle_unit_hash.argtypes = [u64, u64, u64]
         L.oracle_encode.restype = u64
@@ -166,6 +169,17 @@ class OracleTree:
         ex = C.c_size_t(0)
         acc = lib().oracle_advance(self._t, steps, v, cfl, remaining, C.byref(ex))
         return acc, ex.value
+
+
+    def adjoint(self, steps, velocity, cfl, lam_T, remaining=1.7976931348623157e308):
+        """Gradient of <lam_T, u_T> w.r.t. the interior of the current state
+        for advance(steps, velocity, cfl, remaining) on the frozen mesh."""
+        v = np.zeros(3)
+        v[: len(velocity)] = velocity
+        lt = np.ascontiguousarray(lam_T, np.float64).reshape(-1)
+        out = np.zeros_like(lt)
+        lib().oracle_adjoint(self._t, steps, v, cfl, remaining, lt, out)
+        return out.reshape((self.size,) + (self.pad1,) * self.rank)
 
 
 def set_threads(n: int) -> None:

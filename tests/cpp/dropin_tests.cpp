@@ -13,6 +13,7 @@
 #include "ndtree/ndtree.hpp"
 #include "ndtree/patch_layout.hpp"
 #include "solver/AdvectionPhysics.hpp"
+#include "solver/adjoint.hpp"
 #include "solver/amr_solver.hpp"
 #include "solver/cell_types.hpp"
 #include "solver/physics_system.hpp"
@@ -223,10 +224,62 @@ int bench_loop(int argc, char** argv)
     return 0;
 }
 
+// The adjoint through the C++ header: dot-product identity
+// <lambda_T, A u_0> = <A^T lambda_T, u_0> over interior cells on a 2:1 mesh.
+static int adjoint_check()
+{
+    amr_tree_desc d{};
+    d.geom.rank = 2;
+    d.geom.n = 16;
+    d.geom.halo = 1;
+    d.geom.depth = 6;
+    d.geom.lengths[0] = d.geom.lengths[1] = d.geom.lengths[2] = 1.0;
+    d.capacity = 4096;
+    d.dtype    = AMR_F64;
+    amr_tree* t = nullptr;
+    amr::gb300::check(amr_tree_create(&d, &t));
+    amr::gb300::check(amr_tree_refine_uniform(t, 2));
+    std::size_t P = 0, flat = 0;
+    amr::gb300::check(amr_tree_size(t, &P));
+    std::vector<std::int8_t> f(P, 0);
+    f[0] = f[5] = f[9] = 1;
+    amr::gb300::check(amr_tree_set_flags(t, f.data(), P));
+    int changed = 0;
+    amr::gb300::check(amr_tree_remesh(t, &changed));
+    amr::gb300::check(amr_tree_size(t, &P));
+    amr::gb300::check(amr_tree_patch_cells(t, &flat));
+    std::vector<double> u0(P * flat), lt(P * flat), l0(P * flat), ut(P * flat);
+    for (std::size_t i = 0; i < u0.size(); ++i) {
+        u0[i] = unit_hash(1, i, 0) - 0.5;
+        lt[i] = unit_hash(2, i, 0) - 0.5;
+    }
+    amr::gb300::check(amr_tree_upload_state(t, u0.data(), P));
+    double lhs = 0.0, rhs = 0.0;
+    {
+        amr::gb300::adjoint adj(t, 17, { 1.0, -0.5, 0.0 }, 0.4, 5);
+        adj.forward();
+        amr::gb300::check(amr_tree_download_state(t, ut.data(), P));
+        adj.backward_host(lt.data(), l0.data());
+        if (adj.checkpoints() != 5) ++g_failures;
+    }
+    for (std::size_t p = 0; p < P; ++p)
+        for (int r = 1; r <= 16; ++r)
+            for (int c = 1; c <= 16; ++c) {
+                const std::size_t i = p * flat + r * 18 + c;
+                lhs += lt[i] * ut[i];
+                rhs += l0[i] * u0[i];
+            }
+    EXPECT_NEAR(lhs, rhs, 1e-12 * std::abs(lhs));
+    amr_tree_destroy(t);
+    std::cout << (g_failures ? "FAILED" : "PASSED") << " " << g_failures << "\n";
+    return g_failures ? 1 : 0;
+}
+
 int main(int argc, char** argv)
 {
     const std::string mode = argc > 1 ? argv[1] : "tests";
     if (mode == "bench") return bench_loop(argc, argv);
+    if (mode == "adjoint") return adjoint_check();
     PulseCenterMovement<AdvectionTestConfig<2, 10>>();
     PulseCenterMovement<AdvectionTestConfig<2, 50>>();
     PulseCenterMovementAMR<AdvectionTestConfig<2, 10>>();

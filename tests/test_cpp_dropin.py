@@ -55,3 +55,12 @@ def test_benchmark_loop_through_dropin_matches_reference(dropin_exe):
     assert steps == int(z["steps"]) and sum_dt == float(z["sum_dt"])
     np.testing.assert_array_equal(ids, z["final_ids"])
     assert rel_l2(u, z["state_final"].reshape(-1)) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_adjoint_through_cpp_header(dropin_exe):
+    """amr::gb300::adjoint (solver/adjoint.hpp): dot-product identity of the
+    discrete adjoint on a 2:1 mesh, host buffers."""
+    r = subprocess.run([str(dropin_exe), "adjoint"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "PASSED" in r.stdout
