@@ -44,6 +44,7 @@ struct RunBufs {
     int32_t*       maxlev;     // per instance, read by the step prologue
     int32_t*       maxlev_new; // per instance, filled by emit, zero between re-meshes
     const double*  vel;        // per instance x3, or null (launch-wide upwind sides)
+    const int32_t* upcode;     // per instance packed upwind offsets (with vel), or null
     const int32_t* bounds;     // per instance (min, max) level bounds, or null
     uint32_t*      tile_sums;  // scan partials, one per tile
     unsigned long long cap;
@@ -57,7 +58,8 @@ constexpr int kScanTile    = kScanThreads * kScanPer;
 // ---------------------------------------------------------------- steps
 template <typename T, int N, int H, int W, int S>
 __global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int parity, int upx0, int upy0)
+k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+             int parity, int upx0, int upy0)
 {
     if (ctl->err) return;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -68,7 +70,7 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int p
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     step2d_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P, g,
-                            coef, upx0, upy0, &ctl->err, B.keys[tb], B.vel, tiles, bars, p, nwarp);
+                            coef, coef32, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars, p, nwarp);
 }
 
 // Any geometry: ppb patches per block per round, grid-stride over rounds.

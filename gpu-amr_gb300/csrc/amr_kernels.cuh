@@ -65,7 +65,15 @@ __device__ __forceinline__ int instance_of(const Geo& g, const uint64_t* keys, i
 
 // Upwind offset per Morton axis from the sign of the velocity: -1 when the
 // flow comes from the lower side, +1 from the upper side, 0 at rest.
-__device__ __forceinline__ int upwind(double v) { return v > 0.0 ? -1 : (v < 0.0 ? 1 : 0); }
+__host__ __device__ __forceinline__ int upwind(double v) { return v > 0.0 ? -1 : (v < 0.0 ? 1 : 0); }
+
+// The upwind offsets of a velocity packed in one int (2 bits per axis,
+// offset + 1), and unpacked.
+__host__ __device__ __forceinline__ int32_t pack_upwind(const double* v)
+{
+    return (upwind(v[0]) + 1) | ((upwind(v[1]) + 1) << 2) | ((upwind(v[2]) + 1) << 4);
+}
+__host__ __device__ __forceinline__ int unpack_upwind(int32_t code, int axis) { return ((code >> (2 * axis)) & 3) - 1; }
 
 __device__ inline void interior_coords(const Geo& g, int c, int* idx)
 {
@@ -446,7 +454,8 @@ enum : int {
 // velocity; coef row (step s, instance b) starts at (s * ninst + b) * (depth+1).
 __global__ void __launch_bounds__(256)
 k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
-              int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef)
+              int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef,
+              float2* __restrict__ coef32 = nullptr, int32_t* __restrict__ upcode = nullptr)
 {
     __shared__ double dts[1024];
     const int         inst  = blockIdx.x;
@@ -482,11 +491,15 @@ k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __rest
         d.rem[inst] = rem;
         d.cnt[inst] = cnt;
     }
+    if (threadIdx.x == 0 && upcode) upcode[inst] = pack_upwind(v);
     __syncthreads();
     const int nl = g.depth + 1;
     for (int e = threadIdx.x; e < steps * nl; e += blockDim.x) {
-        const int st = e / nl, l = e % nl;
-        coef[(static_cast<size_t>(st) * ninst + inst) * nl + l] = make_coef(g, dts[st], v, l);
+        const int    st = e / nl, l = e % nl;
+        const size_t at = (static_cast<size_t>(st) * ninst + inst) * nl + l;
+        const Coef   c  = make_coef(g, dts[st], v, l);
+        coef[at]        = c;
+        if (coef32) coef32[at] = make_float2(static_cast<float>(c.c[0]), static_cast<float>(c.c[1]));
     }
 }
 
@@ -975,20 +988,40 @@ struct Step2dShape {
     static constexpr uint32_t HI    = ((N + H) * P1 * sizeof(T) + 15u) & ~15u;
     static constexpr uint32_t BYTES = HI - LO;
     static constexpr int      WORDS = BYTES / 16;
-    static constexpr int      SEG   = N * N / 32; // interior cells per lane
+    // Each lane updates a column segment: column (lane % N), rows
+    // (lane / N) * SEG .. + SEG - 1 (interior coordinates).  For a fixed row
+    // offset the warp reads whole rows, so shared-memory accesses are free of
+    // bank conflicts, and the y-neighbours of a lane's cells are its own
+    // registers.
+    static constexpr int      RG    = 32 / N;      // row groups
+    static constexpr int      SEG   = N * N / 32;  // interior cells per lane
     static constexpr size_t   TILE  = FLAT * sizeof(T);
     static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
-    static_assert((N * N) % 32 == 0 && N % SEG == 0, "a lane's cells must stay within one row");
+    static_assert(32 % N == 0 && RG * SEG == N, "a lane's cells must form one column segment");
     // dynamic shared memory of a block of W warps with S tiles each
     static constexpr size_t smem(int W, int S) { return static_cast<size_t>(W) * S * (TILE + 8); }
 };
 
+// Coefficients of one (step, instance, level) row as the 2D kernel reads
+// them: FP32 needs only (c_x, c_y) (difference form), FP64 (c0, c_x, c_y).
+template <typename T>
+struct Coef2 {
+    double c0, cx, cy;
+};
+template <>
+struct Coef2<float> {
+    float cx, cy;
+};
+
+// coef: the full rows (FP64 path); coef32: (c_x, c_y) rows (FP32 path);
+// upcode: per-instance packed upwind offsets, or nullptr for upx0/upy0.
 template <typename T, int N, int H, int S>
 __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restrict__ out,
                                             const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
-                                            const Coef* __restrict__ coef, int upx0, int upy0, int32_t* err,
-                                            const uint64_t* __restrict__ keys, const double* __restrict__ vel,
-                                            T* tiles, uint64_t* bars, int p, int nwarp)
+                                            const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+                                            int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
+                                            const int32_t* __restrict__ upcode, T* tiles, uint64_t* bars, int p,
+                                            int nwarp)
 {
     using Sh                = Step2dShape<T, N, H>;
     constexpr int      P1   = Sh::P1;
@@ -1014,7 +1047,7 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         for (int j = 0; j < S - 1; ++j)
             if (p + j * nwarp < P) request(p + j * nwarp, j);
     uint32_t  phase = 0; // bit b: parity of slot b's next completion
-    const int i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
+    const int cl = lane % N + H, r0 = (lane / N) * SEG + H; // this lane's column and first row
     const int nl = g.depth + 1;
 
     // Ghost job of this lane: lanes 0..N-1 the upwind ghost column (normal
@@ -1032,8 +1065,8 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     // raw ghost source values one ahead.  The instance comes from the key;
     // the upwind sides from its velocity (vel != nullptr) or upx0/upy0.
     struct Side {
-        int ux, uy;
-        Coef cf;
+        int      ux, uy;
+        Coef2<T> cf;
     };
     struct Rec {
         int rel, nb, fid, q0, q1;
@@ -1046,11 +1079,22 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
         sd.ux          = upx0;
         sd.uy          = upy0;
-        if (vel) {
-            sd.ux = upwind(vel[3 * inst]);
-            sd.uy = upwind(vel[3 * inst + 1]);
+        if (upcode) {
+            const int32_t code = upcode[inst];
+            sd.ux              = unpack_upwind(code, 0);
+            sd.uy              = unpack_upwind(code, 1);
         }
-        sd.cf = coef[inst * nl + key_level(key)];
+        const int row = inst * nl + key_level(key);
+        if constexpr (sizeof(T) == 4) {
+            const float2 c = coef32[row];
+            sd.cf.cx       = c.x;
+            sd.cf.cy       = c.y;
+        } else {
+            const Coef& c = coef[row];
+            sd.cf.c0      = c.c0;
+            sd.cf.cx      = c.c[0];
+            sd.cf.cy      = c.c[1];
+        }
     };
     auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
     auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
@@ -1066,32 +1110,30 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     };
     // The halo rules of ghost_value for one 2D face ghost cell, split into
     // issuing the source loads and combining them.
+    // (the source address is formed with selects so lanes with different
+    // relations do not diverge; only the three extra loads of the mean are
+    // predicated)
     auto fetch = [&](int q, const Side& sd, const Rec& m, Raw& raw) {
         raw.kind = 0;
         if (!has_job(sd)) return;
-        const int pos = pos_of(sd);
-        const int gc  = pos ? N + H : H - 1;
-        const int G0 = col ? tg : gc, G1 = col ? gc : tg;
-        const int sh = pos ? -N : N;
-        int       f0 = G0 + (L == 0 ? sh : 0), f1 = G1 + (L == 1 ? sh : 0);
-        raw.kind     = 1;
-        if (m.rel == REL_SAME) {
-            raw.v[0] = in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
-        } else if (m.rel == REL_COARSER) {
-            f0       = H + m.q0 * HALF + (f0 - H) / 2;
-            f1       = H + m.q1 * HALF + (f1 - H) / 2;
-            raw.v[0] = in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
-        } else if (m.rel == REL_FINER) {
-            f0          = ((f0 - H) * 2) % N + H;
-            f1          = ((f1 - H) * 2) % N + H;
-            const T* fp = in + static_cast<size_t>(m.fid) * FLAT + f0 * P1 + f1;
-            raw.v[0]    = fp[0];
-            raw.v[1]    = fp[1];
-            raw.v[2]    = fp[P1];
-            raw.v[3]    = fp[P1 + 1];
-            raw.kind    = 4;
-        } else { // relation none: the buffer's own ghost value
-            raw.v[0] = in[static_cast<size_t>(q) * FLAT + G0 * P1 + G1];
+        const int  pos = pos_of(sd);
+        const int  gc  = pos ? N + H : H - 1;
+        const int  G0 = col ? tg : gc, G1 = col ? gc : tg;
+        const int  sh = pos ? -N : N;
+        const int  s0 = G0 + (L == 0 ? sh : 0), s1 = G1 + (L == 1 ? sh : 0); // same-level source
+        const bool same = m.rel == REL_SAME, coarser = m.rel == REL_COARSER, finer = m.rel == REL_FINER;
+        const int  c0 = H + m.q0 * HALF + (s0 - H) / 2, c1 = H + m.q1 * HALF + (s1 - H) / 2;
+        const int  d0 = ((s0 - H) * 2) % N + H, d1 = ((s1 - H) * 2) % N + H;
+        const int  f0 = same ? s0 : coarser ? c0 : finer ? d0 : G0;
+        const int  f1 = same ? s1 : coarser ? c1 : finer ? d1 : G1;
+        const int  src = (same || coarser) ? m.nb : finer ? m.fid : q;
+        const T*   fp  = in + static_cast<size_t>(src) * FLAT + f0 * P1 + f1;
+        raw.v[0]       = fp[0];
+        raw.kind       = finer ? 4 : 1;
+        if (finer) {
+            raw.v[1] = fp[1];
+            raw.v[2] = fp[P1];
+            raw.v[3] = fp[P1 + 1];
         }
     };
     auto combine = [&](const Raw& raw) -> T {
@@ -1158,35 +1200,42 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         if (has) tile[G0 * P1 + G1] = gv;
         __syncwarp();
         const int ux = sd0.ux, uy = sd0.uy;
-        T         res[SEG];
+        // the lane's column, rows r0-1 .. r0+SEG (the end rows are the
+        // neighbouring segments' cells or the upwind ghost row)
+        T colv[SEG + 2];
+#pragma unroll
+        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+        T res[SEG];
         if constexpr (sizeof(T) == 4) {
             // FP32: u + c (u_up - u), exact for a constant state, so the
             // rounding of the coefficients does not bias the solution
-            const float cx = static_cast<float>(sd0.cf.c[0]), cy = static_cast<float>(sd0.cf.c[1]);
+            const float cx = sd0.cf.cx, cy = sd0.cf.cy;
 #pragma unroll
             for (int k = 0; k < SEG; ++k) {
-                const int   idx = r * P1 + c0 + k;
-                const float u   = tile[idx];
+                const float u   = colv[k + 1];
+                const float xn  = tile[(r0 + k) * P1 + cl + ux];
+                const float yn  = uy < 0 ? colv[k] : colv[k + 2];
                 float       acc = u;
-                if (ux != 0) acc = fmaf(cx, tile[idx + ux] - u, acc);
-                if (uy != 0) acc = fmaf(cy, tile[idx + uy * P1] - u, acc);
+                if (ux != 0) acc = fmaf(cx, xn - u, acc);
+                if (uy != 0) acc = fmaf(cy, yn - u, acc);
                 res[k] = acc;
             }
         } else {
-            const T c00 = static_cast<T>(sd0.cf.c0), cx = static_cast<T>(sd0.cf.c[0]),
-                    cy = static_cast<T>(sd0.cf.c[1]);
+            const T c00 = static_cast<T>(sd0.cf.c0), cx = static_cast<T>(sd0.cf.cx), cy = static_cast<T>(sd0.cf.cy);
 #pragma unroll
             for (int k = 0; k < SEG; ++k) {
-                const int idx = r * P1 + c0 + k;
-                T         acc = c00 * tile[idx];
-                if (ux != 0) acc = fma(cx, tile[idx + ux], acc);
-                if (uy != 0) acc = fma(cy, tile[idx + uy * P1], acc);
+                const T u   = colv[k + 1];
+                const T xn  = tile[(r0 + k) * P1 + cl + ux];
+                const T yn  = uy < 0 ? colv[k] : colv[k + 2];
+                T       acc = c00 * u;
+                if (ux != 0) acc = fma(cx, xn, acc);
+                if (uy != 0) acc = fma(cy, yn, acc);
                 res[k] = acc;
             }
         }
         __syncwarp();
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) tile[r * P1 + c0 + k] = res[k];
+        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
         __syncwarp();
         const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
         uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
@@ -1222,8 +1271,8 @@ struct Step2dOcc {
 template <typename T, int N, int H, int W, int S>
 __global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
 k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
-         const Coef* __restrict__ coef, int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
-         const double* __restrict__ vel)
+         const Coef* __restrict__ coef, const float2* __restrict__ coef32, int upx0, int upy0, int32_t* err,
+         const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     T*        tiles;
@@ -1231,7 +1280,7 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __r
     step2d_smem<T, N, H, W, S>(smem, tiles, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_body<T, N, H, S>(in, out, meta, P, g, coef, upx0, upy0, err, keys, vel, tiles, bars, p, nwarp);
+    step2d_body<T, N, H, S>(in, out, meta, P, g, coef, coef32, upx0, upy0, err, keys, upcode, tiles, bars, p, nwarp);
 }
 
 } // namespace amr_gb300
@@ -1257,6 +1306,7 @@ struct Flags2dShape {
     static constexpr int      SEG   = N * N / 32;
     static constexpr size_t   TILE  = FLAT * sizeof(T);
     static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
+    static_assert(32 % N == 0 && (32 / N) * SEG == N, "a lane's cells must form one column segment");
     static constexpr size_t smem(int W) { return static_cast<size_t>(W) * 2 * (TILE + 8); }
 };
 
@@ -1315,7 +1365,8 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
     };
     if (p < P && lane == 0) request(p, 0);
     uint32_t   phase = 0;
-    const int  i0 = lane * SEG, r = i0 / N + H, c0 = i0 % N + H;
+    // column-segment mapping (conflict-free shared memory, see Step2dShape)
+    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
     // ghost jobs: lanes 0..N-1 column faces (normal layout dim 1) at row tg,
     // lanes N..2N-1 row faces (dim 0) at column tg; pos 0 and 1
     const bool col  = lane < N;
@@ -1397,10 +1448,13 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
         }
         __syncwarp();
         int any = 0, all = 1;
+        T   colv[SEG + 2];
+#pragma unroll
+        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
-            const int idx = r * P1 + c0 + k;
-            const T   xl = tile[idx - 1], xh = tile[idx + 1], yl = tile[idx - P1], yh = tile[idx + P1];
+            const int idx = (r0 + k) * P1 + cl;
+            const T   xl = tile[idx - 1], xh = tile[idx + 1], yl = colv[k], yh = colv[k + 2];
             bool      done = false;
             if (rule.fast) {
                 const float s = grad_sq_f32_2<T>(xl, xh, yl, yh);

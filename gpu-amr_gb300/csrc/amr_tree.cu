@@ -178,6 +178,8 @@ struct amr_tree {
     DtState   dts() const { return DtState{ dt_acc, dt_rem, dt_cnt, dt_tot, dt_ctot }; }
     double*   step_dt = nullptr;
     Coef*     coef    = nullptr;
+    float2*   coef32  = nullptr; // (c_x, c_y) rows of the FP32 2D update
+    int32_t*  upcode  = nullptr; // per instance packed upwind offsets
     size_t    coef_steps = 0;
     bool      batch_open = false;
 
@@ -268,14 +270,14 @@ unsigned step2d_grid(int P, int grid)
 
 template <typename T, int N, int H>
 amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coef,
-                         const int* up, int32_t* err, const uint64_t* keys, const double* vel, const StepCfg& cfg,
-                         cudaStream_t s)
+                         const float2* coef32, const int* up, int32_t* err, const uint64_t* keys,
+                         const int32_t* upcode, const StepCfg& cfg, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
         const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(in, out, meta, P, g, coef,
-                                                                                      up[0], up[1], err, keys, vel);
+        k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
+            in, out, meta, P, g, coef, coef32, up[0], up[1], err, keys, upcode);
         AMR_LAUNCHED("k_step2d");
         return AMR_OK;
     });
@@ -316,9 +318,10 @@ bool lookup_tuned(const amr_tree* t, bool per_leaf, StepCfg& cfg)
 }
 
 template <typename T, int N, int H>
-amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const double* vel, StepCfg& best)
+amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, const int* up, const int32_t* upcode,
+                       StepCfg& best)
 {
-    const TuneKey key = tune_key(t, vel != nullptr);
+    const TuneKey key = tune_key(t, upcode != nullptr);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto                        it = g_tuned.find(key);
@@ -349,16 +352,16 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const int* up, const doubl
                 StepCfg   c{ W, S, grid };
                 for (int rep = 0; rep < 2; ++rep) { // warm-up
                     amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->meta[t->tb], P, t->g, coef, up,
-                                                          t->status + 7, t->keys[t->tb], vel, c, s);
+                                                          t->meta[t->tb], P, t->g, coef, coef32, up,
+                                                          t->status + 7, t->keys[t->tb], upcode, c, s);
                     if (r != AMR_OK) return r;
                 }
                 const int reps = 4;
                 AMR_CUDA(cudaEventRecord(e0, s));
                 for (int rep = 0; rep < reps; ++rep) {
                     amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->meta[t->tb], P, t->g, coef, up,
-                                                          t->status + 7, t->keys[t->tb], vel, c, s);
+                                                          t->meta[t->tb], P, t->g, coef, coef32, up,
+                                                          t->status + 7, t->keys[t->tb], upcode, c, s);
                     if (r != AMR_OK) return r;
                 }
                 AMR_CUDA(cudaEventRecord(e1, s));
@@ -438,6 +441,8 @@ void free_tree(amr_tree* t)
     cudaFree(t->dt_ctot);
     cudaFree(t->step_dt);
     cudaFree(t->coef);
+    cudaFree(t->coef32);
+    cudaFree(t->upcode);
     cudaFree(t->cstats);
     if (t->pinned) cudaFreeHost(t->pinned);
     delete t;
@@ -646,6 +651,7 @@ RunBufs run_bufs(amr_tree* t, bool per_leaf_vel, bool bounds)
     B.maxlev     = t->maxlev;
     B.maxlev_new = t->maxlev_new;
     B.vel        = per_leaf_vel ? t->vel : nullptr;
+    B.upcode     = per_leaf_vel ? t->upcode : nullptr;
     B.bounds     = bounds ? t->bounds : nullptr;
     B.tile_sums  = t->tile_sums;
     B.cap        = t->cap;
@@ -654,14 +660,14 @@ RunBufs run_bufs(amr_tree* t, bool per_leaf_vel, bool bounds)
 }
 
 template <typename T, int N, int H>
-amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, int parity, const int* up,
-                             const StepCfg& cfg, int P, cudaStream_t s)
+amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, const float2* coef32,
+                             int parity, const int* up, const StepCfg& cfg, int P, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
         const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_run_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(B, ctl, g, coef, parity,
-                                                                                          up[0], up[1]);
+        k_run_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(B, ctl, g, coef, coef32,
+                                                                                          parity, up[0], up[1]);
         AMR_LAUNCHED("k_run_step2d");
         return AMR_OK;
     });
@@ -676,17 +682,18 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     const int  K   = t->ninst, nl = g.depth + 1, sms = num_sms();
     RunCtl*    ctl = t->ctl;
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
-                                     t->coef);
+                                     t->coef, t->coef32, t->upcode);
     AMR_LAUNCHED("k_batch_begin");
     const StepCfg cfg{ key.W, key.S, key.grid };
     const int     ppb = std::max(1, 256 / g.cells);
     for (int j = 0; j < key.k; ++j) {
-        const Coef* cf = t->coef + static_cast<size_t>(j) * K * nl;
-        amr_status  st = AMR_OK;
+        const Coef*   cf  = t->coef + static_cast<size_t>(j) * K * nl;
+        const float2* cf2 = t->coef32 + static_cast<size_t>(j) * K * nl;
+        amr_status    st  = AMR_OK;
         if (key.W > 0 && g.n == 16)
-            st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+            st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
         else if (key.W > 0)
-            st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+            st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
         else {
             k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, j & 1, key.up[0], key.up[1], key.up[2], ppb);
             AMR_LAUNCHED("k_run_step");
@@ -858,12 +865,12 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         if (g.n == 16) {
             // tune on the current leaves with a coefficient table of this run
             k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, g, t->vel, p->cfl, 1, BATCH_RESET, 1.0, t->dts(), t->step_dt,
-                                            t->coef);
+                                            t->coef, t->coef32, t->upcode);
             AMR_LAUNCHED("k_batch_begin");
             int up[3] = { key.up[0], key.up[1], key.up[2] };
             amr_status ts = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
                 using T = decltype(z);
-                return tune_step2d<T, 16, 1>(t, t->coef, up, per_leaf ? t->vel : nullptr, cfg);
+                return tune_step2d<T, 16, 1>(t, t->coef, t->coef32, up, per_leaf ? t->upcode : nullptr, cfg);
             });
             if (ts != AMR_OK) return ts;
         }
@@ -1056,6 +1063,8 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->dt_ctot), K * sizeof(uint32_t));
     al(reinterpret_cast<void**>(&t->step_dt), coef_steps * K * sizeof(double));
     al(reinterpret_cast<void**>(&t->coef), coef_steps * K * nl * sizeof(Coef));
+    al(reinterpret_cast<void**>(&t->coef32), coef_steps * K * nl * sizeof(float2));
+    al(reinterpret_cast<void**>(&t->upcode), K * sizeof(int32_t));
     al(reinterpret_cast<void**>(&t->cstats), sizeof(CycleStats));
     t->pinned_bytes = std::max<size_t>(1024, 64 + (K + 1) * 32 + sizeof(RunCtl));
     if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, t->pinned_bytes);
@@ -1350,7 +1359,8 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
         AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
         t->vel_per_leaf = true;
     }
-    const double* vleaf = t->vel_per_leaf ? t->vel : nullptr;
+    const double*  vleaf = t->vel_per_leaf ? t->vel : nullptr;
+    const int32_t* uleaf = t->vel_per_leaf ? t->upcode : nullptr;
     const int P     = static_cast<int>(t->size);
     const int ppb   = std::max(1, 256 / t->g.cells);
     const unsigned grid = grid_for(P, ppb);
@@ -1358,11 +1368,11 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
     bool      first = true;
     size_t    done  = 0;
     StepCfg   cfg;
-    lookup_tuned(t, vleaf != nullptr, cfg);
+    lookup_tuned(t, uleaf != nullptr, cfg);
     while (done < steps || (first && steps == 0)) {
         const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
         k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? first_mode : BATCH_CONTINUE,
-                                        remaining, t->dts(), t->step_dt, t->coef);
+                                        remaining, t->dts(), t->step_dt, t->coef, t->coef32, t->upcode);
         AMR_LAUNCHED("k_batch_begin");
         first = false;
         for (int k = 0; k < chunk; ++k) {
@@ -1382,15 +1392,16 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
             }
             amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
                 using T        = decltype(z);
-                const Coef* cf = t->coef + static_cast<size_t>(k) * K * nl;
-                const T*    in = static_cast<const T*>(t->cur);
-                T*          out = static_cast<T*>(t->nxt);
+                const Coef*   cf  = t->coef + static_cast<size_t>(k) * K * nl;
+                const float2* cf2 = t->coef32 + static_cast<size_t>(k) * K * nl;
+                const T*      in  = static_cast<const T*>(t->cur);
+                T*            out = static_cast<T*>(t->nxt);
                 if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
-                    return launch_step2d<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, up,
-                                                   t->status + 7, t->keys[t->tb], vleaf, cfg, s);
+                    return launch_step2d<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
+                                                   t->keys[t->tb], uleaf, cfg, s);
                 if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
-                    return launch_step2d<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, up,
-                                                  t->status + 7, t->keys[t->tb], vleaf, StepCfg{}, s);
+                    return launch_step2d<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
+                                                  t->keys[t->tb], uleaf, StepCfg{}, s);
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
                                                      up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
                                                      vleaf);
