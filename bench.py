@@ -239,6 +239,7 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
         run_forest(f32)
     ms, launches, stats, clock_info = time_runs(torch, stream, world, args.steps, load32, lambda: run_forest(f32),
                                                 flush, ClockSampler(dev))
+    tuned = f32.step_config()
     cells = sum(s["cell_updates"] for s in stats)
     assert all(s["leaves_min"] == s["leaves_max"] == P for s in stats)
     fin32 = torch.empty_like(ic32)
@@ -322,6 +323,8 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
                   "the state (2 x 0.73 GB) exceeds L2 in any case",
             "sum_dt_instance0": float(acc32[0]),
             "driver": f"graph replays per run: {stats[0]['graph_intervals']} of {stats[0]['intervals']} intervals",
+            "autotuned_update_kernel": {"warps_per_block": tuned[0], "copy_stages": tuned[1],
+                                        "blocks": tuned[2] or "full residency"},
         },
         "e2e": {"value": e2e_cells / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(ic32_host.numel() * 4),
                 "d2h_bytes_per_step": int(out32_host.numel() * 4)},
@@ -440,6 +443,72 @@ def plain_config2(args, torch, A, dev, stream, flush, world):
         "host_driven": {"value": pl_cells / (pl_ms * 1e-3), "unit": UNIT, "gpu_launches": int(pl_launches),
                         "note": "same runs with host-driven launches and a readback every interval"},
         "cpu_baseline": None,
+    }
+
+
+# ---------------------------------------------- further single-tree workloads
+CONFIG3 = dict(rank=3, n=8, halo=1, depth=6, init_levels=1, steps=500, remesh=10, velocity=(1.0, 0.7, 0.3), cfl=0.4,
+               rthr=0.05, cthr=0.01, min_level=1, max_level=4, bump_seed=3, bumps=4, sigma=(0.05, 0.08))
+DEPTH7 = dict(WORKLOAD, max_level=7)
+
+
+def single_tree_runs(torch, A, dev, stream, flush, cfg, dtype, bumps_list, noise, noise_seed, reps):
+    """reps timed runs of one configuration from its initial state; returns
+    (ms per run, stats of the last run, final interior state, ids)."""
+    t = A.Tree(cfg["rank"], cfg["n"], cfg["halo"], cfg["depth"], capacity=1 << 16, dtype=dtype,
+               stream=stream.cuda_stream)
+    t.refine_uniform(cfg["init_levels"])
+    init = A.gaussian_state(t.ids(), cfg["rank"], cfg["n"], cfg["halo"], cfg["depth"], bumps_list, noise, noise_seed)
+    P0 = init.shape[0]
+    dev_init = torch.from_numpy(init).to(f"cuda:{dev}", torch.float64 if dtype == A.F64 else torch.float32)
+    args = dict(steps=cfg["steps"], interval=cfg["remesh"], velocity=cfg["velocity"], cfl=cfg["cfl"],
+                criterion="grad", rthr=cfg["rthr"], cthr=cfg["cthr"], min_level=cfg["min_level"],
+                max_level=cfg["max_level"])
+
+    def setup():
+        t.reset()
+        t.refine_uniform(cfg["init_levels"])
+        t.load_state_device(dev_init.data_ptr(), P0)
+
+    setup()
+    t.run(**args)  # warm-up
+    ms, _, stats, _ = time_runs(torch, stream, 1, reps, setup, lambda: t.run(**args), flush)
+    out = t.download_state()
+    ids = t.ids()
+    t.close()
+    h, n, r = cfg["halo"], cfg["n"], cfg["rank"]
+    inner = out[(slice(None),) + (slice(h, n + h),) * r].astype(np.float64)
+    return ms / reps, stats[-1], inner, ids
+
+
+def config3_extra(torch, A, dev, stream, flush, reps):
+    C = CONFIG3
+    b = A.seeded_bumps(3, C["bumps"], C["bump_seed"], sigma=C["sigma"])
+    ms64, st64, s64, ids64 = single_tree_runs(torch, A, dev, stream, flush, C, A.F64, b, 0.0, 0, reps)
+    ms32, st32, s32, ids32 = single_tree_runs(torch, A, dev, stream, flush, C, A.F32, b, 0.0, 0, reps)
+    same = np.array_equal(ids64, ids32)
+    return {
+        "workload": ("3D linear advection with AMR: 8^3 patches + 1 ghost, level 1 start, max level 4, gradient "
+                     "criterion 0.05/0.01, re-mesh every 10 steps, 4 seeded Gaussian blobs, v = (1, 0.7, 0.3), "
+                     "CFL 0.4, 500 steps"),
+        "fp64": {"value": st64["cell_updates"] / (ms64 * 1e-3), "ms_per_run": ms64, "leaves_max": st64["leaves_max"],
+                 "leaves_mean": st64["leaves_mean"]},
+        "fp32": {"value": st32["cell_updates"] / (ms32 * 1e-3), "ms_per_run": ms32, "leaves_max": st32["leaves_max"]},
+        "same_final_tree": bool(same),
+        "rel_l2_fp32_vs_fp64": (float(np.linalg.norm(s32 - s64) / np.linalg.norm(s64)) if same else None),
+        "unit": UNIT,
+    }
+
+
+def depth7_extra(torch, A, dev, stream, flush, reps):
+    ms, st, _, _ = single_tree_runs(torch, A, dev, stream, flush, DEPTH7, A.F64, bumps(), WORKLOAD["noise"],
+                                    WORKLOAD["noise_seed"], reps)
+    return {
+        "workload": WORKLOAD_NAME.replace("max level 5", "max level 7") + " (max-level-7 variant)",
+        "value": st["cell_updates"] / (ms * 1e-3), "unit": UNIT, "ms_per_run": ms, "dtype": "f64",
+        "leaves_min": st["leaves_min"], "leaves_max": st["leaves_max"], "leaves_mean": st["leaves_mean"],
+        "intervals": {"cluster_kernel": st["persistent_intervals"], "graph": st["graph_intervals"],
+                      "total": st["intervals"]},
     }
 
 
@@ -637,6 +706,8 @@ def gpu_arm(args, rank, world):
     if not args.no_extras:
         extras["plain_fp64_config2"] = plain_config2(args, torch, A, dev, stream, flush, world)
         extras["adjoint"] = adjoint_extra(torch, A, dev, stream, with_oracle=not args.no_cpu_baseline)
+        extras["config3_3d"] = config3_extra(torch, A, dev, stream, flush, max(1, args.steps))
+        extras["plain_fp64_config2_max_level7"] = depth7_extra(torch, A, dev, stream, flush, max(1, args.steps))
         if args.uniform:
             lv = args.uniform_level
             extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)
@@ -770,6 +841,50 @@ def reference_arm(args, rank, world):
     }
 
 
+def profile_case(name, steps):
+    """One untimed run of a workload, for profilers: forest (the batched FP32
+    forest, `steps` steps), adjoint (the adjoint mesh, FP64 forward and
+    backward over `steps` steps), config2 (one config-2 run)."""
+    import torch
+
+    import amr_gb300 as A
+
+    stream = torch.cuda.Stream()
+    if name == "forest":
+        B = BATCHED
+        caps, vel, bmp = batched_instances()
+        f = make_forest(A, A.F32, stream, caps, vel)
+        ids = f.ids()
+        ic64, _ = batched_ic(torch, ids, bmp, 0)
+        ic = ic64.to(torch.float32).contiguous()
+        f.load_state_device(ic.data_ptr(), len(ids))
+        st = f.run(steps, B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+    elif name == "adjoint":
+        J = ADJOINT
+        t, _ = adjoint_mesh(A, A.F64, stream)
+        u0 = A.gaussian_state(t.ids(), 2, J["n"], J["halo"], J["depth"], bumps(), WORKLOAD["noise"],
+                              WORKLOAD["noise_seed"])
+        x = torch.from_numpy(u0).cuda().contiguous()
+        t.load_state_device(x.data_ptr(), t.size)
+        adj = A.Adjoint(t, steps, J["velocity"], J["cfl"], every=J["every"])
+        adj.forward()
+        lam, out = torch.ones_like(x), torch.empty_like(x)
+        adj.backward(lam.data_ptr(), out.data_ptr())
+        st = {"leaves": t.size, "steps": steps}
+    else:
+        W = WORKLOAD
+        t = A.Tree(2, W["n"], W["halo"], W["depth"], capacity=4096, stream=stream.cuda_stream)
+        t.refine_uniform(W["init_levels"])
+        t.upload_state(A.gaussian_state(t.ids(), 2, W["n"], W["halo"], W["depth"], bumps(), W["noise"],
+                                        W["noise_seed"]))
+        t.halo_exchange()
+        st = t.run(steps=W["steps"], interval=W["remesh"], velocity=W["velocity"], cfl=W["cfl"], criterion="grad",
+                   rthr=W["rthr"], cthr=W["cthr"], min_level=W["min_level"], max_level=W["max_level"])
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "stats": {k: (v if isinstance(v, (int, float)) else str(v))
+                                              for k, v in dict(st).items()}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -780,7 +895,13 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--uniform", action="store_true", help="add the uniform kernel-level workloads")
     ap.add_argument("--uniform-level", type=int, default=9)
+    ap.add_argument("--case", choices=["forest", "adjoint", "config2"],
+                    help="run one workload once, untimed (for profilers), and exit")
+    ap.add_argument("--case-steps", type=int, default=30)
     args = ap.parse_args()
+    if args.case:
+        profile_case(args.case, args.case_steps)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

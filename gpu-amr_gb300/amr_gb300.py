@@ -109,6 +109,7 @@ def lib():
         L.amr_tree_set_timing.argtypes = [vp, i32]
         L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.amr_tree_set_instance_params.argtypes = [vp, vp, vp, sz]
+        L.amr_tree_step_config.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
         L.amr_adjoint_destroy.argtypes = [vp]
         L.amr_adjoint_forward.argtypes = [vp]
@@ -322,6 +323,12 @@ class Tree:
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}
+
+    def step_config(self):
+        """(warps per block, copy stages, blocks) of the last 2D update."""
+        w, st, b = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().amr_tree_step_config(self._h, C.byref(w), C.byref(st), C.byref(b)))
+        return w.value, st.value, b.value
 
     def set_timing(self, enabled: bool):
         check(lib().amr_tree_set_timing(self._h, int(enabled)))

@@ -1264,7 +1264,7 @@ __device__ __forceinline__ void step2d_smem(unsigned char* smem, T*& tiles, uint
 // metadata pipeline keeps three patches' records in registers).
 template <typename T, int W>
 struct Step2dOcc {
-    static constexpr int blocks = ((sizeof(T) == 4 ? 32 : 24) / W) > 0 ? ((sizeof(T) == 4 ? 32 : 24) / W) : 1;
+    static constexpr int blocks = ((sizeof(T) == 4 ? 40 : 24) / W) > 0 ? ((sizeof(T) == 4 ? 40 : 24) / W) : 1;
 };
 
 // Host-driven launch: leaf count and buffers from the arguments.

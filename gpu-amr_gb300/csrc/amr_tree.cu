@@ -164,6 +164,7 @@ struct amr_tree {
     bool      vel_inst_set = false;
     std::vector<double> vel_inst_host;
     uint64_t  topo = 0; // changes whenever the leaves may have changed
+    StepCfg   last_cfg{}; // launch shape of the last 2D update
     bool      bounds_set   = false;
     bool      vel_per_leaf = false; // the current advance uses per-instance velocities
     cudaStream_t          cap_stream = nullptr; // private stream for graph capture
@@ -874,9 +875,10 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
             });
             if (ts != AMR_OK) return ts;
         }
-        key.W    = cfg.W;
-        key.S    = cfg.S;
-        key.grid = cfg.grid; // 0: full residency
+        key.W       = cfg.W;
+        key.S       = cfg.S;
+        key.grid    = cfg.grid; // 0: full residency
+        t->last_cfg = cfg;
         // kernel attributes are set outside the capture
         amr_status ps = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
             using T = decltype(z);
@@ -1369,6 +1371,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
     size_t    done  = 0;
     StepCfg   cfg;
     lookup_tuned(t, uleaf != nullptr, cfg);
+    t->last_cfg = cfg;
     while (done < steps || (first && steps == 0)) {
         const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
         k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? first_mode : BATCH_CONTINUE,
@@ -1930,6 +1933,15 @@ amr_status amr_adjoint_checkpoint(amr_adjoint* a, size_t index, void* dst)
     amr_tree* t = a->t;
     AMR_CUDA(cudaMemcpyAsync(dst, a->ckpt[index], t->size * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
+    return AMR_OK;
+}
+
+amr_status amr_tree_step_config(const amr_tree* t, int32_t* warps, int32_t* stages, int32_t* blocks)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (warps) *warps = t->last_cfg.W;
+    if (stages) *stages = t->last_cfg.S;
+    if (blocks) *blocks = t->last_cfg.grid;
     return AMR_OK;
 }
 

@@ -328,6 +328,12 @@ amr_status amr_tree_set_timing(amr_tree* t, int enabled);
 amr_status amr_tree_get_timing(amr_tree* t, double* step_kernel_ms, uint64_t* step_launches,
                                uint64_t* cell_updates);
 
+/* Launch shape of the 2D update kernel used by the tree's last advance or
+ * run: warps per block, copy stages per warp, blocks (0 = full residency).
+ * The autotuner picks it on first use per device, dtype, patch shape and
+ * leaf-count octave (AMR_GB300_AUTOTUNE=0 keeps the default 8, 2, 0). */
+amr_status amr_tree_step_config(const amr_tree* t, int32_t* warps, int32_t* stages, int32_t* blocks);
+
 /* Block until all work queued on the tree's stream has finished. */
 amr_status amr_tree_synchronize(amr_tree* t);
 
