@@ -512,6 +512,50 @@ def depth7_extra(torch, A, dev, stream, flush, reps):
     }
 
 
+# ------------------------------------------------------------- VTK writer
+def vtk_extra(torch, A, dev, stream, with_cpu=True):
+    """The device-resident VTK writer on the adjoint workload's mesh (2629
+    leaves of 16x16, FP64): file size, time of amr_tree_write_vtk (device
+    sections + copy-back + file write) and of the oracle's C writer on the same
+    tree, and whether the two files are identical."""
+    import hashlib
+    import tempfile
+
+    J, W = ADJOINT, WORKLOAD
+    t, log = adjoint_mesh(A, A.F64, stream)
+    u0 = A.gaussian_state(t.ids(), 2, J["n"], J["halo"], J["depth"], bumps(), W["noise"], W["noise_seed"])
+    t.upload_state(u0)
+    out = {"workload": f"VTK snapshot of the adjoint mesh ({t.size} leaves of 16x16, FP64)"}
+    with tempfile.TemporaryDirectory() as d:
+        gp = Path(d) / "gpu.vtk"
+        t.write_vtk(gp)  # warm-up
+        reps = 3
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            t.write_vtk(gp)
+        gsec = (time.perf_counter() - t0) / reps
+        size = gp.stat().st_size
+        out.update({"bytes": size, "gpu_seconds": gsec, "gpu_mb_per_s": size / gsec / 1e6})
+        if with_cpu:
+            from oracle import oracle as O
+
+            O.build()
+            o = O.OracleTree(2, J["n"], J["halo"], J["depth"], 40000)
+            o.refine_all(J["base_level"])
+            for f in log:
+                assert o.reconstruct(f) == 0
+            o.set_state(u0)
+            cp = Path(d) / "cpu.vtk"
+            t0 = time.perf_counter()
+            o.write_vtk(cp)
+            csec = time.perf_counter() - t0
+            same = hashlib.sha256(gp.read_bytes()).digest() == hashlib.sha256(cp.read_bytes()).digest()
+            out.update({"cpu_seconds": csec, "cpu_mb_per_s": size / csec / 1e6, "cpu_kind": "oracle port, 1 thread",
+                        "identical_files": bool(same)})
+    t.close()
+    return out
+
+
 # ------------------------------------------------------------ adjoint form
 ADJOINT = dict(n=16, halo=1, depth=8, base_level=5, max_level=7, rthr=0.01, cthr=0.002, rounds=3, steps=400,
                every=20, cfl=0.4, velocity=(1.0, 0.5), directions=64, eps=1e-4, pert=0.05, seed=7)
@@ -692,6 +736,18 @@ def uniform_extra(A, torch, stream, dtype, level=9, steps=40):
     return out
 
 
+def aggregate_replicas(torch, device, ms, e2e_ms, cells, e2e_cells):
+    """Whole-job figures of N independent replicas: the slowest rank's time
+    (max) and the sum of the cell updates of all ranks."""
+    t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=device)
+    c = torch.tensor([float(cells), float(e2e_cells)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+    ms, e2e_ms = t.tolist()
+    cells, e2e_cells = c.tolist()
+    return ms, e2e_ms, cells, e2e_cells
+
+
 def gpu_arm(args, rank, world):
     import torch
 
@@ -707,6 +763,7 @@ def gpu_arm(args, rank, world):
         extras["plain_fp64_config2"] = plain_config2(args, torch, A, dev, stream, flush, world)
         extras["adjoint"] = adjoint_extra(torch, A, dev, stream, with_oracle=not args.no_cpu_baseline)
         extras["config3_3d"] = config3_extra(torch, A, dev, stream, flush, max(1, args.steps))
+        extras["vtk_writer"] = vtk_extra(torch, A, dev, stream, with_cpu=not args.no_cpu_baseline)
         extras["plain_fp64_config2_max_level7"] = depth7_extra(torch, A, dev, stream, flush, max(1, args.steps))
         if args.uniform:
             lv = args.uniform_level
@@ -714,12 +771,7 @@ def gpu_arm(args, rank, world):
             extras[f"uniform_fp32_level{lv}"] = uniform_extra(A, torch, stream, A.F32, lv)
     ms, e2e_ms, cells, e2e_cells = bt["ms"], bt["e2e_ms"], bt["cells"], bt["e2e_cells"]
     if world > 1:
-        t = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=f"cuda:{dev}")
-        c = torch.tensor([float(cells), float(e2e_cells)], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
-        ms, e2e_ms = t.tolist()
-        cells, e2e_cells = c.tolist()
+        ms, e2e_ms, cells, e2e_cells = aggregate_replicas(torch, f"cuda:{dev}", ms, e2e_ms, cells, e2e_cells)
     if rank != 0:
         return None
     bt["e2e"]["value"] = e2e_cells / (e2e_ms * 1e-3)

@@ -110,6 +110,8 @@ def lib():
         L.amr_tree_get_timing.argtypes = [vp, C.POINTER(dbl), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.amr_tree_set_instance_params.argtypes = [vp, vp, vp, sz]
         L.amr_tree_step_config.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.amr_selftest_wait_timeout.argtypes = [C.c_int32, C.POINTER(C.c_int32)]
+        L.amr_tree_write_vtk.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
         L.amr_adjoint_destroy.argtypes = [vp]
         L.amr_adjoint_forward.argtypes = [vp]
@@ -323,6 +325,10 @@ class Tree:
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}
+
+    def write_vtk(self, path, field="Scalar"):
+        """vtk_print::print of the current leaves and state (legacy binary VTK)."""
+        check(lib().amr_tree_write_vtk(self._h, str(path).encode(), field.encode()))
 
     def step_config(self):
         """(warps per block, copy stages, blocks) of the last 2D update."""

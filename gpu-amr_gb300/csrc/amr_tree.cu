@@ -18,6 +18,7 @@
 #include "amr_gb300.h"
 #include "amr_cycle.cuh"
 #include "amr_graph.cuh"
+#include "amr_vtk.cuh"
 
 using namespace amr_gb300;
 
@@ -127,6 +128,7 @@ struct StepCfg {
 
 struct amr_tree {
     Geo          g{};
+    double       lengths[3] = { 1.0, 1.0, 1.0 }; // domain lengths per Morton axis
     int          ninst    = 1;
     size_t       cap      = 0;
     int          dtype    = AMR_F64;
@@ -991,6 +993,20 @@ bool no_clamp(amr_tree* t, const amr_cycle_params* p, bool inst_params, long lon
     return std::isfinite(need) && p->remaining_time - sum_dt >= need;
 }
 
+// The bounded-wait self-test: an mbarrier expects 16 bytes nobody sends.
+__global__ void k_selftest_wait(int32_t* status, int polls)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+        mbar_expect_tx(&bar, 16);
+        status[0] = mbar_wait_bounded(&bar, 0, polls) ? AMR_OK : AMR_ERR_TIMEOUT;
+    }
+}
+
+__global__ void k_selftest_touch(int32_t* status) { status[1] = 1; }
+
 } // namespace
 
 extern "C" {
@@ -1021,6 +1037,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     amr_tree* t = new amr_tree();
     t->g      = g;
     t->ninst  = K;
+    for (int a = 0; a < 3; ++a) t->lengths[a] = a < g.rank ? desc->geom.lengths[a] : 1.0;
     t->cap    = desc->capacity;
     t->dtype  = desc->dtype;
     t->esize  = desc->dtype == AMR_F64 ? 8 : 4;
@@ -1933,6 +1950,52 @@ amr_status amr_adjoint_checkpoint(amr_adjoint* a, size_t index, void* dst)
     amr_tree* t = a->t;
     AMR_CUDA(cudaMemcpyAsync(dst, a->ckpt[index], t->size * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
     AMR_CUDA(cudaStreamSynchronize(t->stream));
+    return AMR_OK;
+}
+
+amr_status amr_selftest_wait_timeout(int32_t polls, amr_status* observed)
+{
+    if (polls < 1) return fail(AMR_ERR_INVALID, "polls must be positive");
+    int32_t* d = nullptr;
+    AMR_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), 2 * sizeof(int32_t)));
+    int32_t h[2] = { -1, 0 };
+    cudaError_t e = cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_selftest_wait<<<1, 32>>>(d, polls);
+        g_launches.fetch_add(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_selftest_touch<<<1, 1>>>(d);
+        g_launches.fetch_add(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "amr_selftest_wait_timeout");
+    if (observed) *observed = static_cast<amr_status>(h[0]);
+    if (h[1] != 1) return fail(AMR_ERR_CUDA, "the context did not run the follow-up kernel");
+    if (h[0] != AMR_ERR_TIMEOUT) return fail(AMR_ERR_INVALID, "the wait did not time out");
+    return AMR_OK;
+}
+
+amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_name)
+{
+    if (!t || !path) return fail(AMR_ERR_INVALID, "null argument");
+    VtkTree v{};
+    v.g     = t->g;
+    for (int a = 0; a < 3; ++a) v.dom.lengths[a] = t->lengths[a];
+    v.keys   = t->keys[t->tb];
+    v.state  = t->cur;
+    v.size   = t->size;
+    v.esize  = t->esize;
+    v.stream = t->stream;
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    std::string      err;
+    const amr_status st = vtk_write(v, path, field_name ? field_name : "Scalar", err);
+    // six section kernels per chunk of 2^22 cells
+    g_launches.fetch_add(6 * std::max<uint64_t>(1, (t->size * t->g.cells + (1ull << 22) - 1) >> 22));
+    if (st != AMR_OK) return fail(st, err);
     return AMR_OK;
 }
 

@@ -328,6 +328,14 @@ amr_status amr_tree_set_timing(amr_tree* t, int enabled);
 amr_status amr_tree_get_timing(amr_tree* t, double* step_kernel_ms, uint64_t* step_launches,
                                uint64_t* cell_updates);
 
+/* vtk_print::print (include/ndtree/vtk_print.hpp:53-257) of the current
+ * leaves and state: legacy binary VTK (big-endian), one quad (2D) or voxel
+ * (3D) per interior cell, CELL_DATA cell_index, is_halo and the field named
+ * field_name (an FP32 tree writes its values as "float").  Every section is
+ * built on the device; byte-identical to the reference writer for FP64
+ * trees. */
+amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_name);
+
 /* Launch shape of the 2D update kernel used by the tree's last advance or
  * run: warps per block, copy stages per warp, blocks (0 = full residency).
  * The autotuner picks it on first use per device, dtype, patch shape and
@@ -368,6 +376,13 @@ amr_status amr_remesh_noalloc(const amr_patch_geometry* geom, size_t num_leaves,
                               size_t out_capacity, uint64_t* device_ids_out, int32_t* device_levels_out,
                               amr_halo_meta* device_meta_out, double* device_state_out,
                               uint32_t* device_out_count, size_t* host_out_count, void* stream);
+
+/* Self-test of the bounded waits: one warp waits on an mbarrier whose
+ * transaction never arrives, gives up after `polls` polls and records
+ * AMR_ERR_TIMEOUT, which the host reads; then a second kernel runs to show
+ * the context is still usable.  *observed = the status the kernel recorded.
+ * Returns AMR_OK when the wait timed out as designed. */
+amr_status amr_selftest_wait_timeout(int32_t polls, amr_status* observed);
 
 /* Kernel launches issued by this library since load (for launch accounting). */
 uint64_t amr_launch_count(void);

@@ -10,6 +10,7 @@
 
 #include <math.h>
 #include <stdlib.h>
+#include <stdio.h>
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -981,6 +982,115 @@ double oracle_advance(oracle_tree* t, size_t steps, const double* v, double cfl,
     }
     if (executed) *executed = count;
     return acc;
+}
+
+/* ------------------------------------------------------------ VTK file */
+/* vtk_print::print (include/ndtree/vtk_print.hpp:53-257): legacy VTK,
+ * BINARY (big-endian), DATASET UNSTRUCTURED_GRID with one quad (2D, type 9)
+ * or voxel (3D, type 11) per interior cell; corner coordinates from
+ * physics_system::patch_coord / cell_sizes (physics_system.hpp:62-104) on the
+ * unit domain; CELL_DATA cell_index, is_halo (the reference evaluates
+ * is_halo_cell on the padded layout for linear indices 0 .. n^rank - 1 of
+ * every patch, vtk_print.hpp:217-228) and the scalar field. */
+static void put_be(FILE* f, const void* v, size_t n)
+{
+    unsigned char b[8];
+    memcpy(b, v, n);
+    for (size_t i = 0; i < n / 2; ++i) {
+        const unsigned char x = b[i];
+        b[i]                  = b[n - 1 - i];
+        b[n - 1 - i]          = x;
+    }
+    fwrite(b, 1, n, f);
+}
+static void put_f64(FILE* f, double v) { put_be(f, &v, 8); }
+static void put_i32(FILE* f, int v) { put_be(f, &v, 4); }
+
+static int padded_is_halo(const oracle_tree* t, size_t li)
+{
+    size_t stride = 1;
+    for (int k = 1; k < t->rank; ++k) stride *= t->pad1;
+    for (int k = 0; k < t->rank; ++k) {
+        const size_t rel = li / stride;
+        if (rel < (size_t)t->h || rel >= t->pad1 - (size_t)t->h) return 1;
+        li %= stride;
+        stride /= t->pad1;
+    }
+    return 0;
+}
+
+int oracle_write_vtk(const oracle_tree* t, const char* path, const char* field)
+{
+    FILE* f = fopen(path, "wb");
+    if (!f) return -1;
+    const int    rank = t->rank, n = t->n, h = t->h;
+    const size_t box = (size_t)1 << rank, per = ipow((size_t)n, rank), cells = t->size * per;
+    const double maxc = (double)(1u << t->depth);
+    fprintf(f, "# vtk DataFile Version 3.0\nAMR Tree Structure\nBINARY\nDATASET UNSTRUCTURED_GRID\n");
+    fprintf(f, "POINTS %zu double\n", cells * box);
+    for (size_t p = 0; p < t->size; ++p) {
+        uint32_t c[3] = { 0, 0, 0 };
+        int      level;
+        oracle_decode(rank, t->ids[p], c, &level);
+        double origin[3], cs[3];
+        for (int k = 0; k < rank; ++k) {
+            origin[k]         = 1.0 * (double)c[k] / maxc;
+            const double size = 1.0 * (double)(1u << (t->depth - level)) / maxc;
+            cs[k]             = size / (double)n;
+        }
+        int idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    if (rank == 2) {
+                        const double x = origin[0] + (double)(idx[1] - h) * cs[0];
+                        const double y = origin[1] + (double)(idx[0] - h) * cs[1];
+                        const double X = x + cs[0], Y = y + cs[1];
+                        put_f64(f, x); put_f64(f, y); put_f64(f, 0.0);
+                        put_f64(f, X); put_f64(f, y); put_f64(f, 0.0);
+                        put_f64(f, X); put_f64(f, Y); put_f64(f, 0.0);
+                        put_f64(f, x); put_f64(f, Y); put_f64(f, 0.0);
+                    } else {
+                        const double x = origin[0] + (double)(idx[2] - h) * cs[0];
+                        const double y = origin[1] + (double)(idx[1] - h) * cs[1];
+                        const double z = origin[2] + (double)(idx[0] - h) * cs[2];
+                        const double X = x + cs[0], Y = y + cs[1], Z = z + cs[2];
+                        put_f64(f, x); put_f64(f, y); put_f64(f, z);
+                        put_f64(f, X); put_f64(f, y); put_f64(f, z);
+                        put_f64(f, x); put_f64(f, Y); put_f64(f, z);
+                        put_f64(f, X); put_f64(f, Y); put_f64(f, z);
+                        put_f64(f, x); put_f64(f, y); put_f64(f, Z);
+                        put_f64(f, X); put_f64(f, y); put_f64(f, Z);
+                        put_f64(f, x); put_f64(f, Y); put_f64(f, Z);
+                        put_f64(f, X); put_f64(f, Y); put_f64(f, Z);
+                    }
+                }
+    }
+    fprintf(f, "CELLS %zu %zu\n", cells, cells * (box + 1));
+    for (size_t i = 0; i < cells; ++i) {
+        put_i32(f, (int)box);
+        for (size_t j = 0; j < box; ++j) put_i32(f, (int)(i * box + j));
+    }
+    fprintf(f, "CELL_TYPES %zu\n", cells);
+    for (size_t i = 0; i < cells; ++i) put_i32(f, rank == 2 ? 9 : 11);
+    fprintf(f, "CELL_DATA %zu\nSCALARS cell_index int 1\nLOOKUP_TABLE default\n", cells);
+    for (size_t i = 0; i < cells; ++i) put_i32(f, (int)i);
+    fprintf(f, "SCALARS is_halo int 1\nLOOKUP_TABLE default\n");
+    for (size_t p = 0; p < t->size; ++p)
+        for (size_t j = 0; j < per; ++j) put_i32(f, padded_is_halo(t, j));
+    fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", field);
+    for (size_t p = 0; p < t->size; ++p) {
+        const double* u = t->cur + p * t->flat;
+        int           idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    size_t li = 0;
+                    for (int k = 0; k < rank; ++k) li = li * t->pad1 + (size_t)idx[k];
+                    put_f64(f, u[li]);
+                }
+    }
+    return fclose(f) == 0 ? 0 : -1;
 }
 
 /* ------------------------------------------------------------- adjoint */

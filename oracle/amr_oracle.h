@@ -70,6 +70,10 @@ void oracle_random_state(oracle_tree* t, uint64_t seed);
 double oracle_compute_dt(const oracle_tree* t, const double* velocity, double cfl);
 double oracle_advance(oracle_tree* t, size_t steps, const double* velocity,
                       double cfl, double remaining, size_t* executed);
+/* vtk_print::print of the current tree and state (legacy binary VTK, one
+ * quad/voxel per interior cell); field = the scalar's name.  0 on success. */
+int oracle_write_vtk(const oracle_tree* t, const char* path, const char* field);
+
 /* Gradient of <lam_T, u_T> w.r.t. the interior of u_0 for oracle_advance on
  * the current (frozen) mesh: transposed steps in reverse order (size*flat
  * padded buffers; ghost entries of lam_0 are zero).  Returns executed steps. */

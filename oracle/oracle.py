@@ -61,6 +61,8 @@ def lib():
         L.oracle_compute_dt.argtypes = [vp, P(np.float64, flags="C"), dbl]
         L.oracle_advance.restype = dbl
         L.oracle_advance.argtypes = [vp, sz, P(np.float64, flags="C"), dbl, dbl, C.POINTER(sz)]
+        L.oracle_write_vtk.restype = C.c_int
+        L.oracle_write_vtk.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.oracle_adjoint.restype = sz
         L.oracle_adjoint.argtypes = [vp, sz, P(np.float64, flags="C"), dbl, dbl, P(np.float64, flags="C"),
                                      P(np.float64, flags="C")]
@@ -170,6 +172,10 @@ class OracleTree:
         acc = lib().oracle_advance(self._t, steps, v, cfl, remaining, C.byref(ex))
         return acc, ex.value
 
+
+    def write_vtk(self, path, field="Scalar"):
+        if lib().oracle_write_vtk(self._t, str(path).encode(), field.encode()) != 0:
+            raise OSError(f"cannot write {path}")
 
     def adjoint(self, steps, velocity, cfl, lam_T, remaining=1.7976931348623157e308):
         """Gradient of <lam_T, u_T> w.r.t. the interior of the current state

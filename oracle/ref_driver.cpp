@@ -19,6 +19,9 @@
 //                       include/dg_helpers/globals/amr_indicators.hpp:186-225.
 //   max criterion      - the max-value rule of tests/advection_equation_amr.t.cpp:155-170.
 //   random criterion   - hash-driven flags for tree-operation coverage.
+//   vtk=<name>          - after the mode, the reference's VTK writer
+//                       (include/ndtree/vtk_print.hpp) prints the tree to
+//                       vtk_output/<name>.vtk.
 #include "containers/static_layout.hpp"
 #include "containers/static_shape.hpp"
 #include "containers/static_vector.hpp"
@@ -26,6 +29,7 @@
 #include "ndtree/intergrid_operator.hpp"
 #include "ndtree/ndtree.hpp"
 #include "ndtree/patch_layout.hpp"
+#include "ndtree/vtk_print.hpp"
 #include "solver/amr_solver.hpp"
 #include "solver/cell_types.hpp"
 #include "solver/physics_system.hpp"
@@ -530,8 +534,14 @@ int dispatch(params const& p)
     writer w(p.str("out", "dump.bin"));
     auto   h = std::make_unique<harness<DIM, N, H, Depth>>(p, w);
     const auto mode = p.str("mode", "run");
-    if (mode == "tree") return h->tree_mode();
-    return h->run();
+    const int  rc   = mode == "tree" ? h->tree_mode() : h->run();
+    if (rc == 0 && p.has("vtk"))
+    {
+        using geometry_t = typename harness<DIM, N, H, Depth>::geometry_t;
+        amr::ndt::print::vtk_print<geometry_t> printer(p.str("vtk", "tree"));
+        printer.print(h->tree(), ".vtk");
+    }
+    return rc;
 }
 
 } // namespace harness

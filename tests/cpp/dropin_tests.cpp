@@ -12,6 +12,7 @@
 #include "ndtree/intergrid_operator.hpp"
 #include "ndtree/ndtree.hpp"
 #include "ndtree/patch_layout.hpp"
+#include "ndtree/vtk_print.hpp"
 #include "solver/AdvectionPhysics.hpp"
 #include "solver/adjoint.hpp"
 #include "solver/amr_solver.hpp"

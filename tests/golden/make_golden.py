@@ -134,11 +134,46 @@ def scenario_tree(name, cfg, rank, n, h, params, keep_states=None):
     return info
 
 
+VTK_SCENARIOS = {
+    # name of the npz fixture whose final tree and state are printed -> driver arguments
+    "config1_uniform_2d": ("2d8h1", dict(mode="run", init_levels=2, steps=100, remesh=0, vel="1,0.5", cfl=0.4,
+                                         bumps="0.3,0.3,0.05,1", noise=1e-3, noise_seed=1, crit="none")),
+    "tree_random_2d_n8": ("2d8h1", dict(mode="tree", seed=12, passes=6, init_levels=1, max_level=5, min_level=1,
+                                        p_refine=0.3, p_coarsen=0.4)),
+    "tree_random_3d_n4": ("3d4h1", dict(mode="tree", seed=13, passes=5, init_levels=1, max_level=4, min_level=1,
+                                        p_refine=0.25, p_coarsen=0.5)),
+    "tree_random_2d_h2": ("2d10h2", dict(mode="tree", seed=14, passes=4, init_levels=1, max_level=4, min_level=1,
+                                         p_refine=0.3, p_coarsen=0.5)),
+}
+
+
+def vtk_golden():
+    """The reference's VTK writer (include/ndtree/vtk_print.hpp) on the final
+    tree and state of four fixtures: SHA-256 and length of each file."""
+    import hashlib
+    import tempfile
+
+    out = {}
+    for name, (cfg, params) in VTK_SCENARIOS.items():
+        with tempfile.TemporaryDirectory() as d:
+            cmd = ([str(DRIVER), f"cfg={cfg}"] + [f"{k}={v}" for k, v in params.items()]
+                   + [f"out={d}/dump.bin", f"vtk={name}"])
+            subprocess.run(cmd, check=True, capture_output=True, text=True, cwd=d)
+            data = (Path(d) / "vtk_output" / f"{name}.vtk").read_bytes()
+        out[name] = {"sha256": hashlib.sha256(data).hexdigest(), "bytes": len(data), "field": "Scalar"}
+    (HERE / "vtk.json").write_text(json.dumps(out, indent=1) + "\n")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--vtk-only", action="store_true", help="only the VTK writer fixture")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={a.ref}"], check=True)
+    if a.vtk_only:
+        print(vtk_golden())
+        return
 
     # 1: 2D uniform depth 2, 16 leaves of 8x8, FP64, 100 steps, config as in the
     #    reference's config.yaml: CFL 0.4, v = (1, 0.5), Gaussian at (0.3,0.3)
@@ -173,6 +208,7 @@ def main():
         keep_states={0, 4}))
     print(scenario_tree("tree_random_2d_h2", "2d10h2", 2, 10, 2, dict(
         seed=14, passes=4, init_levels=1, max_level=4, min_level=1, p_refine=0.3, p_coarsen=0.5)))
+    print(vtk_golden())
 
 
 if __name__ == "__main__":

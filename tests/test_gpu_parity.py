@@ -359,3 +359,19 @@ def test_update_all_velocity_signs_against_oracle(amr, oracle_mod, n, h, vel):
     a = interior(t.download_state(), rank, n, h)
     b = interior(o.state(), rank, n, h)
     assert rel_l2(a, b) <= STATE_TOL
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(amr):
+    """A bulk-copy wait that never completes gives up after its poll limit,
+    records AMR_ERR_TIMEOUT for the host, and leaves the context usable (a
+    follow-up kernel and a full tree run afterwards)."""
+    import ctypes as C
+
+    obs = C.c_int32(-1)
+    amr.check(amr.lib().amr_selftest_wait_timeout(1 << 12, C.byref(obs)))
+    assert obs.value == 7  # AMR_ERR_TIMEOUT
+    t = amr.Tree(2, 16, 1, 5, capacity=1024)
+    t.refine_uniform(2)
+    t.upload_state(np.random.default_rng(0).random((t.size, 18, 18)))
+    st = t.run(20, 10, (1.0, 0.5), 0.4, "grad", 0.05, 0.01, 1, 3)
+    assert st["executed_steps"] == 20
