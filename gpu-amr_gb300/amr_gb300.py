@@ -112,6 +112,8 @@ def lib():
         L.amr_tree_step_config.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.amr_selftest_wait_timeout.argtypes = [C.c_int32, C.POINTER(C.c_int32)]
         L.amr_tree_write_vtk.argtypes = [vp, C.c_char_p, C.c_char_p]
+        L.amr_tree_reserve.argtypes = [vp, sz]
+        L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
         L.amr_adjoint_destroy.argtypes = [vp]
         L.amr_adjoint_forward.argtypes = [vp]
@@ -190,6 +192,16 @@ class Tree:
         s = C.c_size_t()
         check(lib().amr_tree_size(self._h, C.byref(s)))
         return s.value
+
+    @property
+    def capacity(self) -> int:
+        s = C.c_size_t()
+        check(lib().amr_tree_capacity(self._h, C.byref(s)))
+        return s.value
+
+    def reserve(self, capacity):
+        """Change the capacity, keeping leaves, state, tables and flags."""
+        check(lib().amr_tree_reserve(self._h, capacity))
 
     @property
     def flat(self) -> int:

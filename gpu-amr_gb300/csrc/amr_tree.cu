@@ -1116,6 +1116,107 @@ amr_status amr_tree_size(const amr_tree* t, size_t* out)
     return AMR_OK;
 }
 
+amr_status amr_tree_capacity(const amr_tree* t, size_t* out)
+{
+    if (!t || !out) return fail(AMR_ERR_INVALID, "null argument");
+    *out = t->cap;
+    return AMR_OK;
+}
+
+amr_status amr_tree_reserve(amr_tree* t, size_t cap)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (cap < t->size || cap < static_cast<size_t>(t->ninst) || cap > (1ull << 30))
+        return fail(AMR_ERR_INVALID, "capacity does not hold the current leaves");
+    if (cap == t->cap) return AMR_OK;
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    const Geo&   g = t->g;
+    const size_t P = t->size;
+    std::vector<void*> fresh;
+    cudaError_t        e  = cudaSuccess;
+    auto               al = [&](size_t bytes) -> void* {
+        void* q = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&q, bytes);
+        if (q) fresh.push_back(q);
+        return q;
+    };
+    const size_t flat_b = static_cast<size_t>(g.flat) * t->esize;
+    void*        sb0    = al(cap * flat_b);
+    void*        sb1    = al(cap * flat_b);
+    void*        k0     = al(cap * sizeof(uint64_t));
+    void*        k1     = al(cap * sizeof(uint64_t));
+    void*        l0     = al(cap * sizeof(int32_t));
+    void*        l1     = al(cap * sizeof(int32_t));
+    void*        m0     = al(cap * g.ndir * sizeof(amr_halo_meta));
+    void*        m1     = al(cap * g.ndir * sizeof(amr_halo_meta));
+    void*        fl     = al(cap);
+    void*        rm     = al(cap);
+    void*        ch     = al(cap);
+    void*        cn     = al((cap + 1) * sizeof(uint32_t));
+    void*        ps     = al((cap + 1) * sizeof(uint32_t));
+    void*        sr     = al(cap * sizeof(int32_t));
+    void*        sk     = al(cap);
+    void*        ts     = al(((cap + kScanTile - 1) / kScanTile + 1) * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        for (void* q : fresh) cudaFree(q);
+        return cuda_fail(e, "amr_tree_reserve allocation");
+    }
+    // the current tree and both state buffers (the next buffer may hold the
+    // scratch the caller reads through amr_tree_device_state)
+    const int cs = t->cur == t->sbuf[0] ? 0 : 1;
+    void*     nsb[2] = { sb0, sb1 };
+    AMR_CUDA(cudaMemcpyAsync(nsb[cs], t->cur, P * flat_b, cudaMemcpyDeviceToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(nsb[cs ^ 1], t->nxt, P * flat_b, cudaMemcpyDeviceToDevice, t->stream));
+    void* nk[2] = { k0, k1 };
+    void* nlv[2] = { l0, l1 };
+    void* nm[2] = { m0, m1 };
+    AMR_CUDA(cudaMemcpyAsync(nk[t->tb], t->keys[t->tb], P * sizeof(uint64_t), cudaMemcpyDeviceToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(nlv[t->tb], t->levels[t->tb], P * sizeof(int32_t), cudaMemcpyDeviceToDevice, t->stream));
+    AMR_CUDA(cudaMemcpyAsync(nm[t->tb], t->meta[t->tb], P * g.ndir * sizeof(amr_halo_meta), cudaMemcpyDeviceToDevice,
+                             t->stream));
+    AMR_CUDA(cudaMemcpyAsync(fl, t->flags, P, cudaMemcpyDeviceToDevice, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    cudaFree(t->sbuf[0]);
+    cudaFree(t->sbuf[1]);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(t->keys[b]);
+        cudaFree(t->levels[b]);
+        cudaFree(t->meta[b]);
+    }
+    cudaFree(t->flags);
+    cudaFree(t->rmark);
+    cudaFree(t->chead);
+    cudaFree(t->cnt);
+    cudaFree(t->pos);
+    cudaFree(t->src);
+    cudaFree(t->skind);
+    cudaFree(t->tile_sums);
+    t->sbuf[0] = sb0;
+    t->sbuf[1] = sb1;
+    t->cur     = nsb[cs];
+    t->nxt     = nsb[cs ^ 1];
+    for (int b = 0; b < 2; ++b) {
+        t->keys[b]   = static_cast<uint64_t*>(nk[b]);
+        t->levels[b] = static_cast<int32_t*>(nlv[b]);
+        t->meta[b]   = static_cast<amr_halo_meta*>(nm[b]);
+    }
+    t->flags     = static_cast<int8_t*>(fl);
+    t->rmark     = static_cast<uint8_t*>(rm);
+    t->chead     = static_cast<uint8_t*>(ch);
+    t->cnt       = static_cast<uint32_t*>(cn);
+    t->pos       = static_cast<uint32_t*>(ps);
+    t->src       = static_cast<int32_t*>(sr);
+    t->skind     = static_cast<int8_t*>(sk);
+    t->tile_sums = static_cast<uint32_t*>(ts);
+    t->cap       = cap;
+    for (auto& ge : t->graphs) { // captured graphs name the old buffers
+        if (ge.exec) cudaGraphExecDestroy(ge.exec);
+        if (ge.graph) cudaGraphDestroy(ge.graph);
+    }
+    t->graphs.clear();
+    return AMR_OK;
+}
+
 amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out)
 {
     if (!t || !out) return fail(AMR_ERR_INVALID, "null argument");

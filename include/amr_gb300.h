@@ -157,6 +157,12 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out);
 amr_status amr_tree_destroy(amr_tree* t);
 /* ndtree::size() */
 amr_status amr_tree_size(const amr_tree* t, size_t* out);
+/* Change the capacity (the maximum number of leaves) keeping the leaves,
+ * their state, ids, levels, neighbour tables and flags; new_capacity must
+ * hold the current leaves.  Device buffers move, so pointers from
+ * amr_tree_device_state taken before the call are invalid after it. */
+amr_status amr_tree_reserve(amr_tree* t, size_t new_capacity);
+amr_status amr_tree_capacity(const amr_tree* t, size_t* out);
 /* Flat cell count of one padded patch. */
 amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out);
 

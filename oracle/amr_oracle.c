@@ -200,8 +200,9 @@ static void map_erase(idmap* m, uint64_t k)
 
 /* --------------------------------------------------------------- tree */
 struct oracle_tree {
-    int    rank, n, h, depth, nd, nf, ndir;
-    size_t cap, size, flat, pad1;
+    int    rank, n, h, depth, nd, nf, ndir, nvar;
+    double lengths[3]; /* physics_system's Domain_Sizes per Morton axis */
+    size_t cap, size, flat, pad1, pstride; /* pstride = nvar * flat: fields of a patch, contiguous */
     uint64_t*        ids;      /* m_linear_index_map  ndtree.hpp:2149 */
     oracle_neighbor* nb;       /* m_neighbors         ndtree.hpp:2152 */
     int8_t*          status;   /* m_refine_status_buffer ndtree.hpp:2151 */
@@ -253,7 +254,12 @@ static void append(oracle_tree* t, uint64_t id, const oracle_neighbor* arr)
 
 oracle_tree* oracle_create(int rank, int n, int halo, int depth, size_t capacity)
 {
-    if ((rank != 2 && rank != 3) || n < 2 * halo || n % 2 || halo < 1) return NULL;
+    return oracle_create_fields(rank, n, halo, depth, capacity, 1);
+}
+
+oracle_tree* oracle_create_fields(int rank, int n, int halo, int depth, size_t capacity, int nvar)
+{
+    if ((rank != 2 && rank != 3) || n < 2 * halo || n % 2 || halo < 1 || nvar < 1) return NULL;
     oracle_tree* t = (oracle_tree*)calloc(1, sizeof *t);
     t->rank = rank;
     t->n    = n;
@@ -265,15 +271,18 @@ oracle_tree* oracle_create(int rank, int n, int halo, int depth, size_t capacity
     t->cap  = capacity;
     t->pad1 = (size_t)(n + 2 * halo);
     t->flat = ipow(t->pad1, rank);
+    t->nvar    = nvar;
+    t->pstride = t->flat * (size_t)nvar;
+    t->lengths[0] = t->lengths[1] = t->lengths[2] = 1.0;
     t->ids  = (uint64_t*)calloc(capacity, sizeof(uint64_t));
     t->nb   = (oracle_neighbor*)calloc(capacity * (size_t)t->ndir, sizeof(oracle_neighbor));
     t->status = (int8_t*)calloc(capacity, 1);
-    t->cur  = (double*)calloc(capacity * t->flat, sizeof(double));
-    t->nxt  = (double*)calloc(capacity * t->flat, sizeof(double));
+    t->cur  = (double*)calloc(capacity * t->pstride, sizeof(double));
+    t->nxt  = (double*)calloc(capacity * t->pstride, sizeof(double));
     t->to_refine  = (uint64_t*)malloc(capacity * sizeof(uint64_t));
     t->to_coarsen = (uint64_t*)malloc(capacity * sizeof(uint64_t));
     t->refine_mark = (uint8_t*)calloc(capacity, 1);
-    t->scratch = (double*)malloc(t->flat * sizeof(double));
+    t->scratch = (double*)malloc(t->pstride * sizeof(double));
     t->perm    = (size_t*)malloc(capacity * sizeof(size_t));
     map_init(&t->map, capacity);
     /* root with periodic self-neighbours, ndtree.hpp:411-421 */
@@ -312,12 +321,13 @@ void oracle_get_neighbors(const oracle_tree* t, oracle_neighbor* out)
 }
 void oracle_get_state(const oracle_tree* t, double* out)
 {
-    memcpy(out, t->cur, t->size * t->flat * sizeof(double));
+    memcpy(out, t->cur, t->size * t->pstride * sizeof(double));
 }
 void oracle_set_state(oracle_tree* t, const double* in)
 {
-    memcpy(t->cur, in, t->size * t->flat * sizeof(double));
+    memcpy(t->cur, in, t->size * t->pstride * sizeof(double));
 }
+int oracle_nvar(const oracle_tree* t) { return t->nvar; }
 
 /* ------------------------------------------------- neighbour utilities */
 /* Hypercube multi-index of a child offset, row-major with layout dim 0
@@ -500,7 +510,14 @@ static void symmetry_after_recombining(oracle_tree* t, uint64_t parent, const or
 /* patch_mapping_impl + interpolate_patch / restrict_patches,
  * ndtree.hpp:1463-1555; linear_interpolator, intergrid_operator.hpp:41-107.
  * fn(kind): 0 interpolate (parent at `a` -> children a2..), 1 restrict. */
+static void intergrid_field(oracle_tree* t, size_t coarse, size_t fine_start, int restrict_mode, int field);
 static void intergrid(oracle_tree* t, size_t coarse, size_t fine_start, int restrict_mode)
+{
+    /* every field of the cell type moves the same way (patch_mapping_impl
+     * over the deconstructed map types, ndtree.hpp:1463-1497) */
+    for (int f = 0; f < t->nvar; ++f) intergrid_field(t, coarse, fine_start, restrict_mode, f);
+}
+static void intergrid_field(oracle_tree* t, size_t coarse, size_t fine_start, int restrict_mode, int field)
 {
     const int    rank = t->rank, n = t->n, h = t->h;
     const size_t P1 = t->pad1;
@@ -526,8 +543,8 @@ static void intergrid(oracle_tree* t, size_t coarse, size_t fine_start, int rest
                     coarse_idx = ((size_t)idx[0] * P1 + (size_t)idx[1]) * P1 + (size_t)idx[2];
                     base_idx   = ((size_t)base[0] * P1 + (size_t)base[1]) * P1 + (size_t)base[2];
                 }
-                double*       cp = buf + coarse * t->flat;
-                double*       fp = buf + (fine_start + (size_t)child) * t->flat;
+                double*       cp = buf + coarse * t->pstride + (size_t)field * t->flat;
+                double*       fp = buf + (fine_start + (size_t)child) * t->pstride + (size_t)field * t->flat;
                 /* hypercube_offset<layout,2> order: row-major, dim 0 slowest
                  * (patch_utils.hpp:203-234) */
                 size_t off[8];
@@ -703,9 +720,9 @@ static void swap_entries(oracle_tree* t, size_t i, size_t j)
     memcpy(tmp, &t->nb[i * t->ndir], sizeof(oracle_neighbor) * (size_t)t->ndir);
     memcpy(&t->nb[i * t->ndir], &t->nb[j * t->ndir], sizeof(oracle_neighbor) * (size_t)t->ndir);
     memcpy(&t->nb[j * t->ndir], tmp, sizeof(oracle_neighbor) * (size_t)t->ndir);
-    memcpy(t->scratch, &t->cur[i * t->flat], t->flat * sizeof(double));
-    memcpy(&t->cur[i * t->flat], &t->cur[j * t->flat], t->flat * sizeof(double));
-    memcpy(&t->cur[j * t->flat], t->scratch, t->flat * sizeof(double));
+    memcpy(t->scratch, &t->cur[i * t->pstride], t->pstride * sizeof(double));
+    memcpy(&t->cur[i * t->pstride], &t->cur[j * t->pstride], t->pstride * sizeof(double));
+    memcpy(&t->cur[j * t->pstride], t->scratch, t->pstride * sizeof(double));
 }
 
 /* compact, ndtree.hpp:1919-1948. */
@@ -744,12 +761,12 @@ static void sort_buffers(oracle_tree* t)
         ids[i]         = t->ids[s];
         st[i]          = t->status[s];
         memcpy(&nb[i * t->ndir], &t->nb[s * t->ndir], sizeof(oracle_neighbor) * (size_t)t->ndir);
-        memcpy(&t->nxt[i * t->flat], &t->cur[s * t->flat], t->flat * sizeof(double));
+        memcpy(&t->nxt[i * t->pstride], &t->cur[s * t->pstride], t->pstride * sizeof(double));
     }
     memcpy(t->ids, ids, t->size * sizeof(uint64_t));
     memcpy(t->status, st, t->size);
     memcpy(t->nb, nb, t->size * (size_t)t->ndir * sizeof(oracle_neighbor));
-    memcpy(t->cur, t->nxt, t->size * t->flat * sizeof(double));
+    memcpy(t->cur, t->nxt, t->size * t->pstride * sizeof(double));
     free(ids);
     free(st);
     free(nb);
@@ -797,11 +814,19 @@ void oracle_refine_all(oracle_tree* t, int levels)
 /* halo_apply over all directions, patch_utils.hpp:162-251; per relation
  * same_t :315-332, finer_t :334-386, coarser_t :388-441; boundary: no-op
  * (:303-313). Face ghost slabs only (patch_layout.hpp:183-221). */
+static void halo_one_field(oracle_tree* t, size_t i, int field);
 static void halo_one(oracle_tree* t, size_t i)
+{
+    /* every field of the cell type (halo_exchange_update loops over the map
+     * types, ndtree.hpp:1581-1596) */
+    for (int f = 0; f < t->nvar; ++f) halo_one_field(t, i, f);
+}
+static void halo_one_field(oracle_tree* t, size_t i, int field)
 {
     const int    rank = t->rank, n = t->n, h = t->h;
     const size_t P1 = t->pad1;
-    double*      self = t->cur + i * t->flat;
+    const size_t fo = (size_t)field * t->flat;
+    double*      self = t->cur + i * t->pstride + fo;
     for (int d = 0; d < t->ndir; ++d) {
         const oracle_neighbor* nb = &t->nb[i * t->ndir + d];
         if (nb->kind == NB_NONE) continue;
@@ -823,9 +848,9 @@ static void halo_one(oracle_tree* t, size_t i)
         const double* other[4] = { 0, 0, 0, 0 };
         int           ok       = 1;
         if (nb->kind == NB_SAME || nb->kind == NB_COARSER)
-            other[0] = t->cur + index_of(t, nb->ids[0], &ok) * t->flat;
+            other[0] = t->cur + index_of(t, nb->ids[0], &ok) * t->pstride + fo;
         else
-            for (int k = 0; k < t->nf; ++k) other[k] = t->cur + index_of(t, nb->ids[k], &ok) * t->flat;
+            for (int k = 0; k < t->nf; ++k) other[k] = t->cur + index_of(t, nb->ids[k], &ok) * t->pstride + fo;
         for (idx[0] = lo[0]; idx[0] < hi[0]; ++idx[0])
             for (idx[1] = lo[1]; idx[1] < hi[1]; ++idx[1])
                 for (idx[2] = lo[2]; idx[2] < hi[2]; ++idx[2]) {
@@ -897,9 +922,14 @@ static void cell_sizes(const oracle_tree* t, uint64_t id, double* cs)
     const uint32_t psm = 1u << (t->depth - level_of(id));
     const double   maxc = (double)(1u << t->depth);
     for (int k = 0; k < t->rank; ++k) {
-        const double patch = 1.0 * (double)psm / maxc;
+        const double patch = t->lengths[k] * (double)psm / maxc;
         cs[k]              = patch / (double)t->n;
     }
+}
+
+void oracle_set_lengths(oracle_tree* t, const double* lengths)
+{
+    for (int k = 0; k < t->rank; ++k) t->lengths[k] = lengths[k];
 }
 
 /* ------------------------------------------------------------- solver */
@@ -935,8 +965,8 @@ static void time_step(oracle_tree* t, const double* v, double dt)
         const size_t  p = (size_t)pi;
         double        cs[3];
         cell_sizes(t, t->ids[p], cs);
-        const double* in  = t->cur + p * t->flat;
-        double*       out = t->nxt + p * t->flat;
+        const double* in  = t->cur + p * t->pstride;
+        double*       out = t->nxt + p * t->pstride;
         int           idx[3];
         for (idx[0] = h; idx[0] < n + h; ++idx[0])
             for (idx[1] = h; idx[1] < n + h; ++idx[1])
@@ -1019,7 +1049,7 @@ static int padded_is_halo(const oracle_tree* t, size_t li)
     return 0;
 }
 
-int oracle_write_vtk(const oracle_tree* t, const char* path, const char* field)
+int oracle_write_vtk(const oracle_tree* t, const char* path, const char* fields)
 {
     FILE* f = fopen(path, "wb");
     if (!f) return -1;
@@ -1078,17 +1108,25 @@ int oracle_write_vtk(const oracle_tree* t, const char* path, const char* field)
     fprintf(f, "SCALARS is_halo int 1\nLOOKUP_TABLE default\n");
     for (size_t p = 0; p < t->size; ++p)
         for (size_t j = 0; j < per; ++j) put_i32(f, padded_is_halo(t, j));
-    fprintf(f, "SCALARS %s double 1\nLOOKUP_TABLE default\n", field);
-    for (size_t p = 0; p < t->size; ++p) {
-        const double* u = t->cur + p * t->flat;
-        int           idx[3];
-        for (idx[0] = h; idx[0] < n + h; ++idx[0])
-            for (idx[1] = h; idx[1] < n + h; ++idx[1])
-                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
-                    size_t li = 0;
-                    for (int k = 0; k < rank; ++k) li = li * t->pad1 + (size_t)idx[k];
-                    put_f64(f, u[li]);
-                }
+    /* one SCALARS block per field, in tuple order; `fields` names them,
+     * separated by commas */
+    const char* name = fields;
+    for (int fi = 0; fi < t->nvar; ++fi) {
+        size_t len = 0;
+        while (name[len] && name[len] != ',') ++len;
+        fprintf(f, "SCALARS %.*s double 1\nLOOKUP_TABLE default\n", (int)len, name);
+        name += len + (name[len] == ',' ? 1 : 0);
+        for (size_t p = 0; p < t->size; ++p) {
+            const double* u = t->cur + p * t->pstride + (size_t)fi * t->flat;
+            int           idx[3];
+            for (idx[0] = h; idx[0] < n + h; ++idx[0])
+                for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                    for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                        size_t li = 0;
+                        for (int k = 0; k < rank; ++k) li = li * t->pad1 + (size_t)idx[k];
+                        put_f64(f, u[li]);
+                    }
+        }
     }
     return fclose(f) == 0 ? 0 : -1;
 }
@@ -1266,6 +1304,205 @@ size_t oracle_adjoint(oracle_tree* t, size_t steps, const double* v, double cfl,
     return ex;
 }
 
+/* ---------------------------------------------------------------- Euler */
+/* EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) with
+ * amr_solver's time_step_cpu / compute_time_step_cpu / initialize
+ * (amr_solver.hpp:105-145, 265-413): NVAR = DIM + 2 conservative fields
+ * (rho, rho u_d, E), Rusanov flux with the maximum of |u_dir| + a of the two
+ * sides, each face flux evaluated by both cells (as the reference does),
+ * forward Euler. */
+static double max_d(double a, double b) { return (a < b) ? b : a; } /* std::max */
+
+static void euler_flux(int dim, const double* UL, const double* UR, double* flux, int dir, double gamma)
+{
+    const double inv_rho_L = 1.0 / UL[0];
+    double       K_L       = 0.0;
+    for (int d = 0; d < dim; ++d) K_L += UL[1 + d] * UL[1 + d];
+    K_L *= 0.5 * inv_rho_L;
+    const double p_L     = (gamma - 1.0) * (UL[dim + 1] - K_L);
+    const double a_L     = sqrt(gamma * p_L * inv_rho_L);
+    const double u_dir_L = UL[1 + dir] * inv_rho_L;
+    const double inv_rho_R = 1.0 / UR[0];
+    double       K_R       = 0.0;
+    for (int d = 0; d < dim; ++d) K_R += UR[1 + d] * UR[1 + d];
+    K_R *= 0.5 * inv_rho_R;
+    const double p_R     = (gamma - 1.0) * (UR[dim + 1] - K_R);
+    const double a_R     = sqrt(gamma * p_R * inv_rho_R);
+    const double u_dir_R = UR[1 + dir] * inv_rho_R;
+    const double smax    = max_d(fabs(u_dir_L) + a_L, fabs(u_dir_R) + a_R);
+    flux[0] = 0.5 * (UL[1 + dir] + UR[1 + dir] - smax * (UR[0] - UL[0]));
+    for (int d = 0; d < dim; ++d) {
+        double fL_mom = UL[1 + d] * u_dir_L;
+        double fR_mom = UR[1 + d] * u_dir_R;
+        if (d == dir) {
+            fL_mom += p_L;
+            fR_mom += p_R;
+        }
+        flux[1 + d] = 0.5 * (fL_mom + fR_mom - smax * (UR[1 + d] - UL[1 + d]));
+    }
+    const double fL_E = u_dir_L * (UL[dim + 1] + p_L);
+    const double fR_E = u_dir_R * (UR[dim + 1] + p_R);
+    flux[dim + 1]     = 0.5 * (fL_E + fR_E - smax * (UR[dim + 1] - UL[dim + 1]));
+}
+
+/* getMaxSpeed: |u_dir| + a of one cell */
+static double euler_speed(int dim, const double* U, int dir, double gamma)
+{
+    const double inv_rho = 1.0 / U[0];
+    double       K       = 0.0;
+    for (int d = 0; d < dim; ++d) K += U[1 + d] * U[1 + d];
+    K *= 0.5 * inv_rho;
+    const double p     = (gamma - 1.0) * (U[dim + 1] - K);
+    const double a     = sqrt(gamma * p * inv_rho);
+    const double u_dir = U[1 + dir] * inv_rho;
+    return fabs(u_dir) + a;
+}
+
+static void gather_cell(const oracle_tree* t, const double* patch, size_t li, double* U)
+{
+    for (int f = 0; f < t->nvar; ++f) U[f] = patch[(size_t)f * t->flat + li];
+}
+
+double oracle_euler_dt(const oracle_tree* t, double gamma, double cfl)
+{
+    const int    rank = t->rank, n = t->n, h = t->h;
+    const size_t P1 = t->pad1;
+    double       dt = 1.7976931348623157e308;
+    for (size_t p = 0; p < t->size; ++p) {
+        double cs[3];
+        cell_sizes(t, t->ids[p], cs);
+        const double* u = t->cur + p * t->pstride;
+        int           idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    size_t li = 0;
+                    for (int k = 0; k < rank; ++k) li = li * P1 + (size_t)idx[k];
+                    double U[5];
+                    gather_cell(t, u, li, U);
+                    for (int d = 0; d < rank; ++d) {
+                        const double speed = euler_speed(rank, U, d, gamma);
+                        if (speed > 1e-12) {
+                            const double c = cs[d] / speed;
+                            if (c < dt) dt = c;
+                        }
+                    }
+                }
+    }
+    return cfl * dt;
+}
+
+static void euler_step(oracle_tree* t, double gamma, double dt)
+{
+    const int    rank = t->rank, n = t->n, h = t->h, nv = t->nvar;
+    const size_t P1 = t->pad1;
+    const size_t stride[3] = { 1, P1, P1 * P1 };
+    const long   np = (long)t->size;
+#pragma omp parallel for schedule(static) if (np > 16) num_threads(g_threads > 0 ? g_threads : 1)
+    for (long pi = 0; pi < np; ++pi) {
+        const size_t  p = (size_t)pi;
+        double        cs[3];
+        cell_sizes(t, t->ids[p], cs);
+        const double* in  = t->cur + p * t->pstride;
+        double*       out = t->nxt + p * t->pstride;
+        int           idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    size_t li = 0;
+                    for (int k = 0; k < rank; ++k) li = li * P1 + (size_t)idx[k];
+                    double total[5] = { 0, 0, 0, 0, 0 }, Uc[5], UL[5], UR[5], fL[5], fR[5];
+                    gather_cell(t, in, li, Uc);
+                    for (int d = 0; d < rank; ++d) {
+                        gather_cell(t, in, li - stride[d], UL);
+                        gather_cell(t, in, li + stride[d], UR);
+                        euler_flux(rank, UL, Uc, fL, d, gamma);
+                        euler_flux(rank, Uc, UR, fR, d, gamma);
+                        const double dt_over_dx = dt / cs[d];
+                        for (int k = 0; k < nv; ++k) total[k] -= dt_over_dx * (fR[k] - fL[k]);
+                    }
+                    for (int k = 0; k < nv; ++k) out[(size_t)k * t->flat + li] = in[(size_t)k * t->flat + li] + total[k];
+                }
+    }
+    double* tmp = t->cur;
+    t->cur      = t->nxt;
+    t->nxt      = tmp;
+    oracle_halo_exchange(t);
+}
+
+/* advance_batch_async (CPU branch) with EulerPhysics; fills dts (if not
+ * NULL, room for `steps`) with the step sizes. */
+double oracle_euler_advance(oracle_tree* t, size_t steps, double gamma, double cfl, double remaining,
+                            size_t* executed, double* dts)
+{
+    double acc   = 0.0;
+    size_t count = 0;
+    for (size_t s = 0; s < steps; ++s) {
+        if (remaining <= 0.0) break;
+        const double dt      = oracle_euler_dt(t, gamma, cfl);
+        const double step_dt = dt < remaining ? dt : remaining;
+        if (step_dt <= 0.0) break;
+        euler_step(t, gamma, step_dt);
+        if (dts) dts[count] = step_dt;
+        acc += step_dt;
+        remaining -= step_dt;
+        ++count;
+    }
+    if (executed) *executed = count;
+    return acc;
+}
+
+/* amr_solver::initialize with the acoustic pulse of
+ * benchmark/bench_fvm_solver_integration.b.cpp:140-178: primitive state
+ * (rho_bg + 0.2 A e, 0, .., p_bg + A e), e = exp(-|x - c|^2 / width_sq),
+ * converted by primitiveToConservative at each cell centre
+ * (physics_system::cell_coord + 0.5 cell size). */
+void oracle_euler_init_pulse(oracle_tree* t, double gamma, double rho_bg, double p_bg, double amplitude,
+                             double width_sq, const double* centre)
+{
+    const int    rank = t->rank, n = t->n, h = t->h;
+    const size_t P1 = t->pad1;
+    const double maxc = (double)(1u << t->depth);
+    for (size_t p = 0; p < t->size; ++p) {
+        uint32_t mc[3];
+        int      level;
+        oracle_decode(rank, t->ids[p], mc, &level);
+        double cs[3], origin[3];
+        cell_sizes(t, t->ids[p], cs);
+        for (int k = 0; k < rank; ++k) origin[k] = t->lengths[k] * (double)mc[k] / maxc;
+        double* u = t->cur + p * t->pstride;
+        int     idx[3];
+        for (idx[0] = h; idx[0] < n + h; ++idx[0])
+            for (idx[1] = h; idx[1] < n + h; ++idx[1])
+                for (idx[2] = (rank == 3 ? h : 0); idx[2] < (rank == 3 ? n + h : 1); ++idx[2]) {
+                    size_t li = 0;
+                    for (int k = 0; k < rank; ++k) li = li * P1 + (size_t)idx[k];
+                    double x[3];
+                    for (int k = 0; k < rank; ++k) {
+                        const double cell = origin[k] + (double)(idx[rank - 1 - k] - h) * cs[k];
+                        x[k]              = cell + 0.5 * cs[k];
+                    }
+                    double r_sq = 0.0;
+                    for (int k = 0; k < rank; ++k) {
+                        const double dx = x[k] - centre[k];
+                        r_sq += dx * dx;
+                    }
+                    const double pert = amplitude * exp(-r_sq / width_sq);
+                    const double rho  = rho_bg + (pert * 0.2);
+                    const double pres = p_bg + pert;
+                    /* primitiveToConservative (EulerPhysics.hpp:34-60), u = 0 */
+                    double vel_squared = 0.0;
+                    u[li] = rho;
+                    for (int d = 0; d < rank; ++d) {
+                        const double ud                        = 0.0;
+                        u[(size_t)(1 + d) * t->flat + li] = rho * ud;
+                        vel_squared += ud * ud;
+                    }
+                    u[(size_t)(rank + 1) * t->flat + li] = pres / (gamma - 1.0) + 0.5 * rho * vel_squared;
+                }
+    }
+}
+
 /* ------------------------------------------------------------ criteria */
 /* max|grad u|*h with central differences over face ghosts and the any/all
  * patch rule of dg_helpers/globals/amr_indicators.hpp:186-225; level bounds
@@ -1277,7 +1514,7 @@ void oracle_flags_gradient(const oracle_tree* t, double rthr, double cthr, int m
     const size_t P1 = t->pad1;
     const size_t stride[3] = { 1, P1, P1 * P1 };
     for (size_t p = 0; p < t->size; ++p) {
-        const double* u = t->cur + p * t->flat;
+        const double* u = t->cur + p * t->pstride;
         int any = 0, all = 1, idx[3];
         for (idx[0] = h; idx[0] < n + h; ++idx[0])
             for (idx[1] = h; idx[1] < n + h; ++idx[1])
@@ -1305,7 +1542,7 @@ void oracle_flags_max(const oracle_tree* t, double rthr, double cthr, int min_le
                       int8_t* out)
 {
     for (size_t p = 0; p < t->size; ++p) {
-        const double* u = t->cur + p * t->flat;
+        const double* u = t->cur + p * t->pstride; /* the first field (e.g. Rho) */
         double        m = 0.0;
         for (size_t c = 0; c < t->flat; ++c)
             if (u[c] > m) m = u[c];
@@ -1349,7 +1586,7 @@ void oracle_init_state(oracle_tree* t, const double* bumps, int nbumps, double n
         double cs[3], origin[3];
         cell_sizes(t, t->ids[p], cs);
         for (int k = 0; k < rank; ++k) origin[k] = 1.0 * (double)mc[k] / maxc;
-        double*  u    = t->cur + p * t->flat;
+        double*  u    = t->cur + p * t->pstride;
         uint64_t cell = 0;
         int      idx[3];
         for (idx[0] = h; idx[0] < n + h; ++idx[0])
@@ -1384,6 +1621,6 @@ void oracle_init_state(oracle_tree* t, const double* bumps, int nbumps, double n
 void oracle_random_state(oracle_tree* t, uint64_t seed)
 {
     for (size_t p = 0; p < t->size; ++p)
-        for (size_t c = 0; c < t->flat; ++c)
-            t->cur[p * t->flat + c] = oracle_unit_hash(seed, t->ids[p], c) - 0.5;
+        for (size_t c = 0; c < t->pstride; ++c)
+            t->cur[p * t->pstride + c] = oracle_unit_hash(seed, t->ids[p], c) - 0.5;
 }

@@ -36,14 +36,19 @@ typedef struct oracle_neighbor {
 
 /* rank 2|3, n cells per dim (even, >= 2*halo), halo width, Morton depth. */
 oracle_tree* oracle_create(int rank, int n, int halo, int depth, size_t capacity);
+/* The same with nvar fields per cell (the reference's SoA field tuple,
+ * e.g. EulerCell2D = Rho, Rhou, Rhov, E2D); state layout per patch:
+ * nvar padded patches, field-major. */
+oracle_tree* oracle_create_fields(int rank, int n, int halo, int depth, size_t capacity, int nvar);
+int          oracle_nvar(const oracle_tree* t);
 void         oracle_destroy(oracle_tree* t);
 
 size_t oracle_size(const oracle_tree* t);
 size_t oracle_flat(const oracle_tree* t);
 void   oracle_get_ids(const oracle_tree* t, uint64_t* out);
 void   oracle_get_neighbors(const oracle_tree* t, oracle_neighbor* out);
-void   oracle_get_state(const oracle_tree* t, double* out);        /* size*flat */
-void   oracle_set_state(oracle_tree* t, const double* in);          /* size*flat */
+void   oracle_get_state(const oracle_tree* t, double* out);        /* size*nvar*flat */
+void   oracle_set_state(oracle_tree* t, const double* in);          /* size*nvar*flat */
 
 /* Tree operations. reconstruct returns 0, or a negative code where the
  * reference would stop (e.g. coarsening into the root, ndtree.hpp:1106). */
@@ -70,9 +75,22 @@ void oracle_random_state(oracle_tree* t, uint64_t seed);
 double oracle_compute_dt(const oracle_tree* t, const double* velocity, double cfl);
 double oracle_advance(oracle_tree* t, size_t steps, const double* velocity,
                       double cfl, double remaining, size_t* executed);
+/* Domain lengths per Morton axis (physics_system's Domain_Sizes; default 1). */
+void oracle_set_lengths(oracle_tree* t, const double* lengths);
+
+/* Euler physics (EulerPhysics<DIM>, nvar = rank + 2 fields): the CFL step
+ * (compute_time_step_cpu x cfl), advance_batch_async (CPU branch; dts, if
+ * not NULL, receives the executed step sizes) and the acoustic-pulse
+ * initial state of the reference's Euler benchmark. */
+double oracle_euler_dt(const oracle_tree* t, double gamma, double cfl);
+double oracle_euler_advance(oracle_tree* t, size_t steps, double gamma, double cfl, double remaining,
+                            size_t* executed, double* dts);
+void   oracle_euler_init_pulse(oracle_tree* t, double gamma, double rho_bg, double p_bg, double amplitude,
+                               double width_sq, const double* centre);
+
 /* vtk_print::print of the current tree and state (legacy binary VTK, one
  * quad/voxel per interior cell); field = the scalar's name.  0 on success. */
-int oracle_write_vtk(const oracle_tree* t, const char* path, const char* field);
+int oracle_write_vtk(const oracle_tree* t, const char* path, const char* fields); /* names, comma-separated */
 
 /* Gradient of <lam_T, u_T> w.r.t. the interior of u_0 for oracle_advance on
  * the current (frozen) mesh: transposed steps in reverse order (size*flat

@@ -76,6 +76,16 @@ def lib():
         L.oracle_parent_of.restype = u64
         L.oracle_parent_of.argtypes = [i32, i32, u64]
         L.oracle_set_threads.argtypes = [i32]
+        L.oracle_create_fields.restype = vp
+        L.oracle_create_fields.argtypes = [i32, i32, i32, i32, sz, i32]
+        L.oracle_nvar.restype = i32
+        L.oracle_nvar.argtypes = [vp]
+        L.oracle_set_lengths.argtypes = [vp, P(np.float64, flags="C")]
+        L.oracle_euler_dt.restype = dbl
+        L.oracle_euler_dt.argtypes = [vp, dbl, dbl]
+        L.oracle_euler_advance.restype = dbl
+        L.oracle_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl, C.POINTER(sz), vp]
+        L.oracle_euler_init_pulse.argtypes = [vp, dbl, dbl, dbl, dbl, dbl, P(np.float64, flags="C")]
         _lib = L
     return _lib
 
@@ -83,12 +93,17 @@ def lib():
 class OracleTree:
     """CPU restatement of ``ndtree`` + ``amr_solver`` for one scalar field."""
 
-    def __init__(self, rank: int, n: int, halo: int = 1, depth: int = 7, capacity: int = 20000):
-        self.rank, self.n, self.halo, self.depth = rank, n, halo, depth
-        self._t = lib().oracle_create(rank, n, halo, depth, capacity)
+    def __init__(self, rank: int, n: int, halo: int = 1, depth: int = 7, capacity: int = 20000, nvar: int = 1,
+                 lengths=None):
+        """nvar > 1: that many fields per cell (Euler: rank + 2); lengths:
+        domain lengths per Morton axis (default 1)."""
+        self.rank, self.n, self.halo, self.depth, self.nvar = rank, n, halo, depth, nvar
+        self._t = lib().oracle_create_fields(rank, n, halo, depth, capacity, nvar)
         if not self._t:
             raise ValueError("bad oracle tree parameters")
         self.pad1 = n + 2 * halo
+        if lengths is not None:
+            lib().oracle_set_lengths(self._t, np.ascontiguousarray(lengths, np.float64))
 
     def __del__(self):
         t = getattr(self, "_t", None)
@@ -115,14 +130,35 @@ class OracleTree:
         return out.reshape(self.size, 2 * self.rank)
 
     def state(self) -> np.ndarray:
-        out = np.empty(self.size * self.flat, np.float64)
+        """(size, pad1, ...) for one field, (size, nvar, pad1, ...) for several."""
+        out = np.empty(self.size * self.flat * self.nvar, np.float64)
         lib().oracle_get_state(self._t, out)
-        return out.reshape((self.size,) + (self.pad1,) * self.rank)
+        if self.nvar == 1:
+            return out.reshape((self.size,) + (self.pad1,) * self.rank)
+        return out.reshape((self.size, self.nvar) + (self.pad1,) * self.rank)
 
     def set_state(self, s: np.ndarray) -> None:
         s = np.ascontiguousarray(s, np.float64).reshape(-1)
-        assert s.size == self.size * self.flat
+        assert s.size == self.size * self.flat * self.nvar
         lib().oracle_set_state(self._t, s)
+
+    # -------------------------------------------------------------- Euler
+    def euler_init_pulse(self, gamma=1.4, rho_bg=0.5, p_bg=1.0, amplitude=10.0, width_sq=0.01 * 1000.0 * 1000.0,
+                         centre=(500.0, 500.0, 500.0)):
+        c = np.zeros(3)
+        c[: len(centre)] = centre
+        lib().oracle_euler_init_pulse(self._t, gamma, rho_bg, p_bg, amplitude, width_sq, c)
+
+    def euler_dt(self, gamma, cfl) -> float:
+        return lib().oracle_euler_dt(self._t, gamma, cfl)
+
+    def euler_advance(self, steps, gamma, cfl, remaining=1.7976931348623157e308):
+        """(simulated time, executed steps, step sizes)."""
+        ex = C.c_size_t(0)
+        dts = np.zeros(max(1, steps))
+        acc = lib().oracle_euler_advance(self._t, steps, gamma, cfl, remaining, C.byref(ex),
+                                         dts.ctypes.data_as(C.c_void_p))
+        return acc, ex.value, dts[: ex.value]
 
     def reconstruct(self, flags: np.ndarray) -> int:
         f = np.ascontiguousarray(flags, np.int8)

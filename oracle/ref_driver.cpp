@@ -19,6 +19,11 @@
 //                       include/dg_helpers/globals/amr_indicators.hpp:186-225.
 //   max criterion      - the max-value rule of tests/advection_equation_amr.t.cpp:155-170.
 //   random criterion   - hash-driven flags for tree-operation coverage.
+//   mode=euler          - the reference's amr_solver with EulerPhysics<DIM>
+//                       on the acoustic pulse of its Euler benchmark
+//                       (benchmark/bench_fvm_solver_integration.b.cpp:
+//                       95-178: domain 1000^DIM, max-Rho criterion over the
+//                       padded patch, re-mesh every `remesh` steps).
 //   vtk=<name>          - after the mode, the reference's VTK writer
 //                       (include/ndtree/vtk_print.hpp) prints the tree to
 //                       vtk_output/<name>.vtk.
@@ -30,6 +35,7 @@
 #include "ndtree/ndtree.hpp"
 #include "ndtree/patch_layout.hpp"
 #include "ndtree/vtk_print.hpp"
+#include "solver/EulerPhysics.hpp"
 #include "solver/amr_solver.hpp"
 #include "solver/cell_types.hpp"
 #include "solver/physics_system.hpp"
@@ -174,6 +180,62 @@ struct RuntimeAdvection
     }
 };
 
+// TAG_TREE record of a tree: per leaf its Morton id and, per direction, the
+// neighbour variant (kind, contact quadrant, ids).
+template <int DIM, typename Tree>
+void dump_tree_records(Tree& t, writer& W, std::uint32_t step)
+{
+    using dir_t                  = typename Tree::patch_direction_t;
+    const std::uint64_t n        = t.size();
+    const std::uint64_t per_dir  = 4 + 4 + 4 * 8;
+    W.header(TAG_TREE, step, 8 + n * (8 + 2 * DIM * per_dir));
+    W.put(n);
+    for (std::size_t i = 0; i != n; ++i)
+    {
+        W.put(static_cast<std::uint64_t>(t.get_node_index_at(i).id()));
+        for (auto d = dir_t::first(); d != dir_t::sentinel(); d.advance())
+        {
+            const auto    nb     = t.get_neighbor_at(i, d);
+            std::uint8_t  kind   = 0;
+            std::uint8_t  q[3]   = { 0, 0, 0 };
+            std::uint64_t ids[4] = { 0, 0, 0, 0 };
+            using nv_t           = std::remove_cvref_t<decltype(nb)>;
+            std::visit(
+                [&](auto const& v)
+                {
+                    using V = std::remove_cvref_t<decltype(v)>;
+                    if constexpr (std::is_same_v<V, typename nv_t::none>)
+                    {
+                        kind = 0;
+                    }
+                    else if constexpr (std::is_same_v<V, typename nv_t::same>)
+                    {
+                        kind   = 1;
+                        ids[0] = v.id.id();
+                    }
+                    else if constexpr (std::is_same_v<V, typename nv_t::finer>)
+                    {
+                        kind = 2;
+                        for (std::size_t k = 0; k != v.ids.size(); ++k) ids[k] = v.ids[k].id();
+                    }
+                    else
+                    {
+                        kind   = 3;
+                        ids[0] = v.id.id();
+                        for (std::size_t k = 0; k != v.contact_quadrant.size(); ++k)
+                            q[k] = static_cast<std::uint8_t>(v.contact_quadrant[k]);
+                    }
+                },
+                nb.data
+            );
+            W.put(kind);
+            W.bytes(q, 3);
+            W.put(std::uint32_t{ 0 });
+            W.bytes(ids, sizeof(ids));
+        }
+    }
+}
+
 template <int DIM, std::size_t N, std::size_t H, unsigned Depth>
 struct harness
 {
@@ -214,58 +276,7 @@ struct harness
     auto tree() -> tree_t& { return solver.get_tree(); }
 
     // ---- dumps
-    void dump_tree(std::uint32_t step)
-    {
-        auto&               t = tree();
-        const std::uint64_t n = t.size();
-        const std::uint64_t per_dir = 4 + 4 + 4 * 8;
-        W.header(TAG_TREE, step, 8 + n * (8 + 2 * DIM * per_dir));
-        W.put(n);
-        for (std::size_t i = 0; i != n; ++i)
-        {
-            W.put(static_cast<std::uint64_t>(t.get_node_index_at(i).id()));
-            for (auto d = dir_t::first(); d != dir_t::sentinel(); d.advance())
-            {
-                const auto     nb = t.get_neighbor_at(i, d);
-                std::uint8_t   kind = 0;
-                std::uint8_t   q[3] = { 0, 0, 0 };
-                std::uint64_t  ids[4] = { 0, 0, 0, 0 };
-                using nv_t = std::remove_cvref_t<decltype(nb)>;
-                std::visit(
-                    [&](auto const& v)
-                    {
-                        using V = std::remove_cvref_t<decltype(v)>;
-                        if constexpr (std::is_same_v<V, typename nv_t::none>)
-                        {
-                            kind = 0;
-                        }
-                        else if constexpr (std::is_same_v<V, typename nv_t::same>)
-                        {
-                            kind   = 1;
-                            ids[0] = v.id.id();
-                        }
-                        else if constexpr (std::is_same_v<V, typename nv_t::finer>)
-                        {
-                            kind = 2;
-                            for (std::size_t k = 0; k != v.ids.size(); ++k) ids[k] = v.ids[k].id();
-                        }
-                        else
-                        {
-                            kind   = 3;
-                            ids[0] = v.id.id();
-                            for (std::size_t k = 0; k != v.contact_quadrant.size(); ++k)
-                                q[k] = static_cast<std::uint8_t>(v.contact_quadrant[k]);
-                        }
-                    },
-                    nb.data
-                );
-                W.put(kind);
-                W.bytes(q, 3);
-                W.put(std::uint32_t{ 0 });
-                W.bytes(ids, sizeof(ids));
-            }
-        }
-    }
+    void dump_tree(std::uint32_t step) { dump_tree_records<DIM>(tree(), W, step); }
 
     void dump_flags(std::uint32_t step)
     {
@@ -528,12 +539,169 @@ struct harness
     }
 };
 
+// ------------------------------------------------------------ Euler
+template <int DIM, std::size_t N, std::size_t H, unsigned Depth>
+struct euler_harness
+{
+    using shape_t = std::conditional_t<
+        DIM == 2,
+        amr::containers::static_shape<N, N>,
+        amr::containers::static_shape<N, N, N>>;
+    using layout_t       = amr::containers::static_layout<shape_t>;
+    using patch_index_t  = amr::ndt::morton::morton_id<Depth, unsigned(DIM)>;
+    using patch_layout_t = amr::ndt::patches::patch_layout<layout_t, H>;
+    using interp_t = amr::ndt::intergrid_operator::linear_interpolator<patch_layout_t>;
+    using cell_t   = std::conditional_t<DIM == 2, amr::cell::EulerCell2D, amr::cell::EulerCell3D>;
+    using tree_t   = amr::ndt::tree::ndtree<cell_t, patch_index_t, patch_layout_t, interp_t>;
+    static constexpr std::array<double, DIM> lengths = [] {
+        std::array<double, DIM> l{};
+        for (auto& e : l) e = 1000.0;
+        return l;
+    }();
+    using geometry_t = amr::ndt::solver::physics_system<patch_index_t, patch_layout_t, lengths>;
+    using phys_t     = EulerPhysics<DIM>;
+    using solver_t   = amr_solver<tree_t, geometry_t, phys_t, DIM>;
+    using padded_t   = typename patch_layout_t::padded_layout_t;
+    using status_t   = typename tree_t::refine_status_t;
+    using fields_t   = typename phys_t::FieldTags;
+    static constexpr std::size_t flat = patch_layout_t::flat_size();
+    static constexpr int         NVAR = phys_t::NVAR;
+
+    params const&            P;
+    writer&                  W;
+    solver_t                 solver;
+    std::vector<std::int8_t> last_flags;
+
+    euler_harness(params const& p, writer& w)
+        : P(p), W(w),
+          solver(static_cast<std::size_t>(p.integer("capacity", 20000)), p.num("gamma", 1.4), p.num("cfl", 0.3))
+    {
+    }
+
+    auto tree() -> tree_t& { return solver.get_tree(); }
+
+    void dump_state(std::uint32_t step)
+    {
+        auto&               t = tree();
+        const std::uint64_t n = t.size();
+        // patch-major, fields in tuple order within a patch
+        W.header(TAG_STATE, step, 16 + n * NVAR * flat * 8);
+        W.put(n * NVAR);
+        W.put(static_cast<std::uint64_t>(flat));
+        for (std::size_t i = 0; i != n; ++i)
+        {
+            [&]<std::size_t... Is>(std::index_sequence<Is...>)
+            {
+                (
+                    [&]
+                    {
+                        auto const& p = t.template get_patch<std::tuple_element_t<Is, fields_t>>(i);
+                        for (std::size_t c = 0; c != flat; ++c)
+                        {
+                            double v = p[static_cast<typename padded_t::index_t>(c)];
+                            W.put(v);
+                        }
+                    }(),
+                    ...);
+            }(std::make_index_sequence<NVAR>{});
+        }
+    }
+
+    // the benchmark's acoustic_wave_amr_criterion: max Rho over the padded patch
+    auto max_rho_status(patch_index_t const& idx) -> status_t
+    {
+        const double rthr = P.num("rthr", 0.53);
+        const double cthr = P.num("cthr", 0.49);
+        const int    minl = static_cast<int>(P.integer("min_level", 1));
+        const int    maxl = static_cast<int>(P.integer("max_level", 6));
+        auto const&  p    = tree().template get_patch<amr::cell::Rho>(idx);
+        double       m    = 0.0;
+        for (std::size_t c = 0; c != flat; ++c) m = std::max(p[static_cast<typename padded_t::index_t>(c)], m);
+        const int level = static_cast<int>(idx.level());
+        if (level < maxl && m > rthr) return status_t::Refine;
+        if (level > minl && m < cthr) return status_t::Coarsen;
+        return status_t::Stable;
+    }
+
+    int run()
+    {
+        auto refine_all = [](patch_index_t const&) { return status_t::Refine; };
+        for (long i = 0; i < P.integer("init_levels", 3); ++i)
+        {
+            tree().reconstruct_tree(refine_all);
+            tree().halo_exchange_update();
+        }
+        const double rho_bg = P.num("rho_bg", 0.5), p_bg = P.num("p_bg", 1.0), amp = P.num("amp", 10.0);
+        const double width_sq = P.num("width_sq", 0.01 * 1000.0 * 1000.0);
+        auto         pulse    = [&](auto const& coords) -> amr::containers::static_vector<double, NVAR>
+        {
+            double r_sq = 0.0;
+            for (int d = 0; d < DIM; ++d)
+            {
+                const double dx = coords[d] - 0.5 * 1000.0;
+                r_sq += dx * dx;
+            }
+            const double perturbation = amp * std::exp(-r_sq / width_sq);
+            amr::containers::static_vector<double, NVAR> prim;
+            prim[0] = rho_bg + (perturbation * 0.2);
+            for (int d = 0; d < DIM; ++d) prim[1 + d] = 0.0;
+            prim[DIM + 1] = p_bg + perturbation;
+            return prim;
+        };
+        solver.initialize(pulse);
+        tree().halo_exchange_update();
+        dump_tree_records<DIM>(tree(), W, 0);
+        dump_state(0);
+        const long   steps    = P.integer("steps", 60);
+        const long   interval = P.integer("remesh", 10);
+        const double tmax     = P.num("tmax", 1e300);
+        long         done = 0, batch = 0;
+        double       t = 0.0;
+        while (done < steps && t < tmax)
+        {
+            const long k = std::min(interval, steps - done);
+            solver.advance_batch_async(static_cast<std::size_t>(k), tmax - t);
+            std::size_t executed = 0;
+            t += solver.finish_advance_batch(&executed);
+            done += static_cast<long>(executed);
+            ++batch;
+            last_flags.clear();
+            auto recording = [&](patch_index_t const& idx) -> status_t
+            {
+                const auto st = max_rho_status(idx);
+                last_flags.push_back(static_cast<std::int8_t>(st));
+                return st;
+            };
+            tree().reconstruct_tree(recording);
+            tree().halo_exchange_update();
+            W.header(TAG_FLAGS, static_cast<std::uint32_t>(done), 8 + last_flags.size());
+            W.put(static_cast<std::uint64_t>(last_flags.size()));
+            W.bytes(last_flags.data(), last_flags.size());
+            dump_tree_records<DIM>(tree(), W, static_cast<std::uint32_t>(done));
+            if (P.integer("state_every", 0) > 0 && batch % P.integer("state_every", 0) == 0)
+                dump_state(static_cast<std::uint32_t>(done));
+            if (executed == 0) break;
+        }
+        dump_state(static_cast<std::uint32_t>(done));
+        W.header(TAG_DT, static_cast<std::uint32_t>(done), 16);
+        W.put(t);
+        W.put(static_cast<std::uint64_t>(done));
+        std::printf("{\"steps\": %ld, \"time\": %.17g, \"leaves\": %zu}\n", done, t, tree().size());
+        return 0;
+    }
+};
+
 template <int DIM, std::size_t N, std::size_t H, unsigned Depth>
 int dispatch(params const& p)
 {
     writer w(p.str("out", "dump.bin"));
-    auto   h = std::make_unique<harness<DIM, N, H, Depth>>(p, w);
     const auto mode = p.str("mode", "run");
+    if (mode == "euler")
+    {
+        auto e = std::make_unique<euler_harness<DIM, N, H, Depth>>(p, w);
+        return e->run();
+    }
+    auto h = std::make_unique<harness<DIM, N, H, Depth>>(p, w);
     const int  rc   = mode == "tree" ? h->tree_mode() : h->run();
     if (rc == 0 && p.has("vtk"))
     {

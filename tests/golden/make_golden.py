@@ -134,6 +134,52 @@ def scenario_tree(name, cfg, rank, n, h, params, keep_states=None):
     return info
 
 
+def scenario_euler(name, cfg, rank, n, h, params):
+    """The reference's amr_solver with EulerPhysics<rank> on the acoustic
+    pulse (domain 1000^rank): trees and flags after every re-mesh, initial
+    and final states (all fields), simulated time."""
+    nvar = rank + 2
+    tmp = Path("/tmp") / f"golden_{name}.bin"
+    info = run(dict(cfg=cfg, mode="euler", **params), tmp)
+    recs = read_records(str(tmp), rank)
+    trees = [r for r in recs if r[0] == TAG_TREE]
+    flags = [r for r in recs if r[0] == TAG_FLAGS]
+    states = [r for r in recs if r[0] == TAG_STATE]
+    (time, steps) = [r for r in recs if r[0] == TAG_DT][0][2]
+    P1 = n + 2 * h
+    out = {
+        "meta": np.array(json.dumps({"cfg": cfg, "rank": rank, "n": n, "halo": h, "depth": 7, "nvar": nvar,
+                                     "lengths": [1000.0] * rank, "params": params, "info": info})),
+        "remeshes": np.int64(len(flags)),
+        "ids_init": trees[0][2]["ids"],
+        "state_init": states[0][2].reshape((-1, nvar) + (P1,) * rank),
+        "state_final": states[-1][2].reshape((-1, nvar) + (P1,) * rank),
+        "time": np.float64(time),
+        "steps": np.int64(steps),
+    }
+    for k, (fl, tr) in enumerate(zip(flags, trees[1:])):
+        ids = tr[2]["ids"]
+        kind, nbid, quad = linear_neighbors(ids, tr[2]["nb"])
+        out[f"flags_{k}"] = fl[2]
+        out[f"ids_{k}"] = ids
+        out[f"kind_{k}"] = kind
+        out[f"nbid_{k}"] = nbid
+        out[f"quad_{k}"] = quad
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    return info
+
+
+EULER_SCENARIOS = [
+    # the reference Euler benchmark's set-up on smaller patches: 8x8 + 1 ghost,
+    # 3 uniform levels, max-Rho criterion 0.53 / 0.49 on levels 1..4, gamma 1.4,
+    # CFL 0.3, re-mesh every 10 steps
+    ("euler_pulse_2d", "2d8h1", 2, 8, 1, dict(init_levels=3, steps=60, remesh=10, max_level=4, min_level=1,
+                                              gamma=1.4, cfl=0.3)),
+    ("euler_pulse_3d", "3d4h1", 3, 4, 1, dict(init_levels=2, steps=30, remesh=10, max_level=3, min_level=1,
+                                              gamma=1.4, cfl=0.3)),
+]
+
+
 VTK_SCENARIOS = {
     # name of the npz fixture whose final tree and state are printed -> driver arguments
     "config1_uniform_2d": ("2d8h1", dict(mode="run", init_levels=2, steps=100, remesh=0, vel="1,0.5", cfl=0.4,
@@ -169,10 +215,15 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--vtk-only", action="store_true", help="only the VTK writer fixture")
+    ap.add_argument("--euler-only", action="store_true", help="only the Euler fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={a.ref}"], check=True)
     if a.vtk_only:
         print(vtk_golden())
+        return
+    if a.euler_only:
+        for sc in EULER_SCENARIOS:
+            print(scenario_euler(*sc))
         return
 
     # 1: 2D uniform depth 2, 16 leaves of 8x8, FP64, 100 steps, config as in the
@@ -208,6 +259,8 @@ def main():
         keep_states={0, 4}))
     print(scenario_tree("tree_random_2d_h2", "2d10h2", 2, 10, 2, dict(
         seed=14, passes=4, init_levels=1, max_level=4, min_level=1, p_refine=0.3, p_coarsen=0.5)))
+    for sc in EULER_SCENARIOS:
+        print(scenario_euler(*sc))
     print(vtk_golden())
 
 

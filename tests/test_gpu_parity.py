@@ -375,3 +375,34 @@ def test_bounded_wait_reports_timeout_and_context_survives(amr):
     t.upload_state(np.random.default_rng(0).random((t.size, 18, 18)))
     st = t.run(20, 10, (1.0, 0.5), 0.4, "grad", 0.05, 0.01, 1, 3)
     assert st["executed_steps"] == 20
+
+
+def test_reserve_keeps_the_tree_and_runs_continue(amr):
+    """amr_tree_reserve grows (and shrinks) the capacity in place: leaves,
+    state and tables survive, and a run continued after it equals the run
+    without it, on both drivers (the interval graph is re-captured)."""
+    import amr_gb300 as A
+
+    b = A.seeded_bumps(2, 6, 4, sigma=(0.03, 0.06), amp=(0.5, 2.0), lo=0.05, hi=0.95)
+    res = []
+    for grow in (False, True):
+        t = amr.Tree(2, 16, 1, 7, capacity=8000)
+        t.refine_uniform(4)
+        t.upload_state(A.gaussian_state(t.ids(), 2, 16, 1, 7, b))
+        t.run(12, 4, (0.8, 0.6), 0.4, "grad", 0.02, 0.004, 2, 6, per_launch=True)
+        if grow:
+            ids, nb, st = t.ids(), t.neighbors(), t.download_state()
+            t.reserve(20000)
+            assert t.capacity == 20000
+            np.testing.assert_array_equal(t.ids(), ids)
+            np.testing.assert_array_equal(t.neighbors(), nb)
+            np.testing.assert_array_equal(t.download_state(), st)
+        t.run(12, 4, (0.8, 0.6), 0.4, "grad", 0.02, 0.004, 2, 6, per_launch=True)
+        if grow:
+            t.reserve(t.size)  # shrink to fit
+            assert t.capacity == t.size
+        res.append((t.ids(), interior(t.download_state(), 2, 16, 1)))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    with pytest.raises(amr.AmrError):
+        t.reserve(t.size - 1)
