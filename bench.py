@@ -556,6 +556,133 @@ def vtk_extra(torch, A, dev, stream, with_cpu=True):
     return out
 
 
+# ------------------------------------------------------------ Euler form
+# The reference's Euler benchmark (benchmark/bench_fvm_solver_integration.
+# b.cpp:34-250): 2D EulerPhysics, 64x64 patches + 1 ghost, Morton depth 7,
+# domain 1000 x 1000, three uniform levels, acoustic pulse (rho_bg 0.5, p_bg
+# 1, amplitude 10, width^2 = 0.01 L^2, centre (500, 500)), gamma 1.4, CFL
+# 0.3, max-Rho criterion 0.53 / 0.49 on levels 1..6, re-mesh every 10
+# steps, until t = 50.
+EULER = dict(n=64, halo=1, depth=7, lengths=(1000.0, 1000.0), init_levels=3, gamma=1.4, cfl=0.3, end_time=50.0,
+             interval=10, rthr=0.53, cthr=0.49, min_level=1, max_level=6, capacity=10000, rho_bg=0.5, p_bg=1.0,
+             amp=10.0, width_sq=0.01 * 1000.0 * 1000.0, centre=(500.0, 500.0), cpu_seconds=15.0, cpu_max_intervals=40)
+
+
+def euler_ic(A, ids):
+    """The acoustic pulse at the cell centres, primitive (rho, 0, 0, p) to
+    conservative; host array (4, P, n+2, n+2), ghosts zero."""
+    E = EULER
+    n, h = E["n"], E["halo"]
+    x = A.cell_centres(ids, 2, n, E["depth"], E["lengths"])
+    r2 = (x[..., 0] - E["centre"][0]) ** 2 + (x[..., 1] - E["centre"][1]) ** 2
+    pert = E["amp"] * np.exp(-r2 / E["width_sq"])
+    rho = E["rho_bg"] + pert * 0.2
+    pres = E["p_bg"] + pert
+    st = np.zeros((4, len(ids), n + 2 * h, n + 2 * h))
+    st[0][:, h:n + h, h:n + h] = rho
+    st[3][:, h:n + h, h:n + h] = pres / (E["gamma"] - 1.0)
+    return st
+
+
+def euler_tree(A, stream, capacity=None):
+    E = EULER
+    t = A.Tree(2, E["n"], E["halo"], E["depth"], capacity=capacity or E["capacity"], dtype=A.F64,
+               lengths=E["lengths"] + (1.0,), stream=stream.cuda_stream, fields=4)
+    t.refine_uniform(E["init_levels"])
+    st0 = euler_ic(A, t.ids())
+    t.upload_state(st0)
+    t.halo_exchange()
+    return t, st0
+
+
+def euler_run(t, steps):
+    E = EULER
+    return t.euler_run(steps, E["interval"], E["gamma"], E["cfl"], E["end_time"], E["rthr"], E["cthr"],
+                       E["min_level"], E["max_level"])
+
+
+def euler_extra(torch, A, stream, with_cpu=True):
+    """The reference's Euler benchmark loop to t = 50 through
+    amr_tree_euler_run (wall clock around the loop, as the reference times
+    it); the step kernels timed with CUDA events on the final mesh; and the
+    oracle (C restatement, OpenMP over patches) on the first intervals of the
+    same run, whose state the GPU run must reproduce bit for bit."""
+    E = EULER
+    out = {"workload": "reference Euler benchmark: 2D, 64x64 patches + 1 ghost, acoustic pulse on 1000 x 1000, "
+                       "levels 1..6 by max Rho 0.53/0.49, re-mesh every 10 steps, t = 0..50, FP64"}
+    t, _ = euler_tree(A, stream)
+    euler_run(t, 20)  # warm-up
+    t.close()
+    t, st0 = euler_tree(A, stream)
+    torch.cuda.synchronize()
+    l0 = A.launch_count()
+    t0 = time.perf_counter()
+    st = euler_run(t, 10 ** 9)
+    secs = time.perf_counter() - t0
+    cells = int(st["cell_updates"])
+    flat_cells = cells * (E["n"] + 2 * E["halo"]) ** 2 // E["n"] ** 2
+    out.update({"value": cells / secs, "unit": "cell-updates/s (interior cells)", "seconds": secs,
+                "reference_count_value": flat_cells / secs,
+                "reference_count_note": "the reference's printout counts executed x patches x flat_size (ghosts "
+                                        "included, 66^2 per patch)",
+                "sim_time": st["sum_dt"], "steps": int(st["executed_steps"]), "remeshes": int(st["remeshes"]),
+                "leaves_min": int(st["leaves_min"]), "leaves_max": int(st["leaves_max"]),
+                "leaves_final": t.size, "gpu_launches": int(A.launch_count() - l0)})
+    # step kernels on the final mesh: finalize + update + halo per step
+    k = 50
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t.euler_advance(5, E["gamma"], E["cfl"])
+        ev0.record(stream)
+        t.euler_advance(k, E["gamma"], E["cfl"])
+        ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / k
+    step_cells = t.size * E["n"] ** 2
+    out["final_mesh_step"] = {"ms": ms, "cells": step_cells, "cell_updates_per_s": step_cells / (ms * 1e-3),
+                              "bytes_per_cell": 2 * (4 + 5) * 8,
+                              "note": "state (4 fields) and primitives (u, v, p, |u|+a, |v|+a) read and written"}
+    t.close()
+    if with_cpu:
+        from oracle import oracle as O
+
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        o = O.OracleTree(2, E["n"], E["halo"], E["depth"], E["capacity"], nvar=4, lengths=E["lengths"])
+        o.refine_all(E["init_levels"])
+        o.set_state(np.moveaxis(st0, 0, 1))
+        o.halo_exchange()
+        ccells, csecs, sim, intervals = 0, 0.0, 0.0, 0
+        while csecs < E["cpu_seconds"] and intervals < E["cpu_max_intervals"] and sim < E["end_time"]:
+            leaves = o.size
+            c0 = time.perf_counter()
+            acc, ex, _ = o.euler_advance(E["interval"], E["gamma"], E["cfl"], E["end_time"] - sim)
+            f = o.flags_max(E["rthr"], E["cthr"], E["min_level"], E["max_level"])
+            assert o.reconstruct(f) == 0
+            o.halo_exchange()
+            csecs += time.perf_counter() - c0
+            sim += acc
+            ccells += ex * leaves * E["n"] ** 2
+            intervals += 1
+        out["cpu_baseline"] = {"value": ccells / csecs, "unit": "cell-updates/s (interior cells)", "cores": threads,
+                               "kind": "port", "sample": f"first {intervals} intervals ({intervals * E['interval']} "
+                                                         f"steps) of the same run, OpenMP over patches"}
+        # the GPU over the same intervals: the state must be the oracle's
+        g, _ = euler_tree(A, stream)
+        euler_run(g, intervals * E["interval"])
+        same_tree = bool(np.array_equal(g.ids(), o.ids()))
+        m = np.ones((E["n"] + 2,) * 2, bool)
+        m[0, 0] = m[0, -1] = m[-1, 0] = m[-1, -1] = False
+        a = g.download_state()[..., m]
+        b = np.moveaxis(o.state(), 1, 0)[..., m] if same_tree else None
+        out["parity"] = {"intervals": intervals, "same_tree": same_tree,
+                         "bit_exact": bool(same_tree and np.array_equal(a, b)),
+                         "max_abs_diff": float(np.max(np.abs(a - b))) if same_tree else None}
+        g.close()
+    return out
+
+
 # ------------------------------------------------------------ adjoint form
 ADJOINT = dict(n=16, halo=1, depth=8, base_level=5, max_level=7, rthr=0.01, cthr=0.002, rounds=3, steps=400,
                every=20, cfl=0.4, velocity=(1.0, 0.5), directions=64, eps=1e-4, pert=0.05, seed=7)
@@ -760,11 +887,18 @@ def gpu_arm(args, rank, world):
     bt = batched_arm(args, torch, A, dev, stream, flush, world)
     extras = {}
     if not args.no_extras:
-        extras["plain_fp64_config2"] = plain_config2(args, torch, A, dev, stream, flush, world)
-        extras["adjoint"] = adjoint_extra(torch, A, dev, stream, with_oracle=not args.no_cpu_baseline)
-        extras["config3_3d"] = config3_extra(torch, A, dev, stream, flush, max(1, args.steps))
-        extras["vtk_writer"] = vtk_extra(torch, A, dev, stream, with_cpu=not args.no_cpu_baseline)
-        extras["plain_fp64_config2_max_level7"] = depth7_extra(torch, A, dev, stream, flush, max(1, args.steps))
+        cpu = not args.no_cpu_baseline
+        table = {
+            "plain_fp64_config2": lambda: plain_config2(args, torch, A, dev, stream, flush, world),
+            "adjoint": lambda: adjoint_extra(torch, A, dev, stream, with_oracle=cpu),
+            "config3_3d": lambda: config3_extra(torch, A, dev, stream, flush, max(1, args.steps)),
+            "vtk_writer": lambda: vtk_extra(torch, A, dev, stream, with_cpu=cpu),
+            "plain_fp64_config2_max_level7": lambda: depth7_extra(torch, A, dev, stream, flush, max(1, args.steps)),
+            "euler_benchmark": lambda: euler_extra(torch, A, stream, with_cpu=cpu),
+        }
+        for name, fn in table.items():
+            if args.extra is None or name in args.extra:
+                extras[name] = fn()
         if args.uniform:
             lv = args.uniform_level
             extras[f"uniform_fp64_level{lv}"] = uniform_extra(A, torch, stream, A.F64, lv)
@@ -896,7 +1030,8 @@ def reference_arm(args, rank, world):
 def profile_case(name, steps):
     """One untimed run of a workload, for profilers: forest (the batched FP32
     forest, `steps` steps), adjoint (the adjoint mesh, FP64 forward and
-    backward over `steps` steps), config2 (one config-2 run)."""
+    backward over `steps` steps), config2 (one config-2 run), euler (the Euler
+    benchmark's first `steps` steps)."""
     import torch
 
     import amr_gb300 as A
@@ -923,6 +1058,9 @@ def profile_case(name, steps):
         lam, out = torch.ones_like(x), torch.empty_like(x)
         adj.backward(lam.data_ptr(), out.data_ptr())
         st = {"leaves": t.size, "steps": steps}
+    elif name == "euler":
+        t, _ = euler_tree(A, stream, capacity=4000)  # about 1.5 GB of state and primitives
+        st = euler_run(t, steps)
     else:
         W = WORKLOAD
         t = A.Tree(2, W["n"], W["halo"], W["depth"], capacity=4096, stream=stream.cuda_stream)
@@ -947,7 +1085,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--uniform", action="store_true", help="add the uniform kernel-level workloads")
     ap.add_argument("--uniform-level", type=int, default=9)
-    ap.add_argument("--case", choices=["forest", "adjoint", "config2"],
+    ap.add_argument("--extra", action="append", default=None,
+                    help="run only the named extra workloads after the headline (repeatable)")
+    ap.add_argument("--case", choices=["forest", "adjoint", "config2", "euler"],
                     help="run one workload once, untimed (for profilers), and exit")
     ap.add_argument("--case-steps", type=int, default=30)
     args = ap.parse_args()

@@ -42,7 +42,13 @@ class PatchGeometry(C.Structure):
 
 class TreeDesc(C.Structure):
     _fields_ = [("geom", PatchGeometry), ("capacity", C.c_size_t), ("dtype", C.c_int32), ("stream", C.c_void_p),
-                ("instances", C.c_int32)]
+                ("instances", C.c_int32), ("fields", C.c_int32)]
+
+
+class EulerParams(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("remesh_interval", C.c_uint64), ("gamma", C.c_double), ("cfl", C.c_double),
+                ("end_time", C.c_double), ("refine_threshold", C.c_double), ("coarsen_threshold", C.c_double),
+                ("min_level", C.c_int32), ("max_level", C.c_int32)]
 
 
 class CycleParams(C.Structure):
@@ -113,6 +119,8 @@ def lib():
         L.amr_selftest_wait_timeout.argtypes = [C.c_int32, C.POINTER(C.c_int32)]
         L.amr_tree_write_vtk.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.amr_tree_reserve.argtypes = [vp, sz]
+        L.amr_tree_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl]
+        L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
         L.amr_adjoint_destroy.argtypes = [vp]
@@ -160,13 +168,16 @@ def _vec3(v):
 
 
 class Tree:
-    """Device-resident ndtree + amr_solver state for one scalar field."""
+    """Device-resident ndtree + amr_solver state: one scalar field, or
+    `fields` fields (the Euler cell: rho, rho u_d, E)."""
 
     def __init__(self, rank, n, halo=1, depth=7, capacity=20000, dtype=F64, lengths=(1.0, 1.0, 1.0), stream=None,
-                 instances=1):
-        """instances > 1 makes a forest of independent trees (one root each)."""
+                 instances=1, fields=1):
+        """instances > 1 makes a forest of independent trees (one root each).
+        With fields > 1, host states are (fields, size, padded patch)."""
         self.rank, self.n, self.halo, self.depth = rank, n, halo, depth
         self.instances = int(instances)
+        self.fields = int(fields)
         self.dtype = dtype
         self.np_dtype = np.float64 if dtype == F64 else np.float32
         self.pad1 = n + 2 * halo
@@ -176,6 +187,7 @@ class Tree:
         d.dtype = dtype
         d.stream = stream
         d.instances = self.instances
+        d.fields = self.fields
         h = C.c_void_p()
         check(lib().amr_tree_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -211,12 +223,13 @@ class Tree:
 
     def upload_state(self, state):
         a = np.ascontiguousarray(state, self.np_dtype)
-        if a.size % self.flat:
+        if a.size % (self.flat * self.fields):
             raise AmrError(AMR_ERR_INVALID, "state is not a whole number of patches")
-        check(lib().amr_tree_upload_state(self._h, a.ctypes.data, a.size // self.flat))
+        check(lib().amr_tree_upload_state(self._h, a.ctypes.data, a.size // (self.flat * self.fields)))
 
     def download_state(self):
-        out = np.empty((self.size,) + (self.pad1,) * self.rank, self.np_dtype)
+        lead = (self.fields, self.size) if self.fields > 1 else (self.size,)
+        out = np.empty(lead + (self.pad1,) * self.rank, self.np_dtype)
         check(lib().amr_tree_download_state(self._h, out.ctypes.data, self.size))
         return out
 
@@ -338,8 +351,27 @@ class Tree:
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}
 
+    # -------------------------------------------------------------- Euler
+    def euler_advance(self, steps, gamma, cfl, remaining=1.7976931348623157e308):
+        """advance_batch_async with EulerPhysics: `steps` CFL steps (clamped
+        to `remaining`); finish_advance() gives (simulated time, steps)."""
+        check(lib().amr_tree_euler_advance(self._h, steps, gamma, cfl, remaining))
+
+    def euler_run(self, steps, interval, gamma, cfl, end_time, rthr, cthr, min_level, max_level) -> dict:
+        """The reference's Euler benchmark loop (advance `interval` steps with
+        the time left, max-Rho flags, re-mesh) until `steps` steps ran or the
+        simulated time reaches end_time; returns the run statistics."""
+        prm = EulerParams()
+        prm.steps, prm.remesh_interval, prm.gamma, prm.cfl, prm.end_time = steps, interval, gamma, cfl, end_time
+        prm.refine_threshold, prm.coarsen_threshold = rthr, cthr
+        prm.min_level, prm.max_level = min_level, max_level
+        st = CycleStats()
+        check(lib().amr_tree_euler_run(self._h, C.byref(prm), C.byref(st)))
+        return {f: getattr(st, f) for f, _ in CycleStats._fields_}
+
     def write_vtk(self, path, field="Scalar"):
-        """vtk_print::print of the current leaves and state (legacy binary VTK)."""
+        """vtk_print::print of the current leaves and state (legacy binary VTK);
+        with several fields, `field` names them separated by commas."""
         check(lib().amr_tree_write_vtk(self._h, str(path).encode(), field.encode()))
 
     def step_config(self):

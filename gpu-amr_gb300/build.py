@@ -35,8 +35,17 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+# Translation units whose arithmetic must match the reference's CPU code
+# operation for operation: no multiply-add contraction.
+NO_CONTRACTION = {"amr_euler.cu"}
+
+
 def sources():
     return sorted(CSRC.glob("*.cu"))
+
+
+def flags_for(src: Path):
+    return ["-fmad=false"] if src.name in NO_CONTRACTION else []
 
 
 def _stale(out: Path, deps) -> bool:
@@ -55,7 +64,7 @@ def build(verbose: bool = False, extra=None) -> Path:
     for src in sources():
         obj = BUILD / (src.stem + ".o")
         if _stale(obj, [src, *headers, Path(__file__)]):
-            jobs.append([nv, *ARCH, *NVFLAGS, *(extra or []), "-c", str(src), "-o", str(obj)])
+            jobs.append([nv, *ARCH, *NVFLAGS, *flags_for(src), *(extra or []), "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         if verbose:

@@ -183,10 +183,12 @@ __device__ inline void halo_cell(T* buf, const amr_halo_meta* meta, const Geo& g
     self[padded_index(g, G)] = static_cast<T>(ghost_value<T>(buf, g.flat, m, G, L, pos, g, self));
 }
 
+// blockIdx.y = field of a multi-field state (fields fstride elements apart).
 template <typename T>
 __global__ void __launch_bounds__(256) k_halo(T* __restrict__ buf, const amr_halo_meta* __restrict__ meta,
-                                              long long total, Geo g)
+                                              long long total, Geo g, size_t fstride = 0)
 {
+    buf += blockIdx.y * fstride;
     for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
          t += static_cast<long long>(gridDim.x) * blockDim.x)
         halo_cell<T>(buf, meta, g, t);
@@ -711,12 +713,15 @@ __device__ inline void remap_cell(const T* old_state, T* new_state, const Geo& g
 }
 
 // One block per new leaf; kept patches move whole (16-byte words, ghosts
-// included), new ones are built cell by cell.
+// included), new ones are built cell by cell.  blockIdx.y = field of a
+// multi-field state (fields fstride elements apart).
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_t* __restrict__ src,
-        const int8_t* __restrict__ skind, int P, Geo g)
+        const int8_t* __restrict__ skind, int P, Geo g, size_t fstride = 0)
 {
+    old_state += blockIdx.y * fstride;
+    new_state += blockIdx.y * fstride;
     const int j = blockIdx.x;
     if (j >= P) return;
     const int kind = skind[j];

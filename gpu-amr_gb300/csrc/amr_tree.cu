@@ -17,6 +17,7 @@
 
 #include "amr_gb300.h"
 #include "amr_cycle.cuh"
+#include "amr_euler.cuh"
 #include "amr_graph.cuh"
 #include "amr_vtk.cuh"
 
@@ -133,6 +134,7 @@ struct amr_tree {
     size_t       cap      = 0;
     int          dtype    = AMR_F64;
     size_t       esize    = 8;
+    int          nvar     = 1; // state fields; field f of a buffer starts at f * fstride() elements
     cudaStream_t stream   = nullptr;
     size_t       size     = 0;
     int          max_level_host = 0;
@@ -194,6 +196,17 @@ struct amr_tree {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
     std::vector<uint64_t>                         event_cells;
     size_t                                        events_used = 0;
+
+    // Euler solver scratch: per-step minima of dx / (|u| + a) as ordered
+    // bit patterns (two slots, alternating) and the step size in use
+    unsigned long long* euler_min = nullptr;
+    double*             euler_dt  = nullptr;
+    int32_t*            euler_ctl = nullptr;
+    double*             prim[2]{}; // primitive quantities beside sbuf[0] / sbuf[1]
+    size_t              prim_cap = 0;
+
+    size_t fstride() const { return cap * static_cast<size_t>(g.flat); }
+    size_t field_bytes(size_t patches) const { return patches * static_cast<size_t>(g.flat) * esize; }
 };
 
 namespace {
@@ -447,6 +460,11 @@ void free_tree(amr_tree* t)
     cudaFree(t->coef32);
     cudaFree(t->upcode);
     cudaFree(t->cstats);
+    cudaFree(t->euler_min);
+    cudaFree(t->euler_dt);
+    cudaFree(t->euler_ctl);
+    cudaFree(t->prim[0]);
+    cudaFree(t->prim[1]);
     if (t->pinned) cudaFreeHost(t->pinned);
     delete t;
 }
@@ -457,7 +475,8 @@ amr_status launch_halo(amr_tree* t)
     const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
     return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
-        k_halo<T><<<grid, 256, 0, t->stream>>>(static_cast<T*>(t->cur), t->meta[t->tb], total, t->g);
+        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(t->cur), t->meta[t->tb], total, t->g,
+                                                             t->fstride());
         AMR_LAUNCHED("k_halo");
         t->ghosts_valid = true;
         return AMR_OK;
@@ -485,7 +504,7 @@ amr_status init_root(amr_tree* t)
             m.padding[0] = m.padding[1] = m.padding[2] = 0;
         }
     }
-    const size_t state_bytes = t->cap * g.flat * t->esize;
+    const size_t state_bytes = t->nvar * t->field_bytes(t->cap);
     t->tb  = 0;
     t->cur = t->sbuf[0];
     t->nxt = t->sbuf[1];
@@ -1032,6 +1051,9 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
         if (g.inst_shift + bits > 64) return fail(AMR_ERR_INVALID, "too many instances for the tree depth");
     }
     if (static_cast<size_t>(K) > desc->capacity) return fail(AMR_ERR_INVALID, "capacity below the instance count");
+    if (desc->fields < 0 || desc->fields > 8) return fail(AMR_ERR_INVALID, "bad field count");
+    const int nvar = desc->fields > 1 ? desc->fields : 1;
+    if (nvar > 1 && K > 1) return fail(AMR_ERR_INVALID, "forests hold one field");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(AMR_ERR_NO_DEVICE, "no CUDA device");
     amr_tree* t = new amr_tree();
@@ -1041,8 +1063,9 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     t->cap    = desc->capacity;
     t->dtype  = desc->dtype;
     t->esize  = desc->dtype == AMR_F64 ? 8 : 4;
+    t->nvar   = nvar;
     t->stream = static_cast<cudaStream_t>(desc->stream);
-    const size_t cap = t->cap, state_bytes = cap * g.flat * t->esize;
+    const size_t cap = t->cap, state_bytes = nvar * t->field_bytes(cap);
     cudaError_t  e   = cudaSuccess;
     auto         al  = [&](void** p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, bytes);
@@ -1085,6 +1108,9 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->coef32), coef_steps * K * nl * sizeof(float2));
     al(reinterpret_cast<void**>(&t->upcode), K * sizeof(int32_t));
     al(reinterpret_cast<void**>(&t->cstats), sizeof(CycleStats));
+    al(reinterpret_cast<void**>(&t->euler_min), 2 * sizeof(unsigned long long));
+    al(reinterpret_cast<void**>(&t->euler_dt), sizeof(double));
+    al(reinterpret_cast<void**>(&t->euler_ctl), 2 * sizeof(int32_t));
     t->pinned_bytes = std::max<size_t>(1024, 64 + (K + 1) * 32 + sizeof(RunCtl));
     if (e == cudaSuccess) e = cudaMallocHost(&t->pinned, t->pinned_bytes);
     if (e != cudaSuccess) {
@@ -1141,8 +1167,8 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
         return q;
     };
     const size_t flat_b = static_cast<size_t>(g.flat) * t->esize;
-    void*        sb0    = al(cap * flat_b);
-    void*        sb1    = al(cap * flat_b);
+    void*        sb0    = al(t->nvar * cap * flat_b);
+    void*        sb1    = al(t->nvar * cap * flat_b);
     void*        k0     = al(cap * sizeof(uint64_t));
     void*        k1     = al(cap * sizeof(uint64_t));
     void*        l0     = al(cap * sizeof(int32_t));
@@ -1165,8 +1191,13 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     // scratch the caller reads through amr_tree_device_state)
     const int cs = t->cur == t->sbuf[0] ? 0 : 1;
     void*     nsb[2] = { sb0, sb1 };
-    AMR_CUDA(cudaMemcpyAsync(nsb[cs], t->cur, P * flat_b, cudaMemcpyDeviceToDevice, t->stream));
-    AMR_CUDA(cudaMemcpyAsync(nsb[cs ^ 1], t->nxt, P * flat_b, cudaMemcpyDeviceToDevice, t->stream));
+    for (int f = 0; f < t->nvar; ++f) {
+        const size_t so = f * t->cap * flat_b, dn = f * cap * flat_b;
+        AMR_CUDA(cudaMemcpyAsync(static_cast<char*>(nsb[cs]) + dn, static_cast<const char*>(t->cur) + so, P * flat_b,
+                                 cudaMemcpyDeviceToDevice, t->stream));
+        AMR_CUDA(cudaMemcpyAsync(static_cast<char*>(nsb[cs ^ 1]) + dn, static_cast<const char*>(t->nxt) + so,
+                                 P * flat_b, cudaMemcpyDeviceToDevice, t->stream));
+    }
     void* nk[2] = { k0, k1 };
     void* nlv[2] = { l0, l1 };
     void* nm[2] = { m0, m1 };
@@ -1191,6 +1222,10 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     cudaFree(t->src);
     cudaFree(t->skind);
     cudaFree(t->tile_sums);
+    cudaFree(t->prim[0]); // rebuilt by the next Euler advance
+    cudaFree(t->prim[1]);
+    t->prim[0] = t->prim[1] = nullptr;
+    t->prim_cap = 0;
     t->sbuf[0] = sb0;
     t->sbuf[1] = sb1;
     t->cur     = nsb[cs];
@@ -1224,11 +1259,25 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out)
     return AMR_OK;
 }
 
+// Copies `num` patches of every field between the tree's state (field f at f
+// * fstride) and a buffer holding the fields one after another (field f at f *
+// num patches).
+static amr_status copy_fields(amr_tree* t, void* dst, const void* src, size_t num, cudaMemcpyKind kind, bool to_tree)
+{
+    const size_t fb = t->field_bytes(num), tstride = t->field_bytes(t->cap);
+    for (int f = 0; f < t->nvar; ++f) {
+        char*       d = static_cast<char*>(dst) + f * (to_tree ? tstride : fb);
+        const char* s = static_cast<const char*>(src) + f * (to_tree ? fb : tstride);
+        AMR_CUDA(cudaMemcpyAsync(d, s, fb, kind, t->stream));
+    }
+    return AMR_OK;
+}
+
 amr_status amr_tree_upload_state(amr_tree* t, const void* host, size_t num)
 {
     if (!t || !host) return fail(AMR_ERR_INVALID, "null argument");
     if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
-    AMR_CUDA(cudaMemcpyAsync(t->cur, host, num * t->g.flat * t->esize, cudaMemcpyHostToDevice, t->stream));
+    if (amr_status s = copy_fields(t, t->cur, host, num, cudaMemcpyHostToDevice, true); s != AMR_OK) return s;
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     t->ghosts_valid = true; // caller's ghosts, as in sync_current_to_device
     return AMR_OK;
@@ -1238,7 +1287,7 @@ amr_status amr_tree_download_state(amr_tree* t, void* host, size_t num)
 {
     if (!t || !host) return fail(AMR_ERR_INVALID, "null argument");
     if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
-    AMR_CUDA(cudaMemcpyAsync(host, t->cur, num * t->g.flat * t->esize, cudaMemcpyDeviceToHost, t->stream));
+    if (amr_status s = copy_fields(t, host, t->cur, num, cudaMemcpyDeviceToHost, false); s != AMR_OK) return s;
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     return AMR_OK;
 }
@@ -1247,7 +1296,8 @@ amr_status amr_tree_load_state_device(amr_tree* t, const void* device_state, siz
 {
     if (!t || !device_state) return fail(AMR_ERR_INVALID, "null argument");
     if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
-    AMR_CUDA(cudaMemcpyAsync(t->cur, device_state, num * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
+    if (amr_status s = copy_fields(t, t->cur, device_state, num, cudaMemcpyDeviceToDevice, true); s != AMR_OK)
+        return s;
     t->ghosts_valid = true;
     return AMR_OK;
 }
@@ -1256,7 +1306,8 @@ amr_status amr_tree_download_state_device(amr_tree* t, void* device_dst, size_t 
 {
     if (!t || !device_dst) return fail(AMR_ERR_INVALID, "null argument");
     if (num != t->size) return fail(AMR_ERR_INVALID, "patch count does not match tree size");
-    AMR_CUDA(cudaMemcpyAsync(device_dst, t->cur, num * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
+    if (amr_status s = copy_fields(t, device_dst, t->cur, num, cudaMemcpyDeviceToDevice, false); s != AMR_OK)
+        return s;
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     return AMR_OK;
 }
@@ -1418,7 +1469,8 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     AMR_LAUNCHED("k_emit");
     amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
-        k_remap<T><<<NP, 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->src, t->skind, NP, g);
+        k_remap<T><<<dim3(NP, t->nvar), 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->src,
+                                                     t->skind, NP, g, t->fstride());
         AMR_LAUNCHED("k_remap");
         return AMR_OK;
     });
@@ -1464,6 +1516,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                         int first_mode)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the advection update takes a one-field tree");
     if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
     cudaStream_t s = t->stream;
     const int    K = t->ninst;
@@ -1585,6 +1638,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
 {
     if (!t || !p) return fail(AMR_ERR_INVALID, "null argument");
     if (p->criterion < 0 || p->criterion > 2) return fail(AMR_ERR_INVALID, "unknown criterion");
+    if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the advection run takes a one-field tree");
     const bool inst_params = (p->options & AMR_RUN_INSTANCE_PARAMS) != 0;
     if (inst_params && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no per-instance velocities set");
     if (p->criterion != 0) ++t->topo;
@@ -1874,6 +1928,7 @@ amr_status amr_adjoint_create(amr_tree* t, size_t steps, const double* velocity3
 {
     if (!t || !out) return fail(AMR_ERR_INVALID, "null argument");
     *out = nullptr;
+    if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the adjoint takes a one-field tree");
     if (every < 1 || every > t->coef_steps) return fail(AMR_ERR_INVALID, "checkpoint interval out of range");
     if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
     amr_adjoint* a = new amr_adjoint();
@@ -2080,6 +2135,124 @@ amr_status amr_selftest_wait_timeout(int32_t polls, amr_status* observed)
     return AMR_OK;
 }
 
+// ------------------------------------------------------------------ Euler
+static amr_status euler_check(amr_tree* t)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (t->nvar != t->g.rank + 2) return fail(AMR_ERR_INVALID, "the Euler solver takes a tree of rank + 2 fields");
+    if (t->dtype != AMR_F64) return fail(AMR_ERR_INVALID, "the Euler solver is FP64");
+    if (!euler_supported(t->g)) return fail(AMR_ERR_INVALID, "patch too large for the Euler update");
+    return AMR_OK;
+}
+
+static amr_status euler_advance_impl(amr_tree* t, size_t steps, double gamma, double cfl, double remaining)
+{
+    const size_t prim_elems = static_cast<size_t>(2 * t->g.rank + 1) * t->fstride();
+    if (t->prim_cap != t->cap) {
+        cudaFree(t->prim[0]);
+        cudaFree(t->prim[1]);
+        t->prim[0] = t->prim[1] = nullptr;
+        t->prim_cap = 0;
+        AMR_CUDA(cudaMalloc(&t->prim[0], prim_elems * sizeof(double)));
+        AMR_CUDA(cudaMalloc(&t->prim[1], prim_elems * sizeof(double)));
+        t->prim_cap = t->cap;
+    }
+    if (!t->ghosts_valid) {
+        amr_status s = launch_halo(t);
+        if (s != AMR_OK) return s;
+    }
+    EulerBufs b{};
+    b.g        = t->g;
+    b.P        = static_cast<int>(t->size);
+    b.fstride  = t->fstride();
+    b.levels   = t->levels[t->tb];
+    b.meta     = t->meta[t->tb];
+    b.state[0] = static_cast<double*>(t->sbuf[0]);
+    b.state[1] = static_cast<double*>(t->sbuf[1]);
+    b.prim[0]  = t->prim[0];
+    b.prim[1]  = t->prim[1];
+    b.min_slot = t->euler_min;
+    b.step_dt  = t->euler_dt;
+    b.ctl      = t->euler_ctl;
+    b.acc      = t->dt_acc;
+    b.rem      = t->dt_rem;
+    b.cnt      = t->dt_cnt;
+    b.stream   = t->stream;
+    int      cur      = t->cur == t->sbuf[0] ? 0 : 1;
+    uint64_t launches = 0;
+    cudaError_t e = euler_begin(b, cur, gamma, remaining, &launches);
+    for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
+        e = euler_step(b, cur, static_cast<int>(k & 1), gamma, cfl, &launches);
+        cur ^= 1;
+    }
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
+    if (e != cudaSuccess) return cuda_fail(e, "Euler step");
+    t->cur          = t->sbuf[cur];
+    t->nxt          = t->sbuf[cur ^ 1];
+    t->ghosts_valid = true; // the last step's halo filled every field
+    t->batch_open   = true;
+    return AMR_OK;
+}
+
+amr_status amr_tree_euler_advance(amr_tree* t, size_t steps, double gamma, double cfl, double remaining)
+{
+    if (amr_status s = euler_check(t); s != AMR_OK) return s;
+    return euler_advance_impl(t, steps, gamma, cfl, remaining);
+}
+
+amr_status amr_tree_euler_run(amr_tree* t, const amr_euler_params* p, amr_cycle_stats* out)
+{
+    if (amr_status s = euler_check(t); s != AMR_OK) return s;
+    if (!p) return fail(AMR_ERR_INVALID, "null argument");
+    if (p->remesh_interval < 1) return fail(AMR_ERR_INVALID, "re-mesh interval must be positive");
+    RunTotals tot;
+    double    time = 0.0;
+    while (tot.done < static_cast<long long>(p->steps) && time < p->end_time) {
+        const size_t k = static_cast<size_t>(
+            std::min<long long>(static_cast<long long>(p->remesh_interval), static_cast<long long>(p->steps) - tot.done));
+        const size_t leaves = t->size;
+        amr_status   st     = euler_advance_impl(t, k, p->gamma, p->cfl, p->end_time - time);
+        if (st != AMR_OK) return st;
+        // the benchmark's criterion: max Rho over the patch, then re-mesh
+        st = amr_tree_flags_max(t, p->refine_threshold, p->coarsen_threshold, p->min_level, p->max_level);
+        if (st != AMR_OK) return st;
+        int changed = 0;
+        st          = amr_tree_remesh(t, &changed);
+        if (st != AMR_OK) return st;
+        ++tot.remeshes;
+        double acc = 0.0;
+        size_t ex  = 0;
+        st         = amr_tree_finish_advance(t, &acc, &ex);
+        if (st != AMR_OK) return st;
+        time += acc;
+        tot.done += static_cast<long long>(ex);
+        tot.executed += ex;
+        tot.cells += static_cast<uint64_t>(ex) * leaves * t->g.cells;
+        ++tot.intervals;
+        tot.leaves_sum += leaves;
+        tot.lmin = std::min<uint64_t>(tot.lmin, leaves);
+        tot.lmax = std::max<uint64_t>(tot.lmax, leaves);
+        if (ex == 0) break;
+    }
+    if (!t->ghosts_valid) {
+        amr_status s = launch_halo(t);
+        if (s != AMR_OK) return s;
+    }
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        out->executed_steps = tot.executed;
+        out->sum_dt         = time;
+        out->cell_updates   = tot.cells;
+        out->remeshes       = tot.remeshes;
+        out->intervals      = tot.intervals;
+        out->leaves_min     = tot.intervals ? tot.lmin : t->size;
+        out->leaves_max     = tot.intervals ? tot.lmax : t->size;
+        out->leaves_mean    = tot.intervals ? static_cast<double>(tot.leaves_sum) / tot.intervals : 0.0;
+    }
+    return AMR_OK;
+}
+
 amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_name)
 {
     if (!t || !path) return fail(AMR_ERR_INVALID, "null argument");
@@ -2090,12 +2263,14 @@ amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_n
     v.state  = t->cur;
     v.size   = t->size;
     v.esize  = t->esize;
+    v.nvar   = t->nvar;
+    v.fstride = t->fstride();
     v.stream = t->stream;
     AMR_CUDA(cudaStreamSynchronize(t->stream));
     std::string      err;
     const amr_status st = vtk_write(v, path, field_name ? field_name : "Scalar", err);
-    // six section kernels per chunk of 2^22 cells
-    g_launches.fetch_add(6 * std::max<uint64_t>(1, (t->size * t->g.cells + (1ull << 22) - 1) >> 22));
+    // five section kernels, and one per field, per chunk of 2^22 cells
+    g_launches.fetch_add((5 + t->nvar) * std::max<uint64_t>(1, (t->size * t->g.cells + (1ull << 22) - 1) >> 22));
     if (st != AMR_OK) return fail(st, err);
     return AMR_OK;
 }

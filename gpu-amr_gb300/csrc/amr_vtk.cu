@@ -138,7 +138,7 @@ __global__ void k_vtk_values(const T* __restrict__ state, Geo g, long long first
 
 } // namespace
 
-amr_status vtk_write(const VtkTree& v, const char* path, const char* field, std::string& err)
+amr_status vtk_write(const VtkTree& v, const char* path, const char* fields, std::string& err)
 {
     const Geo&      g     = v.g;
     const long long cells = static_cast<long long>(v.size) * g.cells;
@@ -202,13 +202,23 @@ amr_status vtk_write(const VtkTree& v, const char* path, const char* field, std:
             k_vtk_ints<<<grid, 256, 0, v.stream>>>(g, 2, 0, first, n, dbuf);
         });
     }
-    if (ok) {
-        std::fprintf(f, "SCALARS %s %s 1\nLOOKUP_TABLE default\n", field, v.esize == 8 ? "double" : "float");
+    // one SCALARS block per field, in field order (vtk_print.hpp writes the
+    // cell type's fields in tuple order)
+    const char* name = fields;
+    for (int fi = 0; ok && fi < v.nvar; ++fi) {
+        size_t len = 0;
+        while (name[len] && name[len] != ',') ++len;
+        std::fprintf(f, "SCALARS %.*s %s 1\nLOOKUP_TABLE default\n", static_cast<int>(len), name,
+                     v.esize == 8 ? "double" : "float");
+        name += len + (name[len] == ',' ? 1 : 0);
+        const size_t off = fi * v.fstride;
         ok = section(v.esize, [&](long long first, long long n, unsigned grid) {
             if (v.esize == 8)
-                k_vtk_values<double><<<grid, 256, 0, v.stream>>>(static_cast<const double*>(v.state), g, first, n, dbuf);
+                k_vtk_values<double><<<grid, 256, 0, v.stream>>>(static_cast<const double*>(v.state) + off, g, first,
+                                                                 n, dbuf);
             else
-                k_vtk_values<float><<<grid, 256, 0, v.stream>>>(static_cast<const float*>(v.state), g, first, n, dbuf);
+                k_vtk_values<float><<<grid, 256, 0, v.stream>>>(static_cast<const float*>(v.state) + off, g, first, n,
+                                                                dbuf);
         });
     }
     if (dbuf) cudaFree(dbuf);

@@ -18,9 +18,12 @@ struct VtkTree {
     const void*     state; // device, padded patches
     size_t          size;  // leaves
     size_t          esize; // bytes per state value
+    int             nvar;    // fields, one SCALARS block each
+    size_t          fstride; // elements between fields
     cudaStream_t    stream;
 };
 
-amr_status vtk_write(const VtkTree& v, const char* path, const char* field, std::string& err);
+// `fields`: the field names, separated by commas, one per field.
+amr_status vtk_write(const VtkTree& v, const char* path, const char* fields, std::string& err);
 
 } // namespace amr_gb300

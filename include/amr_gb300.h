@@ -143,6 +143,8 @@ typedef struct amr_tree_desc {
     void*              stream;    /* cudaStream_t for every call on this tree */
     int32_t            instances; /* independent trees held together (a forest);
                                      0 or 1 = one tree */
+    int32_t            fields;    /* state fields per cell (the cell type's SoA
+                                     tuple; Euler: rank + 2); 0 or 1 = one */
 } amr_tree_desc;
 
 /* ndtree(capacity) (include/ndtree/ndtree.hpp:320-425): one root leaf with
@@ -168,7 +170,8 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out);
 
 /* State transfer, the reference's sync_current_{to,from}_device
  * (ndtree.hpp:583-613); host layout = size() padded patches in Morton order,
- * elements of the tree's dtype. */
+ * elements of the tree's dtype; with several fields, field by field (the
+ * reference's SoA buffers: fields x size() x padded patch). */
 amr_status amr_tree_upload_state(amr_tree* t, const void* host_state, size_t num_patches);
 amr_status amr_tree_download_state(amr_tree* t, void* host_state, size_t num_patches);
 /* Device-to-device state load and copy-out (same layout as upload_state). */
@@ -267,6 +270,37 @@ typedef struct amr_cycle_stats {
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_stats* stats);
 
+/* ------------------------------------------------------------- Euler
+ * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through
+ * amr_solver (amr_solver.hpp:155-413) on a tree created with fields =
+ * rank + 2 (rho, rho u_d, E; FP64): each step takes the CFL step from the
+ * current state (min over cells and axes of dx / (|u_d| + a), times cfl,
+ * clamped to the remaining time) and applies the Rusanov update with face
+ * ghosts from the neighbours by the halo rules, every field.  The arithmetic
+ * is the reference's, operation for operation (no contraction), so states
+ * are bit-identical to its CPU path.  Use amr_tree_finish_advance for the
+ * simulated time and executed steps. */
+amr_status amr_tree_euler_advance(amr_tree* t, size_t steps, double gamma, double cfl, double remaining_time);
+
+/* The reference's Euler benchmark loop (benchmark/bench_fvm_solver_
+ * integration.b.cpp:208-250): repeat { advance min(remesh_interval, steps
+ * left) steps with the remaining time end_time - t; flags from the maximum
+ * of rho over interior and face-ghost cells (Refine above refine_threshold
+ * below max_level, Coarsen under coarsen_threshold above min_level);
+ * re-mesh } until `steps` steps ran or t reaches end_time. */
+typedef struct amr_euler_params {
+    uint64_t steps;
+    uint64_t remesh_interval;
+    double   gamma;
+    double   cfl;
+    double   end_time;
+    double   refine_threshold;
+    double   coarsen_threshold;
+    int32_t  min_level;
+    int32_t  max_level;
+} amr_euler_params;
+amr_status amr_tree_euler_run(amr_tree* t, const amr_euler_params* params, amr_cycle_stats* stats);
+
 /* ----------------------------------------------------------- forests
  * Per-instance parameters (instances > 1): velocity (3 per instance, Morton
  * axis order x, y, z) and level bounds (min_level, max_level per instance).
@@ -337,9 +371,10 @@ amr_status amr_tree_get_timing(amr_tree* t, double* step_kernel_ms, uint64_t* st
 /* vtk_print::print (include/ndtree/vtk_print.hpp:53-257) of the current
  * leaves and state: legacy binary VTK (big-endian), one quad (2D) or voxel
  * (3D) per interior cell, CELL_DATA cell_index, is_halo and the field named
- * field_name (an FP32 tree writes its values as "float").  Every section is
- * built on the device; byte-identical to the reference writer for FP64
- * trees. */
+ * field_name (an FP32 tree writes its values as "float"; with several fields,
+ * field_name lists their names separated by commas and each gets its own
+ * SCALARS block).  Every section is built on the device; byte-identical to
+ * the reference writer for FP64 trees. */
 amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_name);
 
 /* Launch shape of the 2D update kernel used by the tree's last advance or

@@ -1064,8 +1064,9 @@ int oracle_write_vtk(const oracle_tree* t, const char* path, const char* fields)
         oracle_decode(rank, t->ids[p], c, &level);
         double origin[3], cs[3];
         for (int k = 0; k < rank; ++k) {
-            origin[k]         = 1.0 * (double)c[k] / maxc;
-            const double size = 1.0 * (double)(1u << (t->depth - level)) / maxc;
+            /* physics_system::patch_coord / patch_sizes (physics_system.hpp:58-97) */
+            origin[k]         = t->lengths[k] * (double)c[k] / maxc;
+            const double size = t->lengths[k] * (double)(1u << (t->depth - level)) / maxc;
             cs[k]             = size / (double)n;
         }
         int idx[3];
@@ -1367,9 +1368,14 @@ double oracle_euler_dt(const oracle_tree* t, double gamma, double cfl)
 {
     const int    rank = t->rank, n = t->n, h = t->h;
     const size_t P1 = t->pad1;
+    const long   np = (long)t->size;
     double       dt = 1.7976931348623157e308;
-    for (size_t p = 0; p < t->size; ++p) {
-        double cs[3];
+    /* a minimum: the same value in any order (EXECUTION=PAR reduces in
+     * parallel as well) */
+#pragma omp parallel for schedule(static) reduction(min : dt) if (np > 16) num_threads(g_threads > 0 ? g_threads : 1)
+    for (long pi = 0; pi < np; ++pi) {
+        const size_t p = (size_t)pi;
+        double       cs[3];
         cell_sizes(t, t->ids[p], cs);
         const double* u = t->cur + p * t->pstride;
         int           idx[3];

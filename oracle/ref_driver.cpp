@@ -698,8 +698,15 @@ int dispatch(params const& p)
     const auto mode = p.str("mode", "run");
     if (mode == "euler")
     {
-        auto e = std::make_unique<euler_harness<DIM, N, H, Depth>>(p, w);
-        return e->run();
+        auto      e  = std::make_unique<euler_harness<DIM, N, H, Depth>>(p, w);
+        const int rc = e->run();
+        if (rc == 0 && p.has("vtk"))
+        {
+            using geometry_t = typename euler_harness<DIM, N, H, Depth>::geometry_t;
+            amr::ndt::print::vtk_print<geometry_t> printer(p.str("vtk", "tree"));
+            printer.print(e->tree(), ".vtk");
+        }
+        return rc;
     }
     auto h = std::make_unique<harness<DIM, N, H, Depth>>(p, w);
     const int  rc   = mode == "tree" ? h->tree_mode() : h->run();

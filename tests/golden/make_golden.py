@@ -207,6 +207,15 @@ def vtk_golden():
             subprocess.run(cmd, check=True, capture_output=True, text=True, cwd=d)
             data = (Path(d) / "vtk_output" / f"{name}.vtk").read_bytes()
         out[name] = {"sha256": hashlib.sha256(data).hexdigest(), "bytes": len(data), "field": "Scalar"}
+    # the Euler pulse fixtures: every field, domain lengths 1000
+    for name, cfg, rank, _, _, params in EULER_SCENARIOS:
+        with tempfile.TemporaryDirectory() as d:
+            cmd = ([str(DRIVER), f"cfg={cfg}", "mode=euler"] + [f"{k}={v}" for k, v in params.items()]
+                   + [f"out={d}/dump.bin", f"vtk={name}"])
+            subprocess.run(cmd, check=True, capture_output=True, text=True, cwd=d)
+            data = (Path(d) / "vtk_output" / f"{name}.vtk").read_bytes()
+        names = ["Rho", "Rhou", "Rhov"] + (["Rhow"] if rank == 3 else []) + [f"E{rank}D"]
+        out[name] = {"sha256": hashlib.sha256(data).hexdigest(), "bytes": len(data), "field": ",".join(names)}
     (HERE / "vtk.json").write_text(json.dumps(out, indent=1) + "\n")
     return out
 

@@ -1,13 +1,13 @@
 """The device-resident VTK writer (amr_tree_write_vtk) against the reference
 writer's files (SHA-256 and length from the reference build,
-tests/golden/vtk.json) on the final tree and state of four fixtures (2D,
-3D, halo 2): byte-identical."""
+tests/golden/vtk.json) on the final tree and state of six fixtures (2D,
+3D, halo 2, the Euler fields on a 1000-long domain): byte-identical."""
 import hashlib
 
 import numpy as np
 import pytest
 
-from vtk_cases import cases, rebuild
+from vtk_cases import cases, fields, lengths, rebuild
 
 pytestmark = pytest.mark.gpu
 
@@ -18,13 +18,15 @@ def test_gpu_vtk_matches_reference(tmp_path, name):
 
     want = cases()[name]
     meta, flags, state, ids, init = rebuild(name)
-    t = A.Tree(meta["rank"], meta["n"], meta["halo"], meta["depth"], capacity=20000)
+    nvar = fields(meta)
+    t = A.Tree(meta["rank"], meta["n"], meta["halo"], meta["depth"], capacity=20000, fields=nvar,
+               lengths=lengths(meta, meta["rank"]))
     t.refine_uniform(init)
     for f in flags:
         t.set_flags(f)
         t.remesh()
     np.testing.assert_array_equal(t.ids(), ids)
-    t.upload_state(state)
+    t.upload_state(np.moveaxis(state, 1, 0) if nvar > 1 else state)
     path = tmp_path / f"{name}.vtk"
     t.write_vtk(path, want["field"])
     data = path.read_bytes()

@@ -1,5 +1,6 @@
 """Trees and states of the VTK writer fixtures (tests/golden/vtk.json): the
-final tree and state of four reference fixtures, rebuilt from their flags."""
+final tree and state of six reference fixtures (four scalar, two Euler),
+rebuilt from their flags."""
 import json
 
 import numpy as np
@@ -18,7 +19,12 @@ def rebuild(name):
     P1 = n + 2 * h
     p = meta["params"]
     init = int(p["init_levels"])
-    if "passes" in z.files:
+    if "remeshes" in z.files:  # Euler fixtures: (size, nvar, ...) states
+        k = int(z["remeshes"])
+        flags = [z[f"flags_{i}"] for i in range(k)]
+        state = z["state_final"]
+        ids = z[f"ids_{k - 1}"]
+    elif "passes" in z.files:
         passes = int(z["passes"])
         flags = [z[f"flags_{k}"] for k in range(passes)]
         state = z[f"state_{passes - 1}"]
@@ -30,3 +36,11 @@ def rebuild(name):
         state[(slice(None),) + (slice(h, n + h),) * rank] = inner
         ids = z["final_ids"]
     return meta, flags, state, ids, init
+
+
+def fields(meta):
+    return int(meta.get("nvar", 1))
+
+
+def lengths(meta, rank):
+    return tuple(meta.get("lengths", [1.0] * rank))
