@@ -628,7 +628,8 @@ def euler_extra(torch, A, stream, with_cpu=True):
                 "sim_time": st["sum_dt"], "steps": int(st["executed_steps"]), "remeshes": int(st["remeshes"]),
                 "leaves_min": int(st["leaves_min"]), "leaves_max": int(st["leaves_max"]),
                 "leaves_final": t.size, "gpu_launches": int(A.launch_count() - l0)})
-    # step kernels on the final mesh: finalize + update + halo per step
+    # on the final mesh: whole steps (finalize + update + halo) and the
+    # update kernel alone (CUDA events on the tree's stream)
     k = 50
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
@@ -638,10 +639,23 @@ def euler_extra(torch, A, stream, with_cpu=True):
         ev1.record(stream)
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1) / k
+    t.set_timing(True)
+    t.euler_advance(k, E["gamma"], E["cfl"])
+    kms, kl, kcells = t.get_timing()
+    t.set_timing(False)
     step_cells = t.size * E["n"] ** 2
     out["final_mesh_step"] = {"ms": ms, "cells": step_cells, "cell_updates_per_s": step_cells / (ms * 1e-3),
-                              "bytes_per_cell": 2 * (4 + 5) * 8,
-                              "note": "state (4 fields) and primitives (u, v, p, |u|+a, |v|+a) read and written"}
+                              "update_kernel_ms": kms / kl, "update_kernel_share": (kms / kl) / ms}
+    prof = json.loads((REPO / "profiles" / "k_euler_step_fp64_benchmark.json").read_text())
+    per_cell = prof["fp64_add_mul_fma_per_cell"]
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = prof["fp64_peak_thread_inst_per_cycle_per_sm"] * sms * measured_peaks().get("sm_max_mhz", 2070.0) * 1e6
+    achieved = per_cell * kcells / (kms * 1e-3)
+    out["roofline"] = {"bound": "fp64", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G FP64 inst/s",
+                       "frac": achieved / peak, "traffic": prof["dram_bytes_per_cell"] * step_cells,
+                       "note": f"{per_cell:.0f} FP64 add/mul/fma per cell update (ncu, committed profile) x cells / "
+                               f"CUDA-event time of k_euler_step; peak = 2 per cycle per SM x SMs x max SM clock; "
+                               f"traffic = DRAM bytes per cell (ncu) x cells of one launch"}
     t.close()
     if with_cpu:
         from oracle import oracle as O

@@ -7,19 +7,23 @@
 // the correctly rounded IEEE operations, so each cell's result equals the
 // reference CPU path's bit for bit.  What changes is how much is computed,
 // never how: a face flux depends only on its two cells, so it is evaluated
-// once per face (the reference evaluates it from both sides); a cell's
-// primitive quantities (u_d, p, |u_d| + a) depend only on the cell, so they
-// are formed once, when the cell's value is written, and kept beside the
-// state; and because correctly rounded division is monotonic, the minimum of
-// dx_d / s over a patch's cells is dx_d / (maximum s), one division per patch
-// and axis instead of one per cell.
+// once per face (the reference evaluates it from both sides); the terms of a
+// face flux that depend on one side only (the wave speed s_d = |u_d| + a and
+// the physical flux m_k u_d + [k = d] p, u_d (E + p) of each direction d)
+// depend only on the cell, so they are formed once, when the cell's value is
+// written, and kept beside the state; and because correctly rounded
+// division is monotonic, the minimum of dx_d / s over a patch's cells is
+// dx_d / (maximum s), one division per patch and axis instead of one per
+// cell.  Speeds are non-negative or NaN, so their comparisons and maxima
+// are integer operations on the bit patterns (with the reference's NaN
+// outcomes), which keeps them off the FP64 pipe, the bound of this kernel.
 //
 // One step is three launches: k_euler_finalize (step size from the previous
 // minimum, clamped to the remaining time), k_euler_step (one block per tile
 // of a patch: stage the tile and its face neighbours in shared memory, face
-// fluxes, cell updates, primitives and the patch maximum of the new state),
-// k_euler_halo (face ghosts of every field by the halo rules, and their
-// primitives).
+// fluxes, cell updates, side terms and the patch maximum of the new state),
+// k_euler_halo (face ghosts of every field by the halo rules, and their side
+// terms).
 #include <algorithm>
 #include <atomic>
 #include <cfloat>
@@ -44,7 +48,9 @@ struct ETile {
 template <int R>
 constexpr int kNV = R + 2; // conservative fields
 template <int R>
-constexpr int kNQ = kNV<R> + 2 * R + 1; // staged quantities: U, u_d, p, s_d
+constexpr int kNP = R * (R + 2); // per direction d: s_d, m_k u_d + [k = d] p (k < R), u_d (E + p)
+template <int R>
+constexpr int kNQ = kNV<R> + kNP<R>; // staged quantities per cell
 
 int largest_divisor_le(int n, int cap)
 {
@@ -89,79 +95,98 @@ bool pick_tile(const Geo& g, ETile<R>& t)
     return false;
 }
 
-// The per-side prologue of rusanovFlux / getMaxSpeed (EulerPhysics.hpp:
-// 83-90, 137-160): u_d = m_d / rho, p, and s_d = |u_d| + a.
+// The one-side terms of rusanovFlux (EulerPhysics.hpp:83-90, 113-127) and
+// getMaxSpeed for every direction d, in the reference's operation order:
+// q[d*(R+2)] = |u_d| + a, q[d*(R+2) + 1 + k] = m_k u_d (+ p when k = d),
+// q[d*(R+2) + R + 1] = u_d (E + p).
 template <int R>
-__device__ __forceinline__ void primitives(const double* U, double gamma, double* u, double& p, double* s)
+__device__ __forceinline__ void side_terms(const double* U, double gamma, double* q)
 {
     const double inv_rho = 1.0 / U[0];
     double       K       = 0.0;
 #pragma unroll
     for (int d = 0; d < R; ++d) K += U[1 + d] * U[1 + d];
     K *= 0.5 * inv_rho;
-    p              = (gamma - 1.0) * (U[R + 1] - K);
-    const double a = sqrt(gamma * p * inv_rho);
+    const double p  = (gamma - 1.0) * (U[R + 1] - K);
+    const double a  = sqrt(gamma * p * inv_rho);
+    const double Ep = U[R + 1] + p;
 #pragma unroll
     for (int d = 0; d < R; ++d) {
-        u[d] = U[1 + d] * inv_rho;
-        s[d] = fabs(u[d]) + a;
+        const double u = U[1 + d] * inv_rho;
+        double*      o = q + d * (R + 2);
+        o[0]           = fabs(u) + a;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            double f = U[1 + k] * u;
+            if (k == d) f += p;
+            o[1 + k] = f;
+        }
+        o[R + 1] = u * Ep;
     }
 }
 
-// Writes the primitive quantities of one cell (padded index li of patch
-// base pb) to the primitive buffer.
 template <int R>
-__device__ __forceinline__ void store_prims(double* prim, size_t fs, size_t at, const double* u, double p,
-                                            const double* s)
+__device__ __forceinline__ void store_terms(double* prim, size_t fs, size_t at, const double* q)
 {
 #pragma unroll
-    for (int d = 0; d < R; ++d) prim[d * fs + at] = u[d];
-    prim[R * fs + at] = p;
-#pragma unroll
-    for (int d = 0; d < R; ++d) prim[(R + 1 + d) * fs + at] = s[d];
+    for (int j = 0; j < kNP<R>; ++j) prim[j * fs + at] = q[j];
+}
+
+// Wave speeds are |u| + a: +0 or positive, or NaN.  For such values the
+// order of the bit patterns is the numeric order, so std::max(left, right)
+// = (left < right) ? right : left is decided on the integers, NaN included
+// (any comparison with NaN is false: the left value is kept).
+__device__ __forceinline__ bool is_nan_bits(unsigned long long b) { return (b << 1) > (0x7FF0000000000000ull << 1); }
+
+__device__ __forceinline__ double speed_max(double l, double r)
+{
+    const unsigned long long bl = static_cast<unsigned long long>(__double_as_longlong(l));
+    const unsigned long long br = static_cast<unsigned long long>(__double_as_longlong(r));
+    return (!is_nan_bits(bl) && !is_nan_bits(br) && bl < br) ? r : l;
+}
+
+// Running maximum of speeds as bit patterns; NaN speeds never count (they
+// fail the reference's `speed > 1e-12`).
+__device__ __forceinline__ unsigned long long speed_fold(unsigned long long m, double s)
+{
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(s));
+    return (!is_nan_bits(b) && b > m) ? b : m;
 }
 
 // Rusanov flux across the face between staged cells cl (left) and cr
-// (right) along Morton axis dir (EulerPhysics.hpp:102-128).
+// (right) along Morton axis dir (EulerPhysics.hpp:102-128), from the states
+// and the one-side terms of the two cells.
 template <int R>
 __device__ __forceinline__ void face_flux(const double* cq, int BC, int cl, int cr, int dir, double* F)
 {
     constexpr int NV = kNV<R>;
-    const double  uL = cq[(NV + dir) * BC + cl], uR = cq[(NV + dir) * BC + cr];
-    const double  pL = cq[(NV + R) * BC + cl], pR = cq[(NV + R) * BC + cr];
-    const double  sL = cq[(NV + R + 1 + dir) * BC + cl], sR = cq[(NV + R + 1 + dir) * BC + cr];
-    const double  smax = (sL < sR) ? sR : sL; // std::max(left, right)
+    const int     q0 = (NV + dir * (R + 2)) * BC; // this direction's side terms
+    const double  smax = speed_max(cq[q0 + cl], cq[q0 + cr]);
     F[0] = 0.5 * (cq[(1 + dir) * BC + cl] + cq[(1 + dir) * BC + cr] - smax * (cq[cr] - cq[cl]));
 #pragma unroll
-    for (int d = 0; d < R; ++d) {
-        const double mL = cq[(1 + d) * BC + cl], mR = cq[(1 + d) * BC + cr];
-        double       fL = mL * uL;
-        double       fR = mR * uR;
-        if (d == dir) {
-            fL += pL;
-            fR += pR;
-        }
-        F[1 + d] = 0.5 * (fL + fR - smax * (mR - mL));
+    for (int k = 0; k < R; ++k) {
+        const double mL = cq[(1 + k) * BC + cl], mR = cq[(1 + k) * BC + cr];
+        F[1 + k] = 0.5 * (cq[q0 + (1 + k) * BC + cl] + cq[q0 + (1 + k) * BC + cr] - smax * (mR - mL));
     }
     const double EL = cq[(R + 1) * BC + cl], ER = cq[(R + 1) * BC + cr];
-    const double fLE = uL * (EL + pL);
-    const double fRE = uR * (ER + pR);
-    F[R + 1]         = 0.5 * (fLE + fRE - smax * (ER - EL));
+    F[R + 1] = 0.5 * (cq[q0 + (R + 1) * BC + cl] + cq[q0 + (R + 1) * BC + cr] - smax * (ER - EL));
 }
 
-// Block maximum of the per-thread speed maxima, then thread 0 folds
-// dx_d / max into the global minimum (ordered bit patterns of non-negative
-// doubles).  Speeds of at most 1e-12 never count (compute_time_step_cpu,
-// amr_solver.hpp:384-397); NaN speeds are skipped by fmax as by the
-// reference's `speed > 1e-12`.
+// Block maximum of the per-thread speed maxima (bit patterns), then thread
+// 0 folds dx_d / max into the global minimum (ordered bit patterns of
+// non-negative doubles).  Speeds of at most 1e-12 never count
+// (compute_time_step_cpu, amr_solver.hpp:384-397).
 template <int R>
-__device__ void fold_min_dt(double* smax, const double* cs, unsigned long long* slot)
+__device__ void fold_min_dt(unsigned long long* smax, const double* cs, unsigned long long* slot)
 {
-    __shared__ double red[32][R];
+    __shared__ unsigned long long red[32][R];
 #pragma unroll
     for (int d = 0; d < R; ++d) {
-        double v = smax[d];
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        unsigned long long v = smax[d];
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+            v                          = w > v ? w : v;
+        }
         smax[d] = v;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -174,8 +199,9 @@ __device__ void fold_min_dt(double* smax, const double* cs, unsigned long long* 
         double    m  = DBL_MAX;
 #pragma unroll
         for (int d = 0; d < R; ++d) {
-            double S = red[0][d];
-            for (int w = 1; w < nw; ++w) S = fmax(S, red[w][d]);
+            unsigned long long b = red[0][d];
+            for (int w = 1; w < nw; ++w) b = red[w][d] > b ? red[w][d] : b;
+            const double S = __longlong_as_double(static_cast<long long>(b));
             if (S > 1e-12) {
                 const double c = cs[d] / S;
                 if (c < m) m = c;
@@ -198,8 +224,8 @@ __global__ void k_euler_begin(unsigned long long* min_slot, int32_t* ctl, double
     cnt[0]      = 0;
 }
 
-// Primitive quantities of the interior and face-ghost cells of every patch,
-// and the minimum for the first step.  One block per patch.
+// Side terms of the interior and face-ghost cells of every patch, and the
+// minimum for the first step.  One block per patch.
 template <int R>
 __global__ void __launch_bounds__(256)
 k_euler_prims(const double* __restrict__ state, double* __restrict__ prim, size_t fs, const int32_t* __restrict__ levels,
@@ -208,10 +234,10 @@ k_euler_prims(const double* __restrict__ state, double* __restrict__ prim, size_
     constexpr int NV = kNV<R>;
     const int     p  = blockIdx.x;
     if (p >= P) return; // uniform per block
-    const size_t pb = static_cast<size_t>(p) * g.flat;
-    double       smax[R];
+    const size_t       pb = static_cast<size_t>(p) * g.flat;
+    unsigned long long smax[R];
 #pragma unroll
-    for (int d = 0; d < R; ++d) smax[d] = 0.0;
+    for (int d = 0; d < R; ++d) smax[d] = 0ull;
     for (int c = threadIdx.x; c < g.flat; c += blockDim.x) {
         int outside = 0, rem = c;
 #pragma unroll
@@ -221,14 +247,14 @@ k_euler_prims(const double* __restrict__ state, double* __restrict__ prim, size_
             outside += (i < g.h || i >= g.n + g.h) ? 1 : 0;
         }
         if (outside > 1) continue; // edge and corner ghosts: never read
-        double U[NV], u[R], pr, s[R];
+        double U[NV], q[kNP<R>];
 #pragma unroll
         for (int k = 0; k < NV; ++k) U[k] = state[k * fs + pb + c];
-        primitives<R>(U, gamma, u, pr, s);
-        store_prims<R>(prim, fs, pb + c, u, pr, s);
+        side_terms<R>(U, gamma, q);
+        store_terms<R>(prim, fs, pb + c, q);
         if (outside == 0)
 #pragma unroll
-            for (int d = 0; d < R; ++d) smax[d] = fmax(smax[d], s[d]);
+            for (int d = 0; d < R; ++d) smax[d] = speed_fold(smax[d], q[d * (R + 2)]);
     }
     double cs[R];
 #pragma unroll
@@ -322,7 +348,7 @@ __global__ void __launch_bounds__(256) k_euler_step(EulerStepArgs<R> a)
 #pragma unroll
             for (int k = 0; k < NV; ++k) out[k * fs + li] = in[k * fs + li];
 #pragma unroll
-            for (int q = 0; q < 2 * R + 1; ++q) po[q * fs + li] = pi[q * fs + li];
+            for (int q = 0; q < kNP<R>; ++q) po[q * fs + li] = pi[q * fs + li];
         }
         return;
     }
@@ -343,7 +369,7 @@ __global__ void __launch_bounds__(256) k_euler_step(EulerStepArgs<R> a)
 #pragma unroll
         for (int k = 0; k < NV; ++k) cq[k * t.BC + c] = in[k * fs + li];
 #pragma unroll
-        for (int q = 0; q < 2 * R + 1; ++q) cq[(NV + q) * t.BC + c] = pi[q * fs + li];
+        for (int q = 0; q < kNP<R>; ++q) cq[(NV + q) * t.BC + c] = pi[q * fs + li];
     }
     __syncthreads();
     // face fluxes, each face once
@@ -365,13 +391,15 @@ __global__ void __launch_bounds__(256) k_euler_step(EulerStepArgs<R> a)
         for (int k = 0; k < NV; ++k) fq[k * FT + f] = F[k];
     }
     __syncthreads();
-    const int    level = a.levels[p];
-    const double dt    = a.step_dt[0];
-    double       cs[R], smax[R];
+    const int          level = a.levels[p];
+    const double       dt    = a.step_dt[0];
+    double             cs[R], dt_over_dx[R];
+    unsigned long long smax[R];
 #pragma unroll
     for (int d = 0; d < R; ++d) {
-        cs[d]   = cell_size(g, d, level);
-        smax[d] = 0.0;
+        cs[d]         = cell_size(g, d, level);
+        dt_over_dx[d] = dt / cs[d]; // the same for every cell of the patch
+        smax[d]       = 0ull;
     }
     // cell updates: total -= dt/dx_d (F_right - F_left) over d = 0..rank-1
     for (int c = threadIdx.x; c < t.TC; c += blockDim.x) {
@@ -396,10 +424,9 @@ __global__ void __launch_bounds__(256) k_euler_step(EulerStepArgs<R> a)
             int sL = 1; // stride of dim L among this dim's faces
 #pragma unroll
             for (int M = R - 1; M > L; --M) sL *= t.T[M];
-            const double dt_over_dx = dt / cs[d];
-            const int    left = t.foff[L] + fi, right = left + sL;
+            const int left = t.foff[L] + fi, right = left + sL;
 #pragma unroll
-            for (int k = 0; k < NV; ++k) total[k] -= dt_over_dx * (fq[k * FT + right] - fq[k * FT + left]);
+            for (int k = 0; k < NV; ++k) total[k] -= dt_over_dx[d] * (fq[k * FT + right] - fq[k * FT + left]);
         }
         int bc = 0;
 #pragma unroll
@@ -412,17 +439,17 @@ __global__ void __launch_bounds__(256) k_euler_step(EulerStepArgs<R> a)
         const int li = padded_of<R>(g, o, z);
 #pragma unroll
         for (int k = 0; k < NV; ++k) out[k * fs + li] = U[k];
-        double u[R], pr, s[R];
-        primitives<R>(U, a.gamma, u, pr, s);
-        store_prims<R>(po, fs, li, u, pr, s);
+        double q[kNP<R>];
+        side_terms<R>(U, a.gamma, q);
+        store_terms<R>(po, fs, li, q);
 #pragma unroll
-        for (int d = 0; d < R; ++d) smax[d] = fmax(smax[d], s[d]);
+        for (int d = 0; d < R; ++d) smax[d] = speed_fold(smax[d], q[d * (R + 2)]);
     }
     fold_min_dt<R>(smax, cs, a.next_min);
 }
 
 // Face halo of every field (the same rules and arithmetic as the one-field
-// exchange), then the primitives of the ghost layer next to the interior.
+// exchange), then the side terms of the ghost layer next to the interior.
 template <int R>
 __global__ void __launch_bounds__(256)
 k_euler_halo(double* __restrict__ buf, double* __restrict__ prim, size_t fs, const amr_halo_meta* __restrict__ meta,
@@ -459,15 +486,16 @@ k_euler_halo(double* __restrict__ buf, double* __restrict__ prim, size_t fs, con
             }
         }
         if (G[L] == (pos ? g.n + g.h : g.h - 1)) {
-            double u[R], pr, s[R];
-            primitives<R>(U, gamma, u, pr, s);
-            store_prims<R>(prim, fs, at, u, pr, s);
+            double q[kNP<R>];
+            side_terms<R>(U, gamma, q);
+            store_terms<R>(prim, fs, at, q);
         }
     }
 }
 
 template <int R>
-cudaError_t step_r(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches)
+cudaError_t step_r(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches,
+                   cudaEvent_t ev0, cudaEvent_t ev1)
 {
     ETile<R> t{};
     if (!pick_tile<R>(b.g, t)) return cudaErrorInvalidValue;
@@ -495,8 +523,10 @@ cudaError_t step_r(const EulerBufs& b, int cur, int slot, double gamma, double c
     a.ctl      = b.ctl;
     a.next_min = b.min_slot + (slot ^ 1);
     a.gamma    = gamma;
+    if (ev0) cudaEventRecord(ev0, b.stream);
     if (b.P > 0)
         k_euler_step<R><<<static_cast<unsigned>(b.P) * t.ntiles, t.threads, t.smem, b.stream>>>(a);
+    if (ev1) cudaEventRecord(ev1, b.stream);
     const long long total = static_cast<long long>(b.P) * b.g.ndir * b.g.h * (b.g.cells / b.g.n);
     if (total > 0) {
         const unsigned grid = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 64));
@@ -526,10 +556,11 @@ cudaError_t euler_begin(const EulerBufs& b, int cur, double gamma, double remain
                          : begin_r<3>(b, cur, gamma, remaining, launches);
 }
 
-cudaError_t euler_step(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches)
+cudaError_t euler_step(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches,
+                       cudaEvent_t ev0, cudaEvent_t ev1)
 {
-    return b.g.rank == 2 ? step_r<2>(b, cur, slot, gamma, cfl, launches)
-                         : step_r<3>(b, cur, slot, gamma, cfl, launches);
+    return b.g.rank == 2 ? step_r<2>(b, cur, slot, gamma, cfl, launches, ev0, ev1)
+                         : step_r<3>(b, cur, slot, gamma, cfl, launches, ev0, ev1);
 }
 
 bool euler_supported(const Geo& g)

@@ -8,9 +8,10 @@
 namespace amr_gb300 {
 
 // Device buffers of one Euler advance.  State fields (rho, rho u_d, E) and
-// primitive quantities (u_d, p, |u_d| + a) are each fstride elements apart;
-// state[b] and prim[b] belong together (buffer b).  Primitive quantities
-// are kept for interior and face-ghost cells.
+// the one-side flux terms of each direction d (|u_d| + a, m_k u_d + [k = d]
+// p, u_d (E + p): rank * (rank + 2) quantities) are each fstride elements
+// apart; state[b] and prim[b] belong together (buffer b).  Side terms are
+// kept for interior and face-ghost cells.
 struct EulerBufs {
     Geo                  g;
     int                  P;
@@ -29,16 +30,19 @@ struct EulerBufs {
 };
 
 // Starts an advance on state[cur] (face ghosts current): resets the time
-// bookkeeping to `remaining`, computes the primitive quantities of
-// state[cur] into prim[cur] and the minimum for the first step into slot 0.
+// bookkeeping to `remaining`, computes the side terms of state[cur] into
+// prim[cur] and the minimum for the first step into slot 0.
 // Adds the kernels launched to *launches.
 cudaError_t euler_begin(const EulerBufs& b, int cur, double gamma, double remaining, uint64_t* launches);
 
 // One step from state[cur] into state[1 - cur]: the step size from slot
 // `slot` (clamped to the remaining time), the Rusanov update of every field,
-// the primitives and the next step's minimum (slot 1 - slot), then the face
-// halo of every field with the ghosts' primitives.
-cudaError_t euler_step(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches);
+// the side terms and the next step's minimum (slot 1 - slot), then the face
+// halo of every field with the ghosts' side terms.
+// ev0 / ev1 (optional) are recorded on the stream right before and after the
+// update kernel.
+cudaError_t euler_step(const EulerBufs& b, int cur, int slot, double gamma, double cfl, uint64_t* launches,
+                       cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 
 // Threads and shared memory of the update kernel for a patch shape; false
 // when no tile of the patch fits in shared memory.

@@ -202,7 +202,7 @@ struct amr_tree {
     unsigned long long* euler_min = nullptr;
     double*             euler_dt  = nullptr;
     int32_t*            euler_ctl = nullptr;
-    double*             prim[2]{}; // primitive quantities beside sbuf[0] / sbuf[1]
+    double*             prim[2]{}; // one-side flux terms beside sbuf[0] / sbuf[1]
     size_t              prim_cap = 0;
 
     size_t fstride() const { return cap * static_cast<size_t>(g.flat); }
@@ -1222,7 +1222,7 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     cudaFree(t->src);
     cudaFree(t->skind);
     cudaFree(t->tile_sums);
-    cudaFree(t->prim[0]); // rebuilt by the next Euler advance
+    cudaFree(t->prim[0]); // side terms: rebuilt by the next Euler advance
     cudaFree(t->prim[1]);
     t->prim[0] = t->prim[1] = nullptr;
     t->prim_cap = 0;
@@ -2147,7 +2147,7 @@ static amr_status euler_check(amr_tree* t)
 
 static amr_status euler_advance_impl(amr_tree* t, size_t steps, double gamma, double cfl, double remaining)
 {
-    const size_t prim_elems = static_cast<size_t>(2 * t->g.rank + 1) * t->fstride();
+    const size_t prim_elems = static_cast<size_t>(t->g.rank * (t->g.rank + 2)) * t->fstride();
     if (t->prim_cap != t->cap) {
         cudaFree(t->prim[0]);
         cudaFree(t->prim[1]);
@@ -2182,7 +2182,21 @@ static amr_status euler_advance_impl(amr_tree* t, size_t steps, double gamma, do
     uint64_t launches = 0;
     cudaError_t e = euler_begin(b, cur, gamma, remaining, &launches);
     for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
-        e = euler_step(b, cur, static_cast<int>(k & 1), gamma, cfl, &launches);
+        std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
+        if (t->timing) { // opt-in timing of the update kernel
+            if (t->events_used == t->events.size()) {
+                std::pair<cudaEvent_t, cudaEvent_t> pe;
+                AMR_CUDA(cudaEventCreate(&pe.first));
+                AMR_CUDA(cudaEventCreate(&pe.second));
+                t->events.push_back(pe);
+                t->event_cells.push_back(0);
+            }
+            ev = &t->events[t->events_used];
+            t->event_cells[t->events_used] = static_cast<uint64_t>(b.P) * t->g.cells;
+            ++t->events_used;
+        }
+        e = euler_step(b, cur, static_cast<int>(k & 1), gamma, cfl, &launches, ev ? ev->first : nullptr,
+                       ev ? ev->second : nullptr);
         cur ^= 1;
     }
     g_launches.fetch_add(launches, std::memory_order_relaxed);

@@ -359,8 +359,8 @@ amr_status amr_adjoint_backward_host(amr_adjoint* a, const void* host_lambda_T, 
 amr_status amr_adjoint_checkpoint(amr_adjoint* a, size_t index, void* device_dst);
 amr_status amr_adjoint_checkpoint_count(const amr_adjoint* a, size_t* count);
 
-/* Per-launch timing of the fused update kernel with CUDA events on the tree's
- * stream (the counterpart of the reference's profiler ranges,
+/* Per-launch timing of the fused update kernel (advection or Euler) with CUDA
+ * events on the tree's stream (the counterpart of the reference's profiler ranges,
  * include/cuda/profiler.hpp:7-30).  get_timing synchronizes, returns the
  * summed kernel time, launch count and cell updates since the last call, and
  * clears them. */
