@@ -9,8 +9,11 @@
 // C ABI become std::runtime_error, the reference's convention
 // (src/cuda/device_buffer.cu:17-27).
 //
-// Supported: one scalar field (the advection cell), cubic patches, halo >= 1,
-// rank 2 or 3.
+// Supported: cells of FP64 fields (the advection cell, the Euler cells), one
+// device array per field; cubic patches, halo >= 1, rank 2 or 3.  Edge and
+// corner ghosts, which the face halo exchange never writes, read as -1000
+// through get_patch, the value the reference's checking build leaves in them
+// (swap_buffers, ndtree.hpp:1558-1579).
 #pragma once
 
 #include "amr_gb300.h"
@@ -28,6 +31,7 @@
 #include <string>
 #include <tuple>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 namespace amr::gb300
@@ -55,10 +59,32 @@ public:
     template <typename Map_Type>
     using patch_t = patches::patch<typename Map_Type::type, patch_layout_t>;
 
-    static_assert(std::tuple_size_v<deconstructed_raw_map_types_t> == 1,
-                  "the GPU path carries one scalar field per cell");
+    static constexpr std::size_t n_fields = std::tuple_size_v<deconstructed_raw_map_types_t>;
     using field_t = std::tuple_element_t<0, deconstructed_raw_map_types_t>;
-    static_assert(std::is_same_v<typename field_t::type, double>, "FP64 state");
+    static_assert([]<std::size_t... I>(std::index_sequence<I...>) {
+        return (std::is_same_v<typename std::tuple_element_t<I, deconstructed_raw_map_types_t>::type, double> && ...);
+    }(std::make_index_sequence<n_fields>{}), "FP64 fields");
+
+    // position of a field tag in the cell's tuple (its device array)
+    template <typename Map_Type>
+    static constexpr auto field_index() noexcept -> std::size_t
+    {
+        return []<std::size_t... I>(std::index_sequence<I...>) {
+            std::size_t r = n_fields;
+            ((std::is_same_v<Map_Type, std::tuple_element_t<I, deconstructed_raw_map_types_t>> ? (r = I) : 0), ...);
+            return r;
+        }(std::make_index_sequence<n_fields>{});
+    }
+
+    // the field names in tuple order, separated by commas (the VTK writer)
+    static auto field_names() -> std::string
+    {
+        std::string out;
+        [&]<std::size_t... I>(std::index_sequence<I...>) {
+            ((out += (I ? "," : ""), out += std::tuple_element_t<I, deconstructed_raw_map_types_t>::name()), ...);
+        }(std::make_index_sequence<n_fields>{});
+        return out;
+    }
 
     enum struct RefinementStatus : std::int8_t { Stable = 0, Refine = 1, Coarsen = 2 };
     using refine_status_t = RefinementStatus;
@@ -89,9 +115,11 @@ public:
         d.capacity = capacity;
         d.dtype    = AMR_F64;
         d.stream   = stream;
+        d.fields   = static_cast<int32_t>(n_fields);
         amr::gb300::check(amr_tree_create(&d, &m_tree));
-        m_host.resize(1);
-        std::memset(m_host.data(), 0, sizeof(patch_t<field_t>));
+        m_capacity = capacity;
+        m_host.resize(n_fields);
+        std::memset(static_cast<void*>(m_host.data()), 0, n_fields * sizeof(patch_t<field_t>));
         m_host_valid = true;
     }
 
@@ -126,17 +154,22 @@ public:
     template <typename Map_Type>
     [[nodiscard]] auto get_patch(linear_index_t i) -> patch_t<Map_Type>&
     {
-        static_assert(std::is_same_v<Map_Type, field_t>);
-        load_host();
-        m_host_dirty = true;
-        return m_host.at(i);
+        static_assert(field_index<Map_Type>() < n_fields, "not a field of this cell");
+        return get_field_patch(field_index<Map_Type>(), i);
     }
     template <typename Map_Type>
     [[nodiscard]] auto get_patch(linear_index_t i) const -> patch_t<Map_Type> const&
     {
-        static_assert(std::is_same_v<Map_Type, field_t>);
+        static_assert(field_index<Map_Type>() < n_fields, "not a field of this cell");
         load_host();
-        return m_host.at(i);
+        return m_host.at(field_index<Map_Type>() * host_patches() + i);
+    }
+    // patch i of field f (tuple position), for code that loops over fields
+    [[nodiscard]] auto get_field_patch(std::size_t f, linear_index_t i) -> patch_t<field_t>&
+    {
+        load_host();
+        m_host_dirty = true;
+        return m_host.at(f * host_patches() + i);
     }
     template <typename Map_Type>
     [[nodiscard]] auto get_patch(patch_index_t id) -> patch_t<Map_Type>&
@@ -156,10 +189,11 @@ public:
         push_host();
         void *cur = nullptr, *nxt = nullptr;
         amr::gb300::check(amr_tree_device_state(m_tree, &cur, &nxt));
+        const std::size_t off = field_index<Map_Type>() * m_capacity; // field arrays, capacity patches apart
         if constexpr (std::is_same_v<std::remove_cvref_t<decltype(Buffer)>, next_buffer_t>)
-            return static_cast<patch_t<Map_Type>*>(nxt);
+            return static_cast<patch_t<Map_Type>*>(nxt) + off;
         else
-            return static_cast<patch_t<Map_Type>*>(cur);
+            return static_cast<patch_t<Map_Type>*>(cur) + off;
     }
 
     void sync_current_to_device()
@@ -250,22 +284,37 @@ private:
         amr::gb300::check(amr_tree_get_ids(m_tree, m_ids.data(), m_ids.size()));
         m_ids_valid = true;
     }
+    auto host_patches() const -> std::size_t { return m_host.size() / n_fields; }
     void load_host() const
     {
         if (m_host_valid) return;
-        m_host.resize(size());
-        amr::gb300::check(amr_tree_download_state(m_tree, m_host.data(), m_host.size()));
+        const std::size_t n = size();
+        m_host.resize(n_fields * n);
+        amr::gb300::check(amr_tree_download_state(m_tree, m_host.data(), n));
+        // edge and corner ghosts: never written by the face halo exchange
+        for (auto& patch : m_host)
+            for (std::size_t li = 0; li != patch_layout_t::flat_size(); ++li)
+                if (edge_or_corner(li)) patch[static_cast<typename patch_layout_t::index_t>(li)] = -1000;
         m_host_valid = true;
         m_host_dirty = false;
+    }
+    static auto edge_or_corner(std::size_t li) -> bool
+    {
+        constexpr std::size_t P1 = patch_layout_t::data_layout_t::sizes()[0] + 2 * patch_layout_t::halo_width();
+        constexpr std::size_t h  = patch_layout_t::halo_width();
+        int                   outside = 0;
+        for (std::size_t k = 0; k < rank(); ++k, li /= P1) outside += (li % P1 < h || li % P1 >= P1 - h) ? 1 : 0;
+        return outside > 1;
     }
     void push_host()
     {
         if (!m_host_dirty) return;
-        amr::gb300::check(amr_tree_upload_state(m_tree, m_host.data(), m_host.size()));
+        amr::gb300::check(amr_tree_upload_state(m_tree, m_host.data(), host_patches()));
         m_host_dirty = false;
     }
 
     amr_tree*                                 m_tree = nullptr;
+    std::size_t                               m_capacity = 0;
     mutable std::vector<patch_t<field_t>>     m_host;
     mutable std::vector<std::uint64_t>        m_ids;
     mutable bool                              m_host_valid = false;

@@ -33,7 +33,7 @@ struct vtk_print
     {
         using tree_t                   = std::remove_cvref_t<decltype(tree)>;
         const std::string full_filename = "vtk_output/" + m_base_filename + filename_extension;
-        const std::string field(tree_t::field_t::name());
+        const std::string field = tree_t::field_names(); // one SCALARS block per field
         auto&             t = const_cast<tree_t&>(tree);
         const amr_status  s = amr_tree_write_vtk(t.handle(), full_filename.c_str(), field.c_str());
         if (s != AMR_OK) throw std::runtime_error("Cannot write file: " + full_filename + ": " + amr_last_error());

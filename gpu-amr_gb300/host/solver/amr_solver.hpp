@@ -2,8 +2,10 @@
 // (include/solver/amr_solver.hpp:28-544) on the GB300 device-resident tree:
 // initialize() evaluates the initial condition on the host like the
 // reference (amr_solver.hpp:105-145); advance_batch_async /
-// finish_advance_batch run forward-Euler Rusanov steps of linear advection on
-// the GPU with dt = cfl * min(dx/|v|) clamped to the remaining time.
+// finish_advance_batch run forward-Euler Rusanov steps on the GPU with the CFL
+// step clamped to the remaining time: linear advection (NVAR = 1, dt = cfl *
+// min dx/|v|) or compressible Euler (NVAR = DIM + 2, EulerPhysics, dt = cfl *
+// min dx/(|u| + a), amr_tree_euler_advance).
 #pragma once
 
 #include "ndtree/ndtree.hpp"
@@ -24,12 +26,15 @@ public:
     static constexpr auto NVAR = EquationT::NVAR;
     using arithmetic_t         = double;
     static_assert(DIM == 2 || DIM == 3, "Error: Wrong dimension");
-    static_assert(NVAR == 1, "the GPU path advects one scalar");
+    static constexpr bool euler = NVAR == DIM + 2;
+    static_assert(NVAR == 1 || euler, "advection (one field) or Euler (DIM + 2 fields)");
+    static_assert(NVAR == static_cast<int>(tree_t::n_fields), "the cell carries the equation's fields");
 
     amr_solver(std::size_t capacity, arithmetic_t gamma_ = 1.4, arithmetic_t cfl_ = 0.1)
         : m_tree(capacity, domain_lengths()), m_gamma(gamma_), m_cfl(cfl_)
     {
-        for (int a = 0; a < 3; ++a) m_velocity[a] = EquationT::Velocity[a];
+        if constexpr (!euler)
+            for (int a = 0; a < 3; ++a) m_velocity[a] = EquationT::Velocity[a];
     }
 
     auto get_tree() -> TreeT& { return m_tree; }
@@ -39,11 +44,9 @@ public:
 
     void initialize(auto&& init_func)
     {
-        using field_t = typename tree_t::field_t;
         for (std::size_t p = 0; p < m_tree.size(); ++p) {
-            const auto id    = m_tree.get_node_index_at(p);
-            const auto cs    = GeometryT::cell_sizes(id);
-            auto&      patch = m_tree.template get_patch<field_t>(p);
+            const auto id = m_tree.get_node_index_at(p);
+            const auto cs = GeometryT::cell_sizes(id);
             for (std::size_t li = 0; li != patch_layout_t::flat_size(); ++li) {
                 if (amr::ndt::utils::patches::is_halo_cell<patch_layout_t>(
                         static_cast<typename patch_layout_t::index_t>(li)))
@@ -54,7 +57,9 @@ public:
                 const auto prim = std::invoke(init_func, coords);
                 amr::containers::static_vector<arithmetic_t, NVAR> cons;
                 EquationT::primitiveToConservative(prim, cons, m_gamma);
-                patch[static_cast<typename patch_layout_t::index_t>(li)] = cons[0];
+                for (int f = 0; f < NVAR; ++f)
+                    m_tree.get_field_patch(static_cast<std::size_t>(f), p)[static_cast<typename patch_layout_t::index_t>(li)] =
+                        cons[f];
             }
         }
     }
@@ -68,7 +73,10 @@ public:
     void advance_batch_async(std::size_t step_count,
                              arithmetic_t remaining_time = std::numeric_limits<arithmetic_t>::max())
     {
-        amr::gb300::check(amr_tree_advance(m_tree.handle(), step_count, m_velocity.data(), m_cfl, remaining_time));
+        if constexpr (euler)
+            amr::gb300::check(amr_tree_euler_advance(m_tree.handle(), step_count, m_gamma, m_cfl, remaining_time));
+        else
+            amr::gb300::check(amr_tree_advance(m_tree.handle(), step_count, m_velocity.data(), m_cfl, remaining_time));
     }
 
     auto finish_advance_batch(std::size_t* executed_step_count = nullptr) -> arithmetic_t
@@ -85,6 +93,7 @@ public:
     auto run(std::size_t steps, std::size_t interval, amr::gb300::gradient_criterion const& c,
              arithmetic_t remaining_time = std::numeric_limits<arithmetic_t>::max()) -> amr_cycle_stats
     {
+        static_assert(!euler, "Euler: run_euler");
         amr_cycle_params prm{};
         prm.steps           = steps;
         prm.remesh_interval = interval;
@@ -98,6 +107,28 @@ public:
         prm.coarsen_threshold = c.coarsen_threshold;
         amr_cycle_stats st{};
         amr::gb300::check(amr_tree_run(m_tree.handle(), &prm, &st));
+        return st;
+    }
+
+    // The Euler benchmark loop on the device (amr_tree_euler_run): advance
+    // `interval` steps with the time left, max-Rho flags, re-mesh, until
+    // `steps` steps ran or the simulated time reaches end_time.
+    auto run_euler(std::size_t steps, std::size_t interval, double end_time,
+                   amr::gb300::max_value_criterion const& c) -> amr_cycle_stats
+    {
+        static_assert(euler, "the equation is not Euler");
+        amr_euler_params prm{};
+        prm.steps             = steps;
+        prm.remesh_interval   = interval;
+        prm.gamma             = m_gamma;
+        prm.cfl               = m_cfl;
+        prm.end_time          = end_time;
+        prm.refine_threshold  = c.refine_threshold;
+        prm.coarsen_threshold = c.coarsen_threshold;
+        prm.min_level         = c.min_level;
+        prm.max_level         = c.max_level;
+        amr_cycle_stats st{};
+        amr::gb300::check(amr_tree_euler_run(m_tree.handle(), &prm, &st));
         return st;
     }
 

@@ -4,7 +4,9 @@
 // GoogleTest is replaced by a minimal EXPECT_NEAR.  A second mode runs the
 // reference benchmark loop (bench_fvm_solver_integration_active_amr.b.cpp:
 // 220-250) on the config-2 workload and prints the final tree and state for
-// comparison with the oracle.
+// comparison with the oracle; a third runs the Euler benchmark's set-up and
+// loop (bench_fvm_solver_integration.b.cpp:34-250: EulerCell2D, acoustic
+// pulse, host max-Rho criterion) on 8x8 patches.
 #include "containers/static_layout.hpp"
 #include "containers/static_shape.hpp"
 #include "containers/static_vector.hpp"
@@ -14,6 +16,7 @@
 #include "ndtree/patch_layout.hpp"
 #include "ndtree/vtk_print.hpp"
 #include "solver/AdvectionPhysics.hpp"
+#include "solver/EulerPhysics.hpp"
 #include "solver/adjoint.hpp"
 #include "solver/amr_solver.hpp"
 #include "solver/cell_types.hpp"
@@ -225,6 +228,90 @@ int bench_loop(int argc, char** argv)
     return 0;
 }
 
+// The Euler benchmark written against the reference's API: amr_solver with
+// EulerPhysics2D, initialize() with the acoustic pulse, a host criterion on
+// the Rho patches through reconstruct_tree, the advance/re-mesh/halo loop.
+// argv: steps remesh init_levels min_level max_level.  Prints the initial and
+// final state (interior and face-ghost cells, field by field), the ids, the
+// simulated time and the executed steps.
+int euler_loop(int argc, char** argv)
+{
+    using shape_t        = amr::containers::static_shape<8u, 8u>;
+    using layout_t       = amr::containers::static_layout<shape_t>;
+    using patch_index_t  = amr::ndt::morton::morton_id<7u, 2u>;
+    using patch_layout_t = amr::ndt::patches::patch_layout<layout_t, 1>;
+    using interp_t       = amr::ndt::intergrid_operator::linear_interpolator<patch_layout_t>;
+    using tree_t         = amr::ndt::tree::ndtree<amr::cell::EulerCell2D, patch_index_t, patch_layout_t, interp_t>;
+    static constexpr std::array<double, 2> lengths = { 1000.0, 1000.0 };
+    using physics_t = amr::ndt::solver::physics_system<patch_index_t, patch_layout_t, lengths>;
+    (void)argc;
+    const long steps = std::atol(argv[2]), interval = std::atol(argv[3]);
+    const int  init = std::atoi(argv[4]), min_level = std::atoi(argv[5]), max_level = std::atoi(argv[6]);
+
+    amr_solver<tree_t, physics_t, EulerPhysics2D, 2> solver(20000, 1.4, 0.3);
+    auto& tree       = solver.get_tree();
+    auto  refine_all = [](patch_index_t const&) { return tree_t::refine_status_t::Refine; };
+    for (int i = 0; i < init; ++i) {
+        tree.reconstruct_tree(refine_all);
+        tree.halo_exchange_update();
+    }
+    // acoustic pulse: rho = 0.5 + 0.2 A e, p = 1 + A e, e = exp(-r^2 / w^2)
+    const double amp = 10.0, width_sq = 0.01 * lengths[0] * lengths[1];
+    solver.initialize([&](auto const& x) -> amr::containers::static_vector<double, 4> {
+        const double dx = x[0] - 0.5 * lengths[0], dy = x[1] - 0.5 * lengths[1];
+        const double e  = amp * std::exp(-(dx * dx + dy * dy) / width_sq);
+        return { 0.5 + (e * 0.2), 0.0, 0.0, 1.0 + e };
+    });
+    tree.sync_current_to_device();
+    tree.halo_exchange_update();
+    auto print_state = [&](const char* tag) {
+        const auto faces = [](std::size_t li) {
+            int outside = 0;
+            for (int k = 0; k < 2; ++k, li /= 10) outside += (li % 10 == 0 || li % 10 == 9) ? 1 : 0;
+            return outside <= 1;
+        };
+        for (std::size_t f = 0; f < 4; ++f)
+            for (std::size_t p = 0; p < tree.size(); ++p) {
+                auto const& u = tree.get_field_patch(f, p);
+                for (std::size_t li = 0; li != patch_layout_t::flat_size(); ++li)
+                    if (faces(li)) std::printf("%s %.17g\n", tag, u[li]);
+            }
+    };
+    print_state("s0");
+    // the benchmark's criterion, evaluated on the host over the Rho patch
+    struct rho_criterion
+    {
+        tree_t& t;
+        double  rthr, cthr;
+        int     minl, maxl;
+        auto operator()(patch_index_t const& idx) const -> tree_t::refine_status_t
+        {
+            auto const& rho = t.template get_patch<amr::cell::Rho>(idx);
+            double      m   = 0.0;
+            for (std::size_t li = 0; li != patch_layout_t::flat_size(); ++li) m = std::max(rho[li], m);
+            if (idx.level() < maxl && m > rthr) return tree_t::refine_status_t::Refine;
+            if (idx.level() > minl && m < cthr) return tree_t::refine_status_t::Coarsen;
+            return tree_t::refine_status_t::Stable;
+        }
+    };
+    const rho_criterion crit{ tree, 0.53, 0.49, min_level, max_level };
+    double t = 0.0;
+    long   done = 0;
+    while (done < steps) {
+        solver.advance_batch_async(static_cast<std::size_t>(std::min(interval, steps - done)));
+        tree.reconstruct_tree(crit);
+        tree.halo_exchange_update();
+        std::size_t executed = 0;
+        t += solver.finish_advance_batch(&executed);
+        done += static_cast<long>(executed);
+        if (executed == 0) break;
+    }
+    std::printf("time %.17g steps %ld leaves %zu\n", t, done, tree.size());
+    for (std::size_t p = 0; p < tree.size(); ++p) std::printf("id %llu\n", (unsigned long long)tree.get_node_index_at(p).id());
+    print_state("s1");
+    return 0;
+}
+
 // The adjoint through the C++ header: dot-product identity
 // <lambda_T, A u_0> = <A^T lambda_T, u_0> over interior cells on a 2:1 mesh.
 static int adjoint_check()
@@ -281,6 +368,7 @@ int main(int argc, char** argv)
     const std::string mode = argc > 1 ? argv[1] : "tests";
     if (mode == "bench") return bench_loop(argc, argv);
     if (mode == "adjoint") return adjoint_check();
+    if (mode == "euler") return euler_loop(argc, argv);
     PulseCenterMovement<AdvectionTestConfig<2, 10>>();
     PulseCenterMovement<AdvectionTestConfig<2, 50>>();
     PulseCenterMovementAMR<AdvectionTestConfig<2, 10>>();

@@ -64,3 +64,41 @@ def test_adjoint_through_cpp_header(dropin_exe):
     r = subprocess.run([str(dropin_exe), "adjoint"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "PASSED" in r.stdout
+
+
+@pytest.mark.gpu
+def test_euler_benchmark_through_dropin_matches_reference(dropin_exe):
+    """The Euler benchmark's set-up and loop written against the reference's
+    API (amr_solver<..., EulerPhysics2D, 2>, initialize, host max-Rho
+    criterion through reconstruct_tree) on the 2D Euler fixture's
+    configuration: initial state, trees, final state of every field
+    (interior and face-ghost cells) and the simulated time equal the
+    reference's run.  The initial condition goes through the host's exp; if
+    that differs from the fixture machine's in a last bit, the bars fall
+    back to 1e-12 relative."""
+    from conftest import face_mask
+
+    z, meta = load_golden("euler_pulse_2d")
+    p = meta["params"]
+    args = [str(dropin_exe), "euler", str(p["steps"]), str(p["remesh"]), str(p["init_levels"]),
+            str(p["min_level"]), str(p["max_level"])]
+    r = subprocess.run(args, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    s0 = np.array([float(l.split()[1]) for l in lines if l.startswith("s0 ")])
+    s1 = np.array([float(l.split()[1]) for l in lines if l.startswith("s1 ")])
+    head = [l for l in lines if l.startswith("time ")][0].split()
+    time, steps = float(head[1]), int(head[3])
+    ids = np.array([int(l.split()[1]) for l in lines if l.startswith("id ")], np.uint64)
+    m = face_mask(2, 8, 1)
+    want0 = np.moveaxis(z["state_init"], 1, 0)[..., m].ravel()
+    want1 = np.moveaxis(z["state_final"], 1, 0)[..., m].ravel()
+    k = int(z["remeshes"]) - 1
+    np.testing.assert_array_equal(ids, z[f"ids_{k}"])
+    assert steps == int(z["steps"])
+    if np.array_equal(s0, want0):
+        np.testing.assert_array_equal(s1, want1)
+        assert time == float(z["time"])
+    else:
+        assert rel_l2(s0, want0) <= 1e-15
+        assert rel_l2(s1, want1) <= 1e-12 and abs(time - float(z["time"])) <= 1e-12 * float(z["time"])
