@@ -25,7 +25,8 @@ struct RunCtl {
     int32_t nerr;       // neighbour rebuild error of the pending re-mesh
     int32_t leaves_min; // over interval starts
     int32_t leaves_max;
-    int32_t pad[2];
+    int32_t uniform;    // every neighbour relation of the current tree is "same level"
+    int32_t pad;
     unsigned long long cell_updates, leaves_sum, intervals, remeshes;
 };
 
@@ -71,6 +72,36 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     step2d_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P, g,
                             coef, coef32, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars, p, nwarp);
+}
+
+// Two steps per pass (trees of same-level relations only; the interval's
+// guard has checked ctl->uniform).  parity selects the buffers of this pass.
+template <typename T, int N, int H, int W, int S>
+__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
+k_run_step2d_pair(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coefA, const float2* __restrict__ coef32A,
+                  const Coef* __restrict__ coefB, const float2* __restrict__ coef32B, int parity, int upx0, int upy0)
+{
+    if (ctl->err) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
+    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    step2d_pair_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P, g,
+                                 coefA, coef32A, coefB, coef32B, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles,
+                                 bars, p, nwarp);
+}
+
+// First kernel of an interval captured with two-step passes: when a re-mesh
+// has made the tree non-uniform, the interval must not run; kRetryUniform
+// stops every later kernel of the replay, and the host re-runs the interval
+// with one-step launches.
+constexpr int32_t kRetryUniform = 100;
+__global__ void k_run_require_uniform(RunCtl* ctl)
+{
+    if (threadIdx.x == 0 && ctl->err == 0 && !ctl->uniform) ctl->err = kRetryUniform;
 }
 
 // Any geometry: ppb patches per block per round, grid-stride over rounds.
@@ -311,6 +342,7 @@ __global__ void k_run_emit(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->changed) return;
     const int P = ctl->P, tb = ctl->tb, nb = tb ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->uniform = 1; // k_run_neighbors clears it
     AMR_RUN_LEAVES(P)
     emit_leaf(B.keys[tb], B.rmark, B.chead, B.pos, g, B.keys[nb], B.levels[nb], B.src, B.skind, B.maxlev_new, i);
 }
@@ -341,8 +373,10 @@ __global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->changed) return;
     const int NP = ctl->NP, nb = ctl->tb ^ 1;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < NP * g.ndir; t += gridDim.x * blockDim.x)
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < NP * g.ndir; t += gridDim.x * blockDim.x) {
         neighbor_entry(B.keys[nb], NP, g, B.meta[nb], &ctl->nerr, t);
+        if (B.meta[nb][t].relation != REL_SAME) ctl->uniform = 0;
+    }
 }
 
 // End of an interval (one block): statistics of the interval just run and

@@ -457,9 +457,11 @@ enum : int {
 __global__ void __launch_bounds__(256)
 k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
               int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef,
-              float2* __restrict__ coef32 = nullptr, int32_t* __restrict__ upcode = nullptr)
+              float2* __restrict__ coef32 = nullptr, int32_t* __restrict__ upcode = nullptr,
+              const int32_t* __restrict__ skip = nullptr)
 {
     __shared__ double dts[1024];
+    if (skip && *skip) return; // a graph interval that was stopped before it began
     const int         inst  = blockIdx.x;
     const int         ninst = gridDim.x;
     const double      v[3]  = { vel[3 * inst], vel[3 * inst + 1], vel[3 * inst + 2] };
@@ -733,6 +735,14 @@ k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_
         return;
     }
     for (int c = threadIdx.x; c < g.cells; c += blockDim.x) remap_cell<T>(old_state, new_state, g, kind, src[j], j, c);
+}
+
+// flag = 1 when some neighbour record is not "same level" (flag zeroed first).
+__global__ void k_any_not_same(const amr_halo_meta* __restrict__ meta, long long n, int32_t* flag)
+{
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+        if (meta[t].relation != REL_SAME) *flag = 1;
 }
 
 __device__ inline int upper_bound_u64(const uint64_t* a, int n, uint64_t x)
@@ -1018,6 +1028,27 @@ struct Coef2<float> {
     float cx, cy;
 };
 
+// One cell update of the 2D kernels from the cell u, its upwind x neighbour
+// xn and upwind y neighbour yn.  FP32: u + c (u_up - u), exact for a constant
+// state, so the rounding of the coefficients does not bias the solution;
+// FP64: c0 u + c_x u_x + c_y u_y.  Every 2D update goes through this one
+// function, so fused and separate steps round alike.
+template <typename T>
+__device__ __forceinline__ T upd2d(T u, T xn, T yn, const Coef2<T>& cf, int ux, int uy)
+{
+    if constexpr (sizeof(T) == 4) {
+        float acc = u;
+        if (ux != 0) acc = fmaf(cf.cx, xn - u, acc);
+        if (uy != 0) acc = fmaf(cf.cy, yn - u, acc);
+        return acc;
+    } else {
+        T acc = static_cast<T>(cf.c0) * u;
+        if (ux != 0) acc = fma(static_cast<T>(cf.cx), xn, acc);
+        if (uy != 0) acc = fma(static_cast<T>(cf.cy), yn, acc);
+        return acc;
+    }
+}
+
 // coef: the full rows (FP64 path); coef32: (c_x, c_y) rows (FP32 path);
 // upcode: per-instance packed upwind offsets, or nullptr for upx0/upy0.
 template <typename T, int N, int H, int S>
@@ -1211,33 +1242,9 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
 #pragma unroll
         for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
         T res[SEG];
-        if constexpr (sizeof(T) == 4) {
-            // FP32: u + c (u_up - u), exact for a constant state, so the
-            // rounding of the coefficients does not bias the solution
-            const float cx = sd0.cf.cx, cy = sd0.cf.cy;
 #pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const float u   = colv[k + 1];
-                const float xn  = tile[(r0 + k) * P1 + cl + ux];
-                const float yn  = uy < 0 ? colv[k] : colv[k + 2];
-                float       acc = u;
-                if (ux != 0) acc = fmaf(cx, xn - u, acc);
-                if (uy != 0) acc = fmaf(cy, yn - u, acc);
-                res[k] = acc;
-            }
-        } else {
-            const T c00 = static_cast<T>(sd0.cf.c0), cx = static_cast<T>(sd0.cf.cx), cy = static_cast<T>(sd0.cf.cy);
-#pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const T u   = colv[k + 1];
-                const T xn  = tile[(r0 + k) * P1 + cl + ux];
-                const T yn  = uy < 0 ? colv[k] : colv[k + 2];
-                T       acc = c00 * u;
-                if (ux != 0) acc = fma(cx, xn, acc);
-                if (uy != 0) acc = fma(cy, yn, acc);
-                res[k] = acc;
-            }
-        }
+        for (int k = 0; k < SEG; ++k)
+            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.cf, ux, uy);
         __syncwarp();
 #pragma unroll
         for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
@@ -1249,6 +1256,232 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
         // rotate the pipeline
         sd0 = sd1;
         g0  = g1;
+        sd1 = sd2;
+        m1  = m2;
+        k2  = k3;
+    }
+}
+
+// ------------------------------------------------ 2D update, two steps per pass
+// Two consecutive steps of a tree whose every neighbour relation is "same
+// level" (each instance uniform, as in the batched forests), in one pass over
+// memory: the patch is read once and written once per two steps.  Step one
+// needs the upwind ghost column and row of u^n (the neighbours' edge cells,
+// as in the one-step kernel); step two needs the same ghosts of u^{n+1}, which
+// are the neighbours' edge cells after step one: the warp recomputes them
+// with upd2d from the neighbours' two outermost columns / rows of u^n and the
+// diagonal neighbour's corner cell.  Every value is formed by the same
+// operation on the same inputs as in two separate steps (the halo exchange
+// of a same-level neighbour is a copy), so the result is bit-identical.
+//
+// Lanes 0..N-1 own ghost-column row i = lane, lanes N..2N-1 ghost-row column
+// j = lane - N; each holds the ghost cell of u^n (v1) and the cell one
+// further upwind (v2).  Lane 0 also holds the corner (i_g, j_g).  Metadata
+// pipeline as in step2d_body, with the diagonal's index one patch ahead and
+// the corner value loaded before the tile wait.
+template <typename T, int N, int H, int S>
+__device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __restrict__ out,
+                                                 const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
+                                                 const Coef* __restrict__ coefA, const float2* __restrict__ coef32A,
+                                                 const Coef* __restrict__ coefB, const float2* __restrict__ coef32B,
+                                                 int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
+                                                 const int32_t* __restrict__ upcode, T* tiles, uint64_t* bars, int p,
+                                                 int nwarp)
+{
+    using Sh                = Step2dShape<T, N, H>;
+    constexpr int      P1   = Sh::P1;
+    constexpr int      FLAT = Sh::FLAT;
+    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
+    constexpr int      SEG  = Sh::SEG;
+    const int          lane = threadIdx.x & 31;
+    if (lane == 0) {
+        for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const char* in_bytes = reinterpret_cast<const char*>(in);
+    auto        request  = [&](int q, int slot) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[slot], BYTES);
+        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
+                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
+    };
+    if (lane == 0)
+        for (int j = 0; j < S - 1; ++j)
+            if (p + j * nwarp < P) request(p + j * nwarp, j);
+    uint32_t  phase = 0;
+    const int cl = lane % N + H, r0 = (lane / N) * SEG + H;
+    const int nl = g.depth + 1;
+    const bool col = lane < N;
+    const bool job = lane < 2 * N;
+    const int  L   = col ? 1 : 0;
+    const int  tg  = (col ? lane : lane - N) + H; // tangential padded coordinate of the lane's ghost
+
+    struct Side {
+        int      ux, uy;
+        Coef2<T> a, b; // coefficient rows of the two steps
+    };
+    struct Rec {
+        int nb;   // same-level neighbour across the lane's ghost face
+        int diag; // lane 0: the x-neighbour's y-neighbour (one patch ahead)
+    };
+    auto row_of = [&](const Coef* cf, const float2* cf32, int row, Coef2<T>& c) {
+        if constexpr (sizeof(T) == 4) {
+            const float2 v = cf32[row];
+            c.cx           = v.x;
+            c.cy           = v.y;
+        } else {
+            const Coef& v = cf[row];
+            c.c0          = v.c0;
+            c.cx          = v.c[0];
+            c.cy          = v.c[1];
+        }
+    };
+    auto side_of = [&](uint64_t key, Side& sd) {
+        const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+        sd.ux          = upx0;
+        sd.uy          = upy0;
+        if (upcode) {
+            const int32_t code = upcode[inst];
+            sd.ux              = unpack_upwind(code, 0);
+            sd.uy              = unpack_upwind(code, 1);
+        }
+        const int row = inst * nl + key_level(key);
+        row_of(coefA, coef32A, row, sd.a);
+        row_of(coefB, coef32B, row, sd.b);
+    };
+    auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
+    auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
+    // neighbour index of a face record, the patch itself when the record is
+    // not same-level (never for the trees this kernel is chosen for; the
+    // error flag reports it)
+    auto same_nb = [&](const amr_halo_meta* rp, int self) {
+        if (rp->relation != REL_SAME) {
+            atomicExch(err, static_cast<int32_t>(AMR_ERR_UNBALANCED));
+            return self;
+        }
+        return rp->neighbor;
+    };
+    auto rec_of = [&](int q, const Side& sd, Rec& m) {
+        m.nb   = q;
+        m.diag = q;
+        if (has_job(sd)) m.nb = same_nb(meta + static_cast<size_t>(q) * 4 + 2 * L + pos_of(sd), q);
+    };
+    // one patch ahead: the lane's two ghost sources (u^n) and lane 0's
+    // diagonal index
+    auto fetch = [&](const Side& sd, Rec& m, T& v1, T& v2) {
+        v1 = v2 = T(0);
+        if (!has_job(sd)) return;
+        const int pos = pos_of(sd);
+        const int e1  = pos ? H : N + H - 1;      // the neighbour's edge line
+        const int e2  = pos ? H + 1 : N + H - 2;  // the line behind it
+        const T*  nbp = in + static_cast<size_t>(m.nb) * FLAT;
+        if (col) {
+            v1 = nbp[tg * P1 + e1];
+            v2 = nbp[tg * P1 + e2];
+        } else {
+            v1 = nbp[e1 * P1 + tg];
+            v2 = nbp[e2 * P1 + tg];
+        }
+        if (lane == 0 && sd.uy != 0)
+            m.diag = same_nb(meta + static_cast<size_t>(m.nb) * 4 + 0 + (sd.uy > 0 ? 1 : 0), m.nb);
+    };
+
+    const int q1 = p + nwarp, q2 = p + 2 * nwarp;
+    Side      sd0{}, sd1{}, sd2{};
+    Rec       m0{}, m1{}, m2{};
+    T         a1 = T(0), a2 = T(0), b1 = T(0), b2 = T(0); // ghost sources of this patch (a) and the next (b)
+    uint64_t  k2 = 0;
+    if (p < P) {
+        side_of(keys[p], sd0);
+        rec_of(p, sd0, m0);
+        fetch(sd0, m0, a1, a2);
+    }
+    if (q1 < P) {
+        side_of(keys[q1], sd1);
+        rec_of(q1, sd1, m1);
+    }
+    if (q2 < P) k2 = keys[q2];
+
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int b  = it % S;
+        const int pf = p + (S - 1) * nwarp;
+        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
+        const int pa = p + nwarp, pb = p + 2 * nwarp, pc = p + 3 * nwarp;
+        uint64_t  k3 = 0;
+        if (pc < P) k3 = keys[pc];
+        if (pb < P) {
+            side_of(k2, sd2);
+            rec_of(pb, sd2, m2);
+        }
+        if (pa < P) fetch(sd1, m1, b1, b2);
+        // this patch: the corner cell (the diagonal's) for lane 0
+        const int ux = sd0.ux, uy = sd0.uy;
+        const int igp = uy > 0 ? N + H : H - 1, jgp = ux > 0 ? N + H : H - 1; // ghost row / column (padded)
+        T         corner = T(0);
+        if (lane == 0 && ux != 0 && uy != 0)
+            corner = in[static_cast<size_t>(m0.diag) * FLAT + (uy > 0 ? H : N + H - 1) * P1 + (ux > 0 ? H : N + H - 1)];
+        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
+            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
+            phase ^= 1u << b;
+            for (int j = 1; j < S; ++j)
+                if (p + j * nwarp < P) {
+                    const int sl = (it + j) % S;
+                    mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u);
+                    phase ^= 1u << sl;
+                }
+            return;
+        }
+        phase ^= 1u << b;
+        T*         tile = tiles + static_cast<size_t>(b) * FLAT;
+        const bool has  = has_job(sd0);
+        const int  G0 = col ? tg : igp, G1 = col ? jgp : tg; // the lane's ghost cell (padded)
+        if (has) tile[G0 * P1 + G1] = a1;                     // u^n ghosts
+        __syncwarp();
+        // step one: interior cells (registers) ...
+        T colv[SEG + 2];
+#pragma unroll
+        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+        T res[SEG];
+#pragma unroll
+        for (int k = 0; k < SEG; ++k)
+            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.a, ux, uy);
+        // ... and the ghost cells, as the neighbour computes its edge cells:
+        // column lane i needs u^n at (i, j_g + ux) = a2 and (i + uy, j_g)
+        // (the next ghost-column lane, or the corner); row lane j needs
+        // (i_g, j + ux) (the next ghost-row lane, or the corner) and
+        // (i_g + uy, j) = a2
+        const T   cornr = __shfl_sync(0xffffffffu, corner, 0);
+        const int ti    = tg - H; // tangential interior index
+        const int nt    = ti + (col ? uy : ux); // the tangential neighbour of the ghost cell
+        const int src   = (nt >= 0 && nt < N) ? (col ? nt : N + nt) : lane;
+        const T   tnb   = __shfl_sync(0xffffffffu, a1, src);
+        const T   tang  = (nt >= 0 && nt < N) ? tnb : cornr;
+        T         g1    = T(0);
+        if (has) g1 = col ? upd2d<T>(a1, a2, tang, sd0.a, ux, uy) : upd2d<T>(a1, tang, a2, sd0.a, ux, uy);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
+        if (has) tile[G0 * P1 + G1] = g1; // u^{n+1} ghosts
+        __syncwarp();
+        // step two
+#pragma unroll
+        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+#pragma unroll
+        for (int k = 0; k < SEG; ++k)
+            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.b, ux, uy);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
+        __syncwarp();
+        const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
+        uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
+        for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
+        __syncwarp();
+        sd0 = sd1;
+        m0  = m1;
+        a1  = b1;
+        a2  = b2;
         sd1 = sd2;
         m1  = m2;
         k2  = k3;
@@ -1286,6 +1519,25 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __r
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     step2d_body<T, N, H, S>(in, out, meta, P, g, coef, coef32, upx0, upy0, err, keys, upcode, tiles, bars, p, nwarp);
+}
+
+// Host-driven launch of two steps per pass (coefficient rows of the two steps
+// in coefA/coef32A and coefB/coef32B).
+template <typename T, int N, int H, int W, int S>
+__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
+k_step2d_pair(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
+              const Coef* __restrict__ coefA, const float2* __restrict__ coef32A, const Coef* __restrict__ coefB,
+              const float2* __restrict__ coef32B, int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
+              const int32_t* __restrict__ upcode)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    step2d_pair_body<T, N, H, S>(in, out, meta, P, g, coefA, coef32A, coefB, coef32B, upx0, upy0, err, keys, upcode,
+                                 tiles, bars, p, nwarp);
 }
 
 } // namespace amr_gb300

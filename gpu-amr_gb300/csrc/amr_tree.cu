@@ -104,12 +104,14 @@ namespace {
 // a fixed set of parameters.
 struct GraphKey {
     int    k = 0, crit = 0, min_level = 0, max_level = 0, rounds = 0, bounds = 0, vel = 0, W = 0, S = 0, grid = 0;
+    int    pair = 0; // two steps per pass (same-level trees)
     int    up[3] = { 0, 0, 0 };
     double rthr = 0.0, cthr = 0.0, cfl = 0.0;
     bool   operator==(const GraphKey& o) const
     {
         return k == o.k && crit == o.crit && min_level == o.min_level && max_level == o.max_level &&
                rounds == o.rounds && bounds == o.bounds && vel == o.vel && W == o.W && S == o.S && grid == o.grid &&
+               pair == o.pair &&
                up[0] == o.up[0] && up[1] == o.up[1] && up[2] == o.up[2] && std::memcmp(&rthr, &o.rthr, 8) == 0 &&
                std::memcmp(&cthr, &o.cthr, 8) == 0 && std::memcmp(&cfl, &o.cfl, 8) == 0;
     }
@@ -139,6 +141,7 @@ struct amr_tree {
     size_t       size     = 0;
     int          max_level_host = 0;
     bool         ghosts_valid   = false;
+    bool         uniform        = true; // every neighbour relation is "same level" (two-step passes apply)
 
     void*          sbuf[2]{};   // the two state buffers (fixed addresses)
     void*          cur = nullptr; // one of sbuf
@@ -242,6 +245,10 @@ cudaError_t prepare_step2d()
     cudaError_t e    = cudaFuncSetAttribute(k_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_run_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_step2d_pair<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_run_step2d_pair<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess) done.fetch_or(bit);
     return e;
 }
@@ -295,6 +302,23 @@ amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, 
         k_step2d<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
             in, out, meta, P, g, coef, coef32, up[0], up[1], err, keys, upcode);
         AMR_LAUNCHED("k_step2d");
+        return AMR_OK;
+    });
+}
+
+// Two steps per pass (same-level trees): coefficient rows of the two steps.
+template <typename T, int N, int H>
+amr_status launch_step2d_pair(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coefA,
+                              const float2* coef32A, const Coef* coefB, const float2* coef32B, const int* up,
+                              int32_t* err, const uint64_t* keys, const int32_t* upcode, const StepCfg& cfg,
+                              cudaStream_t s)
+{
+    return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
+        AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
+        k_step2d_pair<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
+            in, out, meta, P, g, coefA, coef32A, coefB, coef32B, up[0], up[1], err, keys, upcode);
+        AMR_LAUNCHED("k_step2d_pair");
         return AMR_OK;
     });
 }
@@ -522,7 +546,24 @@ amr_status init_root(amr_tree* t)
     t->max_level_host = 0;
     t->ghosts_valid   = true;
     t->batch_open     = false;
+    t->uniform        = true; // roots are their own same-level neighbours
     ++t->topo;
+    return AMR_OK;
+}
+
+// Whether every neighbour record of the current tree is "same level" (the
+// condition for two-step passes), read back into t->uniform.
+amr_status refresh_uniform(amr_tree* t)
+{
+    int32_t*        hs = static_cast<int32_t*>(t->pinned);
+    const long long n  = static_cast<long long>(t->size) * t->g.ndir;
+    AMR_CUDA(cudaMemsetAsync(t->status + 5, 0, sizeof(int32_t), t->stream));
+    k_any_not_same<<<std::min<unsigned>(grid_for(n, 256), 1024u), 256, 0, t->stream>>>(t->meta[t->tb], n,
+                                                                                          t->status + 5);
+    AMR_LAUNCHED("k_any_not_same");
+    AMR_CUDA(cudaMemcpyAsync(hs + 8, t->status + 5, sizeof(int32_t), cudaMemcpyDeviceToHost, t->stream));
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    t->uniform = hs[8] == 0;
     return AMR_OK;
 }
 
@@ -695,6 +736,21 @@ amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const 
     });
 }
 
+template <typename T, int N, int H>
+amr_status launch_run_step2d_pair(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coefA,
+                                  const float2* coef32A, const Coef* coefB, const float2* coef32B, int parity,
+                                  const int* up, const StepCfg& cfg, int P, cudaStream_t s)
+{
+    return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
+        AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
+        k_run_step2d_pair<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
+            B, ctl, g, coefA, coef32A, coefB, coef32B, parity, up[0], up[1]);
+        AMR_LAUNCHED("k_run_step2d_pair");
+        return AMR_OK;
+    });
+}
+
 // The launch sequence of one interval on stream cs (captured into a graph).
 // Grids are fixed; every kernel takes the leaf count from the control block.
 template <typename T>
@@ -703,26 +759,46 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     const Geo& g   = t->g;
     const int  K   = t->ninst, nl = g.depth + 1, sms = num_sms();
     RunCtl*    ctl = t->ctl;
+    if (key.pair) { // the interval runs only while the tree is same-level
+        k_run_require_uniform<<<1, 32, 0, cs>>>(ctl);
+        AMR_LAUNCHED("k_run_require_uniform");
+    }
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
-                                     t->coef, t->coef32, t->upcode);
+                                     t->coef, t->coef32, t->upcode, key.pair ? &ctl->err : nullptr);
     AMR_LAUNCHED("k_batch_begin");
     const StepCfg cfg{ key.W, key.S, key.grid };
     const int     ppb = std::max(1, 256 / g.cells);
-    for (int j = 0; j < key.k; ++j) {
+    // two-step passes: pass j covers steps 2j and 2j+1, an odd last step
+    // runs alone; the buffers alternate per pass
+    const int passes = key.pair ? key.k / 2 : 0;
+    for (int j = 0; j < passes; ++j) {
+        const Coef*   cf  = t->coef + static_cast<size_t>(2 * j) * K * nl;
+        const float2* cf2 = t->coef32 + static_cast<size_t>(2 * j) * K * nl;
+        const Coef*   cfb = cf + static_cast<size_t>(K) * nl;
+        const float2* c2b = cf2 + static_cast<size_t>(K) * nl;
+        amr_status    st  = g.n == 16 ? launch_run_step2d_pair<T, 16, 1>(B, ctl, g, cf, cf2, cfb, c2b, j & 1, key.up, cfg,
+                                                                          static_cast<int>(t->cap), cs)
+                                      : launch_run_step2d_pair<T, 8, 1>(B, ctl, g, cf, cf2, cfb, c2b, j & 1, key.up, cfg,
+                                                                         static_cast<int>(t->cap), cs);
+        if (st != AMR_OK) return st;
+    }
+    for (int j = 2 * passes; j < key.k; ++j) {
+        const int par = key.pair ? (passes & 1) : (j & 1);
         const Coef*   cf  = t->coef + static_cast<size_t>(j) * K * nl;
         const float2* cf2 = t->coef32 + static_cast<size_t>(j) * K * nl;
         amr_status    st  = AMR_OK;
         if (key.W > 0 && g.n == 16)
-            st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+            st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
         else if (key.W > 0)
-            st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, j & 1, key.up, cfg, static_cast<int>(t->cap), cs);
+            st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
         else {
-            k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, j & 1, key.up[0], key.up[1], key.up[2], ppb);
+            k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, par, key.up[0], key.up[1], key.up[2], ppb);
             AMR_LAUNCHED("k_run_step");
         }
         if (st != AMR_OK) return st;
     }
-    const int sp = key.k & 1;
+    // parity of the buffer holding the interval's result
+    const int sp = key.pair ? ((passes + (key.k & 1)) & 1) : (key.k & 1);
     if (key.crit != 0) {
         if (key.crit == 1 && g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8)) {
             const GradRule rule = make_grad_rule(key.rthr, key.cthr);
@@ -858,6 +934,7 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     c.max_level  = t->max_level_host;
     c.leaves_min = INT_MAX;
     c.leaves_max = 0;
+    c.uniform    = t->uniform ? 1 : 0;
     RunCtl* hc   = reinterpret_cast<RunCtl*>(static_cast<char*>(t->pinned) + 64);
     *hc          = c;
     AMR_CUDA(cudaMemcpyAsync(t->ctl, hc, sizeof(RunCtl), cudaMemcpyHostToDevice, s));
@@ -921,13 +998,17 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     const long long rem   = (nfull < max_intervals) ? left % k : 0;
     cudaGraphExec_t full = nullptr, tail = nullptr;
     uint64_t        nk_full = 0, nk_tail = 0;
+    // same-level trees: two steps per pass, guarded on the device
+    const bool pairs = step2d && t->uniform && key.W > 0;
     if (nfull > 0) {
         key.k         = static_cast<int>(k);
+        key.pair      = pairs && k >= 2 ? 1 : 0;
         amr_status st = interval_graph(t, key, B, &full, &nk_full);
         if (st != AMR_OK) return st;
     }
     if (rem > 0) {
         key.k         = static_cast<int>(rem);
+        key.pair      = pairs && rem >= 2 ? 1 : 0;
         amr_status st = interval_graph(t, key, B, &tail, &nk_tail);
         if (st != AMR_OK) return st;
     }
@@ -955,6 +1036,12 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     t->max_level_host = r.max_level;
     t->ghosts_valid   = false;
     t->batch_open     = true;
+    t->uniform        = r.uniform != 0;
+    // an interval guarded for two-step passes found the tree non-uniform:
+    // it and the rest of the chunk did not run (no state, time or statistic
+    // changed); the caller continues with one-step intervals
+    const bool retry = r.err == kRetryUniform;
+    if (retry) t->uniform = false;
     // time of each instance = its batch totals + the open batch
     double   tmax = 0.0;
     uint32_t cmax = 0;
@@ -969,7 +1056,8 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         if (i == 0 || ti > tmax) tmax = ti;
         cmax = std::max(cmax, ca + cb);
     }
-    tot.done += nfull * k + rem;
+    const long long ran = static_cast<long long>(r.intervals); // intervals committed in this chunk
+    tot.done += ran <= nfull ? ran * k : nfull * k + rem;
     if (K == 1) { // the totals were carried in
         tot.sum_dt   = tmax;
         tot.executed = cmax;
@@ -986,7 +1074,7 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         tot.lmin = std::min<uint64_t>(tot.lmin, static_cast<uint64_t>(r.leaves_min));
         tot.lmax = std::max<uint64_t>(tot.lmax, static_cast<uint64_t>(r.leaves_max));
     }
-    if (r.err) {
+    if (r.err && !retry) {
         const char* what = r.err == AMR_ERR_CAPACITY     ? "re-mesh would exceed the tree capacity"
                            : r.err == AMR_ERR_UNBALANCED ? "neighbour rebuild found a non-2:1 face"
                            : r.err == AMR_ERR_TIMEOUT    ? "a bulk copy did not complete within the wait limit"
@@ -1478,6 +1566,11 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     k_neighbors<<<grid_for(static_cast<long long>(NP) * g.ndir, 128), 128, 0, s>>>(t->keys[nb], NP, g, t->meta[nb],
                                                                                   t->status);
     AMR_LAUNCHED("k_neighbors");
+    AMR_CUDA(cudaMemsetAsync(t->status + 5, 0, sizeof(int32_t), s));
+    k_any_not_same<<<std::min<unsigned>(grid_for(static_cast<long long>(NP) * g.ndir, 256), 1024u), 256, 0, s>>>(
+        t->meta[nb], static_cast<long long>(NP) * g.ndir, t->status + 5);
+    AMR_LAUNCHED("k_any_not_same");
+    AMR_CUDA(cudaMemcpyAsync(hs + 8, t->status + 5, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaMemcpyAsync(hs + 4, t->status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaMemcpyAsync(hs + 5, t->maxlev, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     AMR_CUDA(cudaStreamSynchronize(s));
@@ -1488,6 +1581,7 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     t->size           = static_cast<size_t>(NP);
     t->max_level_host = hs[5];
     t->ghosts_valid   = false;
+    t->uniform        = hs[8] == 0;
     if (changed) *changed = 1;
     if (t->ninst > 1) {
         int m = 0;
@@ -1549,7 +1643,10 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                                         remaining, t->dts(), t->step_dt, t->coef, t->coef32, t->upcode);
         AMR_LAUNCHED("k_batch_begin");
         first = false;
-        for (int k = 0; k < chunk; ++k) {
+        const bool shape2d = t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8);
+        for (int k = 0; k < chunk;) {
+            // two steps per pass where every relation is same-level
+            const bool pair = shape2d && t->uniform && k + 1 < chunk;
             std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
             if (t->timing) {
                 if (t->events_used == t->events.size()) {
@@ -1560,7 +1657,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                     t->event_cells.push_back(0);
                 }
                 ev = &t->events[t->events_used];
-                t->event_cells[t->events_used] = static_cast<uint64_t>(P) * t->g.cells;
+                t->event_cells[t->events_used] = static_cast<uint64_t>(P) * t->g.cells * (pair ? 2 : 1);
                 ++t->events_used;
                 AMR_CUDA(cudaEventRecord(ev->first, s));
             }
@@ -1570,6 +1667,15 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                 const float2* cf2 = t->coef32 + static_cast<size_t>(k) * K * nl;
                 const T*      in  = static_cast<const T*>(t->cur);
                 T*            out = static_cast<T*>(t->nxt);
+                if (pair) {
+                    const Coef*   cfb  = cf + static_cast<size_t>(K) * nl;
+                    const float2* cf2b = cf2 + static_cast<size_t>(K) * nl;
+                    if (t->g.n == 16)
+                        return launch_step2d_pair<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
+                                                            t->status + 7, t->keys[t->tb], uleaf, cfg, s);
+                    return launch_step2d_pair<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
+                                                       t->status + 7, t->keys[t->tb], uleaf, StepCfg{}, s);
+                }
                 if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
                     return launch_step2d<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
                                                    t->keys[t->tb], uleaf, cfg, s);
@@ -1585,6 +1691,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
             if (st != AMR_OK) return st;
             if (ev) AMR_CUDA(cudaEventRecord(ev->second, s));
             std::swap(t->cur, t->nxt);
+            k += pair ? 2 : 1;
         }
         done += chunk;
         if (steps == 0) break;
@@ -1612,6 +1719,8 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
     std::memcpy(&wait_err, hp + 48, sizeof wait_err);
     if (wait_err != 0) {
         AMR_CUDA(cudaMemsetAsync(t->status + 7, 0, sizeof(int32_t), t->stream));
+        if (wait_err != AMR_ERR_TIMEOUT)
+            return fail(static_cast<amr_status>(wait_err), "a two-step pass met a neighbour of another level");
         return fail(AMR_ERR_TIMEOUT, "a bulk copy did not complete within the wait limit");
     }
     // one tree: its time; a forest: the instance furthest ahead
@@ -1734,6 +1843,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             if (cs.cur) std::swap(t->cur, t->nxt);
             t->max_level_host = cs.max_level;
             t->ghosts_valid   = false;
+            if (amr_status us = refresh_uniform(t); us != AMR_OK) return us;
             tot.done += static_cast<long long>(cs.executed);
             tot.sum_dt += cs.sum_dt;
             tot.executed += cs.executed;
