@@ -184,6 +184,13 @@ struct amr_tree {
     double*   dt_tot = nullptr;
     uint32_t* dt_ctot = nullptr;
     DtState   dts() const { return DtState{ dt_acc, dt_rem, dt_cnt, dt_tot, dt_ctot }; }
+    double*   dt_scratch = nullptr; // time bookkeeping of the autotuner's prologue (5 x instances)
+    DtState   scratch_dts() const
+    {
+        const int K = ninst;
+        return DtState{ dt_scratch, dt_scratch + K, reinterpret_cast<uint32_t*>(dt_scratch + 2 * K), dt_scratch + 3 * K,
+                        reinterpret_cast<uint32_t*>(dt_scratch + 4 * K) };
+    }
     double*   step_dt = nullptr;
     Coef*     coef    = nullptr;
     float2*   coef32  = nullptr; // (c_x, c_y) rows of the FP32 2D update
@@ -329,39 +336,42 @@ amr_status launch_step2d_pair(const T* in, T* out, const amr_halo_meta* meta, in
 // buffer, which the following step overwrites).  Results are cached per
 // device, dtype, patch shape and leaf-count octave.
 struct TuneKey {
-    int dev, esize, n, h, octave, per_leaf;
+    int dev, esize, n, h, octave, per_leaf, pair;
     bool operator<(const TuneKey& o) const
     {
-        return std::tie(dev, esize, n, h, octave, per_leaf) < std::tie(o.dev, o.esize, o.n, o.h, o.octave, o.per_leaf);
+        return std::tie(dev, esize, n, h, octave, per_leaf, pair) <
+               std::tie(o.dev, o.esize, o.n, o.h, o.octave, o.per_leaf, o.pair);
     }
 };
 std::mutex                 g_tune_mu;
 std::map<TuneKey, StepCfg> g_tuned;
 std::atomic<int>           g_tune_mode{ 1 }; // 0 off (defaults), 1 on
 
-TuneKey tune_key(const amr_tree* t, bool per_leaf)
+TuneKey tune_key(const amr_tree* t, bool per_leaf, bool pair)
 {
     int dev = 0;
     cudaGetDevice(&dev);
     int oct = 0;
     while ((static_cast<size_t>(1) << oct) < t->size) ++oct;
-    return TuneKey{ dev, static_cast<int>(t->esize), t->g.n, t->g.h, oct, per_leaf ? 1 : 0 };
+    return TuneKey{ dev, static_cast<int>(t->esize), t->g.n, t->g.h, oct, per_leaf ? 1 : 0, pair ? 1 : 0 };
 }
 
-bool lookup_tuned(const amr_tree* t, bool per_leaf, StepCfg& cfg)
+bool lookup_tuned(const amr_tree* t, bool per_leaf, bool pair, StepCfg& cfg)
 {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto                        it = g_tuned.find(tune_key(t, per_leaf));
+    auto                        it = g_tuned.find(tune_key(t, per_leaf, pair));
     if (it == g_tuned.end()) return false;
     cfg = it->second;
     return true;
 }
 
+// pair: time the two-step pass instead (same-level trees); both passes read
+// the prologue's coefficient row.
 template <typename T, int N, int H>
 amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, const int* up, const int32_t* upcode,
-                       StepCfg& best)
+                       StepCfg& best, bool pair = false)
 {
-    const TuneKey key = tune_key(t, upcode != nullptr);
+    const TuneKey key = tune_key(t, upcode != nullptr, pair);
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto                        it = g_tuned.find(key);
@@ -391,17 +401,25 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
                 const int grid = std::min(full, sms * bps);
                 StepCfg   c{ W, S, grid };
                 for (int rep = 0; rep < 2; ++rep) { // warm-up
-                    amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->meta[t->tb], P, t->g, coef, coef32, up,
-                                                          t->status + 7, t->keys[t->tb], upcode, c, s);
+                    amr_status r =
+                        pair ? launch_step2d_pair<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                           t->meta[t->tb], P, t->g, coef, coef32, coef, coef32, up,
+                                                           t->status + 7, t->keys[t->tb], upcode, c, s)
+                             : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                      t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
+                                                      t->keys[t->tb], upcode, c, s);
                     if (r != AMR_OK) return r;
                 }
                 const int reps = 4;
                 AMR_CUDA(cudaEventRecord(e0, s));
                 for (int rep = 0; rep < reps; ++rep) {
-                    amr_status r = launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                          t->meta[t->tb], P, t->g, coef, coef32, up,
-                                                          t->status + 7, t->keys[t->tb], upcode, c, s);
+                    amr_status r =
+                        pair ? launch_step2d_pair<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                           t->meta[t->tb], P, t->g, coef, coef32, coef, coef32, up,
+                                                           t->status + 7, t->keys[t->tb], upcode, c, s)
+                             : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
+                                                      t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
+                                                      t->keys[t->tb], upcode, c, s);
                     if (r != AMR_OK) return r;
                 }
                 AMR_CUDA(cudaEventRecord(e1, s));
@@ -479,6 +497,7 @@ void free_tree(amr_tree* t)
     cudaFree(t->dt_cnt);
     cudaFree(t->dt_tot);
     cudaFree(t->dt_ctot);
+    cudaFree(t->dt_scratch);
     cudaFree(t->step_dt);
     cudaFree(t->coef);
     cudaFree(t->coef32);
@@ -764,7 +783,7 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         AMR_LAUNCHED("k_run_require_uniform");
     }
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
-                                     t->coef, t->coef32, t->upcode, key.pair ? &ctl->err : nullptr);
+                                     t->coef, t->coef32, t->upcode, &ctl->err); // nothing after an error
     AMR_LAUNCHED("k_batch_begin");
     const StepCfg cfg{ key.W, key.S, key.grid };
     const int     ppb = std::max(1, 256 / g.cells);
@@ -963,13 +982,15 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         StepCfg cfg;
         if (g.n == 16) {
             // tune on the current leaves with a coefficient table of this run
-            k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, g, t->vel, p->cfl, 1, BATCH_RESET, 1.0, t->dts(), t->step_dt,
-                                            t->coef, t->coef32, t->upcode);
+            // (its own time bookkeeping: the run's totals stay as they are)
+            k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, g, t->vel, p->cfl, 1, BATCH_RESET, 1.0, t->scratch_dts(),
+                                            t->step_dt, t->coef, t->coef32, t->upcode);
             AMR_LAUNCHED("k_batch_begin");
             int up[3] = { key.up[0], key.up[1], key.up[2] };
             amr_status ts = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
                 using T = decltype(z);
-                return tune_step2d<T, 16, 1>(t, t->coef, t->coef32, up, per_leaf ? t->upcode : nullptr, cfg);
+                return tune_step2d<T, 16, 1>(t, t->coef, t->coef32, up, per_leaf ? t->upcode : nullptr, cfg,
+                                             t->uniform);
             });
             if (ts != AMR_OK) return ts;
         }
@@ -988,11 +1009,15 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         });
         if (ps != AMR_OK) return ps;
     }
-    // per-instance time: the run's totals so far carried in (one tree)
-    k_run_dt_init<<<grid_for(K, 256), 256, 0, s>>>(t->dts(), K, p->remaining_time - tot.sum_dt,
-                                                    K == 1 ? tot.sum_dt : 0.0,
-                                                    K == 1 ? static_cast<uint32_t>(tot.executed) : 0u);
-    AMR_LAUNCHED("k_run_dt_init");
+    // per-instance time: one tree carries the run's totals in from the host;
+    // a forest starts them at the run's first interval and otherwise keeps
+    // its per-instance totals on the device (the next interval folds them)
+    if (K == 1 || tot.intervals == 0) {
+        k_run_dt_init<<<grid_for(K, 256), 256, 0, s>>>(t->dts(), K, p->remaining_time - tot.sum_dt,
+                                                        K == 1 ? tot.sum_dt : 0.0,
+                                                        K == 1 ? static_cast<uint32_t>(tot.executed) : 0u);
+        AMR_LAUNCHED("k_run_dt_init");
+    }
     const long long left  = total - tot.done;
     long long       nfull = std::min(left / k, max_intervals);
     const long long rem   = (nfull < max_intervals) ? left % k : 0;
@@ -1058,13 +1083,9 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     }
     const long long ran = static_cast<long long>(r.intervals); // intervals committed in this chunk
     tot.done += ran <= nfull ? ran * k : nfull * k + rem;
-    if (K == 1) { // the totals were carried in
-        tot.sum_dt   = tmax;
-        tot.executed = cmax;
-    } else {
-        tot.sum_dt += tmax;
-        tot.executed += cmax;
-    }
+    // the device totals cover the whole run (carried in or kept on the device)
+    tot.sum_dt   = tmax;
+    tot.executed = cmax;
     tot.cells += r.cell_updates;
     tot.remeshes += r.remeshes;
     tot.intervals += r.intervals;
@@ -1191,6 +1212,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->dt_cnt), K * sizeof(uint32_t));
     al(reinterpret_cast<void**>(&t->dt_tot), K * sizeof(double));
     al(reinterpret_cast<void**>(&t->dt_ctot), K * sizeof(uint32_t));
+    al(reinterpret_cast<void**>(&t->dt_scratch), 5 * K * sizeof(double));
     al(reinterpret_cast<void**>(&t->step_dt), coef_steps * K * sizeof(double));
     al(reinterpret_cast<void**>(&t->coef), coef_steps * K * nl * sizeof(Coef));
     al(reinterpret_cast<void**>(&t->coef32), coef_steps * K * nl * sizeof(float2));
@@ -1634,9 +1656,10 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
     const int nl    = t->g.depth + 1;
     bool      first = true;
     size_t    done  = 0;
-    StepCfg   cfg;
-    lookup_tuned(t, uleaf != nullptr, cfg);
-    t->last_cfg = cfg;
+    StepCfg   cfg, cfg_pair;
+    lookup_tuned(t, uleaf != nullptr, false, cfg);
+    if (!lookup_tuned(t, uleaf != nullptr, true, cfg_pair)) cfg_pair = cfg;
+    t->last_cfg = t->uniform ? cfg_pair : cfg;
     while (done < steps || (first && steps == 0)) {
         const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
         k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? first_mode : BATCH_CONTINUE,
@@ -1672,7 +1695,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                     const float2* cf2b = cf2 + static_cast<size_t>(K) * nl;
                     if (t->g.n == 16)
                         return launch_step2d_pair<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
-                                                            t->status + 7, t->keys[t->tb], uleaf, cfg, s);
+                                                            t->status + 7, t->keys[t->tb], uleaf, cfg_pair, s);
                     return launch_step2d_pair<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
                                                        t->status + 7, t->keys[t->tb], uleaf, StepCfg{}, s);
                 }
