@@ -74,12 +74,12 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
                             coef, coef32, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars, p, nwarp);
 }
 
-// Two steps per pass (trees of same-level relations only; the interval's
+// D steps per pass (trees of same-level relations only; the interval's
 // guard has checked ctl->uniform).  parity selects the buffers of this pass.
-template <typename T, int N, int H, int W, int S>
+template <typename T, int N, int H, int W, int S, int D>
 __global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_run_step2d_pair(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coefA, const float2* __restrict__ coef32A,
-                  const Coef* __restrict__ coefB, const float2* __restrict__ coef32B, int parity, int upx0, int upy0)
+k_run_step2d_pass(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+                  size_t cstride, int parity, int upx0, int upy0)
 {
     if (ctl->err) return;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -89,12 +89,12 @@ k_run_step2d_pair(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coefA,
     const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pair_body<T, N, H, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P, g,
-                                 coefA, coef32A, coefB, coef32B, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles,
-                                 bars, p, nwarp);
+    step2d_pass_body<T, N, H, S, D>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P,
+                                    g, coef, coef32, cstride, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars,
+                                    p, nwarp);
 }
 
-// First kernel of an interval captured with two-step passes: when a re-mesh
+// First kernel of an interval captured with multi-step passes: when a re-mesh
 // has made the tree non-uniform, the interval must not run; kRetryUniform
 // stops every later kernel of the replay, and the host re-runs the interval
 // with one-step launches.

@@ -1262,37 +1262,49 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     }
 }
 
-// ------------------------------------------------ 2D update, two steps per pass
-// Two consecutive steps of a tree whose every neighbour relation is "same
+// ------------------------------------------------ 2D update, D steps per pass
+// D consecutive steps of a tree whose every neighbour relation is "same
 // level" (each instance uniform, as in the batched forests), in one pass over
-// memory: the patch is read once and written once per two steps.  Step one
-// needs the upwind ghost column and row of u^n (the neighbours' edge cells,
-// as in the one-step kernel); step two needs the same ghosts of u^{n+1}, which
-// are the neighbours' edge cells after step one: the warp recomputes them
-// with upd2d from the neighbours' two outermost columns / rows of u^n and the
-// diagonal neighbour's corner cell.  Every value is formed by the same
-// operation on the same inputs as in two separate steps (the halo exchange
-// of a same-level neighbour is a copy), so the result is bit-identical.
+// memory: the patch is read once and written once per D steps.  Step m needs
+// the upwind ghost column and row of u^{m-1}, which are the neighbours' edge
+// cells after m-1 steps.  The warp recomputes them with upd2d from u^n: the
+// neighbours' D outermost columns / rows (the strips) and the D(D-1)/2 cells
+// of the diagonal neighbour's corner that reach the patch within D steps
+// (upwind distance a in y and b in x, a, b >= 1, a + b <= D).  Each value is
+// formed by the same operation on the same inputs as in D separate steps (the
+// halo exchange of a same-level neighbour is a copy), so the result is
+// bit-identical.
 //
 // Lanes 0..N-1 own ghost-column row i = lane, lanes N..2N-1 ghost-row column
-// j = lane - N; each holds the ghost cell of u^n (v1) and the cell one
-// further upwind (v2).  Lane 0 also holds the corner (i_g, j_g).  Metadata
-// pipeline as in step2d_body, with the diagonal's index one patch ahead and
-// the corner value loaded before the tile wait.
-template <typename T, int N, int H, int S>
-__device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __restrict__ out,
-                                                 const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
-                                                 const Coef* __restrict__ coefA, const float2* __restrict__ coef32A,
-                                                 const Coef* __restrict__ coefB, const float2* __restrict__ coef32B,
-                                                 int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
-                                                 const int32_t* __restrict__ upcode, T* tiles, uint64_t* bars, int p,
-                                                 int nwarp)
+// j = lane - N; each holds its strip s[1..D] (s[d] = the ghost cell at upwind
+// distance d).  Lane 0 holds the corner triangle.  After step m the strips
+// and the corner advance one step on the distances still needed (d <= D-m).
+// Metadata pipeline as in step2d_body (key three patches ahead, neighbour
+// record two ahead, strips and the diagonal's index one ahead, the corner
+// before the tile wait); coefficient rows of the D steps are read at use.
+template <int D>
+__host__ __device__ constexpr int corner_index(int a, int b)
 {
+    int base = 0;
+    for (int r = 1; r < a; ++r) base += D - r;
+    return base + (b - 1);
+}
+
+template <typename T, int N, int H, int S, int D>
+__device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __restrict__ out,
+                                                 const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
+                                                 const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+                                                 size_t cstride, int upx0, int upy0, int32_t* err,
+                                                 const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode,
+                                                 T* tiles, uint64_t* bars, int p, int nwarp)
+{
+    static_assert(D >= 2 && D <= 4, "two to four steps per pass");
     using Sh                = Step2dShape<T, N, H>;
     constexpr int      P1   = Sh::P1;
     constexpr int      FLAT = Sh::FLAT;
     constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
     constexpr int      SEG  = Sh::SEG;
+    constexpr int      NC   = D * (D - 1) / 2; // corner cells
     const int          lane = threadIdx.x & 31;
     if (lane == 0) {
         for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
@@ -1309,29 +1321,28 @@ __device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __
     if (lane == 0)
         for (int j = 0; j < S - 1; ++j)
             if (p + j * nwarp < P) request(p + j * nwarp, j);
-    uint32_t  phase = 0;
-    const int cl = lane % N + H, r0 = (lane / N) * SEG + H;
-    const int nl = g.depth + 1;
+    uint32_t   phase = 0;
+    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
+    const int  nl = g.depth + 1;
     const bool col = lane < N;
     const bool job = lane < 2 * N;
     const int  L   = col ? 1 : 0;
-    const int  tg  = (col ? lane : lane - N) + H; // tangential padded coordinate of the lane's ghost
+    const int  tg  = (col ? lane : lane - N) + H; // tangential padded coordinate of the lane's strip
 
     struct Side {
-        int      ux, uy;
-        Coef2<T> a, b; // coefficient rows of the two steps
+        int ux, uy, row; // upwind offsets, coefficient row (instance, level)
     };
     struct Rec {
         int nb;   // same-level neighbour across the lane's ghost face
         int diag; // lane 0: the x-neighbour's y-neighbour (one patch ahead)
     };
-    auto row_of = [&](const Coef* cf, const float2* cf32, int row, Coef2<T>& c) {
+    auto coef_of = [&](int step, int row, Coef2<T>& c) {
         if constexpr (sizeof(T) == 4) {
-            const float2 v = cf32[row];
+            const float2 v = coef32[step * cstride + row];
             c.cx           = v.x;
             c.cy           = v.y;
         } else {
-            const Coef& v = cf[row];
+            const Coef& v = coef[step * cstride + row];
             c.c0          = v.c0;
             c.cx          = v.c[0];
             c.cy          = v.c[1];
@@ -1346,15 +1357,12 @@ __device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __
             sd.ux              = unpack_upwind(code, 0);
             sd.uy              = unpack_upwind(code, 1);
         }
-        const int row = inst * nl + key_level(key);
-        row_of(coefA, coef32A, row, sd.a);
-        row_of(coefB, coef32B, row, sd.b);
+        sd.row = inst * nl + key_level(key);
     };
     auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
     auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
-    // neighbour index of a face record, the patch itself when the record is
-    // not same-level (never for the trees this kernel is chosen for; the
-    // error flag reports it)
+    // neighbour index of a face record; the patch itself (and the error
+    // flag) when the record is not same-level, which the host rules out
     auto same_nb = [&](const amr_halo_meta* rp, int self) {
         if (rp->relation != REL_SAME) {
             atomicExch(err, static_cast<int32_t>(AMR_ERR_UNBALANCED));
@@ -1367,35 +1375,34 @@ __device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __
         m.diag = q;
         if (has_job(sd)) m.nb = same_nb(meta + static_cast<size_t>(q) * 4 + 2 * L + pos_of(sd), q);
     };
-    // one patch ahead: the lane's two ghost sources (u^n) and lane 0's
+    // one patch ahead: the lane's strip (u^n at distances 1..D) and lane 0's
     // diagonal index
-    auto fetch = [&](const Side& sd, Rec& m, T& v1, T& v2) {
-        v1 = v2 = T(0);
+    auto fetch = [&](const Side& sd, Rec& m, T* v) {
+#pragma unroll
+        for (int d = 1; d <= D; ++d) v[d] = T(0);
         if (!has_job(sd)) return;
         const int pos = pos_of(sd);
-        const int e1  = pos ? H : N + H - 1;      // the neighbour's edge line
-        const int e2  = pos ? H + 1 : N + H - 2;  // the line behind it
         const T*  nbp = in + static_cast<size_t>(m.nb) * FLAT;
-        if (col) {
-            v1 = nbp[tg * P1 + e1];
-            v2 = nbp[tg * P1 + e2];
-        } else {
-            v1 = nbp[e1 * P1 + tg];
-            v2 = nbp[e2 * P1 + tg];
+#pragma unroll
+        for (int d = 1; d <= D; ++d) {
+            const int line = pos ? H + d - 1 : N + H - d; // the neighbour's line at distance d
+            v[d]           = nbp[col ? tg * P1 + line : line * P1 + tg];
         }
         if (lane == 0 && sd.uy != 0)
-            m.diag = same_nb(meta + static_cast<size_t>(m.nb) * 4 + 0 + (sd.uy > 0 ? 1 : 0), m.nb);
+            m.diag = same_nb(meta + static_cast<size_t>(m.nb) * 4 + (sd.uy > 0 ? 1 : 0), m.nb);
     };
 
     const int q1 = p + nwarp, q2 = p + 2 * nwarp;
     Side      sd0{}, sd1{}, sd2{};
     Rec       m0{}, m1{}, m2{};
-    T         a1 = T(0), a2 = T(0), b1 = T(0), b2 = T(0); // ghost sources of this patch (a) and the next (b)
+    T         sa[D + 1], sb[D + 1]; // strips of this patch and the next
     uint64_t  k2 = 0;
+#pragma unroll
+    for (int d = 0; d <= D; ++d) sa[d] = sb[d] = T(0);
     if (p < P) {
         side_of(keys[p], sd0);
         rec_of(p, sd0, m0);
-        fetch(sd0, m0, a1, a2);
+        fetch(sd0, m0, sa);
     }
     if (q1 < P) {
         side_of(keys[q1], sd1);
@@ -1414,13 +1421,24 @@ __device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __
             side_of(k2, sd2);
             rec_of(pb, sd2, m2);
         }
-        if (pa < P) fetch(sd1, m1, b1, b2);
-        // this patch: the corner cell (the diagonal's) for lane 0
+        if (pa < P) fetch(sd1, m1, sb);
+        // this patch
         const int ux = sd0.ux, uy = sd0.uy;
-        const int igp = uy > 0 ? N + H : H - 1, jgp = ux > 0 ? N + H : H - 1; // ghost row / column (padded)
-        T         corner = T(0);
-        if (lane == 0 && ux != 0 && uy != 0)
-            corner = in[static_cast<size_t>(m0.diag) * FLAT + (uy > 0 ? H : N + H - 1) * P1 + (ux > 0 ? H : N + H - 1)];
+        const int igp = uy > 0 ? N + H : H - 1, jgp = ux > 0 ? N + H : H - 1; // distance-1 ghost row / column
+        T         cn[NC > 0 ? NC : 1];
+#pragma unroll
+        for (int c = 0; c < (NC > 0 ? NC : 1); ++c) cn[c] = T(0);
+        if (lane == 0 && ux != 0 && uy != 0) {
+            const T* dg = in + static_cast<size_t>(m0.diag) * FLAT;
+#pragma unroll
+            for (int a = 1; a < D; ++a)
+#pragma unroll
+                for (int bb = 1; a + bb <= D; ++bb)
+                    cn[corner_index<D>(a, bb)] = dg[(uy > 0 ? H + a - 1 : N + H - a) * P1 + (ux > 0 ? H + bb - 1 : N + H - bb)];
+        }
+        Coef2<T> cf[D];
+#pragma unroll
+        for (int m = 0; m < D; ++m) coef_of(m, sd0.row, cf[m]);
         if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
             if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
             phase ^= 1u << b;
@@ -1435,53 +1453,70 @@ __device__ __forceinline__ void step2d_pair_body(const T* __restrict__ in, T* __
         phase ^= 1u << b;
         T*         tile = tiles + static_cast<size_t>(b) * FLAT;
         const bool has  = has_job(sd0);
-        const int  G0 = col ? tg : igp, G1 = col ? jgp : tg; // the lane's ghost cell (padded)
-        if (has) tile[G0 * P1 + G1] = a1;                     // u^n ghosts
-        __syncwarp();
-        // step one: interior cells (registers) ...
-        T colv[SEG + 2];
+        const int  G0 = col ? tg : igp, G1 = col ? jgp : tg; // the lane's distance-1 ghost cell
+        // tangential neighbour of the lane's strip cells: the next strip lane,
+        // or (past the patch edge) the corner
+        const int  ti  = tg - H;
+        const int  nt  = ti + (col ? uy : ux);
+        const bool inr = nt >= 0 && nt < N;
+        const int  src = inr ? (col ? nt : N + nt) : lane;
 #pragma unroll
-        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
-        T res[SEG];
+        for (int m = 1; m <= D; ++m) {
+            if (has) tile[G0 * P1 + G1] = sa[1]; // u^{m-1} ghosts
+            __syncwarp();
+            T colv[SEG + 2];
 #pragma unroll
-        for (int k = 0; k < SEG; ++k)
-            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.a, ux, uy);
-        // ... and the ghost cells, as the neighbour computes its edge cells:
-        // column lane i needs u^n at (i, j_g + ux) = a2 and (i + uy, j_g)
-        // (the next ghost-column lane, or the corner); row lane j needs
-        // (i_g, j + ux) (the next ghost-row lane, or the corner) and
-        // (i_g + uy, j) = a2
-        const T   cornr = __shfl_sync(0xffffffffu, corner, 0);
-        const int ti    = tg - H; // tangential interior index
-        const int nt    = ti + (col ? uy : ux); // the tangential neighbour of the ghost cell
-        const int src   = (nt >= 0 && nt < N) ? (col ? nt : N + nt) : lane;
-        const T   tnb   = __shfl_sync(0xffffffffu, a1, src);
-        const T   tang  = (nt >= 0 && nt < N) ? tnb : cornr;
-        T         g1    = T(0);
-        if (has) g1 = col ? upd2d<T>(a1, a2, tang, sd0.a, ux, uy) : upd2d<T>(a1, tang, a2, sd0.a, ux, uy);
-        __syncwarp();
+            for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+            T res[SEG];
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
-        if (has) tile[G0 * P1 + G1] = g1; // u^{n+1} ghosts
-        __syncwarp();
-        // step two
+            for (int k = 0; k < SEG; ++k)
+                res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], cf[m - 1],
+                                  ux, uy);
+            if (m < D) {
+                // strips and corner to u^m on the distances still needed
+                T tn[D], c1[D], r1[D];
 #pragma unroll
-        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+                for (int d = 1; d <= D - m; ++d) {
+                    tn[d - 1] = __shfl_sync(0xffffffffu, sa[d], src);
+                    c1[d - 1] = __shfl_sync(0xffffffffu, cn[corner_index<D>(1, d)], 0);
+                    r1[d - 1] = __shfl_sync(0xffffffffu, cn[corner_index<D>(d, 1)], 0);
+                }
 #pragma unroll
-        for (int k = 0; k < SEG; ++k)
-            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.b, ux, uy);
-        __syncwarp();
+                for (int d = 1; d <= D - m; ++d) {
+                    const T tang = inr ? tn[d - 1] : (col ? c1[d - 1] : r1[d - 1]);
+                    const T nrm  = sa[d + 1];
+                    sa[d]        = upd2d<T>(sa[d], col ? nrm : tang, col ? tang : nrm, cf[m - 1], ux, uy);
+                }
+                if (NC > 0) {
+                    T nc[NC > 0 ? NC : 1];
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
-        __syncwarp();
+                    for (int a = 1; a < D; ++a)
+#pragma unroll
+                        for (int bb = 1; a + bb <= D; ++bb)
+                            nc[corner_index<D>(a, bb)] = cn[corner_index<D>(a, bb)];
+#pragma unroll
+                    for (int a = 1; a < D; ++a)
+#pragma unroll
+                        for (int bb = 1; a + bb <= D - m; ++bb)
+                            nc[corner_index<D>(a, bb)] = upd2d<T>(cn[corner_index<D>(a, bb)], cn[corner_index<D>(a, bb + 1)],
+                                                                  cn[corner_index<D>(a + 1, bb)], cf[m - 1], ux, uy);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) cn[c] = nc[c];
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
+            __syncwarp();
+        }
         const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
         uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
         for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
         __syncwarp();
         sd0 = sd1;
         m0  = m1;
-        a1  = b1;
-        a2  = b2;
+#pragma unroll
+        for (int d = 1; d <= D; ++d) sa[d] = sb[d];
         sd1 = sd2;
         m1  = m2;
         k2  = k3;
@@ -1521,14 +1556,13 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __r
     step2d_body<T, N, H, S>(in, out, meta, P, g, coef, coef32, upx0, upy0, err, keys, upcode, tiles, bars, p, nwarp);
 }
 
-// Host-driven launch of two steps per pass (coefficient rows of the two steps
-// in coefA/coef32A and coefB/coef32B).
-template <typename T, int N, int H, int W, int S>
+// Host-driven launch of D steps per pass: coefficient rows of step m at
+// coef / coef32 + m * cstride.
+template <typename T, int N, int H, int W, int S, int D>
 __global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_step2d_pair(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
-              const Coef* __restrict__ coefA, const float2* __restrict__ coef32A, const Coef* __restrict__ coefB,
-              const float2* __restrict__ coef32B, int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
-              const int32_t* __restrict__ upcode)
+k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
+              const Coef* __restrict__ coef, const float2* __restrict__ coef32, size_t cstride, int upx0, int upy0,
+              int32_t* err, const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     T*        tiles;
@@ -1536,8 +1570,8 @@ k_step2d_pair(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta
     step2d_smem<T, N, H, W, S>(smem, tiles, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pair_body<T, N, H, S>(in, out, meta, P, g, coefA, coef32A, coefB, coef32B, upx0, upy0, err, keys, upcode,
-                                 tiles, bars, p, nwarp);
+    step2d_pass_body<T, N, H, S, D>(in, out, meta, P, g, coef, coef32, cstride, upx0, upy0, err, keys, upcode, tiles,
+                                    bars, p, nwarp);
 }
 
 } // namespace amr_gb300

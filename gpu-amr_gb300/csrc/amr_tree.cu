@@ -104,7 +104,7 @@ namespace {
 // a fixed set of parameters.
 struct GraphKey {
     int    k = 0, crit = 0, min_level = 0, max_level = 0, rounds = 0, bounds = 0, vel = 0, W = 0, S = 0, grid = 0;
-    int    pair = 0; // two steps per pass (same-level trees)
+    int    pair = 0; // several steps per pass (same-level trees)
     int    up[3] = { 0, 0, 0 };
     double rthr = 0.0, cthr = 0.0, cfl = 0.0;
     bool   operator==(const GraphKey& o) const
@@ -141,7 +141,7 @@ struct amr_tree {
     size_t       size     = 0;
     int          max_level_host = 0;
     bool         ghosts_valid   = false;
-    bool         uniform        = true; // every neighbour relation is "same level" (two-step passes apply)
+    bool         uniform        = true; // every neighbour relation is "same level" (multi-step passes apply)
 
     void*          sbuf[2]{};   // the two state buffers (fixed addresses)
     void*          cur = nullptr; // one of sbuf
@@ -252,10 +252,15 @@ cudaError_t prepare_step2d()
     cudaError_t e    = cudaFuncSetAttribute(k_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_run_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_step2d_pair<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_run_step2d_pair<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    auto pass_attr = [&]<int D>() {
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_step2d_pass<T, N, H, W, S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_run_step2d_pass<T, N, H, W, S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     smem);
+    };
+    pass_attr.template operator()<2>();
+    if constexpr (sizeof(T) == 4) pass_attr.template operator()<4>();
     if (e == cudaSuccess) done.fetch_or(bit);
     return e;
 }
@@ -313,19 +318,35 @@ amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, 
     });
 }
 
-// Two steps per pass (same-level trees): coefficient rows of the two steps.
-template <typename T, int N, int H>
-amr_status launch_step2d_pair(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coefA,
-                              const float2* coef32A, const Coef* coefB, const float2* coef32B, const int* up,
-                              int32_t* err, const uint64_t* keys, const int32_t* upcode, const StepCfg& cfg,
-                              cudaStream_t s)
+// Steps per pass on same-level trees: FP32 four (the pass is bound by the
+// per-patch work, which four steps share), FP64 two (its update is FP64-bound).
+template <typename T>
+constexpr int kPassSteps = sizeof(T) == 4 ? 4 : 2;
+
+// The pass depths covering k steps: passes of kPassSteps, then two, then one.
+inline void pass_plan(int k, int deep, std::vector<int>& plan)
+{
+    plan.clear();
+    while (k > 0) {
+        const int d = k >= deep ? deep : (k >= 2 ? 2 : 1);
+        plan.push_back(d);
+        k -= d;
+    }
+}
+
+// D steps per pass (same-level trees): coefficient rows of step m at coef +
+// m * cstride.
+template <typename T, int N, int H, int D>
+amr_status launch_step2d_pass(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coef,
+                              const float2* coef32, size_t cstride, const int* up, int32_t* err, const uint64_t* keys,
+                              const int32_t* upcode, const StepCfg& cfg, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
         const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_step2d_pair<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
-            in, out, meta, P, g, coefA, coef32A, coefB, coef32B, up[0], up[1], err, keys, upcode);
-        AMR_LAUNCHED("k_step2d_pair");
+        k_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
+            in, out, meta, P, g, coef, coef32, cstride, up[0], up[1], err, keys, upcode);
+        AMR_LAUNCHED("k_step2d_pass");
         return AMR_OK;
     });
 }
@@ -365,8 +386,8 @@ bool lookup_tuned(const amr_tree* t, bool per_leaf, bool pair, StepCfg& cfg)
     return true;
 }
 
-// pair: time the two-step pass instead (same-level trees); both passes read
-// the prologue's coefficient row.
+// pair: time the multi-step pass instead (same-level trees); every step of
+// it reads the prologue's coefficient row (stride 0).
 template <typename T, int N, int H>
 amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, const int* up, const int32_t* upcode,
                        StepCfg& best, bool pair = false)
@@ -402,9 +423,9 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
                 StepCfg   c{ W, S, grid };
                 for (int rep = 0; rep < 2; ++rep) { // warm-up
                     amr_status r =
-                        pair ? launch_step2d_pair<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                           t->meta[t->tb], P, t->g, coef, coef32, coef, coef32, up,
-                                                           t->status + 7, t->keys[t->tb], upcode, c, s)
+                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(
+                                   static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->meta[t->tb], P, t->g,
+                                   coef, coef32, 0, up, t->status + 7, t->keys[t->tb], upcode, c, s)
                              : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
                                                       t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
                                                       t->keys[t->tb], upcode, c, s);
@@ -414,9 +435,9 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
                 AMR_CUDA(cudaEventRecord(e0, s));
                 for (int rep = 0; rep < reps; ++rep) {
                     amr_status r =
-                        pair ? launch_step2d_pair<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                           t->meta[t->tb], P, t->g, coef, coef32, coef, coef32, up,
-                                                           t->status + 7, t->keys[t->tb], upcode, c, s)
+                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(
+                                   static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->meta[t->tb], P, t->g,
+                                   coef, coef32, 0, up, t->status + 7, t->keys[t->tb], upcode, c, s)
                              : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
                                                       t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
                                                       t->keys[t->tb], upcode, c, s);
@@ -755,17 +776,16 @@ amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const 
     });
 }
 
-template <typename T, int N, int H>
-amr_status launch_run_step2d_pair(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coefA,
-                                  const float2* coef32A, const Coef* coefB, const float2* coef32B, int parity,
-                                  const int* up, const StepCfg& cfg, int P, cudaStream_t s)
+template <typename T, int N, int H, int D>
+amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, const float2* coef32,
+                                  size_t cstride, int parity, const int* up, const StepCfg& cfg, int P, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
         const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_run_step2d_pair<T, N, H, W, S><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
-            B, ctl, g, coefA, coef32A, coefB, coef32B, parity, up[0], up[1]);
-        AMR_LAUNCHED("k_run_step2d_pair");
+        k_run_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
+            B, ctl, g, coef, coef32, cstride, parity, up[0], up[1]);
+        AMR_LAUNCHED("k_run_step2d_pass");
         return AMR_OK;
     });
 }
@@ -787,26 +807,28 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     AMR_LAUNCHED("k_batch_begin");
     const StepCfg cfg{ key.W, key.S, key.grid };
     const int     ppb = std::max(1, 256 / g.cells);
-    // two-step passes: pass j covers steps 2j and 2j+1, an odd last step
-    // runs alone; the buffers alternate per pass
-    const int passes = key.pair ? key.k / 2 : 0;
-    for (int j = 0; j < passes; ++j) {
-        const Coef*   cf  = t->coef + static_cast<size_t>(2 * j) * K * nl;
-        const float2* cf2 = t->coef32 + static_cast<size_t>(2 * j) * K * nl;
-        const Coef*   cfb = cf + static_cast<size_t>(K) * nl;
-        const float2* c2b = cf2 + static_cast<size_t>(K) * nl;
-        amr_status    st  = g.n == 16 ? launch_run_step2d_pair<T, 16, 1>(B, ctl, g, cf, cf2, cfb, c2b, j & 1, key.up, cfg,
-                                                                          static_cast<int>(t->cap), cs)
-                                      : launch_run_step2d_pair<T, 8, 1>(B, ctl, g, cf, cf2, cfb, c2b, j & 1, key.up, cfg,
-                                                                         static_cast<int>(t->cap), cs);
-        if (st != AMR_OK) return st;
-    }
-    for (int j = 2 * passes; j < key.k; ++j) {
-        const int par = key.pair ? (passes & 1) : (j & 1);
-        const Coef*   cf  = t->coef + static_cast<size_t>(j) * K * nl;
-        const float2* cf2 = t->coef32 + static_cast<size_t>(j) * K * nl;
+    // multi-step passes on same-level trees (pass_plan), one launch per step
+    // otherwise; the buffers alternate per launch
+    std::vector<int> plan;
+    if (key.pair) pass_plan(key.k, kPassSteps<T>, plan);
+    else plan.assign(static_cast<size_t>(key.k), 1);
+    int step = 0;
+    for (size_t j = 0; j < plan.size(); ++j) {
+        const int     D   = plan[j];
+        const int     par = static_cast<int>(j & 1);
+        const Coef*   cf  = t->coef + static_cast<size_t>(step) * K * nl;
+        const float2* cf2 = t->coef32 + static_cast<size_t>(step) * K * nl;
+        const size_t  cst = static_cast<size_t>(K) * nl;
         amr_status    st  = AMR_OK;
-        if (key.W > 0 && g.n == 16)
+        auto pass = [&]<int N>() -> amr_status {
+            if constexpr (sizeof(T) == 4)
+                if (D == 4) return launch_run_step2d_pass<T, N, 1, 4>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
+                                                                     static_cast<int>(t->cap), cs);
+            return launch_run_step2d_pass<T, N, 1, 2>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
+                                                      static_cast<int>(t->cap), cs);
+        };
+        if (D > 1) st = g.n == 16 ? pass.template operator()<16>() : pass.template operator()<8>();
+        else if (key.W > 0 && g.n == 16)
             st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
         else if (key.W > 0)
             st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
@@ -815,9 +837,10 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
             AMR_LAUNCHED("k_run_step");
         }
         if (st != AMR_OK) return st;
+        step += D;
     }
     // parity of the buffer holding the interval's result
-    const int sp = key.pair ? ((passes + (key.k & 1)) & 1) : (key.k & 1);
+    const int sp = static_cast<int>(plan.size() & 1);
     if (key.crit != 0) {
         if (key.crit == 1 && g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8)) {
             const GradRule rule = make_grad_rule(key.rthr, key.cthr);
@@ -1667,9 +1690,12 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
         AMR_LAUNCHED("k_batch_begin");
         first = false;
         const bool shape2d = t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8);
+        const int  deep    = t->dtype == AMR_F32 ? kPassSteps<float> : kPassSteps<double>;
         for (int k = 0; k < chunk;) {
-            // two steps per pass where every relation is same-level
-            const bool pair = shape2d && t->uniform && k + 1 < chunk;
+            // several steps per pass where every relation is same-level
+            const int  left = chunk - k;
+            const int  D    = (shape2d && t->uniform) ? (left >= deep ? deep : (left >= 2 ? 2 : 1)) : 1;
+            const bool pair = D > 1;
             std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
             if (t->timing) {
                 if (t->events_used == t->events.size()) {
@@ -1680,7 +1706,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                     t->event_cells.push_back(0);
                 }
                 ev = &t->events[t->events_used];
-                t->event_cells[t->events_used] = static_cast<uint64_t>(P) * t->g.cells * (pair ? 2 : 1);
+                t->event_cells[t->events_used] = static_cast<uint64_t>(P) * t->g.cells * D;
                 ++t->events_used;
                 AMR_CUDA(cudaEventRecord(ev->first, s));
             }
@@ -1691,13 +1717,16 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                 const T*      in  = static_cast<const T*>(t->cur);
                 T*            out = static_cast<T*>(t->nxt);
                 if (pair) {
-                    const Coef*   cfb  = cf + static_cast<size_t>(K) * nl;
-                    const float2* cf2b = cf2 + static_cast<size_t>(K) * nl;
-                    if (t->g.n == 16)
-                        return launch_step2d_pair<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
-                                                            t->status + 7, t->keys[t->tb], uleaf, cfg_pair, s);
-                    return launch_step2d_pair<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cfb, cf2b, up,
-                                                       t->status + 7, t->keys[t->tb], uleaf, StepCfg{}, s);
+                    const size_t cst  = static_cast<size_t>(K) * nl;
+                    auto         pass = [&]<int N>(const StepCfg& c) -> amr_status {
+                        if constexpr (sizeof(T) == 4)
+                            if (D == 4)
+                                return launch_step2d_pass<T, N, 1, 4>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
+                                                                      t->status + 7, t->keys[t->tb], uleaf, c, s);
+                        return launch_step2d_pass<T, N, 1, 2>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
+                                                              t->status + 7, t->keys[t->tb], uleaf, c, s);
+                    };
+                    return t->g.n == 16 ? pass.template operator()<16>(cfg_pair) : pass.template operator()<8>(StepCfg{});
                 }
                 if (t->g.rank == 2 && t->g.n == 16 && t->g.h == 1)
                     return launch_step2d<T, 16, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
@@ -1714,7 +1743,7 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
             if (st != AMR_OK) return st;
             if (ev) AMR_CUDA(cudaEventRecord(ev->second, s));
             std::swap(t->cur, t->nxt);
-            k += pair ? 2 : 1;
+            k += D;
         }
         done += chunk;
         if (steps == 0) break;
