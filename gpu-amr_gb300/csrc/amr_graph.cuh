@@ -26,7 +26,7 @@ struct RunCtl {
     int32_t leaves_min; // over interval starts
     int32_t leaves_max;
     int32_t uniform;    // every neighbour relation of the current tree is "same level"
-    int32_t pad;
+    int32_t flagged;    // some leaf of the pending re-mesh is flagged (zeroed at each commit)
     unsigned long long cell_updates, leaves_sum, intervals, remeshes;
 };
 
@@ -230,26 +230,32 @@ __global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
     if (ctl->err) return;
     const int P = ctl->P, tb = ctl->tb;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->changed = 0;
-    AMR_RUN_LEAVES(P) mark_leaf(B.keys[tb], B.flags, P, g, B.rmark, B.chead, i);
+    AMR_RUN_LEAVES(P)
+    {
+        mark_leaf(B.keys[tb], B.flags, P, g, B.rmark, B.chead, i);
+        if (B.flags[i] != FLAG_STABLE) ctl->flagged = 1;
+    }
 }
 
+// With no leaf flagged the re-mesh changes nothing (reconstruction_is_noop,
+// ndtree.hpp:1242-1246): closure, veto, count and scan return at once.
 __global__ void k_run_closure(RunBufs B, RunCtl* ctl, Geo g)
 {
-    if (ctl->err) return;
+    if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P) closure_leaf(B.meta[tb], g, B.rmark, i);
 }
 
 __global__ void k_run_veto(RunBufs B, RunCtl* ctl, Geo g)
 {
-    if (ctl->err) return;
+    if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P) veto_leaf(B.meta[tb], g, B.rmark, B.chead, i);
 }
 
 __global__ void k_run_count(RunBufs B, RunCtl* ctl, Geo g)
 {
-    if (ctl->err) return;
+    if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P) count_leaf(B.keys[tb], B.rmark, B.chead, g, B.cnt, &ctl->changed, i);
 }
@@ -284,7 +290,7 @@ __device__ inline uint32_t scan_block_exclusive(uint32_t v, uint32_t* warp_sums,
 // Scan, pass 1: sum of the counts of each tile of kScanTile leaves.
 __global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunCtl* ctl)
 {
-    if (ctl->err) return;
+    if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P;
     __shared__ uint32_t ws[kScanThreads / 32];
     for (int tile = blockIdx.x; tile * kScanTile < P; tile += gridDim.x) {
@@ -304,7 +310,7 @@ __global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunC
 // flags AMR_ERR_CAPACITY when it exceeds the capacity.
 __global__ void __launch_bounds__(kScanThreads) k_run_scan_apply(RunBufs B, RunCtl* ctl)
 {
-    if (ctl->err) return;
+    if (ctl->err || !ctl->flagged) return;
     const int P      = ctl->P;
     const int ntiles = (P + kScanTile - 1) / kScanTile;
     __shared__ uint32_t ws[kScanThreads / 32];
@@ -390,6 +396,7 @@ __global__ void __launch_bounds__(256) k_run_commit(RunBufs B, RunCtl* ctl, int 
         const int  P  = ctl->P;
         const bool ok = ctl->err == 0;
         chg           = (remesh && ok && ctl->changed) ? 1 : 0;
+        ctl->flagged  = 0; // the next interval's marks set it again
         if (ok) {
             ctl->sb ^= sp;
             ctl->cell_updates += static_cast<unsigned long long>(P) * steps * cells;
