@@ -120,6 +120,7 @@ def lib():
         L.amr_tree_write_vtk.argtypes = [vp, C.c_char_p, C.c_char_p]
         L.amr_tree_reserve.argtypes = [vp, sz]
         L.amr_tree_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl]
+        L.amr_tree_advance_ssprk.argtypes = [vp, sz, i32, C.POINTER(dbl), dbl, dbl]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -350,6 +351,12 @@ class Tree:
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}
+
+    def advance_ssprk(self, steps, order, velocity, cfl, remaining=1.7976931348623157e308):
+        """SSPRK2 (order 2) or SSPRK3 (order 3) steps of advection; velocity
+        None: the per-instance velocities.  finish_advance() as for advance."""
+        v = None if velocity is None else _vec3(velocity)
+        check(lib().amr_tree_advance_ssprk(self._h, steps, order, v, cfl, remaining))
 
     # -------------------------------------------------------------- Euler
     def euler_advance(self, steps, gamma, cfl, remaining=1.7976931348623157e308):

@@ -184,14 +184,24 @@ __device__ inline void halo_cell(T* buf, const amr_halo_meta* meta, const Geo& g
 }
 
 // blockIdx.y = field of a multi-field state (fields fstride elements apart).
+// With step_dt (per instance), patches of instances whose step is not taken
+// (step size 0: past the time limit) keep their ghosts.
 template <typename T>
 __global__ void __launch_bounds__(256) k_halo(T* __restrict__ buf, const amr_halo_meta* __restrict__ meta,
-                                              long long total, Geo g, size_t fstride = 0)
+                                              long long total, Geo g, size_t fstride = 0,
+                                              const uint64_t* __restrict__ keys = nullptr,
+                                              const double* __restrict__ step_dt = nullptr)
 {
     buf += blockIdx.y * fstride;
+    const long long per_patch = static_cast<long long>(g.h) * (g.cells / g.n) * g.ndir;
     for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
-         t += static_cast<long long>(gridDim.x) * blockDim.x)
+         t += static_cast<long long>(gridDim.x) * blockDim.x) {
+        if (step_dt) {
+            const int p = static_cast<int>(t / per_patch);
+            if (!(step_dt[instance_of(g, keys, p)] > 0.0)) continue;
+        }
         halo_cell<T>(buf, meta, g, t);
+    }
 }
 
 // ------------------------------------------------------------------ flags

@@ -18,6 +18,7 @@
 #include "amr_gb300.h"
 #include "amr_cycle.cuh"
 #include "amr_euler.cuh"
+#include "amr_ssprk.cuh"
 #include "amr_graph.cuh"
 #include "amr_vtk.cuh"
 
@@ -214,6 +215,8 @@ struct amr_tree {
     int32_t*            euler_ctl = nullptr;
     double*             prim[2]{}; // one-side flux terms beside sbuf[0] / sbuf[1]
     size_t              prim_cap = 0;
+    void*               stage_buf = nullptr; // SSPRK intermediate stage (capacity patches)
+    size_t              stage_cap = 0;
 
     size_t fstride() const { return cap * static_cast<size_t>(g.flat); }
     size_t field_bytes(size_t patches) const { return patches * static_cast<size_t>(g.flat) * esize; }
@@ -529,8 +532,24 @@ void free_tree(amr_tree* t)
     cudaFree(t->euler_ctl);
     cudaFree(t->prim[0]);
     cudaFree(t->prim[1]);
+    cudaFree(t->stage_buf);
     if (t->pinned) cudaFreeHost(t->pinned);
     delete t;
+}
+
+// Face halo of every field of an arbitrary state buffer of the tree (does
+// not touch ghosts_valid); with step_dt, only instances whose step is taken.
+amr_status halo_buffer(amr_tree* t, void* buf, const double* step_dt = nullptr)
+{
+    const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
+    return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+        using T = decltype(z);
+        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(buf), t->meta[t->tb], total, t->g,
+                                                             t->fstride(), t->keys[t->tb], step_dt);
+        AMR_LAUNCHED("k_halo");
+        return AMR_OK;
+    });
 }
 
 amr_status launch_halo(amr_tree* t)
@@ -1359,6 +1378,9 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     cudaFree(t->prim[1]);
     t->prim[0] = t->prim[1] = nullptr;
     t->prim_cap = 0;
+    cudaFree(t->stage_buf); // SSPRK scratch: allocated again at the next SSPRK advance
+    t->stage_buf = nullptr;
+    t->stage_cap = 0;
     t->sbuf[0] = sb0;
     t->sbuf[1] = sb1;
     t->cur     = nsb[cs];
@@ -1756,6 +1778,88 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
 amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining)
 {
     return advance_impl(t, steps, velocity3, cfl, remaining, BATCH_RESET);
+}
+
+amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const double* velocity3, double cfl,
+                                  double remaining)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (order != 2 && order != 3) return fail(AMR_ERR_INVALID, "SSPRK order is 2 or 3");
+    if (t->nvar != 1 || t->dtype != AMR_F64) return fail(AMR_ERR_INVALID, "SSPRK advances a one-field FP64 tree");
+    if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
+    cudaStream_t s = t->stream;
+    const int    K = t->ninst;
+    if (velocity3) {
+        std::vector<double> v(3 * static_cast<size_t>(K));
+        for (int i = 0; i < K; ++i)
+            for (int a = 0; a < 3; ++a) v[3 * i + a] = velocity3[a];
+        AMR_CUDA(cudaMemcpyAsync(t->vel, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    } else {
+        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    if (t->stage_cap != t->cap) {
+        cudaFree(t->stage_buf);
+        t->stage_buf = nullptr;
+        t->stage_cap = 0;
+        AMR_CUDA(cudaMalloc(&t->stage_buf, t->field_bytes(t->cap)));
+        t->stage_cap = t->cap;
+    }
+    SsprkStage st{};
+    st.keys   = t->keys[t->tb];
+    st.P      = static_cast<int>(t->size);
+    st.g      = t->g;
+    st.vel    = t->vel;
+    st.stream = s;
+    uint64_t launches = 0;
+    auto     stage    = [&](const void* in, const void* un, void* out, int mode, const double* dts) -> amr_status {
+        st.in      = static_cast<const double*>(in);
+        st.un      = static_cast<const double*>(un);
+        st.out     = static_cast<double*>(out);
+        st.mode    = mode;
+        st.step_dt = dts;
+        AMR_CUDA(ssprk_stage(st));
+        ++launches;
+        return AMR_OK;
+    };
+    bool   first = true;
+    size_t done  = 0;
+    while (done < steps || (first && steps == 0)) {
+        // CFL steps of this chunk (as amr_tree_advance: the finest level,
+        // clamped to the remaining time), and the time bookkeeping
+        const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
+        k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? BATCH_RESET : BATCH_CONTINUE,
+                                        remaining, t->dts(), t->step_dt, t->coef, t->coef32, t->upcode);
+        AMR_LAUNCHED("k_batch_begin");
+        first = false;
+        for (int k = 0; k < chunk; ++k) {
+            const double* dts = t->step_dt + static_cast<size_t>(k) * K;
+            // (a step past the time limit, step size 0, changes nothing:
+            // no halo, and every stage copies)
+            if (amr_status hs = halo_buffer(t, t->cur, dts); hs != AMR_OK) return hs;
+            amr_status rs = AMR_OK;
+            if (order == 2) {
+                if ((rs = stage(t->cur, t->cur, t->stage_buf, 0, dts)) != AMR_OK) return rs;
+                if ((rs = halo_buffer(t, t->stage_buf, dts)) != AMR_OK) return rs;
+                if ((rs = stage(t->stage_buf, t->cur, t->nxt, 2, dts)) != AMR_OK) return rs;
+            } else {
+                if ((rs = stage(t->cur, t->cur, t->nxt, 0, dts)) != AMR_OK) return rs;
+                if ((rs = halo_buffer(t, t->nxt, dts)) != AMR_OK) return rs;
+                if ((rs = stage(t->nxt, t->cur, t->stage_buf, 31, dts)) != AMR_OK) return rs;
+                if ((rs = halo_buffer(t, t->stage_buf, dts)) != AMR_OK) return rs;
+                if ((rs = stage(t->stage_buf, t->cur, t->nxt, 32, dts)) != AMR_OK) return rs;
+            }
+            std::swap(t->cur, t->nxt);
+        }
+        done += chunk;
+        if (steps == 0) break;
+    }
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
+    // the buffer's ghost cells hold the last stage's combination, which is
+    // what the reference's tree holds between steps (no halo exchange follows
+    // the last stage); criteria read them from the buffer as it does
+    t->ghosts_valid = true;
+    t->batch_open   = true;
+    return AMR_OK;
 }
 
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed)

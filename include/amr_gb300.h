@@ -270,6 +270,21 @@ typedef struct amr_cycle_stats {
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_stats* stats);
 
+/* Strong-stability-preserving Runge-Kutta steps of linear advection: the
+ * reference's SSPRK2 / SSPRK3 integrators (include/dg_helpers/
+ * time_integration/time.hpp:83-272, driven with a halo exchange before every
+ * stage as include/dg_helpers/solver.hpp:159-232 does) on the FV residual
+ * -sum_d (F_R - F_L) / dx_d with the Rusanov flux of AdvectionPhysics.  The
+ * step size is amr_tree_advance's (CFL from the finest level, clamped to the
+ * remaining time); a one-field FP64 tree; velocity3 NULL = the per-instance
+ * velocities.  As in the reference, every stage combines whole padded
+ * patches and no halo exchange follows the last stage, so a criterion
+ * evaluated after the advance reads the combined ghost cells.  States are
+ * bit-identical to the reference's CPU path.  Use amr_tree_finish_advance
+ * for the simulated time and executed steps. */
+amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const double* velocity3, double cfl,
+                                  double remaining_time);
+
 /* ------------------------------------------------------------- Euler
  * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through
  * amr_solver (amr_solver.hpp:155-413) on a tree created with fields =

@@ -1014,12 +1014,123 @@ double oracle_advance(oracle_tree* t, size_t steps, const double* v, double cfl,
     return acc;
 }
 
+/* ---------------------------------------------------------------- SSPRK */
+/* The strong-stability-preserving Runge-Kutta integrators of the reference
+ * (include/dg_helpers/time_integration/time.hpp:83-272, used there per
+ * patch with a halo exchange before every stage, solver.hpp:159-232) applied
+ * to the FV advection operator: the residual of a stage is
+ *   R = -sum_d (F_R - F_L) / dx_d
+ * with the Rusanov flux of AdvectionPhysics (as in time_step), and the
+ * stage combinations are the reference's, operation for operation:
+ *   stage 0           u* = u + R dt
+ *   SSPRK2 stage 1    u' = ((u^n + u*) + R dt) * 0.5
+ *   SSPRK3 stage 1    u2 = u^n * 0.75 + (u1 + R dt) * 0.25
+ *   SSPRK3 stage 2    u' = u^n * (1/3) + (u2 + R dt) * (2/3)
+ * mode: 0, 2, 31, 32 for the four forms.  Like the reference, which
+ * combines whole padded containers, every cell of `out` is written (the
+ * ghost cells with R = 0), and no halo exchange follows the last stage: the
+ * next step starts with one (solver.hpp:170), and a criterion evaluated
+ * between steps sees the combined ghosts, as in the reference. */
+static void ssprk_stage(const oracle_tree* t, const double* v, double dt, int mode, const double* in,
+                        const double* un, double* out)
+{
+    const int    rank = t->rank, n = t->n, h = t->h;
+    const size_t P1 = t->pad1;
+    const size_t stride[3] = { 1, P1, P1 * P1 };
+    const long   np = (long)t->size;
+#pragma omp parallel for schedule(static) if (np > 16) num_threads(g_threads > 0 ? g_threads : 1)
+    for (long pi = 0; pi < np; ++pi) {
+        const size_t p = (size_t)pi;
+        double       cs[3];
+        cell_sizes(t, t->ids[p], cs);
+        const double* a = in + p * t->pstride;
+        const double* b = un + p * t->pstride;
+        double*       o = out + p * t->pstride;
+        /* every cell of the padded patch, as the reference combines whole
+         * containers; the residual is zero outside the interior */
+        for (size_t li = 0; li < t->flat; ++li) {
+            int    interior = 1;
+            size_t r        = li;
+            for (int k = 0; k < rank; ++k) {
+                const size_t c = r % P1;
+                r /= P1;
+                if (c < (size_t)h || c >= (size_t)(n + h)) interior = 0;
+            }
+            const double uc = a[li];
+            double       R  = 0.0;
+            if (interior)
+                for (int d = 0; d < rank; ++d) {
+                    const double uL = a[li - stride[d]];
+                    const double uR = a[li + stride[d]];
+                    const double sp = fabs(v[d]);
+                    const double fL = 0.5 * (uL * v[d] + uc * v[d]) - 0.5 * sp * (uc - uL);
+                    const double fR = 0.5 * (uc * v[d] + uR * v[d]) - 0.5 * sp * (uR - uc);
+                    R -= (fR - fL) / cs[d];
+                }
+            const double Rdt = R * dt;
+            double       res;
+            if (mode == 0) res = uc + Rdt;
+            else if (mode == 2) res = (b[li] + uc + Rdt) * 0.5;
+            else if (mode == 31) res = b[li] * 0.75 + (uc + Rdt) * 0.25;
+            else res = b[li] * (1.0 / 3.0) + (uc + Rdt) * (2.0 / 3.0);
+            o[li] = res;
+        }
+    }
+}
+
+/* halo exchange of an arbitrary state buffer of the tree */
+static void halo_buffer(oracle_tree* t, double* buf)
+{
+    double* keep = t->cur;
+    t->cur       = buf;
+    oracle_halo_exchange(t);
+    t->cur = keep;
+}
+
+/* advance_batch_async's loop (CFL step from compute_time_step_cpu, clamped to
+ * the remaining time) with SSPRK2 (order 2) or SSPRK3 (order 3) steps. */
+double oracle_ssprk_advance(oracle_tree* t, size_t steps, int order, const double* v, double cfl, double remaining,
+                            size_t* executed)
+{
+    double* A = (double*)malloc((t->size > 0 ? t->size : 1) * t->pstride * sizeof(double));
+    double  acc   = 0.0;
+    size_t  count = 0;
+    if (A) memset(A, 0, (t->size > 0 ? t->size : 1) * t->pstride * sizeof(double));
+    for (size_t s = 0; A && s < steps; ++s) {
+        if (remaining <= 0.0) break;
+        const double dt      = oracle_compute_dt(t, v, cfl);
+        const double step_dt = dt < remaining ? dt : remaining;
+        if (step_dt <= 0.0) break;
+        oracle_halo_exchange(t);
+        if (order == 2) {
+            ssprk_stage(t, v, step_dt, 0, t->cur, t->cur, A);
+            halo_buffer(t, A);
+            ssprk_stage(t, v, step_dt, 2, A, t->cur, t->nxt);
+        } else {
+            ssprk_stage(t, v, step_dt, 0, t->cur, t->cur, t->nxt);
+            halo_buffer(t, t->nxt);
+            ssprk_stage(t, v, step_dt, 31, t->nxt, t->cur, A);
+            halo_buffer(t, A);
+            ssprk_stage(t, v, step_dt, 32, A, t->cur, t->nxt);
+        }
+        double* tmp = t->cur;
+        t->cur      = t->nxt;
+        t->nxt      = tmp;
+        acc += step_dt;
+        remaining -= step_dt;
+        ++count;
+    }
+    free(A);
+    if (executed) *executed = count;
+    return acc;
+}
+
 /* ------------------------------------------------------------ VTK file */
 /* vtk_print::print (include/ndtree/vtk_print.hpp:53-257): legacy VTK,
  * BINARY (big-endian), DATASET UNSTRUCTURED_GRID with one quad (2D, type 9)
  * or voxel (3D, type 11) per interior cell; corner coordinates from
- * physics_system::patch_coord / cell_sizes (physics_system.hpp:62-104) on the
- * unit domain; CELL_DATA cell_index, is_halo (the reference evaluates
+ * physics_system::patch_coord / cell_sizes (physics_system.hpp:58-104) on the
+ * tree's domain lengths; CELL_DATA cell_index, is_halo (the reference evaluates
  * is_halo_cell on the padded layout for linear indices 0 .. n^rank - 1 of
  * every patch, vtk_print.hpp:217-228) and the scalar field. */
 static void put_be(FILE* f, const void* v, size_t n)

@@ -75,6 +75,9 @@ void oracle_random_state(oracle_tree* t, uint64_t seed);
 double oracle_compute_dt(const oracle_tree* t, const double* velocity, double cfl);
 double oracle_advance(oracle_tree* t, size_t steps, const double* velocity,
                       double cfl, double remaining, size_t* executed);
+/* SSPRK2 / SSPRK3 steps of the FV advection operator (see amr_oracle.c). */
+double oracle_ssprk_advance(oracle_tree* t, size_t steps, int order, const double* v, double cfl, double remaining,
+                            size_t* executed);
 /* Domain lengths per Morton axis (physics_system's Domain_Sizes; default 1). */
 void oracle_set_lengths(oracle_tree* t, const double* lengths);
 

@@ -83,6 +83,8 @@ def lib():
         L.oracle_set_lengths.argtypes = [vp, P(np.float64, flags="C")]
         L.oracle_euler_dt.restype = dbl
         L.oracle_euler_dt.argtypes = [vp, dbl, dbl]
+        L.oracle_ssprk_advance.restype = dbl
+        L.oracle_ssprk_advance.argtypes = [vp, sz, C.c_int, P(np.float64, flags="C"), dbl, dbl, C.POINTER(sz)]
         L.oracle_euler_advance.restype = dbl
         L.oracle_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl, C.POINTER(sz), vp]
         L.oracle_euler_init_pulse.argtypes = [vp, dbl, dbl, dbl, dbl, dbl, P(np.float64, flags="C")]
@@ -159,6 +161,14 @@ class OracleTree:
         acc = lib().oracle_euler_advance(self._t, steps, gamma, cfl, remaining, C.byref(ex),
                                          dts.ctypes.data_as(C.c_void_p))
         return acc, ex.value, dts[: ex.value]
+
+    def ssprk_advance(self, steps, order, velocity, cfl, remaining=1.7976931348623157e308):
+        """(simulated time, executed steps) of SSPRK2/3 steps of advection."""
+        v = np.zeros(3)
+        v[: len(velocity)] = velocity
+        ex = C.c_size_t(0)
+        acc = lib().oracle_ssprk_advance(self._t, steps, order, v, cfl, remaining, C.byref(ex))
+        return acc, ex.value
 
     def reconstruct(self, flags: np.ndarray) -> int:
         f = np.ascontiguousarray(flags, np.int8)

@@ -24,6 +24,13 @@
 //                       (benchmark/bench_fvm_solver_integration.b.cpp:
 //                       95-178: domain 1000^DIM, max-Rho criterion over the
 //                       padded patch, re-mesh every `remesh` steps).
+//   mode=ssprk order=2|3 - the reference's SSPRK2 / SSPRK3 classes
+//                       (include/dg_helpers/time_integration/time.hpp) driving
+//                       the FV advection residual -sum_d (F_R - F_L)/dx_d
+//                       (RuntimeAdvection's Rusanov flux) patch by patch, with
+//                       a halo exchange before every stage as the DG solver
+//                       does (include/dg_helpers/solver.hpp:159-232); CFL step
+//                       as compute_time_step_cpu; gradient re-mesh as in run.
 //   vtk=<name>          - after the mode, the reference's VTK writer
 //                       (include/ndtree/vtk_print.hpp) prints the tree to
 //                       vtk_output/<name>.vtk.
@@ -35,6 +42,8 @@
 #include "ndtree/ndtree.hpp"
 #include "ndtree/patch_layout.hpp"
 #include "ndtree/vtk_print.hpp"
+#include "containers/container_operations.hpp"
+#include "dg_helpers/time_integration/time.hpp"
 #include "solver/EulerPhysics.hpp"
 #include "solver/amr_solver.hpp"
 #include "solver/cell_types.hpp"
@@ -517,6 +526,116 @@ struct harness
         return 0;
     }
 
+    // ---- SSPRK (mode=ssprk)
+    using container_t = amr::containers::static_tensor<double, padded_t>;
+
+    // compute_time_step_cpu (amr_solver.hpp:355-413) for the advection speeds
+    auto cfl_dt(double cfl) -> double
+    {
+        double dt = std::numeric_limits<double>::max();
+        auto&  t  = tree();
+        for (std::size_t i = 0; i != t.size(); ++i)
+        {
+            const auto cs = geometry_t::cell_sizes(t.get_node_index_at(i));
+            for (int d = 0; d < DIM; ++d)
+            {
+                const double speed = std::abs(g_velocity[d]);
+                if (speed > 1e-12) dt = std::min(dt, cs[d] / speed);
+            }
+        }
+        return cfl * dt;
+    }
+
+    template <typename Integrator>
+    void ssprk_step(double dt)
+    {
+        auto&             t = tree();
+        const std::size_t n = t.size();
+        std::vector<Integrator> integ(n);
+        t.halo_exchange_update();
+        for (std::size_t i = 0; i != n; ++i) integ[i].begin_step(t.template get_patch<amr::cell::Scalar>(i).data());
+        for (int s = 0; s < Integrator::num_stages(); ++s)
+        {
+            t.halo_exchange_update();
+            for (std::size_t i = 0; i != n; ++i)
+            {
+                auto&      patch = t.template get_patch<amr::cell::Scalar>(i);
+                const auto cs    = geometry_t::cell_sizes(t.get_node_index_at(i));
+                auto residual = [&](container_t& update, const container_t& cur, double)
+                {
+                    amr::containers::manipulators::shaped_for<
+                        typename patch_layout_t::interior_iteration_control_t>(
+                        [&](auto const& idxs)
+                        {
+                            const std::size_t li = padded_t::linear_index(idxs);
+                            double            R  = 0.0;
+                            for (int d = 0; d < DIM; ++d)
+                            {
+                                const std::size_t st = d == 0 ? 1 : (d == 1 ? padded1 : padded1 * padded1);
+                                using sv             = amr::containers::static_vector<double, 1>;
+                                sv UL, UC, UR, fL, fR;
+                                UL[0] = cur[static_cast<typename padded_t::index_t>(li - st)];
+                                UC[0] = cur[static_cast<typename padded_t::index_t>(li)];
+                                UR[0] = cur[static_cast<typename padded_t::index_t>(li + st)];
+                                RuntimeAdvection<DIM>::rusanovFlux(UL, UC, fL, d, 0.0);
+                                RuntimeAdvection<DIM>::rusanovFlux(UC, UR, fR, d, 0.0);
+                                R -= (fR[0] - fL[0]) / cs[d];
+                            }
+                            update[static_cast<typename padded_t::index_t>(li)] = R;
+                        }
+                    );
+                };
+                integ[i].compute_stage(s, residual, patch.data(), 0.0, dt);
+                patch.data() = integ[i].stage_result(s, patch.data());
+            }
+        }
+        for (std::size_t i = 0; i != n; ++i) integ[i].finish_step(t.template get_patch<amr::cell::Scalar>(i).data());
+    }
+
+    int ssprk_mode()
+    {
+        auto vel = P.list("vel");
+        for (std::size_t d = 0; d < vel.size() && d < 3; ++d) g_velocity[d] = vel[d];
+        uniform_refine(static_cast<int>(P.integer("init_levels", 2)));
+        init_state();
+        tree().halo_exchange_update();
+        dump_tree(0);
+        dump_state(0);
+        const int    order    = static_cast<int>(P.integer("order", 2));
+        const long   steps    = P.integer("steps", 40);
+        const long   interval = P.integer("remesh", 10);
+        const double cfl      = P.num("cfl", 0.4);
+        double       sum_dt   = 0.0;
+        double       batch    = 0.0; // steps since the last re-mesh, added like finish_advance_batch
+        for (long s = 1; s <= steps; ++s)
+        {
+            const double dt = cfl_dt(cfl);
+            if (order == 3)
+                ssprk_step<amr::time_integration::SSPRK3<container_t>>(dt);
+            else
+                ssprk_step<amr::time_integration::SSPRK2<container_t>>(dt);
+            batch += dt;
+            if ((interval > 0 && s % interval == 0) || s == steps)
+            {
+                sum_dt += batch;
+                batch = 0.0;
+            }
+            if (interval > 0 && s % interval == 0)
+            {
+                remesh([&](patch_index_t const& i) { return gradient_status(i); });
+                dump_flags(static_cast<std::uint32_t>(s));
+                dump_tree(static_cast<std::uint32_t>(s));
+            }
+        }
+        tree().halo_exchange_update();
+        dump_state(static_cast<std::uint32_t>(steps));
+        W.header(TAG_DT, static_cast<std::uint32_t>(steps), 16);
+        W.put(sum_dt);
+        W.put(static_cast<std::uint64_t>(steps));
+        std::printf("{\"steps\": %ld, \"sum_dt\": %.17g, \"leaves\": %zu}\n", steps, sum_dt, tree().size());
+        return 0;
+    }
+
     int tree_mode()
     {
         const std::uint64_t seed   = static_cast<std::uint64_t>(P.integer("seed", 1));
@@ -709,7 +828,7 @@ int dispatch(params const& p)
         return rc;
     }
     auto h = std::make_unique<harness<DIM, N, H, Depth>>(p, w);
-    const int  rc   = mode == "tree" ? h->tree_mode() : h->run();
+    const int  rc   = mode == "tree" ? h->tree_mode() : (mode == "ssprk" ? h->ssprk_mode() : h->run());
     if (rc == 0 && p.has("vtk"))
     {
         using geometry_t = typename harness<DIM, N, H, Depth>::geometry_t;

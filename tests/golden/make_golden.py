@@ -180,6 +180,51 @@ EULER_SCENARIOS = [
 ]
 
 
+def scenario_ssprk(name, cfg, rank, n, h, params):
+    """The reference's SSPRK2 / SSPRK3 classes driving the FV advection
+    residual patch by patch (halo exchange before every stage), CFL step,
+    gradient re-mesh: trees and flags after every re-mesh, initial and final
+    padded states, simulated time."""
+    tmp = Path("/tmp") / f"golden_{name}.bin"
+    info = run(dict(cfg=cfg, mode="ssprk", **params), tmp)
+    recs = read_records(str(tmp), rank)
+    trees = [r for r in recs if r[0] == TAG_TREE]
+    flags = [r for r in recs if r[0] == TAG_FLAGS]
+    states = [r for r in recs if r[0] == TAG_STATE]
+    (time, steps) = [r for r in recs if r[0] == TAG_DT][0][2]
+    P1 = n + 2 * h
+    out = {
+        "meta": np.array(json.dumps({"cfg": cfg, "rank": rank, "n": n, "halo": h, "depth": 7,
+                                     "params": params, "info": info})),
+        "remeshes": np.int64(len(flags)),
+        "ids_init": trees[0][2]["ids"],
+        "state_init": states[0][2].reshape((-1,) + (P1,) * rank),
+        "state_final": states[-1][2].reshape((-1,) + (P1,) * rank),
+        "time": np.float64(time),
+        "steps": np.int64(steps),
+    }
+    for k, (fl, tr) in enumerate(zip(flags, trees[1:])):
+        out[f"flags_{k}"] = fl[2]
+        out[f"ids_{k}"] = tr[2]["ids"]
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    return info
+
+
+SSPRK_SCENARIOS = [
+    # 2D advection, 8x8 patches + 1 ghost, two uniform levels, two seeded
+    # bumps plus noise, gradient re-mesh every 10 steps (levels 1..4), CFL 0.4
+    ("ssprk2_advection_2d", "2d8h1", 2, 8, 1, dict(order=2, init_levels=2, steps=30, remesh=10, vel="1,0.5", cfl=0.4,
+                                                    bumps="0.3,0.3,0.05,1,0.7,0.6,0.04,1.5", noise=1e-3, noise_seed=3,
+                                                    rthr=0.05, cthr=0.01, min_level=1, max_level=4)),
+    ("ssprk3_advection_2d", "2d8h1", 2, 8, 1, dict(order=3, init_levels=2, steps=30, remesh=10, vel="-0.7,0.4",
+                                                    cfl=0.4, bumps="0.35,0.6,0.05,1,0.65,0.3,0.04,1.5", noise=1e-3,
+                                                    noise_seed=4, rthr=0.05, cthr=0.01, min_level=1, max_level=4)),
+    ("ssprk3_advection_3d", "3d4h1", 3, 4, 1, dict(order=3, init_levels=2, steps=12, remesh=6, vel="0.6,-0.5,0.8",
+                                                    cfl=0.4, bumps="0.4,0.5,0.6,0.08,1.2", noise=1e-3, noise_seed=5,
+                                                    rthr=0.05, cthr=0.01, min_level=1, max_level=3)),
+]
+
+
 VTK_SCENARIOS = {
     # name of the npz fixture whose final tree and state are printed -> driver arguments
     "config1_uniform_2d": ("2d8h1", dict(mode="run", init_levels=2, steps=100, remesh=0, vel="1,0.5", cfl=0.4,
@@ -225,6 +270,7 @@ def main():
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--vtk-only", action="store_true", help="only the VTK writer fixture")
     ap.add_argument("--euler-only", action="store_true", help="only the Euler fixtures")
+    ap.add_argument("--ssprk-only", action="store_true", help="only the SSPRK fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={a.ref}"], check=True)
     if a.vtk_only:
@@ -233,6 +279,10 @@ def main():
     if a.euler_only:
         for sc in EULER_SCENARIOS:
             print(scenario_euler(*sc))
+        return
+    if a.ssprk_only:
+        for sc in SSPRK_SCENARIOS:
+            print(scenario_ssprk(*sc))
         return
 
     # 1: 2D uniform depth 2, 16 leaves of 8x8, FP64, 100 steps, config as in the
