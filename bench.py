@@ -706,6 +706,75 @@ def euler_extra(torch, A, stream, with_cpu=True):
     return out
 
 
+# ------------------------------------------------------------ SSPRK form
+# SSPRK2 / SSPRK3 steps (the reference's integrators on the FV advection
+# residual) on a uniform level-7 tree of 16x16 patches (16384 patches, 4.2 M
+# cells), FP64, velocity (1, 0.5), CFL 0.4, Gaussian bumps plus noise.
+SSPRK = dict(n=16, halo=1, depth=8, level=7, steps=60, cfl=0.4, velocity=(1.0, 0.5), cpu_steps=4)
+
+
+def ssprk_extra(torch, A, stream, with_cpu=True):
+    """SSPRK steps through amr_tree_advance_ssprk (CUDA events on the tree's
+    stream around `steps` steps), and the oracle on the host cores for a few
+    steps of the same tree; the states must agree bit for bit."""
+    S, W = SSPRK, WORKLOAD
+    out = {"workload": f"SSPRK2/3 advection, uniform level {S['level']} of 16x16 patches + 1 ghost (FP64), "
+                       f"{S['steps']} steps, CFL {S['cfl']}, v = {S['velocity']}"}
+    for order in (2, 3):
+        t = A.Tree(2, S["n"], S["halo"], S["depth"], capacity=20000, dtype=A.F64, stream=stream.cuda_stream)
+        t.refine_uniform(S["level"])
+        u0 = A.gaussian_state(t.ids(), 2, S["n"], S["halo"], S["depth"], bumps(), W["noise"], W["noise_seed"])
+        t.upload_state(u0)
+        t.halo_exchange()
+        t.advance_ssprk(4, order, S["velocity"], S["cfl"])  # warm-up
+        t.finish_advance()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            t.advance_ssprk(S["steps"], order, S["velocity"], S["cfl"])
+            ev1.record(stream)
+        ev1.synchronize()
+        _, ex = t.finish_advance()
+        ms = ev0.elapsed_time(ev1)
+        cells = ex * t.size * S["n"] ** 2
+        rate = cells / (ms * 1e-3)
+        alg = 3 * 8 * order  # per stage: read the stage input and u^n, write the result (FP64)
+        hbm = measured_peaks().get("hbm_gbs")
+        rec = {"value": rate, "unit": "cell-updates/s", "ms_per_step": ms / ex, "leaves": t.size,
+               "roofline": {"bound": "hbm", "achieved": alg * rate / 1e9, "peak": hbm, "unit": "GB/s",
+                            "frac": alg * rate / 1e9 / hbm if hbm else None,
+                            "algorithmic_bytes_per_cell_update": alg,
+                            "note": "each stage reads its input and u^n and writes its output once (halo "
+                                    "exchanges and neighbour reads beside)"}}
+        if with_cpu:
+            from oracle import oracle as O
+
+            O.build()
+            threads = os.cpu_count() or 1
+            O.set_threads(threads)
+            o = O.OracleTree(2, S["n"], S["halo"], S["depth"], 40000)
+            o.refine_all(S["level"])
+            o.set_state(u0)
+            o.halo_exchange()
+            c0 = time.perf_counter()
+            _, cex = o.ssprk_advance(S["cpu_steps"], order, S["velocity"], S["cfl"])
+            csec = time.perf_counter() - c0
+            g = A.Tree(2, S["n"], S["halo"], S["depth"], capacity=20000, dtype=A.F64, stream=stream.cuda_stream)
+            g.refine_uniform(S["level"])
+            g.upload_state(u0)
+            g.halo_exchange()
+            g.advance_ssprk(S["cpu_steps"], order, S["velocity"], S["cfl"])
+            g.finish_advance()
+            rec["cpu_baseline"] = {"value": cex * o.size * S["n"] ** 2 / csec, "unit": "cell-updates/s",
+                                   "cores": threads, "kind": "port",
+                                   "sample": f"first {S['cpu_steps']} steps of the same tree, OpenMP over patches"}
+            rec["parity_first_steps_bit_exact"] = bool(np.array_equal(g.download_state(), o.state()))
+            g.close()
+        t.close()
+        out[f"ssprk{order}"] = rec
+    return out
+
+
 # ------------------------------------------------------------ adjoint form
 ADJOINT = dict(n=16, halo=1, depth=8, base_level=5, max_level=7, rthr=0.01, cthr=0.002, rounds=3, steps=400,
                every=20, cfl=0.4, velocity=(1.0, 0.5), directions=64, eps=1e-4, pert=0.05, seed=7)
@@ -918,6 +987,7 @@ def gpu_arm(args, rank, world):
             "vtk_writer": lambda: vtk_extra(torch, A, dev, stream, with_cpu=cpu),
             "plain_fp64_config2_max_level7": lambda: depth7_extra(torch, A, dev, stream, flush, max(1, args.steps)),
             "euler_benchmark": lambda: euler_extra(torch, A, stream, with_cpu=cpu),
+            "ssprk_advection": lambda: ssprk_extra(torch, A, stream, with_cpu=cpu),
         }
         for name, fn in table.items():
             if args.extra is None or name in args.extra:

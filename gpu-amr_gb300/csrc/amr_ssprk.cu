@@ -15,57 +15,80 @@
 //     SSPRK2 stage 1   u' = ((u^n + u*) + R dt) * 0.5
 //     SSPRK3 stage 1   u2 = u^n * 0.75 + (u1 + R dt) * 0.25
 //     SSPRK3 stage 2   u' = u^n * (1/3) + (u2 + R dt) * (2/3)
+#include <cmath>
+
 #include "amr_ssprk.cuh"
 
 namespace amr_gb300 {
 namespace {
 
+// x / dx for a cell size of level `lev`: dx = dx_root / 2^lev exactly (a
+// power-of-two scaling).  When dx_root is itself a power of two, dx is one
+// and x * (1 / dx) equals x / dx bit for bit (the reciprocal is exact), so
+// the division becomes a multiplication; otherwise the division stays.
+struct InvDx {
+    double dx, inv;
+    bool   pow2;
+};
+
+__device__ __forceinline__ double div_dx(double x, const InvDx& c) { return c.pow2 ? x * c.inv : x / c.dx; }
+
+// One block per patch (grid-stride over patches), threads over the padded
+// cells of the patch.
 template <int R>
 __global__ void __launch_bounds__(256)
 k_ssprk_stage(const double* __restrict__ in, const double* __restrict__ un, double* __restrict__ out,
-              const uint64_t* __restrict__ keys, long long total, Geo g, const double* __restrict__ vel,
-              const double* __restrict__ step_dt, int mode)
+              const uint64_t* __restrict__ keys, int P, Geo g, const double* __restrict__ vel,
+              const double* __restrict__ step_dt, int mode, unsigned pow2_mask)
 {
-    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
-         t += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const long long p  = t / g.flat;
-        const int       li = static_cast<int>(t - p * g.flat);
-        const uint64_t  key  = keys[p];
-        const int       inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
-        const int       lev  = key_level(key);
-        const double    dt   = step_dt[inst];
-        const double*   a    = in + p * g.flat;
-        int             r = li, interior = 1;
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        const uint64_t key  = keys[p];
+        const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+        const int      lev  = key_level(key);
+        const double   dt   = step_dt[inst];
+        InvDx          cdx[R];
+        double         v[R];
 #pragma unroll
-        for (int L = R - 1; L >= 0; --L) {
-            const int c = r % g.P1;
-            r /= g.P1;
-            if (c < g.h || c >= g.n + g.h) interior = 0;
+        for (int d = 0; d < R; ++d) {
+            cdx[d].dx   = cell_size(g, d, lev);
+            cdx[d].pow2 = (pow2_mask >> d) & 1u;
+            cdx[d].inv  = 1.0 / cdx[d].dx;
+            v[d]        = vel[3 * inst + d];
         }
-        const double uc = a[li];
-        double       Rs = 0.0;
-        if (interior) {
+        const size_t  pb = static_cast<size_t>(p) * g.flat;
+        const double* a  = in + pb;
+        for (int li = threadIdx.x; li < g.flat; li += blockDim.x) {
+            int r = li, interior = 1;
 #pragma unroll
-            for (int d = 0; d < R; ++d) {
-                const int    st = g.s[R - 1 - d]; // Morton axis d
-                const double v  = vel[3 * inst + d];
-                const double uL = a[li - st];
-                const double uR = a[li + st];
-                const double sp = fabs(v);
-                const double fL = 0.5 * (uL * v + uc * v) - 0.5 * sp * (uc - uL);
-                const double fR = 0.5 * (uc * v + uR * v) - 0.5 * sp * (uR - uc);
-                Rs -= (fR - fL) / cell_size(g, d, lev);
+            for (int L = R - 1; L >= 0; --L) {
+                const int c = r % g.P1;
+                r /= g.P1;
+                if (c < g.h || c >= g.n + g.h) interior = 0;
             }
+            const double uc = a[li];
+            double       Rs = 0.0;
+            if (interior) {
+#pragma unroll
+                for (int d = 0; d < R; ++d) {
+                    const int    st = g.s[R - 1 - d]; // Morton axis d
+                    const double uL = a[li - st];
+                    const double uR = a[li + st];
+                    const double sp = fabs(v[d]);
+                    const double fL = 0.5 * (uL * v[d] + uc * v[d]) - 0.5 * sp * (uc - uL);
+                    const double fR = 0.5 * (uc * v[d] + uR * v[d]) - 0.5 * sp * (uR - uc);
+                    Rs -= div_dx(fR - fL, cdx[d]);
+                }
+            }
+            const double Rdt = Rs * dt;
+            const double b   = un[pb + li];
+            double       res;
+            if (!(dt > 0.0)) res = mode == 0 ? uc : b; // a step past the time limit leaves the state as it is
+            else if (mode == 0) res = uc + Rdt;
+            else if (mode == 2) res = (b + uc + Rdt) * 0.5;
+            else if (mode == 31) res = b * 0.75 + (uc + Rdt) * 0.25;
+            else res = b * (1.0 / 3.0) + (uc + Rdt) * (2.0 / 3.0);
+            out[pb + li] = res;
         }
-        const double Rdt = Rs * dt;
-        const double b   = un[p * g.flat + li];
-        double       res;
-        if (!(dt > 0.0)) res = mode == 0 ? uc : b; // a step past the time limit leaves the state as it is
-        else if (mode == 0) res = uc + Rdt;
-        else if (mode == 2) res = (b + uc + Rdt) * 0.5;
-        else if (mode == 31) res = b * 0.75 + (uc + Rdt) * 0.25;
-        else res = b * (1.0 / 3.0) + (uc + Rdt) * (2.0 / 3.0);
-        out[p * g.flat + li] = res;
     }
 }
 
@@ -73,13 +96,21 @@ k_ssprk_stage(const double* __restrict__ in, const double* __restrict__ un, doub
 
 cudaError_t ssprk_stage(const SsprkStage& s)
 {
-    const long long total = static_cast<long long>(s.P) * s.g.flat;
-    if (total <= 0) return cudaSuccess;
-    const unsigned grid = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 64));
+    if (s.P <= 0) return cudaSuccess;
+    // axes whose root cell size is a power of two
+    unsigned mask = 0;
+    for (int d = 0; d < s.g.rank; ++d) {
+        int e = 0;
+        if (std::frexp(s.g.dx_root[d], &e) == 0.5) mask |= 1u << d;
+    }
+    const unsigned grid    = static_cast<unsigned>(std::min(s.P, 152 * 32));
+    const int      threads = s.g.flat >= 256 ? 256 : ((s.g.flat + 31) / 32) * 32;
     if (s.g.rank == 2)
-        k_ssprk_stage<2><<<grid, 256, 0, s.stream>>>(s.in, s.un, s.out, s.keys, total, s.g, s.vel, s.step_dt, s.mode);
+        k_ssprk_stage<2><<<grid, threads, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.vel, s.step_dt,
+                                                         s.mode, mask);
     else
-        k_ssprk_stage<3><<<grid, 256, 0, s.stream>>>(s.in, s.un, s.out, s.keys, total, s.g, s.vel, s.step_dt, s.mode);
+        k_ssprk_stage<3><<<grid, threads, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.vel, s.step_dt,
+                                                         s.mode, mask);
     return cudaGetLastError();
 }
 
