@@ -1308,7 +1308,7 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
                                                  const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode,
                                                  T* tiles, uint64_t* bars, int p, int nwarp)
 {
-    static_assert(D >= 2 && D <= 4, "two to four steps per pass");
+    static_assert(D >= 2 && D <= 6, "two to six steps per pass");
     using Sh                = Step2dShape<T, N, H>;
     constexpr int      P1   = Sh::P1;
     constexpr int      FLAT = Sh::FLAT;
@@ -1446,9 +1446,6 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
                 for (int bb = 1; a + bb <= D; ++bb)
                     cn[corner_index<D>(a, bb)] = dg[(uy > 0 ? H + a - 1 : N + H - a) * P1 + (ux > 0 ? H + bb - 1 : N + H - bb)];
         }
-        Coef2<T> cf[D];
-#pragma unroll
-        for (int m = 0; m < D; ++m) coef_of(m, sd0.row, cf[m]);
         if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
             if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
             phase ^= 1u << b;
@@ -1472,6 +1469,8 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         const int  src = inr ? (col ? nt : N + nt) : lane;
 #pragma unroll
         for (int m = 1; m <= D; ++m) {
+            Coef2<T> cf;
+            coef_of(m - 1, sd0.row, cf);
             if (has) tile[G0 * P1 + G1] = sa[1]; // u^{m-1} ghosts
             __syncwarp();
             T colv[SEG + 2];
@@ -1480,38 +1479,32 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
             T res[SEG];
 #pragma unroll
             for (int k = 0; k < SEG; ++k)
-                res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], cf[m - 1],
-                                  ux, uy);
+                res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], cf, ux,
+                                  uy);
             if (m < D) {
-                // strips and corner to u^m on the distances still needed
-                T tn[D], c1[D], r1[D];
+                // strips to u^m on the distances still needed, ascending: a
+                // lane's distance d+1 and its neighbours' distance d are
+                // still u^{m-1} when distance d is updated (the shuffles of
+                // distance d precede every lane's update of it)
 #pragma unroll
                 for (int d = 1; d <= D - m; ++d) {
-                    tn[d - 1] = __shfl_sync(0xffffffffu, sa[d], src);
-                    c1[d - 1] = __shfl_sync(0xffffffffu, cn[corner_index<D>(1, d)], 0);
-                    r1[d - 1] = __shfl_sync(0xffffffffu, cn[corner_index<D>(d, 1)], 0);
-                }
-#pragma unroll
-                for (int d = 1; d <= D - m; ++d) {
-                    const T tang = inr ? tn[d - 1] : (col ? c1[d - 1] : r1[d - 1]);
+                    const T tnb  = __shfl_sync(0xffffffffu, sa[d], src);
+                    const T c1   = __shfl_sync(0xffffffffu, cn[corner_index<D>(1, d)], 0);
+                    const T r1   = __shfl_sync(0xffffffffu, cn[corner_index<D>(d, 1)], 0);
+                    const T tang = inr ? tnb : (col ? c1 : r1);
                     const T nrm  = sa[d + 1];
-                    sa[d]        = upd2d<T>(sa[d], col ? nrm : tang, col ? tang : nrm, cf[m - 1], ux, uy);
+                    sa[d]        = upd2d<T>(sa[d], col ? nrm : tang, col ? tang : nrm, cf, ux, uy);
                 }
+                // the corner in place, by increasing distance a + b: a cell
+                // reads the cells at distance + 1, still u^{m-1}
                 if (NC > 0) {
-                    T nc[NC > 0 ? NC : 1];
 #pragma unroll
-                    for (int a = 1; a < D; ++a)
+                    for (int sum = 2; sum <= D - m; ++sum)
 #pragma unroll
-                        for (int bb = 1; a + bb <= D; ++bb)
-                            nc[corner_index<D>(a, bb)] = cn[corner_index<D>(a, bb)];
-#pragma unroll
-                    for (int a = 1; a < D; ++a)
-#pragma unroll
-                        for (int bb = 1; a + bb <= D - m; ++bb)
-                            nc[corner_index<D>(a, bb)] = upd2d<T>(cn[corner_index<D>(a, bb)], cn[corner_index<D>(a, bb + 1)],
-                                                                  cn[corner_index<D>(a + 1, bb)], cf[m - 1], ux, uy);
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) cn[c] = nc[c];
+                        for (int a = 1; a < sum; ++a)
+                            cn[corner_index<D>(a, sum - a)] =
+                                upd2d<T>(cn[corner_index<D>(a, sum - a)], cn[corner_index<D>(a, sum - a + 1)],
+                                         cn[corner_index<D>(a + 1, sum - a)], cf, ux, uy);
                 }
             }
             __syncwarp();

@@ -263,7 +263,11 @@ cudaError_t prepare_step2d()
                                      smem);
     };
     pass_attr.template operator()<2>();
-    if constexpr (sizeof(T) == 4) pass_attr.template operator()<4>();
+    if constexpr (sizeof(T) == 4) {
+        pass_attr.template operator()<3>();
+        pass_attr.template operator()<4>();
+        pass_attr.template operator()<5>();
+    }
     if (e == cudaSuccess) done.fetch_or(bit);
     return e;
 }
@@ -321,20 +325,33 @@ amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, 
     });
 }
 
-// Steps per pass on same-level trees: FP32 four (the pass is bound by the
-// per-patch work, which four steps share), FP64 two (its update is FP64-bound).
+// Steps per pass on same-level trees: FP32 five (a pass costs a fixed share,
+// the state's read and write and the per-patch work, plus a share per step),
+// FP64 two (its update is FP64-bound).
 template <typename T>
-constexpr int kPassSteps = sizeof(T) == 4 ? 4 : 2;
+constexpr int kPassSteps = sizeof(T) == 4 ? 5 : 2;
 
-// The pass depths covering k steps: passes of kPassSteps, then two, then one.
+// The pass depths covering k steps: as few passes as depth `deep` allows,
+// their depths as equal as possible (10 steps at depth 5: 5 + 5; 6: 3 + 3).
 inline void pass_plan(int k, int deep, std::vector<int>& plan)
 {
     plan.clear();
-    while (k > 0) {
-        const int d = k >= deep ? deep : (k >= 2 ? 2 : 1);
-        plan.push_back(d);
-        k -= d;
+    if (k <= 0) return;
+    const int np = (k + deep - 1) / deep;
+    for (int i = 0; i < np; ++i) plan.push_back(k / np + (i < k % np ? 1 : 0));
+}
+
+// Depth D of a pass as a template argument (FP32 2..5, FP64 2).
+template <typename T, typename F>
+amr_status with_depth(int D, F&& f)
+{
+    if constexpr (sizeof(T) == 4) {
+        if (D == 5) return f.template operator()<5>();
+        if (D == 4) return f.template operator()<4>();
+        if (D == 3) return f.template operator()<3>();
     }
+    if (D == 2) return f.template operator()<2>();
+    return fail(AMR_ERR_INVALID, "unsupported pass depth");
 }
 
 // D steps per pass (same-level trees): coefficient rows of step m at coef +
@@ -840,11 +857,10 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         const size_t  cst = static_cast<size_t>(K) * nl;
         amr_status    st  = AMR_OK;
         auto pass = [&]<int N>() -> amr_status {
-            if constexpr (sizeof(T) == 4)
-                if (D == 4) return launch_run_step2d_pass<T, N, 1, 4>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
-                                                                     static_cast<int>(t->cap), cs);
-            return launch_run_step2d_pass<T, N, 1, 2>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
-                                                      static_cast<int>(t->cap), cs);
+            return with_depth<T>(D, [&]<int DD>() -> amr_status {
+                return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
+                                                           static_cast<int>(t->cap), cs);
+            });
         };
         if (D > 1) st = g.n == 16 ? pass.template operator()<16>() : pass.template operator()<8>();
         else if (key.W > 0 && g.n == 16)
@@ -1713,10 +1729,12 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
         first = false;
         const bool shape2d = t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8);
         const int  deep    = t->dtype == AMR_F32 ? kPassSteps<float> : kPassSteps<double>;
-        for (int k = 0; k < chunk;) {
-            // several steps per pass where every relation is same-level
-            const int  left = chunk - k;
-            const int  D    = (shape2d && t->uniform) ? (left >= deep ? deep : (left >= 2 ? 2 : 1)) : 1;
+        std::vector<int> plan;
+        if (shape2d && t->uniform) pass_plan(chunk, deep, plan); // several steps per pass where every relation is same-level
+        else plan.assign(static_cast<size_t>(chunk), 1);
+        size_t pi = 0;
+        for (int k = 0; k < chunk; ++pi) {
+            const int  D    = plan[pi];
             const bool pair = D > 1;
             std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
             if (t->timing) {
@@ -1741,12 +1759,10 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                 if (pair) {
                     const size_t cst  = static_cast<size_t>(K) * nl;
                     auto         pass = [&]<int N>(const StepCfg& c) -> amr_status {
-                        if constexpr (sizeof(T) == 4)
-                            if (D == 4)
-                                return launch_step2d_pass<T, N, 1, 4>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
-                                                                      t->status + 7, t->keys[t->tb], uleaf, c, s);
-                        return launch_step2d_pass<T, N, 1, 2>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
-                                                              t->status + 7, t->keys[t->tb], uleaf, c, s);
+                        return with_depth<T>(D, [&]<int DD>() -> amr_status {
+                            return launch_step2d_pass<T, N, 1, DD>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
+                                                                   t->status + 7, t->keys[t->tb], uleaf, c, s);
+                        });
                     };
                     return t->g.n == 16 ? pass.template operator()<16>(cfg_pair) : pass.template operator()<8>(StepCfg{});
                 }
