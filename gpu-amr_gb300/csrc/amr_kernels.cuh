@@ -1741,25 +1741,34 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
             tile[b0 * P1 + b1] = gv1;
         }
         __syncwarp();
-        int any = 0, all = 1;
-        T   colv[SEG + 2];
+        // Both decisions depend on the lane's largest squared gradient only
+        // (refine: some cell at or above the threshold; coarsen: every cell
+        // below it), so the FP32 maximum decides them when it lies outside
+        // both bands and every FP32 value is finite; otherwise each cell is
+        // evaluated exactly.  Same outcome as a per-cell decision.
+        int   any = 0, all = 1;
+        T     colv[SEG + 2];
+        float smax = 0.0f;
+        bool  bad  = false;
 #pragma unroll
         for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
-            const int idx = (r0 + k) * P1 + cl;
-            const T   xl = tile[idx - 1], xh = tile[idx + 1], yl = colv[k], yh = colv[k + 2];
-            bool      done = false;
-            if (rule.fast) {
-                const float s = grad_sq_f32_2<T>(xl, xh, yl, yh);
-                if (isfinite(s) && (s >= rule.r_hi || s < rule.r_lo) && (s < rule.c_lo || s >= rule.c_hi)) {
-                    if (s >= rule.r_hi) any = 1;
-                    if (s >= rule.c_hi) all = 0;
-                    done = true;
-                }
-            }
-            if (!done) {
-                const double s = grad_sq_exact2<T>(xl, xh, yl, yh);
+            const int   idx = (r0 + k) * P1 + cl;
+            const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
+            smax            = fmaxf(smax, s);
+            bad |= !(fabsf(s) < INFINITY);
+        }
+        const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
+                           (smax < rule.c_lo || smax >= rule.c_hi);
+        if (known) {
+            any = smax >= rule.r_hi ? 1 : 0;
+            all = smax < rule.c_lo ? 1 : 0;
+        } else {
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                const int    idx = (r0 + k) * P1 + cl;
+                const double s   = grad_sq_exact2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
                 if (s >= rule.rsq) any = 1;
                 if (!(s < rule.csq)) all = 0;
             }
