@@ -174,7 +174,7 @@ k_run_flags_grad(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, in
 
 // 2D gradient flags of the sized kernel (flags2d_body), ghosts on the fly.
 template <typename T, int N, int H>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_run_flags2d(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int max_level, int sp)
 {
     if (ctl->err) return;

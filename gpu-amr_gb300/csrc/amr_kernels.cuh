@@ -1798,7 +1798,7 @@ __device__ __forceinline__ void flags2d_smem(unsigned char* smem, int W, T*& til
 }
 
 template <typename T, int N, int H, bool FromBuffer>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_flags2d(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys, int P,
           Geo g, GradRule rule, int min_level, int max_level, const int32_t* __restrict__ bounds,
           int8_t* __restrict__ flags, int32_t* err)
