@@ -47,6 +47,7 @@ struct RunBufs {
     const double*  vel;        // per instance x3, or null (launch-wide upwind sides)
     const int32_t* upcode;     // per instance packed upwind offsets (with vel), or null
     const int32_t* bounds;     // per instance (min, max) level bounds, or null
+    int4*          prec;       // pass records of the current tree (multi-step passes)
     uint32_t*      tile_sums;  // scan partials, one per tile
     unsigned long long cap;
     int            ninst;
@@ -74,24 +75,35 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
                             coef, coef32, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars, p, nwarp);
 }
 
+// Pass records of the current tree (first kernel of an interval run with
+// multi-step passes, after the guard).
+__global__ void __launch_bounds__(256) k_run_pass_records(RunBufs B, RunCtl* ctl, Geo g, int upx0, int upy0)
+{
+    if (ctl->err) return;
+    const int P = ctl->P, tb = ctl->tb;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P; q += gridDim.x * blockDim.x)
+        pass_record(B.meta[tb], B.keys[tb], B.upcode, upx0, upy0, g, q, B.prec, &ctl->err);
+}
+
 // D steps per pass (trees of same-level relations only; the interval's
-// guard has checked ctl->uniform).  parity selects the buffers of this pass.
+// guard has checked ctl->uniform and k_run_pass_records has built the
+// records).  parity selects the buffers of this pass.
 template <typename T, int N, int H, int W, int S, int D>
-__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_run_step2d_pass(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
-                  size_t cstride, int parity, int upx0, int upy0)
+__global__ void __launch_bounds__(W * 32, Pass2dOcc<T, W>::blocks)
+k_run_step2d_pass(RunBufs B, RunCtl* ctl, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+                  size_t cstride, int parity)
 {
     if (ctl->err) return;
     extern __shared__ __align__(128) unsigned char smem[];
     T*        tiles;
+    T*        xy;
     uint64_t* bars;
-    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
-    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    pass2d_smem<T, N, H, W, S>(smem, tiles, xy, bars);
+    const int P = ctl->P, s = ctl->sb ^ parity;
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pass_body<T, N, H, S, D>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb], P,
-                                    g, coef, coef32, cstride, upx0, upy0, &ctl->err, B.keys[tb], B.upcode, tiles, bars,
-                                    p, nwarp);
+    step2d_pass_body<T, N, H, S, D>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.prec, P,
+                                    coef, coef32, cstride, &ctl->err, tiles, xy, bars, p, nwarp);
 }
 
 // First kernel of an interval captured with multi-step passes: when a re-mesh

@@ -1044,19 +1044,31 @@ struct Coef2<float> {
 // FP64: c0 u + c_x u_x + c_y u_y.  Every 2D update goes through this one
 // function, so fused and separate steps round alike.
 template <typename T>
-__device__ __forceinline__ T upd2d(T u, T xn, T yn, const Coef2<T>& cf, int ux, int uy)
+__device__ __forceinline__ T upd2d_core(T u, T xn, T yn, const Coef2<T>& cf, bool xu, bool yu)
 {
     if constexpr (sizeof(T) == 4) {
         float acc = u;
-        if (ux != 0) acc = fmaf(cf.cx, xn - u, acc);
-        if (uy != 0) acc = fmaf(cf.cy, yn - u, acc);
+        if (xu) acc = fmaf(cf.cx, xn - u, acc);
+        if (yu) acc = fmaf(cf.cy, yn - u, acc);
         return acc;
     } else {
         T acc = static_cast<T>(cf.c0) * u;
-        if (ux != 0) acc = fma(static_cast<T>(cf.cx), xn, acc);
-        if (uy != 0) acc = fma(static_cast<T>(cf.cy), yn, acc);
+        if (xu) acc = fma(static_cast<T>(cf.cx), xn, acc);
+        if (yu) acc = fma(static_cast<T>(cf.cy), yn, acc);
         return acc;
     }
+}
+template <typename T>
+__device__ __forceinline__ T upd2d(T u, T xn, T yn, const Coef2<T>& cf, int ux, int uy)
+{
+    return upd2d_core<T>(u, xn, yn, cf, ux != 0, uy != 0);
+}
+// The same update with the upwind axes known at compile time (the multi-step
+// pass branches once per patch on them).
+template <typename T, bool XU, bool YU>
+__device__ __forceinline__ T upd2d_fixed(T u, T xn, T yn, const Coef2<T>& cf)
+{
+    return upd2d_core<T>(u, xn, yn, cf, XU, YU);
 }
 
 // coef: the full rows (FP64 path); coef32: (c_x, c_y) rows (FP32 path);
@@ -1272,6 +1284,59 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
     }
 }
 
+// ------------------------------------------------ pass records
+// One 16-byte record per leaf for the multi-step pass: the same-level
+// neighbours across the upwind x face (x) and y face (y), the x-neighbour's
+// y-neighbour (z: the diagonal whose corner reaches the patch within a
+// pass), and the upwind offsets with the coefficient row packed into w.  A
+// zero velocity component names the patch itself.  The records are built
+// once per mesh and velocity field, so the pass reads one record per patch
+// instead of a chain of dependent face-record loads.  A face that is not
+// same-level sets AMR_ERR_UNBALANCED (passes run only where every relation
+// is same-level).
+__host__ __device__ __forceinline__ int pass_code(int ux, int uy, int row) { return (row << 4) | ((ux + 1) << 2) | (uy + 1); }
+__host__ __device__ __forceinline__ int pass_ux(int code) { return ((code >> 2) & 3) - 1; }
+__host__ __device__ __forceinline__ int pass_uy(int code) { return (code & 3) - 1; }
+__host__ __device__ __forceinline__ int pass_row(int code) { return code >> 4; }
+
+__device__ __forceinline__ void pass_record(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
+                                            const int32_t* __restrict__ upcode, int upx0, int upy0, const Geo& g,
+                                            int q, int4* __restrict__ rec, int32_t* err)
+{
+    const uint64_t key  = keys[q];
+    const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+    int            ux = upx0, uy = upy0;
+    if (upcode) {
+        const int32_t code = upcode[inst];
+        ux                 = unpack_upwind(code, 0);
+        uy                 = unpack_upwind(code, 1);
+    }
+    auto same = [&](const amr_halo_meta& m, int self) {
+        if (m.relation != REL_SAME) {
+            atomicExch(err, static_cast<int32_t>(AMR_ERR_UNBALANCED));
+            return self;
+        }
+        return m.neighbor;
+    };
+    int4 r;
+    r.x    = ux != 0 ? same(meta[static_cast<size_t>(q) * 4 + 2 + (ux > 0 ? 1 : 0)], q) : q;
+    r.y    = uy != 0 ? same(meta[static_cast<size_t>(q) * 4 + (uy > 0 ? 1 : 0)], q) : q;
+    r.z    = ux != 0 && uy != 0 ? same(meta[static_cast<size_t>(r.x) * 4 + (uy > 0 ? 1 : 0)], r.x) : q;
+    r.w    = pass_code(ux, uy, inst * (g.depth + 1) + key_level(key));
+    rec[q] = r;
+}
+
+// Host-driven build: P leaves, upwind offsets per instance (upcode) or
+// launch-wide (upx0, upy0).
+__global__ void __launch_bounds__(256)
+k_pass_records(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
+               const int32_t* __restrict__ upcode, int upx0, int upy0, int P, Geo g, int4* __restrict__ rec,
+               int32_t* err)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P; q += gridDim.x * blockDim.x)
+        pass_record(meta, keys, upcode, upx0, upy0, g, q, rec, err);
+}
+
 // ------------------------------------------------ 2D update, D steps per pass
 // D consecutive steps of a tree whose every neighbour relation is "same
 // level" (each instance uniform, as in the batched forests), in one pass over
@@ -1285,13 +1350,28 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
 // halo exchange of a same-level neighbour is a copy), so the result is
 // bit-identical.
 //
-// Lanes 0..N-1 own ghost-column row i = lane, lanes N..2N-1 ghost-row column
-// j = lane - N; each holds its strip s[1..D] (s[d] = the ghost cell at upwind
-// distance d).  Lane 0 holds the corner triangle.  After step m the strips
-// and the corner advance one step on the distances still needed (d <= D-m).
-// Metadata pipeline as in step2d_body (key three patches ahead, neighbour
-// record two ahead, strips and the diagonal's index one ahead, the corner
-// before the tile wait); coefficient rows of the D steps are read at use.
+// Between the tile load and the write-back the cells stay in registers, in
+// upwind-normalized coordinates: on an axis whose upwind side is + the
+// normalized index i' is N-1-i (i the interior index), otherwise i, so a
+// cell's upwind neighbours are always at i'-1 and j'-1.  Lane (r, c) =
+// (lane / 8, lane % 8) owns the BR x BC block of normalized rows r*BR..,
+// columns c*BC..  Per step only block edges cross lanes, through two small
+// shared buffers per warp: X[c][i'] holds, for normalized row i', the cell
+// left of block column c (normalized column c*BC-1, the distance-1 ghost for
+// c = 0); Y[r][j'] the cell above block row r.  Each lane stores its last
+// column and its last row (one vector store each) and loads its block's
+// upwind edges (one vector load each); the buffers alternate between steps,
+// so one warp barrier per step orders them.
+//
+// Strips: lanes 0..N-1 hold the ghost column of normalized row lane, lanes
+// N..2N-1 the ghost row of normalized column lane-N; each holds s[1..D]
+// (s[d] = the ghost cell at upwind distance d) and stores s[1] into X[0] /
+// Y[0] every step.  Lanes 0 and N hold the corner triangle.  After step m
+// the strips and the corner advance one step on the distances still needed
+// (d <= D-m).  Per patch the warp reads its pass record two patches ahead,
+// its strips one ahead and the corner before the tile wait; the steps branch
+// once on which velocity components are non-zero, and each step's
+// coefficient row is read one step ahead.
 template <int D>
 __host__ __device__ constexpr int corner_index(int a, int b)
 {
@@ -1300,20 +1380,90 @@ __host__ __device__ constexpr int corner_index(int a, int b)
     return base + (b - 1);
 }
 
+// Warp layout and shared memory of the multi-step pass.
+template <typename T, int N, int H>
+struct PassShape {
+    using Sh                = Step2dShape<T, N, H>;
+    static constexpr int RB = 4, CB = 8;           // block rows and block columns of the warp
+    static constexpr int BR = N / RB, BC = N / CB; // cells of a lane's block
+    // X rows are padded by 16 bytes: the lanes of one block row store and
+    // load X rows c = 0..7 at the same offset, and the padding spreads them
+    // over distinct banks (Y rows are contiguous across lanes already)
+    static constexpr int XN = N + 16 / static_cast<int>(sizeof(T));
+    static constexpr int XS = (CB + 1) * XN;       // X[c][i'], c = 0..CB
+    static constexpr int YS = (RB + 1) * N;        // Y[r][j'], r = 0..RB
+    static constexpr int XY = 2 * (XS + YS);       // elements per warp: two of each
+    static_assert(BR * RB == N && BC * CB == N, "patch edge must be a multiple of 8");
+    static_assert((XS * sizeof(T)) % 16 == 0 && (YS * sizeof(T)) % 16 == 0, "exchange buffers stay 16-byte aligned");
+    // dynamic shared memory of a block of W warps with S tiles each: the
+    // tiles, the exchange buffers, the barriers
+    static constexpr size_t smem(int W, int S)
+    {
+        return static_cast<size_t>(W) * (S * (Sh::TILE + 8) + XY * sizeof(T));
+    }
+};
+
+// K consecutive shared-memory elements moved as the widest aligned vectors
+// (callers' offsets are multiples of K elements).
+template <typename T, int K>
+__device__ __forceinline__ void lds_vec(const T* p, T (&v)[K])
+{
+    if constexpr ((K * sizeof(T)) % 16 == 0) {
+#pragma unroll
+        for (int i = 0; i < static_cast<int>(K * sizeof(T) / 16); ++i) {
+            if constexpr (sizeof(T) == 4) {
+                const float4 w = reinterpret_cast<const float4*>(p)[i];
+                v[4 * i]       = w.x;
+                v[4 * i + 1]   = w.y;
+                v[4 * i + 2]   = w.z;
+                v[4 * i + 3]   = w.w;
+            } else {
+                const double2 w = reinterpret_cast<const double2*>(p)[i];
+                v[2 * i]        = w.x;
+                v[2 * i + 1]    = w.y;
+            }
+        }
+    } else if constexpr (sizeof(T) == 4 && K == 2) {
+        const float2 w = *reinterpret_cast<const float2*>(p);
+        v[0]           = w.x;
+        v[1]           = w.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) v[i] = p[i];
+    }
+}
+template <typename T, int K>
+__device__ __forceinline__ void sts_vec(T* p, const T (&v)[K])
+{
+    if constexpr ((K * sizeof(T)) % 16 == 0) {
+#pragma unroll
+        for (int i = 0; i < static_cast<int>(K * sizeof(T) / 16); ++i) {
+            if constexpr (sizeof(T) == 4)
+                reinterpret_cast<float4*>(p)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            else
+                reinterpret_cast<double2*>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+        }
+    } else if constexpr (sizeof(T) == 4 && K == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) p[i] = v[i];
+    }
+}
+
 template <typename T, int N, int H, int S, int D>
 __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __restrict__ out,
-                                                 const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
-                                                 const Coef* __restrict__ coef, const float2* __restrict__ coef32,
-                                                 size_t cstride, int upx0, int upy0, int32_t* err,
-                                                 const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode,
-                                                 T* tiles, uint64_t* bars, int p, int nwarp)
+                                                                                                  const int4* __restrict__ rec, int P, const Coef* __restrict__ coef,
+                                                 const float2* __restrict__ coef32, size_t cstride, int32_t* err,
+                                                 T* tiles, T* xy, uint64_t* bars, int p, int nwarp)
 {
     static_assert(D >= 2 && D <= 6, "two to six steps per pass");
     using Sh                = Step2dShape<T, N, H>;
+    using Ps                = PassShape<T, N, H>;
     constexpr int      P1   = Sh::P1;
     constexpr int      FLAT = Sh::FLAT;
     constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
-    constexpr int      SEG  = Sh::SEG;
+    constexpr int      BR = Ps::BR, BC = Ps::BC, XN = Ps::XN, XS = Ps::XS, YS = Ps::YS;
     constexpr int      NC   = D * (D - 1) / 2; // corner cells
     const int          lane = threadIdx.x & 31;
     if (lane == 0) {
@@ -1332,20 +1482,14 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         for (int j = 0; j < S - 1; ++j)
             if (p + j * nwarp < P) request(p + j * nwarp, j);
     uint32_t   phase = 0;
-    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
-    const int  nl = g.depth + 1;
-    const bool col = lane < N;
-    const bool job = lane < 2 * N;
-    const int  L   = col ? 1 : 0;
-    const int  tg  = (col ? lane : lane - N) + H; // tangential padded coordinate of the lane's strip
+    const int  rb = lane >> 3, cb = lane & 7; // the lane's block
+    const bool col  = lane < N;              // ghost-column strip of normalized row `lane`
+    const bool job  = lane < 2 * N;
+    const int  sl   = col ? lane : lane - N; // normalized tangential index of the lane's strip
+    const bool inr  = sl > 0;                // tangential upwind neighbour: the previous strip lane, else the corner
+    const int  src  = inr ? lane - 1 : lane;
+    const bool hold = lane == 0 || lane == N; // corner holders
 
-    struct Side {
-        int ux, uy, row; // upwind offsets, coefficient row (instance, level)
-    };
-    struct Rec {
-        int nb;   // same-level neighbour across the lane's ghost face
-        int diag; // lane 0: the x-neighbour's y-neighbour (one patch ahead)
-    };
     auto coef_of = [&](int step, int row, Coef2<T>& c) {
         if constexpr (sizeof(T) == 4) {
             const float2 v = coef32[step * cstride + row];
@@ -1358,88 +1502,52 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
             c.cy          = v.c[1];
         }
     };
-    auto side_of = [&](uint64_t key, Side& sd) {
-        const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
-        sd.ux          = upx0;
-        sd.uy          = upy0;
-        if (upcode) {
-            const int32_t code = upcode[inst];
-            sd.ux              = unpack_upwind(code, 0);
-            sd.uy              = unpack_upwind(code, 1);
-        }
-        sd.row = inst * nl + key_level(key);
-    };
-    auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
-    auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
-    // neighbour index of a face record; the patch itself (and the error
-    // flag) when the record is not same-level, which the host rules out
-    auto same_nb = [&](const amr_halo_meta* rp, int self) {
-        if (rp->relation != REL_SAME) {
-            atomicExch(err, static_cast<int32_t>(AMR_ERR_UNBALANCED));
-            return self;
-        }
-        return rp->neighbor;
-    };
-    auto rec_of = [&](int q, const Side& sd, Rec& m) {
-        m.nb   = q;
-        m.diag = q;
-        if (has_job(sd)) m.nb = same_nb(meta + static_cast<size_t>(q) * 4 + 2 * L + pos_of(sd), q);
-    };
-    // one patch ahead: the lane's strip (u^n at distances 1..D) and lane 0's
-    // diagonal index
-    auto fetch = [&](const Side& sd, Rec& m, T* v) {
+    auto has_job = [&](int ux, int uy) { return job && (col ? ux != 0 : uy != 0); };
+    // one patch ahead: the lane's strip (u^n at distances 1..D, at the actual
+    // tangential coordinate of its normalized index)
+    auto fetch = [&](const int4& r, T* v) {
 #pragma unroll
         for (int d = 1; d <= D; ++d) v[d] = T(0);
-        if (!has_job(sd)) return;
-        const int pos = pos_of(sd);
-        const T*  nbp = in + static_cast<size_t>(m.nb) * FLAT;
+        const int ux = pass_ux(r.w), uy = pass_uy(r.w);
+        if (!has_job(ux, uy)) return;
+        const int pos = col ? (ux > 0 ? 1 : 0) : (uy > 0 ? 1 : 0);
+        const int tg  = ((col ? uy : ux) > 0 ? N - 1 - sl : sl) + H;
+        const T*  nbp = in + static_cast<size_t>(col ? r.x : r.y) * FLAT;
 #pragma unroll
         for (int d = 1; d <= D; ++d) {
             const int line = pos ? H + d - 1 : N + H - d; // the neighbour's line at distance d
             v[d]           = nbp[col ? tg * P1 + line : line * P1 + tg];
         }
-        if (lane == 0 && sd.uy != 0)
-            m.diag = same_nb(meta + static_cast<size_t>(m.nb) * 4 + (sd.uy > 0 ? 1 : 0), m.nb);
     };
 
-    const int q1 = p + nwarp, q2 = p + 2 * nwarp;
-    Side      sd0{}, sd1{}, sd2{};
-    Rec       m0{}, m1{}, m2{};
+    // records two patches ahead, strips one ahead
+    const int q1 = p + nwarp;
+    int4      r0{}, r1{}, r2{};
     T         sa[D + 1], sb[D + 1]; // strips of this patch and the next
-    uint64_t  k2 = 0;
 #pragma unroll
     for (int d = 0; d <= D; ++d) sa[d] = sb[d] = T(0);
     if (p < P) {
-        side_of(keys[p], sd0);
-        rec_of(p, sd0, m0);
-        fetch(sd0, m0, sa);
+        r0 = __ldg(rec + p);
+        fetch(r0, sa);
     }
-    if (q1 < P) {
-        side_of(keys[q1], sd1);
-        rec_of(q1, sd1, m1);
-    }
-    if (q2 < P) k2 = keys[q2];
+    if (q1 < P) r1 = __ldg(rec + q1);
+    // the strip's distance-1 ghost in X[0] / Y[0] of the first buffer
+    T* const gx = xy + (col ? sl : XS + sl);
 
     for (int it = 0; p < P; ++it, p += nwarp) {
         const int b  = it % S;
         const int pf = p + (S - 1) * nwarp;
         if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
-        const int pa = p + nwarp, pb = p + 2 * nwarp, pc = p + 3 * nwarp;
-        uint64_t  k3 = 0;
-        if (pc < P) k3 = keys[pc];
-        if (pb < P) {
-            side_of(k2, sd2);
-            rec_of(pb, sd2, m2);
-        }
-        if (pa < P) fetch(sd1, m1, sb);
+        const int pa = p + nwarp, pb = p + 2 * nwarp;
+        if (pb < P) r2 = __ldg(rec + pb);
+        if (pa < P) fetch(r1, sb);
         // this patch
-        const int ux = sd0.ux, uy = sd0.uy;
-        const int igp = uy > 0 ? N + H : H - 1, jgp = ux > 0 ? N + H : H - 1; // distance-1 ghost row / column
+        const int ux = pass_ux(r0.w), uy = pass_uy(r0.w), row = pass_row(r0.w);
         T         cn[NC > 0 ? NC : 1];
 #pragma unroll
         for (int c = 0; c < (NC > 0 ? NC : 1); ++c) cn[c] = T(0);
-        if (lane == 0 && ux != 0 && uy != 0) {
-            const T* dg = in + static_cast<size_t>(m0.diag) * FLAT;
+        if (hold && ux != 0 && uy != 0) {
+            const T* dg = in + static_cast<size_t>(r0.z) * FLAT;
 #pragma unroll
             for (int a = 1; a < D; ++a)
 #pragma unroll
@@ -1451,79 +1559,113 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
             phase ^= 1u << b;
             for (int j = 1; j < S; ++j)
                 if (p + j * nwarp < P) {
-                    const int sl = (it + j) % S;
-                    mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u);
-                    phase ^= 1u << sl;
+                    const int sl2 = (it + j) % S;
+                    mbar_wait_bounded(&bars[sl2], (phase >> sl2) & 1u);
+                    phase ^= 1u << sl2;
                 }
             return;
         }
         phase ^= 1u << b;
         T*         tile = tiles + static_cast<size_t>(b) * FLAT;
-        const bool has  = has_job(sd0);
-        const int  G0 = col ? tg : igp, G1 = col ? jgp : tg; // the lane's distance-1 ghost cell
-        // tangential neighbour of the lane's strip cells: the next strip lane,
-        // or (past the patch edge) the corner
-        const int  ti  = tg - H;
-        const int  nt  = ti + (col ? uy : ux);
-        const bool inr = nt >= 0 && nt < N;
-        const int  src = inr ? (col ? nt : N + nt) : lane;
+        const bool has  = has_job(ux, uy);
+        // the lane's block: normalized cell (rb*BR + a, cb*BC + e) is the
+        // tile cell cell[a * sr + e * sc]
+        const int sr = uy > 0 ? -P1 : P1, sc = ux > 0 ? -1 : 1;
+        T*        cell = tile + (H + (uy > 0 ? N - 1 - rb * BR : rb * BR)) * P1 + H + (ux > 0 ? N - 1 - cb * BC : cb * BC);
+        T         v[BR][BC];
 #pragma unroll
-        for (int m = 1; m <= D; ++m) {
-            Coef2<T> cf;
-            coef_of(m - 1, sd0.row, cf);
-            if (has) tile[G0 * P1 + G1] = sa[1]; // u^{m-1} ghosts
-            __syncwarp();
-            T colv[SEG + 2];
+        for (int a = 0; a < BR; ++a)
 #pragma unroll
-            for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
-            T res[SEG];
+            for (int e = 0; e < BC; ++e) v[a][e] = cell[a * sr + e * sc];
+        // the D steps, compiled once per combination of upwind axes
+        auto steps = [&]<bool XU, bool YU>() {
+            Coef2<T> cf, cfn;
+            coef_of(0, row, cf);
 #pragma unroll
-            for (int k = 0; k < SEG; ++k)
-                res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], cf, ux,
-                                  uy);
-            if (m < D) {
-                // strips to u^m on the distances still needed, ascending: a
-                // lane's distance d+1 and its neighbours' distance d are
-                // still u^{m-1} when distance d is updated (the shuffles of
-                // distance d precede every lane's update of it)
+            for (int m = 1; m <= D; ++m) {
+                if (m < D) coef_of(m, row, cfn); // the next step's row, one step ahead
+                T* const X = xy + (m & 1) * (XS + YS);
+                T* const Y = X + XS;
+                {
+                    T last[BR];
 #pragma unroll
-                for (int d = 1; d <= D - m; ++d) {
-                    const T tnb  = __shfl_sync(0xffffffffu, sa[d], src);
-                    const T c1   = __shfl_sync(0xffffffffu, cn[corner_index<D>(1, d)], 0);
-                    const T r1   = __shfl_sync(0xffffffffu, cn[corner_index<D>(d, 1)], 0);
-                    const T tang = inr ? tnb : (col ? c1 : r1);
-                    const T nrm  = sa[d + 1];
-                    sa[d]        = upd2d<T>(sa[d], col ? nrm : tang, col ? tang : nrm, cf, ux, uy);
+                    for (int a = 0; a < BR; ++a) last[a] = v[a][BC - 1];
+                    sts_vec<T, BR>(X + (cb + 1) * XN + rb * BR, last);
                 }
-                // the corner in place, by increasing distance a + b: a cell
-                // reads the cells at distance + 1, still u^{m-1}
-                if (NC > 0) {
+                sts_vec<T, BC>(Y + (rb + 1) * N + cb * BC, v[BR - 1]);
+                if (has) gx[(m & 1) * (XS + YS)] = sa[1]; // u^{m-1} ghosts
+                __syncwarp();
+                T xin[BR], yin[BC];
+                lds_vec<T, BR>(X + cb * XN + rb * BR, xin);
+                lds_vec<T, BC>(Y + rb * N + cb * BC, yin);
+                // in place, last row and column first: a cell's upwind
+                // neighbours are still u^{m-1} when it is updated
 #pragma unroll
-                    for (int sum = 2; sum <= D - m; ++sum)
+                for (int a = BR - 1; a >= 0; --a)
 #pragma unroll
-                        for (int a = 1; a < sum; ++a)
-                            cn[corner_index<D>(a, sum - a)] =
-                                upd2d<T>(cn[corner_index<D>(a, sum - a)], cn[corner_index<D>(a, sum - a + 1)],
-                                         cn[corner_index<D>(a + 1, sum - a)], cf, ux, uy);
+                    for (int e = BC - 1; e >= 0; --e)
+                        v[a][e] = upd2d_fixed<T, XU, YU>(v[a][e], e == 0 ? xin[a] : v[a][e - 1],
+                                                         a == 0 ? yin[e] : v[a - 1][e], cf);
+                if (m < D) {
+                    // strips to u^m on the distances still needed, ascending:
+                    // a lane's distance d+1 and its neighbours' distance d
+                    // are still u^{m-1} when distance d is updated (the
+                    // shuffles of distance d precede every lane's update)
+#pragma unroll
+                    for (int d = 1; d <= D - m; ++d) {
+                        const T tnb  = __shfl_sync(0xffffffffu, sa[d], src);
+                        const T tang = inr ? tnb : (col ? cn[corner_index<D>(1, d)] : cn[corner_index<D>(d, 1)]);
+                        const T nrm  = sa[d + 1];
+                        sa[d]        = upd2d_fixed<T, XU, YU>(sa[d], col ? nrm : tang, col ? tang : nrm, cf);
+                    }
+                    // the corner in place, by increasing distance a + b: a
+                    // cell reads the cells at distance + 1, still u^{m-1}
+                    if (NC > 0 && XU && YU) {
+#pragma unroll
+                        for (int sum = 2; sum <= D - m; ++sum)
+#pragma unroll
+                            for (int a = 1; a < sum; ++a)
+                                cn[corner_index<D>(a, sum - a)] = upd2d_fixed<T, XU, YU>(
+                                    cn[corner_index<D>(a, sum - a)], cn[corner_index<D>(a, sum - a + 1)],
+                                    cn[corner_index<D>(a + 1, sum - a)], cf);
+                    }
+                    cf = cfn;
                 }
             }
-            __syncwarp();
+        };
+        if (ux != 0 && uy != 0) steps.template operator()<true, true>();
+        else if (ux != 0) steps.template operator()<true, false>();
+        else if (uy != 0) steps.template operator()<false, true>();
+        else steps.template operator()<false, false>();
+        // back into the tile in its own orientation, then the interior rows out
 #pragma unroll
-            for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
-            __syncwarp();
-        }
+        for (int a = 0; a < BR; ++a)
+#pragma unroll
+            for (int e = 0; e < BC; ++e) cell[a * sr + e * sc] = v[a][e];
+        __syncwarp();
         const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
         uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
         for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
         __syncwarp();
-        sd0 = sd1;
-        m0  = m1;
+        r0 = r1;
+        r1 = r2;
 #pragma unroll
         for (int d = 1; d <= D; ++d) sa[d] = sb[d];
-        sd1 = sd2;
-        m1  = m2;
-        k2  = k3;
     }
+}
+
+// Warp w of the block: its S tiles, its exchange buffers and its S barriers
+// in dynamic shared memory (multi-step pass).
+template <typename T, int N, int H, int W, int S>
+__device__ __forceinline__ void pass2d_smem(unsigned char* smem, T*& tiles, T*& xy, uint64_t*& bars)
+{
+    using Sh      = Step2dShape<T, N, H>;
+    using Ps      = PassShape<T, N, H>;
+    const int wib = threadIdx.x >> 5;
+    tiles         = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * S * Sh::FLAT;
+    xy            = reinterpret_cast<T*>(smem + static_cast<size_t>(W) * S * Sh::TILE) + static_cast<size_t>(wib) * Ps::XY;
+    bars          = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * (S * Sh::TILE + Ps::XY * sizeof(T))) +
+           wib * S;
 }
 
 // Warp w of the block: its S tiles and S barriers in dynamic shared memory.
@@ -1559,22 +1701,29 @@ k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __r
     step2d_body<T, N, H, S>(in, out, meta, P, g, coef, coef32, upx0, upy0, err, keys, upcode, tiles, bars, p, nwarp);
 }
 
+// Register budget of the multi-step pass: 24 resident warps per SM (the
+// lane's cell block, its strips and the corner stay in registers for the
+// whole pass; two tiles in flight per warp keep the memory system busy).
+template <typename T, int W>
+struct Pass2dOcc {
+    static constexpr int blocks = (24 / W) > 0 ? (24 / W) : 1;
+};
+
 // Host-driven launch of D steps per pass: coefficient rows of step m at
 // coef / coef32 + m * cstride.
 template <typename T, int N, int H, int W, int S, int D>
-__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
-              const Coef* __restrict__ coef, const float2* __restrict__ coef32, size_t cstride, int upx0, int upy0,
-              int32_t* err, const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode)
+__global__ void __launch_bounds__(W * 32, Pass2dOcc<T, W>::blocks)
+k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const int4* __restrict__ rec, int P,
+              const Coef* __restrict__ coef, const float2* __restrict__ coef32, size_t cstride, int32_t* err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     T*        tiles;
+    T*        xy;
     uint64_t* bars;
-    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
+    pass2d_smem<T, N, H, W, S>(smem, tiles, xy, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pass_body<T, N, H, S, D>(in, out, meta, P, g, coef, coef32, cstride, upx0, upy0, err, keys, upcode, tiles,
-                                    bars, p, nwarp);
+    step2d_pass_body<T, N, H, S, D>(in, out, rec, P, coef, coef32, cstride, err, tiles, xy, bars, p, nwarp);
 }
 
 } // namespace amr_gb300

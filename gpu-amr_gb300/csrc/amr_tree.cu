@@ -150,6 +150,7 @@ struct amr_tree {
     uint64_t*      keys[2]{};
     int32_t*       levels[2]{};
     amr_halo_meta* meta[2]{};
+    int4*          prec = nullptr; // pass records, one per leaf (multi-step passes)
     int            tb = 0;
 
     int8_t*   flags  = nullptr;
@@ -255,12 +256,14 @@ cudaError_t prepare_step2d()
     cudaError_t e    = cudaFuncSetAttribute(k_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_run_step2d<T, N, H, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    auto pass_attr = [&]<int D>() {
+    const int pass_smem = static_cast<int>(PassShape<T, N, H>::smem(W, S));
+    auto      pass_attr = [&]<int D>() {
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_step2d_pass<T, N, H, W, S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            e = cudaFuncSetAttribute(k_step2d_pass<T, N, H, W, S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     pass_smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_run_step2d_pass<T, N, H, W, S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     smem);
+                                     pass_smem);
     };
     pass_attr.template operator()<2>();
     if constexpr (sizeof(T) == 4) {
@@ -285,6 +288,20 @@ int step2d_occupancy()
     return nb;
 }
 
+// Resident blocks per SM of the multi-step pass (W, S), which also holds the
+// warps' exchange buffers.
+template <typename T, int N, int H, int W, int S>
+int pass2d_occupancy()
+{
+    if (prepare_step2d<T, N, H, W, S>() != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run_step2d_pass<T, N, H, W, S, 2>, W * 32,
+                                                      PassShape<T, N, H>::smem(W, S)) != cudaSuccess)
+        nb = 0;
+    cudaGetLastError();
+    return nb;
+}
+
 // Calls f.template operator()<W, S>() for the (W, S) pair of the config; the
 // pairs the autotuner searches.
 template <typename F>
@@ -295,18 +312,21 @@ amr_status with_ws(int W, int S, F&& f)
     if (W == 8 && S == 1) return f.template operator()<8, 1>();
     if (W == 8 && S == 2) return f.template operator()<8, 2>();
     if (W == 8 && S == 3) return f.template operator()<8, 3>();
+    if (W == 8 && S == 4) return f.template operator()<8, 4>();
     if (W == 16 && S == 2) return f.template operator()<16, 2>();
+    if (W == 16 && S == 3) return f.template operator()<16, 3>();
+    if (W == 16 && S == 4) return f.template operator()<16, 4>();
     return fail(AMR_ERR_INVALID, "unsupported update kernel configuration");
 }
-constexpr int kStepConfigs[][2] = { { 4, 2 }, { 4, 3 }, { 8, 1 }, { 8, 2 }, { 8, 3 }, { 16, 2 } };
+constexpr int kStepConfigs[][2] = { { 4, 2 }, { 4, 3 }, { 8, 1 }, { 8, 2 }, { 8, 3 }, { 8, 4 }, { 16, 2 }, { 16, 3 }, { 16, 4 } };
 
 // Grid of the 2D update kernel: cfg.grid, or one warp per patch capped at
 // full residency.
 template <typename T, int N, int H, int W, int S>
-unsigned step2d_grid(int P, int grid)
+unsigned step2d_grid(int P, int grid, bool pass = false)
 {
     if (grid > 0) return static_cast<unsigned>(grid);
-    const int occ = std::max(1, step2d_occupancy<T, N, H, W, S>());
+    const int occ = std::max(1, pass ? pass2d_occupancy<T, N, H, W, S>() : step2d_occupancy<T, N, H, W, S>());
     return static_cast<unsigned>(std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
 }
 
@@ -354,21 +374,33 @@ amr_status with_depth(int D, F&& f)
     return fail(AMR_ERR_INVALID, "unsupported pass depth");
 }
 
-// D steps per pass (same-level trees): coefficient rows of step m at coef +
-// m * cstride.
+// D steps per pass (same-level trees, pass records built): coefficient rows
+// of step m at coef + m * cstride.
 template <typename T, int N, int H, int D>
-amr_status launch_step2d_pass(const T* in, T* out, const amr_halo_meta* meta, int P, const Geo& g, const Coef* coef,
-                              const float2* coef32, size_t cstride, const int* up, int32_t* err, const uint64_t* keys,
-                              const int32_t* upcode, const StepCfg& cfg, cudaStream_t s)
+amr_status launch_step2d_pass(const T* in, T* out, const int4* rec, int P, const Coef* coef, const float2* coef32,
+                              size_t cstride, int32_t* err, const StepCfg& cfg, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
-        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
-            in, out, meta, P, g, coef, coef32, cstride, up[0], up[1], err, keys, upcode);
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, true);
+        k_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(in, out, rec, P, coef,
+                                                                                           coef32, cstride, err);
         AMR_LAUNCHED("k_step2d_pass");
         return AMR_OK;
     });
+}
+
+// Pass records of the tree's current leaves (host-driven passes and the
+// tuner); upwind offsets per instance (upcode) or launch-wide (up).
+amr_status build_pass_records(amr_tree* t, const int32_t* upcode, const int* up, cudaStream_t s)
+{
+    const int P = static_cast<int>(t->size);
+    if (P == 0) return AMR_OK;
+    const unsigned grid = static_cast<unsigned>(std::min<long long>((P + 255) / 256, 8LL * num_sms()));
+    k_pass_records<<<grid, 256, 0, s>>>(t->meta[t->tb], t->keys[t->tb], upcode, up[0], up[1], P, t->g, t->prec,
+                                        t->status + 7);
+    AMR_LAUNCHED("k_pass_records");
+    return AMR_OK;
 }
 
 // ------------------------------------------------------------ autotuner
@@ -432,9 +464,13 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
     float     best_ms = 0.0f;
     bool      have    = false;
     const int sms     = num_sms();
+    if (pair) {
+        const amr_status rs = build_pass_records(t, upcode, up, s);
+        if (rs != AMR_OK) return rs;
+    }
     for (const auto& ws : kStepConfigs) {
         amr_status st = with_ws(ws[0], ws[1], [&]<int W, int S>() -> amr_status {
-            const int occ = step2d_occupancy<T, N, H, W, S>();
+            const int occ = pair ? pass2d_occupancy<T, N, H, W, S>() : step2d_occupancy<T, N, H, W, S>();
             if (occ < 1) return AMR_OK;
             const int full = static_cast<int>(grid_for(P, W));
             for (int bps : { 1, 2, 3, 4, 6, 8, 12, 16 }) {
@@ -443,9 +479,9 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
                 StepCfg   c{ W, S, grid };
                 for (int rep = 0; rep < 2; ++rep) { // warm-up
                     amr_status r =
-                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(
-                                   static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->meta[t->tb], P, t->g,
-                                   coef, coef32, 0, up, t->status + 7, t->keys[t->tb], upcode, c, s)
+                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(static_cast<const T*>(t->cur),
+                                                                          static_cast<T*>(t->nxt), t->prec, P, coef,
+                                                                          coef32, 0, t->status + 7, c, s)
                              : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
                                                       t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
                                                       t->keys[t->tb], upcode, c, s);
@@ -455,9 +491,9 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
                 AMR_CUDA(cudaEventRecord(e0, s));
                 for (int rep = 0; rep < reps; ++rep) {
                     amr_status r =
-                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(
-                                   static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->meta[t->tb], P, t->g,
-                                   coef, coef32, 0, up, t->status + 7, t->keys[t->tb], upcode, c, s)
+                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(static_cast<const T*>(t->cur),
+                                                                          static_cast<T*>(t->nxt), t->prec, P, coef,
+                                                                          coef32, 0, t->status + 7, c, s)
                              : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
                                                       t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
                                                       t->keys[t->tb], upcode, c, s);
@@ -516,6 +552,7 @@ void free_tree(amr_tree* t)
         cudaFree(t->levels[b]);
         cudaFree(t->meta[b]);
     }
+    cudaFree(t->prec);
     cudaFree(t->flags);
     cudaFree(t->rmark);
     cudaFree(t->chead);
@@ -791,6 +828,7 @@ RunBufs run_bufs(amr_tree* t, bool per_leaf_vel, bool bounds)
     B.maxlev_new = t->maxlev_new;
     B.vel        = per_leaf_vel ? t->vel : nullptr;
     B.upcode     = per_leaf_vel ? t->upcode : nullptr;
+    B.prec       = t->prec;
     B.bounds     = bounds ? t->bounds : nullptr;
     B.tile_sums  = t->tile_sums;
     B.cap        = t->cap;
@@ -813,14 +851,14 @@ amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const 
 }
 
 template <typename T, int N, int H, int D>
-amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, const float2* coef32,
-                                  size_t cstride, int parity, const int* up, const StepCfg& cfg, int P, cudaStream_t s)
+amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, const Coef* coef, const float2* coef32,
+                                  size_t cstride, int parity, const StepCfg& cfg, int P, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
-        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid);
-        k_run_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, Step2dShape<T, N, H>::smem(W, S), s>>>(
-            B, ctl, g, coef, coef32, cstride, parity, up[0], up[1]);
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, true);
+        k_run_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(B, ctl, coef, coef32,
+                                                                                               cstride, parity);
         AMR_LAUNCHED("k_run_step2d_pass");
         return AMR_OK;
     });
@@ -841,6 +879,12 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
                                      t->coef, t->coef32, t->upcode, &ctl->err); // nothing after an error
     AMR_LAUNCHED("k_batch_begin");
+    if (key.pair) { // records of this interval's tree, with the upwind codes just written
+        const unsigned rgrid =
+            static_cast<unsigned>(std::min<long long>((static_cast<long long>(t->cap) + 255) / 256, 8LL * sms));
+        k_run_pass_records<<<rgrid, 256, 0, cs>>>(B, ctl, g, key.up[0], key.up[1]);
+        AMR_LAUNCHED("k_run_pass_records");
+    }
     const StepCfg cfg{ key.W, key.S, key.grid };
     const int     ppb = std::max(1, 256 / g.cells);
     // multi-step passes on same-level trees (pass_plan), one launch per step
@@ -858,8 +902,8 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         amr_status    st  = AMR_OK;
         auto pass = [&]<int N>() -> amr_status {
             return with_depth<T>(D, [&]<int DD>() -> amr_status {
-                return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, g, cf, cf2, cst, par, key.up, cfg,
-                                                           static_cast<int>(t->cap), cs);
+                return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, cf, cf2, cst, par, cfg, static_cast<int>(t->cap),
+                                                           cs);
             });
         };
         if (D > 1) st = g.n == 16 ? pass.template operator()<16>() : pass.template operator()<8>();
@@ -1244,6 +1288,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
         al(reinterpret_cast<void**>(&t->levels[b]), cap * sizeof(int32_t));
         al(reinterpret_cast<void**>(&t->meta[b]), cap * g.ndir * sizeof(amr_halo_meta));
     }
+    al(reinterpret_cast<void**>(&t->prec), cap * sizeof(int4));
     al(reinterpret_cast<void**>(&t->flags), cap);
     al(reinterpret_cast<void**>(&t->rmark), cap);
     al(reinterpret_cast<void**>(&t->chead), cap);
@@ -1343,6 +1388,7 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     void*        l1     = al(cap * sizeof(int32_t));
     void*        m0     = al(cap * g.ndir * sizeof(amr_halo_meta));
     void*        m1     = al(cap * g.ndir * sizeof(amr_halo_meta));
+    void*        pr     = al(cap * sizeof(int4)); // pass records: rebuilt before every use
     void*        fl     = al(cap);
     void*        rm     = al(cap);
     void*        ch     = al(cap);
@@ -1382,6 +1428,8 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
         cudaFree(t->levels[b]);
         cudaFree(t->meta[b]);
     }
+    cudaFree(t->prec);
+    t->prec = static_cast<int4*>(pr);
     cudaFree(t->flags);
     cudaFree(t->rmark);
     cudaFree(t->chead);
@@ -1721,13 +1769,17 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
     lookup_tuned(t, uleaf != nullptr, false, cfg);
     if (!lookup_tuned(t, uleaf != nullptr, true, cfg_pair)) cfg_pair = cfg;
     t->last_cfg = t->uniform ? cfg_pair : cfg;
+    const bool shape2d = t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8);
     while (done < steps || (first && steps == 0)) {
         const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
         k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? first_mode : BATCH_CONTINUE,
                                         remaining, t->dts(), t->step_dt, t->coef, t->coef32, t->upcode);
         AMR_LAUNCHED("k_batch_begin");
+        if (first && shape2d && t->uniform && steps > 1) { // records of the multi-step passes (after the
+            const amr_status rs = build_pass_records(t, uleaf, up, s); // upwind codes of this advance)
+            if (rs != AMR_OK) return rs;
+        }
         first = false;
-        const bool shape2d = t->g.rank == 2 && t->g.h == 1 && (t->g.n == 16 || t->g.n == 8);
         const int  deep    = t->dtype == AMR_F32 ? kPassSteps<float> : kPassSteps<double>;
         std::vector<int> plan;
         if (shape2d && t->uniform) pass_plan(chunk, deep, plan); // several steps per pass where every relation is same-level
@@ -1760,8 +1812,8 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                     const size_t cst  = static_cast<size_t>(K) * nl;
                     auto         pass = [&]<int N>(const StepCfg& c) -> amr_status {
                         return with_depth<T>(D, [&]<int DD>() -> amr_status {
-                            return launch_step2d_pass<T, N, 1, DD>(in, out, t->meta[t->tb], P, t->g, cf, cf2, cst, up,
-                                                                   t->status + 7, t->keys[t->tb], uleaf, c, s);
+                            return launch_step2d_pass<T, N, 1, DD>(in, out, t->prec, P, cf, cf2, cst, t->status + 7,
+                                                                   c, s);
                         });
                     };
                     return t->g.n == 16 ? pass.template operator()<16>(cfg_pair) : pass.template operator()<8>(StepCfg{});
