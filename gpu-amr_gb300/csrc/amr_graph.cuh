@@ -27,6 +27,7 @@ struct RunCtl {
     int32_t leaves_max;
     int32_t uniform;    // every neighbour relation of the current tree is "same level"
     int32_t flagged;    // some leaf of the pending re-mesh is flagged (zeroed at each commit)
+    int32_t recs;       // the pass and face records describe the current tree (zero at a run's start)
     unsigned long long cell_updates, leaves_sum, intervals, remeshes;
 };
 
@@ -48,6 +49,7 @@ struct RunBufs {
     const int32_t* upcode;     // per instance packed upwind offsets (with vel), or null
     const int32_t* bounds;     // per instance (min, max) level bounds, or null
     int4*          prec;       // pass records of the current tree (multi-step passes)
+    int4*          frec;       // face records of the current tree (flags of a same-level tree)
     uint32_t*      tile_sums;  // scan partials, one per tile
     unsigned long long cap;
     int            ninst;
@@ -79,10 +81,10 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
 // multi-step passes, after the guard).
 __global__ void __launch_bounds__(256) k_run_pass_records(RunBufs B, RunCtl* ctl, Geo g, int upx0, int upy0)
 {
-    if (ctl->err) return;
+    if (ctl->err || ctl->recs) return; // still valid: the last interval left the tree as it was
     const int P = ctl->P, tb = ctl->tb;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P; q += gridDim.x * blockDim.x)
-        pass_record(B.meta[tb], B.keys[tb], B.upcode, upx0, upy0, g, q, B.prec, &ctl->err);
+        pass_record(B.meta[tb], B.keys[tb], B.upcode, upx0, upy0, g, q, B.prec, B.frec, &ctl->err);
 }
 
 // D steps per pass (trees of same-level relations only; the interval's
@@ -90,7 +92,7 @@ __global__ void __launch_bounds__(256) k_run_pass_records(RunBufs B, RunCtl* ctl
 // records).  parity selects the buffers of this pass.
 template <typename T, int N, int H, int W, int S, int D>
 __global__ void __launch_bounds__(W * 32, Pass2dOcc<T, W>::blocks)
-k_run_step2d_pass(RunBufs B, RunCtl* ctl, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+k_run_step2d_pass(RunBufs B, RunCtl* ctl, int nl, const Coef* __restrict__ coef, const float2* __restrict__ coef32,
                   size_t cstride, int parity)
 {
     if (ctl->err) return;
@@ -102,7 +104,7 @@ k_run_step2d_pass(RunBufs B, RunCtl* ctl, const Coef* __restrict__ coef, const f
     const int P = ctl->P, s = ctl->sb ^ parity;
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pass_body<T, N, H, S, D>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.prec, P,
+    step2d_pass_body<T, N, H, S, D>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.prec, P, nl,
                                     coef, coef32, cstride, &ctl->err, tiles, xy, bars, p, nwarp);
 }
 
@@ -186,7 +188,7 @@ k_run_flags_grad(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, in
 
 // 2D gradient flags of the sized kernel (flags2d_body), ghosts on the fly.
 template <typename T, int N, int H>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3)
 k_run_flags2d(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int max_level, int sp)
 {
     if (ctl->err) return;
@@ -199,6 +201,23 @@ k_run_flags2d(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int m
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     flags2d_body<T, N, H, false>(static_cast<const T*>(B.state[ctl->sb ^ sp]), B.meta[tb], B.keys[tb], ctl->P, g, rule,
                                  min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp);
+}
+
+// The same flags on a tree whose every relation is same-level, from the pass
+// and face records k_run_pass_records built at the start of the interval.
+template <typename T, int N, int H>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3)
+k_run_flags2d_uniform(RunBufs B, RunCtl* ctl, GradRule rule, int min_level, int max_level, int sp)
+{
+    if (ctl->err) return;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T*        tiles;
+    uint64_t* bars;
+    flags2d_smem<T, N, H, false>(smem, blockDim.x >> 5, tiles, bars);
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    flags2d_uniform_body<T, N, H>(static_cast<const T*>(B.state[ctl->sb ^ sp]), B.prec, B.frec, ctl->P, rule,
+                                  min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp);
 }
 
 // Max-value flags (k_flags_max's rule over the exchanged ghosts), one block
@@ -400,7 +419,8 @@ __global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
 // End of an interval (one block): statistics of the interval just run and
 // the state buffer the steps left current, then, when the re-mesh changed the
 // tree, the switch to the new buffers and the new per-instance finest levels.
-__global__ void __launch_bounds__(256) k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp)
+__global__ void __launch_bounds__(256)
+k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp, int records)
 {
     __shared__ int chg;
     __shared__ int red[256 / 32];
@@ -409,6 +429,7 @@ __global__ void __launch_bounds__(256) k_run_commit(RunBufs B, RunCtl* ctl, int 
         const bool ok = ctl->err == 0;
         chg           = (remesh && ok && ctl->changed) ? 1 : 0;
         ctl->flagged  = 0; // the next interval's marks set it again
+        ctl->recs     = records && ok && !chg ? 1 : 0; // this interval's records outlive it if the tree stays
         if (ok) {
             ctl->sb ^= sp;
             ctl->cell_updates += static_cast<unsigned long long>(P) * steps * cells;

@@ -1288,20 +1288,25 @@ __device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restr
 // One 16-byte record per leaf for the multi-step pass: the same-level
 // neighbours across the upwind x face (x) and y face (y), the x-neighbour's
 // y-neighbour (z: the diagonal whose corner reaches the patch within a
-// pass), and the upwind offsets with the coefficient row packed into w.  A
-// zero velocity component names the patch itself.  The records are built
-// once per mesh and velocity field, so the pass reads one record per patch
-// instead of a chain of dependent face-record loads.  A face that is not
-// same-level sets AMR_ERR_UNBALANCED (passes run only where every relation
-// is same-level).
-__host__ __device__ __forceinline__ int pass_code(int ux, int uy, int row) { return (row << 4) | ((ux + 1) << 2) | (uy + 1); }
+// pass), and the instance, level and upwind offsets packed into w.  A zero
+// velocity component names the patch itself.  Optionally a second record
+// per leaf holds all four face neighbours (x low, x high, y low, y high) for
+// the gradient flags of the same tree.  The records are built once per mesh
+// and velocity field, so the kernels read one record per patch instead of a
+// chain of dependent face-record loads.  A face that is not same-level sets
+// AMR_ERR_UNBALANCED (passes run only where every relation is same-level).
+__host__ __device__ __forceinline__ int pass_code(int ux, int uy, int inst, int level)
+{
+    return (inst << 10) | (level << 4) | ((ux + 1) << 2) | (uy + 1);
+}
 __host__ __device__ __forceinline__ int pass_ux(int code) { return ((code >> 2) & 3) - 1; }
 __host__ __device__ __forceinline__ int pass_uy(int code) { return (code & 3) - 1; }
-__host__ __device__ __forceinline__ int pass_row(int code) { return code >> 4; }
+__host__ __device__ __forceinline__ int pass_level(int code) { return (code >> 4) & 63; }
+__host__ __device__ __forceinline__ int pass_inst(int code) { return code >> 10; }
 
 __device__ __forceinline__ void pass_record(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
                                             const int32_t* __restrict__ upcode, int upx0, int upy0, const Geo& g,
-                                            int q, int4* __restrict__ rec, int32_t* err)
+                                            int q, int4* __restrict__ rec, int4* __restrict__ frec, int32_t* err)
 {
     const uint64_t key  = keys[q];
     const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
@@ -1322,8 +1327,12 @@ __device__ __forceinline__ void pass_record(const amr_halo_meta* __restrict__ me
     r.x    = ux != 0 ? same(meta[static_cast<size_t>(q) * 4 + 2 + (ux > 0 ? 1 : 0)], q) : q;
     r.y    = uy != 0 ? same(meta[static_cast<size_t>(q) * 4 + (uy > 0 ? 1 : 0)], q) : q;
     r.z    = ux != 0 && uy != 0 ? same(meta[static_cast<size_t>(r.x) * 4 + (uy > 0 ? 1 : 0)], r.x) : q;
-    r.w    = pass_code(ux, uy, inst * (g.depth + 1) + key_level(key));
+    r.w    = pass_code(ux, uy, inst, key_level(key));
     rec[q] = r;
+    if (frec) {
+        const amr_halo_meta* m = meta + static_cast<size_t>(q) * 4;
+        frec[q]                = make_int4(same(m[2], q), same(m[3], q), same(m[0], q), same(m[1], q));
+    }
 }
 
 // Host-driven build: P leaves, upwind offsets per instance (upcode) or
@@ -1334,7 +1343,7 @@ k_pass_records(const amr_halo_meta* __restrict__ meta, const uint64_t* __restric
                int32_t* err)
 {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P; q += gridDim.x * blockDim.x)
-        pass_record(meta, keys, upcode, upx0, upy0, g, q, rec, err);
+        pass_record(meta, keys, upcode, upx0, upy0, g, q, rec, nullptr, err);
 }
 
 // ------------------------------------------------ 2D update, D steps per pass
@@ -1453,9 +1462,10 @@ __device__ __forceinline__ void sts_vec(T* p, const T (&v)[K])
 
 template <typename T, int N, int H, int S, int D>
 __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __restrict__ out,
-                                                                                                  const int4* __restrict__ rec, int P, const Coef* __restrict__ coef,
-                                                 const float2* __restrict__ coef32, size_t cstride, int32_t* err,
-                                                 T* tiles, T* xy, uint64_t* bars, int p, int nwarp)
+                                                                                                  const int4* __restrict__ rec, int P, int nl,
+                                                 const Coef* __restrict__ coef, const float2* __restrict__ coef32,
+                                                 size_t cstride, int32_t* err, T* tiles, T* xy, uint64_t* bars, int p,
+                                                 int nwarp)
 {
     static_assert(D >= 2 && D <= 6, "two to six steps per pass");
     using Sh                = Step2dShape<T, N, H>;
@@ -1542,7 +1552,7 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         if (pb < P) r2 = __ldg(rec + pb);
         if (pa < P) fetch(r1, sb);
         // this patch
-        const int ux = pass_ux(r0.w), uy = pass_uy(r0.w), row = pass_row(r0.w);
+        const int ux = pass_ux(r0.w), uy = pass_uy(r0.w), row = pass_inst(r0.w) * nl + pass_level(r0.w);
         T         cn[NC > 0 ? NC : 1];
 #pragma unroll
         for (int c = 0; c < (NC > 0 ? NC : 1); ++c) cn[c] = T(0);
@@ -1713,7 +1723,7 @@ struct Pass2dOcc {
 // coef / coef32 + m * cstride.
 template <typename T, int N, int H, int W, int S, int D>
 __global__ void __launch_bounds__(W * 32, Pass2dOcc<T, W>::blocks)
-k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const int4* __restrict__ rec, int P,
+k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const int4* __restrict__ rec, int P, int nl,
               const Coef* __restrict__ coef, const float2* __restrict__ coef32, size_t cstride, int32_t* err)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1723,7 +1733,7 @@ k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const int4* __restr
     pass2d_smem<T, N, H, W, S>(smem, tiles, xy, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pass_body<T, N, H, S, D>(in, out, rec, P, coef, coef32, cstride, err, tiles, xy, bars, p, nwarp);
+    step2d_pass_body<T, N, H, S, D>(in, out, rec, P, nl, coef, coef32, cstride, err, tiles, xy, bars, p, nwarp);
 }
 
 } // namespace amr_gb300
@@ -1937,6 +1947,143 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
     }
 }
 
+// Gradient flags of a tree whose every relation is same-level (the graph
+// intervals that run multi-step passes).  A ghost face is then a copy of the
+// neighbour's edge line, so each lane fetches its two ghost values (lanes
+// 0..N-1 the low and high ghost column at row tg, lanes N..2N-1 the low and
+// high ghost row at column tg) one patch ahead, from the face record (all
+// four neighbours) read two patches ahead; instance and level come from the
+// pass record.  The cells, the gradient arithmetic and the decision are
+// flags2d_body's, so the flags are identical.
+template <typename T, int N, int H>
+__device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, const int4* __restrict__ prec,
+                                                     const int4* __restrict__ frec, int P, const GradRule& rule,
+                                                     int min_level, int max_level, const int32_t* __restrict__ bounds,
+                                                     int8_t* __restrict__ flags, int32_t* err, T* tiles,
+                                                     uint64_t* bars, int p, int nwarp)
+{
+    using Sh                = Flags2dShape<T, N, H, false>;
+    constexpr int      P1   = Sh::P1;
+    constexpr int      FLAT = Sh::FLAT;
+    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
+    constexpr int      SEG  = Sh::SEG;
+    const int          lane = threadIdx.x & 31;
+    if (lane == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    const char* in_bytes = reinterpret_cast<const char*>(in);
+    auto        request  = [&](int q, int slot) {
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[slot], BYTES);
+        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
+                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
+    };
+    if (p < P && lane == 0) request(p, 0);
+    uint32_t   phase = 0;
+    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
+    const bool col = lane < N;
+    const bool job = lane < 2 * N;
+    const int  tg  = (col ? lane : lane - N) + H;
+    // the lane's ghost cells in the tile and their sources in the low / high
+    // neighbour (the neighbour's last / first interior line)
+    const int  g0 = col ? tg * P1 + (H - 1) : (H - 1) * P1 + tg;
+    const int  g1 = col ? tg * P1 + (N + H) : (N + H) * P1 + tg;
+    const int  s0 = col ? tg * P1 + (N + H - 1) : (N + H - 1) * P1 + tg;
+    const int  s1 = col ? tg * P1 + H : H * P1 + tg;
+    auto       fetch = [&](const int4& f, T& a, T& b) {
+        a = b = T(0);
+        if (!job) return;
+        a = in[static_cast<size_t>(col ? f.x : f.z) * FLAT + s0];
+        b = in[static_cast<size_t>(col ? f.y : f.w) * FLAT + s1];
+    };
+    // face records two patches ahead, ghost values one ahead
+    int4 f0{}, f1{}, f2{};
+    int  c0 = 0, c1 = 0, c2 = 0;
+    T    ga = T(0), gb = T(0), na = T(0), nb = T(0);
+    if (p < P) {
+        f0 = __ldg(frec + p);
+        c0 = __ldg(&prec[p].w);
+        fetch(f0, ga, gb);
+    }
+    if (p + nwarp < P) {
+        f1 = __ldg(frec + p + nwarp);
+        c1 = __ldg(&prec[p + nwarp].w);
+    }
+    for (int it = 0; p < P; ++it, p += nwarp) {
+        const int b  = it & 1;
+        const int pn = p + nwarp, pm = p + 2 * nwarp;
+        if (pn < P && lane == 0) request(pn, b ^ 1);
+        if (pm < P) {
+            f2 = __ldg(frec + pm);
+            c2 = __ldg(&prec[pm].w);
+        }
+        if (pn < P) fetch(f1, na, nb);
+        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
+            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
+            phase ^= 1u << b;
+            if (pn < P) mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
+            return;
+        }
+        phase ^= 1u << b;
+        T* tile = tiles + static_cast<size_t>(b) * FLAT;
+        if (job) {
+            tile[g0] = ga;
+            tile[g1] = gb;
+        }
+        __syncwarp();
+        // the decision rule of flags2d_body: the lane's FP32 maximum decides
+        // unless it lies in a band or some value is not finite
+        int   any = 0, all = 1;
+        T     colv[SEG + 2];
+        float smax = 0.0f;
+        bool  bad  = false;
+#pragma unroll
+        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int   idx = (r0 + k) * P1 + cl;
+            const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
+            smax            = fmaxf(smax, s);
+            bad |= !(fabsf(s) < INFINITY);
+        }
+        const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
+                           (smax < rule.c_lo || smax >= rule.c_hi);
+        if (known) {
+            any = smax >= rule.r_hi ? 1 : 0;
+            all = smax < rule.c_lo ? 1 : 0;
+        } else {
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                const int    idx = (r0 + k) * P1 + cl;
+                const double s   = grad_sq_exact2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
+                if (s >= rule.rsq) any = 1;
+                if (!(s < rule.csq)) all = 0;
+            }
+        }
+        any = __any_sync(0xffffffffu, any);
+        all = __all_sync(0xffffffffu, all);
+        if (lane == 0) {
+            int lo = min_level, hi = max_level;
+            if (bounds) {
+                const int inst = pass_inst(c0);
+                lo             = bounds[2 * inst];
+                hi             = bounds[2 * inst + 1];
+            }
+            flags[p] = gradient_decision(any, all, pass_level(c0), lo, hi);
+        }
+        __syncwarp();
+        f0 = f1;
+        f1 = f2;
+        c0 = c1;
+        c1 = c2;
+        ga = na;
+        gb = nb;
+    }
+}
+
 template <typename T, int N, int H, bool FromBuffer>
 __device__ __forceinline__ void flags2d_smem(unsigned char* smem, int W, T*& tiles, uint64_t*& bars)
 {
@@ -1947,7 +2094,7 @@ __device__ __forceinline__ void flags2d_smem(unsigned char* smem, int W, T*& til
 }
 
 template <typename T, int N, int H, bool FromBuffer>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3)
 k_flags2d(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys, int P,
           Geo g, GradRule rule, int min_level, int max_level, const int32_t* __restrict__ bounds,
           int8_t* __restrict__ flags, int32_t* err)

@@ -151,6 +151,7 @@ struct amr_tree {
     int32_t*       levels[2]{};
     amr_halo_meta* meta[2]{};
     int4*          prec = nullptr; // pass records, one per leaf (multi-step passes)
+    int4*          frec = nullptr; // face records, one per leaf (flags of same-level graph intervals)
     int            tb = 0;
 
     int8_t*   flags  = nullptr;
@@ -288,17 +289,22 @@ int step2d_occupancy()
     return nb;
 }
 
-// Resident blocks per SM of the multi-step pass (W, S), which also holds the
-// warps' exchange buffers.
-template <typename T, int N, int H, int W, int S>
+// Resident blocks per SM of the D-step pass (W, S), which also holds the
+// warps' exchange buffers (registers grow with D).
+template <typename T, int N, int H, int W, int S, int D>
 int pass2d_occupancy()
 {
+    static std::atomic<int> cached[64]; // per device, 0 = not yet known
+    int                     dev = 0;
+    cudaGetDevice(&dev);
+    if (const int c = cached[dev & 63].load(); c > 0) return c;
     if (prepare_step2d<T, N, H, W, S>() != cudaSuccess) return 0;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run_step2d_pass<T, N, H, W, S, 2>, W * 32,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run_step2d_pass<T, N, H, W, S, D>, W * 32,
                                                       PassShape<T, N, H>::smem(W, S)) != cudaSuccess)
         nb = 0;
     cudaGetLastError();
+    if (nb > 0) cached[dev & 63].store(nb);
     return nb;
 }
 
@@ -323,10 +329,10 @@ constexpr int kStepConfigs[][2] = { { 4, 2 }, { 4, 3 }, { 8, 1 }, { 8, 2 }, { 8,
 // Grid of the 2D update kernel: cfg.grid, or one warp per patch capped at
 // full residency.
 template <typename T, int N, int H, int W, int S>
-unsigned step2d_grid(int P, int grid, bool pass = false)
+unsigned step2d_grid(int P, int grid, int pass_occ = 0)
 {
     if (grid > 0) return static_cast<unsigned>(grid);
-    const int occ = std::max(1, pass ? pass2d_occupancy<T, N, H, W, S>() : step2d_occupancy<T, N, H, W, S>());
+    const int occ = std::max(1, pass_occ > 0 ? pass_occ : step2d_occupancy<T, N, H, W, S>());
     return static_cast<unsigned>(std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
 }
 
@@ -377,13 +383,13 @@ amr_status with_depth(int D, F&& f)
 // D steps per pass (same-level trees, pass records built): coefficient rows
 // of step m at coef + m * cstride.
 template <typename T, int N, int H, int D>
-amr_status launch_step2d_pass(const T* in, T* out, const int4* rec, int P, const Coef* coef, const float2* coef32,
-                              size_t cstride, int32_t* err, const StepCfg& cfg, cudaStream_t s)
+amr_status launch_step2d_pass(const T* in, T* out, const int4* rec, int P, int nl, const Coef* coef,
+                              const float2* coef32, size_t cstride, int32_t* err, const StepCfg& cfg, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
-        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, true);
-        k_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(in, out, rec, P, coef,
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, pass2d_occupancy<T, N, H, W, S, D>());
+        k_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(in, out, rec, P, nl, coef,
                                                                                            coef32, cstride, err);
         AMR_LAUNCHED("k_step2d_pass");
         return AMR_OK;
@@ -454,72 +460,79 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
         }
     }
     best = StepCfg{};
+    if (const char* env = std::getenv("AMR_GB300_STEP_CONFIG")) { // "warps,stages,blocks per SM" (0: full residency)
+        int w = 0, st = 0, bps = 0;
+        if (std::sscanf(env, "%d,%d,%d", &w, &st, &bps) == 3 &&
+            with_ws(w, st, []<int W, int S>() -> amr_status { return AMR_OK; }) == AMR_OK && bps >= 0) {
+            best = StepCfg{ w, st, bps > 0 ? bps * num_sms() : 0 };
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tuned[key] = best;
+            return AMR_OK;
+        }
+    }
     if (g_tune_mode.load() == 0) return AMR_OK;
     if (const char* env = std::getenv("AMR_GB300_AUTOTUNE"); env && std::strcmp(env, "0") == 0) return AMR_OK;
     const int    P = static_cast<int>(t->size);
     cudaStream_t s = t->stream;
-    cudaEvent_t  e0, e1;
-    AMR_CUDA(cudaEventCreate(&e0));
-    AMR_CUDA(cudaEventCreate(&e1));
-    float     best_ms = 0.0f;
-    bool      have    = false;
-    const int sms     = num_sms();
+    const int    sms = num_sms();
     if (pair) {
         const amr_status rs = build_pass_records(t, upcode, up, s);
         if (rs != AMR_OK) return rs;
     }
+    auto launch = [&](const StepCfg& c) -> amr_status {
+        return pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(static_cast<const T*>(t->cur),
+                                                                 static_cast<T*>(t->nxt), t->prec, P, t->g.depth + 1,
+                                                                 coef, coef32, 0, t->status + 7, c, s)
+                    : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->meta[t->tb],
+                                             P, t->g, coef, coef32, up, t->status + 7, t->keys[t->tb], upcode, c, s);
+    };
+    // candidates: every (W, S) with its resident block counts up to full
+    // residency or one warp per leaf
+    std::vector<StepCfg> cand;
     for (const auto& ws : kStepConfigs) {
-        amr_status st = with_ws(ws[0], ws[1], [&]<int W, int S>() -> amr_status {
-            const int occ = pair ? pass2d_occupancy<T, N, H, W, S>() : step2d_occupancy<T, N, H, W, S>();
-            if (occ < 1) return AMR_OK;
+        (void)with_ws(ws[0], ws[1], [&]<int W, int S>() -> amr_status {
+            const int occ =
+                pair ? pass2d_occupancy<T, N, H, W, S, kPassSteps<T>>() : step2d_occupancy<T, N, H, W, S>();
             const int full = static_cast<int>(grid_for(P, W));
             for (int bps : { 1, 2, 3, 4, 6, 8, 12, 16 }) {
                 if (bps > occ) break;
                 const int grid = std::min(full, sms * bps);
-                StepCfg   c{ W, S, grid };
-                for (int rep = 0; rep < 2; ++rep) { // warm-up
-                    amr_status r =
-                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(static_cast<const T*>(t->cur),
-                                                                          static_cast<T*>(t->nxt), t->prec, P, coef,
-                                                                          coef32, 0, t->status + 7, c, s)
-                             : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                      t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
-                                                      t->keys[t->tb], upcode, c, s);
-                    if (r != AMR_OK) return r;
-                }
-                const int reps = 4;
-                AMR_CUDA(cudaEventRecord(e0, s));
-                for (int rep = 0; rep < reps; ++rep) {
-                    amr_status r =
-                        pair ? launch_step2d_pass<T, N, H, kPassSteps<T>>(static_cast<const T*>(t->cur),
-                                                                          static_cast<T*>(t->nxt), t->prec, P, coef,
-                                                                          coef32, 0, t->status + 7, c, s)
-                             : launch_step2d<T, N, H>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt),
-                                                      t->meta[t->tb], P, t->g, coef, coef32, up, t->status + 7,
-                                                      t->keys[t->tb], upcode, c, s);
-                    if (r != AMR_OK) return r;
-                }
-                AMR_CUDA(cudaEventRecord(e1, s));
-                AMR_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.0f;
-                AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (!have || ms < best_ms) {
-                    best_ms = ms;
-                    best    = c;
-                    have    = true;
-                }
+                cand.push_back(StepCfg{ W, S, grid });
                 if (grid == full) break; // more blocks would idle
             }
             return AMR_OK;
         });
-        if (st != AMR_OK) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return st;
+    }
+    // rounds over all candidates, each candidate's best round counts: a
+    // candidate is not judged on one sample taken during a transient
+    cudaEvent_t e0, e1;
+    AMR_CUDA(cudaEventCreate(&e0));
+    AMR_CUDA(cudaEventCreate(&e1));
+    std::vector<float> best_ms(cand.size(), 0.0f);
+    amr_status         st = AMR_OK;
+    constexpr int      kRounds = 3, kReps = 3;
+    for (int round = 0; round < kRounds && st == AMR_OK; ++round) {
+        for (size_t i = 0; i < cand.size() && st == AMR_OK; ++i) {
+            st = launch(cand[i]); // warm-up
+            if (st != AMR_OK) break;
+            if (cudaEventRecord(e0, s) != cudaSuccess) st = fail(AMR_ERR_CUDA, "tuner event");
+            for (int rep = 0; rep < kReps && st == AMR_OK; ++rep) st = launch(cand[i]);
+            if (st != AMR_OK) break;
+            float ms = 0.0f;
+            if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                st = fail(AMR_ERR_CUDA, "tuner timing");
+            else if (round == 0 || ms < best_ms[i])
+                best_ms[i] = ms;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st != AMR_OK) return st;
+    size_t bi = 0;
+    for (size_t i = 1; i < cand.size(); ++i)
+        if (best_ms[i] < best_ms[bi]) bi = i;
+    if (!cand.empty()) best = cand[bi];
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tuned[key] = best;
     return AMR_OK;
@@ -553,6 +566,7 @@ void free_tree(amr_tree* t)
         cudaFree(t->meta[b]);
     }
     cudaFree(t->prec);
+    cudaFree(t->frec);
     cudaFree(t->flags);
     cudaFree(t->rmark);
     cudaFree(t->chead);
@@ -829,6 +843,7 @@ RunBufs run_bufs(amr_tree* t, bool per_leaf_vel, bool bounds)
     B.vel        = per_leaf_vel ? t->vel : nullptr;
     B.upcode     = per_leaf_vel ? t->upcode : nullptr;
     B.prec       = t->prec;
+    B.frec       = t->frec;
     B.bounds     = bounds ? t->bounds : nullptr;
     B.tile_sums  = t->tile_sums;
     B.cap        = t->cap;
@@ -851,14 +866,14 @@ amr_status launch_run_step2d(const RunBufs& B, RunCtl* ctl, const Geo& g, const 
 }
 
 template <typename T, int N, int H, int D>
-amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, const Coef* coef, const float2* coef32,
+amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, int nl, const Coef* coef, const float2* coef32,
                                   size_t cstride, int parity, const StepCfg& cfg, int P, cudaStream_t s)
 {
     return with_ws(cfg.W, cfg.S, [&]<int W, int S>() -> amr_status {
         AMR_CUDA((prepare_step2d<T, N, H, W, S>()));
-        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, true);
-        k_run_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(B, ctl, coef, coef32,
-                                                                                               cstride, parity);
+        const unsigned grid = step2d_grid<T, N, H, W, S>(P, cfg.grid, pass2d_occupancy<T, N, H, W, S, D>());
+        k_run_step2d_pass<T, N, H, W, S, D><<<grid, W * 32, PassShape<T, N, H>::smem(W, S), s>>>(B, ctl, nl, coef,
+                                                                                               coef32, cstride, parity);
         AMR_LAUNCHED("k_run_step2d_pass");
         return AMR_OK;
     });
@@ -902,8 +917,8 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         amr_status    st  = AMR_OK;
         auto pass = [&]<int N>() -> amr_status {
             return with_depth<T>(D, [&]<int DD>() -> amr_status {
-                return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, cf, cf2, cst, par, cfg, static_cast<int>(t->cap),
-                                                           cs);
+                return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, nl, cf, cf2, cst, par, cfg,
+                                                           static_cast<int>(t->cap), cs);
             });
         };
         if (D > 1) st = g.n == 16 ? pass.template operator()<16>() : pass.template operator()<8>();
@@ -924,13 +939,23 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         if (key.crit == 1 && g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8)) {
             const GradRule rule = make_grad_rule(key.rthr, key.cthr);
             const unsigned fgrid = static_cast<unsigned>(sms * 4);
-            if (g.n == 16)
-                k_run_flags2d<T, 16, 1><<<fgrid, 256, Flags2dShape<T, 16, 1, false>::smem(8), cs>>>(
-                    B, ctl, g, rule, key.min_level, key.max_level, sp);
-            else
-                k_run_flags2d<T, 8, 1><<<fgrid, 256, Flags2dShape<T, 8, 1, false>::smem(8), cs>>>(
-                    B, ctl, g, rule, key.min_level, key.max_level, sp);
-            AMR_LAUNCHED("k_run_flags2d");
+            if (key.pair) { // same-level tree: ghosts from the interval's face records
+                if (g.n == 16)
+                    k_run_flags2d_uniform<T, 16, 1><<<fgrid, 256, Flags2dShape<T, 16, 1, false>::smem(8), cs>>>(
+                        B, ctl, rule, key.min_level, key.max_level, sp);
+                else
+                    k_run_flags2d_uniform<T, 8, 1><<<fgrid, 256, Flags2dShape<T, 8, 1, false>::smem(8), cs>>>(
+                        B, ctl, rule, key.min_level, key.max_level, sp);
+                AMR_LAUNCHED("k_run_flags2d_uniform");
+            } else {
+                if (g.n == 16)
+                    k_run_flags2d<T, 16, 1><<<fgrid, 256, Flags2dShape<T, 16, 1, false>::smem(8), cs>>>(
+                        B, ctl, g, rule, key.min_level, key.max_level, sp);
+                else
+                    k_run_flags2d<T, 8, 1><<<fgrid, 256, Flags2dShape<T, 8, 1, false>::smem(8), cs>>>(
+                        B, ctl, g, rule, key.min_level, key.max_level, sp);
+                AMR_LAUNCHED("k_run_flags2d");
+            }
         } else if (key.crit == 1) {
             if (g.rank == 2)
                 k_run_flags_grad<T, 2><<<sms * 16, 256, 0, cs>>>(B, ctl, g, make_grad_rule(key.rthr, key.cthr),
@@ -969,7 +994,7 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         k_run_neighbors<<<sms * 8, 128, 0, cs>>>(B, ctl, g);
         AMR_LAUNCHED("k_run_neighbors");
     }
-    k_run_commit<<<1, 256, 0, cs>>>(B, ctl, key.k, g.cells, key.crit != 0 ? 1 : 0, sp);
+    k_run_commit<<<1, 256, 0, cs>>>(B, ctl, key.k, g.cells, key.crit != 0 ? 1 : 0, sp, key.pair ? 1 : 0);
     AMR_LAUNCHED("k_run_commit");
     return AMR_OK;
 }
@@ -1289,6 +1314,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
         al(reinterpret_cast<void**>(&t->meta[b]), cap * g.ndir * sizeof(amr_halo_meta));
     }
     al(reinterpret_cast<void**>(&t->prec), cap * sizeof(int4));
+    al(reinterpret_cast<void**>(&t->frec), cap * sizeof(int4));
     al(reinterpret_cast<void**>(&t->flags), cap);
     al(reinterpret_cast<void**>(&t->rmark), cap);
     al(reinterpret_cast<void**>(&t->chead), cap);
@@ -1388,7 +1414,8 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     void*        l1     = al(cap * sizeof(int32_t));
     void*        m0     = al(cap * g.ndir * sizeof(amr_halo_meta));
     void*        m1     = al(cap * g.ndir * sizeof(amr_halo_meta));
-    void*        pr     = al(cap * sizeof(int4)); // pass records: rebuilt before every use
+    void*        pr     = al(cap * sizeof(int4)); // pass and face records: rebuilt before every use
+    void*        fr     = al(cap * sizeof(int4));
     void*        fl     = al(cap);
     void*        rm     = al(cap);
     void*        ch     = al(cap);
@@ -1429,7 +1456,9 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
         cudaFree(t->meta[b]);
     }
     cudaFree(t->prec);
+    cudaFree(t->frec);
     t->prec = static_cast<int4*>(pr);
+    t->frec = static_cast<int4*>(fr);
     cudaFree(t->flags);
     cudaFree(t->rmark);
     cudaFree(t->chead);
@@ -1812,8 +1841,8 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
                     const size_t cst  = static_cast<size_t>(K) * nl;
                     auto         pass = [&]<int N>(const StepCfg& c) -> amr_status {
                         return with_depth<T>(D, [&]<int DD>() -> amr_status {
-                            return launch_step2d_pass<T, N, 1, DD>(in, out, t->prec, P, cf, cf2, cst, t->status + 7,
-                                                                   c, s);
+                            return launch_step2d_pass<T, N, 1, DD>(in, out, t->prec, P, nl, cf, cf2, cst,
+                                                                   t->status + 7, c, s);
                         });
                     };
                     return t->g.n == 16 ? pass.template operator()<16>(cfg_pair) : pass.template operator()<8>(StepCfg{});

@@ -395,7 +395,10 @@ amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_n
 /* Launch shape of the 2D update kernel used by the tree's last advance or
  * run: warps per block, copy stages per warp, blocks (0 = full residency).
  * The autotuner picks it on first use per device, dtype, patch shape and
- * leaf-count octave (AMR_GB300_AUTOTUNE=0 keeps the default 8, 2, 0). */
+ * leaf-count octave (AMR_GB300_AUTOTUNE=0 keeps the default 8, 2, 0;
+ * AMR_GB300_STEP_CONFIG="warps,stages,blocks_per_sm" fixes it, with
+ * blocks_per_sm 0 for full residency, warps and stages one of the tuned
+ * pairs). */
 amr_status amr_tree_step_config(const amr_tree* t, int32_t* warps, int32_t* stages, int32_t* blocks);
 
 /* Block until all work queued on the tree's stream has finished. */
