@@ -181,7 +181,9 @@ k_run_flags_grad(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, in
                 lo             = B.bounds[2 * inst];
                 hi             = B.bounds[2 * inst + 1];
             }
-            B.flags[p] = gradient_decision(any, all, B.levels[tb][p], lo, hi);
+            const int8_t f = gradient_decision(any, all, B.levels[tb][p], lo, hi);
+            B.flags[p]     = f;
+            if (f != FLAG_STABLE) ctl->flagged = 1;
         }
     }
 }
@@ -200,7 +202,8 @@ k_run_flags2d(RunBufs B, RunCtl* ctl, Geo g, GradRule rule, int min_level, int m
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     flags2d_body<T, N, H, false>(static_cast<const T*>(B.state[ctl->sb ^ sp]), B.meta[tb], B.keys[tb], ctl->P, g, rule,
-                                 min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp);
+                                 min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp,
+                                 &ctl->flagged);
 }
 
 // The same flags on a tree whose every relation is same-level, from the pass
@@ -217,7 +220,8 @@ k_run_flags2d_uniform(RunBufs B, RunCtl* ctl, GradRule rule, int min_level, int 
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     flags2d_uniform_body<T, N, H>(static_cast<const T*>(B.state[ctl->sb ^ sp]), B.prec, B.frec, ctl->P, rule,
-                                  min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp);
+                                  min_level, max_level, B.bounds, B.flags, &ctl->err, tiles, bars, p, nwarp,
+                                  &ctl->flagged);
 }
 
 // Max-value flags (k_flags_max's rule over the exchanged ghosts), one block
@@ -247,7 +251,11 @@ k_run_flags_max(RunBufs B, RunCtl* ctl, Geo g, double rthr, double cthr, int min
             if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
             __syncthreads();
         }
-        if (threadIdx.x == 0) B.flags[p] = max_decision(red[0], B.levels[tb][p], rthr, cthr, lo, hi);
+        if (threadIdx.x == 0) {
+            const int8_t f = max_decision(red[0], B.levels[tb][p], rthr, cthr, lo, hi);
+            B.flags[p]     = f;
+            if (f != FLAG_STABLE) ctl->flagged = 1;
+        }
         __syncthreads();
     }
 }
@@ -256,16 +264,17 @@ k_run_flags_max(RunBufs B, RunCtl* ctl, Geo g, double rthr, double cthr, int min
 #define AMR_RUN_LEAVES(P)                                                                              \
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (P); i += gridDim.x * blockDim.x)
 
+// The flag kernels set ctl->flagged when they flag some leaf; without one
+// the re-mesh changes nothing (reconstruction_is_noop, ndtree.hpp:1242-1246)
+// and the marks are not needed.
 __global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err) return;
-    const int P = ctl->P, tb = ctl->tb;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->changed = 0;
+    if (!ctl->flagged) return;
+    const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P)
-    {
-        mark_leaf(B.keys[tb], B.flags, P, g, B.rmark, B.chead, i);
-        if (B.flags[i] != FLAG_STABLE) ctl->flagged = 1;
-    }
+    mark_leaf(B.keys[tb], B.flags, P, g, B.rmark, B.chead, i);
 }
 
 // With no leaf flagged the re-mesh changes nothing (reconstruction_is_noop,
@@ -428,7 +437,7 @@ k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp, i
         const int  P  = ctl->P;
         const bool ok = ctl->err == 0;
         chg           = (remesh && ok && ctl->changed) ? 1 : 0;
-        ctl->flagged  = 0; // the next interval's marks set it again
+        ctl->flagged  = 0; // the next interval's flag kernels set it again
         ctl->recs     = records && ok && !chg ? 1 : 0; // this interval's records outlive it if the tree stays
         if (ok) {
             ctl->sb ^= sp;

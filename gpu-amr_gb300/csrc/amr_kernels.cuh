@@ -1794,7 +1794,8 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
                                              const uint64_t* __restrict__ keys, int P, const Geo& g,
                                              const GradRule& rule, int min_level, int max_level,
                                              const int32_t* __restrict__ bounds, int8_t* __restrict__ flags,
-                                             int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp)
+                                             int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp,
+                                             int32_t* flagged = nullptr)
 {
     using Sh                = Flags2dShape<T, N, H, FromBuffer>;
     constexpr int      P1   = Sh::P1;
@@ -1941,7 +1942,9 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
                 lo             = bounds[2 * inst];
                 hi             = bounds[2 * inst + 1];
             }
-            flags[p] = gradient_decision(any, all, key_level(key), lo, hi);
+            const int8_t f = gradient_decision(any, all, key_level(key), lo, hi);
+            flags[p]       = f;
+            if (flagged && f != FLAG_STABLE) *flagged = 1; // some leaf will change: the re-mesh runs
         }
         __syncwarp();
     }
@@ -1960,7 +1963,7 @@ __device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, c
                                                      const int4* __restrict__ frec, int P, const GradRule& rule,
                                                      int min_level, int max_level, const int32_t* __restrict__ bounds,
                                                      int8_t* __restrict__ flags, int32_t* err, T* tiles,
-                                                     uint64_t* bars, int p, int nwarp)
+                                                     uint64_t* bars, int p, int nwarp, int32_t* flagged)
 {
     using Sh                = Flags2dShape<T, N, H, false>;
     constexpr int      P1   = Sh::P1;
@@ -2072,7 +2075,9 @@ __device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, c
                 lo             = bounds[2 * inst];
                 hi             = bounds[2 * inst + 1];
             }
-            flags[p] = gradient_decision(any, all, pass_level(c0), lo, hi);
+            const int8_t f = gradient_decision(any, all, pass_level(c0), lo, hi);
+            flags[p]       = f;
+            if (f != FLAG_STABLE) *flagged = 1; // some leaf will change: the re-mesh runs
         }
         __syncwarp();
         f0 = f1;
