@@ -139,6 +139,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
                  : "memory");
     return ok != 0;
 }
+// 1D bulk copy shared -> global in a bulk async-group of the issuing
+// thread, and that thread's waits: until the sources of all but the newest
+// `Pending` groups have been read (the shared memory may be reused), or
+// until every group has completed (the global writes are done).
+__device__ __forceinline__ void bulk_copy_s2g(void* dst, const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int Pending>
+__device__ __forceinline__ void bulk_wait_read()
+{
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(Pending) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 constexpr int kWaitLimit = 1 << 22;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit = kWaitLimit)
 {

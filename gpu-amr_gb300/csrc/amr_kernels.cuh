@@ -1488,8 +1488,13 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
                       in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
     };
+    // A tiles are in flight ahead of the current one; a slot is refilled only
+    // once the bulk store of its previous patch has read it, and at most
+    // PEND stores (the newest) may still be reading when a slot is refilled
+    constexpr int A    = S >= 2 ? S - 2 : 0;
+    constexpr int PEND = S - 1 - A;
     if (lane == 0)
-        for (int j = 0; j < S - 1; ++j)
+        for (int j = 0; j < A; ++j)
             if (p + j * nwarp < P) request(p + j * nwarp, j);
     uint32_t   phase = 0;
     const int  rb = lane >> 3, cb = lane & 7; // the lane's block
@@ -1546,8 +1551,11 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
 
     for (int it = 0; p < P; ++it, p += nwarp) {
         const int b  = it % S;
-        const int pf = p + (S - 1) * nwarp;
-        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
+        const int pf = p + A * nwarp;
+        if (pf < P && lane == 0) {
+            bulk_wait_read<PEND>(); // the slot's last store has read it
+            request(pf, (it + A) % S);
+        }
         const int pa = p + nwarp, pb = p + 2 * nwarp;
         if (pb < P) r2 = __ldg(rec + pb);
         if (pa < P) fetch(r1, sb);
@@ -1567,12 +1575,13 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
             if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
             phase ^= 1u << b;
-            for (int j = 1; j < S; ++j)
+            for (int j = 1; j <= A; ++j)
                 if (p + j * nwarp < P) {
                     const int sl2 = (it + j) % S;
                     mbar_wait_bounded(&bars[sl2], (phase >> sl2) & 1u);
                     phase ^= 1u << sl2;
                 }
+            if (lane == 0) bulk_wait_all();
             return;
         }
         phase ^= 1u << b;
@@ -1647,21 +1656,25 @@ __device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __
         else if (ux != 0) steps.template operator()<true, false>();
         else if (uy != 0) steps.template operator()<false, true>();
         else steps.template operator()<false, false>();
-        // back into the tile in its own orientation, then the interior rows out
+        // back into the tile in its own orientation, then the interior rows
+        // out by one bulk store (the async proxy sees every lane's writes)
 #pragma unroll
         for (int a = 0; a < BR; ++a)
 #pragma unroll
             for (int e = 0; e < BC; ++e) cell[a * sr + e * sc] = v[a][e];
+        fence_proxy_async_smem();
         __syncwarp();
-        const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
-        uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
-        for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
-        __syncwarp();
+        if (lane == 0) {
+            bulk_copy_s2g(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO,
+                          reinterpret_cast<const char*>(tile) + LO, BYTES);
+            bulk_commit();
+        }
         r0 = r1;
         r1 = r2;
 #pragma unroll
         for (int d = 1; d <= D; ++d) sa[d] = sb[d];
     }
+    if (lane == 0) bulk_wait_all(); // the last stores complete before the block's shared memory goes
 }
 
 // Warp w of the block: its S tiles, its exchange buffers and its S barriers
