@@ -781,6 +781,99 @@ def ssprk_extra(torch, A, stream, with_cpu=True):
     return out
 
 
+# ------------------------------------------------------------ DG patch solver
+# The reference's DG configuration (order 2, 2D, 4x4 cells per patch, four
+# advected variables per node, SSPRK2, velocity 1): its own main loop runs a
+# uniform level-5 start (1024 leaves); the throughput line uses level 9
+# (262144 leaves, 4.2 M cells, 16 nodal values each: 1.2 GB per state buffer).
+DG = dict(levels=(5, 9), steps={5: 200, 9: 20}, dt0=0.01, cpu_level=5, cpu_steps=3)
+
+
+def dg_extra(torch, A, stream, with_cpu=True):
+    """DG steps through amr_tree_dg_advance (CUDA events on the tree's stream
+    around the timed steps, after the first step at the initial dt), and the
+    numpy restatement on the host for a few steps of the level-5 tree; the
+    states must agree bit for bit."""
+    from oracle import dg_oracle as G
+
+    D = DG
+    out = {"workload": "nodal DG advection (the reference's dg_helpers configuration: order 2, 2D, 4x4 cells per "
+                       "patch + 1 ghost, 4 variables per node, SSPRK2, velocity 1, initial dt 0.01 then the CFL "
+                       "step), uniform levels, no re-mesh",
+           "unit": "cell-updates/s (interior cells, each with 16 nodal values)"}
+    for lv in D["levels"]:
+        t = A.Tree(2, 4, 1, 10, capacity=(1 << (2 * lv)) + 64, dtype=A.F64, fields=16, stream=stream.cuda_stream)
+        t.refine_uniform(lv)
+        cells = t.size * 16
+        # the initial nodal field of the reference's scenario, built per patch
+        # on the host from the restatement (sin at the nodes)
+        u0 = np.zeros((16, t.size, 6, 6))
+        U = G.initial_state(lv) if lv <= 6 else None
+        if U is not None:
+            u0 = _dg_fields(G.to_leaves(U, lv))
+        else:
+            rng = np.random.default_rng(11)
+            u0[:, :, 1:5, 1:5] = rng.uniform(-1.0, 1.0, (16, t.size, 4, 4))
+        t.upload_state(u0)
+        dt, tm = t.dg_advance(1, D["dt0"])  # the first step at the initial dt; warm-up
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = D["steps"][lv]
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            dt, tm = t.dg_advance(n, dt, tm)
+            ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        rate = cells * n / (ms * 1e-3)
+        # per stage the kernel reads the stage input (16 x 8 B per cell; the
+        # neighbours' values come from L1/L2) and, in the second stage, u^n,
+        # and writes the result: 2 + 3 = 5 x 128 B per cell and step
+        alg = 5 * 128
+        hbm = measured_peaks().get("hbm_gbs")
+        rec = {"value": rate, "unit": "cell-updates/s", "ms_per_step": ms / n, "leaves": t.size, "cells": cells,
+               "steps_timed": n, "dt_after": dt,
+               "roofline": {"bound": "hbm", "achieved": alg * rate / 1e9, "peak": hbm, "unit": "GB/s",
+                            "frac": alg * rate / 1e9 / hbm if hbm else None,
+                            "algorithmic_bytes_per_cell_update": alg,
+                            "note": "two stages per step, each reads its input state and writes its output; "
+                                    "the second also reads u^n; the FP64 arithmetic (about 1100 operations "
+                                    "per cell and step, no contraction) is the likelier bound"}}
+        if with_cpu and lv == D["cpu_level"]:
+            L0 = D["cpu_level"]
+            U0 = G.initial_state(L0)
+            c0 = time.perf_counter()
+            outs, _ = G.run(L0, D["cpu_steps"], dt0=D["dt0"], U=U0)
+            csec = time.perf_counter() - c0
+            g = A.Tree(2, 4, 1, 10, capacity=(1 << (2 * L0)) + 64, dtype=A.F64, fields=16,
+                       stream=stream.cuda_stream)
+            g.refine_uniform(L0)
+            g.upload_state(_dg_fields(G.to_leaves(U0, L0)))
+            g.dg_advance(D["cpu_steps"], D["dt0"])
+            mine = _dg_leaves(g.download_state())
+            rec["cpu_baseline"] = {"value": (16 << (2 * L0)) * D["cpu_steps"] / csec, "unit": "cell-updates/s",
+                                   "cores": 1, "kind": "port",
+                                   "sample": f"first {D['cpu_steps']} steps of the level-{L0} tree, numpy "
+                                             "restatement (vectorised over cells, one thread)"}
+            rec["parity_first_steps_bit_exact"] = bool(np.array_equal(mine, G.to_leaves(outs[-1], L0)))
+            g.close()
+        t.close()
+        out[f"level{lv}"] = rec
+    return out
+
+
+def _dg_fields(st):
+    """[leaf, cell, node, var] -> the tree's [field, leaf, 6, 6] (ghosts zero)."""
+    P = st.shape[0]
+    a = np.zeros((16, P, 6, 6))
+    a[:, :, 1:5, 1:5] = st.reshape(P, 4, 4, 4, 4).transpose(3, 4, 0, 1, 2).reshape(16, P, 4, 4)
+    return a
+
+
+def _dg_leaves(a):
+    P = a.shape[1]
+    return a[:, :, 1:5, 1:5].reshape(4, 4, P, 4, 4).transpose(2, 3, 4, 0, 1).reshape(P, 16, 4, 4)
+
+
 # ------------------------------------------------------------ adjoint form
 ADJOINT = dict(n=16, halo=1, depth=8, base_level=5, max_level=7, rthr=0.01, cthr=0.002, rounds=3, steps=400,
                every=20, cfl=0.4, velocity=(1.0, 0.5), directions=64, eps=1e-4, pert=0.05, seed=7)
@@ -994,6 +1087,7 @@ def gpu_arm(args, rank, world):
             "plain_fp64_config2_max_level7": lambda: depth7_extra(torch, A, dev, stream, flush, max(1, args.steps)),
             "euler_benchmark": lambda: euler_extra(torch, A, stream, with_cpu=cpu),
             "ssprk_advection": lambda: ssprk_extra(torch, A, stream, with_cpu=cpu),
+            "dg_advection": lambda: dg_extra(torch, A, stream, with_cpu=cpu),
         }
         for name, fn in table.items():
             if args.extra is None or name in args.extra:

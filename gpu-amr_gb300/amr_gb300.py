@@ -121,6 +121,7 @@ def lib():
         L.amr_tree_reserve.argtypes = [vp, sz]
         L.amr_tree_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl]
         L.amr_tree_advance_ssprk.argtypes = [vp, sz, i32, C.POINTER(dbl), dbl, dbl]
+        L.amr_tree_dg_advance.argtypes = [vp, sz, C.POINTER(dbl), C.POINTER(dbl)]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -357,6 +358,14 @@ class Tree:
         None: the per-instance velocities.  finish_advance() as for advance."""
         v = None if velocity is None else _vec3(velocity)
         check(lib().amr_tree_advance_ssprk(self._h, steps, order, v, cfl, remaining))
+
+    # -------------------------------------------------------------- DG
+    def dg_advance(self, steps, dt, time=0.0):
+        """Nodal DG steps (order 2, 2D, 16 fields): returns (next step size,
+        time).  dt is the step size of the first step."""
+        d, t = C.c_double(dt), C.c_double(time)
+        check(lib().amr_tree_dg_advance(self._h, steps, C.byref(d), C.byref(t)))
+        return d.value, t.value
 
     # -------------------------------------------------------------- Euler
     def euler_advance(self, steps, gamma, cfl, remaining=1.7976931348623157e308):

@@ -37,7 +37,7 @@ def nvcc() -> str:
 
 # Translation units whose arithmetic must match the reference's CPU code
 # operation for operation: no multiply-add contraction.
-NO_CONTRACTION = {"amr_euler.cu", "amr_ssprk.cu"}
+NO_CONTRACTION = {"amr_euler.cu", "amr_ssprk.cu", "amr_dg.cu"}
 
 
 def sources():

@@ -1,0 +1,43 @@
+// Interface of the nodal DG stage kernel (amr_dg.cu, compiled without
+// multiply-add contraction).
+#pragma once
+
+#include "amr_device.cuh"
+
+namespace amr_gb300 {
+
+// The reference's DG patch solver configuration (include/config/
+// generated_config.hpp): order 2 (2 x 2 Gauss-Legendre nodes per cell), 2D,
+// 4 variables per node, 4 x 4 cells per patch with one ghost cell, linear
+// advection with velocity 1.  On the tree a cell's 16 nodal values are 16
+// fields (field = node * 4 + variable, node = x-node * 2 + y-node).
+constexpr int kDgOrder = 2, kDgVars = 4, kDgFields = 16, kDgPatch = 4;
+
+// Basis tables: face kernels k[s][i] = L_i(s) (s = 0, 1) and the derivative
+// tensor d[i][j] = L_i'(x_j) of the 1D Lagrange basis at the Gauss-Legendre
+// points on [0, 1].
+struct DgTables {
+    double k[2][2];
+    double d[2][2];
+};
+DgTables dg_tables();
+
+// One SSPRK2 stage over every cell of P padded patches.  mode 0: out = in +
+// dt R(in); mode 1: out = ((un + in) + dt R(in)) * 0.5.  Ghost cells take a
+// zero residual (the reference combines whole patch containers).  out may
+// alias un.
+struct DgStage {
+    const double*   in;
+    const double*   un;
+    double*         out;
+    const uint64_t* keys;
+    int             P;
+    Geo             g;
+    size_t          fstride;
+    double          dt;
+    int             mode;
+    cudaStream_t    stream;
+};
+cudaError_t dg_stage(const DgStage& s);
+
+} // namespace amr_gb300

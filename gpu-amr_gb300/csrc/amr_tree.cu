@@ -19,6 +19,7 @@
 #include "amr_cycle.cuh"
 #include "amr_euler.cuh"
 #include "amr_ssprk.cuh"
+#include "amr_dg.cuh"
 #include "amr_graph.cuh"
 #include "amr_vtk.cuh"
 
@@ -1287,7 +1288,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
         if (g.inst_shift + bits > 64) return fail(AMR_ERR_INVALID, "too many instances for the tree depth");
     }
     if (static_cast<size_t>(K) > desc->capacity) return fail(AMR_ERR_INVALID, "capacity below the instance count");
-    if (desc->fields < 0 || desc->fields > 8) return fail(AMR_ERR_INVALID, "bad field count");
+    if (desc->fields < 0 || desc->fields > 16) return fail(AMR_ERR_INVALID, "bad field count");
     const int nvar = desc->fields > 1 ? desc->fields : 1;
     if (nvar > 1 && K > 1) return fail(AMR_ERR_INVALID, "forests hold one field");
     int ndev = 0;
@@ -1956,6 +1957,51 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
     // the last stage); criteria read them from the buffer as it does
     t->ghosts_valid = true;
     t->batch_open   = true;
+    return AMR_OK;
+}
+
+amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time)
+{
+    if (!t || !dt) return fail(AMR_ERR_INVALID, "null argument");
+    const Geo& g = t->g;
+    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
+        return fail(AMR_ERR_INVALID, "the DG advance needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
+    if (!t->uniform) return fail(AMR_ERR_INVALID, "the DG advance needs a tree whose every relation is same-level");
+    if (!(*dt > 0.0)) return fail(AMR_ERR_INVALID, "the DG step size must be positive");
+    cudaStream_t s = t->stream;
+    DgStage      st{};
+    st.keys    = t->keys[t->tb];
+    st.P       = static_cast<int>(t->size);
+    st.g       = g;
+    st.fstride = t->fstride();
+    st.stream  = s;
+    // CFL step of the finest cells (solver.hpp:221-226 with |v| = 1)
+    const double edge   = (1.0 / static_cast<double>(1u << t->max_level_host)) / static_cast<double>(kDgPatch);
+    const double scale  = 1.0 / (std::pow(static_cast<double>(kDgOrder), 2.0) + 1.0);
+    const double dt_cfl = scale * 0.5 * edge / 1.0;
+    double       h      = *dt, acc = time ? *time : 0.0;
+    uint64_t     launches = 0;
+    for (size_t k = 0; k < steps; ++k) {
+        if (amr_status hs = halo_buffer(t, t->cur); hs != AMR_OK) return hs;
+        st.in   = static_cast<const double*>(t->cur);
+        st.un   = static_cast<const double*>(t->cur);
+        st.out  = static_cast<double*>(t->nxt);
+        st.dt   = h;
+        st.mode = 0;
+        AMR_CUDA(dg_stage(st));
+        if (amr_status hs = halo_buffer(t, t->nxt); hs != AMR_OK) return hs;
+        st.in   = static_cast<const double*>(t->nxt);
+        st.out  = static_cast<double*>(t->cur); // u^n is read and replaced cell by cell
+        st.mode = 1;
+        AMR_CUDA(dg_stage(st));
+        launches += 2;
+        acc += h;
+        h = std::min(h, std::min(h, dt_cfl));
+    }
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
+    t->ghosts_valid = true; // the ghosts the reference's tree holds after a step
+    *dt             = h;
+    if (time) *time = acc;
     return AMR_OK;
 }
 

@@ -144,7 +144,8 @@ typedef struct amr_tree_desc {
     int32_t            instances; /* independent trees held together (a forest);
                                      0 or 1 = one tree */
     int32_t            fields;    /* state fields per cell (the cell type's SoA
-                                     tuple; Euler: rank + 2); 0 or 1 = one */
+                                     tuple; Euler: rank + 2; DG: 16); 0 or 1 =
+                                     one, at most 16 */
 } amr_tree_desc;
 
 /* ndtree(capacity) (include/ndtree/ndtree.hpp:320-425): one root leaf with
@@ -284,6 +285,27 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_s
  * for the simulated time and executed steps. */
 amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const double* velocity3, double cfl,
                                   double remaining_time);
+
+/* ------------------------------------------------------------- DG
+ * Nodal discontinuous-Galerkin steps of the reference's DG patch solver
+ * (include/dg_helpers: DGSolver::advance_patches, solver.hpp:159-232, with
+ * RHSEvaluator::evaluate, rhs.hpp:117-255, and SSPRK2, time.hpp:134-168) in
+ * its generated configuration (include/config/generated_config.hpp): order
+ * 2, 2D, 4 x 4 cells per patch with one ghost cell, four advected variables
+ * per node, velocity 1, Courant number 0.5.  The tree holds the 16 nodal
+ * values of a cell as 16 FP64 fields (field = node * 4 + variable, node =
+ * x-node * 2 + y-node); create it with rank 2, n 4, halo 1, 16 fields.
+ * Every relation must be same-level (the DG re-mesh is not provided):
+ * AMR_ERR_INVALID otherwise.  Each step: halo exchange, the first stage,
+ * halo exchange, the second stage; no halo exchange follows the last stage
+ * (the ghost cells hold the stage combination, as the reference's tree
+ * does).  *dt: on entry the step size of the first step (the reference's
+ * initial_dt for a new run), on return the next one; each step then takes
+ * dt = min(dt, 0.1 x finest cell edge), the reference's CFL rule for this
+ * order (1 / (order^dim + 1) x Courant x edge / |v|).  *time (optional)
+ * accumulates the step sizes taken.  Interior states are bit-identical to
+ * the reference's CPU path. */
+amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time);
 
 /* ------------------------------------------------------------- Euler
  * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through

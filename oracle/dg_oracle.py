@@ -1,0 +1,221 @@
+"""CPU restatement (numpy, FP64) of the reference's nodal DG patch solver on a
+uniform periodic tree.  Test infrastructure only: it checks the CUDA DG path
+and never runs inside it.
+
+Reference (paths within the reference project):
+  configuration  include/config/generated_config.hpp (order 2, 2D, 4 variables
+                 per node, 4x4 cells per patch, one ghost cell, SSPRK2,
+                 advection with velocity 1, Courant number 0.5)
+  basis          include/dg_helpers/basis/gauss_legendre.hpp:16-35 (points and
+                 weights on [0, 1]), lagrange.hpp:37-67 (L_i, L_i'),
+                 polynomial.hpp:85-93 (face kernels)
+  tables         include/dg_helpers/globals/kernels.hpp:15-73 (face kernels at
+                 0 and 1, mass tensors w (x) w and their inverse, derivative
+                 tensor D[i][j] = L_i'(x_j))
+  flux           include/dg_helpers/equations/advection.hpp:19-35 (F_d = v u)
+  RHS            include/dg_helpers/rhs.hpp:117-255 with volume.hpp:24-44 and
+                 surface.hpp:36-113 (Rusanov flux, surface mass, lift)
+  stages         include/dg_helpers/time_integration/time.hpp:134-168 (SSPRK2)
+  step loop      include/dg_helpers/solver.hpp:117-232 (dt = initial dt for the
+                 first step, then min(dt, 0.1 x cell edge / |v| ...))
+
+Each elementwise operation is evaluated in the reference's order and
+grouping, so results are bit-identical to the reference on the same inputs
+(pinned against fixtures produced by running the reference itself,
+tests/golden/make_dg_golden.py).
+
+State layout: U[cy, cx, ix, iy, v] over the global cell grid of a uniform
+level (C = 4 * 2^level cells per side, cy rows, cx columns), nodes ix (x) and
+iy (y), variables v.
+"""
+import numpy as np
+
+ORDER, DIM, NVAR, PATCH = 2, 2, 4, 4
+COURANT = 0.5
+VELOCITY = 1.0
+
+
+def tables():
+    """Basis tables of the order-2 tensor Lagrange basis at Gauss-Legendre
+    points on [0, 1], computed with the reference's arithmetic."""
+    pre_p = np.array([-0.5773502691896257, 0.5773502691896257])
+    pre_w = np.array([1.0, 1.0])
+    half = (1.0 - 0.0) / 2.0
+    mid = (0.0 + 1.0) / 2.0
+    p = mid + half * pre_p
+    w = pre_w * half
+
+    def lag(i, x):
+        num, den = 1.0, 1.0
+        for k in range(ORDER):
+            if k == i:
+                continue
+            num *= (x - p[k])
+            den *= (p[i] - p[k])
+        return num / den
+
+    def dlag(i, x):
+        res = 0.0
+        for j in range(ORDER):
+            if j == i:
+                continue
+            term = 1.0 / (p[i] - p[j])
+            for k in range(ORDER):
+                if k in (i, j):
+                    continue
+                term *= (x - p[k]) / (p[i] - p[k])
+            res += term
+        return res
+
+    kern = np.array([[lag(i, 0.0) for i in range(ORDER)], [lag(i, 1.0) for i in range(ORDER)]])
+    D = np.array([[dlag(i, p[j]) for j in range(ORDER)] for i in range(ORDER)])
+    mass = np.outer(w, w)
+    inv_w = 1.0 / w
+    inv_mass = np.outer(inv_w, inv_w)
+    return dict(points=p, weights=w, kern=kern, D=D, mass=mass, inv_mass=inv_mass, smass=w.copy())
+
+
+T = tables()
+
+
+def initial_state(level, t=0.0):
+    """Nodal initial values of the advection scenario (advection.hpp:69-86):
+    v0 = sin(2 pi (x + y - 2t)), v1 = sin(2 pi (y - t)), v2 = v3 = 1 at each
+    node position (cell centre + (node - 0.5) x cell size)."""
+    C = PATCH << level
+    cell = (1.0 / float(1 << level)) / float(PATCH)
+    U = np.empty((C, C, ORDER, ORDER, NVAR))
+    cidx = np.arange(C, dtype=np.float64)
+    # cell centres: patch corner + (local + 0.5) * cell; uniform grid gives
+    # the same value as (global index + 0.5) * cell only up to rounding, so
+    # follow the reference's corner + local form
+    for cy in range(C):
+        for cx in range(C):
+            pcx, lcx = divmod(cx, PATCH)
+            pcy, lcy = divmod(cy, PATCH)
+            corner_x = float(pcx << (6 - level)) * (1.0 / float(1 << 6))
+            corner_y = float(pcy << (6 - level)) * (1.0 / float(1 << 6))
+            ccx = corner_x + (float(lcx) + 0.5) * cell
+            ccy = corner_y + (float(lcy) + 0.5) * cell
+            for ix in range(ORDER):
+                for iy in range(ORDER):
+                    x = ccx + (T["points"][ix] - 0.5) * cell
+                    y = ccy + (T["points"][iy] - 0.5) * cell
+                    U[cy, cx, ix, iy, 0] = np.sin(2.0 * 3.14159265358979323846 * (x + y - 2.0 * t))
+                    U[cy, cx, ix, iy, 1] = np.sin(2.0 * 3.14159265358979323846 * (y - t))
+                    U[cy, cx, ix, iy, 2:] = 1.0
+    del cidx
+    return U
+
+
+def _contract(A, k, dim):
+    """contract<dim>(A, k) (container_algorithms.hpp:217-298): the first term,
+    then the second added (order 2)."""
+    if dim == 0:
+        return A[..., 0, :, :] * k[0] + A[..., 1, :, :] * k[1]
+    return A[..., :, 0, :] * k[0] + A[..., :, 1, :] * k[1]
+
+
+def rhs(U, edge):
+    """Residual R(U) of every interior cell (rhs.hpp: volume, surface, inverse
+    mass) on the periodic grid."""
+    K, D, M = T["kern"], T["D"], T["mass"]
+    vol = edge * edge  # volume(): 1.0 * edge * edge
+    vol = (1.0 * edge) * edge
+    area = 1.0 * edge
+    inv_jac = 1.0 / edge
+    F = VELOCITY * U  # both flux components
+    G = F * M[None, None, :, :, None]  # tensor_dot(flux, volume_mass)
+    s = inv_jac * vol
+    du = np.zeros_like(U)
+    # derivative_contraction(D, G, 0): r[i][j] = (0 + D[i,0] G[0][j]) + D[i,1] G[1][j]
+    c0 = np.empty_like(U)
+    for i in range(ORDER):
+        c0[:, :, i, :, :] = (0.0 + D[i, 0] * G[:, :, 0, :, :]) + D[i, 1] * G[:, :, 1, :, :]
+    du = du + s * c0
+    c1 = np.empty_like(U)
+    for j in range(ORDER):
+        c1[:, :, :, j, :] = (0.0 + D[j, 0] * G[:, :, :, 0, :]) + D[j, 1] * G[:, :, :, 1, :]
+    du = du + s * c1
+    lam = 1.0  # |v|: the running maximum over the faces is 1 from the first face on
+    # faces in the reference's direction order: padded dimension 0 (y) -, +,
+    # then dimension 1 (x) -, +; tensor dimension = 1 - padded dimension
+    for pdim, sign in ((0, -1), (0, 1), (1, -1), (1, 1)):
+        adim = 1 - pdim
+        sidx = 0 if sign < 0 else 1
+        shift = (1, 0) if pdim == 0 else (0, 1)
+        Un = np.roll(U, shift=(-sign * shift[0], -sign * shift[1]), axis=(0, 1))
+        Fn = VELOCITY * Un
+        uf = _contract(U, K[sidx], adim)
+        ff = _contract(F, K[sidx], adim)
+        un = _contract(Un, K[1 - sidx], adim)
+        fn = _contract(Fn, K[1 - sidx], adim)
+        nf = (float(sign) * (ff + fn) * 0.5 + (uf - un) * (0.5 * lam)) * area
+        wf = nf * T["smass"][None, None, :, None]
+        kv = K[sidx]
+        if adim == 1:  # tensor_product(weighted, kernel): [face node][normal node]
+            face = wf[:, :, :, None, :] * kv[None, None, None, :, None]
+        else:          # tensor_product(kernel, weighted): [normal node][face node]
+            face = kv[None, None, :, None, None] * wf[:, :, None, :, :]
+        du = du - face
+    return du * (T["inv_mass"] / vol)[None, None, :, :, None]
+
+
+def ssprk2_step(U, edge, dt):
+    """One SSPRK2 step (time.hpp:134-168): u* = u + dt R(u);
+    u' = ((u + u*) + dt R(u*)) * 0.5."""
+    us = U + rhs(U, edge) * dt
+    return (U + us + rhs(us, edge) * dt) * 0.5
+
+
+def run(level, steps, dt0=0.01, U=None):
+    """The reference's step loop on a uniform level without re-mesh: returns
+    the states after each step and the step sizes used."""
+    edge = (1.0 / float(1 << level)) / float(PATCH)
+    if U is None:
+        U = initial_state(level)
+    scale = 1.0 / (float(ORDER) ** DIM + 1.0)
+    dt_cfl = scale * COURANT * edge / 1.0
+    dt = dt0
+    out, dts = [], []
+    for _ in range(steps):
+        U = ssprk2_step(U, edge, dt)
+        out.append(U)
+        dts.append(dt)
+        dt = min(dt, min(dt, dt_cfl))
+    return out, dts
+
+
+# ---------------------------------------------------------------- layout
+def morton_patch_order(level):
+    """Patch (py, px) of each leaf of a uniform level in Morton order (x bits
+    at even positions)."""
+    n = 1 << level
+    order = []
+    for m in range(n * n):
+        x = y = 0
+        for b in range(level):
+            x |= ((m >> (2 * b)) & 1) << b
+            y |= ((m >> (2 * b + 1)) & 1) << b
+        order.append((y, x))
+    return order
+
+
+def to_leaves(U, level):
+    """Grid state -> leaves in Morton order, [leaf, cell (row-major, x
+    fastest), node (ix * 2 + iy), variable]: the reference's dump layout."""
+    P = PATCH
+    out = []
+    for (py, px) in morton_patch_order(level):
+        blk = U[py * P:(py + 1) * P, px * P:(px + 1) * P]  # [ly, lx, ix, iy, v]
+        out.append(blk.reshape(P * P, ORDER * ORDER, NVAR))
+    return np.stack(out)
+
+
+def from_leaves(L, level):
+    P = PATCH
+    C = P << level
+    U = np.empty((C, C, ORDER, ORDER, NVAR))
+    for n, (py, px) in enumerate(morton_patch_order(level)):
+        U[py * P:(py + 1) * P, px * P:(px + 1) * P] = L[n].reshape(P, P, ORDER, ORDER, NVAR)
+    return U

@@ -1,0 +1,69 @@
+"""Generate the DG golden fixtures in this folder from the REAL reference.
+
+Builds oracle/_ref/ref_dg_driver (the unmodified reference DG patch solver,
+include/dg_helpers, compiled by oracle/Makefile; needs the reference
+checkout, so this runs only where it is present) and records each scenario
+as a compressed .npz:
+
+  ids            Morton ids of the leaves (uniform level, Morton order)
+  state          [dump, leaf, cell, node, variable] interior nodal values;
+                 dump 0 is the initial state, dump k the state after step k
+  dt             [dump] step size used to reach each dump (0 for dump 0)
+
+Usage:  python tests/golden/make_dg_golden.py
+"""
+from __future__ import annotations
+
+import struct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+DRIVER = REPO / "oracle" / "_ref" / "ref_dg_driver"
+
+SCENARIOS = {
+    # name: (level, steps, initial dt)
+    "dg_advection_l2": (2, 3, 0.01),
+    "dg_advection_l3": (3, 4, 0.01),
+    "dg_advection_l3_small_dt": (3, 3, 0.001),
+}
+
+
+def read_dumps(path: Path):
+    b = path.read_bytes()
+    assert b[:4] == b"DGS1"
+    o = 4
+    ids = None
+    states, dts = [], []
+    while o < len(b):
+        step, = struct.unpack_from("<I", b, o)
+        o += 4
+        dt, = struct.unpack_from("<d", b, o)
+        o += 8
+        P, = struct.unpack_from("<Q", b, o)
+        o += 8
+        ids = np.frombuffer(b, np.uint64, P, o).copy()
+        o += 8 * P
+        st = np.frombuffer(b, np.float64, P * 16 * 4 * 4, o).reshape(P, 16, 4, 4).copy()
+        o += 8 * P * 256
+        assert step == len(states)
+        states.append(st)
+        dts.append(dt)
+    return ids, np.stack(states), np.array(dts)
+
+
+def main():
+    subprocess.run(["make", "-C", str(REPO / "oracle"), "ref"], check=True)
+    for name, (level, steps, dt0) in SCENARIOS.items():
+        out = Path("/tmp") / f"{name}.bin"
+        subprocess.run([str(DRIVER), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"out={out}"], check=True)
+        ids, state, dts = read_dumps(out)
+        np.savez_compressed(HERE / f"{name}.npz", ids=ids, state=state, dt=dts, level=level)
+        print(name, state.shape, dts)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,63 @@
+"""The CUDA DG path (amr_tree_dg_advance) against the reference's DG patch
+solver (golden fixtures, bit for bit) and against the numpy restatement on
+larger uniform trees; argument checks."""
+import numpy as np
+import pytest
+
+from oracle import dg_oracle as G
+from dg_cases import CASES, fields_to_leaves, leaves_to_fields, load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def amr():
+    import amr_gb300 as A
+
+    A.lib()
+    return A
+
+
+def _dg_tree(amr, level):
+    t = amr.Tree(2, 4, 1, 6, capacity=(1 << (2 * level)) + 64, dtype=amr.F64, fields=16)
+    t.refine_uniform(level)
+    return t
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_dg_matches_reference(amr, name):
+    z = load(name)
+    L = int(z["level"])
+    st, dts = z["state"], z["dt"]
+    t = _dg_tree(amr, L)
+    np.testing.assert_array_equal(t.ids(), z["ids"])
+    t.upload_state(leaves_to_fields(st[0]))
+    dt, time = float(dts[1]), 0.0
+    for k in range(1, len(st)):
+        assert dt == dts[k]
+        dt, time = t.dg_advance(1, dt, time)
+        np.testing.assert_array_equal(fields_to_leaves(t.download_state()), st[k])
+    assert time == pytest.approx(float(np.sum(dts)), rel=1e-15)
+
+
+@pytest.mark.parametrize("level,steps", [(4, 12), (5, 6)])
+def test_gpu_dg_matches_oracle(amr, level, steps):
+    U0 = G.initial_state(level)
+    t = _dg_tree(amr, level)
+    t.upload_state(leaves_to_fields(G.to_leaves(U0, level)))
+    dt, time = t.dg_advance(steps, 0.01)
+    outs, dts = G.run(level, steps, dt0=0.01, U=U0)
+    np.testing.assert_array_equal(fields_to_leaves(t.download_state()), G.to_leaves(outs[-1], level))
+    assert dt == min(dts[-1], (1.0 / (2 ** 2 + 1.0)) * 0.5 * ((1.0 / (1 << level)) / 4) / 1.0)
+
+
+def test_gpu_dg_rejects_other_trees(amr):
+    t = amr.Tree(2, 8, 1, 5, capacity=64, dtype=amr.F64, fields=16)
+    with pytest.raises(amr.AmrError):
+        t.dg_advance(1, 0.01)
+    t = amr.Tree(2, 4, 1, 6, capacity=64, dtype=amr.F64, fields=4)
+    with pytest.raises(amr.AmrError):
+        t.dg_advance(1, 0.01)
+    t = _dg_tree(amr, 1)
+    with pytest.raises(amr.AmrError):
+        t.dg_advance(1, 0.0)
