@@ -122,6 +122,7 @@ def lib():
         L.amr_tree_euler_advance.argtypes = [vp, sz, dbl, dbl, dbl]
         L.amr_tree_advance_ssprk.argtypes = [vp, sz, i32, C.POINTER(dbl), dbl, dbl]
         L.amr_tree_dg_advance.argtypes = [vp, sz, C.POINTER(dbl), C.POINTER(dbl)]
+        L.amr_tree_dg_remesh.argtypes = [vp, dbl, dbl, C.POINTER(i32)]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -366,6 +367,13 @@ class Tree:
         d, t = C.c_double(dt), C.c_double(time)
         check(lib().amr_tree_dg_advance(self._h, steps, C.byref(d), C.byref(t)))
         return d.value, t.value
+
+    def dg_remesh(self, refine_threshold=0.05, coarsen_threshold=0.01):
+        """The DG solver's re-mesh (gradient indicator, polynomial
+        prolongation / restriction): returns whether the tree changed."""
+        ch = C.c_int32(0)
+        check(lib().amr_tree_dg_remesh(self._h, refine_threshold, coarsen_threshold, C.byref(ch)))
+        return bool(ch.value)
 
     # -------------------------------------------------------------- Euler
     def euler_advance(self, steps, gamma, cfl, remaining=1.7976931348623157e308):

@@ -184,7 +184,250 @@ k_dg_stage(const double* __restrict__ in, const double* un, double* out, const u
     }
 }
 
+// ------------------------------------------------ DG prolongation / restriction
+// The tree's DefaultAMRPolicy (include/dg_helpers/tree_builder.hpp:59-289)
+// for the DG tensor: a fine cell's nodal values are the coarse cell's
+// polynomial at the fine nodes (interpolation), a coarse cell's nodal values
+// the polynomial of the fine cell holding each node (restriction).  Child
+// offsets number the fine cells of a coarse cell with bit 0 = x half, bit 1 =
+// y half.  Lagrange values and the basis sum follow Lagrange::evaluate
+// (lagrange.hpp:37-50) and Basis::evaluate_basis (polynomial.hpp:36-57).
+__device__ __forceinline__ double dg_lag(const double (&p)[2], int i, double x)
+{
+    double num = 1.0, den = 1.0;
+    num *= (x - p[1 - i]);
+    den *= (p[i] - p[1 - i]);
+    return num / den;
+}
+
+// polynomial with nodal values C[ix][iy] at reference point (x0, x1)
+__device__ __forceinline__ double dg_eval(const double (&C)[2][2], const double (&p)[2], double x0, double x1)
+{
+    const double lx[2] = { dg_lag(p, 0, x0), dg_lag(p, 1, x0) };
+    const double ly[2] = { dg_lag(p, 0, x1), dg_lag(p, 1, x1) };
+    double       sum   = 0.0;
+#pragma unroll
+    for (int i0 = 0; i0 < 2; ++i0)
+#pragma unroll
+        for (int i1 = 0; i1 < 2; ++i1) {
+            double prod = 1.0;
+            prod *= lx[i0];
+            prod *= ly[i1];
+            sum = sum + C[i0][i1] * prod;
+        }
+    return sum;
+}
+
+// fine cell `co` of coarse cell (field base pointers fields apart): all 16
+// nodal values into dst (fields apart)
+__device__ __forceinline__ void dg_interp(const double* src, double* dst, size_t fstride, int co,
+                                          const double (&p)[2])
+{
+    const double o0 = (co & 1) ? 0.5 : 0.0, o1 = (co & 2) ? 0.5 : 0.0;
+#pragma unroll 1
+    for (int v = 0; v < kDgVars; ++v) {
+        double C[2][2];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) C[a][b] = src[((a * 2 + b) * kDgVars + v) * fstride];
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+            for (int iy = 0; iy < 2; ++iy)
+                dst[((ix * 2 + iy) * kDgVars + v) * fstride] = dg_eval(C, p, 0.5 * p[ix] + o0, 0.5 * p[iy] + o1);
+    }
+}
+
+// coarse cell from its four fine cells (child offset order), all 16 values
+__device__ __forceinline__ void dg_restrict(const double* const (&child)[4], double* dst, size_t fstride,
+                                            const double (&p)[2])
+{
+#pragma unroll 1
+    for (int v = 0; v < kDgVars; ++v)
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+            for (int iy = 0; iy < 2; ++iy) {
+                const double pp0 = p[ix], pp1 = p[iy];
+                const int    co  = (pp0 >= 0.5 ? 1 : 0) | (pp1 >= 0.5 ? 2 : 0);
+                const double o0 = (co & 1) ? 0.5 : 0.0, o1 = (co & 2) ? 0.5 : 0.0;
+                const double c0 = 2.0 * pp0 - (o0 > 0.0 ? 1.0 : 0.0);
+                const double c1 = 2.0 * pp1 - (o1 > 0.0 ? 1.0 : 0.0);
+                double       C[2][2];
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) C[a][b] = child[co][((a * 2 + b) * kDgVars + v) * fstride];
+                dst[((ix * 2 + iy) * kDgVars + v) * fstride] = dg_eval(C, p, c0, c1);
+            }
+}
+
+// Halo of a DG tree: same-level faces copy, a ghost facing finer leaves is
+// the restriction of the 2 x 2 fine cells behind the face (patch_utils.hpp:
+// 334-386), a ghost facing a coarser leaf the interpolation of the coarse
+// cell at the ghost's position (patch_utils.hpp:388-441).  One thread per
+// ghost cell of a face, all 16 fields.
+__global__ void __launch_bounds__(256)
+k_dg_halo(double* buf, const amr_halo_meta* __restrict__ meta, long long total, Geo g, size_t fstride, double p0,
+          double p1)
+{
+    const double p[2] = { p0, p1 };
+    const int    n = g.n, h = g.h, half = n / 2;
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int  pidx = static_cast<int>(t / (4 * n));
+        const int  r    = static_cast<int>(t % (4 * n));
+        const int  d = r / n, f = r % n;
+        const int  L = d / 2, pos = d % 2;
+        int        G0 = L == 0 ? (pos ? n + h : h - 1) : f + h;
+        int        G1 = L == 1 ? (pos ? n + h : h - 1) : f + h;
+        const amr_halo_meta m = meta[static_cast<size_t>(pidx) * 4 + d];
+        if (m.relation == REL_NONE) continue;
+        double*    dst = buf + static_cast<size_t>(pidx) * g.flat + G0 * g.s[0] + G1;
+        const int  sh  = pos ? -n : n;
+        int        f0 = G0 + (L == 0 ? sh : 0), f1 = G1 + (L == 1 ? sh : 0);
+        if (m.relation == REL_SAME) {
+            const double* src = buf + static_cast<size_t>(m.neighbor) * g.flat + f0 * g.s[0] + f1;
+#pragma unroll 4
+            for (int k = 0; k < kDgFields; ++k) dst[k * fstride] = src[k * fstride];
+        } else if (m.relation == REL_COARSER) {
+            const int cy = L == 0 ? (pos ? 0 : 1) : (G0 - h) % 2;
+            const int cx = L == 1 ? (pos ? 0 : 1) : (G1 - h) % 2;
+            f0           = h + m.quadrant[0] * half + (f0 - h) / 2;
+            f1           = h + m.quadrant[1] * half + (f1 - h) / 2;
+            dg_interp(buf + static_cast<size_t>(m.neighbor) * g.flat + f0 * g.s[0] + f1, dst, fstride, cy * 2 + cx,
+                      p);
+        } else if (m.relation == REL_FINER) {
+            f0            = ((f0 - h) * 2) % n + h;
+            f1            = ((f1 - h) * 2) % n + h;
+            const int fpi = L == 0 ? (G1 - h) / half : (G0 - h) / half;
+            const int id  = fpi == 0 ? m.finer_ids[0] : m.finer_ids[1];
+            const double* fp = buf + static_cast<size_t>(id) * g.flat + f0 * g.s[0] + f1;
+            const double* const ch[4] = { fp, fp + 1, fp + g.s[0], fp + g.s[0] + 1 };
+            dg_restrict(ch, dst, fstride, p);
+        }
+    }
+}
+
+// Re-mesh of a DG state: one block per new leaf; kept leaves move whole,
+// refined children interpolate their parent's cells, coarsened parents
+// restrict their children's cells (ndtree.hpp:1499-1555 with the policy).
+__global__ void __launch_bounds__(64)
+k_dg_remap(const double* __restrict__ old_state, double* __restrict__ new_state, const int32_t* __restrict__ src,
+           const int8_t* __restrict__ skind, int P, Geo g, size_t fstride, double p0, double p1)
+{
+    const double p[2] = { p0, p1 };
+    const int    j    = blockIdx.x;
+    if (j >= P) return;
+    const int kind = skind[j];
+    const int n = g.n, h = g.h, half = n / 2;
+    if (kind == 0) {
+        for (int e = threadIdx.x; e < kDgFields * g.flat; e += blockDim.x) {
+            const int k = e / g.flat, li = e % g.flat;
+            new_state[k * fstride + static_cast<size_t>(j) * g.flat + li] =
+                old_state[k * fstride + static_cast<size_t>(src[j]) * g.flat + li];
+        }
+        return;
+    }
+    for (int c = threadIdx.x; c < n * n; c += blockDim.x) {
+        const int y = c / n + h, x = c % n + h; // padded coordinates
+        double*   dst = new_state + static_cast<size_t>(j) * g.flat + y * g.s[0] + x;
+        if (kind > 0) {
+            const int off = kind - 1;
+            const int py  = h + child_coord(g, off, 0) * half + (y - h) / 2;
+            const int px  = h + child_coord(g, off, 1) * half + (x - h) / 2;
+            const int co  = ((y - h) % 2) * 2 + (x - h) % 2;
+            dg_interp(old_state + static_cast<size_t>(src[j]) * g.flat + py * g.s[0] + px, dst, fstride, co, p);
+        } else {
+            const int child = ((y - h) / half) * 2 + (x - h) / half;
+            const int by = ((y - h) % half) * 2 + h, bx = ((x - h) % half) * 2 + h;
+            const double* fp = old_state + static_cast<size_t>(src[j] + child) * g.flat + by * g.s[0] + bx;
+            const double* const ch[4] = { fp, fp + 1, fp + g.s[0], fp + g.s[0] + 1 };
+            dg_restrict(ch, dst, fstride, p);
+        }
+    }
+}
+
+// Re-mesh decisions of GradientAMRIndicator::compute_patch_decisions
+// (include/dg_helpers/globals/amr_indicators.hpp:86-225): per interior cell
+// the largest nodal range of the variables 0..dim-1 over |mean of variable
+// dim| + 1e-10; refine if some cell exceeds rthr, coarsen if every cell is
+// below cthr.  Sixteen threads per patch.
+__global__ void __launch_bounds__(256)
+k_dg_flags(const double* __restrict__ in, int P, Geo g, size_t fstride, double rthr, double cthr,
+           int8_t* __restrict__ flags)
+{
+    const int       n = g.n, h = g.h;
+    const long long total = static_cast<long long>(P) * 16;
+    const int       lane  = threadIdx.x & 31;
+    // whole warps iterate together (two patches per warp); lanes past the
+    // last patch take part in the votes without a cell
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c - lane < total;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const bool valid = c < total;
+        const int  p = static_cast<int>(c >> 4), k = static_cast<int>(c & 15);
+        double     ind = 0.0;
+        if (valid) {
+            const size_t base    = static_cast<size_t>(p) * g.flat + (k / n + h) * g.s[0] + (k % n + h);
+            double       vmin[2] = { 1.7976931348623157e308, 1.7976931348623157e308 };
+            double       vmax[2] = { -1.7976931348623157e308, -1.7976931348623157e308 };
+            double       rho_sum = 0.0;
+#pragma unroll
+            for (int node = 0; node < 4; ++node) {
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    const double val = in[(node * kDgVars + d) * fstride + base];
+                    vmin[d]          = val < vmin[d] ? val : vmin[d]; // std::min(vmin, val)
+                    vmax[d]          = vmax[d] < val ? val : vmax[d]; // std::max(vmax, val)
+                }
+                rho_sum += in[(node * kDgVars + 2) * fstride + base];
+            }
+            const double mean_rho = rho_sum / 4.0;
+            const double inv_rho  = 1.0 / (fabs(mean_rho) + 1.0e-10);
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const double r = (vmax[d] - vmin[d]) * inv_rho;
+                ind            = ind < r ? r : ind; // std::max(indicator, r)
+            }
+        }
+        const unsigned grp = 0xffffu << (lane & 16);
+        const unsigned up  = __ballot_sync(0xffffffffu, valid && ind > rthr);
+        const unsigned lo  = __ballot_sync(0xffffffffu, !valid || !(ind >= cthr));
+        if (valid && k == 0) flags[p] = (up & grp) ? FLAG_REFINE : ((lo & grp) == grp ? FLAG_COARSEN : FLAG_STABLE);
+    }
+}
+
 } // namespace
+
+cudaError_t dg_halo(double* buf, const amr_halo_meta* meta, int P, const Geo& g, size_t fstride, cudaStream_t s)
+{
+    if (P <= 0) return cudaSuccess;
+    const double    p0 = 0.5 + 0.5 * -0.5773502691896257, p1 = 0.5 + 0.5 * 0.5773502691896257;
+    const long long total = static_cast<long long>(P) * 4 * g.n;
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 16));
+    k_dg_halo<<<grid, 256, 0, s>>>(buf, meta, total, g, fstride, p0, p1);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_remap(const double* old_state, double* new_state, const int32_t* src, const int8_t* skind, int P,
+                     const Geo& g, size_t fstride, cudaStream_t s)
+{
+    if (P <= 0) return cudaSuccess;
+    const double p0 = 0.5 + 0.5 * -0.5773502691896257, p1 = 0.5 + 0.5 * 0.5773502691896257;
+    k_dg_remap<<<P, 64, 0, s>>>(old_state, new_state, src, skind, P, g, fstride, p0, p1);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_flags(const double* in, int P, const Geo& g, size_t fstride, double rthr, double cthr, int8_t* flags,
+                     cudaStream_t s)
+{
+    if (P <= 0) return cudaSuccess;
+    const long long total = static_cast<long long>(P) * 16;
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 16));
+    k_dg_flags<<<grid, 256, 0, s>>>(in, P, g, fstride, rthr, cthr, flags);
+    return cudaGetLastError();
+}
 
 cudaError_t dg_stage(const DgStage& s)
 {

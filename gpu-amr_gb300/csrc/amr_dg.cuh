@@ -40,4 +40,18 @@ struct DgStage {
 };
 cudaError_t dg_stage(const DgStage& s);
 
+// Halo exchange of a DG state (16 fields fstride apart): same-level faces
+// copy, coarse-fine faces restrict or interpolate the DG polynomials.
+cudaError_t dg_halo(double* buf, const amr_halo_meta* meta, int P, const Geo& g, size_t fstride, cudaStream_t s);
+
+// Re-mesh of a DG state from the re-mesh source table (src, skind as for
+// the FV remap): copies, polynomial interpolation, polynomial restriction.
+cudaError_t dg_remap(const double* old_state, double* new_state, const int32_t* src, const int8_t* skind, int P,
+                     const Geo& g, size_t fstride, cudaStream_t s);
+
+// Refine / coarsen / stable per leaf by the reference's DG gradient
+// indicator with thresholds rthr / cthr.
+cudaError_t dg_flags(const double* in, int P, const Geo& g, size_t fstride, double rthr, double cthr, int8_t* flags,
+                     cudaStream_t s);
+
 } // namespace amr_gb300

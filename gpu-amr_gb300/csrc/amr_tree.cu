@@ -153,6 +153,7 @@ struct amr_tree {
     amr_halo_meta* meta[2]{};
     int4*          prec = nullptr; // pass records, one per leaf (multi-step passes)
     int4*          frec = nullptr; // face records, one per leaf (flags of same-level graph intervals)
+    bool           dg_state = false; // the re-mesh in progress carries a DG state (polynomial remap)
     int            tb = 0;
 
     int8_t*   flags  = nullptr;
@@ -1718,6 +1719,14 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
     AMR_LAUNCHED("k_emit");
     amr_status st = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
         using T = decltype(z);
+        if constexpr (sizeof(T) == 8) {
+            if (t->dg_state) {
+                AMR_CUDA(dg_remap(static_cast<const double*>(t->cur), static_cast<double*>(t->nxt), t->src, t->skind,
+                                  NP, g, t->fstride(), s));
+                AMR_LAUNCHED("k_dg_remap");
+                return AMR_OK;
+            }
+        }
         k_remap<T><<<dim3(NP, t->nvar), 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->src,
                                                      t->skind, NP, g, t->fstride());
         AMR_LAUNCHED("k_remap");
@@ -1966,7 +1975,6 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
     const Geo& g = t->g;
     if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
         return fail(AMR_ERR_INVALID, "the DG advance needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
-    if (!t->uniform) return fail(AMR_ERR_INVALID, "the DG advance needs a tree whose every relation is same-level");
     if (!(*dt > 0.0)) return fail(AMR_ERR_INVALID, "the DG step size must be positive");
     cudaStream_t s = t->stream;
     DgStage      st{};
@@ -1981,20 +1989,21 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
     const double dt_cfl = scale * 0.5 * edge / 1.0;
     double       h      = *dt, acc = time ? *time : 0.0;
     uint64_t     launches = 0;
+    const amr_halo_meta* meta = t->meta[t->tb];
     for (size_t k = 0; k < steps; ++k) {
-        if (amr_status hs = halo_buffer(t, t->cur); hs != AMR_OK) return hs;
+        AMR_CUDA(dg_halo(static_cast<double*>(t->cur), meta, st.P, g, st.fstride, s));
         st.in   = static_cast<const double*>(t->cur);
         st.un   = static_cast<const double*>(t->cur);
         st.out  = static_cast<double*>(t->nxt);
         st.dt   = h;
         st.mode = 0;
         AMR_CUDA(dg_stage(st));
-        if (amr_status hs = halo_buffer(t, t->nxt); hs != AMR_OK) return hs;
+        AMR_CUDA(dg_halo(static_cast<double*>(t->nxt), meta, st.P, g, st.fstride, s));
         st.in   = static_cast<const double*>(t->nxt);
         st.out  = static_cast<double*>(t->cur); // u^n is read and replaced cell by cell
         st.mode = 1;
         AMR_CUDA(dg_stage(st));
-        launches += 2;
+        launches += 4;
         acc += h;
         h = std::min(h, std::min(h, dt_cfl));
     }
@@ -2003,6 +2012,21 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
     *dt             = h;
     if (time) *time = acc;
     return AMR_OK;
+}
+
+amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coarsen_threshold, int* changed)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    const Geo& g = t->g;
+    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
+        return fail(AMR_ERR_INVALID, "the DG re-mesh needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
+    AMR_CUDA(dg_flags(static_cast<const double*>(t->cur), static_cast<int>(t->size), g, t->fstride(),
+                      refine_threshold, coarsen_threshold, t->flags, t->stream));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    t->dg_state         = true;
+    const amr_status st = amr_tree_remesh(t, changed);
+    t->dg_state         = false;
+    return st;
 }
 
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed)

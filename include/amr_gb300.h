@@ -294,9 +294,10 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
  * 2, 2D, 4 x 4 cells per patch with one ghost cell, four advected variables
  * per node, velocity 1, Courant number 0.5.  The tree holds the 16 nodal
  * values of a cell as 16 FP64 fields (field = node * 4 + variable, node =
- * x-node * 2 + y-node); create it with rank 2, n 4, halo 1, 16 fields.
- * Every relation must be same-level (the DG re-mesh is not provided):
- * AMR_ERR_INVALID otherwise.  Each step: halo exchange, the first stage,
+ * x-node * 2 + y-node); create it with rank 2, n 4, halo 1, 16 fields
+ * (depth 6 is the reference's MaxDepth).  Each step: halo exchange (same-
+ * level copies; across coarse-fine faces the DG restriction or
+ * interpolation of amr_tree_dg_remesh's policy), the first stage,
  * halo exchange, the second stage; no halo exchange follows the last stage
  * (the ghost cells hold the stage combination, as the reference's tree
  * does).  *dt: on entry the step size of the first step (the reference's
@@ -306,6 +307,19 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
  * accumulates the step sizes taken.  Interior states are bit-identical to
  * the reference's CPU path. */
 amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time);
+
+/* DGSolver::apply_amr (solver.hpp:237-299) on such a tree:
+ * GradientAMRIndicator::compute_patch_decisions (include/dg_helpers/
+ * globals/amr_indicators.hpp:86-225: per cell the largest nodal range of
+ * variables 0..1 over |mean of variable 2| + 1e-10; refine if a cell exceeds
+ * refine_threshold, coarsen if every cell is below coarsen_threshold), then
+ * the re-mesh of amr_tree_remesh with the tree's DG policy
+ * (tree_builder.hpp:59-289): refined cells interpolate the parent cell's
+ * polynomial at their nodes, coarsened cells take the polynomial of the
+ * child holding each node.  The halo of amr_tree_dg_advance applies the same
+ * operators across coarse-fine faces.  *changed (optional) = 1 if the tree
+ * changed. */
+amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coarsen_threshold, int* changed);
 
 /* ------------------------------------------------------------- Euler
  * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through

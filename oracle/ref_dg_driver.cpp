@@ -22,13 +22,22 @@
 //                  patch, the CFL step from the last stage's largest
 //                  eigenvalue, finish_step; the loop's step size rule
 //                  dt = min(dt, dt_min) with dt = initial_dt at the start
-//                  (solver.hpp:117-128).  No re-mesh.
-// Usage: ref_dg_driver level=<L> steps=<K> dt0=<initial dt> out=<file>
+//                  (solver.hpp:117-128);
+//   re-mesh        with amr=<interval> > 0, DGSolver::apply_amr (solver.hpp:
+//                  237-299) after each step from step 1 on, every interval
+//                  steps: GradientAMRIndicator::compute_patch_decisions
+//                  (include/dg_helpers/globals/amr_indicators.hpp:158-225) with
+//                  thresholds rthr / cthr, reconstruct_tree with those
+//                  decisions (the tree's DefaultAMRPolicy prolongation and
+//                  restriction), halo exchange.
+// Usage: ref_dg_driver level=<L> steps=<K> dt0=<initial dt> [amr=<interval>
+//        rthr=<refine> cthr=<coarsen>] out=<file>
 // Records: "DGS1" header, then per dump: step (u32), dt (f64), leaves
 // (u64), ids (u64 x leaves), interior nodal values (f64 x leaves x 16 cells
 // x 4 nodes x 4 variables, cells row-major with x fastest, nodes with the
 // x-node index slowest as in the reference's tensor).
 #include "config/generated_config.hpp"
+#include "dg_helpers/globals/amr_indicators.hpp"
 #include "dg_helpers/globals/global_config.hpp"
 #include "dg_helpers/rhs.hpp"
 #include "dg_helpers/time_integration/time_integration.hpp"
@@ -41,6 +50,7 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 namespace
@@ -158,7 +168,7 @@ int main(int argc, char** argv)
         std::perror(out.c_str());
         return 2;
     }
-    tree_t tree{ (std::size_t{ 1 } << (2 * level)) + 64 };
+    tree_t tree{ static_cast<std::size_t>(arg(argc, argv, "capacity", (1L << (2 * level)) + 64)) };
     auto   refine_all = [](const patch_index_t&) { return tree_t::refine_status_t::Refine; };
     for (int l = 0; l < level; ++l) tree.reconstruct_tree(refine_all);
     for (std::size_t i = 0; i < tree.size(); ++i)
@@ -183,12 +193,29 @@ int main(int argc, char** argv)
     tree.halo_exchange_update();
     std::fwrite("DGS1", 1, 4, f);
     dump(f, tree, 0, 0.0);
+    const int                   amr_every = static_cast<int>(arg(argc, argv, "amr", 0));
+    amr::global::AMRThresholds  thr{ argf(argc, argv, "rthr", 0.05), argf(argc, argv, "cthr", 0.01) };
+    int                         next_amr = 0;
+    using indicator_t = amr::global::GradientAMRIndicator<global_t, policy_t>;
+    using status_t    = tree_t::refine_status_t;
     for (int k = 1; k <= steps; ++k)
     {
         double dt_min = dt;
         step(tree, dt, dt_min);
         const double used = dt;
         dt                = std::min(dt, dt_min);
+        if (amr_every > 0 && k >= next_amr)
+        {
+            const auto decisions = indicator_t::template compute_patch_decisions<tree_t, S1>(tree, thr);
+            std::unordered_map<patch_index_t, status_t> by_id;
+            for (std::size_t i = 0; i < decisions.size(); ++i) by_id[tree.get_node_index_at(i)] = decisions[i];
+            tree.reconstruct_tree([&by_id](const patch_index_t& pid) -> status_t {
+                auto it = by_id.find(pid);
+                return it != by_id.end() ? it->second : status_t::Stable;
+            });
+            tree.halo_exchange_update();
+            next_amr = k + amr_every;
+        }
         dump(f, tree, static_cast<std::uint32_t>(k), used);
     }
     std::fclose(f);

@@ -9,6 +9,8 @@ as a compressed .npz:
   state          [dump, leaf, cell, node, variable] interior nodal values;
                  dump 0 is the initial state, dump k the state after step k
   dt             [dump] step size used to reach each dump (0 for dump 0)
+  with re-mesh:  ids_k / state_k per dump k (the leaf count changes), and
+                 amr (interval), rthr, cthr
 
 Usage:  python tests/golden/make_dg_golden.py
 """
@@ -25,10 +27,15 @@ REPO = HERE.parents[1]
 DRIVER = REPO / "oracle" / "_ref" / "ref_dg_driver"
 
 SCENARIOS = {
-    # name: (level, steps, initial dt)
-    "dg_advection_l2": (2, 3, 0.01),
-    "dg_advection_l3": (3, 4, 0.01),
-    "dg_advection_l3_small_dt": (3, 3, 0.001),
+    # name: (level, steps, initial dt, re-mesh interval (0: none), refine / coarsen thresholds)
+    "dg_advection_l2": (2, 3, 0.01, 0, 0.05, 0.01),
+    "dg_advection_l3": (3, 4, 0.01, 0, 0.05, 0.01),
+    "dg_advection_l3_small_dt": (3, 3, 0.001, 0, 0.05, 0.01),
+    # with the DG solver's re-mesh after steps 1, 3 (and 5): refinement to levels
+    # 4-5 (the reference's thresholds) ...
+    "dg_amr_l3": (3, 4, 0.01, 2, 0.05, 0.01),
+    # ... and refinement to level 6 followed by coarsening back to level 5
+    "dg_amr_l4": (4, 6, 0.001, 2, 0.05, 0.03),
 }
 
 
@@ -36,8 +43,7 @@ def read_dumps(path: Path):
     b = path.read_bytes()
     assert b[:4] == b"DGS1"
     o = 4
-    ids = None
-    states, dts = [], []
+    idss, states, dts = [], [], []
     while o < len(b):
         step, = struct.unpack_from("<I", b, o)
         o += 4
@@ -50,19 +56,27 @@ def read_dumps(path: Path):
         st = np.frombuffer(b, np.float64, P * 16 * 4 * 4, o).reshape(P, 16, 4, 4).copy()
         o += 8 * P * 256
         assert step == len(states)
+        idss.append(ids)
         states.append(st)
         dts.append(dt)
-    return ids, np.stack(states), np.array(dts)
+    return idss, states, np.array(dts)
 
 
 def main():
     subprocess.run(["make", "-C", str(REPO / "oracle"), "ref"], check=True)
-    for name, (level, steps, dt0) in SCENARIOS.items():
+    for name, (level, steps, dt0, amr, rthr, cthr) in SCENARIOS.items():
         out = Path("/tmp") / f"{name}.bin"
-        subprocess.run([str(DRIVER), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"out={out}"], check=True)
-        ids, state, dts = read_dumps(out)
-        np.savez_compressed(HERE / f"{name}.npz", ids=ids, state=state, dt=dts, level=level)
-        print(name, state.shape, dts)
+        subprocess.run([str(DRIVER), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"amr={amr}",
+                        f"rthr={rthr}", f"cthr={cthr}", "capacity=8000", f"out={out}"], check=True)
+        idss, states, dts = read_dumps(out)
+        if amr == 0:
+            np.savez_compressed(HERE / f"{name}.npz", ids=idss[0], state=np.stack(states), dt=dts, level=level)
+        else:
+            extra = {f"ids_{k}": v for k, v in enumerate(idss)}
+            extra.update({f"state_{k}": v for k, v in enumerate(states)})
+            np.savez_compressed(HERE / f"{name}.npz", dt=dts, level=level, amr=amr, rthr=rthr, cthr=cthr,
+                                steps=steps, **extra)
+        print(name, [len(i) for i in idss], dts)
 
 
 if __name__ == "__main__":

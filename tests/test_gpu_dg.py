@@ -61,3 +61,27 @@ def test_gpu_dg_rejects_other_trees(amr):
     t = _dg_tree(amr, 1)
     with pytest.raises(amr.AmrError):
         t.dg_advance(1, 0.0)
+
+
+@pytest.mark.parametrize("name", ["dg_amr_l3", "dg_amr_l4"])
+def test_gpu_dg_remesh_matches_reference(amr, name):
+    """The DG solver loop with its re-mesh (gradient indicator, polynomial
+    prolongation and restriction, DG halo across coarse-fine faces) against
+    the reference run: leaves and interior states after every step, bit for
+    bit."""
+    z = load(name)
+    L, every, steps = int(z["level"]), int(z["amr"]), int(z["steps"])
+    dts = z["dt"]
+    t = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
+    t.refine_uniform(L)
+    np.testing.assert_array_equal(t.ids(), z["ids_0"])
+    t.upload_state(leaves_to_fields(z["state_0"]))
+    dt, time, next_amr = float(dts[1]), 0.0, 0
+    for k in range(1, steps + 1):
+        assert dt == dts[k]
+        dt, time = t.dg_advance(1, dt, time)
+        if k >= next_amr:
+            t.dg_remesh(float(z["rthr"]), float(z["cthr"]))
+            next_amr = k + every
+        np.testing.assert_array_equal(t.ids(), z[f"ids_{k}"])
+        np.testing.assert_array_equal(fields_to_leaves(t.download_state()), z[f"state_{k}"])
