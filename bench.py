@@ -858,7 +858,40 @@ def dg_extra(torch, A, stream, with_cpu=True):
             g.close()
         t.close()
         out[f"level{lv}"] = rec
+    out["solver_loop"] = dg_loop(torch, A, stream)
     return out
+
+
+def dg_loop(torch, A, stream):
+    """The reference's DG main loop (examples/dg_main_loop.e.cpp with
+    DGSolver::run, solver.hpp:117-147): uniform level 5, initial dt 0.01,
+    re-mesh every 20 steps with thresholds 0.05 / 0.01, until t = 1; the
+    reference's count of processed cells (leaves x 16 per step) over the wall
+    time of the loop (host-driven: one call per step and per re-mesh)."""
+    from oracle import dg_oracle as G
+
+    L0 = 5
+    t = A.Tree(2, 4, 1, 6, capacity=8192, dtype=A.F64, fields=16, stream=stream.cuda_stream)
+    t.refine_uniform(L0)
+    t.upload_state(_dg_fields(G.to_leaves(G.initial_state(L0), L0)))
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    dt, tm, step, next_amr, cells, remeshes, lmax = 0.01, 0.0, 0, 0, 0, 0, 0
+    while tm < 1.0:
+        cells += t.size * 16
+        dt, tm = t.dg_advance(1, dt, tm)
+        step += 1
+        if step >= next_amr:
+            t.dg_remesh(0.05, 0.01)
+            remeshes += 1
+            next_amr = step + 20
+            lmax = max(lmax, t.size)
+    t.synchronize()
+    sec = time.perf_counter() - c0
+    t.close()
+    return {"value": cells / sec, "unit": "cell-updates/s (the reference's processed cells/s)", "seconds": sec,
+            "steps": step, "remeshes": remeshes, "leaves_max": lmax, "sim_time": tm,
+            "driver": "host loop: amr_tree_dg_advance per step, amr_tree_dg_remesh every 20 steps"}
 
 
 def _dg_fields(st):
