@@ -87,7 +87,7 @@ __device__ __forceinline__ void dg_ghost(const double* __restrict__ in, const do
 // the FP64 residual runs on full warps), grid-stride over patches; the same
 // threads combine the patch's twenty ghost cells.  The four variables one
 // after another.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(64)
 k_dg_stage(const double* __restrict__ in, const double* un, double* out, const uint64_t* __restrict__ keys, int P,
            Geo g, size_t fstride, DgTables tb, double dt, int mode)
 {
@@ -434,9 +434,11 @@ cudaError_t dg_stage(const DgStage& s)
     if (s.P <= 0) return cudaSuccess;
     const DgTables  tb    = dg_tables();
     if (s.g.n != kDgPatch || s.g.h != 1) return cudaErrorInvalidValue;
+    // 64-thread blocks: a small tree (the reference's level 5 has 16384
+    // cells) still spreads over every SM
     const long long total = static_cast<long long>(s.P) * kDgPatch * kDgPatch;
-    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 16));
-    k_dg_stage<<<grid, 256, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.fstride, tb, s.dt, s.mode);
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 63) / 64, 152LL * 32));
+    k_dg_stage<<<grid, 64, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.fstride, tb, s.dt, s.mode);
     return cudaGetLastError();
 }
 
