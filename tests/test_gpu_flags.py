@@ -63,3 +63,32 @@ def test_gradient_flags_on_the_threshold(amr, oracle_mod, n, dtype, ghosts):
         t.flags_gradient(rthr, cthr, 1, 4)
         np.testing.assert_array_equal(t.get_flags(), fo)
         assert (fo == 1).any() and (fo == 0).any()
+
+
+@pytest.mark.parametrize("n", [16, 8])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_gradient_flags_with_non_finite_cells(amr, oracle_mod, n, dtype):
+    """Infinite, NaN and huge cells (FP32 squares that overflow) next to
+    ordinary ones: the lanes that hold them leave the FP32 pre-filter and
+    decide exactly; flags equal the oracle's."""
+    h, seed = 1, 29
+    o = oracle_mod.OracleTree(2, n, h, 6, 20000)
+    o.refine_all(2)
+    t = amr.Tree(2, n, h, 6, capacity=20000, dtype=amr.F64 if dtype == "f64" else amr.F32)
+    t.refine_uniform(2)
+    o.random_state(seed)
+    st = o.state()
+    rng = np.random.default_rng(seed)
+    P = st.shape[0]
+    for p in rng.choice(P, size=P // 3, replace=False):
+        y, x = rng.integers(h, n + h, size=2)
+        st[p, y, x] = rng.choice([np.inf, -np.inf, np.nan, 1e30, -3e25])
+    if dtype == "f32":
+        st = st.astype(np.float32).astype(np.float64)
+    o.set_state(st)
+    o.halo_exchange()
+    st = o.state()
+    fo = o.flags_gradient(0.05, 0.01, 1, 4)
+    t.upload_state(st)
+    t.flags_gradient(0.05, 0.01, 1, 4)
+    np.testing.assert_array_equal(t.get_flags(), fo)
