@@ -871,27 +871,24 @@ def dg_loop(torch, A, stream):
     from oracle import dg_oracle as G
 
     L0 = 5
-    t = A.Tree(2, 4, 1, 6, capacity=8192, dtype=A.F64, fields=16, stream=stream.cuda_stream)
-    t.refine_uniform(L0)
-    t.upload_state(_dg_fields(G.to_leaves(G.initial_state(L0), L0)))
-    torch.cuda.synchronize()
-    c0 = time.perf_counter()
-    dt, tm, step, next_amr, cells, remeshes, lmax = 0.01, 0.0, 0, 0, 0, 0, 0
-    while tm < 1.0:
-        cells += t.size * 16
-        dt, tm = t.dg_advance(1, dt, tm)
-        step += 1
-        if step >= next_amr:
-            t.dg_remesh(0.05, 0.01)
-            remeshes += 1
-            next_amr = step + 20
-            lmax = max(lmax, t.size)
-    t.synchronize()
-    sec = time.perf_counter() - c0
-    t.close()
-    return {"value": cells / sec, "unit": "cell-updates/s (the reference's processed cells/s)", "seconds": sec,
-            "steps": step, "remeshes": remeshes, "leaves_max": lmax, "sim_time": tm,
-            "driver": "host loop: amr_tree_dg_advance per step, amr_tree_dg_remesh every 20 steps"}
+    u0 = _dg_fields(G.to_leaves(G.initial_state(L0), L0))
+    best = None
+    for _ in range(2):  # the first run includes the first use of the kernels
+        t = A.Tree(2, 4, 1, 6, capacity=8192, dtype=A.F64, fields=16, stream=stream.cuda_stream)
+        t.refine_uniform(L0)
+        t.upload_state(u0)
+        torch.cuda.synchronize()
+        c0 = time.perf_counter()
+        st = t.dg_run(0.01, 1.0, 20, 0.05, 0.01)
+        sec = time.perf_counter() - c0
+        t.close()
+        if best is None or sec < best[0]:
+            best = (sec, st)
+    sec, st = best
+    return {"value": st["cells"] / sec, "unit": "cell-updates/s (the reference's processed cells/s)", "seconds": sec,
+            "steps": st["steps"], "remeshes": st["remeshes"], "leaves_max": st["leaves_max"], "sim_time": st["time"],
+            "driver": "amr_tree_dg_run: the loop in one call (host-driven launches, a leaf-count readback per "
+                      "re-mesh)"}
 
 
 def _dg_fields(st):

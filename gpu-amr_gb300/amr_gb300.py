@@ -65,6 +65,11 @@ class CycleStats(C.Structure):
                 ("graph_intervals", C.c_uint64)]
 
 
+class DgStats(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("remeshes", C.c_uint64), ("cells", C.c_uint64),
+                ("leaves_max", C.c_uint64), ("time", C.c_double), ("next_dt", C.c_double)]
+
+
 CRITERIA = {"none": 0, "grad": 1, "gradient": 1, "max": 2}
 RUN_PER_LAUNCH = 1
 RUN_INSTANCE_PARAMS = 2
@@ -123,6 +128,7 @@ def lib():
         L.amr_tree_advance_ssprk.argtypes = [vp, sz, i32, C.POINTER(dbl), dbl, dbl]
         L.amr_tree_dg_advance.argtypes = [vp, sz, C.POINTER(dbl), C.POINTER(dbl)]
         L.amr_tree_dg_remesh.argtypes = [vp, dbl, dbl, C.POINTER(i32)]
+        L.amr_tree_dg_run.argtypes = [vp, dbl, dbl, i32, dbl, dbl, C.POINTER(DgStats)]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -367,6 +373,16 @@ class Tree:
         d, t = C.c_double(dt), C.c_double(time)
         check(lib().amr_tree_dg_advance(self._h, steps, C.byref(d), C.byref(t)))
         return d.value, t.value
+
+    def dg_run(self, initial_dt=0.01, end_time=1.0, amr_interval=20, refine_threshold=0.05,
+               coarsen_threshold=0.01):
+        """The DG solver's loop (steps and re-meshes) to end_time: a dict of
+        steps, remeshes, cells (the reference's processed-cell count),
+        leaves_max, time, next_dt."""
+        st = DgStats()
+        check(lib().amr_tree_dg_run(self._h, initial_dt, end_time, amr_interval, refine_threshold,
+                                    coarsen_threshold, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in DgStats._fields_}
 
     def dg_remesh(self, refine_threshold=0.05, coarsen_threshold=0.01):
         """The DG solver's re-mesh (gradient indicator, polynomial

@@ -2029,6 +2029,35 @@ amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coars
     return st;
 }
 
+amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int amr_interval,
+                           double refine_threshold, double coarsen_threshold, amr_dg_stats* stats)
+{
+    if (!t || !stats || amr_interval < 0) return fail(AMR_ERR_INVALID, "bad argument");
+    *stats                = amr_dg_stats{};
+    double    dt          = initial_dt, time = 0.0;
+    long long step        = 0, next_amr = 0;
+    size_t    leaves_max  = t->size;
+    while (time < end_time) {
+        stats->cells += static_cast<uint64_t>(t->size) * kDgPatch * kDgPatch;
+        if (amr_status st = amr_tree_dg_advance(t, 1, &dt, &time); st != AMR_OK) return st;
+        ++step;
+        if (amr_interval > 0 && step >= next_amr) {
+            int changed = 0;
+            if (amr_status st = amr_tree_dg_remesh(t, refine_threshold, coarsen_threshold, &changed); st != AMR_OK)
+                return st;
+            ++stats->remeshes;
+            next_amr   = step + amr_interval;
+            leaves_max = std::max(leaves_max, t->size);
+        }
+    }
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    stats->steps      = static_cast<uint64_t>(step);
+    stats->time       = time;
+    stats->next_dt    = dt;
+    stats->leaves_max = static_cast<uint64_t>(leaves_max);
+    return AMR_OK;
+}
+
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");

@@ -321,6 +321,19 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
  * changed. */
 amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coarsen_threshold, int* changed);
 
+/* DGSolver::run (solver.hpp:117-147) without its VTK output: from time 0,
+ * step size initial_dt for the first step, steps while time < end_time,
+ * after step k >= next (next = 0 at the start) a re-mesh and next = k +
+ * amr_interval (0: no re-mesh).  stats: steps, re-meshes, the reference's
+ * processed-cell count (leaves x 16 per step), final time and next step
+ * size, largest leaf count. */
+typedef struct amr_dg_stats {
+    uint64_t steps, remeshes, cells, leaves_max;
+    double   time, next_dt;
+} amr_dg_stats;
+amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int amr_interval,
+                           double refine_threshold, double coarsen_threshold, amr_dg_stats* stats);
+
 /* ------------------------------------------------------------- Euler
  * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through
  * amr_solver (amr_solver.hpp:155-413) on a tree created with fields =

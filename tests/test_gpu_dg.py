@@ -85,3 +85,29 @@ def test_gpu_dg_remesh_matches_reference(amr, name):
             next_amr = k + every
         np.testing.assert_array_equal(t.ids(), z[f"ids_{k}"])
         np.testing.assert_array_equal(fields_to_leaves(t.download_state()), z[f"state_{k}"])
+
+
+def test_gpu_dg_run_equals_the_stepwise_loop(amr):
+    """amr_tree_dg_run (the solver loop in one call) against the same loop
+    driven step by step through amr_tree_dg_advance and amr_tree_dg_remesh:
+    same steps, re-meshes, leaves and states."""
+    U0 = G.initial_state(3)
+    a = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
+    b = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
+    for t in (a, b):
+        t.refine_uniform(3)
+        t.upload_state(leaves_to_fields(G.to_leaves(U0, 3)))
+    st = a.dg_run(0.01, 0.05, 3, 0.05, 0.01)
+    dt, time, step, next_amr, cells, remeshes = 0.01, 0.0, 0, 0, 0, 0
+    while time < 0.05:
+        cells += b.size * 16
+        dt, time = b.dg_advance(1, dt, time)
+        step += 1
+        if step >= next_amr:
+            b.dg_remesh(0.05, 0.01)
+            remeshes += 1
+            next_amr = step + 3
+    assert (st["steps"], st["remeshes"], st["cells"]) == (step, remeshes, cells)
+    assert st["time"] == time and st["next_dt"] == dt
+    np.testing.assert_array_equal(a.ids(), b.ids())
+    np.testing.assert_array_equal(a.download_state(), b.download_state())
