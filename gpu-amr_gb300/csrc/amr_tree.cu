@@ -506,7 +506,7 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
         });
     }
     // rounds over all candidates, each candidate's best round counts: a
-    // candidate is not judged on one sample taken during a transient
+    // candidate's time does not rest on one sample taken during a transient
     cudaEvent_t e0, e1;
     AMR_CUDA(cudaEventCreate(&e0));
     AMR_CUDA(cudaEventCreate(&e1));
