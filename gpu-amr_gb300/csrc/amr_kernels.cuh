@@ -1921,7 +1921,8 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
         // evaluated exactly.  Same outcome as a per-cell decision.
         int   any = 0, all = 1;
         T     colv[SEG + 2];
-        float smax = 0.0f, ssum = 0.0f;
+        float smax = 0.0f;
+        bool  bad  = false;
 #pragma unroll
         for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
 #pragma unroll
@@ -1929,12 +1930,8 @@ __device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr
             const int   idx = (r0 + k) * P1 + cl;
             const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
             smax            = fmaxf(smax, s);
-            ssum += s;
+            bad |= !(fabsf(s) < INFINITY);
         }
-        // squares are never negative: the sum is finite only if every value
-        // is (an overflowing sum sends the lane to the exact path, which
-        // decides the same)
-        const bool bad   = !(ssum < INFINITY);
         const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
                            (smax < rule.c_lo || smax >= rule.c_hi);
         if (known) {
@@ -2057,7 +2054,8 @@ __device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, c
         // unless it lies in a band or some value is not finite
         int   any = 0, all = 1;
         T     colv[SEG + 2];
-        float smax = 0.0f, ssum = 0.0f;
+        float smax = 0.0f;
+        bool  bad  = false;
 #pragma unroll
         for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
 #pragma unroll
@@ -2065,12 +2063,8 @@ __device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, c
             const int   idx = (r0 + k) * P1 + cl;
             const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
             smax            = fmaxf(smax, s);
-            ssum += s;
+            bad |= !(fabsf(s) < INFINITY);
         }
-        // squares are never negative: the sum is finite only if every value
-        // is (an overflowing sum sends the lane to the exact path, which
-        // decides the same)
-        const bool bad   = !(ssum < INFINITY);
         const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
                            (smax < rule.c_lo || smax >= rule.c_hi);
         if (known) {
