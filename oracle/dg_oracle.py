@@ -108,6 +108,69 @@ def initial_state(level, t=0.0):
     return U
 
 
+GAMMA = 1.4  # the Euler equation's default heat capacity ratio (euler.hpp:31)
+
+
+def euler_pressure(U):
+    """compute_pressure (euler.hpp:57-69) per node: variables [mx, my, rho, E]."""
+    rho, E = U[..., 2], U[..., 3]
+    kin = 0.0
+    for d in range(2):
+        kin = kin + 0.5 * U[..., d] * U[..., d] / rho
+    return (GAMMA - 1.0) * (E - kin)
+
+
+def euler_flux(U):
+    """evaluate_flux (euler.hpp:109-143): [F_x, F_y] per node."""
+    rho, E = U[..., 2], U[..., 3]
+    p = euler_pressure(U)
+    out = []
+    for dr in range(2):
+        u = U[..., dr] / rho
+        F = np.empty_like(U)
+        for i in range(2):
+            F[..., i] = U[..., i] * u
+            if i == dr:
+                F[..., i] = F[..., i] + p
+        F[..., 2] = rho * u
+        F[..., 3] = (E + p) * u
+        out.append(F)
+    return out
+
+
+def euler_eig(U, normal):
+    """max_eigenvalue (euler.hpp:149-163): from the cell's first node only,
+    |u_n| + sqrt(gamma p / rho)."""
+    U0 = U[..., 0, 0, :]
+    rho = U0[..., 2]
+    p = euler_pressure(U0)
+    c = np.sqrt(GAMMA * p / rho)
+    return np.abs(U0[..., normal] / rho) + c
+
+
+def euler_initial_state(level):
+    """EulerInitialCondition<2> (euler.hpp:210-233) at the nodes: pressure
+    pulse exp(-100 r^2) + 1, rho 1, zero momentum."""
+    C = PATCH << level
+    cell = (1.0 / float(1 << level)) / float(PATCH)
+    U = np.zeros((C, C, ORDER, ORDER, NVAR))
+    for cy in range(C):
+        for cx in range(C):
+            pcx, lcx = divmod(cx, PATCH)
+            pcy, lcy = divmod(cy, PATCH)
+            ccx = float(pcx << (6 - level)) * (1.0 / float(1 << 6)) + (float(lcx) + 0.5) * cell
+            ccy = float(pcy << (6 - level)) * (1.0 / float(1 << 6)) + (float(lcy) + 0.5) * cell
+            for ix in range(ORDER):
+                for iy in range(ORDER):
+                    x = ccx + (T["points"][ix] - 0.5) * cell
+                    y = ccy + (T["points"][iy] - 0.5) * cell
+                    r2 = (x - 0.5) * (x - 0.5) + (y - 0.5) * (y - 0.5)
+                    p = np.exp(-100.0 * r2) + 1.0
+                    U[cy, cx, ix, iy, 2] = 1.0
+                    U[cy, cx, ix, iy, 3] = p / (1.4 - 1.0)
+    return U
+
+
 def _contract(A, k, dim):
     """contract<dim>(A, k) (container_algorithms.hpp:217-298): the first term,
     then the second added (order 2)."""
@@ -116,41 +179,82 @@ def _contract(A, k, dim):
     return A[..., :, 0, :] * k[0] + A[..., :, 1, :] * k[1]
 
 
-def rhs(U, edge):
+def _patch_running_max(e):
+    """Running maximum of the local face speeds over a patch in the
+    reference's loop order (cells row-major, faces in direction order;
+    rhs.hpp:186-243): e[cy, cx, face] -> lambda[cy, cx, face]."""
+    C = e.shape[0]
+    lam = np.empty_like(e)
+    for py in range(0, C, PATCH):
+        for px in range(0, C, PATCH):
+            run = -np.inf
+            for ly in range(PATCH):
+                for lx in range(PATCH):
+                    for f in range(4):
+                        v = e[py + ly, px + lx, f]
+                        run = v if run < v else run  # std::max(run, v)
+                        lam[py + ly, px + lx, f] = run
+    return lam
+
+
+FACES = ((0, -1), (0, 1), (1, -1), (1, 1))
+
+
+def rhs(U, edge, equation="advection", lam_out=None):
     """Residual R(U) of every interior cell (rhs.hpp: volume, surface, inverse
-    mass) on the periodic grid."""
+    mass) on the periodic grid.  lam_out (list): receives each patch's final
+    running maximum of the face speeds."""
     K, D, M = T["kern"], T["D"], T["mass"]
-    vol = edge * edge  # volume(): 1.0 * edge * edge
     vol = (1.0 * edge) * edge
     area = 1.0 * edge
     inv_jac = 1.0 / edge
-    F = VELOCITY * U  # both flux components
-    G = F * M[None, None, :, :, None]  # tensor_dot(flux, volume_mass)
+    if equation == "advection":
+        F = [VELOCITY * U, VELOCITY * U]
+    else:
+        F = euler_flux(U)
     s = inv_jac * vol
     du = np.zeros_like(U)
     # derivative_contraction(D, G, 0): r[i][j] = (0 + D[i,0] G[0][j]) + D[i,1] G[1][j]
+    G = F[0] * M[None, None, :, :, None]  # tensor_dot(flux_x, volume_mass)
     c0 = np.empty_like(U)
     for i in range(ORDER):
         c0[:, :, i, :, :] = (0.0 + D[i, 0] * G[:, :, 0, :, :]) + D[i, 1] * G[:, :, 1, :, :]
     du = du + s * c0
+    G = F[1] * M[None, None, :, :, None]
     c1 = np.empty_like(U)
     for j in range(ORDER):
         c1[:, :, :, j, :] = (0.0 + D[j, 0] * G[:, :, :, 0, :]) + D[j, 1] * G[:, :, :, 1, :]
     du = du + s * c1
-    lam = 1.0  # |v|: the running maximum over the faces is 1 from the first face on
+    # face speeds: advection |v| = 1; Euler the running maximum over the patch
+    # of max(eig(cell), eig(neighbour)) in the reference's loop order
+    nbrs = []
+    for pdim, sign in FACES:
+        shift = (1, 0) if pdim == 0 else (0, 1)
+        nbrs.append(np.roll(U, shift=(-sign * shift[0], -sign * shift[1]), axis=(0, 1)))
+    if equation == "advection":
+        lam = np.ones(U.shape[:2] + (4,))
+    else:
+        e = np.empty(U.shape[:2] + (4,))
+        for f, (pdim, sign) in enumerate(FACES):
+            adim = 1 - pdim
+            a, b = euler_eig(U, adim), euler_eig(nbrs[f], adim)
+            e[:, :, f] = np.where(a < b, b, a)  # std::max(eig(cell), eig(neighbour))
+        lam = _patch_running_max(e)
+    if lam_out is not None:
+        lam_out.append(lam[PATCH - 1::PATCH, PATCH - 1::PATCH, 3])
     # faces in the reference's direction order: padded dimension 0 (y) -, +,
     # then dimension 1 (x) -, +; tensor dimension = 1 - padded dimension
-    for pdim, sign in ((0, -1), (0, 1), (1, -1), (1, 1)):
+    for f, (pdim, sign) in enumerate(FACES):
         adim = 1 - pdim
         sidx = 0 if sign < 0 else 1
-        shift = (1, 0) if pdim == 0 else (0, 1)
-        Un = np.roll(U, shift=(-sign * shift[0], -sign * shift[1]), axis=(0, 1))
-        Fn = VELOCITY * Un
+        Un = nbrs[f]
+        Fn = [VELOCITY * Un, VELOCITY * Un] if equation == "advection" else euler_flux(Un)
         uf = _contract(U, K[sidx], adim)
-        ff = _contract(F, K[sidx], adim)
+        ff = _contract(F[adim], K[sidx], adim)
         un = _contract(Un, K[1 - sidx], adim)
-        fn = _contract(Fn, K[1 - sidx], adim)
-        nf = (float(sign) * (ff + fn) * 0.5 + (uf - un) * (0.5 * lam)) * area
+        fn = _contract(Fn[adim], K[1 - sidx], adim)
+        lm = lam[:, :, f][:, :, None, None]
+        nf = (float(sign) * (ff + fn) * 0.5 + (uf - un) * (0.5 * lm)) * area
         wf = nf * T["smass"][None, None, :, None]
         kv = K[sidx]
         if adim == 1:  # tensor_product(weighted, kernel): [face node][normal node]
@@ -161,28 +265,33 @@ def rhs(U, edge):
     return du * (T["inv_mass"] / vol)[None, None, :, :, None]
 
 
-def ssprk2_step(U, edge, dt):
+def ssprk2_step(U, edge, dt, equation="advection", lam_out=None):
     """One SSPRK2 step (time.hpp:134-168): u* = u + dt R(u);
-    u' = ((u + u*) + dt R(u*)) * 0.5."""
-    us = U + rhs(U, edge) * dt
-    return (U + us + rhs(us, edge) * dt) * 0.5
+    u' = ((u + u*) + dt R(u*)) * 0.5.  lam_out receives the second stage's
+    per-patch speed maxima."""
+    us = U + rhs(U, edge, equation) * dt
+    return (U + us + rhs(us, edge, equation, lam_out) * dt) * 0.5
 
 
-def run(level, steps, dt0=0.01, U=None):
+def run(level, steps, dt0=0.01, U=None, equation="advection"):
     """The reference's step loop on a uniform level without re-mesh: returns
     the states after each step and the step sizes used."""
     edge = (1.0 / float(1 << level)) / float(PATCH)
     if U is None:
-        U = initial_state(level)
+        U = initial_state(level) if equation == "advection" else euler_initial_state(level)
     scale = 1.0 / (float(ORDER) ** DIM + 1.0)
-    dt_cfl = scale * COURANT * edge / 1.0
     dt = dt0
     out, dts = [], []
     for _ in range(steps):
-        U = ssprk2_step(U, edge, dt)
+        lams = []
+        U = ssprk2_step(U, edge, dt, equation, lams)
         out.append(U)
         dts.append(dt)
-        dt = min(dt, min(dt, dt_cfl))
+        dt_min = dt
+        for lam in lams[0].ravel():  # per patch, in the tree's order (any order gives the minimum)
+            if lam > 0.0:
+                dt_min = min(dt_min, scale * COURANT * edge / lam)
+        dt = min(dt, dt_min)
     return out, dts
 
 

@@ -55,7 +55,18 @@
 
 namespace
 {
-using policy_t          = amr::config::GlobalConfigPolicy;
+// The generated policy fixes the equation to advection; built with
+// -DDG_EULER the driver runs the same configuration with the reference's DG
+// Euler equations (include/dg_helpers/equations/euler.hpp) instead.
+#ifdef DG_EULER
+struct EulerPolicy : amr::config::GlobalConfigPolicy
+{
+    static constexpr amr::config::EquationType equation = amr::config::EquationType::Euler;
+};
+using policy_t = EulerPolicy;
+#else
+using policy_t = amr::config::GlobalConfigPolicy;
+#endif
 using global_t          = amr::global::GlobalConfig<policy_t>;
 using rhs_t             = amr::rhs::RHSEvaluator<global_t, policy_t>;
 using builder_t         = amr::dg_tree::TreeBuilder<global_t, policy_t>;

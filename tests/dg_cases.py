@@ -8,6 +8,7 @@ import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = ["dg_advection_l2", "dg_advection_l3", "dg_advection_l3_small_dt"]
+EULER_CASES = ["dg_euler_l3"]
 PATCH, FIELDS = 4, 16
 
 

@@ -1,9 +1,10 @@
 """Generate the DG golden fixtures in this folder from the REAL reference.
 
-Builds oracle/_ref/ref_dg_driver (the unmodified reference DG patch solver,
-include/dg_helpers, compiled by oracle/Makefile; needs the reference
-checkout, so this runs only where it is present) and records each scenario
-as a compressed .npz:
+Builds oracle/_ref/ref_dg_driver and ref_dg_euler_driver (the unmodified
+reference DG patch solver, include/dg_helpers, compiled by oracle/Makefile,
+the second with the reference's DG Euler equations in place of advection;
+needs the reference checkout, so this runs only where it is present) and
+records each scenario as a compressed .npz:
 
   ids            Morton ids of the leaves (uniform level, Morton order)
   state          [dump, leaf, cell, node, variable] interior nodal values;
@@ -24,18 +25,25 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-DRIVER = REPO / "oracle" / "_ref" / "ref_dg_driver"
+DRIVERS = {"advection": REPO / "oracle" / "_ref" / "ref_dg_driver",
+           "euler": REPO / "oracle" / "_ref" / "ref_dg_euler_driver"}
 
 SCENARIOS = {
-    # name: (level, steps, initial dt, re-mesh interval (0: none), refine / coarsen thresholds)
-    "dg_advection_l2": (2, 3, 0.01, 0, 0.05, 0.01),
-    "dg_advection_l3": (3, 4, 0.01, 0, 0.05, 0.01),
-    "dg_advection_l3_small_dt": (3, 3, 0.001, 0, 0.05, 0.01),
+    # name: (level, steps, initial dt, re-mesh interval (0: none), refine / coarsen thresholds, equation)
+    "dg_advection_l2": (2, 3, 0.01, 0, 0.05, 0.01, "advection"),
+    "dg_advection_l3": (3, 4, 0.01, 0, 0.05, 0.01, "advection"),
+    "dg_advection_l3_small_dt": (3, 3, 0.001, 0, 0.05, 0.01, "advection"),
     # with the DG solver's re-mesh after steps 1, 3 (and 5): refinement to levels
     # 4-5 (the reference's thresholds) ...
-    "dg_amr_l3": (3, 4, 0.01, 2, 0.05, 0.01),
+    "dg_amr_l3": (3, 4, 0.01, 2, 0.05, 0.01, "advection"),
     # ... and refinement to level 6 followed by coarsening back to level 5
-    "dg_amr_l4": (4, 6, 0.001, 2, 0.05, 0.03),
+    "dg_amr_l4": (4, 6, 0.001, 2, 0.05, 0.03, "advection"),
+    # Euler pressure pulse: the first step size above the CFL step, which
+    # the patches' wave speeds then set ...
+    "dg_euler_l3": (3, 5, 0.003, 0, 0.05, 0.01, "euler"),
+    # ... and with re-mesh: coarsening of the flat regions (64 -> 40 leaves),
+    # then refinement along the density front (136, 388 leaves)
+    "dg_euler_amr_l3": (3, 5, 0.002, 2, 0.002, 0.0005, "euler"),
 }
 
 
@@ -64,18 +72,19 @@ def read_dumps(path: Path):
 
 def main():
     subprocess.run(["make", "-C", str(REPO / "oracle"), "ref"], check=True)
-    for name, (level, steps, dt0, amr, rthr, cthr) in SCENARIOS.items():
+    for name, (level, steps, dt0, amr, rthr, cthr, eq) in SCENARIOS.items():
         out = Path("/tmp") / f"{name}.bin"
-        subprocess.run([str(DRIVER), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"amr={amr}",
+        subprocess.run([str(DRIVERS[eq]), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"amr={amr}",
                         f"rthr={rthr}", f"cthr={cthr}", "capacity=8000", f"out={out}"], check=True)
         idss, states, dts = read_dumps(out)
         if amr == 0:
-            np.savez_compressed(HERE / f"{name}.npz", ids=idss[0], state=np.stack(states), dt=dts, level=level)
+            np.savez_compressed(HERE / f"{name}.npz", ids=idss[0], state=np.stack(states), dt=dts, level=level,
+                                equation=eq)
         else:
             extra = {f"ids_{k}": v for k, v in enumerate(idss)}
             extra.update({f"state_{k}": v for k, v in enumerate(states)})
             np.savez_compressed(HERE / f"{name}.npz", dt=dts, level=level, amr=amr, rthr=rthr, cthr=cthr,
-                                steps=steps, **extra)
+                                steps=steps, equation=eq, **extra)
         print(name, [len(i) for i in idss], dts)
 
 

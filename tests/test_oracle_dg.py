@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import dg_oracle as G
-from dg_cases import CASES, load
+from dg_cases import CASES, EULER_CASES, load
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -18,6 +18,24 @@ def test_dg_oracle_matches_reference(name):
     for k, U in enumerate(outs, start=1):
         np.testing.assert_array_equal(G.to_leaves(U, L), st[k])
     np.testing.assert_array_equal(np.array(mine), dts[1:])
+
+
+@pytest.mark.parametrize("name", EULER_CASES)
+def test_dg_euler_oracle_matches_reference(name):
+    """The DG Euler equations (flux, pressure, the patch's running maximum of
+    the face speeds, the CFL step from the last stage) from the reference's
+    initial state: every step and step size bit for bit.  The initial state
+    itself is compared within 4 ulp: the pulse exp(-100 r^2) comes from the
+    C library's exp there and numpy's here."""
+    z = load(name)
+    L = int(z["level"])
+    st, dts = z["state"], z["dt"]
+    np.testing.assert_allclose(G.to_leaves(G.euler_initial_state(L), L), st[0], rtol=4 * 2.0 ** -52, atol=0)
+    outs, mine = G.run(L, len(st) - 1, dt0=float(dts[1]), U=G.from_leaves(st[0], L), equation="euler")
+    for k, U in enumerate(outs, start=1):
+        np.testing.assert_array_equal(G.to_leaves(U, L), st[k])
+    np.testing.assert_array_equal(np.array(mine), dts[1:])
+    assert dts[2] < dts[1]  # the wave speeds set the step after the first
 
 
 def test_dg_tables_match_the_basis():
