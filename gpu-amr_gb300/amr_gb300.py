@@ -22,6 +22,7 @@ LIB_PATH = PKG / "lib" / "libamr_gb300.so"
 
 AMR_OK, AMR_ERR_INVALID, AMR_ERR_CUDA, AMR_ERR_CAPACITY, AMR_ERR_UNBALANCED, AMR_ERR_UNSUPPORTED, AMR_ERR_NO_DEVICE = range(7)
 F64, F32 = 0, 1
+DG_ADVECTION, DG_EULER = 0, 1  # amr_tree_dg_set_equation
 
 HALO_META = np.dtype(
     [("neighbor", "<i4"), ("finer_ids", "<i4", (4,)), ("quadrant", "<i4", (3,)), ("relation", "i1"), ("padding", "i1", (3,))]
@@ -129,6 +130,7 @@ def lib():
         L.amr_tree_dg_advance.argtypes = [vp, sz, C.POINTER(dbl), C.POINTER(dbl)]
         L.amr_tree_dg_remesh.argtypes = [vp, dbl, dbl, C.POINTER(i32)]
         L.amr_tree_dg_run.argtypes = [vp, dbl, dbl, i32, dbl, dbl, C.POINTER(DgStats)]
+        L.amr_tree_dg_set_equation.argtypes = [vp, i32]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -367,6 +369,12 @@ class Tree:
         check(lib().amr_tree_advance_ssprk(self._h, steps, order, v, cfl, remaining))
 
     # -------------------------------------------------------------- DG
+    def dg_set_equation(self, equation):
+        """DG_ADVECTION (default) or DG_EULER ("advection" / "euler")."""
+        if isinstance(equation, str):
+            equation = {"advection": DG_ADVECTION, "euler": DG_EULER}[equation]
+        check(lib().amr_tree_dg_set_equation(self._h, equation))
+
     def dg_advance(self, steps, dt, time=0.0):
         """Nodal DG steps (order 2, 2D, 16 fields): returns (next step size,
         time).  dt is the step size of the first step."""

@@ -184,6 +184,227 @@ k_dg_stage(const double* __restrict__ in, const double* un, double* out, const u
     }
 }
 
+// ------------------------------------------------ DG Euler
+constexpr double kDgGamma = 1.4;
+
+// compute_pressure and compute_velocity (euler.hpp:57-87) of one node
+__device__ __forceinline__ void dg_euler_node(double mx, double my, double rho, double E, double& p, double& u,
+                                              double& v)
+{
+    double kin = 0.0;
+    kin += 0.5 * mx * mx / rho;
+    kin += 0.5 * my * my / rho;
+    p = (kDgGamma - 1.0) * (E - kin);
+    u = mx / rho;
+    v = my / rho;
+}
+
+// max_eigenvalue (euler.hpp:149-163) from a cell's first node
+__device__ __forceinline__ double dg_euler_eig(double m_n, double rho, double p)
+{
+    const double c = sqrt(kDgGamma * p / rho);
+    return fabs(m_n / rho) + c;
+}
+
+__device__ __forceinline__ double dg_max(double a, double b) { return a < b ? b : a; } // std::max(a, b)
+
+// p, u, v per node of every padded cell (ghosts included)
+__global__ void __launch_bounds__(256)
+k_dg_euler_prims(const double* __restrict__ in, double* __restrict__ prims, long long total, size_t fstride)
+{
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
+         c += static_cast<long long>(gridDim.x) * blockDim.x)
+#pragma unroll
+        for (int node = 0; node < 4; ++node) {
+            const double* U = in + node * kDgVars * fstride + c;
+            double        p, u, v;
+            dg_euler_node(U[0], U[fstride], U[2 * fstride], U[3 * fstride], p, u, v);
+            prims[(node * 3 + 0) * fstride + c] = p;
+            prims[(node * 3 + 1) * fstride + c] = u;
+            prims[(node * 3 + 2) * fstride + c] = v;
+        }
+}
+
+// flux component adim (0: x, 1: y) of variable var at one node (evaluate_flux,
+// euler.hpp:109-143): rho u_i u_d (+ p if i = d), rho u_d, (E + p) u_d
+__device__ __forceinline__ double dg_euler_flux(const double* U, const double* pr, size_t fstride, int node, int var,
+                                                int adim)
+{
+    const double ud = pr[(node * 3 + 1 + adim) * fstride];
+    const double q  = U[(node * kDgVars + var) * fstride];
+    if (var < 2) {
+        const double f = q * ud;
+        return var == adim ? f + pr[(node * 3) * fstride] : f;
+    }
+    if (var == 2) return q * ud;
+    return (q + pr[(node * 3) * fstride]) * ud;
+}
+
+// Sixteen threads per patch as k_dg_stage; the face speeds are formed first
+// and the patch's running maximum is a prefix maximum over its 16 cells
+// (the reference visits the cells row-major and each cell's faces in order).
+__global__ void __launch_bounds__(64)
+k_dg_euler_stage(const double* __restrict__ in, const double* un, double* out, const double* __restrict__ prims,
+                 const uint64_t* __restrict__ keys, int P, Geo g, size_t fstride, DgTables tb,
+                 const double* __restrict__ dtp, unsigned long long* dt_min, int mode)
+{
+    constexpr int   P1    = kDgPatch + 2, FLAT = P1 * P1, CELLS = kDgPatch * kDgPatch;
+    const long long total = static_cast<long long>(P) * CELLS;
+    const double    dt    = dtp[0];
+    const int       lane  = threadIdx.x & 31;
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c - lane < total;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const bool   valid = c < total;
+        const int    p = valid ? static_cast<int>(c >> 4) : 0, k = static_cast<int>(c & 15);
+        const int    li   = ((k >> 2) + 1) * P1 + (k & 3) + 1;
+        const size_t base = static_cast<size_t>(p) * FLAT + li;
+        const int    lev  = key_level(keys[p]);
+        const double edge = (1.0 / static_cast<double>(1u << lev)) / static_cast<double>(kDgPatch);
+        const double vol  = (1.0 * edge) * edge;
+        const double area = 1.0 * edge;
+        const double s    = (1.0 / edge) * vol;
+        const double im   = 4.0 / vol;
+        const double* U   = in + base;
+        const double* pr  = prims + base;
+        // face speeds: max(eig(cell), eig(neighbour)) per face, the cell's
+        // running maximum over its faces, then the prefix over the patch
+        double lam[4];
+        {
+            const double eig_cell[2] = { dg_euler_eig(U[0], U[2 * fstride], pr[0]),
+                                         dg_euler_eig(U[fstride], U[2 * fstride], pr[0]) };
+            double       run         = -INFINITY;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                const int     pdim = f >> 1, sign = (f & 1) ? 1 : -1, adim = 1 - pdim;
+                const int     off  = (pdim == 0 ? P1 : 1) * sign;
+                const double* Un   = U + off;
+                const double  en   = dg_euler_eig(Un[adim * fstride], Un[2 * fstride], pr[off]);
+                run                = dg_max(run, dg_max(eig_cell[adim], en));
+                lam[f]             = run;
+            }
+            if (!valid) run = -INFINITY;
+            // exclusive prefix maximum of the cells' maxima over the 16 lanes
+            // of this patch (lanes 0-15 or 16-31 of the warp)
+            double x = run;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, x, o, 16);
+                if ((lane & 15) >= o) x = dg_max(y, x);
+            }
+            double before = __shfl_up_sync(0xffffffffu, x, 1, 16);
+            if ((lane & 15) == 0) before = -INFINITY;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) lam[f] = dg_max(before, lam[f]);
+        }
+        if (valid) {
+#pragma unroll 1
+            for (int v = 0; v < kDgVars; ++v) {
+                double Uv[2][2], du[2][2];
+#pragma unroll
+                for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+                    for (int iy = 0; iy < 2; ++iy) Uv[ix][iy] = U[((ix * 2 + iy) * kDgVars + v) * fstride];
+                // volume: d/dx of F_x and d/dy of F_y against the mass
+                {
+                    double G[2][2];
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) G[i][j] = dg_euler_flux(U, pr, fstride, i * 2 + j, v, 0) * 0.25;
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            const double cx = (0.0 + tb.d[i][0] * G[0][j]) + tb.d[i][1] * G[1][j];
+                            du[i][j]        = 0.0 + s * cx;
+                        }
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) G[i][j] = dg_euler_flux(U, pr, fstride, i * 2 + j, v, 1) * 0.25;
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            const double cy = (0.0 + tb.d[j][0] * G[i][0]) + tb.d[j][1] * G[i][1];
+                            du[i][j]        = du[i][j] + s * cy;
+                        }
+                }
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    const int     pdim = f >> 1, sign = (f & 1) ? 1 : -1, sidx = (f & 1);
+                    const int     adim = 1 - pdim;
+                    const int     off  = (pdim == 0 ? P1 : 1) * sign;
+                    const double* Un   = U + off;
+                    const double* prn  = pr + off;
+                    double        Vn[2][2], Fc[2][2], Fn[2][2];
+#pragma unroll
+                    for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+                        for (int iy = 0; iy < 2; ++iy) {
+                            Vn[ix][iy] = Un[((ix * 2 + iy) * kDgVars + v) * fstride];
+                            Fc[ix][iy] = dg_euler_flux(U, pr, fstride, ix * 2 + iy, v, adim);
+                            Fn[ix][iy] = dg_euler_flux(Un, prn, fstride, ix * 2 + iy, v, adim);
+                        }
+                    double uf[2], ff[2], un2[2], fn2[2];
+                    dg_face_project(Uv, tb.k[sidx], adim, uf);
+                    dg_face_project(Fc, tb.k[sidx], adim, ff);
+                    dg_face_project(Vn, tb.k[1 - sidx], adim, un2);
+                    dg_face_project(Fn, tb.k[1 - sidx], adim, fn2);
+                    double wf[2];
+#pragma unroll
+                    for (int rr = 0; rr < 2; ++rr) {
+                        const double nf = (static_cast<double>(sign) * (ff[rr] + fn2[rr]) * 0.5 +
+                                           (uf[rr] - un2[rr]) * (0.5 * lam[f])) *
+                                          area;
+                        wf[rr] = nf * 0.5;
+                    }
+#pragma unroll
+                    for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+                        for (int iy = 0; iy < 2; ++iy) {
+                            const double face = adim == 1 ? wf[ix] * tb.k[sidx][iy] : tb.k[sidx][ix] * wf[iy];
+                            du[ix][iy]        = du[ix][iy] - face;
+                        }
+                }
+#pragma unroll
+                for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+                    for (int iy = 0; iy < 2; ++iy) {
+                        const size_t at  = ((ix * 2 + iy) * kDgVars + v) * fstride + base;
+                        const double u   = Uv[ix][iy];
+                        const double rdt = (du[ix][iy] * im) * dt;
+                        out[at]          = mode == 0 ? u + rdt : ((un[at] + u) + rdt) * 0.5;
+                    }
+            }
+            // the patch's final speed (last cell, last face) sets its CFL step
+            if (mode == 1 && k == 15 && lam[3] > 0.0) {
+                const double scale = 1.0 / (4.0 + 1.0); // 1 / (order^dim + 1)
+                const double h     = scale * 0.5 * edge / lam[3];
+                atomicMin(dt_min, static_cast<unsigned long long>(__double_as_longlong(h)));
+            }
+            for (int gi = k; gi < 2 * P1 + 2 * kDgPatch; gi += CELLS) {
+                int gr, gc;
+                if (gi < P1) gr = 0, gc = gi;
+                else if (gi < 2 * P1) gr = P1 - 1, gc = gi - P1;
+                else if (gi < 2 * P1 + kDgPatch) gr = gi - 2 * P1 + 1, gc = 0;
+                else gr = gi - 2 * P1 - kDgPatch + 1, gc = P1 - 1;
+                dg_ghost(in, un, out, fstride, static_cast<size_t>(p) * FLAT + gr * P1 + gc, dt, mode);
+            }
+        }
+    }
+}
+
+__global__ void k_dg_euler_next(double* dt, double* time, unsigned long long* dt_min)
+{
+    const double h    = dt[0];
+    const double m    = __longlong_as_double(static_cast<long long>(*dt_min));
+    const double dmin = m < h ? m : h; // dt_min starts at dt (solver.hpp:122)
+    time[0] += h;
+    dt[0]   = h < dmin ? h : dmin;     // dt = std::min(dt, dt_min)
+    *dt_min = 0x7ff0000000000000ull;   // +inf
+}
+
 // ------------------------------------------------ DG prolongation / restriction
 // The tree's DefaultAMRPolicy (include/dg_helpers/tree_builder.hpp:59-289)
 // for the DG tensor: a fine cell's nodal values are the coarse cell's
@@ -426,6 +647,33 @@ cudaError_t dg_flags(const double* in, int P, const Geo& g, size_t fstride, doub
     const long long total = static_cast<long long>(P) * 16;
     const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 16));
     k_dg_flags<<<grid, 256, 0, s>>>(in, P, g, fstride, rthr, cthr, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_euler_prims(const double* in, double* prims, int P, const Geo& g, size_t fstride, cudaStream_t s)
+{
+    if (P <= 0) return cudaSuccess;
+    const long long total = static_cast<long long>(P) * g.flat;
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 255) / 256, 152LL * 16));
+    k_dg_euler_prims<<<grid, 256, 0, s>>>(in, prims, total, fstride);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_euler_stage(const DgEulerStage& s)
+{
+    if (s.P <= 0) return cudaSuccess;
+    if (s.g.n != kDgPatch || s.g.h != 1) return cudaErrorInvalidValue;
+    const DgTables  tb    = dg_tables();
+    const long long total = static_cast<long long>(s.P) * kDgPatch * kDgPatch;
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 63) / 64, 152LL * 32));
+    k_dg_euler_stage<<<grid, 64, 0, s.stream>>>(s.in, s.un, s.out, s.prims, s.keys, s.P, s.g, s.fstride, tb, s.dt,
+                                                s.dt_min, s.mode);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_euler_next(double* dt, double* time, unsigned long long* dt_min, cudaStream_t s)
+{
+    k_dg_euler_next<<<1, 1, 0, s>>>(dt, time, dt_min);
     return cudaGetLastError();
 }
 

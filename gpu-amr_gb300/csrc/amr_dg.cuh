@@ -40,6 +40,35 @@ struct DgStage {
 };
 cudaError_t dg_stage(const DgStage& s);
 
+// The DG Euler equations (include/dg_helpers/equations/euler.hpp, variables
+// [rho u, rho v, rho, E], gamma 1.4) with the same residual structure; the
+// Rusanov speed is the patch's running maximum of max(eig(cell),
+// eig(neighbour)) over its faces in the reference's loop order (cells row-
+// major, faces y-, y+, x-, x+), eig from the cell's first node.
+//   prims: per padded cell and node, p, u, v (12 fields fstride apart),
+//   formed after each halo exchange by dg_euler_prims.
+//   dt: the step in use (device, [0]); in the last stage (mode 1) each patch
+//   folds 0.1 x edge / lambda into dt_min (ordered bit pattern of a positive
+//   double), and dg_euler_next takes dt = min(dt, min(dt, dt_min)), adds the
+//   step to time and resets dt_min.
+struct DgEulerStage {
+    const double*       in;
+    const double*       un;
+    double*             out;
+    const double*       prims;
+    const uint64_t*     keys;
+    int                 P;
+    Geo                 g;
+    size_t              fstride;
+    const double*       dt;
+    unsigned long long* dt_min;
+    int                 mode;
+    cudaStream_t        stream;
+};
+cudaError_t dg_euler_prims(const double* in, double* prims, int P, const Geo& g, size_t fstride, cudaStream_t s);
+cudaError_t dg_euler_stage(const DgEulerStage& s);
+cudaError_t dg_euler_next(double* dt, double* time, unsigned long long* dt_min, cudaStream_t s);
+
 // Halo exchange of a DG state (16 fields fstride apart): same-level faces
 // copy, coarse-fine faces restrict or interpolate the DG polynomials.
 cudaError_t dg_halo(double* buf, const amr_halo_meta* meta, int P, const Geo& g, size_t fstride, cudaStream_t s);

@@ -154,6 +154,11 @@ struct amr_tree {
     int4*          prec = nullptr; // pass records, one per leaf (multi-step passes)
     int4*          frec = nullptr; // face records, one per leaf (flags of same-level graph intervals)
     bool           dg_state = false; // the re-mesh in progress carries a DG state (polynomial remap)
+    int            dg_equation = AMR_DG_ADVECTION;
+    double*        dg_prims    = nullptr; // DG Euler: p, u, v per node and padded cell (12 fields)
+    size_t         dg_prims_cap = 0;       // leaves dg_prims holds
+    double*        dg_scalars  = nullptr; // DG Euler: [0] step size, [1] time
+    unsigned long long* dg_dtmin = nullptr; // DG Euler: smallest CFL step of the last stage (bit pattern)
     int            tb = 0;
 
     int8_t*   flags  = nullptr;
@@ -569,6 +574,9 @@ void free_tree(amr_tree* t)
     }
     cudaFree(t->prec);
     cudaFree(t->frec);
+    cudaFree(t->dg_prims);
+    cudaFree(t->dg_scalars);
+    cudaFree(t->dg_dtmin);
     cudaFree(t->flags);
     cudaFree(t->rmark);
     cudaFree(t->chead);
@@ -1476,6 +1484,9 @@ amr_status amr_tree_reserve(amr_tree* t, size_t cap)
     cudaFree(t->stage_buf); // SSPRK scratch: allocated again at the next SSPRK advance
     t->stage_buf = nullptr;
     t->stage_cap = 0;
+    cudaFree(t->dg_prims); // DG Euler scratch: allocated again at the next DG Euler advance
+    t->dg_prims     = nullptr;
+    t->dg_prims_cap = 0;
     t->sbuf[0] = sb0;
     t->sbuf[1] = sb1;
     t->cur     = nsb[cs];
@@ -1969,6 +1980,78 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
     return AMR_OK;
 }
 
+amr_status amr_tree_dg_set_equation(amr_tree* t, int equation)
+{
+    if (!t) return fail(AMR_ERR_INVALID, "null argument");
+    if (equation != AMR_DG_ADVECTION && equation != AMR_DG_EULER) return fail(AMR_ERR_INVALID, "unknown DG equation");
+    if (equation == AMR_DG_EULER && !t->dg_scalars) {
+        AMR_CUDA(cudaMalloc(&t->dg_scalars, 2 * sizeof(double)));
+        AMR_CUDA(cudaMalloc(&t->dg_dtmin, sizeof(unsigned long long)));
+        const unsigned long long inf = 0x7ff0000000000000ull; // +inf: no patch seen
+        AMR_CUDA(cudaMemcpy(t->dg_dtmin, &inf, sizeof inf, cudaMemcpyHostToDevice));
+    }
+    t->dg_equation = equation;
+    return AMR_OK;
+}
+
+namespace
+{
+// DG Euler steps: the step size lives on the device, set per step from the
+// patches' wave speeds (solver.hpp:221-226), so the host reads it back once
+// per call
+amr_status dg_euler_advance(amr_tree* t, const DgStage& st, size_t steps, double* dt, double* time)
+{
+    cudaStream_t         s    = t->stream;
+    const Geo&           g    = t->g;
+    const amr_halo_meta* meta = t->meta[t->tb];
+    if (t->dg_prims_cap < t->cap) {
+        cudaFree(t->dg_prims);
+        t->dg_prims     = nullptr;
+        t->dg_prims_cap = 0;
+        AMR_CUDA(cudaMalloc(&t->dg_prims, 12 * t->fstride() * sizeof(double)));
+        t->dg_prims_cap = t->cap;
+    }
+    double* hp = static_cast<double*>(t->pinned);
+    hp[0]      = *dt;
+    hp[1]      = time ? *time : 0.0;
+    AMR_CUDA(cudaMemcpyAsync(t->dg_scalars, hp, 2 * sizeof(double), cudaMemcpyHostToDevice, s));
+    DgEulerStage es{};
+    es.prims   = t->dg_prims;
+    es.keys    = st.keys;
+    es.P       = st.P;
+    es.g       = g;
+    es.fstride = st.fstride;
+    es.dt      = t->dg_scalars;
+    es.dt_min  = t->dg_dtmin;
+    es.stream  = s;
+    uint64_t launches = 0;
+    for (size_t k = 0; k < steps; ++k) {
+        AMR_CUDA(dg_halo(static_cast<double*>(t->cur), meta, st.P, g, st.fstride, s));
+        AMR_CUDA(dg_euler_prims(static_cast<const double*>(t->cur), t->dg_prims, st.P, g, st.fstride, s));
+        es.in   = static_cast<const double*>(t->cur);
+        es.un   = static_cast<const double*>(t->cur);
+        es.out  = static_cast<double*>(t->nxt);
+        es.mode = 0;
+        AMR_CUDA(dg_euler_stage(es));
+        AMR_CUDA(dg_halo(static_cast<double*>(t->nxt), meta, st.P, g, st.fstride, s));
+        AMR_CUDA(dg_euler_prims(static_cast<const double*>(t->nxt), t->dg_prims, st.P, g, st.fstride, s));
+        es.in   = static_cast<const double*>(t->nxt);
+        es.out  = static_cast<double*>(t->cur); // u^n is read and replaced cell by cell
+        es.mode = 1;
+        AMR_CUDA(dg_euler_stage(es));
+        AMR_CUDA(dg_euler_next(t->dg_scalars, t->dg_scalars + 1, t->dg_dtmin, s));
+        launches += 7;
+    }
+    AMR_CUDA(cudaMemcpyAsync(hp, t->dg_scalars, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaStreamSynchronize(s));
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
+    t->ghosts_valid = true;
+    *dt             = hp[0];
+    if (time) *time = hp[1];
+    return AMR_OK;
+}
+} // namespace
+
 amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time)
 {
     if (!t || !dt) return fail(AMR_ERR_INVALID, "null argument");
@@ -1983,6 +2066,7 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
     st.g       = g;
     st.fstride = t->fstride();
     st.stream  = s;
+    if (t->dg_equation == AMR_DG_EULER) return dg_euler_advance(t, st, steps, dt, time);
     // CFL step of the finest cells (solver.hpp:221-226 with |v| = 1)
     const double edge   = (1.0 / static_cast<double>(1u << t->max_level_host)) / static_cast<double>(kDgPatch);
     const double scale  = 1.0 / (std::pow(static_cast<double>(kDgOrder), 2.0) + 1.0);

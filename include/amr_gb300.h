@@ -334,6 +334,23 @@ typedef struct amr_dg_stats {
 amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int amr_interval,
                            double refine_threshold, double coarsen_threshold, amr_dg_stats* stats);
 
+/* The equation of the DG tree, the reference's compile-time
+ * GlobalConfigPolicy::equation (include/config/generated_config.hpp,
+ * include/dg_helpers/equations/): AMR_DG_ADVECTION (the default; linear
+ * advection, velocity 1 in both directions, the 4 variables independent) or
+ * AMR_DG_EULER (include/dg_helpers/equations/euler.hpp: variables
+ * [rho u, rho v, rho, E] per node, gamma 1.4).  With Euler the Rusanov speed
+ * of a face is the patch's running maximum, in the reference's loop order,
+ * of max(eigenvalue of the cell, of the neighbour) (|u_n| + sqrt(gamma p /
+ * rho) at the cell's first node), and each step's CFL step comes from every
+ * patch's final speed (0.1 x edge / lambda, solver.hpp:221-226), computed on
+ * the device: amr_tree_dg_advance reads the step size back once per call.
+ * amr_tree_dg_advance, amr_tree_dg_remesh and amr_tree_dg_run apply the
+ * setting; states are bit-identical to the reference's CPU path. */
+#define AMR_DG_ADVECTION 0
+#define AMR_DG_EULER     1
+amr_status amr_tree_dg_set_equation(amr_tree* t, int equation);
+
 /* ------------------------------------------------------------- Euler
  * EulerPhysics<DIM> (include/solver/EulerPhysics.hpp:17-170) through
  * amr_solver (amr_solver.hpp:155-413) on a tree created with fields =

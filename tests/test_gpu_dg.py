@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import dg_oracle as G
-from dg_cases import CASES, fields_to_leaves, leaves_to_fields, load
+from dg_cases import CASES, EULER_CASES, fields_to_leaves, leaves_to_fields, load
 
 pytestmark = pytest.mark.gpu
 
@@ -87,27 +87,92 @@ def test_gpu_dg_remesh_matches_reference(amr, name):
         np.testing.assert_array_equal(fields_to_leaves(t.download_state()), z[f"state_{k}"])
 
 
-def test_gpu_dg_run_equals_the_stepwise_loop(amr):
+@pytest.mark.parametrize("equation", ["advection", "euler"])
+def test_gpu_dg_run_equals_the_stepwise_loop(amr, equation):
     """amr_tree_dg_run (the solver loop in one call) against the same loop
     driven step by step through amr_tree_dg_advance and amr_tree_dg_remesh:
     same steps, re-meshes, leaves and states."""
-    U0 = G.initial_state(3)
+    U0 = G.initial_state(3) if equation == "advection" else G.euler_initial_state(3)
+    rthr, cthr = (0.05, 0.01) if equation == "advection" else (0.002, 0.0005)
+    dt0 = 0.01 if equation == "advection" else 0.002
     a = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
     b = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
     for t in (a, b):
+        t.dg_set_equation(equation)
         t.refine_uniform(3)
         t.upload_state(leaves_to_fields(G.to_leaves(U0, 3)))
-    st = a.dg_run(0.01, 0.05, 3, 0.05, 0.01)
-    dt, time, step, next_amr, cells, remeshes = 0.01, 0.0, 0, 0, 0, 0
+    st = a.dg_run(dt0, 0.05, 3, rthr, cthr)
+    dt, time, step, next_amr, cells, remeshes = dt0, 0.0, 0, 0, 0, 0
     while time < 0.05:
         cells += b.size * 16
         dt, time = b.dg_advance(1, dt, time)
         step += 1
         if step >= next_amr:
-            b.dg_remesh(0.05, 0.01)
+            b.dg_remesh(rthr, cthr)
             remeshes += 1
             next_amr = step + 3
     assert (st["steps"], st["remeshes"], st["cells"]) == (step, remeshes, cells)
     assert st["time"] == time and st["next_dt"] == dt
     np.testing.assert_array_equal(a.ids(), b.ids())
     np.testing.assert_array_equal(a.download_state(), b.download_state())
+
+
+@pytest.mark.parametrize("name", EULER_CASES)
+def test_gpu_dg_euler_matches_reference(amr, name):
+    """DG Euler (flux, pressure, the patch's running maximum of the face
+    speeds, the CFL step reduced on the device) against the reference's DG
+    Euler solver: states and step sizes after every step, bit for bit."""
+    z = load(name)
+    L = int(z["level"])
+    st, dts = z["state"], z["dt"]
+    t = _dg_tree(amr, L)
+    t.dg_set_equation("euler")
+    t.upload_state(leaves_to_fields(st[0]))
+    dt, time = float(dts[1]), 0.0
+    for k in range(1, len(st)):
+        assert dt == dts[k]
+        dt, time = t.dg_advance(1, dt, time)
+        np.testing.assert_array_equal(fields_to_leaves(t.download_state()), st[k])
+    assert dts[2] < dts[1]
+
+
+def test_gpu_dg_euler_remesh_matches_reference(amr):
+    """DG Euler with the solver's re-mesh (coarsening of the flat regions,
+    refinement along the density front) against the reference run."""
+    z = load("dg_euler_amr_l3")
+    L, every, steps = int(z["level"]), int(z["amr"]), int(z["steps"])
+    dts = z["dt"]
+    t = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
+    t.dg_set_equation(amr.DG_EULER)
+    t.refine_uniform(L)
+    t.upload_state(leaves_to_fields(z["state_0"]))
+    dt, time, next_amr = float(dts[1]), 0.0, 0
+    for k in range(1, steps + 1):
+        assert dt == dts[k]
+        dt, time = t.dg_advance(1, dt, time)
+        if k >= next_amr:
+            t.dg_remesh(float(z["rthr"]), float(z["cthr"]))
+            next_amr = k + every
+        np.testing.assert_array_equal(t.ids(), z[f"ids_{k}"])
+        np.testing.assert_array_equal(fields_to_leaves(t.download_state()), z[f"state_{k}"])
+
+
+def test_gpu_dg_euler_matches_oracle(amr):
+    """A larger uniform tree (level 5, 1024 leaves, several steps in one
+    call) against the numpy restatement: final state, step size and time."""
+    L, steps = 5, 4
+    U0 = G.euler_initial_state(L)
+    t = _dg_tree(amr, L)
+    t.dg_set_equation("euler")
+    t.upload_state(leaves_to_fields(G.to_leaves(U0, L)))
+    dt, time = t.dg_advance(steps, 0.003)
+    outs, dts = G.run(L, steps + 1, dt0=0.003, U=U0, equation="euler")
+    np.testing.assert_array_equal(fields_to_leaves(t.download_state()), G.to_leaves(outs[steps - 1], L))
+    assert dt == dts[steps]
+    assert time == ((((0.0 + dts[0]) + dts[1]) + dts[2]) + dts[3])
+
+
+def test_gpu_dg_set_equation_rejects_unknown(amr):
+    t = _dg_tree(amr, 1)
+    with pytest.raises(amr.AmrError):
+        amr.check(amr.lib().amr_tree_dg_set_equation(t._h, 7))
