@@ -891,6 +891,95 @@ def dg_loop(torch, A, stream):
                       "re-mesh)"}
 
 
+DG_EULER = dict(levels=(5, 9), steps={5: 100, 9: 10}, dt0={5: 0.003, 9: 1e-5}, cpu_level=5, cpu_steps=3)
+
+
+def _dg_euler_pulse(lv):
+    """The reference's DG Euler initial state (pressure pulse exp(-100 r^2) + 1
+    at the nodes, rho 1, zero momentum), vectorised for large levels: the
+    tree's [field, leaf, 6, 6] in the Morton leaf order of a uniform level."""
+    P, C = 4, 4 << lv
+    cell = (1.0 / float(1 << lv)) / 4.0
+    pts = (0.5 - 0.5 / np.sqrt(3.0), 0.5 + 0.5 / np.sqrt(3.0))
+    c = (np.arange(C) + 0.5) * cell
+    n = 1 << lv
+    m = np.arange(n * n, dtype=np.int64)
+    px = np.zeros_like(m)
+    py = np.zeros_like(m)
+    for bit in range(lv):
+        px |= ((m >> (2 * bit)) & 1) << bit
+        py |= ((m >> (2 * bit + 1)) & 1) << bit
+    a = np.zeros((16, n * n, 6, 6))
+    for ix in range(2):
+        for iy in range(2):
+            x = c[None, :] + (pts[ix] - 0.5) * cell
+            y = c[:, None] + (pts[iy] - 0.5) * cell
+            p = np.exp(-100.0 * ((x - 0.5) ** 2 + (y - 0.5) ** 2)) + 1.0  # [cy, cx]
+            blk = p.reshape(n, P, n, P).transpose(0, 2, 1, 3)[py, px]     # [leaf, ly, lx]
+            k = ix * 2 + iy
+            a[k * 4 + 2, :, 1:5, 1:5] = 1.0
+            a[k * 4 + 3, :, 1:5, 1:5] = blk / (1.4 - 1.0)
+    return a
+
+
+def dg_euler_extra(torch, A, stream, with_cpu=True):
+    """DG Euler steps (the reference's DG Euler equations in the same order-2
+    configuration: pressure pulse, CFL step from the patches' wave speeds)
+    through amr_tree_dg_advance; the numpy restatement on the host for a few
+    steps of the level-5 tree, bit for bit."""
+    from oracle import dg_oracle as G
+
+    D = DG_EULER
+    out = {"workload": "nodal DG Euler (order 2, 2D, 4x4 cells per patch + 1 ghost, variables [rho u, rho v, rho, "
+                       "E] per node, SSPRK2, Rusanov speed = the patch's running maximum, CFL step from the last "
+                       "stage), pressure pulse, uniform levels, no re-mesh",
+           "unit": "cell-updates/s (interior cells, each with 16 nodal values)"}
+    for lv in D["levels"]:
+        t = A.Tree(2, 4, 1, 10, capacity=(1 << (2 * lv)) + 64, dtype=A.F64, fields=16, stream=stream.cuda_stream)
+        t.dg_set_equation("euler")
+        t.refine_uniform(lv)
+        cells = t.size * 16
+        t.upload_state(_dg_euler_pulse(lv))
+        dt, tm = t.dg_advance(1, D["dt0"][lv])  # warm-up: the first step at the initial dt
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = D["steps"][lv]
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            dt, tm = t.dg_advance(n, dt, tm)
+            ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        rate = cells * n / (ms * 1e-3)
+        rec = {"value": rate, "unit": "cell-updates/s", "ms_per_step": ms / n, "leaves": t.size, "cells": cells,
+               "steps_timed": n, "dt_after": dt,
+               "launches_per_step": 7,
+               "note": "per step: two halo exchanges, two primitive passes (p, u, v per node), two stages and "
+                       "the step-size update; the step size stays on the device"}
+        if with_cpu and lv == D["cpu_level"]:
+            L0 = D["cpu_level"]
+            U0 = G.euler_initial_state(L0)
+            c0 = time.perf_counter()
+            outs, _ = G.run(L0, D["cpu_steps"], dt0=D["dt0"][L0], U=U0, equation="euler")
+            csec = time.perf_counter() - c0
+            g = A.Tree(2, 4, 1, 10, capacity=(1 << (2 * L0)) + 64, dtype=A.F64, fields=16,
+                       stream=stream.cuda_stream)
+            g.dg_set_equation("euler")
+            g.refine_uniform(L0)
+            g.upload_state(_dg_fields(G.to_leaves(U0, L0)))
+            g.dg_advance(D["cpu_steps"], D["dt0"][L0])
+            mine = _dg_leaves(g.download_state())
+            rec["cpu_baseline"] = {"value": (16 << (2 * L0)) * D["cpu_steps"] / csec, "unit": "cell-updates/s",
+                                   "cores": 1, "kind": "port",
+                                   "sample": f"first {D['cpu_steps']} steps of the level-{L0} tree, numpy "
+                                             "restatement (vectorised over cells, the running maximum in a "
+                                             "Python loop, one thread)"}
+            rec["parity_first_steps_bit_exact"] = bool(np.array_equal(mine, G.to_leaves(outs[-1], L0)))
+            g.close()
+        t.close()
+        out[f"level{lv}"] = rec
+    return out
+
+
 def _dg_fields(st):
     """[leaf, cell, node, var] -> the tree's [field, leaf, 6, 6] (ghosts zero)."""
     P = st.shape[0]
@@ -1118,6 +1207,7 @@ def gpu_arm(args, rank, world):
             "euler_benchmark": lambda: euler_extra(torch, A, stream, with_cpu=cpu),
             "ssprk_advection": lambda: ssprk_extra(torch, A, stream, with_cpu=cpu),
             "dg_advection": lambda: dg_extra(torch, A, stream, with_cpu=cpu),
+            "dg_euler": lambda: dg_euler_extra(torch, A, stream, with_cpu=cpu),
         }
         for name, fn in table.items():
             if args.extra is None or name in args.extra:
