@@ -1344,7 +1344,8 @@ def profile_case(name, steps):
     """One untimed run of a workload, for profilers: forest (the batched FP32
     forest, `steps` steps), adjoint (the adjoint mesh, FP64 forward and
     backward over `steps` steps), config2 (one config-2 run), euler (the Euler
-    benchmark's first `steps` steps)."""
+    benchmark's first `steps` steps), dg_euler (`steps` DG Euler steps of the
+    uniform level-8 pressure pulse: 65536 leaves, 0.6 GB of state)."""
     import torch
 
     import amr_gb300 as A
@@ -1374,6 +1375,14 @@ def profile_case(name, steps):
     elif name == "euler":
         t, _ = euler_tree(A, stream, capacity=4000)  # about 1.5 GB of state and primitives
         st = euler_run(t, steps)
+    elif name == "dg_euler":
+        lv = 8
+        t = A.Tree(2, 4, 1, 10, capacity=(1 << (2 * lv)) + 64, dtype=A.F64, fields=16, stream=stream.cuda_stream)
+        t.dg_set_equation("euler")
+        t.refine_uniform(lv)
+        t.upload_state(_dg_euler_pulse(lv))
+        dt, tm = t.dg_advance(steps, 2e-5)
+        st = {"leaves": t.size, "steps": steps, "dt": dt, "time": tm}
     else:
         W = WORKLOAD
         t = A.Tree(2, W["n"], W["halo"], W["depth"], capacity=4096, stream=stream.cuda_stream)
@@ -1400,7 +1409,7 @@ def main():
     ap.add_argument("--uniform-level", type=int, default=9)
     ap.add_argument("--extra", action="append", default=None,
                     help="run only the named extra workloads after the headline (repeatable)")
-    ap.add_argument("--case", choices=["forest", "adjoint", "config2", "euler"],
+    ap.add_argument("--case", choices=["forest", "adjoint", "config2", "euler", "dg_euler"],
                     help="run one workload once, untimed (for profilers), and exit")
     ap.add_argument("--case-steps", type=int, default=30)
     args = ap.parse_args()
