@@ -187,7 +187,9 @@ k_dg_stage(const double* __restrict__ in, const double* un, double* out, const u
 // ------------------------------------------------ DG Euler
 constexpr double kDgGamma = 1.4;
 
-// compute_pressure and compute_velocity (euler.hpp:57-87) of one node
+// compute_pressure and compute_velocity (euler.hpp:57-87) of one node;
+// max_eigenvalue (euler.hpp:149-163) is |m_n / rho| + sqrt(gamma p / rho)
+// at a cell's first node
 __device__ __forceinline__ void dg_euler_node(double mx, double my, double rho, double E, double& p, double& u,
                                               double& v)
 {
@@ -199,30 +201,36 @@ __device__ __forceinline__ void dg_euler_node(double mx, double my, double rho, 
     v = my / rho;
 }
 
-// max_eigenvalue (euler.hpp:149-163) from a cell's first node
-__device__ __forceinline__ double dg_euler_eig(double m_n, double rho, double p)
-{
-    const double c = sqrt(kDgGamma * p / rho);
-    return fabs(m_n / rho) + c;
-}
-
 __device__ __forceinline__ double dg_max(double a, double b) { return a < b ? b : a; } // std::max(a, b)
 
-// p, u, v per node of every padded cell (ghosts included)
+// p, u, v per node, then the cell's eigenvalues in x and y (max_eigenvalue
+// from the first node: |m_d / rho| is that node's velocity component, the
+// same division), of every padded cell the stage reads: the interior and
+// the face ghosts (the four corner ghosts are never read and are skipped)
 __global__ void __launch_bounds__(256)
 k_dg_euler_prims(const double* __restrict__ in, double* __restrict__ prims, long long total, size_t fstride)
 {
+    constexpr int P1 = kDgPatch + 2, FLAT = P1 * P1;
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
-         c += static_cast<long long>(gridDim.x) * blockDim.x)
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int li = static_cast<int>(c % FLAT);
+        if (li == 0 || li == P1 - 1 || li == FLAT - P1 || li == FLAT - 1) continue;
+        double p0 = 0.0, u0 = 0.0, v0 = 0.0, rho0 = 1.0;
 #pragma unroll
         for (int node = 0; node < 4; ++node) {
             const double* U = in + node * kDgVars * fstride + c;
             double        p, u, v;
-            dg_euler_node(U[0], U[fstride], U[2 * fstride], U[3 * fstride], p, u, v);
+            const double  rho = U[2 * fstride];
+            dg_euler_node(U[0], U[fstride], rho, U[3 * fstride], p, u, v);
             prims[(node * 3 + 0) * fstride + c] = p;
             prims[(node * 3 + 1) * fstride + c] = u;
             prims[(node * 3 + 2) * fstride + c] = v;
+            if (node == 0) p0 = p, u0 = u, v0 = v, rho0 = rho;
         }
+        const double a = sqrt(kDgGamma * p0 / rho0);
+        prims[12 * fstride + c] = fabs(u0) + a;
+        prims[13 * fstride + c] = fabs(v0) + a;
+    }
 }
 
 // flux component adim (0: x, 1: y) of variable var at one node (evaluate_flux,
@@ -270,16 +278,14 @@ k_dg_euler_stage(const double* __restrict__ in, const double* un, double* out, c
         // running maximum over its faces, then the prefix over the patch
         double lam[4];
         {
-            const double eig_cell[2] = { dg_euler_eig(U[0], U[2 * fstride], pr[0]),
-                                         dg_euler_eig(U[fstride], U[2 * fstride], pr[0]) };
+            const double eig_cell[2] = { pr[12 * fstride], pr[13 * fstride] };
             double       run         = -INFINITY;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
-                const int     pdim = f >> 1, sign = (f & 1) ? 1 : -1, adim = 1 - pdim;
-                const int     off  = (pdim == 0 ? P1 : 1) * sign;
-                const double* Un   = U + off;
-                const double  en   = dg_euler_eig(Un[adim * fstride], Un[2 * fstride], pr[off]);
-                run                = dg_max(run, dg_max(eig_cell[adim], en));
+                const int    pdim = f >> 1, sign = (f & 1) ? 1 : -1, adim = 1 - pdim;
+                const int    off  = (pdim == 0 ? P1 : 1) * sign;
+                const double en   = pr[(12 + adim) * fstride + off];
+                run               = dg_max(run, dg_max(eig_cell[adim], en));
                 lam[f]             = run;
             }
             if (!valid) run = -INFINITY;

@@ -45,8 +45,9 @@ cudaError_t dg_stage(const DgStage& s);
 // Rusanov speed is the patch's running maximum of max(eig(cell),
 // eig(neighbour)) over its faces in the reference's loop order (cells row-
 // major, faces y-, y+, x-, x+), eig from the cell's first node.
-//   prims: per padded cell and node, p, u, v (12 fields fstride apart),
-//   formed after each halo exchange by dg_euler_prims.
+//   prims: per padded cell and node, p, u, v (fields 0-11, fstride apart),
+//   then the cell's eigenvalues in x and y (fields 12, 13), formed after
+//   each halo exchange by dg_euler_prims (corner ghosts left unset).
 //   dt: the step in use (device, [0]); in the last stage (mode 1) each patch
 //   folds 0.1 x edge / lambda into dt_min (ordered bit pattern of a positive
 //   double), and dg_euler_next takes dt = min(dt, min(dt, dt_min)), adds the

@@ -155,7 +155,7 @@ struct amr_tree {
     int4*          frec = nullptr; // face records, one per leaf (flags of same-level graph intervals)
     bool           dg_state = false; // the re-mesh in progress carries a DG state (polynomial remap)
     int            dg_equation = AMR_DG_ADVECTION;
-    double*        dg_prims    = nullptr; // DG Euler: p, u, v per node and padded cell (12 fields)
+    double*        dg_prims    = nullptr; // DG Euler: p, u, v per node, eigenvalues x, y per padded cell (14 fields)
     size_t         dg_prims_cap = 0;       // leaves dg_prims holds
     double*        dg_scalars  = nullptr; // DG Euler: [0] step size, [1] time
     unsigned long long* dg_dtmin = nullptr; // DG Euler: smallest CFL step of the last stage (bit pattern)
@@ -2008,7 +2008,7 @@ amr_status dg_euler_advance(amr_tree* t, const DgStage& st, size_t steps, double
         cudaFree(t->dg_prims);
         t->dg_prims     = nullptr;
         t->dg_prims_cap = 0;
-        AMR_CUDA(cudaMalloc(&t->dg_prims, 12 * t->fstride() * sizeof(double)));
+        AMR_CUDA(cudaMalloc(&t->dg_prims, 14 * t->fstride() * sizeof(double)));
         t->dg_prims_cap = t->cap;
     }
     double* hp = static_cast<double*>(t->pinned);
