@@ -1984,11 +1984,18 @@ amr_status amr_tree_dg_set_equation(amr_tree* t, int equation)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
     if (equation != AMR_DG_ADVECTION && equation != AMR_DG_EULER) return fail(AMR_ERR_INVALID, "unknown DG equation");
-    if (equation == AMR_DG_EULER && !t->dg_scalars) {
-        AMR_CUDA(cudaMalloc(&t->dg_scalars, 2 * sizeof(double)));
-        AMR_CUDA(cudaMalloc(&t->dg_dtmin, sizeof(unsigned long long)));
-        const unsigned long long inf = 0x7ff0000000000000ull; // +inf: no patch seen
-        AMR_CUDA(cudaMemcpy(t->dg_dtmin, &inf, sizeof inf, cudaMemcpyHostToDevice));
+    if (equation == AMR_DG_EULER) {
+        if (!t->dg_scalars) AMR_CUDA(cudaMalloc(&t->dg_scalars, 2 * sizeof(double)));
+        if (!t->dg_dtmin) {
+            AMR_CUDA(cudaMalloc(&t->dg_dtmin, sizeof(unsigned long long)));
+            const unsigned long long inf = 0x7ff0000000000000ull; // +inf: no patch seen
+            if (const cudaError_t e = cudaMemcpy(t->dg_dtmin, &inf, sizeof inf, cudaMemcpyHostToDevice);
+                e != cudaSuccess) {
+                cudaFree(t->dg_dtmin);
+                t->dg_dtmin = nullptr;
+                return cuda_fail(e, "amr_tree_dg_set_equation");
+            }
+        }
     }
     t->dg_equation = equation;
     return AMR_OK;
