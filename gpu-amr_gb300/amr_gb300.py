@@ -377,7 +377,9 @@ class Tree:
 
     def dg_advance(self, steps, dt, time=0.0):
         """Nodal DG steps (order 2, 2D, 16 fields): returns (next step size,
-        time).  dt is the step size of the first step."""
+        time).  dt is the step size of the first step; as in the reference's
+        loop, each step first takes dt = min(dt, dt_min) and then adds that
+        updated dt to time."""
         d, t = C.c_double(dt), C.c_double(time)
         check(lib().amr_tree_dg_advance(self._h, steps, C.byref(d), C.byref(t)))
         return d.value, t.value

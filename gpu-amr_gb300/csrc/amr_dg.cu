@@ -405,10 +405,11 @@ __global__ void k_dg_euler_next(double* dt, double* time, unsigned long long* dt
 {
     const double h    = dt[0];
     const double m    = __longlong_as_double(static_cast<long long>(*dt_min));
-    const double dmin = m < h ? m : h; // dt_min starts at dt (solver.hpp:122)
-    time[0] += h;
-    dt[0]   = h < dmin ? h : dmin;     // dt = std::min(dt, dt_min)
-    *dt_min = 0x7ff0000000000000ull;   // +inf
+    const double dmin = m < h ? m : h;    // dt_min starts at dt (solver.hpp:127)
+    const double next = dmin < h ? dmin : h; // dt = std::min(dt, dt_min)
+    dt[0]             = next;
+    time[0] += next;                        // time += dt, the updated step (solver.hpp:129, 134)
+    *dt_min = 0x7ff0000000000000ull;        // +inf
 }
 
 // ------------------------------------------------ DG prolongation / restriction

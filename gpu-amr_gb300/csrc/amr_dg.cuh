@@ -50,8 +50,9 @@ cudaError_t dg_stage(const DgStage& s);
 //   each halo exchange by dg_euler_prims (corner ghosts left unset).
 //   dt: the step in use (device, [0]); in the last stage (mode 1) each patch
 //   folds 0.1 x edge / lambda into dt_min (ordered bit pattern of a positive
-//   double), and dg_euler_next takes dt = min(dt, min(dt, dt_min)), adds the
-//   step to time and resets dt_min.
+//   double), and dg_euler_next takes dt = min(dt, min(dt, dt_min)), adds
+//   that updated step to time (the reference's loop order) and resets
+//   dt_min.
 struct DgEulerStage {
     const double*       in;
     const double*       un;

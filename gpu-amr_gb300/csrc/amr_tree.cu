@@ -2095,8 +2095,8 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
         st.mode = 1;
         AMR_CUDA(dg_stage(st));
         launches += 4;
-        acc += h;
         h = std::min(h, std::min(h, dt_cfl));
+        acc += h; // the reference's loop adds the updated step (solver.hpp:129, 134)
     }
     g_launches.fetch_add(launches, std::memory_order_relaxed);
     t->ghosts_valid = true; // the ghosts the reference's tree holds after a step

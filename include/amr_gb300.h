@@ -304,7 +304,9 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
  * initial_dt for a new run), on return the next one; each step then takes
  * dt = min(dt, 0.1 x finest cell edge), the reference's CFL rule for this
  * order (1 / (order^dim + 1) x Courant x edge / |v|).  *time (optional)
- * accumulates the step sizes taken.  Interior states are bit-identical to
+ * then grows by that updated step size, as in the reference's loop
+ * (dt = min(dt, dt_min); time += dt: after k steps it has grown by the
+ * sizes of steps 2..k+1).  Interior states are bit-identical to
  * the reference's CPU path. */
 amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time);
 

@@ -18,6 +18,16 @@ def amr():
     return A
 
 
+def _loop_time(dts, next_dt):
+    """The time of the reference's DG loop (solver.hpp:125-134) after the
+    fixture's steps: each step first takes dt = min(dt, dt_min), then adds
+    that updated dt, so the sizes of steps 2..K and the next step's size."""
+    t = 0.0
+    for d in list(dts[2:]) + [next_dt]:
+        t += float(d)
+    return t
+
+
 def _dg_tree(amr, level):
     t = amr.Tree(2, 4, 1, 6, capacity=(1 << (2 * level)) + 64, dtype=amr.F64, fields=16)
     t.refine_uniform(level)
@@ -37,7 +47,7 @@ def test_gpu_dg_matches_reference(amr, name):
         assert dt == dts[k]
         dt, time = t.dg_advance(1, dt, time)
         np.testing.assert_array_equal(fields_to_leaves(t.download_state()), st[k])
-    assert time == pytest.approx(float(np.sum(dts)), rel=1e-15)
+    assert time == _loop_time(dts, dt)
 
 
 @pytest.mark.parametrize("level,steps", [(4, 12), (5, 6)])
@@ -134,6 +144,7 @@ def test_gpu_dg_euler_matches_reference(amr, name):
         dt, time = t.dg_advance(1, dt, time)
         np.testing.assert_array_equal(fields_to_leaves(t.download_state()), st[k])
     assert dts[2] < dts[1]
+    assert time == _loop_time(dts, dt)
 
 
 def test_gpu_dg_euler_remesh_matches_reference(amr):
@@ -169,7 +180,7 @@ def test_gpu_dg_euler_matches_oracle(amr):
     outs, dts = G.run(L, steps + 1, dt0=0.003, U=U0, equation="euler")
     np.testing.assert_array_equal(fields_to_leaves(t.download_state()), G.to_leaves(outs[steps - 1], L))
     assert dt == dts[steps]
-    assert time == ((((0.0 + dts[0]) + dts[1]) + dts[2]) + dts[3])
+    assert time == ((((0.0 + dts[1]) + dts[2]) + dts[3]) + dts[4])  # the updated steps, as the loop adds them
 
 
 def test_gpu_dg_set_equation_rejects_unknown(amr):
