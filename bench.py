@@ -864,7 +864,7 @@ def dg_extra(torch, A, stream, with_cpu=True):
 
 def dg_loop(torch, A, stream):
     """The reference's DG main loop (examples/dg_main_loop.e.cpp with
-    DGSolver::run, solver.hpp:117-147): uniform level 5, initial dt 0.01,
+    DGSolver::run, solver.hpp:109-151): uniform level 5, initial dt 0.01,
     re-mesh every 20 steps with thresholds 0.05 / 0.01, until t = 1; the
     reference's count of processed cells (leaves x 16 per step) over the wall
     time of the loop (host-driven: one call per step and per re-mesh)."""

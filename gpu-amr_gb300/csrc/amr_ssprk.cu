@@ -1,7 +1,7 @@
 // Strong-stability-preserving Runge-Kutta steps (SSPRK2, SSPRK3) of the FV
 // advection operator on the device tree: the reference's integrators
 // (include/dg_helpers/time_integration/time.hpp:83-272, driven per patch with
-// a halo exchange before every stage as include/dg_helpers/solver.hpp:159-232
+// a halo exchange before every stage as include/dg_helpers/solver.hpp:162-244
 // does) applied to the residual
 //     R = -sum_d (F_R - F_L) / dx_d
 // with the Rusanov flux of AdvectionPhysics (include/solver/

@@ -2004,7 +2004,7 @@ amr_status amr_tree_dg_set_equation(amr_tree* t, int equation)
 namespace
 {
 // DG Euler steps: the step size lives on the device, set per step from the
-// patches' wave speeds (solver.hpp:221-226), so the host reads it back once
+// patches' wave speeds (solver.hpp:227-234), so the host reads it back once
 // per call
 amr_status dg_euler_advance(amr_tree* t, const DgStage& st, size_t steps, double* dt, double* time)
 {
@@ -2074,7 +2074,7 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
     st.fstride = t->fstride();
     st.stream  = s;
     if (t->dg_equation == AMR_DG_EULER) return dg_euler_advance(t, st, steps, dt, time);
-    // CFL step of the finest cells (solver.hpp:221-226 with |v| = 1)
+    // CFL step of the finest cells (solver.hpp:227-234 with |v| = 1)
     const double edge   = (1.0 / static_cast<double>(1u << t->max_level_host)) / static_cast<double>(kDgPatch);
     const double scale  = 1.0 / (std::pow(static_cast<double>(kDgOrder), 2.0) + 1.0);
     const double dt_cfl = scale * 0.5 * edge / 1.0;
@@ -2132,7 +2132,7 @@ amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int 
         stats->cells += static_cast<uint64_t>(t->size) * kDgPatch * kDgPatch;
         if (amr_status st = amr_tree_dg_advance(t, 1, &dt, &time); st != AMR_OK) return st;
         ++step;
-        if (amr_interval > 0 && step >= next_amr) {
+        if (step >= next_amr) { // apply_amr (solver.hpp:249-251): an interval of 0 re-meshes every step
             int changed = 0;
             if (amr_status st = amr_tree_dg_remesh(t, refine_threshold, coarsen_threshold, &changed); st != AMR_OK)
                 return st;

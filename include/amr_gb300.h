@@ -274,7 +274,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_s
 /* Strong-stability-preserving Runge-Kutta steps of linear advection: the
  * reference's SSPRK2 / SSPRK3 integrators (include/dg_helpers/
  * time_integration/time.hpp:83-272, driven with a halo exchange before every
- * stage as include/dg_helpers/solver.hpp:159-232 does) on the FV residual
+ * stage as include/dg_helpers/solver.hpp:162-244 does) on the FV residual
  * -sum_d (F_R - F_L) / dx_d with the Rusanov flux of AdvectionPhysics.  The
  * step size is amr_tree_advance's (CFL from the finest level, clamped to the
  * remaining time); a one-field FP64 tree; velocity3 NULL = the per-instance
@@ -288,7 +288,7 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
 
 /* ------------------------------------------------------------- DG
  * Nodal discontinuous-Galerkin steps of the reference's DG patch solver
- * (include/dg_helpers: DGSolver::advance_patches, solver.hpp:159-232, with
+ * (include/dg_helpers: DGSolver::advance_patches, solver.hpp:162-244, with
  * RHSEvaluator::evaluate, rhs.hpp:117-255, and SSPRK2, time.hpp:134-168) in
  * its generated configuration (include/config/generated_config.hpp): order
  * 2, 2D, 4 x 4 cells per patch with one ghost cell, four advected variables
@@ -310,7 +310,7 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
  * the reference's CPU path. */
 amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time);
 
-/* DGSolver::apply_amr (solver.hpp:237-299) on such a tree:
+/* DGSolver::apply_amr (solver.hpp:249-310) on such a tree:
  * GradientAMRIndicator::compute_patch_decisions (include/dg_helpers/
  * globals/amr_indicators.hpp:86-225: per cell the largest nodal range of
  * variables 0..1 over |mean of variable 2| + 1e-10; refine if a cell exceeds
@@ -323,10 +323,11 @@ amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* ti
  * changed. */
 amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coarsen_threshold, int* changed);
 
-/* DGSolver::run (solver.hpp:117-147) without its VTK output: from time 0,
+/* DGSolver::run (solver.hpp:109-151) without its VTK output: from time 0,
  * step size initial_dt for the first step, steps while time < end_time,
  * after step k >= next (next = 0 at the start) a re-mesh and next = k +
- * amr_interval (0: no re-mesh).  stats: steps, re-meshes, the reference's
+ * amr_interval (0: a re-mesh after every step, as in the reference).
+ * stats: steps, re-meshes, the reference's
  * processed-cell count (leaves x 16 per step), final time and next step
  * size, largest leaf count. */
 typedef struct amr_dg_stats {
@@ -345,7 +346,7 @@ amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int 
  * of a face is the patch's running maximum, in the reference's loop order,
  * of max(eigenvalue of the cell, of the neighbour) (|u_n| + sqrt(gamma p /
  * rho) at the cell's first node), and each step's CFL step comes from every
- * patch's final speed (0.1 x edge / lambda, solver.hpp:221-226), computed on
+ * patch's final speed (0.1 x edge / lambda, solver.hpp:227-234), computed on
  * the device: amr_tree_dg_advance reads the step size back once per call.
  * amr_tree_dg_advance, amr_tree_dg_remesh and amr_tree_dg_run apply the
  * setting; states are bit-identical to the reference's CPU path. */

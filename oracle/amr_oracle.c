@@ -1017,7 +1017,7 @@ double oracle_advance(oracle_tree* t, size_t steps, const double* v, double cfl,
 /* ---------------------------------------------------------------- SSPRK */
 /* The strong-stability-preserving Runge-Kutta integrators of the reference
  * (include/dg_helpers/time_integration/time.hpp:83-272, used there per
- * patch with a halo exchange before every stage, solver.hpp:159-232) applied
+ * patch with a halo exchange before every stage, solver.hpp:162-244) applied
  * to the FV advection operator: the residual of a stage is
  *   R = -sum_d (F_R - F_L) / dx_d
  * with the Rusanov flux of AdvectionPhysics (as in time_step), and the
@@ -1029,7 +1029,7 @@ double oracle_advance(oracle_tree* t, size_t steps, const double* v, double cfl,
  * mode: 0, 2, 31, 32 for the four forms.  Like the reference, which
  * combines whole padded containers, every cell of `out` is written (the
  * ghost cells with R = 0), and no halo exchange follows the last stage: the
- * next step starts with one (solver.hpp:170), and a criterion evaluated
+ * next step starts with one (solver.hpp:174), and a criterion evaluated
  * between steps sees the combined ghosts, as in the reference. */
 static void ssprk_stage(const oracle_tree* t, const double* v, double dt, int mode, const double* in,
                         const double* un, double* out)

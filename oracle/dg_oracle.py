@@ -16,7 +16,7 @@ Reference (paths within the reference project):
   RHS            include/dg_helpers/rhs.hpp:117-255 with volume.hpp:24-44 and
                  surface.hpp:36-113 (Rusanov flux, surface mass, lift)
   stages         include/dg_helpers/time_integration/time.hpp:134-168 (SSPRK2)
-  step loop      include/dg_helpers/solver.hpp:117-232 (dt = initial dt for the
+  step loop      include/dg_helpers/solver.hpp:109-244 (dt = initial dt for the
                  first step, then min(dt, 0.1 x cell edge / |v| ...))
 
 Each elementwise operation is evaluated in the reference's order and

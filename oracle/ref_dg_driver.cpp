@@ -22,7 +22,7 @@
 //                  patch, the CFL step from the last stage's largest
 //                  eigenvalue, finish_step; the loop's step size rule
 //                  dt = min(dt, dt_min) with dt = initial_dt at the start
-//                  (solver.hpp:117-128);
+//                  (solver.hpp:125-134);
 //   re-mesh        with amr=<interval> > 0, DGSolver::apply_amr (solver.hpp:
 //                  237-299) after each step from step 1 on, every interval
 //                  steps: GradientAMRIndicator::compute_patch_decisions

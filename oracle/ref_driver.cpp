@@ -29,7 +29,7 @@
 //                       the FV advection residual -sum_d (F_R - F_L)/dx_d
 //                       (RuntimeAdvection's Rusanov flux) patch by patch, with
 //                       a halo exchange before every stage as the DG solver
-//                       does (include/dg_helpers/solver.hpp:159-232); CFL step
+//                       does (include/dg_helpers/solver.hpp:162-244); CFL step
 //                       as compute_time_step_cpu; gradient re-mesh as in run.
 //   vtk=<name>          - after the mode, the reference's VTK writer
 //                       (include/ndtree/vtk_print.hpp) prints the tree to
