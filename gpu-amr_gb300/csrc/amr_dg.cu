@@ -187,8 +187,8 @@ k_dg_stage(const double* __restrict__ in, const double* un, double* out, const u
 // ------------------------------------------------ DG Euler
 constexpr double kDgGamma = 1.4;
 
-// compute_pressure and compute_velocity (euler.hpp:57-87) of one node;
-// max_eigenvalue (euler.hpp:149-163) is |m_n / rho| + sqrt(gamma p / rho)
+// compute_pressure and compute_velocity (euler.hpp:69-113) of one node;
+// max_eigenvalue (euler.hpp:165-181) is |m_n / rho| + sqrt(gamma p / rho)
 // at a cell's first node
 __device__ __forceinline__ void dg_euler_node(double mx, double my, double rho, double E, double& p, double& u,
                                               double& v)
@@ -234,7 +234,7 @@ k_dg_euler_prims(const double* __restrict__ in, double* __restrict__ prims, long
 }
 
 // flux component adim (0: x, 1: y) of variable var at one node (evaluate_flux,
-// euler.hpp:109-143): rho u_i u_d (+ p if i = d), rho u_d, (E + p) u_d
+// euler.hpp:120-160): rho u_i u_d (+ p if i = d), rho u_d, (E + p) u_d
 __device__ __forceinline__ double dg_euler_flux(const double* U, const double* pr, size_t fstride, int node, int var,
                                                 int adim)
 {

@@ -108,11 +108,11 @@ def initial_state(level, t=0.0):
     return U
 
 
-GAMMA = 1.4  # the Euler equation's default heat capacity ratio (euler.hpp:31)
+GAMMA = 1.4  # the Euler equation's default heat capacity ratio (euler.hpp:38)
 
 
 def euler_pressure(U):
-    """compute_pressure (euler.hpp:57-69) per node: variables [mx, my, rho, E]."""
+    """compute_pressure (euler.hpp:69-82) per node: variables [mx, my, rho, E]."""
     rho, E = U[..., 2], U[..., 3]
     kin = 0.0
     for d in range(2):
@@ -121,7 +121,7 @@ def euler_pressure(U):
 
 
 def euler_flux(U):
-    """evaluate_flux (euler.hpp:109-143): [F_x, F_y] per node."""
+    """evaluate_flux (euler.hpp:120-160): [F_x, F_y] per node."""
     rho, E = U[..., 2], U[..., 3]
     p = euler_pressure(U)
     out = []
@@ -139,7 +139,7 @@ def euler_flux(U):
 
 
 def euler_eig(U, normal):
-    """max_eigenvalue (euler.hpp:149-163): from the cell's first node only,
+    """max_eigenvalue (euler.hpp:165-181): from the cell's first node only,
     |u_n| + sqrt(gamma p / rho)."""
     U0 = U[..., 0, 0, :]
     rho = U0[..., 2]
@@ -149,7 +149,7 @@ def euler_eig(U, normal):
 
 
 def euler_initial_state(level):
-    """EulerInitialCondition<2> (euler.hpp:210-233) at the nodes: pressure
+    """EulerInitialCondition<2> (euler.hpp:227-253) at the nodes: pressure
     pulse exp(-100 r^2) + 1, rho 1, zero momentum."""
     C = PATCH << level
     cell = (1.0 / float(1 << level)) / float(PATCH)

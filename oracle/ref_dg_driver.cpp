@@ -11,11 +11,11 @@
 // 4x4 cells per patch, one ghost cell, SSPRK2, advection with velocity 1).
 // What the driver does, in the reference's own calls:
 //   tree           the TreeBuilder's ndtree type (include/dg_helpers/
-//                  tree_builder.hpp:359-370) with a small capacity (the
+//                  tree_builder.hpp:399-403) with a small capacity (the
 //                  builder itself allocates 500000 leaves), refined
 //                  uniformly with reconstruct_tree;
 //   initial state  GlobalConfig::compute_center and interpolate_initial_dofs
-//                  per interior cell (tree_builder.hpp:396-431);
+//                  per interior cell (tree_builder.hpp:407-466);
 //   one step       DGSolver::advance_patches (include/dg_helpers/solver.hpp:
 //                  159-232): halo exchange, begin_step, per stage a halo
 //                  exchange and RHSEvaluator::evaluate + the SSPRK2 stage per
@@ -26,7 +26,7 @@
 //   re-mesh        with amr=<interval> > 0, DGSolver::apply_amr (solver.hpp:
 //                  237-299) after each step from step 1 on, every interval
 //                  steps: GradientAMRIndicator::compute_patch_decisions
-//                  (include/dg_helpers/globals/amr_indicators.hpp:158-225) with
+//                  (include/dg_helpers/globals/amr_indicators.hpp:169-224) with
 //                  thresholds rthr / cthr, reconstruct_tree with those
 //                  decisions (the tree's DefaultAMRPolicy prolongation and
 //                  restriction), halo exchange.
