@@ -30,8 +30,16 @@
 //                  thresholds rthr / cthr, reconstruct_tree with those
 //                  decisions (the tree's DefaultAMRPolicy prolongation and
 //                  restriction), halo exchange.
+//   main loop      with end=<T> > 0 instead: DGSolver::run's loop (solver.hpp:
+//                  109-151, without its VTK output) from time 0 while time < T:
+//                  a step, dt = min(dt, dt_min), time += dt (the updated
+//                  step), a re-mesh when the step count reaches the next
+//                  re-mesh step, which then moves amr steps on; one dump of
+//                  the final tree (step = steps run, dt = the next step size)
+//                  and a line "steps remeshes cells leaves_max time next_dt"
+//                  on stdout.
 // Usage: ref_dg_driver level=<L> steps=<K> dt0=<initial dt> [amr=<interval>
-//        rthr=<refine> cthr=<coarsen>] out=<file>
+//        rthr=<refine> cthr=<coarsen>] [end=<T>] out=<file>
 // Records: "DGS1" header, then per dump: step (u32), dt (f64), leaves
 // (u64), ids (u64 x leaves), interior nodal values (f64 x leaves x 16 cells
 // x 4 nodes x 4 variables, cells row-major with x fastest, nodes with the
@@ -209,6 +217,44 @@ int main(int argc, char** argv)
     int                         next_amr = 0;
     using indicator_t = amr::global::GradientAMRIndicator<global_t, policy_t>;
     using status_t    = tree_t::refine_status_t;
+    auto remesh       = [&]() {
+        const auto decisions = indicator_t::template compute_patch_decisions<tree_t, S1>(tree, thr);
+        std::unordered_map<patch_index_t, status_t> by_id;
+        for (std::size_t i = 0; i < decisions.size(); ++i) by_id[tree.get_node_index_at(i)] = decisions[i];
+        tree.reconstruct_tree([&by_id](const patch_index_t& pid) -> status_t {
+            auto it = by_id.find(pid);
+            return it != by_id.end() ? it->second : status_t::Stable;
+        });
+        tree.halo_exchange_update();
+    };
+    const double end = argf(argc, argv, "end", 0.0);
+    if (end > 0.0)
+    {
+        double        time = 0.0;
+        std::uint64_t k = 0, remeshes = 0, cells = 0, leaves_max = tree.size();
+        while (time < end)
+        {
+            double dt_min = dt;
+            step(tree, dt, dt_min);
+            dt = std::min(dt, dt_min);
+            cells += tree.size() * 16;
+            time += dt;
+            ++k;
+            if (static_cast<long>(k) >= next_amr)
+            {
+                remesh();
+                ++remeshes;
+                next_amr   = static_cast<int>(k) + amr_every;
+                leaves_max = std::max<std::uint64_t>(leaves_max, tree.size());
+            }
+        }
+        dump(f, tree, static_cast<std::uint32_t>(k), dt);
+        std::fclose(f);
+        std::printf("%llu %llu %llu %llu %.17g %.17g\n", static_cast<unsigned long long>(k),
+                    static_cast<unsigned long long>(remeshes), static_cast<unsigned long long>(cells),
+                    static_cast<unsigned long long>(leaves_max), time, dt);
+        return 0;
+    }
     for (int k = 1; k <= steps; ++k)
     {
         double dt_min = dt;
@@ -217,14 +263,7 @@ int main(int argc, char** argv)
         dt                = std::min(dt, dt_min);
         if (amr_every > 0 && k >= next_amr)
         {
-            const auto decisions = indicator_t::template compute_patch_decisions<tree_t, S1>(tree, thr);
-            std::unordered_map<patch_index_t, status_t> by_id;
-            for (std::size_t i = 0; i < decisions.size(); ++i) by_id[tree.get_node_index_at(i)] = decisions[i];
-            tree.reconstruct_tree([&by_id](const patch_index_t& pid) -> status_t {
-                auto it = by_id.find(pid);
-                return it != by_id.end() ? it->second : status_t::Stable;
-            });
-            tree.halo_exchange_update();
+            remesh();
             next_amr = k + amr_every;
         }
         dump(f, tree, static_cast<std::uint32_t>(k), used);

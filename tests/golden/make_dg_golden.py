@@ -12,6 +12,10 @@ records each scenario as a compressed .npz:
   dt             [dump] step size used to reach each dump (0 for dump 0)
   with re-mesh:  ids_k / state_k per dump k (the leaf count changes), and
                  amr (interval), rthr, cthr
+  main loop:     dg_main_loop.npz, the reference's DGSolver::run loop to
+                 t = 1 (the example's configuration): the final leaves,
+                 the SHA-256 of the final interior state ([leaf, cell, node,
+                 variable] little-endian float64) and the loop's counts
 
 Usage:  python tests/golden/make_dg_golden.py
 """
@@ -45,6 +49,59 @@ SCENARIOS = {
     # then refinement along the density front (136, 388 leaves)
     "dg_euler_amr_l3": (3, 5, 0.002, 2, 0.002, 0.0005, "euler"),
 }
+
+
+# the reference's DG main loop: level, initial dt, re-mesh interval,
+# thresholds, end time
+MAIN_LOOP = (5, 0.01, 20, 0.05, 0.01, 1.0)
+
+
+def main_loop():
+    """Run DGSolver::run's loop (CPU, about ten minutes) and record it.  The
+    run starts from the reference's initial state, which the numpy
+    restatement reproduces bit for bit at this level (checked here), so a
+    test can start from the restatement's."""
+    import hashlib
+    import sys
+
+    sys.path.insert(0, str(REPO))
+    from oracle import dg_oracle as G
+
+    level, dt0, amr, rthr, cthr, end = MAIN_LOOP
+    init = Path("/tmp") / "dg_main_loop_init.bin"
+    subprocess.run([str(DRIVERS["advection"]), f"level={level}", "steps=0", "capacity=8192", f"out={init}"],
+                   check=True)
+    _, st0, _ = read_dumps(init)
+    assert np.array_equal(G.to_leaves(G.initial_state(level), level), st0[0])
+    out = Path("/tmp") / "dg_main_loop.bin"
+    r = subprocess.run([str(DRIVERS["advection"]), f"level={level}", f"dt0={dt0}", f"amr={amr}", f"rthr={rthr}",
+                        f"cthr={cthr}", f"end={end}", "capacity=8192", f"out={out}"],
+                       check=True, capture_output=True, text=True)
+    steps, remeshes, cells, leaves_max, time, next_dt = r.stdout.split()
+    idss, states, _ = read_dumps_any(out)
+    digest = hashlib.sha256(np.ascontiguousarray(states[0], dtype="<f8").tobytes()).hexdigest()
+    np.savez_compressed(HERE / "dg_main_loop.npz", ids=idss[0], state_sha256=digest, level=level, dt0=dt0, amr=amr,
+                        rthr=rthr, cthr=cthr, end=end, steps=int(steps), remeshes=int(remeshes), cells=int(cells),
+                        leaves_max=int(leaves_max), time=float(time), next_dt=float(next_dt),
+                        state_sum=float(states[0].sum()))
+    print("dg_main_loop", steps, remeshes, cells, leaves_max, time, next_dt, len(idss[0]))
+
+
+def read_dumps_any(path: Path):
+    """The dumps of a file whose first record may carry any step number."""
+    b = path.read_bytes()
+    assert b[:4] == b"DGS1"
+    o = 4
+    idss, states = [], []
+    while o < len(b):
+        o += 12
+        P, = struct.unpack_from("<Q", b, o)
+        o += 8
+        idss.append(np.frombuffer(b, np.uint64, P, o).copy())
+        o += 8 * P
+        states.append(np.frombuffer(b, np.float64, P * 256, o).reshape(P, 16, 4, 4).copy())
+        o += 8 * P * 256
+    return idss, states, None
 
 
 def read_dumps(path: Path):
@@ -86,6 +143,7 @@ def main():
             np.savez_compressed(HERE / f"{name}.npz", dt=dts, level=level, amr=amr, rthr=rthr, cthr=cthr,
                                 steps=steps, equation=eq, **extra)
         print(name, [len(i) for i in idss], dts)
+    main_loop()
 
 
 if __name__ == "__main__":

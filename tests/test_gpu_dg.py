@@ -1,6 +1,8 @@
 """The CUDA DG path (amr_tree_dg_advance) against the reference's DG patch
 solver (golden fixtures, bit for bit) and against the numpy restatement on
 larger uniform trees; argument checks."""
+import hashlib
+
 import numpy as np
 import pytest
 
@@ -187,3 +189,25 @@ def test_gpu_dg_set_equation_rejects_unknown(amr):
     t = _dg_tree(amr, 1)
     with pytest.raises(amr.AmrError):
         amr.check(amr.lib().amr_tree_dg_set_equation(t._h, 7))
+
+
+def test_gpu_dg_run_matches_the_reference_main_loop(amr):
+    """amr_tree_dg_run against the reference's whole DG main loop
+    (DGSolver::run to t = 1 from a uniform level-5 start, re-mesh every 20
+    steps, thresholds 0.05 / 0.01; run on the CPU by the reference's own
+    code): the step and re-mesh counts, processed cells, largest leaf count,
+    final time and next step size, the final leaves, and the final interior
+    state bit for bit (its SHA-256)."""
+    z = load("dg_main_loop")
+    L = int(z["level"])
+    t = amr.Tree(2, 4, 1, 6, capacity=8192, dtype=amr.F64, fields=16)
+    t.refine_uniform(L)
+    t.upload_state(leaves_to_fields(G.to_leaves(G.initial_state(L), L)))
+    st = t.dg_run(float(z["dt0"]), float(z["end"]), int(z["amr"]), float(z["rthr"]), float(z["cthr"]))
+    assert (st["steps"], st["remeshes"], st["cells"], st["leaves_max"]) == (
+        int(z["steps"]), int(z["remeshes"]), int(z["cells"]), int(z["leaves_max"]))
+    assert st["time"] == float(z["time"]) and st["next_dt"] == float(z["next_dt"])
+    np.testing.assert_array_equal(t.ids(), z["ids"])
+    final = np.ascontiguousarray(fields_to_leaves(t.download_state()), dtype="<f8")
+    assert final.sum() == float(z["state_sum"])
+    assert hashlib.sha256(final.tobytes()).hexdigest() == str(z["state_sha256"])

@@ -52,3 +52,20 @@ def test_dg_oracle_advects_a_constant_unchanged():
     U = np.ones((8, 8, 2, 2, 4))
     R = G.rhs(U, 1.0 / 8)
     assert np.all(np.abs(R) < 1e-12)
+
+
+def test_dg_main_loop_fixture_is_consistent():
+    """The reference main-loop record: the loop stopped at the first time
+    >= end (time grows by the updated step), re-meshed after step 1 and then
+    every `amr` steps, and its final leaves are sorted, unique Morton ids of
+    levels 1..6 whose cells make up the unit square."""
+    z = load("dg_main_loop")
+    end, every, steps = float(z["end"]), int(z["amr"]), int(z["steps"])
+    assert z["time"] >= end and z["time"] - z["next_dt"] < end
+    assert int(z["remeshes"]) == 1 + (steps - 1) // every
+    ids = z["ids"]
+    assert np.all(ids[1:] > ids[:-1]) and len(ids) <= int(z["leaves_max"])
+    levels = (ids & np.uint64(63)).astype(int)
+    assert levels.min() >= 1 and levels.max() <= 6
+    assert np.sum(4.0 ** -levels) == 1.0
+    assert int(z["cells"]) % 16 == 0 and 16 * steps <= int(z["cells"]) <= 16 * int(z["leaves_max"]) * steps
