@@ -328,3 +328,90 @@ def from_leaves(L, level):
     for n, (py, px) in enumerate(morton_patch_order(level)):
         U[py * P:(py + 1) * P, px * P:(px + 1) * P] = L[n].reshape(P, P, ORDER, ORDER, NVAR)
     return U
+
+
+# ---------------------------------------------------------------- printer
+MAX_DEPTH = 6  # morton_id<MaxDepth = 6, 2> of the DG tree (generated_config.hpp:32)
+
+
+def _lagrange_quad_index(i, j, order):
+    """point_idx_lagrange_quad (print_dg_tree_v2.hpp:61-97): VTK Lagrange
+    quadrilateral point order (corners, edges, face)."""
+    ib, jb = i in (0, order), j in (0, order)
+    if ib and jb:
+        return (2 if j > 0 else 1) if i > 0 else (3 if j > 0 else 0)
+    if not ib and jb:
+        return (i - 1) + (2 * (order - 1) if j > 0 else 0) + 4
+    if ib and not jb:
+        return (j - 1) + ((order - 1) if i > 0 else 3 * (order - 1)) + 4
+    return 4 + 4 * (order - 1) + (i - 1) + (order - 1) * (j - 1)
+
+
+def _decode(ids):
+    """Patch origin of Morton ids (interleave << 6 | level) on the finest
+    grid (2^MAX_DEPTH cells per axis): x from the even bits, y from the odd."""
+    m = ids.astype(np.uint64) >> np.uint64(6)
+    x = np.zeros(len(ids), np.int64)
+    y = np.zeros(len(ids), np.int64)
+    for b in range(MAX_DEPTH):
+        x |= ((m >> np.uint64(2 * b)) & np.uint64(1)).astype(np.int64) << b
+        y |= ((m >> np.uint64(2 * b + 1)) & np.uint64(1)).astype(np.int64) << b
+    return x, y, (ids & np.uint64(63)).astype(np.int64)
+
+
+def dg_vtk_bytes(ids, leaves):
+    """dg_tree_printer_2d::print (print_dg_tree_v2.hpp:145-370) as bytes:
+    every interior cell becomes a VTK Lagrange quadrilateral (type 70) with
+    its polynomial (Basis::evaluate_basis, polynomial.hpp:36-55) evaluated at
+    the (order + 1)^2 points xi, eta in {0, 1/2, 1}; legacy binary,
+    big-endian.  ids: Morton ids in leaf order; leaves: [leaf, cell
+    (row-major, x fastest), node (x-node * 2 + y-node), variable]."""
+    T = tables()
+    p = T["points"]
+    lag = lambda i, x: (1.0 * (x - p[1 - i])) / (1.0 * (p[i] - p[1 - i]))  # Lagrange::evaluate
+    P = len(ids)
+    px, py, lv = _decode(np.asarray(ids, np.uint64))
+    norm = float(1 << MAX_DEPTH)
+    pts, vals, conn = [], [], []
+    for n in range(P):
+        csg = float(1 << (MAX_DEPTH - int(lv[n]))) / float(PATCH)
+        for ly in range(PATCH):
+            for lx in range(PATCH):
+                cx = (float(px[n]) + (float(lx) + 0.5) * csg) / norm
+                cy = (float(py[n]) + (float(ly) + 0.5) * csg) / norm
+                h = csg / norm
+                C = leaves[n, ly * PATCH + lx].reshape(ORDER, ORDER, NVAR)
+                c = [0] * 9
+                for jj in range(3):
+                    for ii in range(3):
+                        xi, eta = float(ii) / 2.0, float(jj) / 2.0
+                        c[_lagrange_quad_index(ii, jj, 2)] = len(pts)
+                        pts.append((cx + (2.0 * xi - 1.0) * (0.5 * h), cy + (2.0 * eta - 1.0) * (0.5 * h), 0.0))
+                        s = np.zeros(NVAR)
+                        for i0 in range(ORDER):
+                            for i1 in range(ORDER):
+                                prod = 1.0
+                                prod *= lag(i0, xi)
+                                prod *= lag(i1, eta)
+                                s = s + C[i0, i1] * prod
+                        vals.append(s)
+                conn.append(c)
+    out = [b"# vtk DataFile Version 3.0\nDG 2D Printer (Order=2)\nBINARY\nDATASET UNSTRUCTURED_GRID\n"]
+    out.append(f"POINTS {len(pts)} double\n".encode())
+    out.append(np.array(pts, ">f8").reshape(-1, 3).tobytes())
+    ncell = len(conn)
+    out.append(f"CELLS {ncell} {ncell * 10}\n".encode())
+    cells = np.empty((ncell, 10), ">i4")
+    cells[:, 0] = 9
+    if ncell:
+        cells[:, 1:] = np.array(conn)
+    out.append(cells.tobytes())
+    out.append(f"CELL_TYPES {ncell}\n".encode())
+    out.append(np.full(ncell, 70, ">i4").tobytes())
+    if pts:
+        V = np.array(vals)
+        out.append(f"POINT_DATA {len(pts)}\n".encode())
+        for comp in range(NVAR):
+            out.append(f"SCALARS dof_component_{comp} double 1\nLOOKUP_TABLE default\n".encode())
+            out.append(V[:, comp].astype(">f8").tobytes())
+    return b"".join(out)

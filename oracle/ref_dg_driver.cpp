@@ -38,8 +38,12 @@
 //                  the final tree (step = steps run, dt = the next step size)
 //                  and a line "steps remeshes cells leaves_max time next_dt"
 //                  on stdout.
+//   printer        with vtk=<file>: the final tree through the reference's DG
+//                  printer (ndt::print::dg_tree_printer_2d, include/ndtree/
+//                  print_dg_tree_v2.hpp; it writes under ./vtk_output, which
+//                  it clears), the file then moved to <file>.
 // Usage: ref_dg_driver level=<L> steps=<K> dt0=<initial dt> [amr=<interval>
-//        rthr=<refine> cthr=<coarsen>] [end=<T>] out=<file>
+//        rthr=<refine> cthr=<coarsen>] [end=<T>] [vtk=<file>] out=<file>
 // Records: "DGS1" header, then per dump: step (u32), dt (f64), leaves
 // (u64), ids (u64 x leaves), interior nodal values (f64 x leaves x 16 cells
 // x 4 nodes x 4 variables, cells row-major with x fastest, nodes with the
@@ -50,12 +54,14 @@
 #include "dg_helpers/rhs.hpp"
 #include "dg_helpers/time_integration/time_integration.hpp"
 #include "dg_helpers/tree_builder.hpp"
+#include "ndtree/print_dg_tree_v2.hpp"
 
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <limits>
 #include <string>
 #include <unordered_map>
@@ -227,6 +233,17 @@ int main(int argc, char** argv)
         });
         tree.halo_exchange_update();
     };
+    const std::string vtk = args(argc, argv, "vtk", "");
+    auto print_vtk        = [&]() {
+        if (vtk.empty()) return;
+        ::ndt::print::dg_tree_printer_2d<global_t, policy_t> printer("dg");
+        printer.template print<S1>(tree, "_final.vtk");
+        for (const auto& e : std::filesystem::directory_iterator("vtk_output"))
+        {
+            std::filesystem::copy_file(e.path(), vtk, std::filesystem::copy_options::overwrite_existing);
+            std::filesystem::remove(e.path());
+        }
+    };
     const double end = argf(argc, argv, "end", 0.0);
     if (end > 0.0)
     {
@@ -250,6 +267,7 @@ int main(int argc, char** argv)
         }
         dump(f, tree, static_cast<std::uint32_t>(k), dt);
         std::fclose(f);
+        print_vtk();
         std::printf("%llu %llu %llu %llu %.17g %.17g\n", static_cast<unsigned long long>(k),
                     static_cast<unsigned long long>(remeshes), static_cast<unsigned long long>(cells),
                     static_cast<unsigned long long>(leaves_max), time, dt);
@@ -269,5 +287,6 @@ int main(int argc, char** argv)
         dump(f, tree, static_cast<std::uint32_t>(k), used);
     }
     std::fclose(f);
+    print_vtk();
     return 0;
 }

@@ -31,3 +31,18 @@ def fields_to_leaves(a):
     P = a.shape[1]
     inner = a[:, :, 1:PATCH + 1, 1:PATCH + 1].reshape(4, 4, P, PATCH, PATCH)  # node, var, leaf, ly, lx
     return inner.transpose(2, 3, 4, 0, 1).reshape(P, PATCH * PATCH, 4, 4)
+
+
+def fixture_tree(name, dump):
+    """(Morton ids, [leaf, cell, node, var] state) of dump `dump` of a DG
+    fixture (uniform fixtures keep one id list, re-mesh fixtures one per dump)."""
+    z = load(name)
+    if "state" in z:
+        return z["ids"], z["state"][dump]
+    return z[f"ids_{dump}"], z[f"state_{dump}"]
+
+
+def printer_cases():
+    import json
+
+    return json.loads((GOLDEN / "dg_vtk.json").read_text())

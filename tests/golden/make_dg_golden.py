@@ -87,6 +87,37 @@ def main_loop():
     print("dg_main_loop", steps, remeshes, cells, leaves_max, time, next_dt, len(idss[0]))
 
 
+# the reference's DG printer on fixture trees: name -> (fixture, dump, driver,
+# driver arguments reproducing that dump as the final tree)
+PRINTS = {
+    "dg_vtk_l2": ("dg_advection_l2", 0, "advection", ["level=2", "steps=0"]),
+    "dg_vtk_amr_l3": ("dg_amr_l3", 4, "advection",
+                      ["level=3", "steps=4", "dt0=0.01", "amr=2", "rthr=0.05", "cthr=0.01"]),
+    "dg_vtk_euler_amr_l3": ("dg_euler_amr_l3", 5, "euler",
+                            ["level=3", "steps=5", "dt0=0.002", "amr=2", "rthr=0.002", "cthr=0.0005"]),
+}
+
+
+def printer_golden():
+    """SHA-256 and length of the reference printer's file for each PRINTS
+    entry (dg_vtk.json); the driver runs in a scratch folder because the
+    printer clears ./vtk_output."""
+    import hashlib
+    import json
+
+    work = Path("/tmp") / "dg_vtk_golden"
+    work.mkdir(exist_ok=True)
+    rec = {}
+    for name, (fixture, dump, eq, dargs) in PRINTS.items():
+        vtk = work / f"{name}.vtk"
+        subprocess.run([str(DRIVERS[eq]), *dargs, "capacity=8000", f"out={work / 'dump.bin'}", f"vtk={vtk}"],
+                       check=True, cwd=work)
+        b = vtk.read_bytes()
+        rec[name] = {"fixture": fixture, "dump": dump, "sha256": hashlib.sha256(b).hexdigest(), "bytes": len(b)}
+    (HERE / "dg_vtk.json").write_text(json.dumps(rec, indent=1) + "\n")
+    print("dg_vtk", {k: v["bytes"] for k, v in rec.items()})
+
+
 def read_dumps_any(path: Path):
     """The dumps of a file whose first record may carry any step number."""
     b = path.read_bytes()
@@ -143,6 +174,7 @@ def main():
             np.savez_compressed(HERE / f"{name}.npz", dt=dts, level=level, amr=amr, rthr=rthr, cthr=cthr,
                                 steps=steps, equation=eq, **extra)
         print(name, [len(i) for i in idss], dts)
+    printer_golden()
     main_loop()
 
 
