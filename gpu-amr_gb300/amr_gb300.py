@@ -131,6 +131,7 @@ def lib():
         L.amr_tree_dg_remesh.argtypes = [vp, dbl, dbl, C.POINTER(i32)]
         L.amr_tree_dg_run.argtypes = [vp, dbl, dbl, i32, dbl, dbl, C.POINTER(DgStats)]
         L.amr_tree_dg_set_equation.argtypes = [vp, i32]
+        L.amr_tree_dg_write_vtk.argtypes = [vp, C.c_char_p]
         L.amr_tree_euler_run.argtypes = [vp, C.POINTER(EulerParams), C.POINTER(CycleStats)]
         L.amr_tree_capacity.argtypes = [vp, C.POINTER(sz)]
         L.amr_adjoint_create.argtypes = [vp, sz, vp, dbl, dbl, sz, C.POINTER(vp)]
@@ -374,6 +375,11 @@ class Tree:
         if isinstance(equation, str):
             equation = {"advection": DG_ADVECTION, "euler": DG_EULER}[equation]
         check(lib().amr_tree_dg_set_equation(self._h, equation))
+
+    def dg_write_vtk(self, path):
+        """The reference's DG printer (VTK Lagrange quadrilaterals, the
+        cells' polynomials at 9 points each) for the current state."""
+        check(lib().amr_tree_dg_write_vtk(self._h, str(path).encode()))
 
     def dg_advance(self, steps, dt, time=0.0):
         """Nodal DG steps (order 2, 2D, 16 fields): returns (next step size,

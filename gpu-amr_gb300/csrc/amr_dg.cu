@@ -16,7 +16,10 @@
 //            times the face area, the surface weights, lifted back with the
 //            face kernel and subtracted
 //   mass     du * (4 / edge^2)
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <string>
 
 #include "amr_dg.cuh"
 
@@ -695,6 +698,181 @@ cudaError_t dg_stage(const DgStage& s)
     const unsigned  grid  = static_cast<unsigned>(std::min<long long>((total + 63) / 64, 152LL * 32));
     k_dg_stage<<<grid, 64, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.fstride, tb, s.dt, s.mode);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------ DG printer
+// dg_tree_printer_2d (include/ndtree/print_dg_tree_v2.hpp:145-370): every
+// interior cell is a VTK Lagrange quadrilateral whose (order + 1)^2 = 9
+// points (xi, eta in {0, 1/2, 1}, eta slowest) carry the cell's polynomial
+// evaluated there.  One thread per cell and section, big-endian output.
+namespace {
+
+__device__ __forceinline__ void dgv_be32(unsigned char* d, uint32_t v)
+{
+    *reinterpret_cast<uint32_t*>(d) = __byte_perm(v, 0, 0x0123);
+}
+__device__ __forceinline__ void dgv_be64(unsigned char* d, double v)
+{
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    dgv_be32(d, static_cast<uint32_t>(b >> 32));
+    dgv_be32(d + 4, static_cast<uint32_t>(b));
+}
+
+// centre and edge of interior cell `cell` on the unit square (the printer's
+// finest-grid arithmetic: the patch origin in finest cells, cell size
+// 2^(depth - level) / 4, divided by 2^depth)
+__device__ __forceinline__ void dgv_cell(const uint64_t* keys, const Geo& g, long long cell, int& p, int& lx, int& ly,
+                                         double& cx, double& cy, double& h)
+{
+    p  = static_cast<int>(cell >> 4);
+    lx = static_cast<int>(cell & 3);
+    ly = static_cast<int>((cell >> 2) & 3);
+    uint32_t c[3];
+    key_decode(g, keys[p], c);
+    const int    lev  = key_level(keys[p]);
+    const double csg  = static_cast<double>(1u << (g.depth - lev)) / static_cast<double>(kDgPatch);
+    const double norm = static_cast<double>(1u << g.depth);
+    cx                = (static_cast<double>(c[0]) + (static_cast<double>(lx) + 0.5) * csg) / norm;
+    cy                = (static_cast<double>(c[1]) + (static_cast<double>(ly) + 0.5) * csg) / norm;
+    h                 = csg / norm;
+}
+
+// POINTS: 9 x (x, y, 0) per cell
+__global__ void k_dgvtk_points(const uint64_t* __restrict__ keys, Geo g, long long first, long long count,
+                               unsigned char* __restrict__ out)
+{
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int    p, lx, ly;
+        double cx, cy, h;
+        dgv_cell(keys, g, first + i, p, lx, ly, cx, cy, h);
+        unsigned char* d = out + i * 9 * 24;
+        for (int jj = 0; jj < 3; ++jj)
+            for (int ii = 0; ii < 3; ++ii) {
+                const double xi = static_cast<double>(ii) / 2.0, eta = static_cast<double>(jj) / 2.0;
+                const double x  = cx + (2.0 * xi - 1.0) * (0.5 * h);
+                const double y  = cy + (2.0 * eta - 1.0) * (0.5 * h);
+                unsigned char* q = d + (jj * 3 + ii) * 24;
+                dgv_be64(q, x);
+                dgv_be64(q + 8, y);
+                dgv_be64(q + 16, 0.0);
+            }
+    }
+}
+
+// CELLS: 9, then the cell's point ids in VTK Lagrange-quad order (corners,
+// edges, face; point_idx_lagrange_quad, print_dg_tree_v2.hpp:61-97): the
+// point (ii, jj) of cell c is 9 c + 3 jj + ii
+__global__ void k_dgvtk_cells(long long first, long long count, unsigned char* __restrict__ out)
+{
+    constexpr int order[9] = { 0, 2, 8, 6, 1, 5, 7, 3, 4 };
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        unsigned char*  d    = out + i * 40;
+        const long long base = (first + i) * 9;
+        dgv_be32(d, 9u);
+        for (int v = 0; v < 9; ++v) dgv_be32(d + 4 * (v + 1), static_cast<uint32_t>(static_cast<int>(base + order[v])));
+    }
+}
+
+__global__ void k_dgvtk_types(long long count, unsigned char* __restrict__ out)
+{
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        dgv_be32(out + 4 * i, 70u); // VTK_LAGRANGE_QUADRILATERAL
+}
+
+// POINT_DATA component `var`: Basis::evaluate_basis (polynomial.hpp:36-55)
+// at the 9 points, sum over the nodes in tensor order of value x (1 x L_i0(xi)
+// x L_i1(eta))
+__global__ void k_dgvtk_values(const double* __restrict__ state, Geo g, size_t fstride, int var, double p0, double p1, long long first, long long count,
+                               unsigned char* __restrict__ out)
+{
+    const double pts[2] = { p0, p1 };
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long cell = first + i;
+        const int       p = static_cast<int>(cell >> 4), lx = static_cast<int>(cell & 3);
+        const int       ly = static_cast<int>((cell >> 2) & 3);
+        const size_t    at = static_cast<size_t>(p) * g.flat + (ly + 1) * (kDgPatch + 2) + lx + 1;
+        double          C[2][2];
+        for (int i0 = 0; i0 < 2; ++i0)
+            for (int i1 = 0; i1 < 2; ++i1) C[i0][i1] = state[((i0 * 2 + i1) * kDgVars + var) * fstride + at];
+        unsigned char* d = out + i * 9 * 8;
+        for (int jj = 0; jj < 3; ++jj)
+            for (int ii = 0; ii < 3; ++ii) {
+                const double xi = static_cast<double>(ii) / 2.0, eta = static_cast<double>(jj) / 2.0;
+                dgv_be64(d + (jj * 3 + ii) * 8, dg_eval(C, pts, xi, eta));
+            }
+    }
+}
+
+} // namespace
+
+amr_status dg_write_vtk(const uint64_t* keys, const double* state, size_t size, const Geo& g, size_t fstride,
+                        cudaStream_t s, const char* path, std::string& err, uint64_t& launches)
+{
+    const long long cells = static_cast<long long>(size) * kDgPatch * kDgPatch;
+    FILE*           f     = std::fopen(path, "wb");
+    if (!f) {
+        err = std::string("cannot open ") + path;
+        return AMR_ERR_INVALID;
+    }
+    // staging: at most 2^18 cells of the widest section (points, 216 B a cell)
+    const long long chunk     = std::min<long long>(std::max<long long>(cells, 1), 1LL << 18);
+    const size_t    max_bytes = static_cast<size_t>(chunk) * 9 * 24;
+    unsigned char*  dbuf      = nullptr;
+    unsigned char*  hbuf      = nullptr;
+    cudaError_t     e         = cudaMalloc(&dbuf, max_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&hbuf, max_bytes);
+    bool io_ok   = true;
+    auto section = [&](size_t per_cell, auto&& launch) {
+        for (long long first = 0; first < cells && e == cudaSuccess && io_ok; first += chunk) {
+            const long long n    = std::min(chunk, cells - first);
+            const unsigned  grid = static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 32));
+            launch(first, n, grid);
+            ++launches;
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpyAsync(hbuf, dbuf, n * per_cell, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e == cudaSuccess && std::fwrite(hbuf, 1, n * per_cell, f) != static_cast<size_t>(n * per_cell))
+                io_ok = false;
+        }
+    };
+    const double p0 = 0.5 + 0.5 * -0.5773502691896257, p1 = 0.5 + 0.5 * 0.5773502691896257;
+    if (e == cudaSuccess) {
+        std::fprintf(f, "# vtk DataFile Version 3.0\nDG 2D Printer (Order=%d)\nBINARY\nDATASET UNSTRUCTURED_GRID\n",
+                     kDgOrder);
+        std::fprintf(f, "POINTS %lld double\n", cells * 9);
+        section(9 * 24, [&](long long first, long long n, unsigned grid) {
+            k_dgvtk_points<<<grid, 256, 0, s>>>(keys, g, first, n, dbuf);
+        });
+        std::fprintf(f, "CELLS %lld %lld\n", cells, cells * 10);
+        section(40, [&](long long first, long long n, unsigned grid) {
+            k_dgvtk_cells<<<grid, 256, 0, s>>>(first, n, dbuf);
+        });
+        std::fprintf(f, "CELL_TYPES %lld\n", cells);
+        section(4, [&](long long, long long n, unsigned grid) { k_dgvtk_types<<<grid, 256, 0, s>>>(n, dbuf); });
+        if (cells > 0) std::fprintf(f, "POINT_DATA %lld\n", cells * 9);
+        for (int var = 0; cells > 0 && var < kDgVars; ++var) {
+            std::fprintf(f, "SCALARS dof_component_%d double 1\nLOOKUP_TABLE default\n", var);
+            section(9 * 8, [&](long long first, long long n, unsigned grid) {
+                k_dgvtk_values<<<grid, 256, 0, s>>>(state, g, fstride, var, p0, p1, first, n, dbuf);
+            });
+        }
+    }
+    if (dbuf) cudaFree(dbuf);
+    if (hbuf) cudaFreeHost(hbuf);
+    const bool closed = std::fclose(f) == 0;
+    if (e != cudaSuccess) {
+        err = std::string("DG printer: ") + cudaGetErrorString(e);
+        return AMR_ERR_CUDA;
+    }
+    if (!io_ok || !closed) {
+        err = "DG printer: write failed";
+        return AMR_ERR_INVALID;
+    }
+    return AMR_OK;
 }
 
 } // namespace amr_gb300

@@ -2,7 +2,10 @@
 // multiply-add contraction).
 #pragma once
 
+#include <string>
+
 #include "amr_device.cuh"
+#include "amr_gb300.h"
 
 namespace amr_gb300 {
 
@@ -70,6 +73,11 @@ struct DgEulerStage {
 cudaError_t dg_euler_prims(const double* in, double* prims, int P, const Geo& g, size_t fstride, cudaStream_t s);
 cudaError_t dg_euler_stage(const DgEulerStage& s);
 cudaError_t dg_euler_next(double* dt, double* time, unsigned long long* dt_min, cudaStream_t s);
+
+// The reference's DG printer (dg_tree_printer_2d) for the tree's leaves and
+// DG state, written to `path`; `launches` counts the kernels run.
+amr_status dg_write_vtk(const uint64_t* keys, const double* state, size_t size, const Geo& g, size_t fstride,
+                        cudaStream_t s, const char* path, std::string& err, uint64_t& launches);
 
 // Halo exchange of a DG state (16 fields fstride apart): same-level faces
 // copy, coarse-fine faces restrict or interpolate the DG polynomials.

@@ -2120,6 +2120,22 @@ amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coars
     return st;
 }
 
+amr_status amr_tree_dg_write_vtk(amr_tree* t, const char* path)
+{
+    if (!t || !path) return fail(AMR_ERR_INVALID, "null argument");
+    const Geo& g = t->g;
+    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
+        return fail(AMR_ERR_INVALID, "the DG printer needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
+    AMR_CUDA(cudaStreamSynchronize(t->stream));
+    std::string      err;
+    uint64_t         launches = 0;
+    const amr_status st = dg_write_vtk(t->keys[t->tb], static_cast<const double*>(t->cur), t->size, g, t->fstride(),
+                                       t->stream, path, err, launches);
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
+    if (st != AMR_OK) return fail(st, err);
+    return AMR_OK;
+}
+
 amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int amr_interval,
                            double refine_threshold, double coarsen_threshold, amr_dg_stats* stats)
 {

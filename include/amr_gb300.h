@@ -350,6 +350,17 @@ amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int 
  * the device: amr_tree_dg_advance reads the step size back once per call.
  * amr_tree_dg_advance, amr_tree_dg_remesh and amr_tree_dg_run apply the
  * setting; states are bit-identical to the reference's CPU path. */
+/* The reference's DG printer (ndt::print::dg_tree_printer_2d::print,
+ * include/ndtree/print_dg_tree_v2.hpp:145-370) for the tree's current
+ * leaves and DG state, written to `path` (the reference builds the name
+ * vtk_output/DG_<equation>_ord2_<integrator><suffix> itself): a legacy
+ * binary big-endian unstructured grid with one VTK Lagrange quadrilateral
+ * (type 70) per interior cell, its 9 points at xi, eta in {0, 1/2, 1} and
+ * four POINT_DATA arrays dof_component_0..3, the cell's polynomial evaluated
+ * there.  Built on the device in chunks; the file is byte-identical to the
+ * reference's. */
+amr_status amr_tree_dg_write_vtk(amr_tree* t, const char* path);
+
 #define AMR_DG_ADVECTION 0
 #define AMR_DG_EULER     1
 amr_status amr_tree_dg_set_equation(amr_tree* t, int equation);

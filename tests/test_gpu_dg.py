@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import dg_oracle as G
-from dg_cases import CASES, EULER_CASES, fields_to_leaves, leaves_to_fields, load
+from dg_cases import CASES, EULER_CASES, fields_to_leaves, leaves_to_fields, load, printer_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -211,3 +211,47 @@ def test_gpu_dg_run_matches_the_reference_main_loop(amr):
     final = np.ascontiguousarray(fields_to_leaves(t.download_state()), dtype="<f8")
     assert final.sum() == float(z["state_sum"])
     assert hashlib.sha256(final.tobytes()).hexdigest() == str(z["state_sha256"])
+
+
+def _fixture_tree_on_gpu(amr, name, dump):
+    """The tree of dump `dump` of a DG fixture on the device: the uniform
+    level, or the fixture's re-mesh loop replayed to that dump, then the
+    fixture's state of that dump uploaded."""
+    z = load(name)
+    L = int(z["level"])
+    t = amr.Tree(2, 4, 1, 6, capacity=8000, dtype=amr.F64, fields=16)
+    t.dg_set_equation(str(z["equation"]))
+    t.refine_uniform(L)
+    if "state" in z:
+        t.upload_state(leaves_to_fields(z["state"][dump]))
+        return t
+    every, dts = int(z["amr"]), z["dt"]
+    t.upload_state(leaves_to_fields(z["state_0"]))
+    dt, time, next_amr = float(dts[1]), 0.0, 0
+    for k in range(1, dump + 1):
+        dt, time = t.dg_advance(1, dt, time)
+        if k >= next_amr:
+            t.dg_remesh(float(z["rthr"]), float(z["cthr"]))
+            next_amr = k + every
+    np.testing.assert_array_equal(t.ids(), z[f"ids_{dump}"])
+    t.upload_state(leaves_to_fields(z[f"state_{dump}"]))
+    return t
+
+
+@pytest.mark.parametrize("name", sorted(printer_cases()))
+def test_gpu_dg_printer_matches_reference(amr, name, tmp_path):
+    """amr_tree_dg_write_vtk against the file the reference's
+    dg_tree_printer_2d wrote for the same tree and state: byte for byte
+    (SHA-256 and length)."""
+    c = printer_cases()[name]
+    t = _fixture_tree_on_gpu(amr, c["fixture"], c["dump"])
+    path = tmp_path / f"{name}.vtk"
+    t.dg_write_vtk(path)
+    b = path.read_bytes()
+    assert len(b) == c["bytes"] and hashlib.sha256(b).hexdigest() == c["sha256"]
+
+
+def test_gpu_dg_printer_rejects_other_trees(amr, tmp_path):
+    t = amr.Tree(2, 8, 1, 5, capacity=64, dtype=amr.F64, fields=16)
+    with pytest.raises(amr.AmrError):
+        t.dg_write_vtk(tmp_path / "x.vtk")
