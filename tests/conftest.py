@@ -13,6 +13,13 @@ sys.path.insert(0, str(REPO / "gpu-amr_gb300"))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "endtoend: a whole solver loop or output file; runs after every other test")
+
+
+def pytest_collection_modifyitems(config, items):
+    """End-to-end tests (whole solver loops, output files) run last, so that
+    a run stopping at its first failure has run every unit and parity test."""
+    items.sort(key=lambda item: item.get_closest_marker("endtoend") is not None)
 
 
 def load_golden(name):

@@ -191,6 +191,7 @@ def test_gpu_dg_set_equation_rejects_unknown(amr):
         amr.check(amr.lib().amr_tree_dg_set_equation(t._h, 7))
 
 
+@pytest.mark.endtoend
 def test_gpu_dg_run_matches_the_reference_main_loop(amr):
     """amr_tree_dg_run against the reference's whole DG main loop
     (DGSolver::run to t = 1 from a uniform level-5 start, re-mesh every 20
@@ -238,6 +239,7 @@ def _fixture_tree_on_gpu(amr, name, dump):
     return t
 
 
+@pytest.mark.endtoend
 @pytest.mark.parametrize("name", sorted(printer_cases()))
 def test_gpu_dg_printer_matches_reference(amr, name, tmp_path):
     """amr_tree_dg_write_vtk against the file the reference's
