@@ -102,3 +102,65 @@ def test_euler_benchmark_through_dropin_matches_reference(dropin_exe):
     else:
         assert rel_l2(s0, want0) <= 1e-15
         assert rel_l2(s1, want1) <= 1e-12 and abs(time - float(z["time"])) <= 1e-12 * float(z["time"])
+
+
+DG_SRC = REPO / "tests" / "cpp" / "dg_dropin.cpp"
+
+
+def test_dg_dropin_headers_compile():
+    """dg_helpers/solver.hpp and config/generated_config.hpp (the reference's
+    DG solver API) compile with a program written like the reference's DG
+    example."""
+    subprocess.run(["g++", *FLAGS, "-fsyntax-only", str(DG_SRC)], check=True)
+
+
+def _read_trees(path):
+    raw = path.read_bytes()
+    out, o = [], 0
+    while o < len(raw):
+        P = int(np.frombuffer(raw, np.uint64, 1, o)[0])
+        o += 8
+        ids = np.frombuffer(raw, np.uint64, P, o).copy()
+        o += 8 * P
+        state = np.frombuffer(raw, np.float64, 16 * P * 36, o).reshape(16, P, 6, 6).copy()
+        o += 8 * 16 * P * 36
+        out.append((ids, state))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.endtoend
+def test_dg_solver_through_cpp_header_equals_dg_run(tmp_path):
+    """DGSolver<Policy>::run() of the C++ header (level-5 start, initial dt
+    0.01, re-mesh every 20 steps, output every 0.01, to t = 0.05) against
+    amr_tree_dg_run from the same initial state: processed cells, final
+    leaves and interior states bit for bit; one VTK file at time 0 and one
+    per plot time reached.  The header's initial values (the equation's
+    initial condition at the nodes, through the host's sin) agree with the
+    numpy restatement's to 4 ulp."""
+    import __graft_entry__ as g
+    import amr_gb300 as A
+    from dg_cases import fields_to_leaves
+    from oracle import dg_oracle as G
+
+    lib = g.build_library()
+    exe = tmp_path / "dg_dropin"
+    subprocess.run(["g++", *FLAGS, str(DG_SRC), "-o", str(exe), "-L", str(lib.parent), "-lamr_gb300",
+                    f"-Wl,-rpath,{lib.parent}"], check=True)
+    r = subprocess.run([str(exe), str(tmp_path / "trees.bin")], capture_output=True, text=True, timeout=600,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    words = r.stdout.split()
+    processed, files = int(words[1]), int(words[3])
+    (ids0, s0), (ids1, s1) = _read_trees(tmp_path / "trees.bin")
+    np.testing.assert_allclose(fields_to_leaves(s0), G.to_leaves(G.initial_state(5), 5), rtol=4 * 2.0 ** -52,
+                               atol=4 * 2.0 ** -52)
+    t = A.Tree(2, 4, 1, 6, capacity=8192, dtype=A.F64, fields=16)
+    t.refine_uniform(5)
+    np.testing.assert_array_equal(t.ids(), ids0)
+    t.upload_state(s0)
+    st = t.dg_run(0.01, 0.05, 20, 0.05, 0.01)
+    assert processed == st["cells"]
+    np.testing.assert_array_equal(t.ids(), ids1)
+    np.testing.assert_array_equal(fields_to_leaves(t.download_state()), fields_to_leaves(s1))
+    assert 5 <= files <= 6
