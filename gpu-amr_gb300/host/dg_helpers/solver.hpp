@@ -121,15 +121,24 @@ private:
         }
     }
 
-    // TreeBuilder's initial state: per interior cell, the centre (patch
-    // corner + (local + 0.5) x cell edge) and the values at the nodes
-    // centre + (point - 1/2) x edge; fields x leaves x 6 x 6, ghosts zero
     void upload_initial_values()
     {
         std::size_t P = 0;
         detail::dg_check(amr_tree_size(m_tree, &P));
         std::vector<uint64_t> ids(P);
         detail::dg_check(amr_tree_get_ids(m_tree, ids.data(), P));
+        const std::vector<double> state = initial_state(ids);
+        detail::dg_check(amr_tree_upload_state(m_tree, state.data(), P));
+    }
+
+public:
+    // TreeBuilder's initial state for the leaves `ids` (Morton ids of this
+    // policy's depth): per interior cell, the centre (patch corner + (local +
+    // 0.5) x cell edge) and the values at the nodes centre + (point - 1/2) x
+    // edge; fields x leaves x 6 x 6, ghosts zero
+    static std::vector<double> initial_state(const std::vector<uint64_t>& ids)
+    {
+        const std::size_t   P = ids.size();
         std::vector<double> state(16 * P * 36, 0.0);
         const double        pts[2] = { 0.5 + 0.5 * -0.5773502691896257, 0.5 + 0.5 * 0.5773502691896257 };
         const double        unit   = 1.0 / static_cast<double>(1u << Policy::MaxDepth);
@@ -155,10 +164,9 @@ private:
                         }
                 }
         }
-        detail::dg_check(amr_tree_upload_state(m_tree, state.data(), P));
+        return state;
     }
 
-public:
     // DGSolver::run (solver.hpp:109-151): output at time 0, then steps while
     // time < EndTime: the step (dt = min(dt, dt_min), time += dt), a
     // re-mesh when the step count reaches the next re-mesh step

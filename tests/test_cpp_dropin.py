@@ -164,3 +164,23 @@ def test_dg_solver_through_cpp_header_equals_dg_run(tmp_path):
     np.testing.assert_array_equal(t.ids(), ids1)
     np.testing.assert_array_equal(fields_to_leaves(t.download_state()), fields_to_leaves(s1))
     assert 5 <= files <= 6
+
+
+@pytest.mark.parametrize("name", ["dg_advection_l3", "dg_euler_l3"])
+def test_dg_dropin_initial_state_matches_reference(name, tmp_path):
+    """DGSolver<Policy>::initial_state (the TreeBuilder's nodal initial
+    values, host arithmetic only) for the reference's level-3 tree against
+    the initial state the reference's own TreeBuilder arithmetic produced
+    (dump 0 of the DG fixtures, advection and Euler): bit for bit."""
+    from dg_cases import fields_to_leaves, load
+
+    z = load(name)
+    ids, st0 = z["ids"], z["state"][0]
+    exe = tmp_path / "dg_initial_state"
+    subprocess.run(["g++", *FLAGS, str(REPO / "tests" / "cpp" / "dg_initial_state.cpp"), "-o", str(exe)],
+                   check=True)
+    (tmp_path / "ids.bin").write_bytes(np.ascontiguousarray(ids, dtype=np.uint64).tobytes())
+    eq = str(z["equation"])
+    subprocess.run([str(exe), eq, str(tmp_path / "ids.bin"), str(tmp_path / "state.bin")], check=True)
+    state = np.fromfile(tmp_path / "state.bin", np.float64).reshape(16, len(ids), 6, 6)
+    np.testing.assert_array_equal(fields_to_leaves(state), st0)
