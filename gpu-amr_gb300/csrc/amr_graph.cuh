@@ -79,7 +79,7 @@ k_run_step2d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
 
 // Pass records of the current tree (first kernel of an interval run with
 // multi-step passes, after the guard).
-__global__ void __launch_bounds__(256) k_run_pass_records(RunBufs B, RunCtl* ctl, Geo g, int upx0, int upy0)
+static __global__ void __launch_bounds__(256) k_run_pass_records(RunBufs B, RunCtl* ctl, Geo g, int upx0, int upy0)
 {
     if (ctl->err || ctl->recs) return; // still valid: the last interval left the tree as it was
     const int P = ctl->P, tb = ctl->tb;
@@ -113,7 +113,7 @@ k_run_step2d_pass(RunBufs B, RunCtl* ctl, int nl, const Coef* __restrict__ coef,
 // stops every later kernel of the replay, and the host re-runs the interval
 // with one-step launches.
 constexpr int32_t kRetryUniform = 100;
-__global__ void k_run_require_uniform(RunCtl* ctl)
+static __global__ void k_run_require_uniform(RunCtl* ctl)
 {
     if (threadIdx.x == 0 && ctl->err == 0 && !ctl->uniform) ctl->err = kRetryUniform;
 }
@@ -267,7 +267,7 @@ k_run_flags_max(RunBufs B, RunCtl* ctl, Geo g, double rthr, double cthr, int min
 // The flag kernels set ctl->flagged when they flag some leaf; without one
 // the re-mesh changes nothing (reconstruction_is_noop, ndtree.hpp:1242-1246)
 // and the marks are not needed.
-__global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->changed = 0;
@@ -279,21 +279,21 @@ __global__ void k_run_mark(RunBufs B, RunCtl* ctl, Geo g)
 
 // With no leaf flagged the re-mesh changes nothing (reconstruction_is_noop,
 // ndtree.hpp:1242-1246): closure, veto, count and scan return at once.
-__global__ void k_run_closure(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_closure(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P) closure_leaf(B.meta[tb], g, B.rmark, i);
 }
 
-__global__ void k_run_veto(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_veto(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
     AMR_RUN_LEAVES(P) veto_leaf(B.meta[tb], g, B.rmark, B.chead, i);
 }
 
-__global__ void k_run_count(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_count(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P, tb = ctl->tb;
@@ -328,7 +328,7 @@ __device__ inline uint32_t scan_block_exclusive(uint32_t v, uint32_t* warp_sums,
 }
 
 // Scan, pass 1: sum of the counts of each tile of kScanTile leaves.
-__global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunCtl* ctl)
+static __global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunCtl* ctl)
 {
     if (ctl->err || !ctl->flagged) return;
     const int P = ctl->P;
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kScanThreads) k_run_scan_tiles(RunBufs B, RunC
 // Scan, pass 2: each tile adds the sums of the tiles before it and writes
 // its exclusive positions; the last tile writes pos[P] and the new size and
 // flags AMR_ERR_CAPACITY when it exceeds the capacity.
-__global__ void __launch_bounds__(kScanThreads) k_run_scan_apply(RunBufs B, RunCtl* ctl)
+static __global__ void __launch_bounds__(kScanThreads) k_run_scan_apply(RunBufs B, RunCtl* ctl)
 {
     if (ctl->err || !ctl->flagged) return;
     const int P      = ctl->P;
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kScanThreads) k_run_scan_apply(RunBufs B, RunC
     }
 }
 
-__global__ void k_run_emit(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_emit(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->changed) return;
     const int P = ctl->P, tb = ctl->tb, nb = tb ^ 1;
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(256) k_run_remap(RunBufs B, RunCtl* ctl, Geo g
     }
 }
 
-__global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
+static __global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
 {
     if (ctl->err || !ctl->changed) return;
     const int NP = ctl->NP, nb = ctl->tb ^ 1;
@@ -428,7 +428,7 @@ __global__ void k_run_neighbors(RunBufs B, RunCtl* ctl, Geo g)
 // End of an interval (one block): statistics of the interval just run and
 // the state buffer the steps left current, then, when the re-mesh changed the
 // tree, the switch to the new buffers and the new per-instance finest levels.
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
 k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp, int records)
 {
     __shared__ int chg;
@@ -475,7 +475,7 @@ k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp, i
 // Per-instance time bookkeeping at the start of a graph chunk: an empty
 // batch, the remaining time, and the totals carried in from earlier work of
 // the run (tot0, ctot0).
-__global__ void k_run_dt_init(DtState d, int ninst, double remaining0, double tot0, uint32_t ctot0)
+static __global__ void k_run_dt_init(DtState d, int ninst, double remaining0, double tot0, uint32_t ctot0)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ninst) return;
@@ -487,7 +487,7 @@ __global__ void k_run_dt_init(DtState d, int ninst, double remaining0, double to
 }
 
 // offsets[i] = first leaf of instance i (lower bound of its key prefix).
-__global__ void k_instance_offsets(const uint64_t* __restrict__ keys, int P, Geo g, int ninst,
+static __global__ void k_instance_offsets(const uint64_t* __restrict__ keys, int P, Geo g, int ninst,
                                    unsigned long long* __restrict__ offsets)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

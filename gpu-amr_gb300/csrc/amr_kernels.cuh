@@ -464,7 +464,7 @@ enum : int {
 
 // Block b handles instance b: its CFL step from its own finest level and
 // velocity; coef row (step s, instance b) starts at (s * ninst + b) * (depth+1).
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
 k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
               int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef,
               float2* __restrict__ coef32 = nullptr, int32_t* __restrict__ upcode = nullptr,
@@ -518,7 +518,7 @@ k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __rest
 }
 
 // Refinement flags that refine every leaf below its instance's target level.
-__global__ void k_flags_to_level(const uint64_t* __restrict__ keys, int P, Geo g, const int32_t* __restrict__ target,
+static __global__ void k_flags_to_level(const uint64_t* __restrict__ keys, int P, Geo g, const int32_t* __restrict__ target,
                                  int8_t* __restrict__ flags)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -527,7 +527,7 @@ __global__ void k_flags_to_level(const uint64_t* __restrict__ keys, int P, Geo g
 }
 
 // Maximum level over a level array.
-__global__ void k_max_level(const int32_t* __restrict__ levels, int P, int32_t* __restrict__ out)
+static __global__ void k_max_level(const int32_t* __restrict__ levels, int P, int32_t* __restrict__ out)
 {
     int m = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) m = max(m, levels[i]);
@@ -748,7 +748,7 @@ k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_
 }
 
 // flag = 1 when some neighbour record is not "same level" (flag zeroed first).
-__global__ void k_any_not_same(const amr_halo_meta* __restrict__ meta, long long n, int32_t* flag)
+static __global__ void k_any_not_same(const amr_halo_meta* __restrict__ meta, long long n, int32_t* flag)
 {
     for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n;
          t += static_cast<long long>(gridDim.x) * blockDim.x)
@@ -846,27 +846,27 @@ __device__ inline void neighbor_entry(const uint64_t* keys, int P, const Geo& g,
 }
 
 // --------------------------------------------- per-launch re-mesh kernels
-__global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restrict__ flags, int P, Geo g,
+static __global__ void k_mark(const uint64_t* __restrict__ keys, const int8_t* __restrict__ flags, int P, Geo g,
                        uint8_t* __restrict__ rmark, uint8_t* __restrict__ chead)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P) mark_leaf(keys, flags, P, g, rmark, chead, i);
 }
 
-__global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, uint8_t* rmark)
+static __global__ void k_closure(const amr_halo_meta* __restrict__ meta, int P, Geo g, uint8_t* rmark)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P) closure_leaf(meta, g, rmark, i);
 }
 
-__global__ void k_veto(const amr_halo_meta* __restrict__ meta, int P, Geo g, const uint8_t* __restrict__ rmark,
+static __global__ void k_veto(const amr_halo_meta* __restrict__ meta, int P, Geo g, const uint8_t* __restrict__ rmark,
                        uint8_t* __restrict__ chead)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < P) veto_leaf(meta, g, rmark, chead, i);
 }
 
-__global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+static __global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
                         const uint8_t* __restrict__ chead, int P, Geo g, uint32_t* __restrict__ cnt,
                         int32_t* __restrict__ changed)
 {
@@ -874,14 +874,14 @@ __global__ void k_count(const uint64_t* __restrict__ keys, const uint8_t* __rest
     if (i < P) count_leaf(keys, rmark, chead, g, cnt, changed, i);
 }
 
-__global__ void __launch_bounds__(1024)
+static __global__ void __launch_bounds__(1024)
 k_scan(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ pos, int P, size_t cap, int32_t* __restrict__ status)
 {
     __shared__ uint32_t part[1024];
     block_scan(cnt, pos, P, cap, status, part);
 }
 
-__global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
+static __global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restrict__ rmark,
                        const uint8_t* __restrict__ chead, const uint32_t* __restrict__ pos, int P, Geo g,
                        uint64_t* __restrict__ nkeys, int32_t* __restrict__ nlevels, int32_t* __restrict__ src,
                        int8_t* __restrict__ skind, int32_t* __restrict__ max_level)
@@ -890,7 +890,7 @@ __global__ void k_emit(const uint64_t* __restrict__ keys, const uint8_t* __restr
     if (i < P) emit_leaf(keys, rmark, chead, pos, g, nkeys, nlevels, src, skind, max_level, i);
 }
 
-__global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr_halo_meta* __restrict__ meta,
+static __global__ void k_neighbors(const uint64_t* __restrict__ keys, int P, Geo g, amr_halo_meta* __restrict__ meta,
                             int32_t* __restrict__ status)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -948,7 +948,7 @@ k_intergrid(T* __restrict__ buf, const amr_transfer_task* __restrict__ tasks, in
     }
 }
 
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
 k_gather(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t words_per_patch,
          const int32_t* __restrict__ sources, int count)
 {
@@ -959,7 +959,7 @@ k_gather(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t words_pe
     for (size_t w = threadIdx.x; w < words_per_patch; w += blockDim.x) t[w] = f[w];
 }
 
-__global__ void k_gather_bytes(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst,
+static __global__ void k_gather_bytes(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst,
                                size_t bytes, const int32_t* __restrict__ sources, int count)
 {
     const int j = blockIdx.x;
@@ -971,7 +971,7 @@ __global__ void k_gather_bytes(const unsigned char* __restrict__ src, unsigned c
 
 // finalize_step_dt_kernel semantics (fvm_time_step.cu:204-233) for the
 // drop-in dt entry point.
-__global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, double v0, double v1, double v2,
+static __global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo g, double v0, double v1, double v2,
                               double cfl, double* dt_buf, double* acc, double* remaining, uint32_t* count)
 {
     const double v[3]    = { v0, v1, v2 };
@@ -1337,7 +1337,7 @@ __device__ __forceinline__ void pass_record(const amr_halo_meta* __restrict__ me
 
 // Host-driven build: P leaves, upwind offsets per instance (upcode) or
 // launch-wide (upx0, upy0).
-__global__ void __launch_bounds__(256)
+static __global__ void __launch_bounds__(256)
 k_pass_records(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
                const int32_t* __restrict__ upcode, int upx0, int upy0, int P, Geo g, int4* __restrict__ rec,
                int32_t* err)
@@ -2270,7 +2270,7 @@ __global__ void k_zero_ghosts(T* __restrict__ buf, long long total, Geo g)
 
 // Coefficient rows (step s, instance i) of `steps` steps from recorded step
 // sizes dts[s * ninst + i] (the fill of k_batch_begin, without the clamp).
-__global__ void k_coef_from_dt(const double* __restrict__ dts, Geo g, const double* __restrict__ vel, int steps,
+static __global__ void k_coef_from_dt(const double* __restrict__ dts, Geo g, const double* __restrict__ vel, int steps,
                                int ninst, Coef* __restrict__ coef)
 {
     const int nl    = g.depth + 1;

@@ -1,254 +1,20 @@
 // C-ABI of the GB300 AMR path: the device-resident tree and the reference
 // drop-in launchers.  Host code only orchestrates launches; every per-leaf
 // or per-cell loop runs in a kernel from amr_kernels.cuh.
-#include <algorithm>
-#include <atomic>
-#include <climits>
-#include <cmath>
-#include <map>
-#include <limits>
-#include <cstdint>
-#include <cstdio>
-#include <cstdlib>
-#include <cstring>
-#include <mutex>
-#include <string>
-#include <vector>
 
-#include "amr_gb300.h"
-#include "amr_cycle.cuh"
-#include "amr_euler.cuh"
-#include "amr_ssprk.cuh"
-#include "amr_dg.cuh"
-#include "amr_graph.cuh"
-#include "amr_vtk.cuh"
+#include "amr_api.cuh"
 
-using namespace amr_gb300;
-
-namespace {
-
+namespace amr_api {
 thread_local std::string g_last_error;
 std::atomic<uint64_t>    g_launches{ 0 };
-
-amr_status fail(amr_status s, const std::string& what)
-{
-    g_last_error = what;
-    return s;
-}
-
-amr_status cuda_fail(cudaError_t e, const char* where)
-{
-    return fail(AMR_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
-}
-
-#define AMR_CUDA(call)                                          \
-    do {                                                        \
-        cudaError_t e_ = (call);                                \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
-    } while (0)
-
-#define AMR_LAUNCHED(where)                                     \
-    do {                                                        \
-        g_launches.fetch_add(1, std::memory_order_relaxed);     \
-        cudaError_t e_ = cudaGetLastError();                    \
-        if (e_ != cudaSuccess) return cuda_fail(e_, where);     \
-    } while (0)
-
-bool make_geo(const amr_patch_geometry* pg, Geo& g)
-{
-    if (!pg) return false;
-    const int rank = pg->rank, n = pg->n, h = pg->halo, depth = pg->depth;
-    if (rank != 2 && rank != 3) return false;
-    if (h < 1 || n < 2 * h || n % 2 != 0) return false;
-    if (depth < 0 || rank * depth + 6 > 64 || depth > 30) return false;
-    g.rank  = rank;
-    g.n     = n;
-    g.h     = h;
-    g.P1    = n + 2 * h;
-    g.depth = depth;
-    g.nd    = 1 << rank;
-    g.nf    = 1 << (rank - 1);
-    g.ndir  = 2 * rank;
-    g.flat  = 1;
-    g.cells = 1;
-    for (int k = 0; k < rank; ++k) {
-        g.flat *= g.P1;
-        g.cells *= n;
-    }
-    g.s[0] = g.s[1] = g.s[2] = 0;
-    int st = 1;
-    for (int L = rank - 1; L >= 0; --L) {
-        g.s[L] = st;
-        st *= g.P1;
-    }
-    g.inst_shift  = 64;
-    g.morton_mask = (rank * depth >= 64) ? ~0ull : ((1ull << (rank * depth)) - 1ull);
-    for (int a = 0; a < 3; ++a) {
-        const double len = (a < rank) ? pg->lengths[a] : 1.0;
-        if (!(len > 0.0)) return false;
-        // physics_system::cell_sizes at level 0: L*2^D/2^D/n == L/n exactly
-        g.dx_root[a] = len / static_cast<double>(n);
-    }
-    return true;
-}
-
-inline unsigned grid_for(long long work, int block)
-{
-    long long b = (work + block - 1) / block;
-    if (b < 1) b = 1;
-    return static_cast<unsigned>(b);
-}
-
-} // namespace
-
-namespace {
-// One captured interval: the launch sequence of amr_tree_run's graph path for
-// a fixed set of parameters.
-struct GraphKey {
-    int    k = 0, crit = 0, min_level = 0, max_level = 0, rounds = 0, bounds = 0, vel = 0, W = 0, S = 0, grid = 0;
-    int    pair = 0; // several steps per pass (same-level trees)
-    int    up[3] = { 0, 0, 0 };
-    double rthr = 0.0, cthr = 0.0, cfl = 0.0;
-    bool   operator==(const GraphKey& o) const
-    {
-        return k == o.k && crit == o.crit && min_level == o.min_level && max_level == o.max_level &&
-               rounds == o.rounds && bounds == o.bounds && vel == o.vel && W == o.W && S == o.S && grid == o.grid &&
-               pair == o.pair &&
-               up[0] == o.up[0] && up[1] == o.up[1] && up[2] == o.up[2] && std::memcmp(&rthr, &o.rthr, 8) == 0 &&
-               std::memcmp(&cthr, &o.cthr, 8) == 0 && std::memcmp(&cfl, &o.cfl, 8) == 0;
-    }
-};
-struct GraphEntry {
-    GraphKey        key;
-    cudaGraph_t     graph   = nullptr;
-    cudaGraphExec_t exec    = nullptr;
-    uint64_t        kernels = 0; // kernel nodes of one replay
-};
-// Launch configuration of the 2D update kernel: W warps per block, S tiles
-// per warp, `grid` blocks (0 = one warp per patch up to full residency).
-struct StepCfg {
-    int W = 8, S = 2, grid = 0;
-};
-} // namespace
-
-struct amr_tree {
-    Geo          g{};
-    double       lengths[3] = { 1.0, 1.0, 1.0 }; // domain lengths per Morton axis
-    int          ninst    = 1;
-    size_t       cap      = 0;
-    int          dtype    = AMR_F64;
-    size_t       esize    = 8;
-    int          nvar     = 1; // state fields; field f of a buffer starts at f * fstride() elements
-    cudaStream_t stream   = nullptr;
-    size_t       size     = 0;
-    int          max_level_host = 0;
-    bool         ghosts_valid   = false;
-    bool         uniform        = true; // every neighbour relation is "same level" (multi-step passes apply)
-
-    void*          sbuf[2]{};   // the two state buffers (fixed addresses)
-    void*          cur = nullptr; // one of sbuf
-    void*          nxt = nullptr;
-    uint64_t*      keys[2]{};
-    int32_t*       levels[2]{};
-    amr_halo_meta* meta[2]{};
-    int4*          prec = nullptr; // pass records, one per leaf (multi-step passes)
-    int4*          frec = nullptr; // face records, one per leaf (flags of same-level graph intervals)
-    bool           dg_state = false; // the re-mesh in progress carries a DG state (polynomial remap)
-    int            dg_equation = AMR_DG_ADVECTION;
-    double*        dg_prims    = nullptr; // DG Euler: p, u, v per node, eigenvalues x, y per padded cell (14 fields)
-    size_t         dg_prims_cap = 0;       // leaves dg_prims holds
-    double*        dg_scalars  = nullptr; // DG Euler: [0] step size, [1] time
-    unsigned long long* dg_dtmin = nullptr; // DG Euler: smallest CFL step of the last stage (bit pattern)
-    int            tb = 0;
-
-    int8_t*   flags  = nullptr;
-    uint8_t*  rmark  = nullptr;
-    uint8_t*  chead  = nullptr;
-    uint32_t* cnt    = nullptr;
-    uint32_t* pos    = nullptr;
-    int32_t*  src    = nullptr;
-    int8_t*   skind  = nullptr;
-    int32_t*  status = nullptr; // [0] error, [1] changed, [2] new size
-    int32_t*  maxlev = nullptr; // per instance
-    int32_t*  maxlev_new = nullptr; // per instance, zero between graph re-meshes
-    double*   vel    = nullptr; // per instance, 3 each: the velocities in use
-    double*   vel_inst = nullptr; // per instance, as set by amr_tree_set_instance_params
-    int32_t*  bounds = nullptr; // per instance (min, max) level bounds
-    int32_t*  target = nullptr; // per instance target levels (refine_to_levels)
-    unsigned long long* offs = nullptr; // instance offsets, ninst + 1
-    uint32_t* tile_sums = nullptr;
-    RunCtl*   ctl       = nullptr;
-    bool      vel_inst_set = false;
-    std::vector<double> vel_inst_host;
-    uint64_t  topo = 0; // changes whenever the leaves may have changed
-    StepCfg   last_cfg{}; // launch shape of the last 2D update
-    bool      bounds_set   = false;
-    bool      vel_per_leaf = false; // the current advance uses per-instance velocities
-    cudaStream_t          cap_stream = nullptr; // private stream for graph capture
-    std::vector<GraphEntry> graphs;
-    size_t    pinned_bytes = 0;
-
-    double*   dt_acc = nullptr;
-    double*   dt_rem = nullptr;
-    uint32_t* dt_cnt = nullptr;
-    double*   dt_tot = nullptr;
-    uint32_t* dt_ctot = nullptr;
-    DtState   dts() const { return DtState{ dt_acc, dt_rem, dt_cnt, dt_tot, dt_ctot }; }
-    double*   dt_scratch = nullptr; // time bookkeeping of the autotuner's prologue (5 x instances)
-    DtState   scratch_dts() const
-    {
-        const int K = ninst;
-        return DtState{ dt_scratch, dt_scratch + K, reinterpret_cast<uint32_t*>(dt_scratch + 2 * K), dt_scratch + 3 * K,
-                        reinterpret_cast<uint32_t*>(dt_scratch + 4 * K) };
-    }
-    double*   step_dt = nullptr;
-    Coef*     coef    = nullptr;
-    float2*   coef32  = nullptr; // (c_x, c_y) rows of the FP32 2D update
-    int32_t*  upcode  = nullptr; // per instance packed upwind offsets
-    size_t    coef_steps = 0;
-    bool      batch_open = false;
-
-    void* pinned = nullptr; // readback space (pinned_bytes)
-    CycleStats* cstats = nullptr;
-
-    // opt-in launch timing of the update kernel
-    bool                                          timing = false;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
-    std::vector<uint64_t>                         event_cells;
-    size_t                                        events_used = 0;
-
-    // Euler solver scratch: per-step minima of dx / (|u| + a) as ordered
-    // bit patterns (two slots, alternating) and the step size in use
-    unsigned long long* euler_min = nullptr;
-    double*             euler_dt  = nullptr;
-    int32_t*            euler_ctl = nullptr;
-    double*             prim[2]{}; // one-side flux terms beside sbuf[0] / sbuf[1]
-    size_t              prim_cap = 0;
-    void*               stage_buf = nullptr; // SSPRK intermediate stage (capacity patches)
-    size_t              stage_cap = 0;
-
-    size_t fstride() const { return cap * static_cast<size_t>(g.flat); }
-    size_t field_bytes(size_t patches) const { return patches * static_cast<size_t>(g.flat) * esize; }
-};
+} // namespace amr_api
 
 namespace {
 
 constexpr size_t kMaxBatch = 1024;
 
 
-int num_sms()
-{
-    static int sms[64] = {};
-    int        dev     = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) return 152;
-    if (!sms[dev]) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
-        sms[dev] = v;
-    }
-    return sms[dev];
-}
+
 
 // Dynamic shared memory limit of both 2D update kernels of one shape, set
 // once per device.
@@ -545,13 +311,7 @@ amr_status tune_step2d(amr_tree* t, const Coef* coef, const float2* coef32, cons
     return AMR_OK;
 }
 
-template <typename F>
-amr_status dispatch_dtype(int dtype, F&& f)
-{
-    if (dtype == AMR_F64) return f(double{});
-    if (dtype == AMR_F32) return f(float{});
-    return fail(AMR_ERR_INVALID, "unknown dtype");
-}
+
 
 void free_tree(amr_tree* t)
 {
@@ -614,36 +374,6 @@ void free_tree(amr_tree* t)
     if (t->pinned) cudaFreeHost(t->pinned);
     delete t;
 }
-
-// Face halo of every field of an arbitrary state buffer of the tree (does
-// not touch ghosts_valid); with step_dt, only instances whose step is taken.
-amr_status halo_buffer(amr_tree* t, void* buf, const double* step_dt = nullptr)
-{
-    const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
-    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
-    return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
-        using T = decltype(z);
-        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(buf), t->meta[t->tb], total, t->g,
-                                                             t->fstride(), t->keys[t->tb], step_dt);
-        AMR_LAUNCHED("k_halo");
-        return AMR_OK;
-    });
-}
-
-amr_status launch_halo(amr_tree* t)
-{
-    const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
-    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
-    return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
-        using T = decltype(z);
-        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(t->cur), t->meta[t->tb], total, t->g,
-                                                             t->fstride());
-        AMR_LAUNCHED("k_halo");
-        t->ghosts_valid = true;
-        return AMR_OK;
-    });
-}
-
 
 // One root leaf per instance: key i << inst_shift, level 0, periodic
 // self-neighbours (ndtree.hpp:411-421), zero state in both buffers.
@@ -1054,13 +784,6 @@ amr_status interval_graph(amr_tree* t, const GraphKey& key, const RunBufs& B, cu
     return AMR_OK;
 }
 
-struct RunTotals {
-    long long done     = 0;
-    double    sum_dt   = 0.0;
-    uint64_t  executed = 0, cells = 0, remeshes = 0, intervals = 0, leaves_sum = 0, persistent = 0, graphs = 0;
-    uint64_t  lmin = ~0ull, lmax = 0;
-};
-
 // Up to `max_intervals` intervals as graph replays, then one readback of the
 // control block.  Requires that no step is clamped by the remaining time.
 amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_params, long long max_intervals,
@@ -1258,21 +981,41 @@ bool no_clamp(amr_tree* t, const amr_cycle_params* p, bool inst_params, long lon
     return std::isfinite(need) && p->remaining_time - sum_dt >= need;
 }
 
-// The bounded-wait self-test: an mbarrier expects 16 bytes nobody sends.
-__global__ void k_selftest_wait(int32_t* status, int polls)
-{
-    __shared__ __align__(8) uint64_t bar;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        mbar_init_fence();
-        mbar_expect_tx(&bar, 16);
-        status[0] = mbar_wait_bounded(&bar, 0, polls) ? AMR_OK : AMR_ERR_TIMEOUT;
-    }
-}
 
-__global__ void k_selftest_touch(int32_t* status) { status[1] = 1; }
 
 } // namespace
+namespace amr_api {
+// Face halo of every field of an arbitrary state buffer of the tree (does
+// not touch ghosts_valid); with step_dt, only instances whose step is taken.
+amr_status halo_buffer(amr_tree* t, void* buf, const double* step_dt)
+{
+    const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
+    return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+        using T = decltype(z);
+        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(buf), t->meta[t->tb], total, t->g,
+                                                             t->fstride(), t->keys[t->tb], step_dt);
+        AMR_LAUNCHED("k_halo");
+        return AMR_OK;
+    });
+}
+
+amr_status launch_halo(amr_tree* t)
+{
+    const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
+    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
+    return dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+        using T = decltype(z);
+        k_halo<T><<<dim3(grid, t->nvar), 256, 0, t->stream>>>(static_cast<T*>(t->cur), t->meta[t->tb], total, t->g,
+                                                             t->fstride());
+        AMR_LAUNCHED("k_halo");
+        t->ghosts_valid = true;
+        return AMR_OK;
+    });
+}
+
+
+} // namespace amr_api
 
 extern "C" {
 
@@ -1787,7 +1530,9 @@ amr_status amr_tree_refine_uniform(amr_tree* t, int levels)
     return AMR_OK;
 }
 
-static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining,
+} // extern "C"
+
+amr_status amr_api::advance_impl(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining,
                         int first_mode)
 {
     if (!t) return fail(AMR_ERR_INVALID, "null argument");
@@ -1893,276 +1638,11 @@ static amr_status advance_impl(amr_tree* t, size_t steps, const double* velocity
     return AMR_OK;
 }
 
+extern "C" {
+
 amr_status amr_tree_advance(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining)
 {
     return advance_impl(t, steps, velocity3, cfl, remaining, BATCH_RESET);
-}
-
-amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const double* velocity3, double cfl,
-                                  double remaining)
-{
-    if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    if (order != 2 && order != 3) return fail(AMR_ERR_INVALID, "SSPRK order is 2 or 3");
-    if (t->nvar != 1 || t->dtype != AMR_F64) return fail(AMR_ERR_INVALID, "SSPRK advances a one-field FP64 tree");
-    if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
-    cudaStream_t s = t->stream;
-    const int    K = t->ninst;
-    if (velocity3) {
-        std::vector<double> v(3 * static_cast<size_t>(K));
-        for (int i = 0; i < K; ++i)
-            for (int a = 0; a < 3; ++a) v[3 * i + a] = velocity3[a];
-        AMR_CUDA(cudaMemcpyAsync(t->vel, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    } else {
-        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    }
-    if (t->stage_cap != t->cap) {
-        cudaFree(t->stage_buf);
-        t->stage_buf = nullptr;
-        t->stage_cap = 0;
-        AMR_CUDA(cudaMalloc(&t->stage_buf, t->field_bytes(t->cap)));
-        t->stage_cap = t->cap;
-    }
-    SsprkStage st{};
-    st.keys   = t->keys[t->tb];
-    st.P      = static_cast<int>(t->size);
-    st.g      = t->g;
-    st.vel    = t->vel;
-    st.stream = s;
-    uint64_t launches = 0;
-    auto     stage    = [&](const void* in, const void* un, void* out, int mode, const double* dts) -> amr_status {
-        st.in      = static_cast<const double*>(in);
-        st.un      = static_cast<const double*>(un);
-        st.out     = static_cast<double*>(out);
-        st.mode    = mode;
-        st.step_dt = dts;
-        AMR_CUDA(ssprk_stage(st));
-        ++launches;
-        return AMR_OK;
-    };
-    bool   first = true;
-    size_t done  = 0;
-    while (done < steps || (first && steps == 0)) {
-        // CFL steps of this chunk (as amr_tree_advance: the finest level,
-        // clamped to the remaining time), and the time bookkeeping
-        const int chunk = static_cast<int>(std::min(t->coef_steps, steps - done));
-        k_batch_begin<<<K, 256, 0, s>>>(t->maxlev, t->g, t->vel, cfl, chunk, first ? BATCH_RESET : BATCH_CONTINUE,
-                                        remaining, t->dts(), t->step_dt, t->coef, t->coef32, t->upcode);
-        AMR_LAUNCHED("k_batch_begin");
-        first = false;
-        for (int k = 0; k < chunk; ++k) {
-            const double* dts = t->step_dt + static_cast<size_t>(k) * K;
-            // (a step past the time limit, step size 0, changes nothing:
-            // no halo, and every stage copies)
-            if (amr_status hs = halo_buffer(t, t->cur, dts); hs != AMR_OK) return hs;
-            amr_status rs = AMR_OK;
-            if (order == 2) {
-                if ((rs = stage(t->cur, t->cur, t->stage_buf, 0, dts)) != AMR_OK) return rs;
-                if ((rs = halo_buffer(t, t->stage_buf, dts)) != AMR_OK) return rs;
-                if ((rs = stage(t->stage_buf, t->cur, t->nxt, 2, dts)) != AMR_OK) return rs;
-            } else {
-                if ((rs = stage(t->cur, t->cur, t->nxt, 0, dts)) != AMR_OK) return rs;
-                if ((rs = halo_buffer(t, t->nxt, dts)) != AMR_OK) return rs;
-                if ((rs = stage(t->nxt, t->cur, t->stage_buf, 31, dts)) != AMR_OK) return rs;
-                if ((rs = halo_buffer(t, t->stage_buf, dts)) != AMR_OK) return rs;
-                if ((rs = stage(t->stage_buf, t->cur, t->nxt, 32, dts)) != AMR_OK) return rs;
-            }
-            std::swap(t->cur, t->nxt);
-        }
-        done += chunk;
-        if (steps == 0) break;
-    }
-    g_launches.fetch_add(launches, std::memory_order_relaxed);
-    // the buffer's ghost cells hold the last stage's combination, which is
-    // what the reference's tree holds between steps (no halo exchange follows
-    // the last stage); criteria read them from the buffer as it does
-    t->ghosts_valid = true;
-    t->batch_open   = true;
-    return AMR_OK;
-}
-
-amr_status amr_tree_dg_set_equation(amr_tree* t, int equation)
-{
-    if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    if (equation != AMR_DG_ADVECTION && equation != AMR_DG_EULER) return fail(AMR_ERR_INVALID, "unknown DG equation");
-    if (equation == AMR_DG_EULER) {
-        if (!t->dg_scalars) AMR_CUDA(cudaMalloc(&t->dg_scalars, 2 * sizeof(double)));
-        if (!t->dg_dtmin) {
-            AMR_CUDA(cudaMalloc(&t->dg_dtmin, sizeof(unsigned long long)));
-            const unsigned long long inf = 0x7ff0000000000000ull; // +inf: no patch seen
-            if (const cudaError_t e = cudaMemcpy(t->dg_dtmin, &inf, sizeof inf, cudaMemcpyHostToDevice);
-                e != cudaSuccess) {
-                cudaFree(t->dg_dtmin);
-                t->dg_dtmin = nullptr;
-                return cuda_fail(e, "amr_tree_dg_set_equation");
-            }
-        }
-    }
-    t->dg_equation = equation;
-    return AMR_OK;
-}
-
-namespace
-{
-// DG Euler steps: the step size lives on the device, set per step from the
-// patches' wave speeds (solver.hpp:227-234), so the host reads it back once
-// per call
-amr_status dg_euler_advance(amr_tree* t, const DgStage& st, size_t steps, double* dt, double* time)
-{
-    cudaStream_t         s    = t->stream;
-    const Geo&           g    = t->g;
-    const amr_halo_meta* meta = t->meta[t->tb];
-    if (t->dg_prims_cap < t->cap) {
-        cudaFree(t->dg_prims);
-        t->dg_prims     = nullptr;
-        t->dg_prims_cap = 0;
-        AMR_CUDA(cudaMalloc(&t->dg_prims, 14 * t->fstride() * sizeof(double)));
-        t->dg_prims_cap = t->cap;
-    }
-    double* hp = static_cast<double*>(t->pinned);
-    hp[0]      = *dt;
-    hp[1]      = time ? *time : 0.0;
-    AMR_CUDA(cudaMemcpyAsync(t->dg_scalars, hp, 2 * sizeof(double), cudaMemcpyHostToDevice, s));
-    DgEulerStage es{};
-    es.prims   = t->dg_prims;
-    es.keys    = st.keys;
-    es.P       = st.P;
-    es.g       = g;
-    es.fstride = st.fstride;
-    es.dt      = t->dg_scalars;
-    es.dt_min  = t->dg_dtmin;
-    es.stream  = s;
-    uint64_t launches = 0;
-    for (size_t k = 0; k < steps; ++k) {
-        AMR_CUDA(dg_halo(static_cast<double*>(t->cur), meta, st.P, g, st.fstride, s));
-        AMR_CUDA(dg_euler_prims(static_cast<const double*>(t->cur), t->dg_prims, st.P, g, st.fstride, s));
-        es.in   = static_cast<const double*>(t->cur);
-        es.un   = static_cast<const double*>(t->cur);
-        es.out  = static_cast<double*>(t->nxt);
-        es.mode = 0;
-        AMR_CUDA(dg_euler_stage(es));
-        AMR_CUDA(dg_halo(static_cast<double*>(t->nxt), meta, st.P, g, st.fstride, s));
-        AMR_CUDA(dg_euler_prims(static_cast<const double*>(t->nxt), t->dg_prims, st.P, g, st.fstride, s));
-        es.in   = static_cast<const double*>(t->nxt);
-        es.out  = static_cast<double*>(t->cur); // u^n is read and replaced cell by cell
-        es.mode = 1;
-        AMR_CUDA(dg_euler_stage(es));
-        AMR_CUDA(dg_euler_next(t->dg_scalars, t->dg_scalars + 1, t->dg_dtmin, s));
-        launches += 7;
-    }
-    AMR_CUDA(cudaMemcpyAsync(hp, t->dg_scalars, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    AMR_CUDA(cudaStreamSynchronize(s));
-    g_launches.fetch_add(launches, std::memory_order_relaxed);
-    t->ghosts_valid = true;
-    *dt             = hp[0];
-    if (time) *time = hp[1];
-    return AMR_OK;
-}
-} // namespace
-
-amr_status amr_tree_dg_advance(amr_tree* t, size_t steps, double* dt, double* time)
-{
-    if (!t || !dt) return fail(AMR_ERR_INVALID, "null argument");
-    const Geo& g = t->g;
-    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
-        return fail(AMR_ERR_INVALID, "the DG advance needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
-    if (!(*dt > 0.0)) return fail(AMR_ERR_INVALID, "the DG step size must be positive");
-    cudaStream_t s = t->stream;
-    DgStage      st{};
-    st.keys    = t->keys[t->tb];
-    st.P       = static_cast<int>(t->size);
-    st.g       = g;
-    st.fstride = t->fstride();
-    st.stream  = s;
-    if (t->dg_equation == AMR_DG_EULER) return dg_euler_advance(t, st, steps, dt, time);
-    // CFL step of the finest cells (solver.hpp:227-234 with |v| = 1)
-    const double edge   = (1.0 / static_cast<double>(1u << t->max_level_host)) / static_cast<double>(kDgPatch);
-    const double scale  = 1.0 / (std::pow(static_cast<double>(kDgOrder), 2.0) + 1.0);
-    const double dt_cfl = scale * 0.5 * edge / 1.0;
-    double       h      = *dt, acc = time ? *time : 0.0;
-    uint64_t     launches = 0;
-    const amr_halo_meta* meta = t->meta[t->tb];
-    for (size_t k = 0; k < steps; ++k) {
-        AMR_CUDA(dg_halo(static_cast<double*>(t->cur), meta, st.P, g, st.fstride, s));
-        st.in   = static_cast<const double*>(t->cur);
-        st.un   = static_cast<const double*>(t->cur);
-        st.out  = static_cast<double*>(t->nxt);
-        st.dt   = h;
-        st.mode = 0;
-        AMR_CUDA(dg_stage(st));
-        AMR_CUDA(dg_halo(static_cast<double*>(t->nxt), meta, st.P, g, st.fstride, s));
-        st.in   = static_cast<const double*>(t->nxt);
-        st.out  = static_cast<double*>(t->cur); // u^n is read and replaced cell by cell
-        st.mode = 1;
-        AMR_CUDA(dg_stage(st));
-        launches += 4;
-        h = std::min(h, std::min(h, dt_cfl));
-        acc += h; // the reference's loop adds the updated step (solver.hpp:129, 134)
-    }
-    g_launches.fetch_add(launches, std::memory_order_relaxed);
-    t->ghosts_valid = true; // the ghosts the reference's tree holds after a step
-    *dt             = h;
-    if (time) *time = acc;
-    return AMR_OK;
-}
-
-amr_status amr_tree_dg_remesh(amr_tree* t, double refine_threshold, double coarsen_threshold, int* changed)
-{
-    if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    const Geo& g = t->g;
-    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
-        return fail(AMR_ERR_INVALID, "the DG re-mesh needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
-    AMR_CUDA(dg_flags(static_cast<const double*>(t->cur), static_cast<int>(t->size), g, t->fstride(),
-                      refine_threshold, coarsen_threshold, t->flags, t->stream));
-    g_launches.fetch_add(1, std::memory_order_relaxed);
-    t->dg_state         = true;
-    const amr_status st = amr_tree_remesh(t, changed);
-    t->dg_state         = false;
-    return st;
-}
-
-amr_status amr_tree_dg_write_vtk(amr_tree* t, const char* path)
-{
-    if (!t || !path) return fail(AMR_ERR_INVALID, "null argument");
-    const Geo& g = t->g;
-    if (g.rank != 2 || g.n != kDgPatch || g.h != 1 || t->nvar != kDgFields || t->dtype != AMR_F64)
-        return fail(AMR_ERR_INVALID, "the DG printer needs a 2D FP64 tree of 4x4 patches, one ghost cell, 16 fields");
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    std::string      err;
-    uint64_t         launches = 0;
-    const amr_status st = dg_write_vtk(t->keys[t->tb], static_cast<const double*>(t->cur), t->size, g, t->fstride(),
-                                       t->stream, path, err, launches);
-    g_launches.fetch_add(launches, std::memory_order_relaxed);
-    if (st != AMR_OK) return fail(st, err);
-    return AMR_OK;
-}
-
-amr_status amr_tree_dg_run(amr_tree* t, double initial_dt, double end_time, int amr_interval,
-                           double refine_threshold, double coarsen_threshold, amr_dg_stats* stats)
-{
-    if (!t || !stats || amr_interval < 0) return fail(AMR_ERR_INVALID, "bad argument");
-    *stats                = amr_dg_stats{};
-    double    dt          = initial_dt, time = 0.0;
-    long long step        = 0, next_amr = 0;
-    size_t    leaves_max  = t->size;
-    while (time < end_time) {
-        stats->cells += static_cast<uint64_t>(t->size) * kDgPatch * kDgPatch;
-        if (amr_status st = amr_tree_dg_advance(t, 1, &dt, &time); st != AMR_OK) return st;
-        ++step;
-        if (step >= next_amr) { // apply_amr (solver.hpp:249-251): an interval of 0 re-meshes every step
-            int changed = 0;
-            if (amr_status st = amr_tree_dg_remesh(t, refine_threshold, coarsen_threshold, &changed); st != AMR_OK)
-                return st;
-            ++stats->remeshes;
-            next_amr   = step + amr_interval;
-            leaves_max = std::max(leaves_max, t->size);
-        }
-    }
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    stats->steps      = static_cast<uint64_t>(step);
-    stats->time       = time;
-    stats->next_dt    = dt;
-    stats->leaves_max = static_cast<uint64_t>(leaves_max);
-    return AMR_OK;
 }
 
 amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed)
@@ -2463,400 +1943,7 @@ amr_status amr_tree_instance_time(amr_tree* t, double* sum_dt, uint32_t* execute
 
 } // extern "C"
 
-struct amr_adjoint {
-    amr_tree*          t = nullptr;
-    size_t             steps = 0, every = 1, nseg = 0;
-    double             vel3[3] = { 0, 0, 0 };
-    bool               per_instance = false;
-    double             cfl = 0.0, remaining = 0.0;
-    uint64_t           topo = 0;
-    std::vector<void*> ckpt;    // nseg + 1 states
-    double*            dts = nullptr; // steps * ninst step sizes
-    double*            vel = nullptr; // velocities of the run (3 per instance)
-    void*              lam[2]{};
-    bool               forward_done = false;
-};
-
-namespace {
-void free_adjoint(amr_adjoint* a)
-{
-    if (!a) return;
-    for (void* c : a->ckpt) cudaFree(c);
-    cudaFree(a->dts);
-    cudaFree(a->vel);
-    cudaFree(a->lam[0]);
-    cudaFree(a->lam[1]);
-    delete a;
-}
-} // namespace
-
 extern "C" {
-
-amr_status amr_adjoint_create(amr_tree* t, size_t steps, const double* velocity3, double cfl, double remaining,
-                              size_t every, amr_adjoint** out)
-{
-    if (!t || !out) return fail(AMR_ERR_INVALID, "null argument");
-    *out = nullptr;
-    if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the adjoint takes a one-field tree");
-    if (every < 1 || every > t->coef_steps) return fail(AMR_ERR_INVALID, "checkpoint interval out of range");
-    if (!velocity3 && !t->vel_inst_set) return fail(AMR_ERR_INVALID, "no velocity given and none set per instance");
-    amr_adjoint* a = new amr_adjoint();
-    a->t           = t;
-    a->steps       = steps;
-    a->every       = every;
-    a->nseg        = (steps + every - 1) / every;
-    a->cfl         = cfl;
-    a->remaining   = remaining;
-    a->topo        = t->topo;
-    a->per_instance = velocity3 == nullptr;
-    if (velocity3)
-        for (int k = 0; k < 3; ++k) a->vel3[k] = velocity3[k];
-    const size_t bytes = t->cap * t->g.flat * t->esize; // room for the tree's capacity
-    const size_t K     = static_cast<size_t>(t->ninst);
-    cudaError_t  e     = cudaSuccess;
-    a->ckpt.assign(a->nseg + 1, nullptr);
-    for (auto& c : a->ckpt)
-        if (e == cudaSuccess) e = cudaMalloc(&c, t->size * t->g.flat * t->esize);
-    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a->dts), std::max<size_t>(1, steps) * K * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a->vel), 3 * K * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&a->lam[0], bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&a->lam[1], bytes);
-    if (e != cudaSuccess) {
-        free_adjoint(a);
-        return cuda_fail(e, "amr_adjoint_create allocation");
-    }
-    *out = a;
-    return AMR_OK;
-}
-
-amr_status amr_adjoint_destroy(amr_adjoint* a)
-{
-    if (!a) return AMR_OK;
-    cudaStreamSynchronize(a->t->stream);
-    free_adjoint(a);
-    return AMR_OK;
-}
-
-amr_status amr_adjoint_checkpoint_count(const amr_adjoint* a, size_t* count)
-{
-    if (!a || !count) return fail(AMR_ERR_INVALID, "null argument");
-    *count = a->ckpt.size();
-    return AMR_OK;
-}
-
-amr_status amr_adjoint_forward(amr_adjoint* a)
-{
-    if (!a) return fail(AMR_ERR_INVALID, "null argument");
-    amr_tree* t = a->t;
-    if (t->topo != a->topo) return fail(AMR_ERR_INVALID, "the tree was re-meshed after the adjoint was created");
-    cudaStream_t s     = t->stream;
-    const size_t bytes = t->size * t->g.flat * t->esize;
-    const size_t K     = static_cast<size_t>(t->ninst);
-    AMR_CUDA(cudaMemcpyAsync(a->ckpt[0], t->cur, bytes, cudaMemcpyDeviceToDevice, s));
-    for (size_t m = 0; m < a->nseg; ++m) {
-        const size_t k  = std::min(a->every, a->steps - m * a->every);
-        amr_status   st = advance_impl(t, k, a->per_instance ? nullptr : a->vel3, a->cfl, a->remaining,
-                                       m == 0 ? BATCH_RESET : BATCH_CONTINUE);
-        if (st != AMR_OK) return st;
-        if (m == 0) // velocities in use (per instance)
-            AMR_CUDA(cudaMemcpyAsync(a->vel, t->vel, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        AMR_CUDA(cudaMemcpyAsync(a->dts + m * a->every * K, t->step_dt, k * K * sizeof(double),
-                                 cudaMemcpyDeviceToDevice, s));
-        AMR_CUDA(cudaMemcpyAsync(a->ckpt[m + 1], t->cur, bytes, cudaMemcpyDeviceToDevice, s));
-    }
-    if (a->nseg == 0 && a->per_instance)
-        AMR_CUDA(cudaMemcpyAsync(a->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    AMR_CUDA(cudaStreamSynchronize(s));
-    int32_t wait_err = 0;
-    AMR_CUDA(cudaMemcpy(&wait_err, t->status + 7, sizeof wait_err, cudaMemcpyDeviceToHost));
-    if (wait_err) {
-        AMR_CUDA(cudaMemset(t->status + 7, 0, sizeof(int32_t)));
-        return fail(AMR_ERR_TIMEOUT, "a bulk copy did not complete within the wait limit");
-    }
-    a->forward_done = true;
-    return AMR_OK;
-}
-
-} // extern "C"
-
-namespace {
-// The reverse sweep on the adjoint's own buffers: lambda_T in lam[0] on
-// entry; returns the index of the buffer holding lambda_0.
-amr_status adjoint_sweep(amr_adjoint* a, int* result)
-{
-    amr_tree*       t     = a->t;
-    cudaStream_t    s     = t->stream;
-    const Geo&      g     = t->g;
-    const int       P     = static_cast<int>(t->size);
-    const int       K     = t->ninst;
-    const int       nl    = g.depth + 1;
-    const size_t    bytes = static_cast<size_t>(P) * g.flat * t->esize;
-    const long long total = static_cast<long long>(P) * g.flat;
-    int up[3] = { 0, 0, 0 };
-    if (!a->per_instance)
-        for (int k = 0; k < g.rank; ++k) up[k] = a->vel3[k] > 0.0 ? -1 : (a->vel3[k] < 0.0 ? 1 : 0);
-    const double*  vleaf = a->per_instance ? a->vel : nullptr;
-    const int      ppb   = std::max(1, 256 / g.cells);
-    const unsigned grid  = grid_for(P, ppb);
-    int            cur   = 0;
-    amr_status     st    = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
-        using T = decltype(z);
-        AMR_CUDA(cudaMemsetAsync(a->lam[1], 0, bytes, s));
-        const unsigned zg = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 32));
-        k_zero_ghosts<T><<<zg, 256, 0, s>>>(static_cast<T*>(a->lam[0]), total, g);
-        AMR_LAUNCHED("k_zero_ghosts");
-        for (size_t m = a->nseg; m-- > 0;) {
-            const int k = static_cast<int>(std::min(a->every, a->steps - m * a->every));
-            k_coef_from_dt<<<grid_for(static_cast<long long>(k) * K * nl, 256), 256, 0, s>>>(
-                a->dts + m * a->every * K, g, a->vel, k, K, t->coef);
-            AMR_LAUNCHED("k_coef_from_dt");
-            for (int j = k - 1; j >= 0; --j) {
-                const Coef* cf = t->coef + static_cast<size_t>(j) * K * nl;
-                k_adjoint<T><<<grid, 256, 0, s>>>(static_cast<const T*>(a->lam[cur]), static_cast<T*>(a->lam[cur ^ 1]),
-                                                  t->meta[t->tb], t->keys[t->tb], P, g, cf, up[0], up[1], up[2],
-                                                  vleaf, ppb);
-                AMR_LAUNCHED("k_adjoint");
-                cur ^= 1;
-            }
-        }
-        return AMR_OK;
-    });
-    *result = cur;
-    return st;
-}
-
-amr_status adjoint_ready(amr_adjoint* a)
-{
-    if (a->t->topo != a->topo) return fail(AMR_ERR_INVALID, "the tree was re-meshed after the adjoint was created");
-    if (!a->forward_done) return fail(AMR_ERR_INVALID, "amr_adjoint_forward has not run");
-    return AMR_OK;
-}
-} // namespace
-
-extern "C" {
-
-amr_status amr_adjoint_backward(amr_adjoint* a, const void* lam_T, void* lam_0)
-{
-    if (!a || !lam_T || !lam_0) return fail(AMR_ERR_INVALID, "null argument");
-    amr_status st = adjoint_ready(a);
-    if (st != AMR_OK) return st;
-    amr_tree*    t     = a->t;
-    const size_t bytes = t->size * t->g.flat * t->esize;
-    AMR_CUDA(cudaMemcpyAsync(a->lam[0], lam_T, bytes, cudaMemcpyDeviceToDevice, t->stream));
-    int res = 0;
-    st      = adjoint_sweep(a, &res);
-    if (st != AMR_OK) return st;
-    AMR_CUDA(cudaMemcpyAsync(lam_0, a->lam[res], bytes, cudaMemcpyDeviceToDevice, t->stream));
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    return AMR_OK;
-}
-
-amr_status amr_adjoint_backward_host(amr_adjoint* a, const void* lam_T, void* lam_0)
-{
-    if (!a || !lam_T || !lam_0) return fail(AMR_ERR_INVALID, "null argument");
-    amr_status st = adjoint_ready(a);
-    if (st != AMR_OK) return st;
-    amr_tree*    t     = a->t;
-    const size_t bytes = t->size * t->g.flat * t->esize;
-    AMR_CUDA(cudaMemcpyAsync(a->lam[0], lam_T, bytes, cudaMemcpyHostToDevice, t->stream));
-    int res = 0;
-    st      = adjoint_sweep(a, &res);
-    if (st != AMR_OK) return st;
-    AMR_CUDA(cudaMemcpyAsync(lam_0, a->lam[res], bytes, cudaMemcpyDeviceToHost, t->stream));
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    return AMR_OK;
-}
-
-amr_status amr_adjoint_checkpoint(amr_adjoint* a, size_t index, void* dst)
-{
-    if (!a || !dst) return fail(AMR_ERR_INVALID, "null argument");
-    if (index >= a->ckpt.size()) return fail(AMR_ERR_INVALID, "checkpoint index out of range");
-    if (!a->forward_done) return fail(AMR_ERR_INVALID, "amr_adjoint_forward has not run");
-    amr_tree* t = a->t;
-    AMR_CUDA(cudaMemcpyAsync(dst, a->ckpt[index], t->size * t->g.flat * t->esize, cudaMemcpyDeviceToDevice, t->stream));
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    return AMR_OK;
-}
-
-amr_status amr_selftest_wait_timeout(int32_t polls, amr_status* observed)
-{
-    if (polls < 1) return fail(AMR_ERR_INVALID, "polls must be positive");
-    int32_t* d = nullptr;
-    AMR_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), 2 * sizeof(int32_t)));
-    int32_t h[2] = { -1, 0 };
-    cudaError_t e = cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-        k_selftest_wait<<<1, 32>>>(d, polls);
-        g_launches.fetch_add(1);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        k_selftest_touch<<<1, 1>>>(d);
-        g_launches.fetch_add(1);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
-    cudaFree(d);
-    if (e != cudaSuccess) return cuda_fail(e, "amr_selftest_wait_timeout");
-    if (observed) *observed = static_cast<amr_status>(h[0]);
-    if (h[1] != 1) return fail(AMR_ERR_CUDA, "the context did not run the follow-up kernel");
-    if (h[0] != AMR_ERR_TIMEOUT) return fail(AMR_ERR_INVALID, "the wait did not time out");
-    return AMR_OK;
-}
-
-// ------------------------------------------------------------------ Euler
-static amr_status euler_check(amr_tree* t)
-{
-    if (!t) return fail(AMR_ERR_INVALID, "null argument");
-    if (t->nvar != t->g.rank + 2) return fail(AMR_ERR_INVALID, "the Euler solver takes a tree of rank + 2 fields");
-    if (t->dtype != AMR_F64) return fail(AMR_ERR_INVALID, "the Euler solver is FP64");
-    if (!euler_supported(t->g)) return fail(AMR_ERR_INVALID, "patch too large for the Euler update");
-    return AMR_OK;
-}
-
-static amr_status euler_advance_impl(amr_tree* t, size_t steps, double gamma, double cfl, double remaining)
-{
-    const size_t prim_elems = static_cast<size_t>(t->g.rank * (t->g.rank + 2)) * t->fstride();
-    if (t->prim_cap != t->cap) {
-        cudaFree(t->prim[0]);
-        cudaFree(t->prim[1]);
-        t->prim[0] = t->prim[1] = nullptr;
-        t->prim_cap = 0;
-        AMR_CUDA(cudaMalloc(&t->prim[0], prim_elems * sizeof(double)));
-        AMR_CUDA(cudaMalloc(&t->prim[1], prim_elems * sizeof(double)));
-        t->prim_cap = t->cap;
-    }
-    if (!t->ghosts_valid) {
-        amr_status s = launch_halo(t);
-        if (s != AMR_OK) return s;
-    }
-    EulerBufs b{};
-    b.g        = t->g;
-    b.P        = static_cast<int>(t->size);
-    b.fstride  = t->fstride();
-    b.levels   = t->levels[t->tb];
-    b.meta     = t->meta[t->tb];
-    b.state[0] = static_cast<double*>(t->sbuf[0]);
-    b.state[1] = static_cast<double*>(t->sbuf[1]);
-    b.prim[0]  = t->prim[0];
-    b.prim[1]  = t->prim[1];
-    b.min_slot = t->euler_min;
-    b.step_dt  = t->euler_dt;
-    b.ctl      = t->euler_ctl;
-    b.acc      = t->dt_acc;
-    b.rem      = t->dt_rem;
-    b.cnt      = t->dt_cnt;
-    b.stream   = t->stream;
-    int      cur      = t->cur == t->sbuf[0] ? 0 : 1;
-    uint64_t launches = 0;
-    cudaError_t e = euler_begin(b, cur, gamma, remaining, &launches);
-    for (size_t k = 0; k < steps && e == cudaSuccess; ++k) {
-        std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
-        if (t->timing) { // opt-in timing of the update kernel
-            if (t->events_used == t->events.size()) {
-                std::pair<cudaEvent_t, cudaEvent_t> pe;
-                AMR_CUDA(cudaEventCreate(&pe.first));
-                AMR_CUDA(cudaEventCreate(&pe.second));
-                t->events.push_back(pe);
-                t->event_cells.push_back(0);
-            }
-            ev = &t->events[t->events_used];
-            t->event_cells[t->events_used] = static_cast<uint64_t>(b.P) * t->g.cells;
-            ++t->events_used;
-        }
-        e = euler_step(b, cur, static_cast<int>(k & 1), gamma, cfl, &launches, ev ? ev->first : nullptr,
-                       ev ? ev->second : nullptr);
-        cur ^= 1;
-    }
-    g_launches.fetch_add(launches, std::memory_order_relaxed);
-    if (e != cudaSuccess) return cuda_fail(e, "Euler step");
-    t->cur          = t->sbuf[cur];
-    t->nxt          = t->sbuf[cur ^ 1];
-    t->ghosts_valid = true; // the last step's halo filled every field
-    t->batch_open   = true;
-    return AMR_OK;
-}
-
-amr_status amr_tree_euler_advance(amr_tree* t, size_t steps, double gamma, double cfl, double remaining)
-{
-    if (amr_status s = euler_check(t); s != AMR_OK) return s;
-    return euler_advance_impl(t, steps, gamma, cfl, remaining);
-}
-
-amr_status amr_tree_euler_run(amr_tree* t, const amr_euler_params* p, amr_cycle_stats* out)
-{
-    if (amr_status s = euler_check(t); s != AMR_OK) return s;
-    if (!p) return fail(AMR_ERR_INVALID, "null argument");
-    if (p->remesh_interval < 1) return fail(AMR_ERR_INVALID, "re-mesh interval must be positive");
-    RunTotals tot;
-    double    time = 0.0;
-    while (tot.done < static_cast<long long>(p->steps) && time < p->end_time) {
-        const size_t k = static_cast<size_t>(
-            std::min<long long>(static_cast<long long>(p->remesh_interval), static_cast<long long>(p->steps) - tot.done));
-        const size_t leaves = t->size;
-        amr_status   st     = euler_advance_impl(t, k, p->gamma, p->cfl, p->end_time - time);
-        if (st != AMR_OK) return st;
-        // the benchmark's criterion: max Rho over the patch, then re-mesh
-        st = amr_tree_flags_max(t, p->refine_threshold, p->coarsen_threshold, p->min_level, p->max_level);
-        if (st != AMR_OK) return st;
-        int changed = 0;
-        st          = amr_tree_remesh(t, &changed);
-        if (st != AMR_OK) return st;
-        ++tot.remeshes;
-        double acc = 0.0;
-        size_t ex  = 0;
-        st         = amr_tree_finish_advance(t, &acc, &ex);
-        if (st != AMR_OK) return st;
-        time += acc;
-        tot.done += static_cast<long long>(ex);
-        tot.executed += ex;
-        tot.cells += static_cast<uint64_t>(ex) * leaves * t->g.cells;
-        ++tot.intervals;
-        tot.leaves_sum += leaves;
-        tot.lmin = std::min<uint64_t>(tot.lmin, leaves);
-        tot.lmax = std::max<uint64_t>(tot.lmax, leaves);
-        if (ex == 0) break;
-    }
-    if (!t->ghosts_valid) {
-        amr_status s = launch_halo(t);
-        if (s != AMR_OK) return s;
-    }
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    if (out) {
-        std::memset(out, 0, sizeof(*out));
-        out->executed_steps = tot.executed;
-        out->sum_dt         = time;
-        out->cell_updates   = tot.cells;
-        out->remeshes       = tot.remeshes;
-        out->intervals      = tot.intervals;
-        out->leaves_min     = tot.intervals ? tot.lmin : t->size;
-        out->leaves_max     = tot.intervals ? tot.lmax : t->size;
-        out->leaves_mean    = tot.intervals ? static_cast<double>(tot.leaves_sum) / tot.intervals : 0.0;
-    }
-    return AMR_OK;
-}
-
-amr_status amr_tree_write_vtk(amr_tree* t, const char* path, const char* field_name)
-{
-    if (!t || !path) return fail(AMR_ERR_INVALID, "null argument");
-    VtkTree v{};
-    v.g     = t->g;
-    for (int a = 0; a < 3; ++a) v.dom.lengths[a] = t->lengths[a];
-    v.keys   = t->keys[t->tb];
-    v.state  = t->cur;
-    v.size   = t->size;
-    v.esize  = t->esize;
-    v.nvar   = t->nvar;
-    v.fstride = t->fstride();
-    v.stream = t->stream;
-    AMR_CUDA(cudaStreamSynchronize(t->stream));
-    std::string      err;
-    const amr_status st = vtk_write(v, path, field_name ? field_name : "Scalar", err);
-    // five section kernels, and one per field, per chunk of 2^22 cells
-    g_launches.fetch_add((5 + t->nvar) * std::max<uint64_t>(1, (t->size * t->g.cells + (1ull << 22) - 1) >> 22));
-    if (st != AMR_OK) return fail(st, err);
-    return AMR_OK;
-}
 
 amr_status amr_tree_step_config(const amr_tree* t, int32_t* warps, int32_t* stages, int32_t* blocks)
 {
@@ -2901,250 +1988,3 @@ amr_status amr_tree_synchronize(amr_tree* t)
 }
 
 } // extern "C"
-
-// ------------------------------------------------------------ drop-ins
-
-namespace {
-
-template <typename T>
-amr_status halo_dropin(T* patches, const amr_halo_meta* meta, size_t meta_count, size_t num,
-                              const amr_patch_geometry* geom, void* stream)
-{
-    Geo g;
-    if (!patches || !meta || !make_geo(geom, g)) return fail(AMR_ERR_INVALID, "bad argument");
-    // the reference validates metadata_count == P * 2 * rank (halo_exchange.cu:363-367)
-    if (meta_count != num * static_cast<size_t>(g.ndir)) return fail(AMR_ERR_INVALID, "metadata count mismatch");
-    if (num == 0) return AMR_OK;
-    const long long total = static_cast<long long>(num) * g.ndir * g.h * (g.cells / g.n);
-    const unsigned  grid  = static_cast<unsigned>(std::min<long long>(grid_for(total, 256), 152LL * 64));
-    k_halo<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(patches, meta, total, g);
-    AMR_LAUNCHED("k_halo");
-    return AMR_OK;
-}
-
-amr_status intergrid_dropin(double* p, const amr_transfer_task* tasks, size_t n,
-                                   const amr_patch_geometry* geom, void* stream, int mode)
-{
-    Geo g;
-    if (!p || (!tasks && n) || !make_geo(geom, g)) return fail(AMR_ERR_INVALID, "bad argument");
-    if (n == 0) return AMR_OK;
-    k_intergrid<double><<<static_cast<unsigned>(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        p, tasks, static_cast<int>(n), g, mode);
-    AMR_LAUNCHED("k_intergrid");
-    return AMR_OK;
-}
-
-} // namespace
-
-extern "C" {
-
-amr_status amr_halo_exchange_f64(double* p, const amr_halo_meta* m, size_t mc, size_t num,
-                                 const amr_patch_geometry* geom, void* stream)
-{
-    return halo_dropin<double>(p, m, mc, num, geom, stream);
-}
-
-amr_status amr_halo_exchange_f32(float* p, const amr_halo_meta* m, size_t mc, size_t num,
-                                 const amr_patch_geometry* geom, void* stream)
-{
-    return halo_dropin<float>(p, m, mc, num, geom, stream);
-}
-
-amr_status amr_interpolate_patches_f64(double* p, const amr_transfer_task* tasks, size_t n,
-                                       const amr_patch_geometry* geom, void* stream)
-{
-    return intergrid_dropin(p, tasks, n, geom, stream, 0);
-}
-
-amr_status amr_restrict_patches_f64(double* p, const amr_transfer_task* tasks, size_t n,
-                                    const amr_patch_geometry* geom, void* stream)
-{
-    return intergrid_dropin(p, tasks, n, geom, stream, 1);
-}
-
-amr_status amr_gather_patches(void* dst, const void* src, size_t patch_bytes, const int32_t* sources, size_t count,
-                              void* stream)
-{
-    if (!dst || !src || (!sources && count) || patch_bytes == 0) return fail(AMR_ERR_INVALID, "bad argument");
-    if (count == 0) return AMR_OK;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const bool aligned = patch_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(dst) % 16 == 0 &&
-                         reinterpret_cast<uintptr_t>(src) % 16 == 0;
-    if (aligned) {
-        k_gather<<<static_cast<unsigned>(count), 256, 0, s>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst),
-                                                             patch_bytes / 16, sources, static_cast<int>(count));
-    } else {
-        k_gather_bytes<<<static_cast<unsigned>(count), 256, 0, s>>>(static_cast<const unsigned char*>(src),
-                                                                   static_cast<unsigned char*>(dst), patch_bytes,
-                                                                   sources, static_cast<int>(count));
-    }
-    AMR_LAUNCHED("k_gather");
-    return AMR_OK;
-}
-
-amr_status amr_compute_step_dt(const int32_t* levels, size_t num, const amr_patch_geometry* geom,
-                               const double* v, double cfl, double* dt, double* acc, double* remaining,
-                               uint32_t* count, void* stream)
-{
-    Geo g;
-    if (!levels || !v || !dt || !acc || !remaining || !count || !make_geo(geom, g) || num == 0)
-        return fail(AMR_ERR_INVALID, "bad argument");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // the maximum level lands in *dt first, then the finalize kernel reads it
-    int32_t* lmax = reinterpret_cast<int32_t*>(dt);
-    AMR_CUDA(cudaMemsetAsync(lmax, 0, sizeof(int32_t), s));
-    k_max_level<<<std::min<unsigned>(grid_for(static_cast<long long>(num), 256), 1024), 256, 0, s>>>(
-        levels, static_cast<int>(num), lmax);
-    AMR_LAUNCHED("k_max_level");
-    k_finalize_dt<<<1, 1, 0, s>>>(lmax, g, v[0], v[1], v[2], cfl, dt, acc, remaining, count);
-    AMR_LAUNCHED("k_finalize_dt");
-    return AMR_OK;
-}
-
-amr_status amr_time_step_f64(const double* in, double* out, const int32_t* levels, size_t num,
-                             const amr_patch_geometry* geom, const double* v, const double* dt, void* stream)
-{
-    Geo g;
-    if (!in || !out || !levels || !v || !dt || !make_geo(geom, g)) return fail(AMR_ERR_INVALID, "bad argument");
-    if (num == 0) return AMR_OK;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    int          up[3] = { 0, 0, 0 };
-    for (int a = 0; a < g.rank; ++a) up[a] = v[a] > 0.0 ? -1 : (v[a] < 0.0 ? 1 : 0);
-    const int ppb = std::min(64, std::max(1, 256 / g.cells));
-    k_step<double, false, true><<<grid_for(static_cast<long long>(num), ppb), 256, 0, s>>>(
-        in, out, levels, nullptr, static_cast<int>(num), g, nullptr, up[0], up[1], up[2], ppb, dt, v[0], v[1], v[2]);
-    AMR_LAUNCHED("k_step");
-    return AMR_OK;
-}
-
-amr_status amr_flags_max_f64(const double* patches, const int32_t* levels, size_t num, const amr_patch_geometry* geom,
-                             double rthr, double cthr, int min_level, int max_level, int8_t* flags, void* stream)
-{
-    Geo g;
-    if (!patches || !levels || !flags || !make_geo(geom, g)) return fail(AMR_ERR_INVALID, "bad argument");
-    if (num == 0) return AMR_OK;
-    k_flags_max<double><<<static_cast<unsigned>(num), 128, 0, static_cast<cudaStream_t>(stream)>>>(
-        patches, levels, static_cast<int>(num), g, rthr, cthr, min_level, max_level, flags);
-    AMR_LAUNCHED("k_flags_max");
-    return AMR_OK;
-}
-
-} // extern "C"
-
-// ---------------------------------------------------- allocation-free re-mesh
-// The tree's re-mesh keeps its working arrays in buffers the tree allocated.
-// amr_remesh_noalloc runs the same kernels with those arrays carved out of one
-// file-scope device array instead, for callers that may not allocate.
-namespace {
-
-constexpr size_t kNoAllocMax = AMR_NOALLOC_MAX_LEAVES;
-
-constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// byte offsets of the working arrays inside the scratch array
-constexpr size_t kOffRmark  = 0;
-constexpr size_t kOffChead  = kOffRmark + align256(kNoAllocMax);
-constexpr size_t kOffCnt    = kOffChead + align256(kNoAllocMax);
-constexpr size_t kOffPos    = kOffCnt + align256((kNoAllocMax + 1) * sizeof(uint32_t));
-constexpr size_t kOffSrc    = kOffPos + align256((kNoAllocMax + 1) * sizeof(uint32_t));
-constexpr size_t kOffSkind  = kOffSrc + align256(kNoAllocMax * sizeof(int32_t));
-constexpr size_t kOffStatus = kOffSkind + align256(kNoAllocMax);
-constexpr size_t kOffMaxlev = kOffStatus + 256;
-constexpr size_t kScratchUsed = kOffMaxlev + 256;
-static_assert(kScratchUsed <= AMR_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
-
-} // namespace
-
-// Every GPU that loads the library holds this array until the process exits.
-static __device__ __align__(256) unsigned char g_remesh_scratch[AMR_NOALLOC_SCRATCH_BYTES];
-
-namespace {
-
-// In host code the name g_remesh_scratch is a host-side stand-in, not a
-// device address; the address comes from cudaGetSymbolAddress, looked up once
-// per device with that device current.
-amr_status noalloc_scratch(unsigned char** out)
-{
-    static std::mutex     mu;
-    static unsigned char* per_device[128] = {};
-    int                   dev             = 0;
-    AMR_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 128) return fail(AMR_ERR_INVALID, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(mu);
-    if (!per_device[dev]) {
-        void*       p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_remesh_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_remesh_scratch)");
-        per_device[dev] = static_cast<unsigned char*>(p);
-    }
-    *out = per_device[dev];
-    return AMR_OK;
-}
-
-} // namespace
-
-extern "C" amr_status amr_remesh_noalloc(const amr_patch_geometry* geom, size_t num, const uint64_t* ids_in,
-                                         const amr_halo_meta* meta_in, const int8_t* flags,
-                                         const double* state_in, size_t out_cap, uint64_t* ids_out,
-                                         int32_t* levels_out, amr_halo_meta* meta_out, double* state_out,
-                                         uint32_t* device_out_count, size_t* host_out_count, void* stream)
-{
-    Geo g;
-    if (!make_geo(geom, g)) return fail(AMR_ERR_INVALID, "bad patch geometry");
-    if (!ids_in || !meta_in || !flags || !state_in || !ids_out || !levels_out || !meta_out || !state_out ||
-        !device_out_count)
-        return fail(AMR_ERR_INVALID, "null argument");
-    if (num < 1 || num > kNoAllocMax)
-        return fail(AMR_ERR_INVALID, "amr_remesh_noalloc: num_leaves must be in [1, AMR_NOALLOC_MAX_LEAVES]");
-    if (out_cap < 1 || out_cap > kNoAllocMax)
-        return fail(AMR_ERR_INVALID, "amr_remesh_noalloc: out_capacity must be in [1, AMR_NOALLOC_MAX_LEAVES]");
-    unsigned char* base = nullptr;
-    amr_status     st   = noalloc_scratch(&base);
-    if (st != AMR_OK) return st;
-    uint8_t*  rmark  = base + kOffRmark;
-    uint8_t*  chead  = base + kOffChead;
-    uint32_t* cnt    = reinterpret_cast<uint32_t*>(base + kOffCnt);
-    uint32_t* pos    = reinterpret_cast<uint32_t*>(base + kOffPos);
-    int32_t*  src    = reinterpret_cast<int32_t*>(base + kOffSrc);
-    int8_t*   skind  = reinterpret_cast<int8_t*>(base + kOffSkind);
-    int32_t*  status = reinterpret_cast<int32_t*>(base + kOffStatus);
-    int32_t*  maxlev = reinterpret_cast<int32_t*>(base + kOffMaxlev);
-
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int    P = static_cast<int>(num);
-    // the array keeps the previous call's contents: clear what must start at zero
-    AMR_CUDA(cudaMemsetAsync(status, 0, 8 * sizeof(int32_t), s));
-    AMR_CUDA(cudaMemsetAsync(maxlev, 0, sizeof(int32_t), s));
-    k_mark<<<grid_for(P, 256), 256, 0, s>>>(ids_in, flags, P, g, rmark, chead);
-    AMR_LAUNCHED("k_mark");
-    for (int r = 0; r < std::max(1, g.depth); ++r) {
-        k_closure<<<grid_for(P, 256), 256, 0, s>>>(meta_in, P, g, rmark);
-        AMR_LAUNCHED("k_closure");
-    }
-    k_veto<<<grid_for(P, 256), 256, 0, s>>>(meta_in, P, g, rmark, chead);
-    AMR_LAUNCHED("k_veto");
-    k_count<<<grid_for(P, 256), 256, 0, s>>>(ids_in, rmark, chead, P, g, cnt, status + 1);
-    AMR_LAUNCHED("k_count");
-    k_scan<<<1, 1024, 0, s>>>(cnt, pos, P, out_cap, status);
-    AMR_LAUNCHED("k_scan");
-    int32_t hs[3] = { 0, 0, 0 };
-    AMR_CUDA(cudaMemcpyAsync(hs, status, sizeof hs, cudaMemcpyDeviceToHost, s));
-    AMR_CUDA(cudaStreamSynchronize(s));
-    if (hs[0] != 0) return fail(static_cast<amr_status>(hs[0]), "re-mesh would exceed out_capacity");
-    const int NP = hs[2];
-    k_emit<<<grid_for(P, 256), 256, 0, s>>>(ids_in, rmark, chead, pos, P, g, ids_out, levels_out, src, skind, maxlev);
-    AMR_LAUNCHED("k_emit");
-    k_remap<double><<<NP, 256, 0, s>>>(state_in, state_out, src, skind, NP, g);
-    AMR_LAUNCHED("k_remap");
-    k_neighbors<<<grid_for(static_cast<long long>(NP) * g.ndir, 128), 128, 0, s>>>(ids_out, NP, g, meta_out, status);
-    AMR_LAUNCHED("k_neighbors");
-    const uint32_t count = static_cast<uint32_t>(NP);
-    AMR_CUDA(cudaMemcpyAsync(device_out_count, &count, sizeof count, cudaMemcpyHostToDevice, s));
-    int32_t err = 0;
-    AMR_CUDA(cudaMemcpyAsync(&err, status, sizeof err, cudaMemcpyDeviceToHost, s));
-    AMR_CUDA(cudaStreamSynchronize(s));
-    if (host_out_count) *host_out_count = static_cast<size_t>(NP);
-    if (err != 0) return fail(static_cast<amr_status>(err), "neighbour rebuild found a non-2:1 face");
-    return AMR_OK;
-}
-

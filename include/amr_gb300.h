@@ -487,9 +487,13 @@ amr_status amr_tree_synchronize(amr_tree* t);
 /* ------------------------------------------------ allocation-free re-mesh
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory, e.g. code running inside a memory pool or arena
- * they do not own, or a host process whose allocator is locked down.  It does
- * what amr_tree_remesh does, on caller-owned buffers, and calls no cudaMalloc,
- * cudaFree or other allocating routine.  Its working storage is one static
+ * they do not own, or a host process whose allocator is locked down.  It runs
+ * the re-mesh of amr_tree_remesh for a finite-volume tree of ONE FP64 field
+ * (the padded state layout; piecewise-constant prolongation and FP64-mean
+ * restriction), on caller-owned buffers, and calls no cudaMalloc, cudaFree or
+ * other allocating routine.  Multi-field trees (Euler) and DG trees, whose
+ * re-mesh remaps several fields or interpolates polynomials, are not served
+ * by it.  Its working storage is one static
  * device array of AMR_NOALLOC_SCRATCH_BYTES per GPU that loads the library,
  * held until the process exits; that bounds the input to
  * AMR_NOALLOC_MAX_LEAVES leaves, and larger inputs (or out_capacity) are

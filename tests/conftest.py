@@ -17,9 +17,12 @@ def pytest_configure(config):
 
 
 def pytest_collection_modifyitems(config, items):
-    """End-to-end tests (whole solver loops, output files) run last, so that
-    a run stopping at its first failure has run every unit and parity test."""
-    items.sort(key=lambda item: item.get_closest_marker("endtoend") is not None)
+    """End-to-end tests (whole solver loops, output files) run after the unit
+    and parity tests, and the allocation-free re-mesh test (its own file)
+    after everything, so that a run stopping at its first failure has run
+    every other test before it."""
+    items.sort(key=lambda item: (item.path.name == "test_zz_no_alloc.py",
+                                 item.get_closest_marker("endtoend") is not None))
 
 
 def load_golden(name):

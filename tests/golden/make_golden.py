@@ -267,12 +267,15 @@ def vtk_golden():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference checkout (default: $AMR_REFERENCE, else the location oracle/Makefile names)")
     ap.add_argument("--vtk-only", action="store_true", help="only the VTK writer fixture")
     ap.add_argument("--euler-only", action="store_true", help="only the Euler fixtures")
     ap.add_argument("--ssprk-only", action="store_true", help="only the SSPRK fixtures")
     a = ap.parse_args()
-    subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={a.ref}"], check=True)
+    ref = a.ref or subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "print-ref"], check=True,
+                                  capture_output=True, text=True).stdout.strip()
+    subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref", f"REF={ref}"], check=True)
     if a.vtk_only:
         print(vtk_golden())
         return

@@ -4,8 +4,9 @@ a process whose device allocator is locked).  It must give the same tree,
 neighbour tables and state as the tree's own re-mesh (amr_tree_remesh), on two
 calls in a row, with the second call fed the first call's output.
 
-This file sorts last so that a run stopping at its first failure has run
-every other test before it."""
+This file runs last (conftest.py orders it after the end-to-end tests), so
+that a run stopping at its first failure has run every other test before
+it."""
 import ctypes as C
 
 import numpy as np
