@@ -17,7 +17,8 @@ records each scenario as a compressed .npz:
                  the SHA-256 of the final interior state ([leaf, cell, node,
                  variable] little-endian float64) and the loop's counts
 
-Usage:  python tests/golden/make_dg_golden.py
+Usage:  python tests/golden/make_dg_golden.py              (every fixture)
+        python tests/golden/make_dg_golden.py main_loop    (dg_main_loop.npz only)
 """
 from __future__ import annotations
 
@@ -78,13 +79,17 @@ def main_loop():
                         f"cthr={cthr}", f"end={end}", "capacity=8192", f"out={out}"],
                        check=True, capture_output=True, text=True)
     steps, remeshes, cells, leaves_max, time, next_dt = r.stdout.split()
+    # the driver writes the initial tree first and the tree at the end of the
+    # loop last: the record is the last dump
     idss, states, _ = read_dumps_any(out)
-    digest = hashlib.sha256(np.ascontiguousarray(states[0], dtype="<f8").tobytes()).hexdigest()
-    np.savez_compressed(HERE / "dg_main_loop.npz", ids=idss[0], state_sha256=digest, level=level, dt0=dt0, amr=amr,
+    assert len(idss) == 2 and len(idss[0]) == 4 ** level
+    final_ids, final = idss[-1], states[-1]
+    digest = hashlib.sha256(np.ascontiguousarray(final, dtype="<f8").tobytes()).hexdigest()
+    np.savez_compressed(HERE / "dg_main_loop.npz", ids=final_ids, state_sha256=digest, level=level, dt0=dt0, amr=amr,
                         rthr=rthr, cthr=cthr, end=end, steps=int(steps), remeshes=int(remeshes), cells=int(cells),
                         leaves_max=int(leaves_max), time=float(time), next_dt=float(next_dt),
-                        state_sum=float(states[0].sum()))
-    print("dg_main_loop", steps, remeshes, cells, leaves_max, time, next_dt, len(idss[0]))
+                        state_sum=float(final.sum()))
+    print("dg_main_loop", steps, remeshes, cells, leaves_max, time, next_dt, len(final_ids))
 
 
 # the reference's DG printer on fixture trees: name -> (fixture, dump, driver,
@@ -159,7 +164,12 @@ def read_dumps(path: Path):
 
 
 def main():
+    import sys
+
     subprocess.run(["make", "-C", str(REPO / "oracle"), "ref"], check=True)
+    if sys.argv[1:] == ["main_loop"]:
+        main_loop()
+        return
     for name, (level, steps, dt0, amr, rthr, cthr, eq) in SCENARIOS.items():
         out = Path("/tmp") / f"{name}.bin"
         subprocess.run([str(DRIVERS[eq]), f"level={level}", f"steps={steps}", f"dt0={dt0}", f"amr={amr}",

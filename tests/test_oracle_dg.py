@@ -69,6 +69,9 @@ def test_dg_main_loop_fixture_is_consistent():
     assert levels.min() >= 1 and levels.max() <= 6
     assert np.sum(4.0 ** -levels) == 1.0
     assert int(z["cells"]) % 16 == 0 and 16 * steps <= int(z["cells"]) <= 16 * int(z["leaves_max"]) * steps
+    # the record is the tree at the end of the loop, not the uniform start
+    L = int(z["level"])
+    assert not (len(ids) == 4 ** L and np.all(levels == L))
 
 
 @pytest.mark.parametrize("name", sorted(printer_cases()))
