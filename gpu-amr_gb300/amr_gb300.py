@@ -75,6 +75,8 @@ CRITERIA = {"none": 0, "grad": 1, "gradient": 1, "max": 2}
 RUN_PER_LAUNCH = 1
 RUN_INSTANCE_PARAMS = 2
 RUN_NO_GRAPH = 4
+RUN_NO_FUSED = 8
+RUN_FUSED = 16
 
 
 class TransferTask(C.Structure):
@@ -342,11 +344,12 @@ class Tree:
 
     def run(self, steps, interval, velocity, cfl, criterion="grad", rthr=0.05, cthr=0.01, min_level=1,
             max_level=5, remaining=1.7976931348623157e308, per_launch=False, cluster=0, graph=True,
-            instance_params=False) -> dict:
+            instance_params=False, fused=None) -> dict:
         """The benchmark loop (advance `interval` steps, flag, re-mesh) for
         `steps` steps; returns the run statistics.  per_launch: never the
         cluster kernel; graph=False: host-driven intervals; instance_params:
-        per-instance velocities (set_instance_params)."""
+        per-instance velocities (set_instance_params); fused: True / False
+        forces the fused interval kernel on / off (None: the default)."""
         if velocity is None:
             velocity, instance_params = (0.0, 0.0, 0.0), True
         prm = CycleParams()
@@ -358,7 +361,9 @@ class Tree:
         prm.min_level, prm.max_level = min_level, max_level
         prm.refine_threshold, prm.coarsen_threshold = rthr, cthr
         prm.options = ((RUN_PER_LAUNCH if per_launch else 0) | (0 if graph else RUN_NO_GRAPH)
-                       | (RUN_INSTANCE_PARAMS if instance_params else 0) | ((int(cluster) & 0xFF) << 8))
+                       | (RUN_INSTANCE_PARAMS if instance_params else 0)
+                       | (0 if fused is None else (RUN_FUSED if fused else RUN_NO_FUSED))
+                       | ((int(cluster) & 0xFF) << 8))
         st = CycleStats()
         check(lib().amr_tree_run(self._h, C.byref(prm), C.byref(st)))
         return {f: getattr(st, f) for f, _ in CycleStats._fields_}

@@ -112,13 +112,14 @@ namespace amr_api {
 struct GraphKey {
     int    k = 0, crit = 0, min_level = 0, max_level = 0, rounds = 0, bounds = 0, vel = 0, W = 0, S = 0, grid = 0;
     int    pair = 0; // several steps per pass (same-level trees)
+    int    fused = 0; // the whole interval (steps and gradient flags) in one kernel
     int    up[3] = { 0, 0, 0 };
     double rthr = 0.0, cthr = 0.0, cfl = 0.0;
     bool   operator==(const GraphKey& o) const
     {
         return k == o.k && crit == o.crit && min_level == o.min_level && max_level == o.max_level &&
                rounds == o.rounds && bounds == o.bounds && vel == o.vel && W == o.W && S == o.S && grid == o.grid &&
-               pair == o.pair &&
+               pair == o.pair && fused == o.fused &&
                up[0] == o.up[0] && up[1] == o.up[1] && up[2] == o.up[2] && std::memcmp(&rthr, &o.rthr, 8) == 0 &&
                std::memcmp(&cthr, &o.cthr, 8) == 0 && std::memcmp(&cfl, &o.cfl, 8) == 0;
     }
@@ -150,6 +151,7 @@ struct amr_tree {
     int          max_level_host = 0;
     bool         ghosts_valid   = false;
     bool         uniform        = true; // every neighbour relation is "same level" (multi-step passes apply)
+    bool         fused_off      = false; // a fused interval found leaves that are not 4x4 blocks: not again this run
 
     void*          sbuf[2]{};   // the two state buffers (fixed addresses)
     void*          cur = nullptr; // one of sbuf

@@ -3,6 +3,7 @@
 // or per-cell loop runs in a kernel from amr_kernels.cuh.
 
 #include "amr_api.cuh"
+#include "amr_interval.cuh"
 
 namespace amr_api {
 thread_local std::string g_last_error;
@@ -619,10 +620,64 @@ amr_status launch_run_step2d_pass(const RunBufs& B, RunCtl* ctl, int nl, const C
     });
 }
 
-// The launch sequence of one interval on stream cs (captured into a graph).
+// Steps per fused interval (the whole re-mesh interval in one kernel).
+constexpr int kFusedSteps = 10;
+
+// Grid of the fused interval kernel: every resident CTA, capped by the
+// tree's largest block count.
+template <bool FLAGS>
+unsigned fused_grid(amr_tree* t)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_run_interval2d<kFusedSteps, FLAGS>,
+                                                      IntervalShape<kFusedSteps>::THREADS,
+                                                      IntervalShape<kFusedSteps>::smem) != cudaSuccess ||
+        occ < 1)
+        occ = 1;
+    cudaGetLastError();
+    return static_cast<unsigned>(std::max<long long>(1, std::min<long long>(static_cast<long long>(t->cap) / 16,
+                                                                             1LL * num_sms() * occ)));
+}
+
+// Shared-memory limit of the fused interval kernel, set once per device.
+cudaError_t prepare_fused()
+{
+    static std::atomic<uint64_t> done{ 0 };
+    int                          dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (done.load() & bit) return cudaSuccess;
+    const int   smem = static_cast<int>(IntervalShape<kFusedSteps>::smem);
+    cudaError_t e    = cudaFuncSetAttribute(k_run_interval2d<kFusedSteps, true>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_run_interval2d<kFusedSteps, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+    if (e == cudaSuccess) done.fetch_or(bit);
+    return e;
+}
+
+// Event pair around the next update launch of a timed interval (amr_tree_set_timing).
+amr_status timing_slot(amr_tree* t, uint64_t cells, std::pair<cudaEvent_t, cudaEvent_t>** ev)
+{
+    if (t->events_used == t->events.size()) {
+        std::pair<cudaEvent_t, cudaEvent_t> e;
+        AMR_CUDA(cudaEventCreate(&e.first));
+        AMR_CUDA(cudaEventCreate(&e.second));
+        t->events.push_back(e);
+        t->event_cells.push_back(0);
+    }
+    *ev                            = &t->events[t->events_used];
+    t->event_cells[t->events_used] = cells;
+    ++t->events_used;
+    return AMR_OK;
+}
+
+// The launch sequence of one interval on stream cs (captured into a graph,
+// or launched directly with `timed`: CUDA events around the fused launch).
 // Grids are fixed; every kernel takes the leaf count from the control block.
 template <typename T>
-amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaStream_t cs)
+amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaStream_t cs, bool timed = false)
 {
     const Geo& g   = t->g;
     const int  K   = t->ninst, nl = g.depth + 1, sms = num_sms();
@@ -631,9 +686,65 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         k_run_require_uniform<<<1, 32, 0, cs>>>(ctl);
         AMR_LAUNCHED("k_run_require_uniform");
     }
+    if (key.fused) { // ... and is made of aligned 4x4 blocks
+        k_run_require_blocks<<<grid_for(static_cast<long long>(t->cap) / 16, 256), 256, 0, cs>>>(B, ctl, g);
+        AMR_LAUNCHED("k_run_require_blocks");
+    }
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
                                      t->coef, t->coef32, t->upcode, &ctl->err); // nothing after an error
     AMR_LAUNCHED("k_batch_begin");
+    if constexpr (sizeof(T) == 4) {
+        if (key.fused) { // the whole interval: steps and gradient flags in one kernel
+            std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
+            if (timed) {
+                if (amr_status ts = timing_slot(t, static_cast<uint64_t>(t->size) * g.cells * key.k, &ev);
+                    ts != AMR_OK)
+                    return ts;
+                AMR_CUDA(cudaEventRecord(ev->first, cs));
+            }
+            const size_t     cst  = static_cast<size_t>(K) * nl;
+            const GradRule   rule = make_grad_rule(key.rthr, key.cthr);
+            constexpr size_t smem = IntervalShape<kFusedSteps>::smem;
+            constexpr int    nthr = IntervalShape<kFusedSteps>::THREADS;
+            if (key.crit == 1)
+                k_run_interval2d<kFusedSteps, true><<<fused_grid<true>(t), nthr, smem, cs>>>(
+                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, key.up[0], key.up[1], 0);
+            else
+                k_run_interval2d<kFusedSteps, false><<<fused_grid<false>(t), nthr, smem, cs>>>(
+                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, key.up[0], key.up[1], 0);
+            AMR_LAUNCHED("k_run_interval2d");
+            if (timed) AMR_CUDA(cudaEventRecord(ev->second, cs));
+            constexpr int sp = 1; // the interval's result is in the other buffer
+            if (key.crit != 0) {
+                k_run_mark<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+                AMR_LAUNCHED("k_run_mark");
+                for (int r = 0; r < key.rounds; ++r) {
+                    k_run_closure<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+                    AMR_LAUNCHED("k_run_closure");
+                }
+                k_run_veto<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+                AMR_LAUNCHED("k_run_veto");
+                k_run_count<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+                AMR_LAUNCHED("k_run_count");
+                const unsigned ntile = static_cast<unsigned>(
+                    std::min<size_t>(1024, std::max<size_t>(1, (t->cap + kScanTile - 1) / kScanTile)));
+                k_run_scan_tiles<<<ntile, kScanThreads, 0, cs>>>(B, ctl);
+                AMR_LAUNCHED("k_run_scan_tiles");
+                k_run_scan_apply<<<ntile, kScanThreads, 0, cs>>>(B, ctl);
+                AMR_LAUNCHED("k_run_scan_apply");
+                k_run_emit<<<sms * 4, 256, 0, cs>>>(B, ctl, g);
+                AMR_LAUNCHED("k_run_emit");
+                k_run_remap<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, sp);
+                AMR_LAUNCHED("k_run_remap");
+                k_run_neighbors<<<sms * 8, 128, 0, cs>>>(B, ctl, g);
+                AMR_LAUNCHED("k_run_neighbors");
+            }
+            // a fused interval builds no pass or face records
+            k_run_commit<<<1, 256, 0, cs>>>(B, ctl, key.k, g.cells, key.crit != 0 ? 1 : 0, sp, 0);
+            AMR_LAUNCHED("k_run_commit");
+            return AMR_OK;
+        }
+    }
     if (key.pair) { // records of this interval's tree, with the upwind codes just written
         const unsigned rgrid =
             static_cast<unsigned>(std::min<long long>((static_cast<long long>(t->cap) + 255) / 256, 8LL * sms));
@@ -784,6 +895,20 @@ amr_status interval_graph(amr_tree* t, const GraphKey& key, const RunBufs& B, cu
     return AMR_OK;
 }
 
+// Whether a run may use the fused interval kernel: AMR_RUN_FUSED asks for it,
+// AMR_RUN_NO_FUSED forbids it; otherwise the default (on), which
+// AMR_GB300_FUSED=0 in the environment turns off.
+bool fused_enabled(int options)
+{
+    if (options & AMR_RUN_NO_FUSED) return false;
+    if (options & AMR_RUN_FUSED) return true;
+    static const bool on = [] {
+        const char* e = std::getenv("AMR_GB300_FUSED");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 // Up to `max_intervals` intervals as graph replays, then one readback of the
 // control block.  Requires that no step is clamped by the remaining time.
 amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_params, long long max_intervals,
@@ -883,27 +1008,51 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     const long long rem   = (nfull < max_intervals) ? left % k : 0;
     cudaGraphExec_t full = nullptr, tail = nullptr;
     uint64_t        nk_full = 0, nk_tail = 0;
-    // same-level trees: two steps per pass, guarded on the device
+    // same-level trees: two steps per pass, guarded on the device; FP32
+    // forests of 16x16 patches whose interval is kFusedSteps long run the
+    // whole interval (steps and gradient flags) in one kernel
     const bool pairs = step2d && t->uniform && key.W > 0;
+    const bool fused = pairs && t->dtype == AMR_F32 && g.n == 16 && k == kFusedSteps &&
+                       (p->criterion == 0 || p->criterion == 1) && !t->fused_off && fused_enabled(p->options);
+    if (fused) AMR_CUDA(prepare_fused());
+    GraphKey key_full = key, key_tail = key;
     if (nfull > 0) {
-        key.k         = static_cast<int>(k);
-        key.pair      = pairs && k >= 2 ? 1 : 0;
-        amr_status st = interval_graph(t, key, B, &full, &nk_full);
-        if (st != AMR_OK) return st;
+        key_full.k     = static_cast<int>(k);
+        key_full.pair  = pairs && k >= 2 ? 1 : 0;
+        key_full.fused = fused ? 1 : 0;
+        if (!t->timing) {
+            amr_status st = interval_graph(t, key_full, B, &full, &nk_full);
+            if (st != AMR_OK) return st;
+        }
     }
     if (rem > 0) {
-        key.k         = static_cast<int>(rem);
-        key.pair      = pairs && rem >= 2 ? 1 : 0;
-        amr_status st = interval_graph(t, key, B, &tail, &nk_tail);
-        if (st != AMR_OK) return st;
+        key_tail.k    = static_cast<int>(rem);
+        key_tail.pair = pairs && rem >= 2 ? 1 : 0;
+        if (!t->timing) {
+            amr_status st = interval_graph(t, key_tail, B, &tail, &nk_tail);
+            if (st != AMR_OK) return st;
+        }
     }
-    for (long long i = 0; i < nfull; ++i) {
-        AMR_CUDA(cudaGraphLaunch(full, s));
-        g_launches.fetch_add(nk_full);
-    }
-    if (tail) {
-        AMR_CUDA(cudaGraphLaunch(tail, s));
-        g_launches.fetch_add(nk_tail);
+    if (t->timing) {
+        // timed: the same launch sequence issued directly, CUDA events
+        // around each fused launch
+        auto direct = [&](const GraphKey& kk) -> amr_status {
+            return t->dtype == AMR_F64 ? record_interval<double>(t, kk, B, s, kk.fused != 0)
+                                       : record_interval<float>(t, kk, B, s, kk.fused != 0);
+        };
+        for (long long i = 0; i < nfull; ++i)
+            if (amr_status st = direct(key_full); st != AMR_OK) return st;
+        if (rem > 0)
+            if (amr_status st = direct(key_tail); st != AMR_OK) return st;
+    } else {
+        for (long long i = 0; i < nfull; ++i) {
+            AMR_CUDA(cudaGraphLaunch(full, s));
+            g_launches.fetch_add(nk_full);
+        }
+        if (tail) {
+            AMR_CUDA(cudaGraphLaunch(tail, s));
+            g_launches.fetch_add(nk_tail);
+        }
     }
     // readback
     AMR_CUDA(cudaMemcpyAsync(hc, t->ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost, s));
@@ -925,8 +1074,11 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     // an interval guarded for two-step passes found the tree non-uniform:
     // it and the rest of the chunk did not run (no state, time or statistic
     // changed); the caller continues with one-step intervals
-    const bool retry = r.err == kRetryUniform;
-    if (retry) t->uniform = false;
+    // an interval guarded for the fused kernel found leaves that are not
+    // aligned 4x4 blocks of one level: the same, with the per-leaf kernels
+    const bool retry = r.err == kRetryUniform || r.err == kRetryFused;
+    if (r.err == kRetryUniform) t->uniform = false;
+    if (r.err == kRetryFused) t->fused_off = true;
     // time of each instance = its batch totals + the open batch
     double   tmax = 0.0;
     uint32_t cmax = 0;
@@ -1684,6 +1836,7 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats* out)
 {
+    if (t) t->fused_off = false; // re-evaluated by every run
     if (!t || !p) return fail(AMR_ERR_INVALID, "null argument");
     if (p->criterion < 0 || p->criterion > 2) return fail(AMR_ERR_INVALID, "unknown criterion");
     if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the advection run takes a one-field tree");

@@ -232,7 +232,12 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
  * rebuild) is one CUDA graph whose kernels read the leaf count and the
  * buffer selection from device memory, captured once and replayed with no
  * host round trip between intervals (AMR_RUN_NO_GRAPH: host-driven launches
- * with a readback per re-mesh).  Results are identical on every path. */
+ * with a readback per re-mesh).  On FP32 forests of 16x16 patches whose every
+ * instance is uniform at a level >= 2, an interval of 10 steps with the
+ * gradient criterion (or none) runs its steps and flags in one kernel over
+ * 4x4-patch blocks (AMR_RUN_NO_FUSED: multi-step passes and a separate flag
+ * kernel instead; AMR_RUN_FUSED: the fused kernel even where the
+ * environment turns it off).  Results are identical on every path. */
 typedef struct amr_cycle_params {
     uint64_t steps;
     uint64_t remesh_interval;
@@ -247,6 +252,8 @@ typedef struct amr_cycle_params {
                                 and bounds (amr_tree_set_instance_params);
                                 AMR_RUN_NO_GRAPH: host-driven intervals instead
                                 of the captured interval graph;
+                                AMR_RUN_NO_FUSED / AMR_RUN_FUSED: without / with
+                                the fused interval kernel;
                                 bits 8-15: cluster size (CTAs) to use, 0 = largest that fits */
     double   refine_threshold;
     double   coarsen_threshold;
@@ -255,6 +262,8 @@ typedef struct amr_cycle_params {
 #define AMR_RUN_PER_LAUNCH 1
 #define AMR_RUN_INSTANCE_PARAMS 2
 #define AMR_RUN_NO_GRAPH 4
+#define AMR_RUN_NO_FUSED 8
+#define AMR_RUN_FUSED 16
 
 typedef struct amr_cycle_stats {
     uint64_t executed_steps;   /* steps with dt > 0 */
