@@ -5,8 +5,8 @@
 // instance uniform at its own level L >= 2, as the batched forests are) with
 // 16x16 patches and one ghost layer.  In Morton order the 16 leaves
 // 16b .. 16b+15 of such a tree are one aligned 4x4 block of patches of one
-// instance (64x64 cells), so block b is found from the key of leaf 16b alone;
-// its neighbour patches follow from the block's position and the instance's
+// instance (64x64 cells), described by the key of leaf 16b alone; its
+// neighbour patches follow from the block's position and the instance's
 // level (periodic wrap), with no neighbour records.
 //
 // One CTA per block (grid-stride over blocks), in upwind-normalized
@@ -41,9 +41,10 @@
 //     staged in shared memory and go to memory by one bulk store per patch
 //     plus four single floats at the 16-byte-misaligned ends of each span.
 //
-// The kernel checks that each block is one aligned 4x4 block of one instance
-// at a level >= 2 and that its neighbourhood holds the expected keys before
-// any copy is issued.
+// The guard kernel k_run_require_blocks checks that each block is one aligned
+// 4x4 block of one instance at a level >= 2 and writes its descriptor; the
+// fused kernel checks that every leaf of a block's neighbourhood lies in the
+// tree before it issues a copy.
 #pragma once
 
 #include "amr_graph.cuh"
@@ -62,18 +63,19 @@ struct IntervalShape {
     static constexpr int TY   = 8;              // row groups
     static constexpr int RY   = 10;             // rows per thread
     static constexpr int THREADS = TX * TY;
-    static constexpr int XS   = TY * RY + 2;    // X column pitch in pairs: an odd multiple of 16 bytes
+    static constexpr int XS   = TY * RY + 1;    // X column pitch in pairs (odd: 64-bit accesses hit distinct banks)
     static constexpr int TILES = 6 * (800 + 4 * 1168 + 80); // packed tile rows (bytes), either mirroring
     static constexpr int STAGE = 292;           // floats per staged patch: padded indices 16 .. 307
     static_assert(RW % 4 == 0, "region width is a multiple of four columns");
     static_assert(TY * RY >= RW, "row groups cover the region");
-    static_assert((XS * 8) % 32 == 16, "X pitch spreads 16-byte stores over the banks");
+    static_assert(XS % 2 == 1, "odd X pitch");
     static_assert(D == 10, "tile packing sized for ten steps");
     // shared memory: tiles | X (2 buffers x (TX + 1) columns x XS pairs; the
-    // output stage once the flags are done) | Y (2 buffers x (TY + 1) rows x
-    // TX double pairs) | patch bases, flags, slot table, coefficients, barrier
+    // output stage once the flags are done) | Y (2 buffers x 2 pairs x (TY +
+    // 1) rows x TX) | patch bases, flags, slot table, coefficients, barrier
     static constexpr size_t x_bytes = 2 * (TX + 1) * XS * 8;
-    static constexpr size_t y_bytes = 2 * (TY + 1) * TX * 16;
+    static constexpr int    YB      = (TY + 1) * TX; // pairs of one Y array
+    static constexpr size_t y_bytes = 2 * 2 * YB * 8;
     static constexpr size_t smem    = TILES + x_bytes + y_bytes + 16 * 4 * 3 + 24 * 4 + D * 16 + 16;
     static_assert(16 * STAGE * 4 <= x_bytes, "the output stage fits in the X buffers");
 };
@@ -166,8 +168,10 @@ __device__ __forceinline__ uint64_t grad_pair(uint64_t xl, uint64_t xh, uint64_t
 // k_run_require_uniform, before any kernel changes state or time): every
 // 16 leaves from 16b must be one aligned 4x4 block of one instance at a level
 // >= 2, else kRetryFused stops the replay and the host re-runs the interval
-// with the per-leaf kernels.
-static __global__ void __launch_bounds__(256) k_run_require_blocks(RunBufs B, RunCtl* ctl, Geo g)
+// with the per-leaf kernels.  For each block it writes the descriptor the
+// fused kernel reads (blocks[b], see IntervalBlock), so that kernel needs no
+// dependent loads of keys and upwind codes.
+static __global__ void __launch_bounds__(256) k_run_require_blocks(RunBufs B, RunCtl* ctl, Geo g, int upx0, int upy0)
 {
     if (ctl->err) return;
     const int P = ctl->P;
@@ -180,34 +184,57 @@ static __global__ void __launch_bounds__(256) k_run_require_blocks(RunBufs B, Ru
         const uint64_t k0 = keys[16 * b], k15 = keys[16 * b + 15];
         const int      L  = key_level(k0);
         const uint32_t m0 = static_cast<uint32_t>(((k0 >> 6) & g.morton_mask) >> (2 * (g.depth - L)));
-        if (L < 2 || key_level(k15) != L || key_prefix(g, k15) != key_prefix(g, k0) || (m0 & 15u) != 0u)
+        if (L < 2 || key_level(k15) != L || key_prefix(g, k15) != key_prefix(g, k0) || (m0 & 15u) != 0u) {
             atomicCAS(&ctl->err, 0, kRetryFused);
+            continue;
+        }
+        const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(k0 >> g.inst_shift);
+        int       ux = upx0, uy = upy0;
+        if (B.upcode) {
+            const int32_t code = B.upcode[inst];
+            ux                 = unpack_upwind(code, 0);
+            uy                 = unpack_upwind(code, 1);
+        }
+        B.frec[b] = make_int4(16 * b - static_cast<int>(m0), L | (inst << 8),
+                              static_cast<int>(compact2(m0)) | (static_cast<int>(compact2(m0 >> 1)) << 16),
+                              (ux + 1) | ((uy + 1) << 2));
     }
 }
 
-// What a CTA knows about one block.
+// What a CTA knows about one block, decoded from its descriptor
+// (k_run_require_blocks): x = leaf index of the instance's first patch,
+// y = level | instance << 8, z = block origin x | y << 16 (patch
+// coordinates), w = (upwind x + 1) | (upwind y + 1) << 2.
 struct IntervalBlock {
-    int      base;     // leaf index of the instance's first patch
-    int      L, inst;  // level, instance
-    int      bx0, by0; // block origin (patch coordinates)
-    int      ux, uy;   // upwind offsets
-    uint64_t pre;      // instance key prefix
+    int base, L, inst, bx0, by0, ux, uy;
 };
+__device__ __forceinline__ IntervalBlock interval_block(int4 d)
+{
+    IntervalBlock b;
+    b.base = d.x;
+    b.L    = d.y & 255;
+    b.inst = d.y >> 8;
+    b.bx0  = d.z & 0xFFFF;
+    b.by0  = d.z >> 16;
+    b.ux   = (d.w & 3) - 1;
+    b.uy   = ((d.w >> 2) & 3) - 1;
+    return b;
+}
 
 template <int D, bool FLAGS>
 __global__ void __launch_bounds__(IntervalShape<D>::THREADS, 3)
 k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef32, size_t cstride, int nl,
-                 GradRule rule, int min_level, int max_level, int upx0, int upy0, int parity)
+                 GradRule rule, int min_level, int max_level, int parity)
 {
     using S                = IntervalShape<D>;
-    constexpr int TX       = S::TX, TY = S::TY, RY = S::RY, XS = S::XS, HALO = S::HALO, HW = S::HW;
+    constexpr int TX       = S::TX, RY = S::RY, XS = S::XS, HALO = S::HALO, HW = S::HW, YB = S::YB;
     constexpr int FLAT     = S::FLAT, STAGE = S::STAGE;
     if (ctl->err) return;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char* tiles = smem;
     uint64_t*      Xb    = reinterpret_cast<uint64_t*>(smem + S::TILES);
     float*         stage = reinterpret_cast<float*>(smem + S::TILES); // aliases X after the flags
-    ulonglong2*    Yb    = reinterpret_cast<ulonglong2*>(smem + S::TILES + S::x_bytes);
+    uint64_t*      Yb    = reinterpret_cast<uint64_t*>(smem + S::TILES + S::x_bytes);
     int*           pbase = reinterpret_cast<int*>(smem + S::TILES + S::x_bytes + S::y_bytes);
     int*           pany  = pbase + 16;
     int*           pall  = pany + 16;
@@ -217,63 +244,35 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
-    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    const int P = ctl->P, s = ctl->sb ^ parity;
     const float* __restrict__ in   = static_cast<const float*>(B.state[s]);
     float* __restrict__       out  = static_cast<float*>(B.state[s ^ 1]);
-    const uint64_t* __restrict__ keys = B.keys[tb];
+    const int4* __restrict__  desc = B.frec; // block descriptors (k_run_require_blocks)
     const int nblk = P / 16;
-    if (P % 16 != 0) {
-        if (tid == 0) atomicCAS(&ctl->err, 0, kRetryFused);
-        return;
-    }
     if (tid == 0) {
         mbar_init(bar, 1);
         mbar_init_fence();
     }
-    // rows above the region in the Y buffers are never written: zero once
-    for (int i = tid; i < 2 * TX; i += blockDim.x) Yb[(i / TX) * (TY + 1) * TX + (i % TX)] = make_ulonglong2(0, 0);
+    // rows above the region in the Y arrays are never written: zero once
+    for (int i = tid; i < 4 * TX; i += blockDim.x) Yb[(i / TX) * YB + (i % TX)] = 0ull;
     __syncthreads();
 
-    // the block's description from its first key
-    auto describe = [&](int blk, IntervalBlock& b) -> bool {
-        const uint64_t k0  = __ldg(keys + 16 * blk);
-        const uint64_t k15 = __ldg(keys + 16 * blk + 15);
-        b.L                = key_level(k0);
-        b.pre              = key_prefix(g, k0);
-        const uint32_t m0  = static_cast<uint32_t>(((k0 >> 6) & g.morton_mask) >> (2 * (g.depth - b.L)));
-        b.inst             = g.inst_shift >= 64 ? 0 : static_cast<int>(k0 >> g.inst_shift);
-        b.base             = 16 * blk - static_cast<int>(m0);
-        b.bx0              = static_cast<int>(compact2(m0));
-        b.by0              = static_cast<int>(compact2(m0 >> 1));
-        b.ux               = upx0;
-        b.uy               = upy0;
-        if (B.upcode) {
-            const int32_t code = __ldg(B.upcode + b.inst);
-            b.ux               = unpack_upwind(code, 0);
-            b.uy               = unpack_upwind(code, 1);
-        }
-        return !(b.L < 2 || key_level(k15) != b.L || key_prefix(g, k15) != b.pre || (m0 & 15u) != 0u);
-    };
     // leaf of actual block-relative patch offsets (px, py), periodic
     auto leaf_at = [&](const IntervalBlock& b, int px, int py) -> int {
         const int      Wm = (1 << b.L) - 1;
         const uint32_t x = static_cast<uint32_t>((b.bx0 + px) & Wm), y = static_cast<uint32_t>((b.by0 + py) & Wm);
         return b.base + static_cast<int>(spread2(x) | (spread2(y) << 1));
     };
-    // validate the block and its neighbourhood (every slot's leaf holds the
-    // key of that position at level L), write its slot table, issue the
-    // copies; false when the block is not valid (nothing issued: the CTA
-    // leaves).  Its barriers also order every earlier read of the tiles and
-    // of the slot table before the copies and the new table.
-    auto issue = [&](int blk, IntervalBlock& b) -> bool {
-        int bad = describe(blk, b) ? 0 : 1;
-        if (!bad && tid < 36) {
-            const int      py = tid / 6 - 1, px = tid % 6 - 1;
-            const int      Wm = (1 << b.L) - 1;
-            const uint32_t x = static_cast<uint32_t>((b.bx0 + px) & Wm), y = static_cast<uint32_t>((b.by0 + py) & Wm);
-            const int      q = b.base + static_cast<int>(spread2(x) | (spread2(y) << 1));
-            const uint64_t m = (spread2(x) | (spread2(y) << 1)) << (2 * (g.depth - b.L));
-            bad = q < 0 || q >= P || __ldg(keys + q) != (b.pre | (m << 6) | static_cast<uint64_t>(b.L));
+    // every leaf of the block's 6x6 neighbourhood inside the tree (checked
+    // before any copy is issued), its slot table, its copies; false when a
+    // leaf is out of range (nothing issued: the CTA leaves).  The barriers
+    // also order every earlier read of the tiles and of the slot table
+    // before the copies and the new table.
+    auto issue = [&](const IntervalBlock& b) -> bool {
+        int bad = 0;
+        if (tid < 36) {
+            const int q = leaf_at(b, tid % 6 - 1, tid / 6 - 1);
+            bad         = b.L < 2 || q < 0 || q >= P;
         }
         if (__syncthreads_or(bad)) {
             if (tid == 0) atomicCAS(&ctl->err, 0, static_cast<int32_t>(AMR_ERR_UNBALANCED));
@@ -288,7 +287,8 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
             slot[3 * (tid - 64) + 1] = static_cast<int>(size);
             slot[3 * (tid - 64) + 2] = static_cast<int>(start);
         }
-        fence_proxy_async_smem();
+        // the tiles were only read by the threads since their last copies:
+        // the barrier orders those reads before the new copies
         __syncthreads();
         if (tid < 36) {
             const int py = tid / 6 - 1, px = tid % 6 - 1;
@@ -300,12 +300,30 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         return true;
     };
 
-    IntervalBlock cur{}, nxt{};
+    // per block, loaded one block ahead so that no global load sits on the
+    // path between two barriers: threads < D its coefficient row of step tid,
+    // threads 128 .. 143 its instance's level bounds
+    auto coef_of = [&](const IntervalBlock& b) -> float2 {
+        return tid < D ? __ldg(coef32 + tid * cstride + static_cast<size_t>(b.inst) * nl + b.L) : float2{};
+    };
+    auto bounds_of = [&](const IntervalBlock& b) -> int2 {
+        if (!FLAGS || tid < 128 || tid >= 144) return make_int2(min_level, max_level);
+        return B.bounds ? make_int2(__ldg(B.bounds + 2 * b.inst), __ldg(B.bounds + 2 * b.inst + 1))
+                        : make_int2(min_level, max_level);
+    };
     uint32_t      phase = 0;
     int           blk   = blockIdx.x;
-    if (blk >= nblk || !issue(blk, cur)) return;
+    if (blk >= nblk) return;
+    IntervalBlock cur    = interval_block(__ldg(desc + blk));
+    float2        ccoef  = coef_of(cur);
+    int2          cbound = bounds_of(cur);
+    if (!issue(cur)) return;
 
     while (true) {
+        // the next block's descriptor, needed after this block's register load
+        const int  nb   = blk + static_cast<int>(gridDim.x);
+        const bool more = nb < nblk;
+        const int4 dn   = more ? __ldg(desc + nb) : make_int4(0, 0, 0, 0);
         // ---- 1. the copies of this block
         if (__syncthreads_or(mbar_wait_bounded(bar, phase) ? 0 : 1)) {
             if (tid == 0) atomicExch(&ctl->err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
@@ -315,10 +333,7 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         }
         phase ^= 1u;
         const bool sx = cur.ux > 0, sy = cur.uy > 0;
-        if (tid < D) {
-            const float2 c = __ldg(coef32 + tid * cstride + static_cast<size_t>(cur.inst) * nl + cur.L);
-            cf[tid]        = make_ulonglong2(pk(c.x, c.x), pk(c.y, c.y));
-        }
+        if (tid < D) cf[tid] = make_ulonglong2(pk(ccoef.x, ccoef.x), pk(ccoef.y, ccoef.y));
         if (tid < 16) {
             const int px = tid & 3, py = tid >> 2; // actual block patch
             pbase[tid]   = leaf_at(cur, px, py) * FLAT;
@@ -327,13 +342,16 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         }
 
         // ---- 2. the thread's cells into registers
-        // column k of the thread: 0 -> p1.lo, 1 -> p2.lo, 2 -> p1.hi, 3 -> p2.hi
+        // column k of the thread: 0 -> p1.lo, 1 -> p2.lo, 2 -> p1.hi, 3 -> p2.hi;
+        // its actual block column X, slot column and byte offset in the row
         const int c0 = 2 * tx - HALO;
-        int       colX[4];
+        int       colX[4], cslot[4], cbyte[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int c = c0 + (k & 1) + (k >> 1) * HW;
             colX[k]     = sx ? 63 - c : c;
+            cslot[k]    = (colX[k] >> 4) + 1;
+            cbyte[k]    = ((colX[k] & 15) + 1) * 4;
         }
         const int r0 = ty * RY - HALO;
         uint64_t  v1[RY], v2[RY];
@@ -342,24 +360,25 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
             const int r    = r0 + i;
             float     e[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
             if (r <= 64) {
-                const int      Y  = sy ? 63 - r : r;
-                const int      q  = (Y >> 4) + 1;
-                const int      lo = slot[3 * q], size = slot[3 * q + 1], start = slot[3 * q + 2];
-                const unsigned char* rowp = tiles + start + ((Y & 15) + 1) * 72 + 4 - lo;
+                const int            Y    = sy ? 63 - r : r;
+                const int*           sr   = slot + 3 * ((Y >> 4) + 1);
+                const int            size = sr[1];
+                const unsigned char* rowp = tiles + sr[2] + ((Y & 15) + 1) * 72 - sr[0];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int X = colX[k];
-                    e[k]        = *reinterpret_cast<const float*>(rowp + ((X >> 4) + 1) * size + (X & 15) * 4);
-                }
+                for (int k = 0; k < 4; ++k) e[k] = *reinterpret_cast<const float*>(rowp + cslot[k] * size + cbyte[k]);
             }
             v1[i] = pk(e[0], e[2]);
             v2[i] = pk(e[1], e[3]);
         }
         // ---- the next block's copies land during this block's steps
-        const int  nb   = blk + static_cast<int>(gridDim.x);
-        const bool more = nb < nblk;
+        IntervalBlock nxt{};
+        float2        ncoef{};
+        int2          nbound{};
         if (more) {
-            if (!issue(nb, nxt)) {
+            nxt    = interval_block(dn);
+            ncoef  = coef_of(nxt);
+            nbound = bounds_of(nxt);
+            if (!issue(nxt)) {
                 if (tid < 16) bulk_wait_all();
                 return;
             }
@@ -367,39 +386,37 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
             __syncthreads(); // pbase, cf and the flags' zeroing are visible
         }
 
-        // ---- 3. D steps
+        // ---- 3. D steps; X column tx + 1 holds thread tx's p2, read by thread
+        // tx + 1 as the x-neighbour of its p1.  The last thread's column is
+        // read only by thread 0, whose second half's x-neighbour is the first
+        // half's last column (that thread's p2 low word): the last thread
+        // publishes its low word in both words, every other thread its p2,
+        // and thread 0 reads column TX instead of column 0
+        const bool      last = tx == TX - 1;
+        const int       xsrc = tx == 0 ? TX : tx;
+        auto            pub  = [&](uint64_t v) { return last ? pk(pk_lo(v), pk_lo(v)) : v; };
         auto steps = [&]<bool XU, bool YU>() {
-#pragma unroll 1
+#pragma unroll
             for (int m = 0; m < D; ++m) {
-                uint64_t* const   X = Xb + (m & 1) * (TX + 1) * XS;
-                ulonglong2* const Y = Yb + (m & 1) * (TY + 1) * TX;
+                uint64_t* const X  = Xb + (m & 1) * (TX + 1) * XS;
+                uint64_t* const Y1 = Yb + (m & 1) * 2 * YB;
+                uint64_t* const Y2 = Y1 + YB;
                 {
                     uint64_t* xo = X + (tx + 1) * XS + ty * RY;
 #pragma unroll
-                    for (int i = 0; i < RY; i += 2)
-                        *reinterpret_cast<ulonglong2*>(xo + i) = make_ulonglong2(v2[i], v2[i + 1]);
-                    if (tx == TX - 1) { // the left neighbour of the second half's first column
-                        uint64_t* x0 = X + ty * RY;
-#pragma unroll
-                        for (int i = 0; i < RY; i += 2) {
-                            const float a = pk_lo(v2[i]), b = pk_lo(v2[i + 1]);
-                            *reinterpret_cast<ulonglong2*>(x0 + i) = make_ulonglong2(pk(a, a), pk(b, b));
-                        }
-                    }
-                    Y[(ty + 1) * TX + tx] = make_ulonglong2(v1[RY - 1], v2[RY - 1]);
+                    for (int i = 0; i < RY; ++i) xo[i] = pub(v2[i]);
+                    Y1[(ty + 1) * TX + tx] = v1[RY - 1];
+                    Y2[(ty + 1) * TX + tx] = v2[RY - 1];
                 }
                 __syncthreads();
-                const ulonglong2 c   = cf[m];
-                const ulonglong2 yin = Y[ty * TX + tx];
-                const uint64_t*  xi  = X + tx * XS + ty * RY;
+                const ulonglong2 c  = cf[m];
+                const uint64_t   y1 = Y1[ty * TX + tx], y2 = Y2[ty * TX + tx];
+                const uint64_t*  xi = X + xsrc * XS + ty * RY;
 #pragma unroll
-                for (int i = RY - 2; i >= 0; i -= 2) {
-                    const ulonglong2 xw = *reinterpret_cast<const ulonglong2*>(xi + i);
-                    // row i + 1, then row i: p2 first (its x-neighbour is p1)
-                    v2[i + 1] = upd_pair<XU, YU>(v2[i + 1], v1[i + 1], v2[i], c.x, c.y);
-                    v1[i + 1] = upd_pair<XU, YU>(v1[i + 1], xw.y, v1[i], c.x, c.y);
-                    v2[i]     = upd_pair<XU, YU>(v2[i], v1[i], i > 0 ? v2[i - 1] : yin.y, c.x, c.y);
-                    v1[i]     = upd_pair<XU, YU>(v1[i], xw.x, i > 0 ? v1[i - 1] : yin.x, c.x, c.y);
+                for (int i = RY - 1; i >= 0; --i) {
+                    // p2 first: its x-neighbour is p1
+                    v2[i] = upd_pair<XU, YU>(v2[i], v1[i], i > 0 ? v2[i - 1] : y2, c.x, c.y);
+                    v1[i] = upd_pair<XU, YU>(v1[i], xi[i], i > 0 ? v1[i - 1] : y1, c.x, c.y);
                 }
             }
         };
@@ -413,43 +430,36 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         // ---- 4. flags of the block's 16 patches
         if constexpr (FLAGS) {
             // exchange: p2 to the right neighbour (X buffer 0), p1 to the left
-            // (X buffer 1), last row down (Y buffer 0), first row up (Y buffer 1)
-            uint64_t* const   XL = Xb;
-            uint64_t* const   XR = Xb + (TX + 1) * XS;
-            ulonglong2* const YD = Yb;
-            ulonglong2* const YU = Yb + (TY + 1) * TX;
+            // (X buffer 1), last row down, first row up (Y buffer 0)
+            uint64_t* const XL  = Xb;
+            uint64_t* const XR  = Xb + (TX + 1) * XS;
+            uint64_t* const YD1 = Yb;
+            uint64_t* const YD2 = Yb + YB;
+            uint64_t* const YU1 = Yb + 2 * YB;
+            uint64_t* const YU2 = Yb + 3 * YB;
             {
+                // XR column tx holds thread tx's p1, read by thread tx - 1 as
+                // the right neighbour of its p2; thread 0's column is read only
+                // by the last thread, whose first half's last column has the
+                // second half's first column (thread 0's p1 high word) to its
+                // right: thread 0 publishes that word in both words
                 uint64_t* a = XL + (tx + 1) * XS + ty * RY;
                 uint64_t* b = XR + tx * XS + ty * RY;
 #pragma unroll
-                for (int i = 0; i < RY; i += 2) {
-                    *reinterpret_cast<ulonglong2*>(a + i) = make_ulonglong2(v2[i], v2[i + 1]);
-                    *reinterpret_cast<ulonglong2*>(b + i) = make_ulonglong2(v1[i], v1[i + 1]);
+                for (int i = 0; i < RY; ++i) {
+                    a[i] = pub(v2[i]);
+                    b[i] = tx == 0 ? pk(pk_hi(v1[i]), pk_hi(v1[i])) : v1[i];
                 }
-                if (tx == TX - 1) {
-                    uint64_t* x0 = XL + ty * RY;
-#pragma unroll
-                    for (int i = 0; i < RY; i += 2) {
-                        const float p = pk_lo(v2[i]), q = pk_lo(v2[i + 1]);
-                        *reinterpret_cast<ulonglong2*>(x0 + i) = make_ulonglong2(pk(p, p), pk(q, q));
-                    }
-                }
-                if (tx == 0) { // the right neighbour of the first half's last column
-                    uint64_t* xe = XR + TX * XS + ty * RY;
-#pragma unroll
-                    for (int i = 0; i < RY; i += 2) {
-                        const float p = pk_hi(v1[i]), q = pk_hi(v1[i + 1]);
-                        *reinterpret_cast<ulonglong2*>(xe + i) = make_ulonglong2(pk(p, p), pk(q, q));
-                    }
-                }
-                YD[(ty + 1) * TX + tx] = make_ulonglong2(v1[RY - 1], v2[RY - 1]);
-                YU[ty * TX + tx]       = make_ulonglong2(v1[0], v2[0]);
+                YD1[(ty + 1) * TX + tx] = v1[RY - 1];
+                YD2[(ty + 1) * TX + tx] = v2[RY - 1];
+                YU1[ty * TX + tx]       = v1[0];
+                YU2[ty * TX + tx]       = v2[0];
             }
             __syncthreads();
-            const ulonglong2 ya = YD[ty * TX + tx];       // the row above row 0
-            const ulonglong2 yb = YU[(ty + 1) * TX + tx]; // the row below row RY - 1
-            const uint64_t*  xl = XL + tx * XS + ty * RY;
-            const uint64_t*  xr = XR + (tx + 1) * XS + ty * RY;
+            const uint64_t ya1 = YD1[ty * TX + tx], ya2 = YD2[ty * TX + tx];             // the row above row 0
+            const uint64_t yb1 = YU1[(ty + 1) * TX + tx], yb2 = YU2[(ty + 1) * TX + tx]; // below row RY - 1
+            const uint64_t* xl = XL + xsrc * XS + ty * RY;
+            const uint64_t* xr = XR + (last ? 0 : tx + 1) * XS + ty * RY;
             // per column k and patch-row part (the thread's rows cross at most
             // one patch boundary): the largest FP32 squared gradient as a bit
             // pattern (s >= +0 or NaN, so unsigned order is value order and
@@ -459,65 +469,69 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
             uint32_t  m0[4] = { 0u, 0u, 0u, 0u }, m1[4] = { 0u, 0u, 0u, 0u };
 #pragma unroll
             for (int i = 0; i < RY; ++i) {
-                const int r = r0 + i;
-                if (r < ra || r > rb) continue;
-                const uint64_t up1 = i > 0 ? v1[i - 1] : ya.x, dn1 = i < RY - 1 ? v1[i + 1] : yb.x;
-                const uint64_t up2 = i > 0 ? v2[i - 1] : ya.y, dn2 = i < RY - 1 ? v2[i + 1] : yb.y;
+                const int      r   = r0 + i;
+                const uint64_t up1 = i > 0 ? v1[i - 1] : ya1, dn1 = i < RY - 1 ? v1[i + 1] : yb1;
+                const uint64_t up2 = i > 0 ? v2[i - 1] : ya2, dn2 = i < RY - 1 ? v2[i + 1] : yb2;
                 const uint64_t s1  = grad_pair(xl[i], v2[i], up1, dn1);
                 const uint64_t s2  = grad_pair(v1[i], xr[i], up2, dn2);
                 const uint32_t e[4] = { pk_lo_bits(s1), pk_lo_bits(s2), pk_hi_bits(s1), pk_hi_bits(s2) };
-                if (r >= split) {
+                const bool     inr = r >= ra && r <= rb, hi = r >= split;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) m1[k] = max(m1[k], e[k]);
-                } else {
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t v = inr ? e[k] : 0u;
+                    m0[k]            = max(m0[k], hi ? 0u : v);
+                    m1[k]            = max(m1[k], hi ? v : 0u);
+                }
+            }
+            // per (column k, part h), bit 4h + k: decided by the FP32 maximum
+            // unless it lies in a band or some value is not finite; those take
+            // the exact rule
+            uint32_t kn = 0, an = 0, al = 0;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) m0[k] = max(m0[k], e[k]);
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t mb = b < 4 ? m0[b] : m1[b - 4];
+                const float    sm = __uint_as_float(mb);
+                const bool     k1 = rule.fast && mb < 0x7f800000u && (sm >= rule.r_hi || sm < rule.r_lo) &&
+                                (sm < rule.c_lo || sm >= rule.c_hi);
+                kn |= (k1 ? 1u : 0u) << b;
+                an |= (k1 && sm >= rule.r_hi ? 1u : 0u) << b;
+                al |= (!k1 || sm < rule.c_lo ? 1u : 0u) << b;
+            }
+            if (kn != 0xFFu) { // the exact FP64 rule on every cell of the undecided parts
+#pragma unroll
+                for (int i = 0; i < RY; ++i) {
+                    const int r = r0 + i;
+                    if (r < ra || r > rb) continue;
+                    const int      sh  = r >= split ? 4 : 0;
+                    const uint64_t up1 = i > 0 ? v1[i - 1] : ya1, dn1 = i < RY - 1 ? v1[i + 1] : yb1;
+                    const uint64_t up2 = i > 0 ? v2[i - 1] : ya2, dn2 = i < RY - 1 ? v2[i + 1] : yb2;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if ((kn >> (sh + k)) & 1u) continue;
+                        const uint64_t up = k & 1 ? up2 : up1, dn = k & 1 ? dn2 : dn1;
+                        const uint64_t wl = k & 1 ? v1[i] : xl[i], wh = k & 1 ? xr[i] : v2[i];
+                        const bool     hh = (k >> 1) != 0;
+                        const double   e  = grad_sq_exact2<float>(hh ? pk_hi(wl) : pk_lo(wl), hh ? pk_hi(wh) : pk_lo(wh),
+                                                                  hh ? pk_hi(up) : pk_lo(up), hh ? pk_hi(dn) : pk_lo(dn));
+                        if (e >= rule.rsq) an |= 1u << (sh + k);
+                        if (!(e < rule.csq)) al &= ~(1u << (sh + k));
+                    }
                 }
             }
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int c = c0 + (k & 1) + (k >> 1) * HW;
                 if (c < 0 || c > 63 || ra > rb) continue;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int lo = h ? split : ra, hi = h ? rb : min(rb, split - 1);
-                    if (lo > hi) continue;
-                    const uint32_t mb  = h ? m1[k] : m0[k];
-                    const float    sm  = __uint_as_float(mb);
-                    const bool     bad = mb >= 0x7f800000u;
-                    int            any = 0, all = 1;
-                    const bool known = rule.fast && !bad && (sm >= rule.r_hi || sm < rule.r_lo) &&
-                                       (sm < rule.c_lo || sm >= rule.c_hi);
-                    if (known) {
-                        any = sm >= rule.r_hi ? 1 : 0;
-                        all = sm < rule.c_lo ? 1 : 0;
-                    } else {
-                        // the exact rule on this column's cells of the part
-                        for (int i = 0; i < RY; ++i) {
-                            const int r = r0 + i;
-                            if (r < lo || r > hi) continue;
-                            uint64_t up, dn, wl, wh;
-                            if (k & 1) {
-                                up = i > 0 ? v2[i - 1] : ya.y;
-                                dn = i < RY - 1 ? v2[i + 1] : yb.y;
-                                wl = v1[i];
-                                wh = xr[i];
-                            } else {
-                                up = i > 0 ? v1[i - 1] : ya.x;
-                                dn = i < RY - 1 ? v1[i + 1] : yb.x;
-                                wl = xl[i];
-                                wh = v2[i];
-                            }
-                            const bool   hh = (k >> 1) != 0;
-                            const double e  = grad_sq_exact2<float>(hh ? pk_hi(wl) : pk_lo(wl), hh ? pk_hi(wh) : pk_lo(wh),
-                                                                    hh ? pk_hi(up) : pk_lo(up), hh ? pk_hi(dn) : pk_lo(dn));
-                            if (e >= rule.rsq) any = 1;
-                            if (!(e < rule.csq)) all = 0;
-                        }
-                    }
-                    const int pb = (lo >> 4) * 4 + (c >> 4); // normalized patch
-                    if (any) atomicOr(&pany[pb], 1);
-                    if (!all) atomicAnd(&pall[pb], 0);
+                const int pc = c >> 4;
+                if (ra <= min(rb, split - 1)) { // part 0
+                    const int pb = (ra >> 4) * 4 + pc;
+                    if ((an >> k) & 1u) atomicOr(&pany[pb], 1);
+                    if (!((al >> k) & 1u)) atomicAnd(&pall[pb], 0);
+                }
+                if (split <= rb) { // part 1
+                    const int pb = (split >> 4) * 4 + pc;
+                    if ((an >> (4 + k)) & 1u) atomicOr(&pany[pb], 1);
+                    if (!((al >> (4 + k)) & 1u)) atomicAnd(&pall[pb], 0);
                 }
             }
             __syncthreads(); // the exchange reads end before the stage overwrites X
@@ -527,20 +541,30 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         // px + 4 py keeps padded indices 16 .. 307 at p * STAGE); column X of
         // a patch's row also serves as the ghost column of its neighbour in
         // the block (X & 15 == 15: the next patch's column 0; X & 15 == 0:
-        // the previous patch's column 17)
-#pragma unroll
-        for (int i = 0; i < RY; ++i) {
-            const int r = r0 + i;
-            if (r < 0 || r > 63) continue;
-            const int   Y    = sy ? 63 - r : r;
-            float*      srow = stage + (Y >> 4) * 4 * STAGE + ((Y & 15) + 1) * 18 - 16;
-            const float e[4] = { pk_lo(v1[i]), pk_lo(v2[i]), pk_hi(v1[i]), pk_hi(v2[i]) };
+        // the previous patch's column 17).  Offsets per column k, -1 = none.
+        {
+            int oi[4], og[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int X = colX[k];
-                if (X >= 0 && X <= 63) srow[(X >> 4) * STAGE + (X & 15) + 1] = e[k];
-                if ((X & 15) == 15 && X + 1 >= 0 && X + 1 <= 63) srow[((X + 1) >> 4) * STAGE] = e[k];
-                if ((X & 15) == 0 && X - 1 >= 0 && X - 1 <= 63) srow[((X - 1) >> 4) * STAGE + 17] = e[k];
+                oi[k]       = (X >= 0 && X <= 63) ? (X >> 4) * STAGE + (X & 15) + 1 : -1;
+                og[k]       = ((X & 15) == 15 && X + 1 >= 0 && X + 1 <= 63)  ? ((X + 1) >> 4) * STAGE
+                              : ((X & 15) == 0 && X - 1 >= 0 && X - 1 <= 63) ? ((X - 1) >> 4) * STAGE + 17
+                                                                             : -1;
+            }
+#pragma unroll
+            for (int i = 0; i < RY; ++i) {
+                const int r = r0 + i;
+                if (r >= 0 && r <= 63) {
+                    const int   Y    = sy ? 63 - r : r;
+                    float*      srow = stage + (Y >> 4) * 4 * STAGE + ((Y & 15) + 1) * 18 - 16;
+                    const float e[4] = { pk_lo(v1[i]), pk_lo(v2[i]), pk_hi(v1[i]), pk_hi(v2[i]) };
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (oi[k] >= 0) srow[oi[k]] = e[k];
+                        if (og[k] >= 0) srow[og[k]] = e[k];
+                    }
+                }
             }
         }
         fence_proxy_async_smem(); // the stage writes before the async proxy reads them
@@ -560,12 +584,7 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
                 const int t   = tid - 128;
                 const int bpx = t & 3, bpy = t >> 2; // normalized block patch
                 const int px = sx ? 3 - bpx : bpx, py = sy ? 3 - bpy : bpy;
-                int       lo = min_level, hi = max_level;
-                if (B.bounds) {
-                    lo = __ldg(B.bounds + 2 * cur.inst);
-                    hi = __ldg(B.bounds + 2 * cur.inst + 1);
-                }
-                const int8_t f = gradient_decision(pany[t], pall[t], cur.L, lo, hi);
+                const int8_t f = gradient_decision(pany[t], pall[t], cur.L, cbound.x, cbound.y);
                 B.flags[pbase[py * 4 + px] / FLAT] = f;
                 if (f != FLAG_STABLE) ctl->flagged = 1;
             }
@@ -575,8 +594,10 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         if (tid < 16) bulk_wait_read<0>();
         __syncthreads();
         if (!more) break;
-        blk = nb;
-        cur = nxt;
+        blk    = nb;
+        cur    = nxt;
+        ccoef  = ncoef;
+        cbound = nbound;
     }
     if (tid < 16) bulk_wait_all();
 }

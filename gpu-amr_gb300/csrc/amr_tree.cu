@@ -687,7 +687,8 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         AMR_LAUNCHED("k_run_require_uniform");
     }
     if (key.fused) { // ... and is made of aligned 4x4 blocks
-        k_run_require_blocks<<<grid_for(static_cast<long long>(t->cap) / 16, 256), 256, 0, cs>>>(B, ctl, g);
+        k_run_require_blocks<<<grid_for(static_cast<long long>(t->cap) / 16, 256), 256, 0, cs>>>(B, ctl, g, key.up[0],
+                                                                                                 key.up[1]);
         AMR_LAUNCHED("k_run_require_blocks");
     }
     k_batch_begin<<<K, 256, 0, cs>>>(t->maxlev, g, t->vel, key.cfl, key.k, BATCH_NEXT, 0.0, t->dts(), t->step_dt,
@@ -708,10 +709,10 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
             constexpr int    nthr = IntervalShape<kFusedSteps>::THREADS;
             if (key.crit == 1)
                 k_run_interval2d<kFusedSteps, true><<<fused_grid<true>(t), nthr, smem, cs>>>(
-                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, key.up[0], key.up[1], 0);
+                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, 0);
             else
                 k_run_interval2d<kFusedSteps, false><<<fused_grid<false>(t), nthr, smem, cs>>>(
-                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, key.up[0], key.up[1], 0);
+                    B, ctl, g, t->coef32, cst, nl, rule, key.min_level, key.max_level, 0);
             AMR_LAUNCHED("k_run_interval2d");
             if (timed) AMR_CUDA(cudaEventRecord(ev->second, cs));
             constexpr int sp = 1; // the interval's result is in the other buffer
@@ -739,7 +740,8 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
                 k_run_neighbors<<<sms * 8, 128, 0, cs>>>(B, ctl, g);
                 AMR_LAUNCHED("k_run_neighbors");
             }
-            // a fused interval builds no pass or face records
+            // a fused interval builds no pass or face records (the face-record
+            // storage held its block descriptors)
             k_run_commit<<<1, 256, 0, cs>>>(B, ctl, key.k, g.cells, key.crit != 0 ? 1 : 0, sp, 0);
             AMR_LAUNCHED("k_run_commit");
             return AMR_OK;
