@@ -53,7 +53,7 @@ BATCHED = dict(
     instances=512, n=16, halo=1, depth=6, cap_lo=2, cap_hi=6, steps=1000, remesh=10, cfl=0.4, rthr=0.05, cthr=0.01,
     seed=3, bumps=2, sigma=(0.02, 0.06), amp=(0.5, 2.0),
 )
-BATCHED_NAME = ("batched: 512 independent 2D advection AMR instances in one forest, 16x16 patches + 1 ghost, "
+BATCHED_NAME = ("batched, static caps: 512 independent 2D advection AMR instances in one forest, 16x16 patches + 1 ghost, "
                 "seeded depth caps 2-6 (refined to the cap and held: min = max level), seeded velocities in "
                 "[-1,1]^2, 2 seeded Gaussian bumps each, grad criterion 0.05/0.01, re-mesh every 10 steps "
                 "(one CUDA graph replay per interval), CFL 0.4, 1000 steps, FP32 state")
@@ -179,13 +179,15 @@ def batched_ic(torch, ids, bumps, dev):
     return out, inst
 
 
-def make_forest(A, dtype, stream, caps, vel):
+def make_forest(A, dtype, stream, caps, vel, bounds=None):
+    """The batched forest refined to its caps; level bounds per instance
+    (default: held at the cap)."""
     B = BATCHED
     K = B["instances"]
     cap = int(np.sum(4 ** caps.astype(np.int64))) + 1024
     f = A.Tree(2, B["n"], B["halo"], B["depth"], capacity=cap, dtype=dtype, stream=stream.cuda_stream, instances=K)
     f.refine_to_levels(caps)
-    f.set_instance_params(velocity=vel, level_bounds=np.stack([caps, caps], 1))
+    f.set_instance_params(velocity=vel, level_bounds=np.stack([caps, caps], 1) if bounds is None else bounds)
     return f
 
 
@@ -220,6 +222,56 @@ def time_runs(torch, stream, world, k, setup, body, flush, clocks=None):
     return total_ms, launches, stats, info
 
 
+def e2e_pipeline(torch, stream, f, P, like, host_in, host_out, K, warmup, world):
+    """K complete runs of forest f, each fed from pinned host memory and read
+    back to it, copies overlapped with the runs on a second stream.  Returns
+    (ms of the K runs, cell updates); warm-up runs first."""
+    copy = torch.cuda.Stream()
+    st_in = [torch.empty_like(like) for _ in range(2)]
+    st_out = [torch.empty_like(like) for _ in range(2)]
+    ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("in", "used", "res", "out")}
+
+    def pipeline(n):
+        e0, e1 = _events(torch)
+        e0.record(stream)
+        copy.wait_event(e0)
+        with torch.cuda.stream(copy):
+            st_in[0].copy_(host_in, non_blocking=True)
+            ev["in"][0].record(copy)
+        cells = 0
+        for k in range(n):
+            b = k % 2
+            stream.wait_event(ev["in"][b])
+            f.load_state_device(st_in[b].data_ptr(), P)
+            ev["used"][b].record(stream)
+            if k + 1 < n:  # the next run's input, into the other staging buffer
+                nb = (k + 1) % 2
+                with torch.cuda.stream(copy):
+                    if k >= 1:
+                        copy.wait_event(ev["used"][nb])
+                    st_in[nb].copy_(host_in, non_blocking=True)
+                    ev["in"][nb].record(copy)
+            cells += run_forest(f)["cell_updates"]
+            if k >= 2:
+                stream.wait_event(ev["out"][b])  # run k - 2's download has read st_out[b]
+            f.download_state_device(st_out[b].data_ptr(), P)
+            ev["res"][b].record(stream)
+            with torch.cuda.stream(copy):
+                copy.wait_event(ev["res"][b])
+                host_out[b].copy_(st_out[b], non_blocking=True)
+                ev["out"][b].record(copy)
+        stream.wait_stream(copy)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), cells
+
+    pipeline(max(1, warmup))  # the host buffers' first transfers are not part of a step
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    return pipeline(K)
+
+
 def batched_arm(args, torch, A, dev, stream, flush, world):
     B = BATCHED
     caps, vel, bumps = batched_instances()
@@ -245,17 +297,13 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
     fin32 = torch.empty_like(ic32)
     f32.download_state_device(fin32.data_ptr(), P)
 
-    # end to end: initial state from pinned host memory, final state back
-    def e2e_body():
-        A.check(A.lib().amr_tree_upload_state(f32._h, ic32_host.data_ptr(), P))
-        st = run_forest(f32)
-        A.check(A.lib().amr_tree_download_state(f32._h, out32_host.data_ptr(), P))
-        return st
-
-    for _ in range(args.warmup):  # the host buffers' first transfers are not part of a step
-        e2e_body()
-    e2e_ms, _, e2e_stats, _ = time_runs(torch, stream, world, args.steps, lambda: None, e2e_body, flush)
-    e2e_cells = sum(s["cell_updates"] for s in e2e_stats)
+    # end to end, K runs: each run's initial state comes from pinned host
+    # memory and its final state goes back to pinned host memory; the copies
+    # run on a second stream, the upload of run k + 1 and the download of run
+    # k - 1 beside run k (two device staging buffers each way)
+    out32_host2 = torch.empty_like(ic32_host).pin_memory()
+    e2e_ms, e2e_cells = e2e_pipeline(torch, stream, f32, P, ic32, ic32_host, [out32_host, out32_host2], args.steps,
+                                     args.warmup, world)
 
     # the update kernel alone: CUDA events around each launch on the forest's
     # stream, in a complete run whose intervals are issued directly instead of
@@ -284,6 +332,21 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
     cells64 = sum(s["cell_updates"] for s in stats64)
     fin64 = torch.empty_like(ic64)
     f64.download_state_device(fin64.data_ptr(), P)
+
+    # parity sample: the CPU baseline's instances, the same number of steps,
+    # from the same initial state, in FP64 and FP32 (compared in main())
+    npar, spar = CPU_SAMPLE["instances"], CPU_SAMPLE["steps"]
+    off = f32.instance_offsets()
+    mask = np.uint64((1 << (6 + 2 * B["depth"])) - 1)
+    parity = {"init": [ic64[off[i]:off[i + 1]].cpu().numpy() for i in range(npar)], "steps": spar}
+    for key, f, ic in (("f64", f64, ic64), ("f32", f32, ic32)):
+        f.load_state_device(ic.data_ptr(), P)
+        f.run(spar, B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+        fin = torch.empty_like(ic)
+        f.download_state_device(fin.data_ptr(), P)
+        o = f.instance_offsets()
+        ids = f.ids()
+        parity[key] = [(ids[o[i]:o[i + 1]] & mask, fin[o[i]:o[i + 1]].double().cpu().numpy()) for i in range(npar)]
     n, h = B["n"], B["halo"]
     a = fin32[:, h:n + h, h:n + h].to(torch.float64)
     b = fin64[:, h:n + h, h:n + h]
@@ -318,6 +381,7 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
     value64 = cells64 / (ms64 * 1e-3)
     return {
         "value": value,
+        "parity": parity,
         "ms": ms,
         "cells": cells,
         "e2e_ms": e2e_ms,
@@ -368,6 +432,115 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
             "reference": "FP64 run of the same forest on the GPU (the FP64 path equals the oracle within 1e-12)",
             "fp64_kept_for": "CFL step, coarse-fine restriction/prolongation means, gradient flags",
         },
+    }
+
+
+# ------------------------------------------------ batched form, adapting
+ACTIVE_NAME = ("batched, adapting: the batched workload's 512 instances, each free to coarsen two levels below "
+               "its cap and to refine back to it (level bounds (cap - 2, cap)), so the gradient flags re-mesh "
+               "the forest every interval; 1000 steps, FP32 state")
+
+
+def batched_active_extra(args, torch, A, dev, stream, flush, world):
+    """The batched forest with level bounds that let it adapt: the trees
+    change at the re-meshes, coarse-fine faces appear and the update runs as
+    one-step launches.  FP32 throughput, re-mesh counts and leaf range, the
+    FP64 run of the same forest, a roofline of the one-step update, and the
+    first instances against the oracle."""
+    B = BATCHED
+    caps, vel, bmp = batched_instances()
+    bounds = np.stack([np.maximum(caps - 2, 0), caps], 1).astype(np.int32)
+    f32 = make_forest(A, A.F32, stream, caps, vel, bounds)
+    ids0 = f32.ids()
+    P0 = len(ids0)
+    ic64, _ = batched_ic(torch, ids0, bmp, dev)
+    ic32 = ic64.to(torch.float32).contiguous()
+    # the runs change the forest: each run starts from the refined forest
+    snap_ids = ids0.copy()
+
+    def reset(f, ic):
+        f.reset()
+        f.refine_to_levels(caps)
+        assert np.array_equal(f.ids(), snap_ids)
+        f.load_state_device(ic.data_ptr(), P0)
+
+    def run(f):
+        return f.run(B["steps"], B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+
+    for _ in range(max(1, args.warmup - 1)):
+        reset(f32, ic32)
+        run(f32)
+    ms, launches, stats, _ = time_runs(torch, stream, world, max(1, args.steps), lambda: reset(f32, ic32),
+                                       lambda: run(f32), flush)
+    cells = sum(st["cell_updates"] for st in stats)
+    st0 = stats[0]
+    ids32 = f32.ids()
+    s32 = torch.empty((len(ids32), B["n"] + 2, B["n"] + 2), dtype=torch.float32, device=dev)
+    f32.download_state_device(s32.data_ptr(), len(ids32))
+    # the one-step update timed alone inside a run (CUDA events per launch)
+    reset(f32, ic32)
+    f32.set_timing(True)
+    run(f32)
+    k_ms, k_launches, k_cells = f32.get_timing()
+    f32.set_timing(False)
+    # the same forest in FP64
+    f64 = make_forest(A, A.F64, stream, caps, vel, bounds)
+    reset(f64, ic64)
+    ms64, _, stats64, _ = time_runs(torch, stream, world, 1, lambda: reset(f64, ic64), lambda: run(f64), flush)
+    ids64 = f64.ids()
+    same = bool(np.array_equal(ids64, ids32))
+    rel = None
+    if same:
+        s64 = torch.empty((len(ids64), B["n"] + 2, B["n"] + 2), dtype=torch.float64, device=dev)
+        f64.download_state_device(s64.data_ptr(), len(ids64))
+        n, h = B["n"], B["halo"]
+        a, b = s32[:, h:n + h, h:n + h].double(), s64[:, h:n + h, h:n + h]
+        rel = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    # the first instances against the oracle, 100 steps from the same state
+    npar, spar = 8, 100
+    off = f64.instance_offsets()
+    init = [ic64[off[i]:off[i + 1]].cpu().numpy() for i in range(npar)]
+    reset(f64, ic64)
+    f64.run(spar, B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+    fin = torch.empty((len(f64.ids()), B["n"] + 2, B["n"] + 2), dtype=torch.float64, device=dev)
+    f64.download_state_device(fin.data_ptr(), len(f64.ids()))
+    o, gids = f64.instance_offsets(), f64.ids()
+    mask = np.uint64((1 << (6 + 2 * B["depth"])) - 1)
+    _, _, _, finals = cpu_batched(os.cpu_count() or 1, npar, spar, init=init, bounds=bounds)
+    trees, worst = True, 0.0
+    n, h = B["n"], B["halo"]
+    for i, (oids, ost) in enumerate(finals):
+        trees &= bool(np.array_equal(gids[o[i]:o[i + 1]] & mask, oids))
+        if trees:
+            g = fin[o[i]:o[i + 1]].cpu().numpy()[:, h:n + h, h:n + h]
+            r = ost[:, h:n + h, h:n + h]
+            worst = max(worst, float(np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-300)))
+    f32.close()
+    f64.close()
+    hbm = measured_peaks().get("hbm_gbs")
+    achieved = 8.0 * k_cells / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    value = cells / (ms * 1e-3)
+    return {
+        "workload": ACTIVE_NAME,
+        "value": value, "unit": UNIT, "ms_per_run": ms / max(1, args.steps), "dtype": "f32",
+        "leaves": {"start": P0, "min": int(st0["leaves_min"]), "max": int(st0["leaves_max"]),
+                   "mean": float(st0["leaves_mean"])},
+        "remeshes": int(st0["remeshes"]), "remeshes_changed": int(st0["remeshes_changed"]),
+        "update_share_of_run": (k_ms / (ms / max(1, args.steps))) if ms > 0 else None,
+        "gpu_launches": int(launches // max(1, args.steps)),
+        "fp64_same_forest": {"value": sum(st["cell_updates"] for st in stats64) / (ms64 * 1e-3), "unit": UNIT,
+                             "same_final_tree_as_fp32": same, "rel_l2_fp32_vs_fp64": rel},
+        "roofline": {
+            "bound": "hbm", "kernel": "k_run_step2d<float,16,1,W,S> (one step per launch: the forest has "
+                                      "coarse-fine faces)",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if achieved and hbm else None,
+            "algorithmic_bytes_per_cell_update": 8, "launches": int(k_launches),
+            "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured, burst copy)" if hbm else "missing",
+        },
+        "parity": {"sample": f"instances 0-{npar - 1}, {spar} steps, FP64, against the oracle",
+                   "trees_bit_exact": trees, "max_instance_rel_l2": worst, "bar": 1e-12,
+                   "within_bar": bool(trees and worst <= 1e-12)},
     }
 
 
@@ -1209,6 +1382,7 @@ def gpu_arm(args, rank, world):
     if not args.no_extras:
         cpu = not args.no_cpu_baseline
         table = {
+            "batched_active": lambda: batched_active_extra(args, torch, A, dev, stream, flush, world),
             "plain_fp64_config2": lambda: plain_config2(args, torch, A, dev, stream, flush, world),
             "adjoint": lambda: adjoint_extra(torch, A, dev, stream, with_oracle=cpu),
             "config3_3d": lambda: config3_extra(torch, A, dev, stream, flush, max(1, args.steps)),
@@ -1254,44 +1428,85 @@ def gpu_arm(args, rank, world):
         "precision": bt["precision"],
         "clocks": bt["clocks"],
         "gpu_launches": int(bt["launches"]),
+        "_parity": bt["parity"],
     }
     line.update(extras)
     return line
 
 
 # ------------------------------------------------------------------ CPU arms
-def cpu_batched(threads: int, instances: int, steps: int):
+def cpu_batched(threads: int, instances: int, steps: int, init=None, bounds=None):
     """The oracle (C restatement of the reference) on the host cores: the
     first `instances` instances of the batched workload, each a separate
-    tree, truncated to `steps` steps."""
+    tree, truncated to `steps` steps.  init: per instance the padded FP64
+    initial state the GPU forest starts from (else the oracle's own bumps);
+    bounds: per-instance (min, max) levels (default: held at the cap).
+    Returns the cell updates, the seconds of the loops, the caps, and per
+    instance the final (Morton ids, padded state)."""
     from oracle import oracle as O
 
     O.set_threads(threads)
     B = BATCHED
     caps, vel, bmp = batched_instances()
-    cells, secs = 0, 0.0
+    cells, secs, finals = 0, 0.0, []
     for i in range(instances):
+        lo, hi = (int(caps[i]), int(caps[i])) if bounds is None else (int(bounds[i][0]), int(bounds[i][1]))
+        t = O.OracleTree(2, B["n"], B["halo"], B["depth"], int(4 ** hi) * 2 + 64)
+        t.refine_all(int(caps[i]))
+        if init is None:
+            t.init_state([float(v) for v in bmp[i].ravel()])
+        else:
+            t.set_state(init[i])
+        t.halo_exchange()
         t0 = time.perf_counter()
-        _, _, _, c, _ = O.run_scenario(
-            2, B["n"], B["halo"], B["depth"], init_levels=int(caps[i]), steps=steps, remesh=B["remesh"],
-            velocity=tuple(vel[i]), cfl=B["cfl"], bumps=[float(v) for v in bmp[i].ravel()], crit="grad",
-            rthr=B["rthr"], cthr=B["cthr"], min_level=int(caps[i]), max_level=int(caps[i]),
-            capacity=int(4 ** caps[i]) + 16)
+        done = 0
+        while done < steps:
+            k = min(B["remesh"], steps - done)
+            leaves = t.size
+            _, ex = t.advance(k, tuple(vel[i]), B["cfl"])
+            done += ex
+            cells += ex * leaves * B["n"] ** 2
+            f = t.flags_gradient(B["rthr"], B["cthr"], lo, hi)
+            if t.reconstruct(f) != 0:
+                raise RuntimeError("oracle re-mesh failed")
+            t.halo_exchange()
+            if ex == 0:
+                break
         secs += time.perf_counter() - t0
-        cells += c
-    return cells, secs, caps[:instances]
+        finals.append((t.ids(), t.state()))
+    return cells, secs, caps[:instances], finals
 
 
 CPU_SAMPLE = dict(instances=32, steps=100)
 
 
-def cpu_baseline():
+def parity_report(par, finals):
+    """The headline forest against the oracle on the CPU baseline's sample:
+    per instance the final leaves (bit-exact) and the relative L2 of the
+    interior state, GPU FP64 (bar 1e-12) and GPU FP32 (bar 1e-5)."""
+    n, h = BATCHED["n"], BATCHED["halo"]
+    out = {"sample": f"instances 0-{len(finals) - 1}, {par['steps']} steps from the GPU forest's initial state, "
+                     f"against the oracle (FP64, C restatement pinned to the reference)"}
+    for key, bar in (("f64", 1e-12), ("f32", 1e-5)):
+        trees, worst = True, 0.0
+        for (gids, gst), (oids, ost) in zip(par[key], finals):
+            trees &= bool(np.array_equal(np.asarray(gids, np.uint64), np.asarray(oids, np.uint64)))
+            a, b = gst[:, h:n + h, h:n + h], ost[:, h:n + h, h:n + h]
+            worst = max(worst, float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)))
+        out[key] = {"trees_bit_exact": trees, "max_instance_rel_l2": worst, "bar": bar,
+                    "within_bar": bool(trees and worst <= bar)}
+    return out
+
+
+def cpu_baseline(init=None):
+    """The timed CPU sample; with init (the GPU forest's initial states of the
+    sampled instances) also the sample's final trees and states."""
     threads = os.cpu_count() or 1
-    cells, secs, caps = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"])
+    cells, secs, caps, finals = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"], init=init)
     return {"value": cells / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"instances 0-{CPU_SAMPLE['instances'] - 1} of the batched workload ({int(np.sum(4 ** caps))} "
-                      f"patches), first {CPU_SAMPLE['steps']} steps each, FP64, OpenMP over patches like "
-                      f"EXECUTION=PAR"}
+                      f"patches), first {CPU_SAMPLE['steps']} steps each from the GPU forest's initial state, FP64, "
+                      f"OpenMP over patches like EXECUTION=PAR"}, finals
 
 
 def cpu_plain(steps=600):
@@ -1323,13 +1538,14 @@ def reference_arm(args, rank, world):
         cpu_batched(threads, 4, 20)
     total_cells, total_s, caps = 0, 0.0, None
     for _ in range(args.steps):
-        c, s, caps = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"])
+        c, s, caps, _ = cpu_batched(threads, CPU_SAMPLE["instances"], CPU_SAMPLE["steps"])
         total_cells += c
         total_s += s
     value = total_cells / total_s
     sample = (f"instances 0-{CPU_SAMPLE['instances'] - 1} of the batched workload ({int(np.sum(4 ** caps))} patches), "
-              f"first {CPU_SAMPLE['steps']} steps each, FP64; the C restatement of the reference "
-              f"(the reference's own build is x86-only here), OpenMP over patches")
+              f"first {CPU_SAMPLE['steps']} steps each, FP64; the C restatement of the reference, pinned bit-exact to "
+              f"the reference's own runs (its sources are not on this host, so the reference itself cannot be built "
+              f"here), OpenMP over patches")
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -1448,8 +1664,11 @@ def main():
         torch.distributed.init_process_group("nccl")
     line = gpu_arm(args, rank, world)
     if line is not None:
+        par = line.pop("_parity", None)
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline()
+            line["cpu_baseline"], finals = cpu_baseline(init=par["init"] if par else None)
+            if par:
+                line["parity"] = parity_report(par, finals)
             if "plain_fp64_config2" in line:
                 line["plain_fp64_config2"]["cpu_baseline"] = cpu_plain()
         print(json.dumps(line), flush=True)

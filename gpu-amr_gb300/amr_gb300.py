@@ -63,7 +63,7 @@ class CycleStats(C.Structure):
     _fields_ = [("executed_steps", C.c_uint64), ("sum_dt", C.c_double), ("cell_updates", C.c_uint64),
                 ("remeshes", C.c_uint64), ("intervals", C.c_uint64), ("leaves_min", C.c_uint64),
                 ("leaves_max", C.c_uint64), ("leaves_mean", C.c_double), ("persistent_intervals", C.c_uint64),
-                ("graph_intervals", C.c_uint64)]
+                ("graph_intervals", C.c_uint64), ("remeshes_changed", C.c_uint64)]
 
 
 class DgStats(C.Structure):

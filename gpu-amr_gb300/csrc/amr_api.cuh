@@ -269,6 +269,7 @@ struct RunTotals {
     long long done     = 0;
     double    sum_dt   = 0.0;
     uint64_t  executed = 0, cells = 0, remeshes = 0, intervals = 0, leaves_sum = 0, persistent = 0, graphs = 0;
+    uint64_t  remeshes_changed = 0; // re-meshes that changed the tree
     uint64_t  lmin = ~0ull, lmax = 0;
 };
 

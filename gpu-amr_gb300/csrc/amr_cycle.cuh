@@ -31,7 +31,7 @@ struct CycleStats {
     int32_t  leaves_min, leaves_max;
     int32_t  P, tb, cur, max_level;
     int32_t  error, stopped;
-    double   pad;
+    uint64_t remeshes_changed; // re-meshes that changed the tree
 };
 
 struct CycleArgs {
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
     int       P = A.P0, tb = A.tb0, cur = 0, maxlevel = A.max_level0;
     long long done = 0;
     double    sum_dt = 0.0;
-    uint64_t  executed_total = 0, cell_updates = 0, remeshes = 0, leaves_sum = 0, intervals = 0;
+    uint64_t  executed_total = 0, cell_updates = 0, remeshes = 0, leaves_sum = 0, intervals = 0, remeshes_changed = 0;
     int       lmin = P, lmax = P, error = 0, stopped = 0;
 
     while (done < A.steps_total) {
@@ -236,6 +236,7 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
             break;
         }
         if (changed) {
+            ++remeshes_changed;
             const T* old_state = static_cast<const T*>(A.state[cur]);
             T*       new_state = static_cast<T*>(A.state[cur ^ 1]);
             for (long long t = gtid; t < static_cast<long long>(NP) * g.cells; t += nthreads) {
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
         s.max_level    = maxlevel;
         s.error        = error;
         s.stopped      = stopped;
-        s.pad          = 0.0;
+        s.remeshes_changed = remeshes_changed;
         *A.stats       = s;
     }
 }

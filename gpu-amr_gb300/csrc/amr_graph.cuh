@@ -28,7 +28,7 @@ struct RunCtl {
     int32_t uniform;    // every neighbour relation of the current tree is "same level"
     int32_t flagged;    // some leaf of the pending re-mesh is flagged (zeroed at each commit)
     int32_t recs;       // the pass and face records describe the current tree (zero at a run's start)
-    unsigned long long cell_updates, leaves_sum, intervals, remeshes;
+    unsigned long long cell_updates, leaves_sum, intervals, remeshes, remeshes_changed;
 };
 
 struct RunBufs {
@@ -447,6 +447,7 @@ k_run_commit(RunBufs B, RunCtl* ctl, int steps, int cells, int remesh, int sp, i
             ctl->leaves_min = min(ctl->leaves_min, P);
             ctl->leaves_max = max(ctl->leaves_max, P);
             if (remesh) ctl->remeshes += 1;
+            if (chg) ctl->remeshes_changed += 1;
         }
     }
     __syncthreads();

@@ -372,6 +372,7 @@ amr_status amr_tree_euler_run(amr_tree* t, const amr_euler_params* p, amr_cycle_
         st          = amr_tree_remesh(t, &changed);
         if (st != AMR_OK) return st;
         ++tot.remeshes;
+        if (changed) ++tot.remeshes_changed;
         double acc = 0.0;
         size_t ex  = 0;
         st         = amr_tree_finish_advance(t, &acc, &ex);
@@ -397,6 +398,7 @@ amr_status amr_tree_euler_run(amr_tree* t, const amr_euler_params* p, amr_cycle_
         out->sum_dt         = time;
         out->cell_updates   = tot.cells;
         out->remeshes       = tot.remeshes;
+        out->remeshes_changed = tot.remeshes_changed;
         out->intervals      = tot.intervals;
         out->leaves_min     = tot.intervals ? tot.lmin : t->size;
         out->leaves_max     = tot.intervals ? tot.lmax : t->size;

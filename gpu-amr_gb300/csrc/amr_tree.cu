@@ -674,10 +674,11 @@ amr_status timing_slot(amr_tree* t, uint64_t cells, std::pair<cudaEvent_t, cudaE
 }
 
 // The launch sequence of one interval on stream cs (captured into a graph,
-// or launched directly with `timed`: CUDA events around the fused launch).
+// or launched directly with `timed` > 0: CUDA events around each update
+// launch, `timed` being the interval's leaf count for the cell counts).
 // Grids are fixed; every kernel takes the leaf count from the control block.
 template <typename T>
-amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaStream_t cs, bool timed = false)
+amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, cudaStream_t cs, uint64_t timed = 0)
 {
     const Geo& g   = t->g;
     const int  K   = t->ninst, nl = g.depth + 1, sms = num_sms();
@@ -698,9 +699,7 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         if (key.fused) { // the whole interval: steps and gradient flags in one kernel
             std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
             if (timed) {
-                if (amr_status ts = timing_slot(t, static_cast<uint64_t>(t->size) * g.cells * key.k, &ev);
-                    ts != AMR_OK)
-                    return ts;
+                if (amr_status ts = timing_slot(t, timed * g.cells * key.k, &ev); ts != AMR_OK) return ts;
                 AMR_CUDA(cudaEventRecord(ev->first, cs));
             }
             const size_t     cst  = static_cast<size_t>(K) * nl;
@@ -768,6 +767,11 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
         const float2* cf2 = t->coef32 + static_cast<size_t>(step) * K * nl;
         const size_t  cst = static_cast<size_t>(K) * nl;
         amr_status    st  = AMR_OK;
+        std::pair<cudaEvent_t, cudaEvent_t>* ev = nullptr;
+        if (timed) {
+            if (amr_status ts = timing_slot(t, timed * g.cells * D, &ev); ts != AMR_OK) return ts;
+            AMR_CUDA(cudaEventRecord(ev->first, cs));
+        }
         auto pass = [&]<int N>() -> amr_status {
             return with_depth<T>(D, [&]<int DD>() -> amr_status {
                 return launch_run_step2d_pass<T, N, 1, DD>(B, ctl, nl, cf, cf2, cst, par, cfg,
@@ -784,6 +788,7 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
             AMR_LAUNCHED("k_run_step");
         }
         if (st != AMR_OK) return st;
+        if (timed) AMR_CUDA(cudaEventRecord(ev->second, cs));
         step += D;
     }
     // parity of the buffer holding the interval's result
@@ -1037,10 +1042,15 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     }
     if (t->timing) {
         // timed: the same launch sequence issued directly, CUDA events
-        // around each fused launch
+        // around each update launch; the leaf count of each interval is read
+        // back first (it changes with the re-meshes)
         auto direct = [&](const GraphKey& kk) -> amr_status {
-            return t->dtype == AMR_F64 ? record_interval<double>(t, kk, B, s, kk.fused != 0)
-                                       : record_interval<float>(t, kk, B, s, kk.fused != 0);
+            int32_t* hp = reinterpret_cast<int32_t*>(static_cast<char*>(t->pinned) + 64 + sizeof(RunCtl));
+            AMR_CUDA(cudaMemcpyAsync(hp, &t->ctl->P, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            AMR_CUDA(cudaStreamSynchronize(s));
+            const uint64_t Pi = static_cast<uint64_t>(std::max(1, *hp));
+            return t->dtype == AMR_F64 ? record_interval<double>(t, kk, B, s, Pi)
+                                       : record_interval<float>(t, kk, B, s, Pi);
         };
         for (long long i = 0; i < nfull; ++i)
             if (amr_status st = direct(key_full); st != AMR_OK) return st;
@@ -1102,6 +1112,7 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     tot.executed = cmax;
     tot.cells += r.cell_updates;
     tot.remeshes += r.remeshes;
+    tot.remeshes_changed += r.remeshes_changed;
     tot.intervals += r.intervals;
     tot.graphs += r.intervals;
     tot.leaves_sum += r.leaves_sum;
@@ -1943,6 +1954,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             tot.executed += cs.executed;
             tot.cells += cs.cell_updates;
             tot.remeshes += cs.remeshes;
+            tot.remeshes_changed += cs.remeshes_changed;
             tot.intervals += cs.intervals;
             tot.persistent += cs.intervals;
             tot.leaves_sum += cs.leaves_sum;
@@ -1999,6 +2011,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             st          = amr_tree_remesh(t, &changed);
             if (st != AMR_OK) return st;
             ++tot.remeshes;
+            if (changed) ++tot.remeshes_changed;
         }
         if (ex == 0) break;
     }
@@ -2007,6 +2020,7 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
         out->sum_dt               = tot.sum_dt;
         out->cell_updates         = tot.cells;
         out->remeshes             = tot.remeshes;
+        out->remeshes_changed     = tot.remeshes_changed;
         out->intervals            = tot.intervals;
         out->leaves_min           = tot.intervals ? tot.lmin : t->size;
         out->leaves_max           = tot.intervals ? tot.lmax : t->size;

@@ -276,6 +276,7 @@ typedef struct amr_cycle_stats {
     double   leaves_mean;
     uint64_t persistent_intervals; /* intervals run inside the cluster kernel */
     uint64_t graph_intervals;      /* intervals run as graph replays */
+    uint64_t remeshes_changed;     /* re-meshes that changed the tree */
 } amr_cycle_stats;
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* params, amr_cycle_stats* stats);
