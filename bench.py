@@ -222,6 +222,28 @@ def time_runs(torch, stream, world, k, setup, body, flush, clocks=None):
     return total_ms, launches, stats, info
 
 
+# runs of the end-to-end pipeline: the first upload and the last download
+# are not hidden behind a run, so more runs amortise them
+E2E_RUNS = 8
+
+
+def copy_rates(torch, stream, dev, host_in, host_out):
+    """GB/s of one pinned host -> device and one device -> host copy of the
+    state, each timed alone with CUDA events on the forest's stream."""
+    out = []
+    with torch.cuda.stream(stream):
+        for src, dst in ((host_in, dev), (dev, host_out)):
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            e0, e1 = _events(torch)
+            e0.record(stream)
+            dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out.append(src.numel() * src.element_size() / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    return out
+
+
 def e2e_pipeline(torch, stream, f, P, like, host_in, host_out, K, warmup, world):
     """K complete runs of forest f, each fed from pinned host memory and read
     back to it, copies overlapped with the runs on a second stream.  Returns
@@ -302,8 +324,11 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
     # run on a second stream, the upload of run k + 1 and the download of run
     # k - 1 beside run k (two device staging buffers each way)
     out32_host2 = torch.empty_like(ic32_host).pin_memory()
-    e2e_ms, e2e_cells = e2e_pipeline(torch, stream, f32, P, ic32, ic32_host, [out32_host, out32_host2], args.steps,
+    e2e_runs = max(args.steps, E2E_RUNS)
+    e2e_ms, e2e_cells = e2e_pipeline(torch, stream, f32, P, ic32, ic32_host, [out32_host, out32_host2], e2e_runs,
                                      args.warmup, world)
+    # the host link alone: one state upload and one download, timed apart
+    h2d_gbs, d2h_gbs = copy_rates(torch, stream, ic32, ic32_host, out32_host)
 
     # the update kernel alone: CUDA events around each launch on the forest's
     # stream, in a complete run whose intervals are issued directly instead of
@@ -403,7 +428,10 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
                                         "blocks": tuned[2] or "full residency"},
         },
         "e2e": {"value": e2e_cells / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(ic32_host.numel() * 4),
-                "d2h_bytes_per_step": int(out32_host.numel() * 4)},
+                "d2h_bytes_per_step": int(out32_host.numel() * 4), "runs": e2e_runs,
+                "note": "each run uploads its initial state from pinned host memory and downloads its final state; "
+                        "the copies of neighbouring runs overlap the run on a second stream",
+                "host_link_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}},
         "roofline": {
             "bound": "hbm",
             "kernel": ("k_run_interval2d<10,true> (the whole re-mesh interval, ten steps and the gradient flags, "
@@ -477,8 +505,8 @@ def batched_active_extra(args, torch, A, dev, stream, flush, world):
     ids32 = f32.ids()
     s32 = torch.empty((len(ids32), B["n"] + 2, B["n"] + 2), dtype=torch.float32, device=dev)
     f32.download_state_device(s32.data_ptr(), len(ids32))
-    # the one-step update timed alone inside a run (CUDA events per launch)
-    reset(f32, ic32)
+    # the one-step update timed alone (CUDA events per launch) in a run that
+    # continues from the adapted forest, so every launch is a one-step update
     f32.set_timing(True)
     run(f32)
     k_ms, k_launches, k_cells = f32.get_timing()
@@ -498,9 +526,9 @@ def batched_active_extra(args, torch, A, dev, stream, flush, world):
         rel = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
     # the first instances against the oracle, 100 steps from the same state
     npar, spar = 8, 100
+    reset(f64, ic64)
     off = f64.instance_offsets()
     init = [ic64[off[i]:off[i + 1]].cpu().numpy() for i in range(npar)]
-    reset(f64, ic64)
     f64.run(spar, B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
     fin = torch.empty((len(f64.ids()), B["n"] + 2, B["n"] + 2), dtype=torch.float64, device=dev)
     f64.download_state_device(fin.data_ptr(), len(f64.ids()))
@@ -647,7 +675,14 @@ def plain_config2(args, torch, A, dev, stream, flush, world):
 # ---------------------------------------------- further single-tree workloads
 CONFIG3 = dict(rank=3, n=8, halo=1, depth=6, init_levels=1, steps=500, remesh=10, velocity=(1.0, 0.7, 0.3), cfl=0.4,
                rthr=0.05, cthr=0.01, min_level=1, max_level=4, bump_seed=3, bumps=4, sigma=(0.05, 0.08))
-DEPTH7 = dict(WORKLOAD, max_level=7)
+# config 2's tree never passes ~43 leaves at max level 5, and the gradient
+# criterion at its thresholds stops refining near level 5 whatever the cap;
+# the labelled deep variant lowers the thresholds 50x and allows level 8
+# (Morton depth 8), which keeps ~4-6k leaves of an adapting tree
+DEEP = dict(WORKLOAD, depth=8, init_levels=4, min_level=3, max_level=8, rthr=0.001, cthr=0.0002)
+DEEP_NAME = ("2D linear advection, active AMR, FP64 plain, deep variant of config 2: 16x16 patches + 1 ghost, "
+             "level 4 start, levels 3-8, grad criterion 0.001/0.0002 (config 2's thresholds / 50), re-mesh every "
+             "10 steps, 2 seeded Gaussian bumps, v=(1,0.5), periodic, CFL 0.4, 2000 steps")
 
 
 def single_tree_runs(torch, A, dev, stream, flush, cfg, dtype, bumps_list, noise, noise_seed, reps):
@@ -698,16 +733,81 @@ def config3_extra(torch, A, dev, stream, flush, reps):
     }
 
 
-def depth7_extra(torch, A, dev, stream, flush, reps):
-    ms, st, _, _ = single_tree_runs(torch, A, dev, stream, flush, DEPTH7, A.F64, bumps(), WORKLOAD["noise"],
-                                    WORKLOAD["noise_seed"], reps)
-    return {
-        "workload": WORKLOAD_NAME.replace("max level 5", "max level 7") + " (max-level-7 variant)",
-        "value": st["cell_updates"] / (ms * 1e-3), "unit": UNIT, "ms_per_run": ms, "dtype": "f64",
-        "leaves_min": st["leaves_min"], "leaves_max": st["leaves_max"], "leaves_mean": st["leaves_mean"],
+def deep_extra(torch, A, dev, stream, flush, reps, with_cpu=True):
+    """The deep variant of config 2 (4-6k leaves) in FP64 through the device
+    tree: throughput, leaf range, a roofline of the one-step FP64 update on the
+    adapted tree, and the oracle on the host cores (timed, and the final tree
+    and state compared)."""
+    C = DEEP
+    t = A.Tree(C["rank"], C["n"], C["halo"], C["depth"], capacity=1 << 15, dtype=A.F64, stream=stream.cuda_stream)
+    t.refine_uniform(C["init_levels"])
+    init = A.gaussian_state(t.ids(), C["rank"], C["n"], C["halo"], C["depth"], bumps(), C["noise"], C["noise_seed"])
+    P0 = init.shape[0]
+    dev_init = torch.from_numpy(init).to(f"cuda:{dev}")
+    args = dict(steps=C["steps"], interval=C["remesh"], velocity=C["velocity"], cfl=C["cfl"], criterion="grad",
+                rthr=C["rthr"], cthr=C["cthr"], min_level=C["min_level"], max_level=C["max_level"])
+
+    def setup():
+        t.reset()
+        t.refine_uniform(C["init_levels"])
+        t.load_state_device(dev_init.data_ptr(), P0)
+
+    setup()
+    t.run(**args)  # warm-up
+    ms, _, stats, _ = time_runs(torch, stream, 1, reps, setup, lambda: t.run(**args), flush)
+    st = stats[-1]
+    ids, fin = t.ids(), t.download_state()
+    # the one-step update alone, on the adapted tree (a run continuing it)
+    t.set_timing(True)
+    t.run(**args)
+    k_ms, k_launches, k_cells = t.get_timing()
+    t.set_timing(False)
+    t.close()
+    hbm = measured_peaks().get("hbm_gbs")
+    achieved = 16.0 * k_cells / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+    out = {
+        "workload": DEEP_NAME, "value": st["cell_updates"] / (ms * 1e-3 / reps), "unit": UNIT, "ms_per_run": ms / reps,
+        "dtype": "f64", "leaves_min": st["leaves_min"], "leaves_max": st["leaves_max"],
+        "leaves_mean": st["leaves_mean"], "remeshes_changed": st["remeshes_changed"],
         "intervals": {"cluster_kernel": st["persistent_intervals"], "graph": st["graph_intervals"],
                       "total": st["intervals"]},
+        "roofline": {"bound": "hbm", "kernel": "k_run_step2d<double,16,1,W,S> (one step per launch)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved and hbm else None, "algorithmic_bytes_per_cell_update": 16,
+                     "launches": int(k_launches), "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured, burst copy)" if hbm else "missing"},
     }
+    if with_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        o = O.OracleTree(C["rank"], C["n"], C["halo"], C["depth"], 1 << 15)
+        o.refine_all(C["init_levels"])
+        o.set_state(init)
+        o.halo_exchange()
+        t0, done, cells = time.perf_counter(), 0, 0
+        while done < C["steps"]:
+            leaves = o.size
+            _, ex = o.advance(C["remesh"], C["velocity"], C["cfl"])
+            done += ex
+            cells += ex * leaves * C["n"] ** 2
+            f = o.flags_gradient(C["rthr"], C["cthr"], C["min_level"], C["max_level"])
+            assert o.reconstruct(f) == 0
+            o.halo_exchange()
+        secs = time.perf_counter() - t0
+        n, h = C["n"], C["halo"]
+        same = bool(np.array_equal(ids, o.ids()))
+        out["cpu_baseline"] = {"value": cells / secs, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": "the whole run, FP64, OpenMP over patches like EXECUTION=PAR"}
+        out["parity"] = {"final_tree_bit_exact": same,
+                         "rel_l2": (rel_l2_np(fin[:, h:n + h, h:n + h], o.state()[:, h:n + h, h:n + h])
+                                    if same else None), "bar": 1e-12}
+    return out
+
+
+def rel_l2_np(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
 
 
 # ------------------------------------------------------------- VTK writer
@@ -1387,7 +1487,7 @@ def gpu_arm(args, rank, world):
             "adjoint": lambda: adjoint_extra(torch, A, dev, stream, with_oracle=cpu),
             "config3_3d": lambda: config3_extra(torch, A, dev, stream, flush, max(1, args.steps)),
             "vtk_writer": lambda: vtk_extra(torch, A, dev, stream, with_cpu=cpu),
-            "plain_fp64_config2_max_level7": lambda: depth7_extra(torch, A, dev, stream, flush, max(1, args.steps)),
+            "plain_fp64_config2_deep": lambda: deep_extra(torch, A, dev, stream, flush, max(1, args.steps), with_cpu=cpu),
             "euler_benchmark": lambda: euler_extra(torch, A, stream, with_cpu=cpu),
             "ssprk_advection": lambda: ssprk_extra(torch, A, stream, with_cpu=cpu),
             "dg_advection": lambda: dg_extra(torch, A, stream, with_cpu=cpu),
@@ -1577,15 +1677,24 @@ def profile_case(name, steps):
     import amr_gb300 as A
 
     stream = torch.cuda.Stream()
-    if name == "forest":
+    if name in ("forest", "forest64", "active"):
         B = BATCHED
         caps, vel, bmp = batched_instances()
-        f = make_forest(A, A.F32, stream, caps, vel)
+        bounds = np.stack([np.maximum(caps - 2, 0), caps], 1).astype(np.int32) if name == "active" else None
+        f = make_forest(A, A.F64 if name == "forest64" else A.F32, stream, caps, vel, bounds)
         ids = f.ids()
         ic64, _ = batched_ic(torch, ids, bmp, 0)
-        ic = ic64.to(torch.float32).contiguous()
+        ic = ic64 if name == "forest64" else ic64.to(torch.float32).contiguous()
         f.load_state_device(ic.data_ptr(), len(ids))
         st = f.run(steps, B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+    elif name == "deep":
+        C = DEEP
+        t = A.Tree(C["rank"], C["n"], C["halo"], C["depth"], capacity=1 << 15, stream=stream.cuda_stream)
+        t.refine_uniform(C["init_levels"])
+        t.upload_state(A.gaussian_state(t.ids(), C["rank"], C["n"], C["halo"], C["depth"], bumps(), C["noise"],
+                                        C["noise_seed"]))
+        st = t.run(steps=steps, interval=C["remesh"], velocity=C["velocity"], cfl=C["cfl"], criterion="grad",
+                   rthr=C["rthr"], cthr=C["cthr"], min_level=C["min_level"], max_level=C["max_level"])
     elif name == "adjoint":
         J = ADJOINT
         t, _ = adjoint_mesh(A, A.F64, stream)
@@ -1643,7 +1752,8 @@ def main():
     ap.add_argument("--uniform-level", type=int, default=9)
     ap.add_argument("--extra", action="append", default=None,
                     help="run only the named extra workloads after the headline (repeatable)")
-    ap.add_argument("--case", choices=["forest", "adjoint", "config2", "euler", "dg_euler"],
+    ap.add_argument("--case", choices=["forest", "forest64", "active", "deep", "adjoint", "config2", "euler",
+                                       "dg_euler"],
                     help="run one workload once, untimed (for profilers), and exit")
     ap.add_argument("--case-steps", type=int, default=30)
     args = ap.parse_args()
