@@ -121,11 +121,11 @@ amr_status amr_adjoint_forward(amr_adjoint* a)
     }
     if (a->nseg == 0 && a->per_instance)
         AMR_CUDA(cudaMemcpyAsync(a->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    AMR_CUDA(cudaStreamSynchronize(s));
     int32_t wait_err = 0;
-    AMR_CUDA(cudaMemcpy(&wait_err, t->status + 7, sizeof wait_err, cudaMemcpyDeviceToHost));
+    AMR_CUDA(cudaMemcpyAsync(&wait_err, t->status + 7, sizeof wait_err, cudaMemcpyDeviceToHost, s));
+    AMR_CUDA(cudaStreamSynchronize(s));
     if (wait_err) {
-        AMR_CUDA(cudaMemset(t->status + 7, 0, sizeof(int32_t)));
+        AMR_CUDA(cudaMemsetAsync(t->status + 7, 0, sizeof(int32_t), s));
         return fail(AMR_ERR_TIMEOUT, "a bulk copy did not complete within the wait limit");
     }
     a->forward_done = true;

@@ -188,6 +188,7 @@ struct amr_tree {
     RunCtl*   ctl       = nullptr;
     bool      vel_inst_set = false;
     std::vector<double> vel_inst_host;
+    std::vector<int32_t> bounds_host; // per instance (min, max), as set (no device readback on a run)
     uint64_t  topo = 0; // changes whenever the leaves may have changed
     StepCfg   last_cfg{}; // launch shape of the last 2D update
     bool      bounds_set   = false;

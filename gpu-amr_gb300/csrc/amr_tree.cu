@@ -963,10 +963,8 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
         key.up[a] = p->velocity[a] > 0.0 ? -1 : (p->velocity[a] < 0.0 ? 1 : 0);
     int allowed = p->max_level;
     if (t->bounds_set) {
-        std::vector<int32_t> b(2 * static_cast<size_t>(K));
-        AMR_CUDA(cudaMemcpy(b.data(), t->bounds, b.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
         allowed = 0;
-        for (int i = 0; i < K; ++i) allowed = std::max(allowed, static_cast<int>(b[2 * i + 1]));
+        for (int i = 0; i < K; ++i) allowed = std::max(allowed, static_cast<int>(t->bounds_host[2 * i + 1]));
     }
     key.rounds = std::max(1, std::min(g.depth, std::max(t->max_level_host, allowed)));
     const bool step2d = g.rank == 2 && g.h == 1 && (g.n == 16 || g.n == 8);
@@ -1431,13 +1429,31 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out)
 // Copies `num` patches of every field between the tree's state (field f at f
 // * fstride) and a buffer holding the fields one after another (field f at f *
 // num patches).
+// Device-to-device copy of 16-byte words by the SMs: copies between device
+// buffers then never queue behind host transfers on the copy engines.
+__global__ void __launch_bounds__(256) k_copy16(uint4* __restrict__ dst, const uint4* __restrict__ src, size_t words)
+{
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < words;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        dst[i] = src[i];
+}
+
 static amr_status copy_fields(amr_tree* t, void* dst, const void* src, size_t num, cudaMemcpyKind kind, bool to_tree)
 {
     const size_t fb = t->field_bytes(num), tstride = t->field_bytes(t->cap);
     for (int f = 0; f < t->nvar; ++f) {
         char*       d = static_cast<char*>(dst) + f * (to_tree ? tstride : fb);
         const char* s = static_cast<const char*>(src) + f * (to_tree ? fb : tstride);
-        AMR_CUDA(cudaMemcpyAsync(d, s, fb, kind, t->stream));
+        const bool  words = kind == cudaMemcpyDeviceToDevice && fb % 16 == 0 &&
+                           (reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(s)) % 16 == 0;
+        if (words && fb > 0) {
+            const size_t   n    = fb / 16;
+            const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, 8ull * num_sms()));
+            k_copy16<<<grid, 256, 0, t->stream>>>(reinterpret_cast<uint4*>(d), reinterpret_cast<const uint4*>(s), n);
+            AMR_LAUNCHED("k_copy16");
+        } else if (fb > 0) {
+            AMR_CUDA(cudaMemcpyAsync(d, s, fb, kind, t->stream));
+        }
     }
     return AMR_OK;
 }
@@ -1907,10 +1923,8 @@ amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats*
             A.min_level   = p->min_level;
             A.max_level   = p->max_level;
             if (t->bounds_set) { // one tree: its own (min, max) pair
-                int32_t b[2];
-                AMR_CUDA(cudaMemcpy(b, t->bounds, sizeof b, cudaMemcpyDeviceToHost));
-                A.min_level = b[0];
-                A.max_level = b[1];
+                A.min_level = t->bounds_host[0];
+                A.max_level = t->bounds_host[1];
             }
             if (inst_params) {
                 for (int a = 0; a < 3; ++a) {
@@ -2049,8 +2063,9 @@ amr_status amr_tree_set_instance_params(amr_tree* t, const double* velocity, con
         for (size_t i = 0; i < instances; ++i)
             if (level_bounds[2 * i] < 0 || level_bounds[2 * i + 1] < level_bounds[2 * i])
                 return fail(AMR_ERR_INVALID, "bad level bounds");
-        AMR_CUDA(cudaMemcpyAsync(t->bounds, level_bounds, 2 * instances * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                 t->stream));
+        t->bounds_host.assign(level_bounds, level_bounds + 2 * instances);
+        AMR_CUDA(cudaMemcpyAsync(t->bounds, t->bounds_host.data(), 2 * instances * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice, t->stream));
         t->bounds_set = true;
     }
     AMR_CUDA(cudaStreamSynchronize(t->stream));
