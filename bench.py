@@ -445,6 +445,11 @@ def batched_arm(args, torch, A, dev, stream, flush, world):
             "algorithmic_bytes_per_launch": alg / k_launches if k_launches else None,
             "cell_updates_per_pass": per_pass,
             "algorithmic_bytes_per_cell_update": 8 / per_pass,
+            "per_cell_update_definition": {
+                "achieved": (8.0 * k_cells / (k_ms * 1e-3) / 1e9) if k_ms > 0 else None,
+                "frac": (8.0 * k_cells / (k_ms * 1e-3) / 1e9 / hbm) if (k_ms > 0 and hbm) else None,
+                "note": "8 B (one FP32 read and write) per cell update, as if every step went through HBM; above 1 "
+                        "because a launch applies ten steps to each cell it reads once"},
             "note": "achieved = one FP32 read + write of every interior cell per launch / CUDA-event launch time "
                     "(launches timed inside a complete run)",
             "launches": k_launches, "avg_launch_us": (k_ms * 1e3 / k_launches) if k_launches else None,
