@@ -725,7 +725,44 @@ def config3_extra(torch, A, dev, stream, flush, reps):
     ms64, st64, s64, ids64 = single_tree_runs(torch, A, dev, stream, flush, C, A.F64, b, 0.0, 0, reps)
     ms32, st32, s32, ids32 = single_tree_runs(torch, A, dev, stream, flush, C, A.F32, b, 0.0, 0, reps)
     same = np.array_equal(ids64, ids32)
+    uniform = {4: {}, 5: {}}
+    for lvl, (name, dtype, tdtype, esize) in [(lv, d) for lv in (4, 5) for d in (
+            ("fp64", A.F64, torch.float64, 8), ("fp32", A.F32, torch.float32, 4))]:
+        # a uniform tree of 8^lvl leaves of 8^3 (level 4: 4096 leaves, 33 MB
+        # of FP64 state, L2-resident; level 5: 32768 leaves, 0.26 GB): the
+        # staged update kernel's launches timed with CUDA events, 100 steps,
+        # no re-mesh
+        t = A.Tree(3, C["n"], C["halo"], C["depth"], capacity=8 ** lvl + 64, dtype=dtype, stream=stream.cuda_stream)
+        t.refine_uniform(lvl)
+        u0 = A.gaussian_state(t.ids(), 3, C["n"], C["halo"], C["depth"], b, 0.0, 0)
+        x = torch.from_numpy(u0).to(f"cuda:{dev}", tdtype).contiguous()
+        t.load_state_device(x.data_ptr(), t.size)
+        t.advance(10, C["velocity"], C["cfl"])
+        t.finish_advance()
+        t.set_timing(True)
+        t.advance(100, C["velocity"], C["cfl"])
+        t.finish_advance()
+        k_ms, k_n, k_cells = t.get_timing()
+        t.set_timing(False)
+        t.close()
+        hbm = measured_peaks().get("hbm_gbs")
+        ach = 2.0 * esize * k_cells / (k_ms * 1e-3) / 1e9 if k_ms > 0 else None
+        rec = {"value": k_cells / (k_ms * 1e-3) if k_ms > 0 else None, "launches": k_n,
+               "avg_launch_us": k_ms * 1e3 / k_n if k_n else None,
+               "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                            "frac": ach / hbm if ach and hbm else None,
+                            "algorithmic_bytes_per_cell_update": 2 * esize}}
+        if esize == 8:
+            # c0 u + sum_a c_a u_a: one DMUL and three DFMA per cell update
+            rec["fp64_pipe"] = {"fp64_ops_per_cell_update": 4, "fp64_ops_per_s": 4 * rec["value"] if rec["value"] else
+                                None, "note": "the FP64 update is bound by the FP64 pipe (ncu: FP64 pipe 72% active "
+                                              "on the level-5 tree), not by HBM"}
+        uniform[lvl][name] = rec
     return {
+        "uniform_level4": dict(uniform[4], workload="uniform level 4 (4096 leaves of 8^3 + 1 ghost), the staged "
+                                                    "update kernel alone (k_step3d), 100 steps, CUDA events per launch"),
+        "uniform_level5": dict(uniform[5], workload="uniform level 5 (32768 leaves of 8^3 + 1 ghost), the staged "
+                                                    "update kernel alone (k_step3d), 100 steps, CUDA events per launch"),
         "workload": ("3D linear advection with AMR: 8^3 patches + 1 ghost, level 1 start, max level 4, gradient "
                      "criterion 0.05/0.01, re-mesh every 10 steps, 4 seeded Gaussian blobs, v = (1, 0.7, 0.3), "
                      "CFL 0.4, 500 steps"),
@@ -1712,6 +1749,39 @@ def profile_case(name, steps):
         lam, out = torch.ones_like(x), torch.empty_like(x)
         adj.backward(lam.data_ptr(), out.data_ptr())
         st = {"leaves": t.size, "steps": steps}
+    elif name in ("uniform3d", "uniform3d32"):
+        # a uniform level-5 3D tree (32768 leaves of 8^3 + 1 ghost, 0.26 GB of
+        # FP64 state per buffer, above L2): `steps` update steps, no re-mesh
+        C = CONFIG3
+        dtype = A.F32 if name == "uniform3d32" else A.F64
+        t = A.Tree(3, C["n"], C["halo"], C["depth"], capacity=32768 + 64, dtype=dtype, stream=stream.cuda_stream)
+        t.refine_uniform(5)
+        b = A.seeded_bumps(3, C["bumps"], C["bump_seed"], sigma=C["sigma"])
+        t.upload_state(A.gaussian_state(t.ids(), 3, C["n"], C["halo"], C["depth"], b, 0.0, 0))
+        t.advance(steps, C["velocity"], C["cfl"])
+        t.finish_advance()
+        st = {"leaves": t.size, "steps": steps}
+    elif name in ("config3", "config3_32"):
+        # one full 3D config-3 run (500 steps, re-mesh every 10)
+        C = CONFIG3
+        dtype = A.F32 if name == "config3_32" else A.F64
+        t = A.Tree(3, C["n"], C["halo"], C["depth"], capacity=1 << 16, dtype=dtype, stream=stream.cuda_stream)
+        t.refine_uniform(C["init_levels"])
+        b = A.seeded_bumps(3, C["bumps"], C["bump_seed"], sigma=C["sigma"])
+        t.upload_state(A.gaussian_state(t.ids(), 3, C["n"], C["halo"], C["depth"], b, 0.0, 0))
+        st = t.run(steps=C["steps"], interval=C["remesh"], velocity=C["velocity"], cfl=C["cfl"], criterion="grad",
+                   rthr=C["rthr"], cthr=C["cthr"], min_level=C["min_level"], max_level=C["max_level"])
+    elif name in ("ssprk2", "ssprk3"):
+        # `steps` SSPRK steps of the SSPRK workload (uniform level 7 of 16x16, FP64)
+        S, W = SSPRK, WORKLOAD
+        t = A.Tree(2, S["n"], S["halo"], S["depth"], capacity=20000, dtype=A.F64, stream=stream.cuda_stream)
+        t.refine_uniform(S["level"])
+        t.upload_state(A.gaussian_state(t.ids(), 2, S["n"], S["halo"], S["depth"], bumps(), W["noise"],
+                                        W["noise_seed"]))
+        t.halo_exchange()
+        t.advance_ssprk(steps, 2 if name == "ssprk2" else 3, S["velocity"], S["cfl"])
+        _, ex = t.finish_advance()
+        st = {"leaves": t.size, "steps": ex}
     elif name == "euler":
         t, _ = euler_tree(A, stream, capacity=4000)  # about 1.5 GB of state and primitives
         st = euler_run(t, steps)
@@ -1758,7 +1828,8 @@ def main():
     ap.add_argument("--extra", action="append", default=None,
                     help="run only the named extra workloads after the headline (repeatable)")
     ap.add_argument("--case", choices=["forest", "forest64", "active", "deep", "adjoint", "config2", "euler",
-                                       "dg_euler"],
+                                       "dg_euler", "uniform3d", "uniform3d32", "config3", "config3_32", "ssprk2",
+                                       "ssprk3"],
                     help="run one workload once, untimed (for profilers), and exit")
     ap.add_argument("--case-steps", type=int, default=30)
     args = ap.parse_args()

@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "amr_kernels.cuh"
 
@@ -99,7 +100,7 @@ __device__ inline double patch_max_on_the_fly(const T* buf, const amr_halo_meta*
         }
         G[L]                  = pos ? g.n + g.h + f : f;
         const amr_halo_meta& mm = meta[static_cast<size_t>(p) * g.ndir + d];
-        m = fmax(m, static_cast<double>(static_cast<T>(ghost_value<T>(buf, g.flat, mm, G, L, pos, g, u))));
+        m = fmax(m, static_cast<double>(ghost_value<T, T>(buf, g.flat, mm, G, L, pos, g, u)));
     }
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     return m;
@@ -118,7 +119,9 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
     const int  lane     = threadIdx.x & 31;
     const int  gwarp    = gtid >> 5, nwarps = nthreads >> 5;
     const bool leader   = gtid == 0;
-    Coef*      coef_s   = reinterpret_cast<Coef*>(smem_raw);
+    // coefficient rows in the state type's form (FP32 rows rounded once)
+    using CT            = std::conditional_t<sizeof(T) == 4, CoefT<float>, Coef>;
+    CT*        coef_s   = reinterpret_cast<CT*>(smem_raw);
     double*    dts_s    = reinterpret_cast<double*>(coef_s + static_cast<size_t>(A.interval) * nl);
 
     int       P = A.P0, tb = A.tb0, cur = 0, maxlevel = A.max_level0;
@@ -149,7 +152,11 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
             s_ctl[1] = ex;
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < k * nl; e += blockDim.x) coef_s[e] = make_coef(g, dts_s[e / nl], A.vel, e % nl);
+        for (int e = threadIdx.x; e < k * nl; e += blockDim.x) {
+            const Coef c = make_coef(g, dts_s[e / nl], A.vel, e % nl);
+            if constexpr (sizeof(T) == 4) coef_s[e] = coef_f32(c);
+            else coef_s[e] = c;
+        }
         __syncthreads();
         const double   batch_dt = s_ctl[0];
         const uint64_t executed = static_cast<uint64_t>(s_ctl[1]);
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(kCycleThreads, 1) k_cycle(CycleArgs A)
         for (int s = 0; s < k; ++s) {
             const T*    in  = static_cast<const T*>(A.state[cur]);
             T*          out = static_cast<T*>(A.state[cur ^ 1]);
-            const Coef* row = coef_s + static_cast<size_t>(s) * nl;
+            const CT*   row = coef_s + static_cast<size_t>(s) * nl;
             for (long long t = gtid; t < static_cast<long long>(P) * g.cells; t += nthreads) {
                 const int p = static_cast<int>(t / g.cells);
                 step_cell<T, true>(in, out, mt, g, row[lv[p]], A.up, p, static_cast<int>(t - static_cast<long long>(p) * g.cells));

@@ -192,9 +192,12 @@ __host__ __device__ __forceinline__ int padded_index(const Geo& g, const int* id
 //   none    -> the ghost keeps its current value (:303-313).
 // The mean is formed in double for every state type.  Coordinates are held
 // in scalars (no runtime-indexed arrays) so the function stays in registers.
-template <typename T>
-__device__ __forceinline__ double ghost_value(const T* buf, size_t pstride, const amr_halo_meta& m, const int* G, int L,
-                                              int pos, const Geo& g, const T* self)
+// R = T returns the value rounded to the state type: a copied or injected
+// value as stored (a round trip through double is the identity), the mean
+// rounded once; R = double returns the value before that rounding.
+template <typename T, typename R = double>
+__device__ __forceinline__ R ghost_value(const T* buf, size_t pstride, const amr_halo_meta& m, const int* G, int L,
+                                         int pos, const Geo& g, const T* self)
 {
     const int sh = pos ? -g.n : g.n;
     int       f0 = G[0] + (L == 0 ? sh : 0);
@@ -202,13 +205,13 @@ __device__ __forceinline__ double ghost_value(const T* buf, size_t pstride, cons
     int       f2 = G[2] + (L == 2 ? sh : 0);
     const int rel = m.relation;
     if (rel == REL_SAME)
-        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
+        return static_cast<R>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
     const int half = g.n / 2;
     if (rel == REL_COARSER) {
         f0 = g.h + m.quadrant[0] * half + (f0 - g.h) / 2;
         f1 = g.h + m.quadrant[1] * half + (f1 - g.h) / 2;
         if (g.rank == 3) f2 = g.h + m.quadrant[2] * half + (f2 - g.h) / 2;
-        return static_cast<double>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
+        return static_cast<R>(buf[static_cast<size_t>(m.neighbor) * pstride + f0 * g.s[0] + f1 * g.s[1] + f2 * g.s[2]]);
     }
     if (rel == REL_FINER) {
         // the reference reduces every coordinate modulo the normal
@@ -235,7 +238,7 @@ __device__ __forceinline__ double ghost_value(const T* buf, size_t pstride, cons
             sum += static_cast<double>(fp[1]);
             sum += static_cast<double>(fp[g.s[0]]);
             sum += static_cast<double>(fp[g.s[0] + 1]);
-            return sum / 4.0;
+            return static_cast<R>(sum / 4.0);
         }
         sum += static_cast<double>(fp[0]);
         sum += static_cast<double>(fp[1]);
@@ -245,9 +248,9 @@ __device__ __forceinline__ double ghost_value(const T* buf, size_t pstride, cons
         sum += static_cast<double>(fp[g.s[0] + 1]);
         sum += static_cast<double>(fp[g.s[0] + g.s[1]]);
         sum += static_cast<double>(fp[g.s[0] + g.s[1] + 1]);
-        return sum / 8.0;
+        return static_cast<R>(sum / 8.0);
     }
-    return static_cast<double>(self[G[0] * g.s[0] + G[1] * g.s[1] + G[2] * g.s[2]]);
+    return static_cast<R>(self[G[0] * g.s[0] + G[1] * g.s[1] + G[2] * g.s[2]]);
 }
 
 } // namespace amr_gb300

@@ -118,6 +118,25 @@ static __global__ void k_run_require_uniform(RunCtl* ctl)
     if (threadIdx.x == 0 && ctl->err == 0 && !ctl->uniform) ctl->err = kRetryUniform;
 }
 
+// 3D patches of N^3 cells and one ghost layer, one warp per patch
+// (step3d_body); parity selects the buffers of this step.
+template <typename T, int N, int W, int S>
+__global__ void __launch_bounds__(W * 32)
+k_run_step3d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int parity, int up0, int up1, int up2)
+{
+    if (ctl->err) return;
+    extern __shared__ __align__(128) unsigned char smem3d[];
+    T*        tiles;
+    uint64_t* bars;
+    step3d_smem<T, N, W, S>(smem3d, tiles, bars);
+    const int P = ctl->P, tb = ctl->tb, s = ctl->sb ^ parity;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    step3d_body<T, N, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb],
+                         B.levels[tb], B.keys[tb], P, g, coef, up0, up1, up2, B.vel, &ctl->err, tiles, bars, p,
+                         nwarp);
+}
+
 // Any geometry: ppb patches per block per round, grid-stride over rounds.
 template <typename T>
 __global__ void __launch_bounds__(256)

@@ -10,7 +10,9 @@
 //
 // One stage is one launch over every cell of every padded patch (the
 // reference combines whole patch containers): interior cells take the
-// residual of the halo-exchanged input, ghost cells a zero residual.
+// residual of the halo-exchanged input, ghost cells a zero residual.  2D
+// patches of 8x8 or 16x16 cells with one ghost layer evaluate each face flux
+// once (k_ssprk_stage2d), other shapes per cell (k_ssprk_stage).
 //     stage 0          u* = u + R dt
 //     SSPRK2 stage 1   u' = ((u^n + u*) + R dt) * 0.5
 //     SSPRK3 stage 1   u2 = u^n * 0.75 + (u1 + R dt) * 0.25
@@ -92,6 +94,77 @@ k_ssprk_stage(const double* __restrict__ in, const double* __restrict__ un, doub
     }
 }
 
+// 2D patches of N x N cells and one ghost layer: the same stage with each
+// face flux evaluated once.  A face flux depends only on its two cells and
+// the reference evaluates it the same way from either side (f(a, b) =
+// 0.5 (a v + b v) - (0.5 |v|) (b - a) with a the cell on the minus side), so
+// sharing it between the two cells changes no rounding.  One block per patch:
+// the padded patch and the fluxes of its (N + 1) N faces per axis in shared
+// memory, then every padded cell as above.
+template <int N>
+__global__ void __launch_bounds__(256)
+k_ssprk_stage2d(const double* __restrict__ in, const double* __restrict__ un, double* __restrict__ out,
+                const uint64_t* __restrict__ keys, int P, Geo g, const double* __restrict__ vel,
+                const double* __restrict__ step_dt, int mode, unsigned pow2_mask)
+{
+    constexpr int P1 = N + 2, FLAT = P1 * P1;
+    __shared__ double tile[FLAT];
+    __shared__ double fx[N][N + 1]; // x faces of interior row r: face j between padded columns j and j + 1
+    __shared__ double fy[N + 1][N]; // y faces of interior column c: face i between padded rows i and i + 1
+    for (int p = blockIdx.x; p < P; p += gridDim.x) {
+        const uint64_t key  = keys[p];
+        const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
+        const int      lev  = key_level(key);
+        const double   dt   = step_dt[inst];
+        InvDx          cdx[2];
+        double         v[2], hsp[2];
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            cdx[d].dx   = cell_size(g, d, lev);
+            cdx[d].pow2 = (pow2_mask >> d) & 1u;
+            cdx[d].inv  = 1.0 / cdx[d].dx;
+            v[d]        = vel[3 * inst + d];
+            hsp[d]      = 0.5 * fabs(v[d]); // the reference's 0.5 * sp * (...), left to right
+        }
+        const size_t  pb = static_cast<size_t>(p) * FLAT;
+        const double* a  = in + pb;
+        for (int li = threadIdx.x; li < FLAT; li += blockDim.x) tile[li] = a[li];
+        __syncthreads();
+        for (int k = threadIdx.x; k < N * (N + 1); k += blockDim.x) {
+            {
+                const int    r = k / (N + 1), j = k % (N + 1);
+                const double uL = tile[(r + 1) * P1 + j], uR = tile[(r + 1) * P1 + j + 1];
+                fx[r][j] = 0.5 * (uL * v[0] + uR * v[0]) - hsp[0] * (uR - uL);
+            }
+            {
+                const int    i = k / N, c = k % N;
+                const double uL = tile[i * P1 + c + 1], uR = tile[(i + 1) * P1 + c + 1];
+                fy[i][c] = 0.5 * (uL * v[1] + uR * v[1]) - hsp[1] * (uR - uL);
+            }
+        }
+        __syncthreads();
+        for (int li = threadIdx.x; li < FLAT; li += blockDim.x) {
+            const int    r = li / P1, c = li % P1;
+            const double uc = tile[li];
+            double       Rs = 0.0;
+            if (r >= 1 && r <= N && c >= 1 && c <= N) {
+                Rs -= div_dx(fx[r - 1][c] - fx[r - 1][c - 1], cdx[0]);
+                Rs -= div_dx(fy[r][c - 1] - fy[r - 1][c - 1], cdx[1]);
+            }
+            const double Rdt = Rs * dt;
+            const double b   = un[pb + li];
+            double       res;
+            if (!(dt > 0.0)) res = mode == 0 ? uc : b;
+            else if (mode == 0) res = uc + Rdt;
+            else if (mode == 2) res = (b + uc + Rdt) * 0.5;
+            else if (mode == 31) res = b * 0.75 + (uc + Rdt) * 0.25;
+            else res = b * (1.0 / 3.0) + (uc + Rdt) * (2.0 / 3.0);
+            out[pb + li] = res;
+        }
+        __syncthreads(); // the tile and fluxes are refilled for the next patch
+    }
+}
+
 } // namespace
 
 cudaError_t ssprk_stage(const SsprkStage& s)
@@ -105,7 +178,13 @@ cudaError_t ssprk_stage(const SsprkStage& s)
     }
     const unsigned grid    = static_cast<unsigned>(std::min(s.P, 152 * 32));
     const int      threads = s.g.flat >= 256 ? 256 : ((s.g.flat + 31) / 32) * 32;
-    if (s.g.rank == 2)
+    if (s.g.rank == 2 && s.g.h == 1 && s.g.n == 16)
+        k_ssprk_stage2d<16><<<grid, 256, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.vel, s.step_dt,
+                                                         s.mode, mask);
+    else if (s.g.rank == 2 && s.g.h == 1 && s.g.n == 8)
+        k_ssprk_stage2d<8><<<grid, 128, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.vel, s.step_dt,
+                                                       s.mode, mask);
+    else if (s.g.rank == 2)
         k_ssprk_stage<2><<<grid, threads, 0, s.stream>>>(s.in, s.un, s.out, s.keys, s.P, s.g, s.vel, s.step_dt,
                                                          s.mode, mask);
     else

@@ -125,6 +125,98 @@ amr_status launch_step2d(const T* in, T* out, const amr_halo_meta* meta, int P, 
     });
 }
 
+// ---------------------------------------------------------- 3D update
+// Staged 3D kernels (one warp per patch, a ring of S bulk-copied tiles per
+// warp) serve 4^3 and 8^3 patches with one ghost layer on 16-byte-aligned
+// state buffers.
+inline bool step3d_shape(const Geo& g, const void* in, const void* out)
+{
+    return g.rank == 3 && g.h == 1 && (g.n == 8 || g.n == 4) &&
+           ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+}
+
+// Warps per block and ring depth: 4 x 2 for FP64 8^3 patches (its update is
+// FP64-pipe bound; 64 KB of tiles per block), 8 x 2 otherwise (measured on
+// uniform level-4 and level-5 trees of 8^3 patches against the other built
+// pairs); AMR_GB300_STEP3D="W,S" picks another of (4,2), (4,3), (8,2), (8,3).
+inline std::pair<int, int> step3d_config(int n, size_t esize)
+{
+    static const std::pair<int, int> env = [] {
+        const char* e = std::getenv("AMR_GB300_STEP3D");
+        int         w = 0, s = 0;
+        if (e && std::sscanf(e, "%d,%d", &w, &s) == 2 && (w == 4 || w == 8) && (s == 2 || s == 3))
+            return std::make_pair(w, s);
+        return std::make_pair(0, 0);
+    }();
+    if (env.first) return env;
+    return n == 8 && esize == 8 ? std::make_pair(4, 2) : std::make_pair(8, 2);
+}
+
+template <typename F>
+amr_status with_ws3d(int n, size_t esize, F&& f)
+{
+    const auto [W, S] = step3d_config(n, esize);
+    if (W == 4 && S == 2) return f.template operator()<4, 2>();
+    if (W == 4 && S == 3) return f.template operator()<4, 3>();
+    if (W == 8 && S == 2) return f.template operator()<8, 2>();
+    return f.template operator()<8, 3>();
+}
+
+// Dynamic shared memory limit of both staged 3D kernels of one shape, set
+// once per device; returns the resident blocks per SM (0 on failure).
+template <typename T, int N, int W, int S>
+int prepare_step3d()
+{
+    static std::atomic<int> cached[64];
+    int                     dev = 0;
+    cudaGetDevice(&dev);
+    if (const int c = cached[dev & 63].load(); c > 0) return c;
+    const int   smem = static_cast<int>(Step3dShape<T, N>::smem(W, S));
+    cudaError_t e    = cudaFuncSetAttribute(k_step3d<T, N, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_run_step3d<T, N, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int nb = 0;
+    if (e == cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_run_step3d<T, N, W, S>, W * 32, smem) != cudaSuccess)
+        nb = 0;
+    cudaGetLastError();
+    if (nb > 0) cached[dev & 63].store(nb);
+    return nb;
+}
+
+template <typename T, int N>
+amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
+                         const Coef* coef, const int* up, const uint64_t* keys, const double* vel, int32_t* err,
+                         cudaStream_t s)
+{
+    return with_ws3d(N, sizeof(T), [&]<int W, int S>() -> amr_status {
+        const int occ = prepare_step3d<T, N, W, S>();
+        if (occ <= 0) return fail(AMR_ERR_CUDA, "staged 3D update kernel: shared-memory configuration failed");
+        const unsigned grid = static_cast<unsigned>(
+            std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
+        k_step3d<T, N, W, S><<<grid, W * 32, Step3dShape<T, N>::smem(W, S), s>>>(
+            in, out, levels, meta, P, g, coef, up[0], up[1], up[2], keys, vel, err);
+        AMR_LAUNCHED("k_step3d");
+        return AMR_OK;
+    });
+}
+
+// The graph form: the leaf count is read on the device, so the grid is full
+// residency and the warps stride over the patches.
+template <typename T, int N>
+amr_status launch_run_step3d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, int parity,
+                             const int* up, cudaStream_t s)
+{
+    return with_ws3d(N, sizeof(T), [&]<int W, int S>() -> amr_status {
+        const int occ = prepare_step3d<T, N, W, S>();
+        if (occ <= 0) return fail(AMR_ERR_CUDA, "staged 3D update kernel: shared-memory configuration failed");
+        k_run_step3d<T, N, W, S><<<static_cast<unsigned>(num_sms() * occ), W * 32, Step3dShape<T, N>::smem(W, S),
+                                   s>>>(B, ctl, g, coef, parity, up[0], up[1], up[2]);
+        AMR_LAUNCHED("k_run_step3d");
+        return AMR_OK;
+    });
+}
+
 // Steps per pass on same-level trees: FP32 five (a pass costs a fixed share,
 // the state's read and write and the per-patch work, plus a share per step),
 // FP64 two (its update is FP64-bound).
@@ -783,6 +875,9 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
             st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
         else if (key.W > 0)
             st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
+        else if (step3d_shape(g, B.state[0], B.state[1]))
+            st = g.n == 8 ? launch_run_step3d<T, 8>(B, ctl, g, cf, par, key.up, cs)
+                          : launch_run_step3d<T, 4>(B, ctl, g, cf, par, key.up, cs);
         else {
             k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, par, key.up[0], key.up[1], key.up[2], ppb);
             AMR_LAUNCHED("k_run_step");
@@ -1800,6 +1895,11 @@ amr_status amr_api::advance_impl(amr_tree* t, size_t steps, const double* veloci
                 if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
                     return launch_step2d<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
                                                   t->keys[t->tb], uleaf, StepCfg{}, s);
+                if (step3d_shape(t->g, in, out))
+                    return t->g.n == 8 ? launch_step3d<T, 8>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
+                                                             up, t->keys[t->tb], vleaf, t->status + 7, s)
+                                       : launch_step3d<T, 4>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
+                                                             up, t->keys[t->tb], vleaf, t->status + 7, s);
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
                                                      up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
                                                      vleaf);
