@@ -122,7 +122,8 @@ static __global__ void k_run_require_uniform(RunCtl* ctl)
 // (step3d_body); parity selects the buffers of this step.
 template <typename T, int N, int W, int S>
 __global__ void __launch_bounds__(W * 32)
-k_run_step3d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int parity, int up0, int up1, int up2)
+k_run_step3d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const float4* __restrict__ coef4,
+             int parity, int up0, int up1, int up2)
 {
     if (ctl->err) return;
     extern __shared__ __align__(128) unsigned char smem3d[];
@@ -133,8 +134,8 @@ k_run_step3d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, int p
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     step3d_body<T, N, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb],
-                         B.levels[tb], B.keys[tb], P, g, coef, up0, up1, up2, B.vel, &ctl->err, tiles, bars, p,
-                         nwarp);
+                         B.levels[tb], B.keys[tb], P, g, coef, coef4, up0, up1, up2, B.vel, &ctl->err, tiles, bars,
+                         p, nwarp);
 }
 
 // Any geometry: ppb patches per block per round, grid-stride over rounds.

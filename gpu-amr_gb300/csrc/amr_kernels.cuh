@@ -478,6 +478,8 @@ enum : int {
 
 // Block b handles instance b: its CFL step from its own finest level and
 // velocity; coef row (step s, instance b) starts at (s * ninst + b) * (depth+1).
+// coef32 holds the rows rounded to FP32 once: (c_x, c_y) float2 entries for
+// 2D trees, (c_x, c_y, c_z, c0) float4 entries for 3D trees.
 static __global__ void __launch_bounds__(256)
 k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __restrict__ vel, double cfl, int steps,
               int mode, double remaining0, DtState d, double* __restrict__ step_dt, Coef* __restrict__ coef,
@@ -527,7 +529,14 @@ k_batch_begin(const int32_t* __restrict__ max_level, Geo g, const double* __rest
         const size_t at = (static_cast<size_t>(st) * ninst + inst) * nl + l;
         const Coef   c  = make_coef(g, dts[st], v, l);
         coef[at]        = c;
-        if (coef32) coef32[at] = make_float2(static_cast<float>(c.c[0]), static_cast<float>(c.c[1]));
+        if (coef32) {
+            if (g.rank == 3) // (c_x, c_y, c_z, c0) rows of the 3D FP32 update
+                reinterpret_cast<float4*>(coef32)[at] = make_float4(
+                    static_cast<float>(c.c[0]), static_cast<float>(c.c[1]), static_cast<float>(c.c[2]),
+                    static_cast<float>(c.c0));
+            else
+                coef32[at] = make_float2(static_cast<float>(c.c[0]), static_cast<float>(c.c[1]));
+        }
     }
 }
 
@@ -2331,9 +2340,9 @@ template <typename T, int N, int S>
 __device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restrict__ out,
                                             const amr_halo_meta* __restrict__ meta, const int32_t* __restrict__ levels,
                                             const uint64_t* __restrict__ keys, int P, const Geo& g,
-                                            const Coef* __restrict__ coef, int up0, int up1, int up2,
-                                            const double* __restrict__ vel, int32_t* err, T* tiles, uint64_t* bars,
-                                            int p, int nwarp)
+                                            const Coef* __restrict__ coef, const float4* __restrict__ coef4,
+                                            int up0, int up1, int up2, const double* __restrict__ vel, int32_t* err,
+                                            T* tiles, uint64_t* bars, int p, int nwarp)
 {
     using Sh               = Step3dShape<T, N>;
     constexpr int P1       = Sh::P1, PLANE = Sh::PLANE, FLAT = Sh::FLAT, GPL = Sh::GPL;
@@ -2363,8 +2372,24 @@ __device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restr
         int       up[3] = { up0, up1, up2 };
         if (vel)
             for (int a = 0; a < 3; ++a) up[a] = upwind(vel[3 * inst + a]);
-        const Coef cf = coef[inst * nl + levels[p]];
-        const T*   src = in + static_cast<size_t>(p) * FLAT;
+        // the row of the leaf's level: FP64 from coef, FP32 from the rows
+        // rounded once (coef4)
+        const int row = inst * nl + levels[p];
+        T         c0, ca[3];
+        if constexpr (sizeof(T) == 4) {
+            const float4 c4 = coef4[row];
+            c0              = c4.w;
+            ca[0]           = c4.x;
+            ca[1]           = c4.y;
+            ca[2]           = c4.z;
+        } else {
+            const Coef cf = coef[row];
+            c0            = cf.c0;
+            ca[0]         = cf.c[0];
+            ca[1]         = cf.c[1];
+            ca[2]         = cf.c[2];
+        }
+        const T* src = in + static_cast<size_t>(p) * FLAT;
         // the upwind ghost faces (Morton axis a is layout dim 2 - a): ghost
         // cell k of a face has tangential coordinates (k / N + 1, k % N + 1)
         T gv[3][GPL];
@@ -2414,9 +2439,7 @@ __device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restr
             }
         }
         __syncwarp();
-        const T c0 = static_cast<T>(cf.c0);
-        const T ca[3] = { static_cast<T>(cf.c[0]), static_cast<T>(cf.c[1]), static_cast<T>(cf.c[2]) };
-        T       res[Sh::PER];
+        T res[Sh::PER];
 #pragma unroll
         for (int q = 0; q < Sh::PER; ++q) {
             const int c   = lane + 32 * q;
@@ -2459,8 +2482,9 @@ __device__ __forceinline__ void step3d_smem(unsigned char* smem, T*& tiles, uint
 template <typename T, int N, int W, int S>
 __global__ void __launch_bounds__(W * 32)
 k_step3d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
-         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef, int up0, int up1,
-         int up2, const uint64_t* __restrict__ keys, const double* __restrict__ vel, int32_t* err)
+         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef,
+         const float4* __restrict__ coef4, int up0, int up1, int up2, const uint64_t* __restrict__ keys,
+         const double* __restrict__ vel, int32_t* err)
 {
     extern __shared__ __align__(128) unsigned char smem3d[];
     T*        tiles;
@@ -2468,7 +2492,8 @@ k_step3d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restric
     step3d_smem<T, N, W, S>(smem3d, tiles, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step3d_body<T, N, S>(in, out, meta, levels, keys, P, g, coef, up0, up1, up2, vel, err, tiles, bars, p, nwarp);
+    step3d_body<T, N, S>(in, out, meta, levels, keys, P, g, coef, coef4, up0, up1, up2, vel, err, tiles, bars, p,
+                         nwarp);
 }
 
 } // namespace amr_gb300

@@ -186,8 +186,8 @@ int prepare_step3d()
 
 template <typename T, int N>
 amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
-                         const Coef* coef, const int* up, const uint64_t* keys, const double* vel, int32_t* err,
-                         cudaStream_t s)
+                         const Coef* coef, const float4* coef4, const int* up, const uint64_t* keys, const double* vel,
+                         int32_t* err, cudaStream_t s)
 {
     return with_ws3d(N, sizeof(T), [&]<int W, int S>() -> amr_status {
         const int occ = prepare_step3d<T, N, W, S>();
@@ -195,7 +195,7 @@ amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_h
         const unsigned grid = static_cast<unsigned>(
             std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
         k_step3d<T, N, W, S><<<grid, W * 32, Step3dShape<T, N>::smem(W, S), s>>>(
-            in, out, levels, meta, P, g, coef, up[0], up[1], up[2], keys, vel, err);
+            in, out, levels, meta, P, g, coef, coef4, up[0], up[1], up[2], keys, vel, err);
         AMR_LAUNCHED("k_step3d");
         return AMR_OK;
     });
@@ -204,14 +204,14 @@ amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_h
 // The graph form: the leaf count is read on the device, so the grid is full
 // residency and the warps stride over the patches.
 template <typename T, int N>
-amr_status launch_run_step3d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, int parity,
-                             const int* up, cudaStream_t s)
+amr_status launch_run_step3d(const RunBufs& B, RunCtl* ctl, const Geo& g, const Coef* coef, const float4* coef4,
+                             int parity, const int* up, cudaStream_t s)
 {
     return with_ws3d(N, sizeof(T), [&]<int W, int S>() -> amr_status {
         const int occ = prepare_step3d<T, N, W, S>();
         if (occ <= 0) return fail(AMR_ERR_CUDA, "staged 3D update kernel: shared-memory configuration failed");
         k_run_step3d<T, N, W, S><<<static_cast<unsigned>(num_sms() * occ), W * 32, Step3dShape<T, N>::smem(W, S),
-                                   s>>>(B, ctl, g, coef, parity, up[0], up[1], up[2]);
+                                   s>>>(B, ctl, g, coef, coef4, parity, up[0], up[1], up[2]);
         AMR_LAUNCHED("k_run_step3d");
         return AMR_OK;
     });
@@ -875,10 +875,12 @@ amr_status record_interval(amr_tree* t, const GraphKey& key, const RunBufs& B, c
             st = launch_run_step2d<T, 16, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
         else if (key.W > 0)
             st = launch_run_step2d<T, 8, 1>(B, ctl, g, cf, cf2, par, key.up, cfg, static_cast<int>(t->cap), cs);
-        else if (step3d_shape(g, B.state[0], B.state[1]))
-            st = g.n == 8 ? launch_run_step3d<T, 8>(B, ctl, g, cf, par, key.up, cs)
-                          : launch_run_step3d<T, 4>(B, ctl, g, cf, par, key.up, cs);
-        else {
+        else if (step3d_shape(g, B.state[0], B.state[1])) {
+            // float4 rows of the 3D FP32 update
+            const float4* cf4 = reinterpret_cast<const float4*>(t->coef32) + static_cast<size_t>(step) * K * nl;
+            st = g.n == 8 ? launch_run_step3d<T, 8>(B, ctl, g, cf, cf4, par, key.up, cs)
+                          : launch_run_step3d<T, 4>(B, ctl, g, cf, cf4, par, key.up, cs);
+        } else {
             k_run_step<T><<<sms * 16, 256, 0, cs>>>(B, ctl, g, cf, par, key.up[0], key.up[1], key.up[2], ppb);
             AMR_LAUNCHED("k_run_step");
         }
@@ -1355,7 +1357,7 @@ amr_status amr_tree_create(const amr_tree_desc* desc, amr_tree** out)
     al(reinterpret_cast<void**>(&t->dt_scratch), 5 * K * sizeof(double));
     al(reinterpret_cast<void**>(&t->step_dt), coef_steps * K * sizeof(double));
     al(reinterpret_cast<void**>(&t->coef), coef_steps * K * nl * sizeof(Coef));
-    al(reinterpret_cast<void**>(&t->coef32), coef_steps * K * nl * sizeof(float2));
+    al(reinterpret_cast<void**>(&t->coef32), coef_steps * K * nl * (t->g.rank == 3 ? sizeof(float4) : sizeof(float2)));
     al(reinterpret_cast<void**>(&t->upcode), K * sizeof(int32_t));
     al(reinterpret_cast<void**>(&t->cstats), sizeof(CycleStats));
     al(reinterpret_cast<void**>(&t->euler_min), 2 * sizeof(unsigned long long));
@@ -1895,11 +1897,13 @@ amr_status amr_api::advance_impl(amr_tree* t, size_t steps, const double* veloci
                 if (t->g.rank == 2 && t->g.n == 8 && t->g.h == 1)
                     return launch_step2d<T, 8, 1>(in, out, t->meta[t->tb], P, t->g, cf, cf2, up, t->status + 7,
                                                   t->keys[t->tb], uleaf, StepCfg{}, s);
-                if (step3d_shape(t->g, in, out))
+                if (step3d_shape(t->g, in, out)) {
+                    const float4* cf4 = reinterpret_cast<const float4*>(t->coef32) + static_cast<size_t>(k) * K * nl;
                     return t->g.n == 8 ? launch_step3d<T, 8>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
-                                                             up, t->keys[t->tb], vleaf, t->status + 7, s)
+                                                             cf4, up, t->keys[t->tb], vleaf, t->status + 7, s)
                                        : launch_step3d<T, 4>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
-                                                             up, t->keys[t->tb], vleaf, t->status + 7, s);
+                                                             cf4, up, t->keys[t->tb], vleaf, t->status + 7, s);
+                }
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
                                                      up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
                                                      vleaf);
