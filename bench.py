@@ -474,6 +474,58 @@ ACTIVE_NAME = ("batched, adapting: the batched workload's 512 instances, each fr
                "the forest every interval; 1000 steps, FP32 state")
 
 
+def precision_history(A, torch, stream, caps, vel, bounds, ic32, ic64, reset, dev):
+    """FP32 and FP64 runs of the adapting forest, one re-mesh interval per
+    call; per instance the first interval after which its FP32 tree differs
+    from its FP64 tree (none: the same tree after every re-mesh), and the
+    final relative L2 of FP32 against FP64 per instance."""
+    B = BATCHED
+    f32 = make_forest(A, A.F32, stream, caps, vel, bounds)
+    f64 = make_forest(A, A.F64, stream, caps, vel, bounds)
+    reset(f32, ic32)
+    reset(f64, ic64)
+    K = len(caps)
+    parted = np.full(K, -1, np.int64)
+    nint = B["steps"] // B["remesh"]
+    for k in range(nint):
+        for f in (f32, f64):
+            f.run(B["remesh"], B["remesh"], None, B["cfl"], "grad", B["rthr"], B["cthr"], instance_params=True)
+        a, b = f32.ids(), f64.ids()
+        oa, ob = f32.instance_offsets(), f64.instance_offsets()
+        for i in np.nonzero(parted < 0)[0]:
+            if not np.array_equal(a[oa[i]:oa[i + 1]], b[ob[i]:ob[i + 1]]):
+                parted[i] = k
+    n, h = B["n"], B["halo"]
+    s32 = torch.empty((len(f32.ids()), n + 2, n + 2), dtype=torch.float32, device=dev)
+    s64 = torch.empty((len(f64.ids()), n + 2, n + 2), dtype=torch.float64, device=dev)
+    f32.download_state_device(s32.data_ptr(), len(f32.ids()))
+    f64.download_state_device(s64.data_ptr(), len(f64.ids()))
+    oa, ob = f32.instance_offsets(), f64.instance_offsets()
+    a_all, b_all = f32.ids(), f64.ids()
+    rel = np.full(K, np.nan)
+    for i in range(K):
+        if np.array_equal(a_all[oa[i]:oa[i + 1]], b_all[ob[i]:ob[i + 1]]):
+            x = s32[oa[i]:oa[i + 1], h:n + h, h:n + h].double()
+            y = s64[ob[i]:ob[i + 1], h:n + h, h:n + h]
+            rel[i] = float(torch.linalg.vector_norm(x - y) / torch.linalg.vector_norm(y))
+    f32.close()
+    f64.close()
+    same = parted < 0
+    ok = same & np.isfinite(rel)
+    return {
+        "instances": K, "same_tree_after_every_remesh": int(same.sum()),
+        "max_rel_l2_same_history": float(rel[ok].max()) if ok.any() else None,
+        "median_rel_l2_same_history": float(np.median(rel[ok])) if ok.any() else None,
+        "within_1e-5_same_history": int((rel[ok] <= 1e-5).sum()),
+        "parted": int((~same).sum()),
+        "first_parting_interval_min": int(parted[~same].min()) if (~same).any() else None,
+        "max_rel_l2_parted_same_final_tree": (float(np.nanmax(rel[~same])) if np.isfinite(rel[~same]).any()
+                                              else None),
+        "note": "an instance parts when a re-mesh of its FP32 run flags differently from its FP64 run (a squared "
+                "gradient within rounding of a threshold); from then on the two runs hold different meshes",
+    }
+
+
 def batched_active_extra(args, torch, A, dev, stream, flush, world):
     """The batched forest with level bounds that let it adapt: the trees
     change at the re-meshes, coarse-fine faces appear and the update runs as
@@ -529,6 +581,11 @@ def batched_active_extra(args, torch, A, dev, stream, flush, world):
         n, h = B["n"], B["halo"]
         a, b = s32[:, h:n + h, h:n + h].double(), s64[:, h:n + h, h:n + h]
         rel = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    # FP32 against FP64 per instance, interval by interval: an instance's
+    # trees can part where an FP32 gradient and its FP64 counterpart fall on
+    # either side of a threshold; after that the states differ by the
+    # re-mesh, not by rounding
+    hist = precision_history(A, torch, stream, caps, vel, bounds, ic32, ic64, reset, dev)
     # the first instances against the oracle, 100 steps from the same state
     npar, spar = 8, 100
     reset(f64, ic64)
@@ -562,7 +619,8 @@ def batched_active_extra(args, torch, A, dev, stream, flush, world):
         "update_share_of_run": (k_ms / (ms / max(1, args.steps))) if ms > 0 else None,
         "gpu_launches": int(launches // max(1, args.steps)),
         "fp64_same_forest": {"value": sum(st["cell_updates"] for st in stats64) / (ms64 * 1e-3), "unit": UNIT,
-                             "same_final_tree_as_fp32": same, "rel_l2_fp32_vs_fp64": rel},
+                             "same_final_tree_as_fp32": same, "rel_l2_fp32_vs_fp64": rel,
+                             "per_instance": hist},
         "roofline": {
             "bound": "hbm", "kernel": "k_run_step2d<float,16,1,W,S> (one step per launch: the forest has "
                                       "coarse-fine faces)",
