@@ -1760,7 +1760,11 @@ def reference_arm(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded per-instance caps, velocities and Gaussian bumps; shapes of the named config)",
-        "config": {"workload": BATCHED_NAME},
+        "config": {"workload": BATCHED_NAME, "sample": f"instances 0-{CPU_SAMPLE['instances'] - 1}, first "
+                                                      f"{CPU_SAMPLE['steps']} steps each",
+                   "comparison": "rate of a bounded FP64 sample of the same workload on the host cores against "
+                                 "the GPU arm's rate over the whole forest in FP32: a rate ratio across "
+                                 "precisions, as the metric (FP32 batched against FP64) asks"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
