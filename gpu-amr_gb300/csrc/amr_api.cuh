@@ -152,6 +152,7 @@ struct amr_tree {
     bool         ghosts_valid   = false;
     bool         uniform        = true; // every neighbour relation is "same level" (multi-step passes apply)
     bool         fused_off      = false; // a fused interval found leaves that are not 4x4 blocks: not again this run
+    long long    pair_chunk     = 1;     // intervals of the next same-level graph chunk whose re-mesh may change the tree
 
     void*          sbuf[2]{};   // the two state buffers (fixed addresses)
     void*          cur = nullptr; // one of sbuf
@@ -276,6 +277,8 @@ struct RunTotals {
 
 // Defined in amr_tree.cu, used by the physics entry points.
 amr_status halo_buffer(amr_tree* t, void* buf, const double* step_dt = nullptr);
+// Device-to-device copy of `words` 8-byte words by an SM kernel on stream s.
+amr_status copy_words8(void* dst, const void* src, size_t words, cudaStream_t s);
 amr_status launch_halo(amr_tree* t);
 // Defined in amr_tree.cu: `steps` forward-Euler steps with the batch mode
 // first_mode (BATCH_RESET or BATCH_CONTINUE), used by the adjoint's forward.

@@ -20,7 +20,7 @@ amr_status amr_tree_advance_ssprk(amr_tree* t, size_t steps, int order, const do
             for (int a = 0; a < 3; ++a) v[3 * i + a] = velocity3[a];
         AMR_CUDA(cudaMemcpyAsync(t->vel, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     } else {
-        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (amr_status cs = copy_words8(t->vel, t->vel_inst, 3 * static_cast<size_t>(K), s); cs != AMR_OK) return cs;
     }
     if (t->stage_cap != t->cap) {
         cudaFree(t->stage_buf);

@@ -1013,6 +1013,16 @@ bool fused_enabled(int options)
     return on;
 }
 
+// True when the run's level bounds pin every instance to one level (min =
+// max), so a re-mesh of a same-level tree at those levels changes nothing.
+static bool remesh_keeps_levels(const amr_tree* t, const amr_cycle_params* p)
+{
+    if (!t->bounds_set) return p->min_level == p->max_level;
+    for (int i = 0; i < t->ninst; ++i)
+        if (t->bounds_host[2 * i] != t->bounds_host[2 * i + 1]) return false;
+    return true;
+}
+
 // Up to `max_intervals` intervals as graph replays, then one readback of the
 // control block.  Requires that no step is clamped by the remaining time.
 amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_params, long long max_intervals,
@@ -1026,7 +1036,7 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     const bool      per_leaf = inst_params && K > 1;
     // velocities in use
     if (inst_params) {
-        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (amr_status cs = copy_words8(t->vel, t->vel_inst, 3 * static_cast<size_t>(K), s); cs != AMR_OK) return cs;
     } else {
         std::vector<double> v(3 * static_cast<size_t>(K));
         for (int i = 0; i < K; ++i)
@@ -1105,11 +1115,6 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
                                                         K == 1 ? static_cast<uint32_t>(tot.executed) : 0u);
         AMR_LAUNCHED("k_run_dt_init");
     }
-    const long long left  = total - tot.done;
-    long long       nfull = std::min(left / k, max_intervals);
-    const long long rem   = (nfull < max_intervals) ? left % k : 0;
-    cudaGraphExec_t full = nullptr, tail = nullptr;
-    uint64_t        nk_full = 0, nk_tail = 0;
     // same-level trees: two steps per pass, guarded on the device; FP32
     // forests of 16x16 patches whose interval is kFusedSteps long run the
     // whole interval (steps and gradient flags) in one kernel
@@ -1117,6 +1122,20 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
     const bool fused = pairs && t->dtype == AMR_F32 && g.n == 16 && k == kFusedSteps &&
                        (p->criterion == 0 || p->criterion == 1) && !t->fused_off && fused_enabled(p->options);
     if (fused) AMR_CUDA(prepare_fused());
+    // A same-level graph is guarded on the device: once a re-mesh has made
+    // the tree non-uniform, the replays still queued behind it launch only
+    // kernels that find the guard set.  When the re-mesh may change the tree
+    // (its level bounds allow it), a chunk of such graphs is short at first
+    // and doubles while the tree stays same-level.
+    if (pairs && key.crit != 0 && !remesh_keeps_levels(t, p)) {
+        max_intervals = std::min(max_intervals, t->pair_chunk);
+        t->pair_chunk = std::min<long long>(t->pair_chunk * 2, 1 << 20);
+    }
+    const long long left  = total - tot.done;
+    const long long nfull = std::min(left / k, max_intervals);
+    const long long rem   = (nfull < max_intervals) ? left % k : 0;
+    cudaGraphExec_t full = nullptr, tail = nullptr;
+    uint64_t        nk_full = 0, nk_tail = 0;
     GraphKey key_full = key, key_tail = key;
     if (nfull > 0) {
         key_full.k     = static_cast<int>(k);
@@ -1247,6 +1266,26 @@ bool no_clamp(amr_tree* t, const amr_cycle_params* p, bool inst_params, long lon
 namespace amr_api {
 // Face halo of every field of an arbitrary state buffer of the tree (does
 // not touch ghosts_valid); with step_dt, only instances whose step is taken.
+// Device-to-device copy of 8-byte words by the SMs (small tables such as the
+// velocities a run uses): it never queues behind host transfers on the copy
+// engines.
+static __global__ void __launch_bounds__(256) k_copy8(uint64_t* __restrict__ dst, const uint64_t* __restrict__ src,
+                                                      size_t words)
+{
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < words;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        dst[i] = src[i];
+}
+
+amr_status copy_words8(void* dst, const void* src, size_t words, cudaStream_t s)
+{
+    if (words == 0) return AMR_OK;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((words + 255) / 256, 8ull * num_sms()));
+    k_copy8<<<grid, 256, 0, s>>>(static_cast<uint64_t*>(dst), static_cast<const uint64_t*>(src), words);
+    AMR_LAUNCHED("k_copy8");
+    return AMR_OK;
+}
+
 amr_status halo_buffer(amr_tree* t, void* buf, const double* step_dt)
 {
     const long long total = static_cast<long long>(t->size) * t->g.ndir * t->g.h * (t->g.cells / t->g.n);
@@ -1523,9 +1562,6 @@ amr_status amr_tree_patch_cells(const amr_tree* t, size_t* out)
     return AMR_OK;
 }
 
-// Copies `num` patches of every field between the tree's state (field f at f
-// * fstride) and a buffer holding the fields one after another (field f at f *
-// num patches).
 // Device-to-device copy of 16-byte words by the SMs: copies between device
 // buffers then never queue behind host transfers on the copy engines.
 __global__ void __launch_bounds__(256) k_copy16(uint4* __restrict__ dst, const uint4* __restrict__ src, size_t words)
@@ -1535,6 +1571,9 @@ __global__ void __launch_bounds__(256) k_copy16(uint4* __restrict__ dst, const u
         dst[i] = src[i];
 }
 
+// Copies `num` patches of every field between the tree's state (field f at f
+// * fstride) and a buffer holding the fields one after another (field f at f *
+// num patches).
 static amr_status copy_fields(amr_tree* t, void* dst, const void* src, size_t num, cudaMemcpyKind kind, bool to_tree)
 {
     const size_t fb = t->field_bytes(num), tstride = t->field_bytes(t->cap);
@@ -1827,7 +1866,7 @@ amr_status amr_api::advance_impl(amr_tree* t, size_t steps, const double* veloci
         for (int a = 0; a < t->g.rank; ++a) up[a] = velocity3[a] > 0.0 ? -1 : (velocity3[a] < 0.0 ? 1 : 0);
         t->vel_per_leaf = false;
     } else {
-        AMR_CUDA(cudaMemcpyAsync(t->vel, t->vel_inst, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (amr_status cs = copy_words8(t->vel, t->vel_inst, 3 * static_cast<size_t>(K), s); cs != AMR_OK) return cs;
         t->vel_per_leaf = true;
     }
     const double*  vleaf = t->vel_per_leaf ? t->vel : nullptr;
@@ -1969,7 +2008,10 @@ amr_status amr_tree_finish_advance(amr_tree* t, double* sum_dt, size_t* executed
 
 amr_status amr_tree_run(amr_tree* t, const amr_cycle_params* p, amr_cycle_stats* out)
 {
-    if (t) t->fused_off = false; // re-evaluated by every run
+    if (t) {
+        t->fused_off  = false; // re-evaluated by every run
+        t->pair_chunk = 1;
+    }
     if (!t || !p) return fail(AMR_ERR_INVALID, "null argument");
     if (p->criterion < 0 || p->criterion > 2) return fail(AMR_ERR_INVALID, "unknown criterion");
     if (t->nvar != 1) return fail(AMR_ERR_INVALID, "the advection run takes a one-field tree");
