@@ -134,8 +134,8 @@ k_run_step3d(RunBufs B, RunCtl* ctl, Geo g, const Coef* __restrict__ coef, const
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     step3d_body<T, N, S>(static_cast<const T*>(B.state[s]), static_cast<T*>(B.state[s ^ 1]), B.meta[tb],
-                         B.levels[tb], B.keys[tb], P, g, coef, coef4, up0, up1, up2, B.vel, &ctl->err, tiles, bars,
-                         p, nwarp);
+                         B.levels[tb], B.keys[tb], P, g, coef, coef4, up0, up1, up2, B.upcode,
+                         &ctl->err, tiles, bars, p, nwarp);
 }
 
 // Any geometry: ppb patches per block per round, grid-stride over rounds.

@@ -2341,8 +2341,8 @@ __device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restr
                                             const amr_halo_meta* __restrict__ meta, const int32_t* __restrict__ levels,
                                             const uint64_t* __restrict__ keys, int P, const Geo& g,
                                             const Coef* __restrict__ coef, const float4* __restrict__ coef4,
-                                            int up0, int up1, int up2, const double* __restrict__ vel, int32_t* err,
-                                            T* tiles, uint64_t* bars, int p, int nwarp)
+                                            int up0, int up1, int up2, const int32_t* __restrict__ upcode,
+                                            int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp)
 {
     using Sh               = Step3dShape<T, N>;
     constexpr int P1       = Sh::P1, PLANE = Sh::PLANE, FLAT = Sh::FLAT, GPL = Sh::GPL;
@@ -2370,8 +2370,10 @@ __device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restr
         if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
         const int inst  = keys ? instance_of(g, keys, p) : 0;
         int       up[3] = { up0, up1, up2 };
-        if (vel)
-            for (int a = 0; a < 3; ++a) up[a] = upwind(vel[3 * inst + a]);
+        if (upcode) { // per-instance upwind sides, packed (integer decode: no FP64 compares)
+            const int32_t code = upcode[inst];
+            for (int a = 0; a < 3; ++a) up[a] = unpack_upwind(code, a);
+        }
         // the row of the leaf's level: FP64 from coef, FP32 from the rows
         // rounded once (coef4)
         const int row = inst * nl + levels[p];
@@ -2484,7 +2486,7 @@ __global__ void __launch_bounds__(W * 32)
 k_step3d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
          const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef,
          const float4* __restrict__ coef4, int up0, int up1, int up2, const uint64_t* __restrict__ keys,
-         const double* __restrict__ vel, int32_t* err)
+         const int32_t* __restrict__ upcode, int32_t* err)
 {
     extern __shared__ __align__(128) unsigned char smem3d[];
     T*        tiles;
@@ -2492,7 +2494,7 @@ k_step3d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restric
     step3d_smem<T, N, W, S>(smem3d, tiles, bars);
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step3d_body<T, N, S>(in, out, meta, levels, keys, P, g, coef, coef4, up0, up1, up2, vel, err, tiles, bars, p,
+    step3d_body<T, N, S>(in, out, meta, levels, keys, P, g, coef, coef4, up0, up1, up2, upcode, err, tiles, bars, p,
                          nwarp);
 }
 

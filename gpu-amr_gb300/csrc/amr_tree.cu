@@ -186,8 +186,8 @@ int prepare_step3d()
 
 template <typename T, int N>
 amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_halo_meta* meta, int P, const Geo& g,
-                         const Coef* coef, const float4* coef4, const int* up, const uint64_t* keys, const double* vel,
-                         int32_t* err, cudaStream_t s)
+                         const Coef* coef, const float4* coef4, const int* up, const uint64_t* keys,
+                         const int32_t* upcode, int32_t* err, cudaStream_t s)
 {
     return with_ws3d(N, sizeof(T), [&]<int W, int S>() -> amr_status {
         const int occ = prepare_step3d<T, N, W, S>();
@@ -195,7 +195,7 @@ amr_status launch_step3d(const T* in, T* out, const int32_t* levels, const amr_h
         const unsigned grid = static_cast<unsigned>(
             std::max<long long>(1, std::min<long long>(grid_for(P, W), 1LL * num_sms() * occ)));
         k_step3d<T, N, W, S><<<grid, W * 32, Step3dShape<T, N>::smem(W, S), s>>>(
-            in, out, levels, meta, P, g, coef, coef4, up[0], up[1], up[2], keys, vel, err);
+            in, out, levels, meta, P, g, coef, coef4, up[0], up[1], up[2], keys, upcode, err);
         AMR_LAUNCHED("k_step3d");
         return AMR_OK;
     });
@@ -1939,9 +1939,9 @@ amr_status amr_api::advance_impl(amr_tree* t, size_t steps, const double* veloci
                 if (step3d_shape(t->g, in, out)) {
                     const float4* cf4 = reinterpret_cast<const float4*>(t->coef32) + static_cast<size_t>(k) * K * nl;
                     return t->g.n == 8 ? launch_step3d<T, 8>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
-                                                             cf4, up, t->keys[t->tb], vleaf, t->status + 7, s)
+                                                             cf4, up, t->keys[t->tb], uleaf, t->status + 7, s)
                                        : launch_step3d<T, 4>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf,
-                                                             cf4, up, t->keys[t->tb], vleaf, t->status + 7, s);
+                                                             cf4, up, t->keys[t->tb], uleaf, t->status + 7, s);
                 }
                 k_step<T, true><<<grid, 256, 0, s>>>(in, out, t->levels[t->tb], t->meta[t->tb], P, t->g, cf, up[0],
                                                      up[1], up[2], ppb, nullptr, 0.0, 0.0, 0.0, t->keys[t->tb],
