@@ -264,22 +264,20 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         return b.base + static_cast<int>(spread2(x) | (spread2(y) << 1));
     };
     // every leaf of the block's 6x6 neighbourhood inside the tree (checked
-    // before any copy is issued), its slot table, its copies; false when a
-    // leaf is out of range (nothing issued: the CTA leaves).  The barriers
-    // also order every earlier read of the tiles and of the slot table
-    // before the copies and the new table.
+    // before any copy is issued: the neighbourhood lies in the instance's
+    // leaf range [base, base + 4^L), the same for every thread), its copies
+    // and slot table; false when that range leaves the tree (nothing issued:
+    // the CTA leaves).  The barrier orders every earlier read of the tiles
+    // and of the slot table before the copies and the new table; the next
+    // block's wait barrier orders the new table before its reads.
     auto issue = [&](const IntervalBlock& b) -> bool {
-        int bad = 0;
-        if (tid < 36) {
-            const int q = leaf_at(b, tid % 6 - 1, tid / 6 - 1);
-            bad         = b.L < 2 || q < 0 || q >= P;
-        }
-        if (__syncthreads_or(bad)) {
+        if (b.L < 2 || b.base < 0 || static_cast<long long>(b.base) + (1ll << (2 * b.L)) > P) {
             if (tid == 0) atomicCAS(&ctl->err, 0, static_cast<int32_t>(AMR_ERR_UNBALANCED));
             return false;
         }
         const bool sy = b.uy > 0;
         if (tid == 0) mbar_expect_tx(bar, S::TILES); // either mirroring packs to TILES bytes
+        __syncthreads(); // the tiles and the slot table were only read since their last copies
         if (tid >= 64 && tid < 70) {
             uint32_t lo, size, start;
             interval_slot_row<D>(tid - 65, sy, lo, size, start);
@@ -287,9 +285,6 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
             slot[3 * (tid - 64) + 1] = static_cast<int>(size);
             slot[3 * (tid - 64) + 2] = static_cast<int>(start);
         }
-        // the tiles were only read by the threads since their last copies:
-        // the barrier orders those reads before the new copies
-        __syncthreads();
         if (tid < 36) {
             const int py = tid / 6 - 1, px = tid % 6 - 1;
             uint32_t  lo, size, start;
@@ -355,17 +350,34 @@ k_run_interval2d(RunBufs B, RunCtl* ctl, Geo g, const float2* __restrict__ coef3
         }
         const int r0 = ty * RY - HALO;
         uint64_t  v1[RY], v2[RY];
+        // the thread's rows cross at most one patch-row boundary: the slot
+        // entries of the first row's patch row (A) and of the next one (B),
+        // and per column the byte offset of row 0 in each
+        const int YA  = sy ? 63 - r0 : r0;
+        const int pyA = YA >> 4;
+        const int pyB = max(-1, min(4, sy ? pyA - 1 : pyA + 1));
+        int       offA[4], offB[4];
+        {
+            const int* sa = slot + 3 * (pyA + 1);
+            const int* sb = slot + 3 * (pyB + 1);
+            const int  a0 = sa[0], a1 = sa[1], a2 = sa[2], b0 = sb[0], b1 = sb[1], b2 = sb[2];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                offA[k] = a2 - a0 + cslot[k] * a1 + cbyte[k];
+                offB[k] = b2 - b0 + cslot[k] * b1 + cbyte[k];
+            }
+        }
 #pragma unroll
         for (int i = 0; i < RY; ++i) {
             const int r    = r0 + i;
             float     e[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
             if (r <= 64) {
-                const int            Y    = sy ? 63 - r : r;
-                const int*           sr   = slot + 3 * ((Y >> 4) + 1);
-                const int            size = sr[1];
-                const unsigned char* rowp = tiles + sr[2] + ((Y & 15) + 1) * 72 - sr[0];
+                const int  Y   = sy ? 63 - r : r;
+                const bool inA = (Y >> 4) == pyA;
+                const int  ro  = ((Y & 15) + 1) * 72;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) e[k] = *reinterpret_cast<const float*>(rowp + cslot[k] * size + cbyte[k]);
+                for (int k = 0; k < 4; ++k)
+                    e[k] = *reinterpret_cast<const float*>(tiles + (inA ? offA[k] : offB[k]) + ro);
             }
             v1[i] = pk(e[0], e[2]);
             v2[i] = pk(e[1], e[3]);
