@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "amr_gb300.h"
+#include "amr_adjoint.cuh"
 #include "amr_cycle.cuh"
 #include "amr_euler.cuh"
 #include "amr_ssprk.cuh"

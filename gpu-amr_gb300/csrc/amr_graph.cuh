@@ -10,7 +10,9 @@
 // returns at once, leaving the tree as it was when the error was found.
 #pragma once
 
-#include "amr_kernels.cuh"
+#include "amr_flags2d.cuh"
+#include "amr_step2d.cuh"
+#include "amr_step3d.cuh"
 
 namespace amr_gb300 {
 

@@ -1,4 +1,8 @@
-// Kernels of the GB300 AMR hot path.
+// Kernels of the GB300 AMR hot path: the per-cell update and halo rules of
+// any geometry, the gradient and max-value flags, the step sizes, the re-mesh
+// and the reference drop-ins.  The shape-specialised kernels live beside it:
+// amr_step2d.cuh (2D updates and passes), amr_flags2d.cuh (2D flags),
+// amr_step3d.cuh (the staged 3D update), amr_adjoint.cuh (the adjoint).
 //
 // Every per-item body is a __device__ function so the same arithmetic runs in
 // the per-launch kernels below and in the persistent cluster kernel
@@ -1005,1497 +1009,6 @@ static __global__ void k_finalize_dt(const int32_t* __restrict__ max_level, Geo 
         *remaining -= step_dt;
         ++(*count);
     }
-}
-
-} // namespace amr_gb300
-
-namespace amr_gb300 {
-
-// ------------------------------------------------ 2D update, sized at compile time
-// One warp per patch (grid-stride over patches: the Morton-ordered leaf array
-// of every instance is the work list).  The whole padded patch is contiguous,
-// so it moves into a per-warp shared-memory tile with one bulk async copy
-// (cp.async.bulk, completed on an mbarrier).  Each warp owns S tiles in a
-// ring and keeps S-1 copies in flight ahead of the patch it works on (S = 1:
-// load, then compute).  Lanes write the upwind ghost column and ghost row
-// into the tile (halo rules, ghost_value), each lane updates a contiguous run
-// of N*N/32 interior cells, the results go back into the tile, and the tile
-// is stored to the output patch whole in 16-byte words (ghost cells pass
-// through), so every HBM access is a full aligned sector.  A copy that does
-// not land within the wait cap sets *err = AMR_ERR_TIMEOUT; the warp then
-// drains its other copies (also capped) and stops.
-template <typename T, int N, int H>
-struct Step2dShape {
-    static constexpr int P1   = N + 2 * H;
-    static constexpr int FLAT = P1 * P1;
-    // Only the interior rows are read and written: the 16-byte-aligned byte
-    // span [LO, HI) covering rows H .. N+H-1 (ghost columns included).  The
-    // upwind ghost row and column are evaluated on the fly, the other ghost
-    // cells are never read.
-    static constexpr uint32_t LO    = (H * P1 * sizeof(T)) & ~15u;
-    static constexpr uint32_t HI    = ((N + H) * P1 * sizeof(T) + 15u) & ~15u;
-    static constexpr uint32_t BYTES = HI - LO;
-    static constexpr int      WORDS = BYTES / 16;
-    // Each lane updates a column segment: column (lane % N), rows
-    // (lane / N) * SEG .. + SEG - 1 (interior coordinates).  For a fixed row
-    // offset the warp reads whole rows, so shared-memory accesses are free of
-    // bank conflicts, and the y-neighbours of a lane's cells are its own
-    // registers.
-    static constexpr int      RG    = 32 / N;      // row groups
-    static constexpr int      SEG   = N * N / 32;  // interior cells per lane
-    static constexpr size_t   TILE  = FLAT * sizeof(T);
-    static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
-    static_assert(32 % N == 0 && RG * SEG == N, "a lane's cells must form one column segment");
-    // dynamic shared memory of a block of W warps with S tiles each
-    static constexpr size_t smem(int W, int S) { return static_cast<size_t>(W) * S * (TILE + 8); }
-};
-
-// Coefficients of one (step, instance, level) row as the 2D kernel reads
-// them: FP32 needs only (c_x, c_y) (difference form), FP64 (c0, c_x, c_y).
-template <typename T>
-struct Coef2 {
-    double c0, cx, cy;
-};
-template <>
-struct Coef2<float> {
-    float cx, cy;
-};
-
-// One cell update of the 2D kernels from the cell u, its upwind x neighbour
-// xn and upwind y neighbour yn.  FP32: u + c (u_up - u), exact for a constant
-// state, so the rounding of the coefficients does not bias the solution;
-// FP64: c0 u + c_x u_x + c_y u_y.  Every 2D update goes through this one
-// function, so fused and separate steps round alike.
-template <typename T>
-__device__ __forceinline__ T upd2d_core(T u, T xn, T yn, const Coef2<T>& cf, bool xu, bool yu)
-{
-    if constexpr (sizeof(T) == 4) {
-        float acc = u;
-        if (xu) acc = fmaf(cf.cx, xn - u, acc);
-        if (yu) acc = fmaf(cf.cy, yn - u, acc);
-        return acc;
-    } else {
-        T acc = static_cast<T>(cf.c0) * u;
-        if (xu) acc = fma(static_cast<T>(cf.cx), xn, acc);
-        if (yu) acc = fma(static_cast<T>(cf.cy), yn, acc);
-        return acc;
-    }
-}
-template <typename T>
-__device__ __forceinline__ T upd2d(T u, T xn, T yn, const Coef2<T>& cf, int ux, int uy)
-{
-    return upd2d_core<T>(u, xn, yn, cf, ux != 0, uy != 0);
-}
-// The same update with the upwind axes known at compile time (the multi-step
-// pass branches once per patch on them).
-template <typename T, bool XU, bool YU>
-__device__ __forceinline__ T upd2d_fixed(T u, T xn, T yn, const Coef2<T>& cf)
-{
-    return upd2d_core<T>(u, xn, yn, cf, XU, YU);
-}
-
-// coef: the full rows (FP64 path); coef32: (c_x, c_y) rows (FP32 path);
-// upcode: per-instance packed upwind offsets, or nullptr for upx0/upy0.
-template <typename T, int N, int H, int S>
-__device__ __forceinline__ void step2d_body(const T* __restrict__ in, T* __restrict__ out,
-                                            const amr_halo_meta* __restrict__ meta, int P, const Geo& g,
-                                            const Coef* __restrict__ coef, const float2* __restrict__ coef32,
-                                            int upx0, int upy0, int32_t* err, const uint64_t* __restrict__ keys,
-                                            const int32_t* __restrict__ upcode, T* tiles, uint64_t* bars, int p,
-                                            int nwarp)
-{
-    using Sh                = Step2dShape<T, N, H>;
-    constexpr int      P1   = Sh::P1;
-    constexpr int      FLAT = Sh::FLAT;
-    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
-    constexpr int      SEG  = Sh::SEG;
-    constexpr int      HALF = N / 2;
-    const int          lane = threadIdx.x & 31;
-    if (lane == 0) {
-        for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
-        mbar_init_fence();
-    }
-    __syncwarp();
-    const char* in_bytes = reinterpret_cast<const char*>(in);
-    auto        request  = [&](int q, int slot) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bars[slot], BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
-                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
-    };
-    // prologue: copies for the first S-1 patches of this warp
-    if (lane == 0)
-        for (int j = 0; j < S - 1; ++j)
-            if (p + j * nwarp < P) request(p + j * nwarp, j);
-    uint32_t  phase = 0; // bit b: parity of slot b's next completion
-    const int cl = lane % N + H, r0 = (lane / N) * SEG + H; // this lane's column and first row
-    const int nl = g.depth + 1;
-
-    // Ghost job of this lane: lanes 0..N-1 the upwind ghost column (normal
-    // layout dim 1), lanes N..2N-1 the upwind ghost row (dim 0); tg is the
-    // tangential padded coordinate, fsel the finer-neighbour section it lies in.
-    const bool col  = lane < N;
-    const bool job  = lane < 2 * N;
-    const int  L    = col ? 1 : 0;
-    const int  tg   = (col ? lane : lane - N) + H;
-    const int  fsel = (tg - H) / HALF;
-
-    // Per-patch metadata, software-pipelined so that no load is consumed in
-    // the iteration that issues it: the key three patches ahead, the upwind
-    // sides, coefficient row and this lane's neighbour record two ahead, the
-    // raw ghost source values one ahead.  The instance comes from the key;
-    // the upwind sides from its velocity (vel != nullptr) or upx0/upy0.
-    struct Side {
-        int      ux, uy;
-        Coef2<T> cf;
-    };
-    struct Rec {
-        int rel, nb, fid, q0, q1;
-    };
-    struct Raw {
-        T   v[4];
-        int kind; // 0 none, 1 one value, 4 mean of four
-    };
-    auto side_of = [&](uint64_t key, Side& sd) {
-        const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
-        sd.ux          = upx0;
-        sd.uy          = upy0;
-        if (upcode) {
-            const int32_t code = upcode[inst];
-            sd.ux              = unpack_upwind(code, 0);
-            sd.uy              = unpack_upwind(code, 1);
-        }
-        const int row = inst * nl + key_level(key);
-        if constexpr (sizeof(T) == 4) {
-            const float2 c = coef32[row];
-            sd.cf.cx       = c.x;
-            sd.cf.cy       = c.y;
-        } else {
-            const Coef& c = coef[row];
-            sd.cf.c0      = c.c0;
-            sd.cf.cx      = c.c[0];
-            sd.cf.cy      = c.c[1];
-        }
-    };
-    auto has_job = [&](const Side& sd) { return job && (col ? sd.ux != 0 : sd.uy != 0); };
-    auto pos_of  = [&](const Side& sd) { return col ? (sd.ux > 0 ? 1 : 0) : (sd.uy > 0 ? 1 : 0); };
-    auto rec_of  = [&](int q, const Side& sd, Rec& m) {
-        m.rel = REL_NONE;
-        if (!has_job(sd)) return;
-        const amr_halo_meta* rp = meta + static_cast<size_t>(q) * 4 + 2 * L + pos_of(sd);
-        m.rel                   = rp->relation;
-        m.nb                    = rp->neighbor;
-        m.fid                   = rp->finer_ids[fsel];
-        m.q0                    = rp->quadrant[0];
-        m.q1                    = rp->quadrant[1];
-    };
-    // The halo rules of ghost_value for one 2D face ghost cell, split into
-    // issuing the source loads and combining them.
-    // (the source address is formed with selects so lanes with different
-    // relations do not diverge; only the three extra loads of the mean are
-    // predicated)
-    auto fetch = [&](int q, const Side& sd, const Rec& m, Raw& raw) {
-        raw.kind = 0;
-        if (!has_job(sd)) return;
-        const int  pos = pos_of(sd);
-        const int  gc  = pos ? N + H : H - 1;
-        const int  G0 = col ? tg : gc, G1 = col ? gc : tg;
-        const int  sh = pos ? -N : N;
-        const int  s0 = G0 + (L == 0 ? sh : 0), s1 = G1 + (L == 1 ? sh : 0); // same-level source
-        const bool same = m.rel == REL_SAME, coarser = m.rel == REL_COARSER, finer = m.rel == REL_FINER;
-        const int  c0 = H + m.q0 * HALF + (s0 - H) / 2, c1 = H + m.q1 * HALF + (s1 - H) / 2;
-        const int  d0 = ((s0 - H) * 2) % N + H, d1 = ((s1 - H) * 2) % N + H;
-        const int  f0 = same ? s0 : coarser ? c0 : finer ? d0 : G0;
-        const int  f1 = same ? s1 : coarser ? c1 : finer ? d1 : G1;
-        const int  src = (same || coarser) ? m.nb : finer ? m.fid : q;
-        const T*   fp  = in + static_cast<size_t>(src) * FLAT + f0 * P1 + f1;
-        raw.v[0]       = fp[0];
-        raw.kind       = finer ? 4 : 1;
-        if (finer) {
-            raw.v[1] = fp[1];
-            raw.v[2] = fp[P1];
-            raw.v[3] = fp[P1 + 1];
-        }
-    };
-    auto combine = [&](const Raw& raw) -> T {
-        if (raw.kind == 4) {
-            double sum = static_cast<double>(raw.v[0]);
-            sum += static_cast<double>(raw.v[1]);
-            sum += static_cast<double>(raw.v[2]);
-            sum += static_cast<double>(raw.v[3]);
-            return static_cast<T>(sum / 4.0);
-        }
-        return raw.v[0];
-    };
-
-    // pipeline prologue
-    const int q1 = p + nwarp, q2 = p + 2 * nwarp;
-    Side      sd0{}, sd1{}, sd2{};
-    Rec       m1{}, m2{};
-    Raw       g0{}, g1{};
-    uint64_t  k2 = 0;
-    if (p < P) {
-        side_of(keys[p], sd0);
-        Rec m0;
-        rec_of(p, sd0, m0);
-        fetch(p, sd0, m0, g0);
-    }
-    if (q1 < P) {
-        side_of(keys[q1], sd1);
-        rec_of(q1, sd1, m1);
-    }
-    if (q2 < P) k2 = keys[q2];
-
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it % S;
-        const int pf = p + (S - 1) * nwarp; // patch whose copy is issued now
-        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
-        // advance the metadata pipeline
-        const int pa = p + nwarp, pb = p + 2 * nwarp, pc = p + 3 * nwarp;
-        uint64_t  k3 = 0;
-        if (pc < P) k3 = keys[pc];
-        if (pb < P) {
-            side_of(k2, sd2);
-            rec_of(pb, sd2, m2);
-        }
-        if (pa < P) fetch(pa, sd1, m1, g1);
-        // this patch
-        const bool has = has_job(sd0);
-        const int  pos = pos_of(sd0);
-        const int  gc  = pos ? N + H : H - 1;
-        const int  G0 = col ? tg : gc, G1 = col ? gc : tg;
-        const T    gv  = combine(g0);
-        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
-            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            phase ^= 1u << b;
-            for (int j = 1; j < S; ++j) // drain the copies still in flight
-                if (p + j * nwarp < P) {
-                    const int sl = (it + j) % S;
-                    mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u);
-                    phase ^= 1u << sl;
-                }
-            return;
-        }
-        phase ^= 1u << b;
-        T* tile = tiles + static_cast<size_t>(b) * FLAT;
-        if (has) tile[G0 * P1 + G1] = gv;
-        __syncwarp();
-        const int ux = sd0.ux, uy = sd0.uy;
-        // the lane's column, rows r0-1 .. r0+SEG (the end rows are the
-        // neighbouring segments' cells or the upwind ghost row)
-        T colv[SEG + 2];
-#pragma unroll
-        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
-        T res[SEG];
-#pragma unroll
-        for (int k = 0; k < SEG; ++k)
-            res[k] = upd2d<T>(colv[k + 1], tile[(r0 + k) * P1 + cl + ux], uy < 0 ? colv[k] : colv[k + 2], sd0.cf, ux, uy);
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < SEG; ++k) tile[(r0 + k) * P1 + cl] = res[k];
-        __syncwarp();
-        const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + LO);
-        uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO);
-        for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
-        __syncwarp();
-        // rotate the pipeline
-        sd0 = sd1;
-        g0  = g1;
-        sd1 = sd2;
-        m1  = m2;
-        k2  = k3;
-    }
-}
-
-// ------------------------------------------------ pass records
-// One 16-byte record per leaf for the multi-step pass: the same-level
-// neighbours across the upwind x face (x) and y face (y), the x-neighbour's
-// y-neighbour (z: the diagonal whose corner reaches the patch within a
-// pass), and the instance, level and upwind offsets packed into w.  A zero
-// velocity component names the patch itself.  Optionally a second record
-// per leaf holds all four face neighbours (x low, x high, y low, y high) for
-// the gradient flags of the same tree.  The records are built once per mesh
-// and velocity field, so the kernels read one record per patch instead of a
-// chain of dependent face-record loads.  A face that is not same-level sets
-// AMR_ERR_UNBALANCED (passes run only where every relation is same-level).
-__host__ __device__ __forceinline__ int pass_code(int ux, int uy, int inst, int level)
-{
-    return (inst << 10) | (level << 4) | ((ux + 1) << 2) | (uy + 1);
-}
-__host__ __device__ __forceinline__ int pass_ux(int code) { return ((code >> 2) & 3) - 1; }
-__host__ __device__ __forceinline__ int pass_uy(int code) { return (code & 3) - 1; }
-__host__ __device__ __forceinline__ int pass_level(int code) { return (code >> 4) & 63; }
-__host__ __device__ __forceinline__ int pass_inst(int code) { return code >> 10; }
-
-__device__ __forceinline__ void pass_record(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
-                                            const int32_t* __restrict__ upcode, int upx0, int upy0, const Geo& g,
-                                            int q, int4* __restrict__ rec, int4* __restrict__ frec, int32_t* err)
-{
-    const uint64_t key  = keys[q];
-    const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
-    int            ux = upx0, uy = upy0;
-    if (upcode) {
-        const int32_t code = upcode[inst];
-        ux                 = unpack_upwind(code, 0);
-        uy                 = unpack_upwind(code, 1);
-    }
-    auto same = [&](const amr_halo_meta& m, int self) {
-        if (m.relation != REL_SAME) {
-            atomicExch(err, static_cast<int32_t>(AMR_ERR_UNBALANCED));
-            return self;
-        }
-        return m.neighbor;
-    };
-    int4 r;
-    r.x    = ux != 0 ? same(meta[static_cast<size_t>(q) * 4 + 2 + (ux > 0 ? 1 : 0)], q) : q;
-    r.y    = uy != 0 ? same(meta[static_cast<size_t>(q) * 4 + (uy > 0 ? 1 : 0)], q) : q;
-    r.z    = ux != 0 && uy != 0 ? same(meta[static_cast<size_t>(r.x) * 4 + (uy > 0 ? 1 : 0)], r.x) : q;
-    r.w    = pass_code(ux, uy, inst, key_level(key));
-    rec[q] = r;
-    if (frec) {
-        const amr_halo_meta* m = meta + static_cast<size_t>(q) * 4;
-        frec[q]                = make_int4(same(m[2], q), same(m[3], q), same(m[0], q), same(m[1], q));
-    }
-}
-
-// Host-driven build: P leaves, upwind offsets per instance (upcode) or
-// launch-wide (upx0, upy0).
-static __global__ void __launch_bounds__(256)
-k_pass_records(const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys,
-               const int32_t* __restrict__ upcode, int upx0, int upy0, int P, Geo g, int4* __restrict__ rec,
-               int32_t* err)
-{
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P; q += gridDim.x * blockDim.x)
-        pass_record(meta, keys, upcode, upx0, upy0, g, q, rec, nullptr, err);
-}
-
-// ------------------------------------------------ 2D update, D steps per pass
-// D consecutive steps of a tree whose every neighbour relation is "same
-// level" (each instance uniform, as in the batched forests), in one pass over
-// memory: the patch is read once and written once per D steps.  Step m needs
-// the upwind ghost column and row of u^{m-1}, which are the neighbours' edge
-// cells after m-1 steps.  The warp recomputes them with upd2d from u^n: the
-// neighbours' D outermost columns / rows (the strips) and the D(D-1)/2 cells
-// of the diagonal neighbour's corner that reach the patch within D steps
-// (upwind distance a in y and b in x, a, b >= 1, a + b <= D).  Each value is
-// formed by the same operation on the same inputs as in D separate steps (the
-// halo exchange of a same-level neighbour is a copy), so the result is
-// bit-identical.
-//
-// Between the tile load and the write-back the cells stay in registers, in
-// upwind-normalized coordinates: on an axis whose upwind side is + the
-// normalized index i' is N-1-i (i the interior index), otherwise i, so a
-// cell's upwind neighbours are always at i'-1 and j'-1.  Lane (r, c) =
-// (lane / 8, lane % 8) owns the BR x BC block of normalized rows r*BR..,
-// columns c*BC..  Per step only block edges cross lanes, through two small
-// shared buffers per warp: X[c][i'] holds, for normalized row i', the cell
-// left of block column c (normalized column c*BC-1, the distance-1 ghost for
-// c = 0); Y[r][j'] the cell above block row r.  Each lane stores its last
-// column and its last row (one vector store each) and loads its block's
-// upwind edges (one vector load each); the buffers alternate between steps,
-// so one warp barrier per step orders them.
-//
-// Strips: lanes 0..N-1 hold the ghost column of normalized row lane, lanes
-// N..2N-1 the ghost row of normalized column lane-N; each holds s[1..D]
-// (s[d] = the ghost cell at upwind distance d) and stores s[1] into X[0] /
-// Y[0] every step.  Lanes 0 and N hold the corner triangle.  After step m
-// the strips and the corner advance one step on the distances still needed
-// (d <= D-m).  Per patch the warp reads its pass record two patches ahead,
-// its strips one ahead and the corner before the tile wait; the steps branch
-// once on which velocity components are non-zero, and each step's
-// coefficient row is read one step ahead.
-template <int D>
-__host__ __device__ constexpr int corner_index(int a, int b)
-{
-    int base = 0;
-    for (int r = 1; r < a; ++r) base += D - r;
-    return base + (b - 1);
-}
-
-// Warp layout and shared memory of the multi-step pass.
-template <typename T, int N, int H>
-struct PassShape {
-    using Sh                = Step2dShape<T, N, H>;
-    static constexpr int RB = 4, CB = 8;           // block rows and block columns of the warp
-    static constexpr int BR = N / RB, BC = N / CB; // cells of a lane's block
-    // X rows are padded by 16 bytes: the lanes of one block row store and
-    // load X rows c = 0..7 at the same offset, and the padding spreads them
-    // over distinct banks (Y rows are contiguous across lanes already)
-    static constexpr int XN = N + 16 / static_cast<int>(sizeof(T));
-    static constexpr int XS = (CB + 1) * XN;       // X[c][i'], c = 0..CB
-    static constexpr int YS = (RB + 1) * N;        // Y[r][j'], r = 0..RB
-    static constexpr int XY = 2 * (XS + YS);       // elements per warp: two of each
-    static_assert(BR * RB == N && BC * CB == N, "patch edge must be a multiple of 8");
-    static_assert((XS * sizeof(T)) % 16 == 0 && (YS * sizeof(T)) % 16 == 0, "exchange buffers stay 16-byte aligned");
-    // dynamic shared memory of a block of W warps with S tiles each: the
-    // tiles, the exchange buffers, the barriers
-    static constexpr size_t smem(int W, int S)
-    {
-        return static_cast<size_t>(W) * (S * (Sh::TILE + 8) + XY * sizeof(T));
-    }
-};
-
-// K consecutive shared-memory elements moved as the widest aligned vectors
-// (callers' offsets are multiples of K elements).
-template <typename T, int K>
-__device__ __forceinline__ void lds_vec(const T* p, T (&v)[K])
-{
-    if constexpr ((K * sizeof(T)) % 16 == 0) {
-#pragma unroll
-        for (int i = 0; i < static_cast<int>(K * sizeof(T) / 16); ++i) {
-            if constexpr (sizeof(T) == 4) {
-                const float4 w = reinterpret_cast<const float4*>(p)[i];
-                v[4 * i]       = w.x;
-                v[4 * i + 1]   = w.y;
-                v[4 * i + 2]   = w.z;
-                v[4 * i + 3]   = w.w;
-            } else {
-                const double2 w = reinterpret_cast<const double2*>(p)[i];
-                v[2 * i]        = w.x;
-                v[2 * i + 1]    = w.y;
-            }
-        }
-    } else if constexpr (sizeof(T) == 4 && K == 2) {
-        const float2 w = *reinterpret_cast<const float2*>(p);
-        v[0]           = w.x;
-        v[1]           = w.y;
-    } else {
-#pragma unroll
-        for (int i = 0; i < K; ++i) v[i] = p[i];
-    }
-}
-template <typename T, int K>
-__device__ __forceinline__ void sts_vec(T* p, const T (&v)[K])
-{
-    if constexpr ((K * sizeof(T)) % 16 == 0) {
-#pragma unroll
-        for (int i = 0; i < static_cast<int>(K * sizeof(T) / 16); ++i) {
-            if constexpr (sizeof(T) == 4)
-                reinterpret_cast<float4*>(p)[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-            else
-                reinterpret_cast<double2*>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
-        }
-    } else if constexpr (sizeof(T) == 4 && K == 2) {
-        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
-    } else {
-#pragma unroll
-        for (int i = 0; i < K; ++i) p[i] = v[i];
-    }
-}
-
-template <typename T, int N, int H, int S, int D>
-__device__ __forceinline__ void step2d_pass_body(const T* __restrict__ in, T* __restrict__ out,
-                                                                                                  const int4* __restrict__ rec, int P, int nl,
-                                                 const Coef* __restrict__ coef, const float2* __restrict__ coef32,
-                                                 size_t cstride, int32_t* err, T* tiles, T* xy, uint64_t* bars, int p,
-                                                 int nwarp)
-{
-    static_assert(D >= 2 && D <= 6, "two to six steps per pass");
-    using Sh                = Step2dShape<T, N, H>;
-    using Ps                = PassShape<T, N, H>;
-    constexpr int      P1   = Sh::P1;
-    constexpr int      FLAT = Sh::FLAT;
-    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
-    constexpr int      BR = Ps::BR, BC = Ps::BC, XN = Ps::XN, XS = Ps::XS, YS = Ps::YS;
-    constexpr int      NC   = D * (D - 1) / 2; // corner cells
-    const int          lane = threadIdx.x & 31;
-    if (lane == 0) {
-        for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
-        mbar_init_fence();
-    }
-    __syncwarp();
-    const char* in_bytes = reinterpret_cast<const char*>(in);
-    auto        request  = [&](int q, int slot) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bars[slot], BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
-                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
-    };
-    // A tiles are in flight ahead of the current one; a slot is refilled only
-    // once the bulk store of its previous patch has read it, and at most
-    // PEND stores (the newest) may still be reading when a slot is refilled
-    constexpr int A    = S >= 2 ? S - 2 : 0;
-    constexpr int PEND = S - 1 - A;
-    if (lane == 0)
-        for (int j = 0; j < A; ++j)
-            if (p + j * nwarp < P) request(p + j * nwarp, j);
-    uint32_t   phase = 0;
-    const int  rb = lane >> 3, cb = lane & 7; // the lane's block
-    const bool col  = lane < N;              // ghost-column strip of normalized row `lane`
-    const bool job  = lane < 2 * N;
-    const int  sl   = col ? lane : lane - N; // normalized tangential index of the lane's strip
-    const bool inr  = sl > 0;                // tangential upwind neighbour: the previous strip lane, else the corner
-    const int  src  = inr ? lane - 1 : lane;
-    const bool hold = lane == 0 || lane == N; // corner holders
-
-    auto coef_of = [&](int step, int row, Coef2<T>& c) {
-        if constexpr (sizeof(T) == 4) {
-            const float2 v = coef32[step * cstride + row];
-            c.cx           = v.x;
-            c.cy           = v.y;
-        } else {
-            const Coef& v = coef[step * cstride + row];
-            c.c0          = v.c0;
-            c.cx          = v.c[0];
-            c.cy          = v.c[1];
-        }
-    };
-    auto has_job = [&](int ux, int uy) { return job && (col ? ux != 0 : uy != 0); };
-    // one patch ahead: the lane's strip (u^n at distances 1..D, at the actual
-    // tangential coordinate of its normalized index)
-    auto fetch = [&](const int4& r, T* v) {
-#pragma unroll
-        for (int d = 1; d <= D; ++d) v[d] = T(0);
-        const int ux = pass_ux(r.w), uy = pass_uy(r.w);
-        if (!has_job(ux, uy)) return;
-        const int pos = col ? (ux > 0 ? 1 : 0) : (uy > 0 ? 1 : 0);
-        const int tg  = ((col ? uy : ux) > 0 ? N - 1 - sl : sl) + H;
-        const T*  nbp = in + static_cast<size_t>(col ? r.x : r.y) * FLAT;
-#pragma unroll
-        for (int d = 1; d <= D; ++d) {
-            const int line = pos ? H + d - 1 : N + H - d; // the neighbour's line at distance d
-            v[d]           = nbp[col ? tg * P1 + line : line * P1 + tg];
-        }
-    };
-
-    // records two patches ahead, strips one ahead
-    const int q1 = p + nwarp;
-    int4      r0{}, r1{}, r2{};
-    T         sa[D + 1], sb[D + 1]; // strips of this patch and the next
-#pragma unroll
-    for (int d = 0; d <= D; ++d) sa[d] = sb[d] = T(0);
-    if (p < P) {
-        r0 = __ldg(rec + p);
-        fetch(r0, sa);
-    }
-    if (q1 < P) r1 = __ldg(rec + q1);
-    // the strip's distance-1 ghost in X[0] / Y[0] of the first buffer
-    T* const gx = xy + (col ? sl : XS + sl);
-
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it % S;
-        const int pf = p + A * nwarp;
-        if (pf < P && lane == 0) {
-            bulk_wait_read<PEND>(); // the slot's last store has read it
-            request(pf, (it + A) % S);
-        }
-        const int pa = p + nwarp, pb = p + 2 * nwarp;
-        if (pb < P) r2 = __ldg(rec + pb);
-        if (pa < P) fetch(r1, sb);
-        // this patch
-        const int ux = pass_ux(r0.w), uy = pass_uy(r0.w), row = pass_inst(r0.w) * nl + pass_level(r0.w);
-        T         cn[NC > 0 ? NC : 1];
-#pragma unroll
-        for (int c = 0; c < (NC > 0 ? NC : 1); ++c) cn[c] = T(0);
-        if (hold && ux != 0 && uy != 0) {
-            const T* dg = in + static_cast<size_t>(r0.z) * FLAT;
-#pragma unroll
-            for (int a = 1; a < D; ++a)
-#pragma unroll
-                for (int bb = 1; a + bb <= D; ++bb)
-                    cn[corner_index<D>(a, bb)] = dg[(uy > 0 ? H + a - 1 : N + H - a) * P1 + (ux > 0 ? H + bb - 1 : N + H - bb)];
-        }
-        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
-            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            phase ^= 1u << b;
-            for (int j = 1; j <= A; ++j)
-                if (p + j * nwarp < P) {
-                    const int sl2 = (it + j) % S;
-                    mbar_wait_bounded(&bars[sl2], (phase >> sl2) & 1u);
-                    phase ^= 1u << sl2;
-                }
-            if (lane == 0) bulk_wait_all();
-            return;
-        }
-        phase ^= 1u << b;
-        T*         tile = tiles + static_cast<size_t>(b) * FLAT;
-        const bool has  = has_job(ux, uy);
-        // the lane's block: normalized cell (rb*BR + a, cb*BC + e) is the
-        // tile cell cell[a * sr + e * sc]
-        const int sr = uy > 0 ? -P1 : P1, sc = ux > 0 ? -1 : 1;
-        T*        cell = tile + (H + (uy > 0 ? N - 1 - rb * BR : rb * BR)) * P1 + H + (ux > 0 ? N - 1 - cb * BC : cb * BC);
-        T         v[BR][BC];
-#pragma unroll
-        for (int a = 0; a < BR; ++a)
-#pragma unroll
-            for (int e = 0; e < BC; ++e) v[a][e] = cell[a * sr + e * sc];
-        // the D steps, compiled once per combination of upwind axes
-        auto steps = [&]<bool XU, bool YU>() {
-            Coef2<T> cf, cfn;
-            coef_of(0, row, cf);
-#pragma unroll
-            for (int m = 1; m <= D; ++m) {
-                if (m < D) coef_of(m, row, cfn); // the next step's row, one step ahead
-                T* const X = xy + (m & 1) * (XS + YS);
-                T* const Y = X + XS;
-                {
-                    T last[BR];
-#pragma unroll
-                    for (int a = 0; a < BR; ++a) last[a] = v[a][BC - 1];
-                    sts_vec<T, BR>(X + (cb + 1) * XN + rb * BR, last);
-                }
-                sts_vec<T, BC>(Y + (rb + 1) * N + cb * BC, v[BR - 1]);
-                if (has) gx[(m & 1) * (XS + YS)] = sa[1]; // u^{m-1} ghosts
-                __syncwarp();
-                T xin[BR], yin[BC];
-                lds_vec<T, BR>(X + cb * XN + rb * BR, xin);
-                lds_vec<T, BC>(Y + rb * N + cb * BC, yin);
-                // in place, last row and column first: a cell's upwind
-                // neighbours are still u^{m-1} when it is updated
-#pragma unroll
-                for (int a = BR - 1; a >= 0; --a)
-#pragma unroll
-                    for (int e = BC - 1; e >= 0; --e)
-                        v[a][e] = upd2d_fixed<T, XU, YU>(v[a][e], e == 0 ? xin[a] : v[a][e - 1],
-                                                         a == 0 ? yin[e] : v[a - 1][e], cf);
-                if (m < D) {
-                    // strips to u^m on the distances still needed, ascending:
-                    // a lane's distance d+1 and its neighbours' distance d
-                    // are still u^{m-1} when distance d is updated (the
-                    // shuffles of distance d precede every lane's update)
-#pragma unroll
-                    for (int d = 1; d <= D - m; ++d) {
-                        const T tnb  = __shfl_sync(0xffffffffu, sa[d], src);
-                        const T tang = inr ? tnb : (col ? cn[corner_index<D>(1, d)] : cn[corner_index<D>(d, 1)]);
-                        const T nrm  = sa[d + 1];
-                        sa[d]        = upd2d_fixed<T, XU, YU>(sa[d], col ? nrm : tang, col ? tang : nrm, cf);
-                    }
-                    // the corner in place, by increasing distance a + b: a
-                    // cell reads the cells at distance + 1, still u^{m-1}
-                    if (NC > 0 && XU && YU) {
-#pragma unroll
-                        for (int sum = 2; sum <= D - m; ++sum)
-#pragma unroll
-                            for (int a = 1; a < sum; ++a)
-                                cn[corner_index<D>(a, sum - a)] = upd2d_fixed<T, XU, YU>(
-                                    cn[corner_index<D>(a, sum - a)], cn[corner_index<D>(a, sum - a + 1)],
-                                    cn[corner_index<D>(a + 1, sum - a)], cf);
-                    }
-                    cf = cfn;
-                }
-            }
-        };
-        if (ux != 0 && uy != 0) steps.template operator()<true, true>();
-        else if (ux != 0) steps.template operator()<true, false>();
-        else if (uy != 0) steps.template operator()<false, true>();
-        else steps.template operator()<false, false>();
-        // back into the tile in its own orientation, then the interior rows
-        // out by one bulk store (the async proxy sees every lane's writes)
-#pragma unroll
-        for (int a = 0; a < BR; ++a)
-#pragma unroll
-            for (int e = 0; e < BC; ++e) cell[a * sr + e * sc] = v[a][e];
-        fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-            bulk_copy_s2g(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + LO,
-                          reinterpret_cast<const char*>(tile) + LO, BYTES);
-            bulk_commit();
-        }
-        r0 = r1;
-        r1 = r2;
-#pragma unroll
-        for (int d = 1; d <= D; ++d) sa[d] = sb[d];
-    }
-    if (lane == 0) bulk_wait_all(); // the last stores complete before the block's shared memory goes
-}
-
-// Warp w of the block: its S tiles, its exchange buffers and its S barriers
-// in dynamic shared memory (multi-step pass).
-template <typename T, int N, int H, int W, int S>
-__device__ __forceinline__ void pass2d_smem(unsigned char* smem, T*& tiles, T*& xy, uint64_t*& bars)
-{
-    using Sh      = Step2dShape<T, N, H>;
-    using Ps      = PassShape<T, N, H>;
-    const int wib = threadIdx.x >> 5;
-    tiles         = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * S * Sh::FLAT;
-    xy            = reinterpret_cast<T*>(smem + static_cast<size_t>(W) * S * Sh::TILE) + static_cast<size_t>(wib) * Ps::XY;
-    bars          = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * (S * Sh::TILE + Ps::XY * sizeof(T))) +
-           wib * S;
-}
-
-// Warp w of the block: its S tiles and S barriers in dynamic shared memory.
-template <typename T, int N, int H, int W, int S>
-__device__ __forceinline__ void step2d_smem(unsigned char* smem, T*& tiles, uint64_t*& bars)
-{
-    using Sh       = Step2dShape<T, N, H>;
-    const int wib  = threadIdx.x >> 5;
-    tiles          = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * S * Sh::FLAT;
-    bars           = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * S * Sh::TILE) + wib * S;
-}
-
-// Register budget: 32 resident warps per SM for FP32, 24 for FP64 (the
-// metadata pipeline keeps three patches' records in registers).
-template <typename T, int W>
-struct Step2dOcc {
-    static constexpr int blocks = ((sizeof(T) == 4 ? 40 : 24) / W) > 0 ? ((sizeof(T) == 4 ? 40 : 24) / W) : 1;
-};
-
-// Host-driven launch: leaf count and buffers from the arguments.
-template <typename T, int N, int H, int W, int S>
-__global__ void __launch_bounds__(W * 32, Step2dOcc<T, W>::blocks)
-k_step2d(const T* __restrict__ in, T* __restrict__ out, const amr_halo_meta* __restrict__ meta, int P, Geo g,
-         const Coef* __restrict__ coef, const float2* __restrict__ coef32, int upx0, int upy0, int32_t* err,
-         const uint64_t* __restrict__ keys, const int32_t* __restrict__ upcode)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    T*        tiles;
-    uint64_t* bars;
-    step2d_smem<T, N, H, W, S>(smem, tiles, bars);
-    const int nwarp = (gridDim.x * blockDim.x) >> 5;
-    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_body<T, N, H, S>(in, out, meta, P, g, coef, coef32, upx0, upy0, err, keys, upcode, tiles, bars, p, nwarp);
-}
-
-// Register budget of the multi-step pass: 24 resident warps per SM (the
-// lane's cell block, its strips and the corner stay in registers for the
-// whole pass; two tiles in flight per warp keep the memory system busy).
-template <typename T, int W>
-struct Pass2dOcc {
-    static constexpr int blocks = (24 / W) > 0 ? (24 / W) : 1;
-};
-
-// Host-driven launch of D steps per pass: coefficient rows of step m at
-// coef / coef32 + m * cstride.
-template <typename T, int N, int H, int W, int S, int D>
-__global__ void __launch_bounds__(W * 32, Pass2dOcc<T, W>::blocks)
-k_step2d_pass(const T* __restrict__ in, T* __restrict__ out, const int4* __restrict__ rec, int P, int nl,
-              const Coef* __restrict__ coef, const float2* __restrict__ coef32, size_t cstride, int32_t* err)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    T*        tiles;
-    T*        xy;
-    uint64_t* bars;
-    pass2d_smem<T, N, H, W, S>(smem, tiles, xy, bars);
-    const int nwarp = (gridDim.x * blockDim.x) >> 5;
-    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step2d_pass_body<T, N, H, S, D>(in, out, rec, P, nl, coef, coef32, cstride, err, tiles, xy, bars, p, nwarp);
-}
-
-} // namespace amr_gb300
-
-namespace amr_gb300 {
-
-// ------------------------------------------------ 2D gradient flags, sized at compile time
-// One warp per patch (grid-stride).  The patch's interior rows move into a
-// per-warp shared-memory tile by bulk async copy (double-buffered); the
-// lanes fill all four ghost faces (lanes 0..N-1 the two ghost columns at row
-// tg, lanes N..2N-1 the two ghost rows at column tg) by the halo rules, the
-// values a halo exchange would store; FromBuffer copies the whole padded
-// patch and takes the buffer's ghosts instead.  Each lane then applies the
-// gradient rule (FP32 sum with the proven band, FP64 inside it, the same
-// arithmetic as gradient_sq_cell) to N*N/32 cells and the warp votes.
-template <typename T, int N, int H, bool FromBuffer>
-struct Flags2dShape {
-    static constexpr int      P1    = N + 2 * H;
-    static constexpr int      FLAT  = P1 * P1;
-    static constexpr uint32_t LO    = FromBuffer ? 0u : ((H * P1 * sizeof(T)) & ~15u);
-    static constexpr uint32_t HI    = FromBuffer ? FLAT * sizeof(T) : (((N + H) * P1 * sizeof(T) + 15u) & ~15u);
-    static constexpr uint32_t BYTES = HI - LO;
-    static constexpr int      SEG   = N * N / 32;
-    static constexpr size_t   TILE  = FLAT * sizeof(T);
-    static_assert(TILE % 16 == 0 && HI <= TILE, "patch is not a whole number of 16-byte words");
-    static_assert(32 % N == 0 && (32 / N) * SEG == N, "a lane's cells must form one column segment");
-    static constexpr size_t smem(int W) { return static_cast<size_t>(W) * 2 * (TILE + 8); }
-};
-
-// FP64 squared gradient of a 2D cell from its four neighbour values, in
-// gradient_sq_cell's order (Morton x, then y) and rounding.
-template <typename T>
-__device__ __forceinline__ double grad_sq_exact2(T xl, T xh, T yl, T yh)
-{
-    const double gx = __dmul_rn(0.5, __dsub_rn(static_cast<double>(xh), static_cast<double>(xl)));
-    double       s  = __dadd_rn(0.0, __dmul_rn(gx, gx));
-    const double gy = __dmul_rn(0.5, __dsub_rn(static_cast<double>(yh), static_cast<double>(yl)));
-    return __dadd_rn(s, __dmul_rn(gy, gy));
-}
-
-template <typename T>
-__device__ __forceinline__ float grad_sq_f32_2(T xl, T xh, T yl, T yh)
-{
-    float dx, dy;
-    if constexpr (sizeof(T) == 4) {
-        dx = xh - xl;
-        dy = yh - yl;
-    } else {
-        dx = static_cast<float>(xh - xl);
-        dy = static_cast<float>(yh - yl);
-    }
-    const float gx = 0.5f * dx, gy = 0.5f * dy;
-    return fmaf(gy, gy, fmaf(gx, gx, 0.0f));
-}
-
-template <typename T, int N, int H, bool FromBuffer>
-__device__ __forceinline__ void flags2d_body(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta,
-                                             const uint64_t* __restrict__ keys, int P, const Geo& g,
-                                             const GradRule& rule, int min_level, int max_level,
-                                             const int32_t* __restrict__ bounds, int8_t* __restrict__ flags,
-                                             int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp,
-                                             int32_t* flagged = nullptr)
-{
-    using Sh                = Flags2dShape<T, N, H, FromBuffer>;
-    constexpr int      P1   = Sh::P1;
-    constexpr int      FLAT = Sh::FLAT;
-    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
-    constexpr int      SEG  = Sh::SEG;
-    constexpr int      HALF = N / 2;
-    const int          lane = threadIdx.x & 31;
-    if (lane == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        mbar_init_fence();
-    }
-    __syncwarp();
-    const char* in_bytes = reinterpret_cast<const char*>(in);
-    auto        request  = [&](int q, int slot) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bars[slot], BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
-                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
-    };
-    if (p < P && lane == 0) request(p, 0);
-    uint32_t   phase = 0;
-    // column-segment mapping (conflict-free shared memory, see Step2dShape)
-    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
-    // ghost jobs: lanes 0..N-1 column faces (normal layout dim 1) at row tg,
-    // lanes N..2N-1 row faces (dim 0) at column tg; pos 0 and 1
-    const bool col  = lane < N;
-    const bool job  = !FromBuffer && lane < 2 * N;
-    const int  L    = col ? 1 : 0;
-    const int  tg   = (col ? lane : lane - N) + H;
-    const int  fsel = (tg - H) / HALF;
-    struct Rec {
-        int rel, nb, fid, q0, q1;
-    };
-    auto rec_of = [&](int q, int pos, Rec& m) {
-        m.rel = REL_NONE;
-        if (!job) return;
-        const amr_halo_meta* rp = meta + static_cast<size_t>(q) * 4 + 2 * L + pos;
-        m.rel                   = rp->relation;
-        m.nb                    = rp->neighbor;
-        m.fid                   = rp->finer_ids[fsel];
-        m.q0                    = rp->quadrant[0];
-        m.q1                    = rp->quadrant[1];
-    };
-    // ghost cell (G0, G1) of face pos from record m: the halo rules of
-    // ghost_value, rounded to T
-    auto ghost = [&](int q, int pos, const Rec& m, int& G0, int& G1) -> T {
-        const int gc = pos ? N + H : H - 1;
-        G0           = col ? tg : gc;
-        G1           = col ? gc : tg;
-        const int sh = pos ? -N : N;
-        int       f0 = G0 + (L == 0 ? sh : 0), f1 = G1 + (L == 1 ? sh : 0);
-        if (m.rel == REL_SAME) return in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
-        if (m.rel == REL_COARSER) {
-            f0 = H + m.q0 * HALF + (f0 - H) / 2;
-            f1 = H + m.q1 * HALF + (f1 - H) / 2;
-            return in[static_cast<size_t>(m.nb) * FLAT + f0 * P1 + f1];
-        }
-        if (m.rel == REL_FINER) {
-            f0           = ((f0 - H) * 2) % N + H;
-            f1           = ((f1 - H) * 2) % N + H;
-            const T* fp  = in + static_cast<size_t>(m.fid) * FLAT + f0 * P1 + f1;
-            double   sum = static_cast<double>(fp[0]);
-            sum += static_cast<double>(fp[1]);
-            sum += static_cast<double>(fp[P1]);
-            sum += static_cast<double>(fp[P1 + 1]);
-            return static_cast<T>(sum / 4.0);
-        }
-        return in[static_cast<size_t>(q) * FLAT + G0 * P1 + G1];
-    };
-    Rec mn0{}, mn1{};
-    if (p < P) {
-        rec_of(p, 0, mn0);
-        rec_of(p, 1, mn1);
-    }
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it & 1;
-        const int pn = p + nwarp;
-        if (pn < P && lane == 0) request(pn, b ^ 1);
-        const uint64_t key = keys[p];
-        const Rec      m0 = mn0, m1 = mn1;
-        if (pn < P) {
-            rec_of(pn, 0, mn0);
-            rec_of(pn, 1, mn1);
-        }
-        T   gv0 = T(0), gv1 = T(0);
-        int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-        if (job) {
-            gv0 = ghost(p, 0, m0, a0, a1);
-            gv1 = ghost(p, 1, m1, b0, b1);
-        }
-        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
-            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            phase ^= 1u << b;
-            if (pn < P) mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-            return;
-        }
-        phase ^= 1u << b;
-        T* tile = tiles + static_cast<size_t>(b) * FLAT;
-        if (job) {
-            tile[a0 * P1 + a1] = gv0;
-            tile[b0 * P1 + b1] = gv1;
-        }
-        __syncwarp();
-        // Both decisions depend on the lane's largest squared gradient only
-        // (refine: some cell at or above the threshold; coarsen: every cell
-        // below it), so the FP32 maximum decides them when it lies outside
-        // both bands and every FP32 value is finite; otherwise each cell is
-        // evaluated exactly.  Same outcome as a per-cell decision.
-        int   any = 0, all = 1;
-        T     colv[SEG + 2];
-        float smax = 0.0f;
-        bool  bad  = false;
-#pragma unroll
-        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
-#pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int   idx = (r0 + k) * P1 + cl;
-            const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
-            smax            = fmaxf(smax, s);
-            bad |= !(fabsf(s) < INFINITY);
-        }
-        const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
-                           (smax < rule.c_lo || smax >= rule.c_hi);
-        if (known) {
-            any = smax >= rule.r_hi ? 1 : 0;
-            all = smax < rule.c_lo ? 1 : 0;
-        } else {
-#pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const int    idx = (r0 + k) * P1 + cl;
-                const double s   = grad_sq_exact2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
-                if (s >= rule.rsq) any = 1;
-                if (!(s < rule.csq)) all = 0;
-            }
-        }
-        any = __any_sync(0xffffffffu, any);
-        all = __all_sync(0xffffffffu, all);
-        if (lane == 0) {
-            int lo = min_level, hi = max_level;
-            if (bounds) {
-                const int inst = g.inst_shift >= 64 ? 0 : static_cast<int>(key >> g.inst_shift);
-                lo             = bounds[2 * inst];
-                hi             = bounds[2 * inst + 1];
-            }
-            const int8_t f = gradient_decision(any, all, key_level(key), lo, hi);
-            flags[p]       = f;
-            if (flagged && f != FLAG_STABLE) *flagged = 1; // some leaf will change: the re-mesh runs
-        }
-        __syncwarp();
-    }
-}
-
-// Gradient flags of a tree whose every relation is same-level (the graph
-// intervals that run multi-step passes).  A ghost face is then a copy of the
-// neighbour's edge line, so each lane fetches its two ghost values (lanes
-// 0..N-1 the low and high ghost column at row tg, lanes N..2N-1 the low and
-// high ghost row at column tg) one patch ahead, from the face record (all
-// four neighbours) read two patches ahead; instance and level come from the
-// pass record.  The cells, the gradient arithmetic and the decision are
-// flags2d_body's, so the flags are identical.
-template <typename T, int N, int H>
-__device__ __forceinline__ void flags2d_uniform_body(const T* __restrict__ in, const int4* __restrict__ prec,
-                                                     const int4* __restrict__ frec, int P, const GradRule& rule,
-                                                     int min_level, int max_level, const int32_t* __restrict__ bounds,
-                                                     int8_t* __restrict__ flags, int32_t* err, T* tiles,
-                                                     uint64_t* bars, int p, int nwarp, int32_t* flagged)
-{
-    using Sh                = Flags2dShape<T, N, H, false>;
-    constexpr int      P1   = Sh::P1;
-    constexpr int      FLAT = Sh::FLAT;
-    constexpr uint32_t LO = Sh::LO, BYTES = Sh::BYTES;
-    constexpr int      SEG  = Sh::SEG;
-    const int          lane = threadIdx.x & 31;
-    if (lane == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        mbar_init_fence();
-    }
-    __syncwarp();
-    const char* in_bytes = reinterpret_cast<const char*>(in);
-    auto        request  = [&](int q, int slot) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bars[slot], BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + LO,
-                      in_bytes + static_cast<size_t>(q) * FLAT * sizeof(T) + LO, BYTES, &bars[slot]);
-    };
-    if (p < P && lane == 0) request(p, 0);
-    uint32_t   phase = 0;
-    const int  cl = lane % N + H, r0 = (lane / N) * SEG + H;
-    const bool col = lane < N;
-    const bool job = lane < 2 * N;
-    const int  tg  = (col ? lane : lane - N) + H;
-    // the lane's ghost cells in the tile and their sources in the low / high
-    // neighbour (the neighbour's last / first interior line)
-    const int  g0 = col ? tg * P1 + (H - 1) : (H - 1) * P1 + tg;
-    const int  g1 = col ? tg * P1 + (N + H) : (N + H) * P1 + tg;
-    const int  s0 = col ? tg * P1 + (N + H - 1) : (N + H - 1) * P1 + tg;
-    const int  s1 = col ? tg * P1 + H : H * P1 + tg;
-    auto       fetch = [&](const int4& f, T& a, T& b) {
-        a = b = T(0);
-        if (!job) return;
-        a = in[static_cast<size_t>(col ? f.x : f.z) * FLAT + s0];
-        b = in[static_cast<size_t>(col ? f.y : f.w) * FLAT + s1];
-    };
-    // face records two patches ahead, ghost values one ahead
-    int4 f0{}, f1{}, f2{};
-    int  c0 = 0, c1 = 0, c2 = 0;
-    T    ga = T(0), gb = T(0), na = T(0), nb = T(0);
-    if (p < P) {
-        f0 = __ldg(frec + p);
-        c0 = __ldg(&prec[p].w);
-        fetch(f0, ga, gb);
-    }
-    if (p + nwarp < P) {
-        f1 = __ldg(frec + p + nwarp);
-        c1 = __ldg(&prec[p + nwarp].w);
-    }
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it & 1;
-        const int pn = p + nwarp, pm = p + 2 * nwarp;
-        if (pn < P && lane == 0) request(pn, b ^ 1);
-        if (pm < P) {
-            f2 = __ldg(frec + pm);
-            c2 = __ldg(&prec[pm].w);
-        }
-        if (pn < P) fetch(f1, na, nb);
-        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
-            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            phase ^= 1u << b;
-            if (pn < P) mbar_wait_bounded(&bars[b ^ 1], (phase >> (b ^ 1)) & 1u);
-            return;
-        }
-        phase ^= 1u << b;
-        T* tile = tiles + static_cast<size_t>(b) * FLAT;
-        if (job) {
-            tile[g0] = ga;
-            tile[g1] = gb;
-        }
-        __syncwarp();
-        // the decision rule of flags2d_body: the lane's FP32 maximum decides
-        // unless it lies in a band or some value is not finite
-        int   any = 0, all = 1;
-        T     colv[SEG + 2];
-        float smax = 0.0f;
-        bool  bad  = false;
-#pragma unroll
-        for (int k = 0; k < SEG + 2; ++k) colv[k] = tile[(r0 - 1 + k) * P1 + cl];
-#pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int   idx = (r0 + k) * P1 + cl;
-            const float s   = grad_sq_f32_2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
-            smax            = fmaxf(smax, s);
-            bad |= !(fabsf(s) < INFINITY);
-        }
-        const bool known = rule.fast && !bad && (smax >= rule.r_hi || smax < rule.r_lo) &&
-                           (smax < rule.c_lo || smax >= rule.c_hi);
-        if (known) {
-            any = smax >= rule.r_hi ? 1 : 0;
-            all = smax < rule.c_lo ? 1 : 0;
-        } else {
-#pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const int    idx = (r0 + k) * P1 + cl;
-                const double s   = grad_sq_exact2<T>(tile[idx - 1], tile[idx + 1], colv[k], colv[k + 2]);
-                if (s >= rule.rsq) any = 1;
-                if (!(s < rule.csq)) all = 0;
-            }
-        }
-        any = __any_sync(0xffffffffu, any);
-        all = __all_sync(0xffffffffu, all);
-        if (lane == 0) {
-            int lo = min_level, hi = max_level;
-            if (bounds) {
-                const int inst = pass_inst(c0);
-                lo             = bounds[2 * inst];
-                hi             = bounds[2 * inst + 1];
-            }
-            const int8_t f = gradient_decision(any, all, pass_level(c0), lo, hi);
-            flags[p]       = f;
-            if (f != FLAG_STABLE) *flagged = 1; // some leaf will change: the re-mesh runs
-        }
-        __syncwarp();
-        f0 = f1;
-        f1 = f2;
-        c0 = c1;
-        c1 = c2;
-        ga = na;
-        gb = nb;
-    }
-}
-
-template <typename T, int N, int H, bool FromBuffer>
-__device__ __forceinline__ void flags2d_smem(unsigned char* smem, int W, T*& tiles, uint64_t*& bars)
-{
-    using Sh      = Flags2dShape<T, N, H, FromBuffer>;
-    const int wib = threadIdx.x >> 5;
-    tiles         = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * 2 * Sh::FLAT;
-    bars          = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * 2 * Sh::TILE) + wib * 2;
-}
-
-template <typename T, int N, int H, bool FromBuffer>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3)
-k_flags2d(const T* __restrict__ in, const amr_halo_meta* __restrict__ meta, const uint64_t* __restrict__ keys, int P,
-          Geo g, GradRule rule, int min_level, int max_level, const int32_t* __restrict__ bounds,
-          int8_t* __restrict__ flags, int32_t* err)
-{
-    extern __shared__ __align__(128) unsigned char smem[];
-    T*        tiles;
-    uint64_t* bars;
-    flags2d_smem<T, N, H, FromBuffer>(smem, blockDim.x >> 5, tiles, bars);
-    const int nwarp = (gridDim.x * blockDim.x) >> 5;
-    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    flags2d_body<T, N, H, FromBuffer>(in, meta, keys, P, g, rule, min_level, max_level, bounds, flags, err, tiles, bars,
-                                      p, nwarp);
-}
-
-} // namespace amr_gb300
-
-namespace amr_gb300 {
-
-// ------------------------------------------------------------- adjoint
-// Transpose of one fused step (step_cell with ghosts on the fly) on a frozen
-// mesh, gathered per interior cell j of patch p: lout_j = c0 lin_j plus, for
-// every axis a with upwind offset up_a, the cells whose update reads j:
-//   * the downwind cell j - up_a inside p (weight c_a of p's level);
-//   * on the downwind face (relation from p's own neighbour record):
-//       same    -> the adjacent cell of the neighbour (its c_a),
-//       finer   -> the 2^(rank-1) fine cells whose coarse ghost injects j
-//                  (ghost_value's coarser rule inverted, each with c_a of
-//                  the fine level),
-//   * in the two layers next to the downwind face, when that neighbour is
-//     coarser: the coarse cell whose ghost is the mean of the 2^rank fine
-//     cells containing j (weight c_a(coarse) / 2^rank).
-// FP32 uses the difference form of the forward (u + c (u_up - u)), whose
-// transpose is lin_j + sum_a (contributions - c_a(p) lin_j).  Ghost cells of
-// lout are not written (the caller keeps them zero).
-template <typename T>
-__device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* meta, const uint64_t* keys,
-                                    const Geo& g, const Coef* coef, const int* up_launch, const double* vel, int p,
-                                    int c)
-{
-    constexpr bool F32 = sizeof(T) == 4;
-    int            idx[3];
-    interior_coords(g, c, idx);
-    const int      nl   = g.depth + 1;
-    const uint64_t kp   = keys[p];
-    const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(kp >> g.inst_shift);
-    int            up[3] = { up_launch[0], up_launch[1], up_launch[2] };
-    if (vel)
-        for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(vel[3 * inst + a]) : 0;
-    const Coef   cp   = coef[inst * nl + key_level(kp)];
-    const size_t base = static_cast<size_t>(p) * g.flat;
-    const int    li   = padded_index(g, idx);
-    const T      lj   = lin[base + li];
-    T            acc  = F32 ? lj : static_cast<T>(cp.c0) * lj;
-    const int    half = g.n / 2;
-    for (int a = 0; a < g.rank; ++a) {
-        if (up[a] == 0) continue;
-        const int L = g.rank - 1 - a, d = -up[a], pos_d = d > 0 ? 1 : 0;
-        const int dist = pos_d ? (g.n + g.h - 1 - idx[L]) : (idx[L] - g.h); // cells to the downwind face
-        const T   ca   = static_cast<T>(cp.c[a]);
-        if (dist > 0) {
-            const T ld = lin[base + li + d * g.s[L]];
-            acc        = F32 ? fma(ca, static_cast<T>(ld - lj), acc) : fma(ca, ld, acc);
-        } else if (F32) {
-            acc = fma(-ca, lj, acc);
-        }
-        if (dist > 1) continue;
-        const amr_halo_meta& m = meta[static_cast<size_t>(p) * g.ndir + 2 * L + pos_d];
-        const int            face = pos_d ? g.h : g.n + g.h - 1; // the neighbour's layer next to the face
-        if (m.relation == REL_COARSER) {
-            int ci[3] = { idx[0], idx[1], idx[2] };
-            for (int k = 0; k < g.rank; ++k)
-                if (k != L) ci[k] = g.h + m.quadrant[k] * half + (idx[k] - g.h) / 2;
-            ci[L]           = face;
-            const Coef cq   = coef[inst * nl + key_level(keys[m.neighbor])];
-            const T    w    = static_cast<T>(static_cast<T>(cq.c[a]) / static_cast<T>(1 << g.rank));
-            acc             = fma(w, lin[static_cast<size_t>(m.neighbor) * g.flat + padded_index(g, ci)], acc);
-        } else if (dist == 0 && m.relation == REL_SAME) {
-            int ci[3] = { idx[0], idx[1], idx[2] };
-            ci[L]     = face;
-            acc = fma(ca, lin[static_cast<size_t>(m.neighbor) * g.flat + padded_index(g, ci)], acc);
-        } else if (dist == 0 && m.relation == REL_FINER) {
-            // section of j across the tangential dims (dim 0 fastest)
-            int fpi = 0, st = 1, sec[3] = { 0, 0, 0 };
-            for (int k = 0; k < g.rank; ++k) {
-                if (k == L) continue;
-                sec[k] = (idx[k] - g.h) / half;
-                fpi += sec[k] * st;
-                st *= 2;
-            }
-            const int   f   = fpi == 0 ? m.finer_ids[0] : fpi == 1 ? m.finer_ids[1] : fpi == 2 ? m.finer_ids[2] : m.finer_ids[3];
-            const Coef  cf  = coef[inst * nl + key_level(keys[f])];
-            const T*    fp  = lin + static_cast<size_t>(f) * g.flat;
-            int         fi[3];
-            fi[L]           = face;
-            int t0 = -1, t1 = -1; // tangential dims
-            for (int k = 0; k < g.rank; ++k)
-                if (k != L) {
-                    fi[k] = g.h + 2 * ((idx[k] - g.h) - sec[k] * half);
-                    if (t0 < 0) t0 = k;
-                    else t1 = k;
-                }
-            if (g.rank == 2) {
-                fi[2] = 0;
-                T s   = fp[padded_index(g, fi)];
-                fi[t0] += 1;
-                s += fp[padded_index(g, fi)];
-                acc = fma(static_cast<T>(cf.c[a]), s, acc);
-            } else {
-                T s = T(0);
-                for (int b0 = 0; b0 < 2; ++b0)
-                    for (int b1 = 0; b1 < 2; ++b1) {
-                        int q[3] = { fi[0], fi[1], fi[2] };
-                        q[t0] += b0;
-                        q[t1] += b1;
-                        s += fp[padded_index(g, q)];
-                    }
-                acc = fma(static_cast<T>(cf.c[a]), s, acc);
-            }
-        }
-    }
-    lout[base + li] = acc;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_adjoint(const T* __restrict__ lin, T* __restrict__ lout, const amr_halo_meta* __restrict__ meta,
-          const uint64_t* __restrict__ keys, int P, Geo g, const Coef* __restrict__ coef, int up0, int up1, int up2,
-          const double* __restrict__ vel, int ppb)
-{
-    const int up[3] = { up0, up1, up2 };
-    const int p0    = blockIdx.x * ppb;
-    for (int t = threadIdx.x; t < ppb * g.cells; t += blockDim.x) {
-        const int p = p0 + t / g.cells;
-        if (p >= P) break;
-        adjoint_cell<T>(lin, lout, meta, keys, g, coef, up, vel, p, t - (p - p0) * g.cells);
-    }
-}
-
-// Ghost cells of every patch set to zero (interior untouched).
-template <typename T>
-__global__ void k_zero_ghosts(T* __restrict__ buf, long long total, Geo g)
-{
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        long long r      = i % g.flat;
-        bool      inside = true;
-        for (int k = g.rank - 1; k >= 0; --k) {
-            const int c = static_cast<int>(r % g.P1);
-            r /= g.P1;
-            inside = inside && c >= g.h && c < g.n + g.h;
-        }
-        if (!inside) buf[i] = T(0);
-    }
-}
-
-// Coefficient rows (step s, instance i) of `steps` steps from recorded step
-// sizes dts[s * ninst + i] (the fill of k_batch_begin, without the clamp).
-static __global__ void k_coef_from_dt(const double* __restrict__ dts, Geo g, const double* __restrict__ vel, int steps,
-                               int ninst, Coef* __restrict__ coef)
-{
-    const int nl    = g.depth + 1;
-    const int total = steps * ninst * nl;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        const int    l = e % nl, si = e / nl, inst = si % ninst;
-        const double v[3] = { vel[3 * inst], vel[3 * inst + 1], vel[3 * inst + 2] };
-        coef[e]           = make_coef(g, dts[si], v, l);
-    }
-}
-
-} // namespace amr_gb300
-
-namespace amr_gb300 {
-
-// ------------------------------------------------ 3D update, staged
-// One step of 3D patches of N^3 cells and one ghost layer, one warp per
-// patch (grid-stride).  The patch's interior planes (ghost rows and columns
-// included, a contiguous 16-byte-aligned span) move into a per-warp
-// shared-memory tile by bulk async copy; each warp owns S tiles in a ring
-// and keeps S-1 copies in flight ahead of the patch it works on.  While the
-// copy lands the lanes evaluate the upwind ghost faces by the halo rules
-// (ghost_value, the values step_cell takes on the fly), then write them into
-// the tile, update N^3/32 cells each from the tile with step_cell's
-// arithmetic, and store the interior planes back as 16-byte words (ghost
-// rows and columns pass through, as in the 2D kernels).  A copy that does
-// not land within the wait cap sets *err = AMR_ERR_TIMEOUT; the warp then
-// drains its other copies (also capped) and stops.
-template <typename T, int N>
-struct Step3dShape {
-    static constexpr int      P1 = N + 2, PLANE = P1 * P1, FLAT = PLANE * P1;
-    static constexpr uint32_t LO    = PLANE * sizeof(T);           // byte span of the interior planes
-    static constexpr uint32_t BYTES = N * PLANE * sizeof(T);
-    static constexpr int      WORDS = BYTES / 16;
-    static constexpr int      PER   = N * N * N / 32;              // cells per lane
-    static constexpr int      GPL   = (N * N + 31) / 32;           // ghost cells per lane and face
-    static constexpr size_t   TILE  = FLAT * sizeof(T);
-    static_assert(LO % 16 == 0 && BYTES % 16 == 0 && TILE % 16 == 0, "planes are whole 16-byte words");
-    static_assert(N * N * N % 32 == 0, "a warp's lanes share the cells evenly");
-    static constexpr size_t smem(int W, int S) { return static_cast<size_t>(W) * S * (TILE + 8); }
-};
-
-template <typename T, int N, int S>
-__device__ __forceinline__ void step3d_body(const T* __restrict__ in, T* __restrict__ out,
-                                            const amr_halo_meta* __restrict__ meta, const int32_t* __restrict__ levels,
-                                            const uint64_t* __restrict__ keys, int P, const Geo& g,
-                                            const Coef* __restrict__ coef, const float4* __restrict__ coef4,
-                                            int up0, int up1, int up2, const int32_t* __restrict__ upcode,
-                                            int32_t* err, T* tiles, uint64_t* bars, int p, int nwarp)
-{
-    using Sh               = Step3dShape<T, N>;
-    constexpr int P1       = Sh::P1, PLANE = Sh::PLANE, FLAT = Sh::FLAT, GPL = Sh::GPL;
-    const int     lane     = threadIdx.x & 31;
-    const int     nl       = g.depth + 1;
-    if (lane == 0) {
-        for (int b = 0; b < S; ++b) mbar_init(&bars[b], 1);
-        mbar_init_fence();
-    }
-    __syncwarp();
-    const char* in_bytes = reinterpret_cast<const char*>(in);
-    auto        request  = [&](int q, int slot) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&bars[slot], Sh::BYTES);
-        bulk_copy_g2s(reinterpret_cast<char*>(tiles + static_cast<size_t>(slot) * FLAT) + Sh::LO,
-                      in_bytes + static_cast<size_t>(q) * Sh::TILE + Sh::LO, Sh::BYTES, &bars[slot]);
-    };
-    if (lane == 0)
-        for (int j = 0; j < S - 1; ++j)
-            if (p + j * nwarp < P) request(p + j * nwarp, j);
-    uint32_t phase = 0; // bit b: parity of slot b's next completion
-    for (int it = 0; p < P; ++it, p += nwarp) {
-        const int b  = it % S;
-        const int pf = p + (S - 1) * nwarp;
-        if (pf < P && lane == 0) request(pf, (it + S - 1) % S);
-        const int inst  = keys ? instance_of(g, keys, p) : 0;
-        int       up[3] = { up0, up1, up2 };
-        if (upcode) { // per-instance upwind sides, packed (integer decode: no FP64 compares)
-            const int32_t code = upcode[inst];
-            for (int a = 0; a < 3; ++a) up[a] = unpack_upwind(code, a);
-        }
-        // the row of the leaf's level: FP64 from coef, FP32 from the rows
-        // rounded once (coef4)
-        const int row = inst * nl + levels[p];
-        T         c0, ca[3];
-        if constexpr (sizeof(T) == 4) {
-            const float4 c4 = coef4[row];
-            c0              = c4.w;
-            ca[0]           = c4.x;
-            ca[1]           = c4.y;
-            ca[2]           = c4.z;
-        } else {
-            const Coef cf = coef[row];
-            c0            = cf.c0;
-            ca[0]         = cf.c[0];
-            ca[1]         = cf.c[1];
-            ca[2]         = cf.c[2];
-        }
-        const T* src = in + static_cast<size_t>(p) * FLAT;
-        // the upwind ghost faces (Morton axis a is layout dim 2 - a): ghost
-        // cell k of a face has tangential coordinates (k / N + 1, k % N + 1)
-        T gv[3][GPL];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int L = 2 - a, pos = up[a] > 0 ? 1 : 0;
-#pragma unroll
-            for (int j = 0; j < GPL; ++j) {
-                const int k = lane + 32 * j;
-                gv[a][j]    = T(0);
-                if (up[a] != 0 && k < N * N) {
-                    int G[3];
-                    G[L]              = pos ? N + 1 : 0;
-                    G[L == 0 ? 1 : 0] = k / N + 1;
-                    G[L == 2 ? 1 : 2] = k % N + 1;
-                    gv[a][j] =
-                        ghost_value<T, T>(in, FLAT, meta[static_cast<size_t>(p) * 6 + 2 * L + pos], G, L, pos, g, src);
-                }
-            }
-        }
-        if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1u)) {
-            if (lane == 0) atomicExch(err, static_cast<int32_t>(AMR_ERR_TIMEOUT));
-            phase ^= 1u << b;
-            for (int j = 1; j < S; ++j) // drain the copies still in flight
-                if (p + j * nwarp < P) {
-                    const int sl = (it + j) % S;
-                    mbar_wait_bounded(&bars[sl], (phase >> sl) & 1u);
-                    phase ^= 1u << sl;
-                }
-            return;
-        }
-        phase ^= 1u << b;
-        T* tile = tiles + static_cast<size_t>(b) * FLAT;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int L = 2 - a;
-#pragma unroll
-            for (int j = 0; j < GPL; ++j) {
-                const int k = lane + 32 * j;
-                if (up[a] != 0 && k < N * N) {
-                    int G[3];
-                    G[L]              = up[a] > 0 ? N + 1 : 0;
-                    G[L == 0 ? 1 : 0] = k / N + 1;
-                    G[L == 2 ? 1 : 2] = k % N + 1;
-                    tile[(G[0] * P1 + G[1]) * P1 + G[2]] = gv[a][j];
-                }
-            }
-        }
-        __syncwarp();
-        T res[Sh::PER];
-#pragma unroll
-        for (int q = 0; q < Sh::PER; ++q) {
-            const int c   = lane + 32 * q;
-            const int li  = ((c / (N * N) + 1) * P1 + (c / N) % N + 1) * P1 + c % N + 1;
-            const T   u   = tile[li];
-            T         acc = sizeof(T) == 4 ? u : c0 * u;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if (up[a] == 0) continue;
-                const int st  = a == 0 ? 1 : (a == 1 ? P1 : PLANE);
-                const T   val = tile[li + up[a] * st];
-                acc = fma(ca[a], sizeof(T) == 4 ? static_cast<T>(val - u) : val, acc);
-            }
-            res[q] = acc;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < Sh::PER; ++q) {
-            const int c                                                          = lane + 32 * q;
-            tile[((c / (N * N) + 1) * P1 + (c / N) % N + 1) * P1 + c % N + 1] = res[q];
-        }
-        __syncwarp();
-        const uint4* t4  = reinterpret_cast<const uint4*>(reinterpret_cast<const char*>(tile) + Sh::LO);
-        uint4*       dst = reinterpret_cast<uint4*>(reinterpret_cast<char*>(out + static_cast<size_t>(p) * FLAT) + Sh::LO);
-        for (int w = lane; w < Sh::WORDS; w += 32) dst[w] = t4[w];
-        __syncwarp(); // the slot is refilled by a later copy
-    }
-}
-
-// Tiles and barriers of warp wib in a block of W warps with S slots each.
-template <typename T, int N, int W, int S>
-__device__ __forceinline__ void step3d_smem(unsigned char* smem, T*& tiles, uint64_t*& bars)
-{
-    const int wib = threadIdx.x >> 5;
-    tiles         = reinterpret_cast<T*>(smem) + static_cast<size_t>(wib) * S * Step3dShape<T, N>::FLAT;
-    bars          = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(W) * S * Step3dShape<T, N>::TILE) + wib * S;
-}
-
-// Host-driven launch: W warps per block, one per patch.
-template <typename T, int N, int W, int S>
-__global__ void __launch_bounds__(W * 32)
-k_step3d(const T* __restrict__ in, T* __restrict__ out, const int32_t* __restrict__ levels,
-         const amr_halo_meta* __restrict__ meta, int P, Geo g, const Coef* __restrict__ coef,
-         const float4* __restrict__ coef4, int up0, int up1, int up2, const uint64_t* __restrict__ keys,
-         const int32_t* __restrict__ upcode, int32_t* err)
-{
-    extern __shared__ __align__(128) unsigned char smem3d[];
-    T*        tiles;
-    uint64_t* bars;
-    step3d_smem<T, N, W, S>(smem3d, tiles, bars);
-    const int nwarp = (gridDim.x * blockDim.x) >> 5;
-    const int p     = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    step3d_body<T, N, S>(in, out, meta, levels, keys, P, g, coef, coef4, up0, up1, up2, upcode, err, tiles, bars, p,
-                         nwarp);
 }
 
 } // namespace amr_gb300
