@@ -415,25 +415,33 @@ static __global__ void k_run_emit(RunBufs B, RunCtl* ctl, Geo g)
     emit_leaf(B.keys[tb], B.rmark, B.chead, B.pos, g, B.keys[nb], B.levels[nb], B.src, B.skind, B.maxlev_new, i);
 }
 
-// One block per new leaf, grid-stride (k_remap's work).
+// The new state (k_remap's work), one unit per 16-byte word of each new
+// leaf, grid-stride over all of them: a kept leaf moves word by word (ghosts
+// included), a refined or coarsened leaf is built cell by cell, each unit
+// taking the same share of its cells.  Every thread has independent loads in
+// flight, instead of one block stepping through the leaves one at a time.
 template <typename T>
 __global__ void __launch_bounds__(256) k_run_remap(RunBufs B, RunCtl* ctl, Geo g, int sp)
 {
     if (ctl->err || !ctl->changed) return;
-    const int NP = ctl->NP;
-    const T*  old_state = static_cast<const T*>(B.state[ctl->sb ^ sp]);
-    T*        new_state = static_cast<T*>(B.state[ctl->sb ^ sp ^ 1]);
-    for (int j = blockIdx.x; j < NP; j += gridDim.x) {
+    const int       NP        = ctl->NP;
+    const T*        old_state = static_cast<const T*>(B.state[ctl->sb ^ sp]);
+    T*              new_state = static_cast<T*>(B.state[ctl->sb ^ sp ^ 1]);
+    const int       words     = g.flat * static_cast<int>(sizeof(T)) / 16; // padded sides are even
+    const int       per       = (g.cells + words - 1) / words;
+    const long long total     = static_cast<long long>(NP) * words;
+    for (long long u = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; u < total;
+         u += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int j    = static_cast<int>(u / words);
+        const int w    = static_cast<int>(u - static_cast<long long>(j) * words);
         const int kind = B.skind[j];
         if (kind == 0) {
-            const size_t bytes = static_cast<size_t>(g.flat) * sizeof(T);
-            const uint4* f4    = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(B.src[j]) * g.flat);
-            uint4*       t4    = reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat);
-            for (size_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) t4[w] = f4[w];
-            continue;
+            const uint4* f4 = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(B.src[j]) * g.flat);
+            reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat)[w] = f4[w];
+        } else {
+            const int c1 = min(g.cells, (w + 1) * per);
+            for (int c = w * per; c < c1; ++c) remap_cell<T>(old_state, new_state, g, kind, B.src[j], j, c);
         }
-        for (int c = threadIdx.x; c < g.cells; c += blockDim.x)
-            remap_cell<T>(old_state, new_state, g, kind, B.src[j], j, c);
     }
 }
 
