@@ -751,9 +751,11 @@ __device__ inline void remap_cell(const T* old_state, T* new_state, const Geo& g
     }
 }
 
-// One block per new leaf; kept patches move whole (16-byte words, ghosts
-// included), new ones are built cell by cell.  blockIdx.y = field of a
-// multi-field state (fields fstride elements apart).
+// The new state, one unit per 16-byte word of each new leaf (grid-stride,
+// any grid): a kept leaf moves word by word (ghosts included), a refined or
+// coarsened leaf is built cell by cell, each unit taking the same share of
+// its cells.  blockIdx.y = field of a multi-field state (fields fstride
+// elements apart).
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_t* __restrict__ src,
@@ -761,17 +763,22 @@ k_remap(const T* __restrict__ old_state, T* __restrict__ new_state, const int32_
 {
     old_state += blockIdx.y * fstride;
     new_state += blockIdx.y * fstride;
-    const int j = blockIdx.x;
-    if (j >= P) return;
-    const int kind = skind[j];
-    if (kind == 0) {
-        const size_t bytes = static_cast<size_t>(g.flat) * sizeof(T);
-        const uint4* f4    = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(src[j]) * g.flat);
-        uint4*       t4    = reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat);
-        for (size_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) t4[w] = f4[w];
-        return;
+    const int       words = g.flat * static_cast<int>(sizeof(T)) / 16; // padded sides are even
+    const int       per   = (g.cells + words - 1) / words;
+    const long long total = static_cast<long long>(P) * words;
+    for (long long u = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; u < total;
+         u += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int j    = static_cast<int>(u / words);
+        const int w    = static_cast<int>(u - static_cast<long long>(j) * words);
+        const int kind = skind[j];
+        if (kind == 0) {
+            const uint4* f4 = reinterpret_cast<const uint4*>(old_state + static_cast<size_t>(src[j]) * g.flat);
+            reinterpret_cast<uint4*>(new_state + static_cast<size_t>(j) * g.flat)[w] = f4[w];
+        } else {
+            const int c1 = min(g.cells, (w + 1) * per);
+            for (int c = w * per; c < c1; ++c) remap_cell<T>(old_state, new_state, g, kind, src[j], j, c);
+        }
     }
-    for (int c = threadIdx.x; c < g.cells; c += blockDim.x) remap_cell<T>(old_state, new_state, g, kind, src[j], j, c);
 }
 
 // flag = 1 when some neighbour record is not "same level" (flag zeroed first).

@@ -1798,8 +1798,11 @@ amr_status amr_tree_remesh(amr_tree* t, int* changed)
                 return AMR_OK;
             }
         }
-        k_remap<T><<<dim3(NP, t->nvar), 256, 0, s>>>(static_cast<const T*>(t->cur), static_cast<T*>(t->nxt), t->src,
-                                                     t->skind, NP, g, t->fstride());
+        const long long units = static_cast<long long>(NP) * (g.flat * static_cast<long long>(sizeof(T)) / 16);
+        const unsigned  rgrid = static_cast<unsigned>(std::min<long long>((units + 255) / 256, 16LL * num_sms()));
+        k_remap<T><<<dim3(std::max(1u, rgrid), t->nvar), 256, 0, s>>>(static_cast<const T*>(t->cur),
+                                                                      static_cast<T*>(t->nxt), t->src, t->skind, NP,
+                                                                      g, t->fstride());
         AMR_LAUNCHED("k_remap");
         return AMR_OK;
     });
