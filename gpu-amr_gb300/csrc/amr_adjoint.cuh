@@ -20,12 +20,31 @@ namespace amr_gb300 {
 //     coarser: the coarse cell whose ghost is the mean of the 2^rank fine
 //     cells containing j (weight c_a(coarse) / 2^rank).
 // FP32 uses the difference form of the forward (u + c (u_up - u)), whose
-// transpose is lin_j + sum_a (contributions - c_a(p) lin_j).  Ghost cells of
-// lout are not written (the caller keeps them zero).
+// transpose is lin_j + sum_a (contributions - c_a(p) lin_j), with the
+// coefficient rows rounded to FP32 once (coef32: (c_x, c_y) float2 entries
+// for 2D trees, (c_x, c_y, c_z, c0) float4 entries for 3D trees, the values
+// the FP64 rows round to).  Upwind sides per instance come from the packed
+// integer codes (upcode), or from the launch.  Ghost cells of lout are not
+// written (the caller keeps them zero).
+template <typename T>
+__device__ __forceinline__ T adjoint_coef(const Coef* coef, const float2* coef32, const Geo& g, int row, int a)
+{
+    if constexpr (sizeof(T) == 4) {
+        if (g.rank == 3) {
+            const float4 c = reinterpret_cast<const float4*>(coef32)[row];
+            return a == 0 ? c.x : (a == 1 ? c.y : c.z);
+        }
+        const float2 c = coef32[row];
+        return a == 0 ? c.x : c.y;
+    } else {
+        return coef[row].c[a];
+    }
+}
+
 template <typename T>
 __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* meta, const uint64_t* keys,
-                                    const Geo& g, const Coef* coef, const int* up_launch, const double* vel, int p,
-                                    int c)
+                                    const Geo& g, const Coef* coef, const float2* coef32, const int* up_launch,
+                                    const int32_t* upcode, int p, int c)
 {
     constexpr bool F32 = sizeof(T) == 4;
     int            idx[3];
@@ -34,19 +53,22 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
     const uint64_t kp   = keys[p];
     const int      inst = g.inst_shift >= 64 ? 0 : static_cast<int>(kp >> g.inst_shift);
     int            up[3] = { up_launch[0], up_launch[1], up_launch[2] };
-    if (vel)
-        for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? upwind(vel[3 * inst + a]) : 0;
-    const Coef   cp   = coef[inst * nl + key_level(kp)];
+    if (upcode) {
+        const int32_t code = upcode[inst];
+        for (int a = 0; a < 3; ++a) up[a] = a < g.rank ? unpack_upwind(code, a) : 0;
+    }
+    const int    rowp = inst * nl + key_level(kp);
     const size_t base = static_cast<size_t>(p) * g.flat;
     const int    li   = padded_index(g, idx);
     const T      lj   = lin[base + li];
-    T            acc  = F32 ? lj : static_cast<T>(cp.c0) * lj;
+    T            acc  = lj;
+    if constexpr (!F32) acc = coef[rowp].c0 * lj;
     const int    half = g.n / 2;
     for (int a = 0; a < g.rank; ++a) {
         if (up[a] == 0) continue;
         const int L = g.rank - 1 - a, d = -up[a], pos_d = d > 0 ? 1 : 0;
         const int dist = pos_d ? (g.n + g.h - 1 - idx[L]) : (idx[L] - g.h); // cells to the downwind face
-        const T   ca   = static_cast<T>(cp.c[a]);
+        const T   ca   = adjoint_coef<T>(coef, coef32, g, rowp, a);
         if (dist > 0) {
             const T ld = lin[base + li + d * g.s[L]];
             acc        = F32 ? fma(ca, static_cast<T>(ld - lj), acc) : fma(ca, ld, acc);
@@ -61,8 +83,8 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
             for (int k = 0; k < g.rank; ++k)
                 if (k != L) ci[k] = g.h + m.quadrant[k] * half + (idx[k] - g.h) / 2;
             ci[L]           = face;
-            const Coef cq   = coef[inst * nl + key_level(keys[m.neighbor])];
-            const T    w    = static_cast<T>(static_cast<T>(cq.c[a]) / static_cast<T>(1 << g.rank));
+            const T    cq   = adjoint_coef<T>(coef, coef32, g, inst * nl + key_level(keys[m.neighbor]), a);
+            const T    w    = static_cast<T>(cq / static_cast<T>(1 << g.rank));
             acc             = fma(w, lin[static_cast<size_t>(m.neighbor) * g.flat + padded_index(g, ci)], acc);
         } else if (dist == 0 && m.relation == REL_SAME) {
             int ci[3] = { idx[0], idx[1], idx[2] };
@@ -78,7 +100,7 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
                 st *= 2;
             }
             const int   f   = fpi == 0 ? m.finer_ids[0] : fpi == 1 ? m.finer_ids[1] : fpi == 2 ? m.finer_ids[2] : m.finer_ids[3];
-            const Coef  cf  = coef[inst * nl + key_level(keys[f])];
+            const T     cfa = adjoint_coef<T>(coef, coef32, g, inst * nl + key_level(keys[f]), a);
             const T*    fp  = lin + static_cast<size_t>(f) * g.flat;
             int         fi[3];
             fi[L]           = face;
@@ -94,7 +116,7 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
                 T s   = fp[padded_index(g, fi)];
                 fi[t0] += 1;
                 s += fp[padded_index(g, fi)];
-                acc = fma(static_cast<T>(cf.c[a]), s, acc);
+                acc = fma(cfa, s, acc);
             } else {
                 T s = T(0);
                 for (int b0 = 0; b0 < 2; ++b0)
@@ -104,7 +126,7 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
                         q[t1] += b1;
                         s += fp[padded_index(g, q)];
                     }
-                acc = fma(static_cast<T>(cf.c[a]), s, acc);
+                acc = fma(cfa, s, acc);
             }
         }
     }
@@ -114,15 +136,15 @@ __device__ inline void adjoint_cell(const T* lin, T* lout, const amr_halo_meta* 
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_adjoint(const T* __restrict__ lin, T* __restrict__ lout, const amr_halo_meta* __restrict__ meta,
-          const uint64_t* __restrict__ keys, int P, Geo g, const Coef* __restrict__ coef, int up0, int up1, int up2,
-          const double* __restrict__ vel, int ppb)
+          const uint64_t* __restrict__ keys, int P, Geo g, const Coef* __restrict__ coef,
+          const float2* __restrict__ coef32, int up0, int up1, int up2, const int32_t* __restrict__ upcode, int ppb)
 {
     const int up[3] = { up0, up1, up2 };
     const int p0    = blockIdx.x * ppb;
     for (int t = threadIdx.x; t < ppb * g.cells; t += blockDim.x) {
         const int p = p0 + t / g.cells;
         if (p >= P) break;
-        adjoint_cell<T>(lin, lout, meta, keys, g, coef, up, vel, p, t - (p - p0) * g.cells);
+        adjoint_cell<T>(lin, lout, meta, keys, g, coef, coef32, up, upcode, p, t - (p - p0) * g.cells);
     }
 }
 
@@ -146,14 +168,20 @@ __global__ void k_zero_ghosts(T* __restrict__ buf, long long total, Geo g)
 // Coefficient rows (step s, instance i) of `steps` steps from recorded step
 // sizes dts[s * ninst + i] (the fill of k_batch_begin, without the clamp).
 static __global__ void k_coef_from_dt(const double* __restrict__ dts, Geo g, const double* __restrict__ vel, int steps,
-                               int ninst, Coef* __restrict__ coef)
+                               int ninst, Coef* __restrict__ coef, float2* __restrict__ coef32)
 {
     const int nl    = g.depth + 1;
     const int total = steps * ninst * nl;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         const int    l = e % nl, si = e / nl, inst = si % ninst;
         const double v[3] = { vel[3 * inst], vel[3 * inst + 1], vel[3 * inst + 2] };
-        coef[e]           = make_coef(g, dts[si], v, l);
+        const Coef   c    = make_coef(g, dts[si], v, l);
+        coef[e]           = c;
+        if (g.rank == 3) // the FP32 rows, laid out as k_batch_begin writes them
+            reinterpret_cast<float4*>(coef32)[e] = make_float4(static_cast<float>(c.c[0]), static_cast<float>(c.c[1]),
+                                                               static_cast<float>(c.c[2]), static_cast<float>(c.c0));
+        else
+            coef32[e] = make_float2(static_cast<float>(c.c[0]), static_cast<float>(c.c[1]));
     }
 }
 

@@ -28,6 +28,7 @@ struct amr_adjoint {
     std::vector<void*> ckpt;    // nseg + 1 states
     double*            dts = nullptr; // steps * ninst step sizes
     double*            vel = nullptr; // velocities of the run (3 per instance)
+    int32_t*           upcode = nullptr; // their packed upwind offsets (per instance)
     void*              lam[2]{};
     bool               forward_done = false;
 };
@@ -39,6 +40,7 @@ void free_adjoint(amr_adjoint* a)
     for (void* c : a->ckpt) cudaFree(c);
     cudaFree(a->dts);
     cudaFree(a->vel);
+    cudaFree(a->upcode);
     cudaFree(a->lam[0]);
     cudaFree(a->lam[1]);
     delete a;
@@ -74,6 +76,7 @@ amr_status amr_adjoint_create(amr_tree* t, size_t steps, const double* velocity3
         if (e == cudaSuccess) e = cudaMalloc(&c, t->size * t->g.flat * t->esize);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a->dts), std::max<size_t>(1, steps) * K * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a->vel), 3 * K * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&a->upcode), K * sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMalloc(&a->lam[0], bytes);
     if (e == cudaSuccess) e = cudaMalloc(&a->lam[1], bytes);
     if (e != cudaSuccess) {
@@ -113,8 +116,10 @@ amr_status amr_adjoint_forward(amr_adjoint* a)
         amr_status   st = advance_impl(t, k, a->per_instance ? nullptr : a->vel3, a->cfl, a->remaining,
                                        m == 0 ? BATCH_RESET : BATCH_CONTINUE);
         if (st != AMR_OK) return st;
-        if (m == 0) // velocities in use (per instance)
+        if (m == 0) { // velocities in use (per instance) and their upwind codes
             AMR_CUDA(cudaMemcpyAsync(a->vel, t->vel, 3 * K * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            AMR_CUDA(cudaMemcpyAsync(a->upcode, t->upcode, K * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+        }
         AMR_CUDA(cudaMemcpyAsync(a->dts + m * a->every * K, t->step_dt, k * K * sizeof(double),
                                  cudaMemcpyDeviceToDevice, s));
         AMR_CUDA(cudaMemcpyAsync(a->ckpt[m + 1], t->cur, bytes, cudaMemcpyDeviceToDevice, s));
@@ -150,7 +155,7 @@ amr_status adjoint_sweep(amr_adjoint* a, int* result)
     int up[3] = { 0, 0, 0 };
     if (!a->per_instance)
         for (int k = 0; k < g.rank; ++k) up[k] = a->vel3[k] > 0.0 ? -1 : (a->vel3[k] < 0.0 ? 1 : 0);
-    const double*  vleaf = a->per_instance ? a->vel : nullptr;
+    const int32_t* uleaf = a->per_instance ? a->upcode : nullptr;
     const int      ppb   = std::max(1, 256 / g.cells);
     const unsigned grid  = grid_for(P, ppb);
     int            cur   = 0;
@@ -163,13 +168,17 @@ amr_status adjoint_sweep(amr_adjoint* a, int* result)
         for (size_t m = a->nseg; m-- > 0;) {
             const int k = static_cast<int>(std::min(a->every, a->steps - m * a->every));
             k_coef_from_dt<<<grid_for(static_cast<long long>(k) * K * nl, 256), 256, 0, s>>>(
-                a->dts + m * a->every * K, g, a->vel, k, K, t->coef);
+                a->dts + m * a->every * K, g, a->vel, k, K, t->coef, t->coef32);
             AMR_LAUNCHED("k_coef_from_dt");
             for (int j = k - 1; j >= 0; --j) {
-                const Coef* cf = t->coef + static_cast<size_t>(j) * K * nl;
+                const size_t  row  = static_cast<size_t>(j) * K * nl;
+                const Coef*   cf   = t->coef + row;
+                const float2* cf32 = g.rank == 3
+                                         ? reinterpret_cast<const float2*>(reinterpret_cast<const float4*>(t->coef32) + row)
+                                         : t->coef32 + row;
                 k_adjoint<T><<<grid, 256, 0, s>>>(static_cast<const T*>(a->lam[cur]), static_cast<T*>(a->lam[cur ^ 1]),
-                                                  t->meta[t->tb], t->keys[t->tb], P, g, cf, up[0], up[1], up[2],
-                                                  vleaf, ppb);
+                                                  t->meta[t->tb], t->keys[t->tb], P, g, cf, cf32, up[0], up[1], up[2],
+                                                  uleaf, ppb);
                 AMR_LAUNCHED("k_adjoint");
                 cur ^= 1;
             }
