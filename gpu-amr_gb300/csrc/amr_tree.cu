@@ -1105,6 +1105,17 @@ amr_status run_graph_chunk(amr_tree* t, const amr_cycle_params* p, bool inst_par
             });
         });
         if (ps != AMR_OK) return ps;
+    } else if (step3d_shape(g, t->sbuf[0], t->sbuf[1])) {
+        // the staged 3D kernel's attributes, likewise outside the capture
+        amr_status ps = dispatch_dtype(t->dtype, [&](auto z) -> amr_status {
+            using T = decltype(z);
+            return with_ws3d(g.n, sizeof(T), [&]<int W, int S>() -> amr_status {
+                const int occ = g.n == 8 ? prepare_step3d<T, 8, W, S>() : prepare_step3d<T, 4, W, S>();
+                return occ > 0 ? AMR_OK
+                               : fail(AMR_ERR_CUDA, "staged 3D update kernel: shared-memory configuration failed");
+            });
+        });
+        if (ps != AMR_OK) return ps;
     }
     // per-instance time: one tree carries the run's totals in from the host;
     // a forest starts them at the run's first interval and otherwise keeps
