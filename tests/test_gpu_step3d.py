@@ -143,3 +143,45 @@ def test_forest_per_instance_velocities_against_oracle(amr, oracle_mod, n):
     for i, o in enumerate(oracle):
         np.testing.assert_array_equal(ids[off[i]:off[i + 1]], o.ids())
         assert rel_l2(st[off[i]:off[i + 1]], interior(o.state(), 3, n, 1)) <= 1e-12, i
+
+
+_SHAPE_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import amr_gb300 as A
+b = A.seeded_bumps(3, 4, 3, sigma=(0.05, 0.08))
+out = []
+for n in (8, 4):
+    for dt in (A.F64, A.F32):
+        t = A.Tree(3, n, 1, 6, capacity=5000, dtype=dt)
+        t.refine_uniform(3)
+        t.upload_state(A.gaussian_state(t.ids(), 3, n, 1, 6, b))
+        t.advance(12, (1.0, -0.7, 0.3), 0.4)
+        t.finish_advance()
+        out.append(t.download_state().astype(np.float64).ravel())
+np.save(sys.argv[2], np.concatenate(out))
+"""
+
+
+def test_launch_shapes_agree(tmp_path):
+    """Every built (warps per block, ring depth) pair of the staged 3D kernel
+    (AMR_GB300_STEP3D, read once per process) gives the same states bit for
+    bit, in FP64 and FP32, for 8^3 and 4^3 patches (each in its own process)."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    pkg = str(Path(__file__).resolve().parents[1] / "gpu-amr_gb300")
+    res = {}
+    for shape in ("", "4,2", "4,3", "8,2", "8,3"):
+        env = dict(os.environ)
+        env.pop("AMR_GB300_STEP3D", None)
+        if shape:
+            env["AMR_GB300_STEP3D"] = shape
+        out = tmp_path / f"s{shape.replace(',', '_') or 'default'}.npy"
+        subprocess.run([sys.executable, "-c", _SHAPE_SCRIPT, pkg, str(out)], env=env, check=True, timeout=600)
+        res[shape] = np.load(out)
+    ref = res[""]
+    for shape, v in res.items():
+        np.testing.assert_array_equal(v, ref, err_msg=shape)
