@@ -406,3 +406,27 @@ def test_reserve_keeps_the_tree_and_runs_continue(amr):
     np.testing.assert_array_equal(res[0][1], res[1][1])
     with pytest.raises(amr.AmrError):
         t.reserve(t.size - 1)
+
+
+@pytest.mark.parametrize("name", ["config2_amr_2d", "config3_amr_3d"])
+def test_persistent_run_cluster_sizes_agree(amr, name):
+    """The cluster kernel's work split (thread-block clusters of 16, 8, 4 or
+    2 CTAs) changes no result: the same leaves and states, bit for bit."""
+    z, meta = load_golden(name)
+    p = meta["params"]
+    rank, n, h = meta["rank"], meta["n"], meta["halo"]
+    res = []
+    for cluster in (16, 8, 4, 2):
+        t = amr.Tree(rank, n, h, meta["depth"], capacity=20000)
+        t.refine_uniform(int(p["init_levels"]))
+        t.upload_state(_pad(z["state_init"], rank, n, h))
+        t.halo_exchange()
+        st = t.run(int(p["steps"]), int(p["remesh"]), vel_of(meta), float(p["cfl"]), criterion="grad",
+                   rthr=float(p["rthr"]), cthr=float(p["cthr"]), min_level=int(p["min_level"]),
+                   max_level=int(p["max_level"]), cluster=cluster)
+        assert st["persistent_intervals"] == st["intervals"] > 0
+        res.append((st["sum_dt"], t.ids(), interior(t.download_state(), rank, n, h)))
+    for sum_dt, ids, s in res[1:]:
+        assert sum_dt == res[0][0]
+        np.testing.assert_array_equal(ids, res[0][1])
+        np.testing.assert_array_equal(s, res[0][2])
